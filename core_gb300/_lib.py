@@ -1,0 +1,125 @@
+"""ctypes binding of libsprgb300.so (the C ABI declared in include/spr_gb300.h).
+
+The library is the only compute path: if it is missing this module raises,
+there is no CPU fallback.
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libsprgb300.so")
+
+SPRG_OK = 0
+SPRG_EINVAL = 1
+SPRG_EPATCH = 2
+SPRG_EFLAGS = 3
+SPRG_ENOMEM = 4
+SPRG_ECUDA = 5
+SPRG_ESTATE = 6
+ERROR_NAMES = {1: "EINVAL", 2: "EPATCH", 3: "EFLAGS", 4: "ENOMEM", 5: "ECUDA", 6: "ESTATE"}
+
+SPRG_FP64 = 0
+SPRG_FP32 = 1
+
+SPLIT = 1 << 0
+DONT_SPLIT = 1 << 1
+COLLAPSE = 1 << 2
+DONT_COLLAPSE = 1 << 3
+NEED_NOT_SPLIT = 1 << 17
+NEED_NOT_COLLAPSE = 1 << 18
+MARK_SPLIT = 0
+MARK_COLLAPSE = 1
+
+# every symbol include/spr_gb300.h declares
+EXPORTS = [
+    "sprg_create", "sprg_destroy", "sprg_last_error", "sprg_set_precision", "sprg_set_stream",
+    "sprg_get_grad_ip_field", "sprg_recover_field", "sprg_get_spr_size_field",
+    "sprg_get_target_spr_size_field", "sprg_measure_edges", "sprg_measure_edges_aniso",
+    "sprg_mark_edges", "sprg_measure_quality", "sprg_estimate_and_mark",
+    "sprg_estimate_and_mark_resident", "sprg_apply_marks", "sprg_last_launch_count",
+    "sprg_box_counts", "sprg_box_fill",
+]
+
+
+class SprgError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{ERROR_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+class MeshView(ctypes.Structure):
+    _fields_ = [
+        ("dim", ctypes.c_int),
+        ("n_verts", ctypes.c_int64),
+        ("n_elems", ctypes.c_int64),
+        ("n_edges", ctypes.c_int64),
+        ("coords", ctypes.c_void_p),
+        ("elem_verts", ctypes.c_void_p),
+        ("edge_verts", ctypes.c_void_p),
+        ("vert_elem_offsets", ctypes.c_void_p),
+        ("vert_elems", ctypes.c_void_p),
+    ]
+
+
+class SizeInfo(ctypes.Structure):
+    _fields_ = [
+        ("eps_star_norm2", ctypes.c_double),
+        ("error_sum", ctypes.c_double),
+        ("size_factor", ctypes.c_double),
+        ("n_expanded", ctypes.c_int64),
+        ("n_fp64_refits", ctypes.c_int64),
+        ("n_guard_edges", ctypes.c_int64),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_lib = None
+
+
+def load():
+    """Returns the loaded library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(
+            f"{LIB_PATH} is missing: build it with `python -m core_gb300.build` "
+            "(the estimate-and-mark pass has no CPU fallback)")
+    lib = ctypes.CDLL(LIB_PATH)
+    P = ctypes.c_void_p
+    I = ctypes.c_int
+    D = ctypes.c_double
+    lib.sprg_create.argtypes = [ctypes.POINTER(MeshView), I, ctypes.POINTER(P)]
+    lib.sprg_destroy.argtypes = [P]
+    lib.sprg_last_error.argtypes = [P]
+    lib.sprg_last_error.restype = ctypes.c_char_p
+    lib.sprg_set_precision.argtypes = [P, I]
+    lib.sprg_set_stream.argtypes = [P, P]
+    lib.sprg_get_grad_ip_field.argtypes = [P, P, I, I, P]
+    lib.sprg_recover_field.argtypes = [P, P, I, P]
+    lib.sprg_get_spr_size_field.argtypes = [P, P, I, D, P, ctypes.POINTER(SizeInfo)]
+    lib.sprg_get_target_spr_size_field.argtypes = [P, P, I, ctypes.c_size_t, D, D, P, ctypes.POINTER(SizeInfo)]
+    lib.sprg_measure_edges.argtypes = [P, P, P]
+    lib.sprg_measure_edges_aniso.argtypes = [P, P, P, P]
+    lib.sprg_mark_edges.argtypes = [P, I, P, ctypes.POINTER(ctypes.c_long)]
+    lib.sprg_measure_quality.argtypes = [P, P, P, P, P]
+    lib.sprg_estimate_and_mark.argtypes = [P, P, D, P, P, ctypes.POINTER(ctypes.c_long),
+                                           ctypes.POINTER(ctypes.c_long), ctypes.POINTER(SizeInfo)]
+    lib.sprg_estimate_and_mark_resident.argtypes = [P, P, D, P, P]
+    lib.sprg_apply_marks.argtypes = [ctypes.c_int64, P, P, P, ctypes.POINTER(ctypes.c_long),
+                                     ctypes.POINTER(ctypes.c_long)]
+    lib.sprg_last_launch_count.argtypes = [P]
+    lib.sprg_last_launch_count.restype = ctypes.c_int64
+    lib.sprg_box_counts.argtypes = [I, I, I, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
+                                    ctypes.POINTER(ctypes.c_int64)]
+    lib.sprg_box_fill.argtypes = [I, I, I, D, D, D, P, P, P]
+    _lib = lib
+    return lib
+
+
+def check(rc, ctx=None):
+    if rc != SPRG_OK:
+        msg = load().sprg_last_error(ctx).decode() if ctx else ""
+        raise SprgError(rc, msg)

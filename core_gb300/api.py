@@ -1,0 +1,202 @@
+"""Host-side mirror of the reference's estimate-and-mark interface.
+
+Method names and argument meaning follow the PUMI calls they replace
+(spr/spr.h:33-62, ma/maSize.h:30-113, ma/maRefine.cc:395,
+ma/maCoarsen.cc:287, ma/maShape.h:24-26); apf fields become numpy arrays
+in MDS index order.  Errors raise :class:`SprgError` where the reference
+would abort.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import SprgError, check  # noqa: F401
+
+
+def _f64(a, shape=None):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if shape is not None and a.shape != shape:
+        a = a.reshape(shape)
+    return a
+
+
+class Context:
+    """A mesh flattened onto one GPU (sprg_create)."""
+
+    def __init__(self, mesh, device=0, precision="fp64"):
+        self._lib = _lib.load()
+        self.mesh = mesh
+        self._view = mesh.view()
+        h = ctypes.c_void_p()
+        rc = self._lib.sprg_create(ctypes.byref(self._view), device, ctypes.byref(h))
+        if rc:
+            raise SprgError(rc, "sprg_create failed")
+        self.h = h
+        self.set_precision(precision)
+
+    # -- lifetime -------------------------------------------------------
+    def close(self):
+        if getattr(self, "h", None):
+            self._lib.sprg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, rc):
+        check(rc, self.h)
+
+    def set_precision(self, precision):
+        code = {"fp64": _lib.SPRG_FP64, "fp32": _lib.SPRG_FP32}[precision]
+        self._check(self._lib.sprg_set_precision(self.h, code))
+        self.precision = precision
+
+    def set_stream(self, stream_handle):
+        self._check(self._lib.sprg_set_stream(self.h, ctypes.c_void_p(stream_handle)))
+
+    @property
+    def last_launch_count(self):
+        return int(self._lib.sprg_last_launch_count(self.h))
+
+    # -- spr ------------------------------------------------------------
+    def getGradIPField(self, f, name="grad", order=1):
+        """spr::getGradIPField: SCALAR (V,) -> (T,3); VECTOR (V,3) -> (T,9)."""
+        f = _f64(f)
+        ncin = 1 if f.ndim == 1 else f.shape[1]
+        out = np.empty((self.mesh.n_elems, 3 * ncin), np.float64)
+        self._check(self._lib.sprg_get_grad_ip_field(self.h, f.ctypes.data, ncin, order, out.ctypes.data))
+        return out
+
+    def recoverField(self, ip):
+        """spr::recoverField: (T,nc) integration-point field -> (V,nc) nodal field."""
+        ip = _f64(ip)
+        nc = ip.shape[1]
+        out = np.empty((self.mesh.n_verts, nc), np.float64)
+        self._check(self._lib.sprg_recover_field(self.h, ip.ctypes.data, nc, out.ctypes.data))
+        return out
+
+    def getSPRSizeField(self, ip, adapt_ratio):
+        """spr::getSPRSizeField: returns (size (V,), info dict)."""
+        ip = _f64(ip)
+        out = np.empty(self.mesh.n_verts, np.float64)
+        info = _lib.SizeInfo()
+        self._check(self._lib.sprg_get_spr_size_field(self.h, ip.ctypes.data, ip.shape[1], float(adapt_ratio),
+                                                      out.ctypes.data, ctypes.byref(info)))
+        return out, info.as_dict()
+
+    def getTargetSPRSizeField(self, ip, target, alpha=0.25, beta=2.0):
+        """spr::getTargetSPRSizeField: returns (size (V,), info dict)."""
+        ip = _f64(ip)
+        out = np.empty(self.mesh.n_verts, np.float64)
+        info = _lib.SizeInfo()
+        self._check(self._lib.sprg_get_target_spr_size_field(self.h, ip.ctypes.data, ip.shape[1], int(target),
+                                                             float(alpha), float(beta), out.ctypes.data,
+                                                             ctypes.byref(info)))
+        return out, info.as_dict()
+
+    # -- ma -------------------------------------------------------------
+    def makeSizeField(self, size=None, sizes=None, frames=None):
+        """ma::makeSizeField(m, size) or ma::makeSizeField(m, sizes, frames, false)."""
+        return SizeField(self, size, sizes, frames)
+
+    def measure_edges(self, size=None):
+        out = np.empty(self.mesh.n_edges, np.float64)
+        p = None if size is None else _f64(size)
+        self._check(self._lib.sprg_measure_edges(self.h, None if p is None else p.ctypes.data, out.ctypes.data))
+        return out
+
+    def measure_edges_aniso(self, sizes, frames):
+        sizes = _f64(sizes)
+        frames = _f64(frames).reshape(self.mesh.n_verts, 9)
+        out = np.empty(self.mesh.n_edges, np.float64)
+        self._check(self._lib.sprg_measure_edges_aniso(self.h, sizes.ctypes.data, frames.ctypes.data,
+                                                       out.ctypes.data))
+        return out
+
+    def _mark(self, which, flags):
+        if flags.dtype != np.int32 or not flags.flags["C_CONTIGUOUS"]:
+            raise TypeError("flags must be a contiguous int32 array")
+        n = ctypes.c_long()
+        self._check(self._lib.sprg_mark_edges(self.h, which, flags.ctypes.data, ctypes.byref(n)))
+        return n.value
+
+    def markEdgesToSplit(self, flags):
+        """ma::markEdgesToSplit on the resident edge lengths; flags updated in place."""
+        return self._mark(_lib.MARK_SPLIT, flags)
+
+    def markEdgesToCollapse(self, flags):
+        """ma::markEdgesToCollapse on the resident edge lengths; flags updated in place."""
+        return self._mark(_lib.MARK_COLLAPSE, flags)
+
+    def measureQuality(self, size=None, sizes=None, frames=None):
+        """measureTetQuality / measureTriQuality (useMax = true) of every element."""
+        q = np.empty(self.mesh.n_elems, np.float64)
+        s = None if size is None else _f64(size)
+        ss = None if sizes is None else _f64(sizes)
+        ff = None if frames is None else _f64(frames).reshape(self.mesh.n_verts, 9)
+        self._check(self._lib.sprg_measure_quality(
+            self.h, None if s is None else s.ctypes.data, None if ss is None else ss.ctypes.data,
+            None if ff is None else ff.ctypes.data, q.ctypes.data))
+        return q
+
+    # -- the whole pass --------------------------------------------------
+    def estimate_and_mark(self, u, adapt_ratio, flags=None):
+        """getGradIPField -> getSPRSizeField -> makeSizeField -> collapse/split marks.
+        Returns (size, flags, n_split, n_collapse, info)."""
+        u = _f64(u)
+        if flags is None:
+            flags = np.zeros(self.mesh.n_edges, np.int32)
+        size = np.empty(self.mesh.n_verts, np.float64)
+        ns, nc = ctypes.c_long(), ctypes.c_long()
+        info = _lib.SizeInfo()
+        self._check(self._lib.sprg_estimate_and_mark(self.h, u.ctypes.data, float(adapt_ratio), size.ctypes.data,
+                                                     flags.ctypes.data, ctypes.byref(ns), ctypes.byref(nc),
+                                                     ctypes.byref(info)))
+        return size, flags, ns.value, nc.value, info.as_dict()
+
+    def estimate_and_mark_resident(self, d_u, adapt_ratio, d_split_bits, d_collapse_bits):
+        """Device-pointer form (ints are raw device addresses); asynchronous."""
+        self._check(self._lib.sprg_estimate_and_mark_resident(self.h, ctypes.c_void_p(d_u), float(adapt_ratio),
+                                                              ctypes.c_void_p(d_split_bits),
+                                                              ctypes.c_void_p(d_collapse_bits)))
+
+
+class SizeField:
+    """ma::SizeField over a context (IsoUserField or AnisoSizeField)."""
+
+    def __init__(self, ctx, size=None, sizes=None, frames=None):
+        self.ctx, self.size, self.sizes, self.frames = ctx, size, sizes, frames
+
+    def measure(self):
+        """MetricSizeField::measure of every edge (MDS edge order)."""
+        if self.sizes is not None:
+            return self.ctx.measure_edges_aniso(self.sizes, self.frames)
+        return self.ctx.measure_edges(self.size)
+
+    def shouldSplit(self):
+        return self.measure() > 1.5
+
+    def shouldCollapse(self):
+        return self.measure() < 0.5
+
+
+def apply_marks(split_bits, collapse_bits, flags):
+    """Host write-back of the device edge-mark bitmaps into ma_flags words."""
+    lib = _lib.load()
+    ns, nc = ctypes.c_long(), ctypes.c_long()
+    sb = None if split_bits is None else np.ascontiguousarray(split_bits, np.uint32)
+    cb = None if collapse_bits is None else np.ascontiguousarray(collapse_bits, np.uint32)
+    check(lib.sprg_apply_marks(flags.shape[0], None if sb is None else sb.ctypes.data,
+                               None if cb is None else cb.ctypes.data, flags.ctypes.data, ctypes.byref(ns),
+                               ctypes.byref(nc)))
+    return ns.value, nc.value

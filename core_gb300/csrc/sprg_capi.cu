@@ -1,0 +1,604 @@
+// C ABI of the estimate-and-mark library: context (flattened mesh on the
+// device), buffer management and the orchestration of the kernels for each
+// reference call.  See include/spr_gb300.h for the contract of every entry.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "spr_gb300.h"
+#include "sprg_internal.h"
+
+using namespace sprg;
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+struct sprg_ctx {
+  int device = 0;
+  cudaStream_t own = nullptr;
+  cudaStream_t stream = nullptr;
+  int precision = SPRG_FP64;
+  DevMesh m{};
+  // mesh
+  DevBuf xyz, xyz32, ev, edv, poff, pel, aoff, ael, tmp;
+  // fields
+  DevBuf f, ip, rec, err, esize, size, L, flags, q, sizes3, frames9;
+  int ip_nc = 0;
+  bool ip_valid = false, size_valid = false, L_valid = false;
+  // scratch
+  DevBuf partials, out3, status, count, xitems, xcount, slab, bits;
+  std::string err_msg;
+  int64_t launches = 0;
+  sprg_size_info last_info{};
+};
+
+namespace {
+
+int fail(sprg_ctx* c, int code, const std::string& msg) {
+  if (c) c->err_msg = msg;
+  return code;
+}
+
+int cuda_fail(sprg_ctx* c, cudaError_t e, const char* where) {
+  std::string msg = std::string(where) + ": " + cudaGetErrorString(e);
+  int code = (e == cudaErrorMemoryAllocation) ? SPRG_ENOMEM : SPRG_ECUDA;
+  return fail(c, code, msg);
+}
+
+#define CK(call)                                              \
+  do {                                                        \
+    cudaError_t e_ = (call);                                  \
+    if (e_ != cudaSuccess) return cuda_fail(c, e_, #call);    \
+  } while (0)
+
+// grow-only device buffer
+int ensure(sprg_ctx* c, DevBuf& b, size_t bytes) {
+  if (bytes == 0) bytes = 16;
+  if (b.bytes >= bytes) return SPRG_OK;
+  if (b.p) cudaFree(b.p);
+  b.p = nullptr;
+  b.bytes = 0;
+  cudaError_t e = cudaMalloc(&b.p, bytes);
+  if (e != cudaSuccess) return cuda_fail(c, e, "cudaMalloc");
+  b.bytes = bytes;
+  return SPRG_OK;
+}
+
+void release(DevBuf& b) {
+  if (b.p) cudaFree(b.p);
+  b.p = nullptr;
+  b.bytes = 0;
+}
+
+template <class T>
+T* P(DevBuf& b) { return static_cast<T*>(b.p); }
+
+#define ENSURE(buf, bytes)                     \
+  do {                                         \
+    int rc_ = ensure(c, (buf), (bytes));       \
+    if (rc_) return rc_;                       \
+  } while (0)
+
+int check_launch(sprg_ctx* c, const char* what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(c, e, what);
+  return SPRG_OK;
+}
+
+int sync_and_status(sprg_ctx* c) {
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamSynchronize");
+  DevStatus st;
+  e = cudaMemcpy(&st, c->status.p, sizeof st, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(c, e, "status readback");
+  if (st.code == SPRG_EPATCH)
+    return fail(c, SPRG_EPATCH,
+                st.where >= 0 ? "SPR: patch construction failed at vertex " + std::to_string(st.where)
+                              : std::string("SPR: expansion list overflow"));
+  if (st.code == SPRG_EFLAGS)
+    return fail(c, SPRG_EFLAGS, "markEntities: edge " + std::to_string(st.where) + " already carries the true flag");
+  if (st.code) return fail(c, st.code, "device status " + std::to_string(st.code));
+  return SPRG_OK;
+}
+
+int reset_status(sprg_ctx* c) {
+  CK(cudaMemsetAsync(c->status.p, 0, sizeof(DevStatus), c->stream));
+  return SPRG_OK;
+}
+
+int set_device(sprg_ctx* c) {
+  CK(cudaSetDevice(c->device));
+  return SPRG_OK;
+}
+
+// ---- pipeline steps on resident buffers -------------------------------
+
+int step_grad(sprg_ctx* c, int ncin) {
+  DevMesh& m = c->m;
+  ENSURE(c->ip, sizeof(double) * (size_t)m.T * 3 * ncin);
+  launch_grad_ip_f64(m, P<double>(c->f), ncin, P<double>(c->ip), c->stream);
+  c->launches += 1;
+  c->ip_nc = 3 * ncin;
+  c->ip_valid = true;
+  return check_launch(c, "grad_ip");
+}
+
+int step_recover(sprg_ctx* c) {
+  DevMesh& m = c->m;
+  int nc = c->ip_nc;
+  ENSURE(c->rec, sizeof(double) * (size_t)m.V * nc);
+  ENSURE(c->xitems, sizeof(int) * (size_t)(m.V > 0 ? m.V : 1));
+  ENSURE(c->xcount, sizeof(int));
+  ENSURE(c->slab, sizeof(double) * (size_t)expand_grid() * expand_max_elems() * (4 + nc + 1));
+  CK(cudaMemsetAsync(c->xcount.p, 0, sizeof(int), c->stream));
+  ExpandList xl{P<int>(c->xitems), P<int>(c->xcount), m.V};
+  launch_recover_f64(m, P<double>(c->ip), nc, P<double>(c->rec), xl, P<DevStatus>(c->status), c->stream);
+  c->launches += 1;
+  int rc = check_launch(c, "recover");
+  if (rc) return rc;
+  // patches that need growth: the reference growth order, on the device
+  launch_expand_f64(m, P<double>(c->ip), nc, P<double>(c->rec), xl, P<double>(c->slab), P<DevStatus>(c->status),
+                    c->stream);
+  c->launches += 1;
+  return check_launch(c, "expand");
+}
+
+int step_size(sprg_ctx* c, int mode, double adapt_ratio, double target, double alpha, double beta) {
+  DevMesh& m = c->m;
+  int nc = c->ip_nc;
+  int nb = error_blocks(m.T);
+  ENSURE(c->err, sizeof(double) * (size_t)m.T);
+  ENSURE(c->esize, sizeof(double) * (size_t)m.T);
+  ENSURE(c->size, sizeof(double) * (size_t)m.V);
+  ENSURE(c->partials, sizeof(double) * 2 * (size_t)(nb > 0 ? nb : 1));
+  ENSURE(c->out3, sizeof(double) * 4);
+  double p = 1, d = m.dim;
+  double gexp = (2 * d) / (2 * p + d);
+  launch_error_f64(m, P<double>(c->ip), nc, P<double>(c->rec), P<double>(c->err), P<double>(c->partials), nb, gexp,
+                   c->stream);
+  launch_size_factor(P<double>(c->partials), nb, mode, adapt_ratio, target, m.dim, P<double>(c->out3), c->stream);
+  launch_esize_f64(m, P<double>(c->err), P<double>(c->out3), mode, alpha, beta, P<double>(c->esize), c->stream);
+  launch_average(m, P<double>(c->esize), P<double>(c->size), c->stream);
+  c->launches += 4;
+  c->size_valid = true;
+  return check_launch(c, "size field");
+}
+
+int step_measure_iso(sprg_ctx* c) {
+  DevMesh& m = c->m;
+  ENSURE(c->L, sizeof(double) * (size_t)m.E);
+  launch_measure_iso_f64(m, P<double>(c->size), P<double>(c->L), c->stream);
+  c->launches += 1;
+  c->L_valid = true;
+  return check_launch(c, "measure");
+}
+
+int fill_info(sprg_ctx* c, sprg_size_info* info) {
+  double o3[3];
+  CK(cudaMemcpy(o3, c->out3.p, sizeof o3, cudaMemcpyDeviceToHost));
+  int xc = 0;
+  CK(cudaMemcpy(&xc, c->xcount.p, sizeof xc, cudaMemcpyDeviceToHost));
+  c->last_info.eps_star_norm2 = o3[0];
+  c->last_info.error_sum = o3[1];
+  c->last_info.size_factor = o3[2];
+  c->last_info.n_expanded = xc;
+  if (info) *info = c->last_info;
+  return SPRG_OK;
+}
+
+int upload_ip(sprg_ctx* c, const double* ip, int ncomp) {
+  if (ncomp != 3 && ncomp != 9) return fail(c, SPRG_EINVAL, "ip field must have 3 or 9 components");
+  if (ip) {
+    ENSURE(c->ip, sizeof(double) * (size_t)c->m.T * ncomp);
+    CK(cudaMemcpyAsync(c->ip.p, ip, sizeof(double) * (size_t)c->m.T * ncomp, cudaMemcpyHostToDevice, c->stream));
+    c->ip_nc = ncomp;
+    c->ip_valid = true;
+  } else {
+    if (!c->ip_valid) return fail(c, SPRG_ESTATE, "no resident integration-point field");
+    if (c->ip_nc != ncomp) return fail(c, SPRG_EINVAL, "component count differs from the resident ip field");
+  }
+  return SPRG_OK;
+}
+
+}  // namespace
+
+// ======================================================================
+// C ABI
+// ======================================================================
+extern "C" {
+
+int sprg_create(const sprg_mesh_view* mv, int device, sprg_ctx** out) {
+  if (!out) return SPRG_EINVAL;
+  *out = nullptr;
+  if (!mv || (mv->dim != 2 && mv->dim != 3) || mv->n_verts <= 0 || mv->n_elems <= 0 || mv->n_edges <= 0 ||
+      !mv->coords || !mv->elem_verts || !mv->edge_verts)
+    return SPRG_EINVAL;
+  if (mv->n_verts > INT32_MAX || mv->n_edges > INT32_MAX || mv->n_elems * (mv->dim + 1) > INT32_MAX)
+    return SPRG_EINVAL;
+  if ((mv->vert_elem_offsets == nullptr) != (mv->vert_elems == nullptr)) return SPRG_EINVAL;
+  sprg_ctx* c = new sprg_ctx();
+  c->device = device;
+  int rc = set_device(c);
+  if (rc) { delete c; return rc; }
+  if (cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking) != cudaSuccess) { delete c; return SPRG_ECUDA; }
+  c->stream = c->own;
+  DevMesh& m = c->m;
+  m.dim = mv->dim;
+  m.nn = mv->dim + 1;
+  m.ne_el = mv->dim == 3 ? 6 : 3;
+  m.V = (int)mv->n_verts;
+  m.T = (int)mv->n_elems;
+  m.E = (int)mv->n_edges;
+  auto bail = [&](int code) { sprg_destroy(c); return code; };
+#define CKC(call)                                                            \
+  do {                                                                       \
+    cudaError_t e_ = (call);                                                 \
+    if (e_ != cudaSuccess) return bail(cuda_fail(c, e_, #call));             \
+  } while (0)
+#define ENSUREC(buf, bytes)                                                  \
+  do {                                                                       \
+    int rc_ = ensure(c, (buf), (bytes));                                     \
+    if (rc_) return bail(rc_);                                               \
+  } while (0)
+  size_t nel = (size_t)m.T * m.nn;
+  ENSUREC(c->xyz, sizeof(double) * 3 * (size_t)m.V);
+  ENSUREC(c->xyz32, sizeof(float) * 4 * (size_t)m.V);
+  ENSUREC(c->ev, sizeof(int) * nel);
+  ENSUREC(c->edv, sizeof(int) * 2 * (size_t)m.E);
+  ENSUREC(c->poff, sizeof(int) * ((size_t)m.V + 1));
+  ENSUREC(c->pel, sizeof(int) * nel);
+  ENSUREC(c->tmp, sizeof(int) * (size_t)m.V);
+  ENSUREC(c->status, sizeof(DevStatus));
+  ENSUREC(c->count, sizeof(unsigned long long));
+  CKC(cudaMemsetAsync(c->status.p, 0, sizeof(DevStatus), c->stream));
+  CKC(cudaMemcpyAsync(c->xyz.p, mv->coords, sizeof(double) * 3 * (size_t)m.V, cudaMemcpyHostToDevice, c->stream));
+  CKC(cudaMemcpyAsync(c->ev.p, mv->elem_verts, sizeof(int) * nel, cudaMemcpyHostToDevice, c->stream));
+  CKC(cudaMemcpyAsync(c->edv.p, mv->edge_verts, sizeof(int) * 2 * (size_t)m.E, cudaMemcpyHostToDevice, c->stream));
+  m.xyz = P<double>(c->xyz);
+  m.xyz32 = P<float>(c->xyz32);
+  m.ev = P<int>(c->ev);
+  m.edv = P<int>(c->edv);
+  if (mv->vert_elem_offsets) {
+    // caller-supplied reference adjacency order for averaging; sorted copy for patches
+    ENSUREC(c->aoff, sizeof(int) * ((size_t)m.V + 1));
+    ENSUREC(c->ael, sizeof(int) * nel);
+    CKC(cudaMemcpyAsync(c->aoff.p, mv->vert_elem_offsets, sizeof(int) * ((size_t)m.V + 1), cudaMemcpyHostToDevice,
+                        c->stream));
+    CKC(cudaMemcpyAsync(c->ael.p, mv->vert_elems, sizeof(int) * nel, cudaMemcpyHostToDevice, c->stream));
+    CKC(cudaMemcpyAsync(c->poff.p, c->aoff.p, sizeof(int) * ((size_t)m.V + 1), cudaMemcpyDeviceToDevice, c->stream));
+    CKC(cudaMemcpyAsync(c->pel.p, c->ael.p, sizeof(int) * nel, cudaMemcpyDeviceToDevice, c->stream));
+    launch_sort_segments(m.V, P<int>(c->poff), P<int>(c->pel), c->stream);
+    m.a_off = P<int>(c->aoff);
+    m.a_el = P<int>(c->ael);
+  } else {
+    launch_build_v2e(m, P<int>(c->poff), P<int>(c->pel), P<int>(c->tmp), c->stream);
+    launch_sort_segments(m.V, P<int>(c->poff), P<int>(c->pel), c->stream);
+    m.a_off = P<int>(c->poff);
+    m.a_el = P<int>(c->pel);
+  }
+  m.p_off = P<int>(c->poff);
+  m.p_el = P<int>(c->pel);
+  launch_xyz_to_f32(m, P<float>(c->xyz32), c->stream);
+  CKC(cudaGetLastError());
+  CKC(cudaStreamSynchronize(c->stream));
+  // validate the adjacency: every offset array must end at T * nn
+  int last = 0;
+  CKC(cudaMemcpy(&last, P<int>(c->poff) + m.V, sizeof(int), cudaMemcpyDeviceToHost));
+  if ((size_t)last != nel) {
+    c->err_msg = "vertex-element adjacency does not cover every element vertex";
+    return bail(SPRG_EINVAL);
+  }
+#undef CKC
+#undef ENSUREC
+  *out = c;
+  return SPRG_OK;
+}
+
+int sprg_destroy(sprg_ctx* c) {
+  if (!c) return SPRG_OK;
+  cudaSetDevice(c->device);
+  if (c->own) cudaStreamSynchronize(c->own);
+  DevBuf* bufs[] = {&c->xyz,   &c->xyz32,   &c->ev,   &c->edv,   &c->poff,    &c->pel,    &c->aoff,
+                    &c->ael,   &c->tmp,     &c->f,    &c->ip,    &c->rec,     &c->err,    &c->esize,
+                    &c->size,  &c->L,       &c->flags, &c->q,    &c->sizes3,  &c->frames9, &c->partials,
+                    &c->out3,  &c->status,  &c->count, &c->xitems, &c->xcount, &c->slab, &c->bits};
+  for (DevBuf* b : bufs) release(*b);
+  if (c->own) cudaStreamDestroy(c->own);
+  delete c;
+  return SPRG_OK;
+}
+
+const char* sprg_last_error(const sprg_ctx* c) { return c ? c->err_msg.c_str() : "null context"; }
+
+int sprg_set_precision(sprg_ctx* c, int precision) {
+  if (!c) return SPRG_EINVAL;
+  if (precision != SPRG_FP64) return fail(c, SPRG_EINVAL, "unsupported precision");
+  c->precision = precision;
+  return SPRG_OK;
+}
+
+int sprg_set_stream(sprg_ctx* c, void* stream) {
+  if (!c) return SPRG_EINVAL;
+  c->stream = stream ? static_cast<cudaStream_t>(stream) : c->own;
+  return SPRG_OK;
+}
+
+int64_t sprg_last_launch_count(const sprg_ctx* c) { return c ? c->launches : 0; }
+
+int sprg_get_grad_ip_field(sprg_ctx* c, const double* f, int ncomp_in, int order, double* ip_out) {
+  if (!c || !f) return SPRG_EINVAL;
+  if (order != 1) return fail(c, SPRG_EINVAL, "only integration order 1 is supported");
+  if (ncomp_in != 1 && ncomp_in != 3) return fail(c, SPRG_EINVAL, "field must be SCALAR (1) or VECTOR (3)");
+  int rc = set_device(c);
+  if (rc) return rc;
+  c->launches = 0;
+  DevMesh& m = c->m;
+  ENSURE(c->f, sizeof(double) * (size_t)m.V * ncomp_in);
+  CK(cudaMemcpyAsync(c->f.p, f, sizeof(double) * (size_t)m.V * ncomp_in, cudaMemcpyHostToDevice, c->stream));
+  int saved = c->precision;
+  c->precision = SPRG_FP64;  // the explicit ip field is always the FP64 one
+  rc = step_grad(c, ncomp_in);
+  c->precision = saved;
+  if (rc) return rc;
+  if (ip_out)
+    CK(cudaMemcpyAsync(ip_out, c->ip.p, sizeof(double) * (size_t)m.T * 3 * ncomp_in, cudaMemcpyDeviceToHost,
+                       c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return SPRG_OK;
+}
+
+int sprg_recover_field(sprg_ctx* c, const double* ip, int ncomp, double* out) {
+  if (!c) return SPRG_EINVAL;
+  int rc = set_device(c);
+  if (rc) return rc;
+  c->launches = 0;
+  int saved = c->precision;
+  rc = upload_ip(c, ip, ncomp);
+  if (rc) return rc;
+  c->precision = SPRG_FP64;  // explicit ip fields take the FP64 path
+  if ((rc = reset_status(c)) || (rc = step_recover(c))) { c->precision = saved; return rc; }
+  c->precision = saved;
+  if (out)
+    CK(cudaMemcpyAsync(out, c->rec.p, sizeof(double) * (size_t)c->m.V * ncomp, cudaMemcpyDeviceToHost, c->stream));
+  return sync_and_status(c);
+}
+
+static int size_field_common(sprg_ctx* c, const double* ip, int ncomp, int mode, double adapt_ratio, double target,
+                             double alpha, double beta, double* size_out, sprg_size_info* info) {
+  int rc = set_device(c);
+  if (rc) return rc;
+  c->launches = 0;
+  rc = upload_ip(c, ip, ncomp);
+  if (rc) return rc;
+  int saved = c->precision;
+  c->precision = SPRG_FP64;
+  if ((rc = reset_status(c)) || (rc = step_recover(c)) ||
+      (rc = step_size(c, mode, adapt_ratio, target, alpha, beta))) {
+    c->precision = saved;
+    return rc;
+  }
+  c->precision = saved;
+  if (size_out)
+    CK(cudaMemcpyAsync(size_out, c->size.p, sizeof(double) * (size_t)c->m.V, cudaMemcpyDeviceToHost, c->stream));
+  rc = sync_and_status(c);
+  if (rc) return rc;
+  return fill_info(c, info);
+}
+
+int sprg_get_spr_size_field(sprg_ctx* c, const double* ip, int ncomp, double adapt_ratio, double* size_out,
+                            sprg_size_info* info) {
+  if (!c) return SPRG_EINVAL;
+  if (!(adapt_ratio > 0)) return fail(c, SPRG_EINVAL, "adapt_ratio must be positive");
+  return size_field_common(c, ip, ncomp, 0, adapt_ratio, 0, 0, 0, size_out, info);
+}
+
+int sprg_get_target_spr_size_field(sprg_ctx* c, const double* ip, int ncomp, size_t target, double alpha,
+                                   double beta, double* size_out, sprg_size_info* info) {
+  if (!c) return SPRG_EINVAL;
+  if (target == 0) return fail(c, SPRG_EINVAL, "target must be > 0");   // spr/sprEstimateTargetError.cc:250
+  if (!(alpha < beta)) return fail(c, SPRG_EINVAL, "alpha must be < beta");  // :251
+  return size_field_common(c, ip, ncomp, 1, 0, (double)target, alpha, beta, size_out, info);
+}
+
+int sprg_measure_edges(sprg_ctx* c, const double* size, double* lengths) {
+  if (!c) return SPRG_EINVAL;
+  int rc = set_device(c);
+  if (rc) return rc;
+  c->launches = 0;
+  if (size) {
+    ENSURE(c->size, sizeof(double) * (size_t)c->m.V);
+    CK(cudaMemcpyAsync(c->size.p, size, sizeof(double) * (size_t)c->m.V, cudaMemcpyHostToDevice, c->stream));
+    c->size_valid = true;
+  } else if (!c->size_valid) {
+    return fail(c, SPRG_ESTATE, "no resident size field");
+  }
+  rc = step_measure_iso(c);
+  if (rc) return rc;
+  if (lengths)
+    CK(cudaMemcpyAsync(lengths, c->L.p, sizeof(double) * (size_t)c->m.E, cudaMemcpyDeviceToHost, c->stream));
+  return sync_and_status(c);
+}
+
+int sprg_measure_edges_aniso(sprg_ctx* c, const double* sizes, const double* frames, double* lengths) {
+  if (!c || !sizes || !frames) return SPRG_EINVAL;
+  int rc = set_device(c);
+  if (rc) return rc;
+  c->launches = 0;
+  DevMesh& m = c->m;
+  ENSURE(c->sizes3, sizeof(double) * 3 * (size_t)m.V);
+  ENSURE(c->frames9, sizeof(double) * 9 * (size_t)m.V);
+  ENSURE(c->L, sizeof(double) * (size_t)m.E);
+  CK(cudaMemcpyAsync(c->sizes3.p, sizes, sizeof(double) * 3 * (size_t)m.V, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->frames9.p, frames, sizeof(double) * 9 * (size_t)m.V, cudaMemcpyHostToDevice, c->stream));
+  launch_measure_aniso_f64(m, P<double>(c->sizes3), P<double>(c->frames9), P<double>(c->L), c->stream);
+  c->launches += 1;
+  rc = check_launch(c, "measure aniso");
+  if (rc) return rc;
+  c->L_valid = true;
+  if (lengths)
+    CK(cudaMemcpyAsync(lengths, c->L.p, sizeof(double) * (size_t)m.E, cudaMemcpyDeviceToHost, c->stream));
+  return sync_and_status(c);
+}
+
+static int apply_bits(sprg_ctx* c, int which, const uint32_t* bits, int* d_flags) {
+  CK(cudaMemsetAsync(c->count.p, 0, sizeof(unsigned long long), c->stream));
+  launch_apply_bits(c->m.E, bits, which, d_flags, P<unsigned long long>(c->count), P<DevStatus>(c->status),
+                    c->stream);
+  c->launches += 1;
+  return check_launch(c, "apply marks");
+}
+
+static int mark_resident(sprg_ctx* c, int which, int* d_flags) {
+  CK(cudaMemsetAsync(c->count.p, 0, sizeof(unsigned long long), c->stream));
+  launch_mark(c->m.E, P<double>(c->L), which, d_flags, P<unsigned long long>(c->count), P<DevStatus>(c->status),
+              c->stream);
+  c->launches += 1;
+  return check_launch(c, "mark");
+}
+
+int sprg_mark_edges(sprg_ctx* c, int which, int32_t* flags, long* count) {
+  if (!c || !flags) return SPRG_EINVAL;
+  if (which != SPRG_MARK_SPLIT && which != SPRG_MARK_COLLAPSE) return fail(c, SPRG_EINVAL, "unknown mark pass");
+  if (!c->L_valid) return fail(c, SPRG_ESTATE, "no resident edge lengths (call sprg_measure_edges first)");
+  int rc = set_device(c);
+  if (rc) return rc;
+  c->launches = 0;
+  DevMesh& m = c->m;
+  ENSURE(c->flags, sizeof(int) * (size_t)m.E);
+  CK(cudaMemcpyAsync(c->flags.p, flags, sizeof(int) * (size_t)m.E, cudaMemcpyHostToDevice, c->stream));
+  if ((rc = reset_status(c)) || (rc = mark_resident(c, which, P<int>(c->flags)))) return rc;
+  unsigned long long n = 0;
+  CK(cudaMemcpyAsync(&n, c->count.p, sizeof n, cudaMemcpyDeviceToHost, c->stream));
+  rc = sync_and_status(c);
+  if (rc) return rc;  // flags left untouched on the host on error
+  CK(cudaMemcpy(flags, c->flags.p, sizeof(int) * (size_t)m.E, cudaMemcpyDeviceToHost));
+  if (count) *count = (long)n;
+  return SPRG_OK;
+}
+
+int sprg_measure_quality(sprg_ctx* c, const double* size, const double* sizes, const double* frames, double* q) {
+  if (!c || !q) return SPRG_EINVAL;
+  if ((sizes == nullptr) != (frames == nullptr)) return fail(c, SPRG_EINVAL, "sizes and frames go together");
+  int rc = set_device(c);
+  if (rc) return rc;
+  c->launches = 0;
+  DevMesh& m = c->m;
+  ENSURE(c->q, sizeof(double) * (size_t)m.T);
+  const double* dsize = nullptr;
+  const double* dsizes = nullptr;
+  const double* dframes = nullptr;
+  if (sizes) {
+    ENSURE(c->sizes3, sizeof(double) * 3 * (size_t)m.V);
+    ENSURE(c->frames9, sizeof(double) * 9 * (size_t)m.V);
+    CK(cudaMemcpyAsync(c->sizes3.p, sizes, sizeof(double) * 3 * (size_t)m.V, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->frames9.p, frames, sizeof(double) * 9 * (size_t)m.V, cudaMemcpyHostToDevice, c->stream));
+    dsizes = P<double>(c->sizes3);
+    dframes = P<double>(c->frames9);
+  } else {
+    if (size) {
+      ENSURE(c->size, sizeof(double) * (size_t)m.V);
+      CK(cudaMemcpyAsync(c->size.p, size, sizeof(double) * (size_t)m.V, cudaMemcpyHostToDevice, c->stream));
+      c->size_valid = true;
+    } else if (!c->size_valid) {
+      return fail(c, SPRG_ESTATE, "no resident size field");
+    }
+    dsize = P<double>(c->size);
+  }
+  launch_quality_f64(m, dsize, dsizes, dframes, P<double>(c->q), c->stream);
+  c->launches += 1;
+  rc = check_launch(c, "quality");
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(q, c->q.p, sizeof(double) * (size_t)m.T, cudaMemcpyDeviceToHost, c->stream));
+  return sync_and_status(c);
+}
+
+static int pass_resident(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_t* d_collapse) {
+  int rc;
+  if ((rc = reset_status(c)) || (rc = step_grad(c, 1)) || (rc = step_recover(c)) ||
+      (rc = step_size(c, 0, adapt_ratio, 0, 0, 0)) || (rc = step_measure_iso(c)))
+    return rc;
+  launch_mark_bits(c->m.E, P<double>(c->L), d_split, d_collapse, c->stream);
+  c->launches += 1;
+  return check_launch(c, "mark bits");
+}
+
+int sprg_estimate_and_mark_resident(sprg_ctx* c, const double* d_u, double adapt_ratio, uint32_t* d_split_bits,
+                                    uint32_t* d_collapse_bits) {
+  if (!c || !d_u || !d_split_bits || !d_collapse_bits) return SPRG_EINVAL;
+  if (!(adapt_ratio > 0)) return fail(c, SPRG_EINVAL, "adapt_ratio must be positive");
+  int rc = set_device(c);
+  if (rc) return rc;
+  c->launches = 0;
+  ENSURE(c->f, sizeof(double) * (size_t)c->m.V);
+  CK(cudaMemcpyAsync(c->f.p, d_u, sizeof(double) * (size_t)c->m.V, cudaMemcpyDeviceToDevice, c->stream));
+  return pass_resident(c, adapt_ratio, d_split_bits, d_collapse_bits);
+}
+
+int sprg_estimate_and_mark(sprg_ctx* c, const double* u, double adapt_ratio, double* size_out, int32_t* flags,
+                           long* n_split, long* n_collapse, sprg_size_info* info) {
+  if (!c || !u) return SPRG_EINVAL;
+  if (!(adapt_ratio > 0)) return fail(c, SPRG_EINVAL, "adapt_ratio must be positive");
+  int rc = set_device(c);
+  if (rc) return rc;
+  c->launches = 0;
+  DevMesh& m = c->m;
+  ENSURE(c->f, sizeof(double) * (size_t)m.V);
+  ENSURE(c->flags, sizeof(int) * (size_t)m.E);
+  CK(cudaMemcpyAsync(c->f.p, u, sizeof(double) * (size_t)m.V, cudaMemcpyHostToDevice, c->stream));
+  if (flags)
+    CK(cudaMemcpyAsync(c->flags.p, flags, sizeof(int) * (size_t)m.E, cudaMemcpyHostToDevice, c->stream));
+  else
+    CK(cudaMemsetAsync(c->flags.p, 0, sizeof(int) * (size_t)m.E, c->stream));
+  size_t nw = ((size_t)m.E + 31) / 32;
+  ENSURE(c->bits, sizeof(uint32_t) * 2 * nw);
+  uint32_t* sb = P<uint32_t>(c->bits);
+  if ((rc = pass_resident(c, adapt_ratio, sb, sb + nw))) return rc;
+  unsigned long long ncol = 0, nspl = 0;
+  if ((rc = apply_bits(c, SPRG_MARK_COLLAPSE, sb + nw, P<int>(c->flags)))) return rc;
+  CK(cudaMemcpyAsync(&ncol, c->count.p, sizeof ncol, cudaMemcpyDeviceToHost, c->stream));
+  if ((rc = apply_bits(c, SPRG_MARK_SPLIT, sb, P<int>(c->flags)))) return rc;
+  CK(cudaMemcpyAsync(&nspl, c->count.p, sizeof nspl, cudaMemcpyDeviceToHost, c->stream));
+  if (size_out)
+    CK(cudaMemcpyAsync(size_out, c->size.p, sizeof(double) * (size_t)m.V, cudaMemcpyDeviceToHost, c->stream));
+  rc = sync_and_status(c);
+  if (rc) return rc;
+  if (flags) CK(cudaMemcpy(flags, c->flags.p, sizeof(int) * (size_t)m.E, cudaMemcpyDeviceToHost));
+  if (n_split) *n_split = (long)nspl;
+  if (n_collapse) *n_collapse = (long)ncol;
+  return fill_info(c, info);
+}
+
+int sprg_apply_marks(int64_t n_edges, const uint32_t* split_bits, const uint32_t* collapse_bits, int32_t* flags,
+                     long* n_split, long* n_collapse) {
+  if (n_edges < 0 || !flags) return SPRG_EINVAL;
+  const int SPLIT_PASS[3] = {SPRG_SPLIT, SPRG_NEED_NOT_SPLIT, SPRG_DONT_SPLIT | SPRG_NEED_NOT_SPLIT};
+  const int COLL_PASS[3] = {SPRG_COLLAPSE, SPRG_NEED_NOT_COLLAPSE, SPRG_DONT_COLLAPSE | SPRG_NEED_NOT_COLLAPSE};
+  // the true flag must be clear on every edge before either pass (ma/maAdapt.cc:304)
+  for (int64_t e = 0; e < n_edges; ++e) {
+    if (collapse_bits && (flags[e] & COLL_PASS[0])) return SPRG_EFLAGS;
+    if (split_bits && (flags[e] & SPLIT_PASS[0])) return SPRG_EFLAGS;
+  }
+  long counts[2] = {0, 0};
+  const uint32_t* bits[2] = {collapse_bits, split_bits};
+  const int* pass[2] = {COLL_PASS, SPLIT_PASS};
+  for (int k = 0; k < 2; ++k) {
+    if (!bits[k]) continue;
+    for (int64_t e = 0; e < n_edges; ++e) {
+      int f = flags[e];
+      if (pass[k][2] & f) continue;
+      if ((bits[k][e >> 5] >> (e & 31)) & 1u) { f |= pass[k][0]; ++counts[k]; }
+      else f |= pass[k][1];
+      flags[e] = f;
+    }
+  }
+  if (n_collapse) *n_collapse = counts[0];
+  if (n_split) *n_split = counts[1];
+  return SPRG_OK;
+}
+
+}  // extern "C"

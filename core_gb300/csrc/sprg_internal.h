@@ -1,0 +1,84 @@
+// Internal declarations shared by the CUDA translation units of the
+// estimate-and-mark library.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+
+#include "spr_gb300.h"
+
+namespace sprg {
+
+// Device view of the flattened mesh.  All index arrays are int32.
+struct DevMesh {
+  int dim;             // 2 or 3
+  int nn;              // vertices per element (dim + 1)
+  int ne_el;           // edges per element (3 or 6)
+  int V, T, E;
+  const double* xyz;   // V x 3 (FP64 master copy)
+  const float* xyz32;  // V x 4 (x, y, z, 0) FP32 copy for the fast path
+  const int* ev;       // T x nn  (getDownward(e,0) order)
+  const int* edv;      // E x 2
+  const int* p_off;    // V + 1, patch CSR: elements of each vertex, ascending
+  const int* p_el;
+  const int* a_off;    // V + 1, averaging CSR (reference getAdjacent order)
+  const int* a_el;
+};
+
+// Device status word written by kernels (first error wins).
+struct DevStatus {
+  int code;        // SPRG_OK or SPRG_E*
+  int where;       // entity index that raised it
+};
+
+// Expansion work list for patches that need growth or are too large for the
+// register path.
+struct ExpandList {
+  int* items;   // vertex ids
+  int* count;   // device counter
+  int cap;
+};
+
+// ---- kernel launchers (sprg_kernels_f64.cu) ---------------------------
+void launch_grad_ip_f64(const DevMesh& m, const double* f, int ncin, double* ip, cudaStream_t s);
+void launch_recover_f64(const DevMesh& m, const double* ip, int nc, double* rec, ExpandList xl,
+                        DevStatus* st, cudaStream_t s);
+// Patches on the expansion list: grow as the reference does, then fit.
+// The list length is read on the device (no host round trip).
+// slab: expand_grid() * expand_max_elems() * (4 + nc + 1) doubles.
+void launch_expand_f64(const DevMesh& m, const double* ip, int nc, double* rec, ExpandList xl, double* slab,
+                       DevStatus* st, cudaStream_t s);
+int expand_max_elems();
+int expand_grid();
+// Per-element error terms + deterministic block partials (2 per block).
+void launch_error_f64(const DevMesh& m, const double* ip, int nc, const double* rec, double* err,
+                      double* partials, int n_blocks, double g_exponent, cudaStream_t s);
+int error_blocks(int T);
+// Sum partials in fixed order, compute size factor.  mode 0: SPR; 1: target.
+void launch_size_factor(const double* partials, int n_blocks, int mode, double adapt_ratio, double target,
+                        int dim, double* out3, cudaStream_t s);
+void launch_esize_f64(const DevMesh& m, const double* err, const double* out3, int mode, double alpha,
+                      double beta, double* esize, cudaStream_t s);
+void launch_average(const DevMesh& m, const double* esize, double* size, cudaStream_t s);
+void launch_measure_iso_f64(const DevMesh& m, const double* size, double* L, cudaStream_t s);
+void launch_measure_aniso_f64(const DevMesh& m, const double* sizes, const double* frames, double* L,
+                              cudaStream_t s);
+void launch_mark(int E, const double* L, int which, int* flags, unsigned long long* count, DevStatus* st,
+                 cudaStream_t s);
+// predicate bitmaps: bit e of split = L[e] > 1.5, of collapse = L[e] < 0.5
+void launch_mark_bits(int E, const double* L, uint32_t* split, uint32_t* collapse, cudaStream_t s);
+// markEntities semantics from a predicate bitmap
+void launch_apply_bits(int E, const uint32_t* bits, int which, int* flags, unsigned long long* count,
+                       DevStatus* st, cudaStream_t s);
+void launch_quality_f64(const DevMesh& m, const double* size, const double* sizes, const double* frames,
+                        double* q, cudaStream_t s);
+
+// ---- adjacency builders (sprg_kernels_f64.cu) ---------------------------
+// Ascending vertex->element CSR via counting sort on the device.
+// off must hold V + 1 ints, el T * nn ints, tmp V ints.
+void launch_build_v2e(const DevMesh& m, int* off, int* el, int* tmp, cudaStream_t s);
+// Sort each CSR segment ascending (segments are short).
+void launch_sort_segments(int V, const int* off, int* el, cudaStream_t s);
+void launch_xyz_to_f32(const DevMesh& m, float* xyz32, cudaStream_t s);
+
+}  // namespace sprg

@@ -1,0 +1,814 @@
+// FP64 ("parity") kernels of the estimate-and-mark pass.
+//
+// Compiled with -fmad=false: element and edge arithmetic follows the
+// reference's operation order (sprg_refmath.cuh), so gradients, element
+// errors, sizes, lengths and qualities round like PUMI's apf/spr/ma code.
+// Two places differ by design and are stated in the parity tests: the
+// patch QR uses warp-tree reductions and applies the reflectors to the
+// right-hand side instead of forming Q (mth/mthQR.cc builds an explicit
+// m x m Q), and the two global integrals are summed by a fixed tree instead
+// of sequentially.  Both move results by a few ulps only.
+#include <cub/cub.cuh>
+
+#include "sprg_internal.h"
+#include "sprg_refmath.cuh"
+
+namespace sprg {
+
+using ref::M3;
+using ref::V3;
+
+namespace {
+
+constexpr int kBlock = 256;
+constexpr int kExpandMaxElems = 1024;
+constexpr int kExpandHash = 4096;
+constexpr int kExpandGrid = 304;  // 2 resident single-warp blocks per SM
+
+__device__ __forceinline__ void set_status(DevStatus* st, int code, int where) {
+  if (atomicCAS(&st->code, 0, code) == 0) st->where = where;
+}
+
+__device__ __forceinline__ double warp_sum(double x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+  return x;
+}
+
+__device__ __forceinline__ V3 load_xyz(const double* __restrict__ xyz, int v) {
+  return V3{{xyz[3 * (size_t)v], xyz[3 * (size_t)v + 1], xyz[3 * (size_t)v + 2]}};
+}
+
+// integration point (mapLocalToGlobal at the order-1 point) of element e,
+// in the reference's interpolation order
+__device__ __forceinline__ V3 elem_ip_point(const DevMesh& m, int e) {
+  double N[4];
+  ref::ip_shape_values(m.dim, N);
+  V3 p{{0, 0, 0}};
+  const int* ev = m.ev + (size_t)e * m.nn;
+  for (int a = 0; a < m.nn; ++a) {
+    V3 x = load_xyz(m.xyz, ev[a]);
+    for (int k = 0; k < 3; ++k) p.v[k] += x.v[k] * N[a];
+  }
+  return p;
+}
+
+// ---------------------------------------------------------------------
+// spr::getGradIPField
+// ---------------------------------------------------------------------
+__global__ void __launch_bounds__(kBlock) k_grad_ip(DevMesh m, const double* __restrict__ f, int ncin,
+                                                    double* __restrict__ ip) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= m.T) return;
+  const int* ev = m.ev + (size_t)e * m.nn;
+  V3 x[4];
+  for (int a = 0; a < m.nn; ++a) x[a] = load_xyz(m.xyz, ev[a]);
+  M3 J = ref::jacobian(x, m.nn, m.dim);
+  M3 jinv = ref::jacobian_inverse(J, m.dim);
+  V3 lg[4], gg[4];
+  ref::shape_grads(m.dim, lg);
+  for (int a = 0; a < m.nn; ++a) gg[a] = ref::mulv(jinv, lg[a]);
+  if (ncin == 1) {
+    V3 g = ref::scale(gg[0], f[ev[0]]);
+    for (int a = 1; a < m.nn; ++a) g = ref::add(g, ref::scale(gg[a], f[ev[a]]));
+    for (int k = 0; k < 3; ++k) ip[(size_t)e * 3 + k] = g.v[k];
+  } else {
+    M3 g;
+    for (int a = 0; a < m.nn; ++a) {
+      V3 u{{f[3 * (size_t)ev[a]], f[3 * (size_t)ev[a] + 1], f[3 * (size_t)ev[a] + 2]}};
+      for (int r = 0; r < 3; ++r) {
+        V3 rw = ref::scale(u, gg[a].v[r]);
+        if (a == 0) ref::setrow(g, r, rw);
+        else ref::setrow(g, r, ref::add(ref::row(g, r), rw));
+      }
+    }
+    for (int r = 0; r < 3; ++r)
+      for (int c = 0; c < 3; ++c) ip[(size_t)e * 9 + 3 * r + c] = g.m[r][c];
+  }
+}
+
+// ---------------------------------------------------------------------
+// spr::recoverField -- register path: one warp per vertex, RPL rows per
+// lane.  Patches that are too small, rank deficient or larger than 32*RPL
+// rows go to the expansion list.
+// ---------------------------------------------------------------------
+template <int NT, int NC, int RPL>
+__global__ void __launch_bounds__(kBlock) k_recover(DevMesh m, const double* __restrict__ ip,
+                                                    double* __restrict__ rec, ExpandList xl) {
+  const int lane = threadIdx.x & 31;
+  const int v = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+  if (v >= m.V) return;
+  const int beg = m.p_off[v];
+  const int cnt = m.p_off[v + 1] - beg;
+  if (cnt < NT || cnt > 32 * RPL) {
+    if (lane == 0) {
+      int slot = atomicAdd(xl.count, 1);
+      if (slot < xl.cap) xl.items[slot] = v;
+    }
+    return;
+  }
+  double a[RPL][NT], b[RPL][NC];
+#pragma unroll
+  for (int r = 0; r < RPL; ++r) {
+    int i = lane + 32 * r;
+    if (i < cnt) {
+      int el = m.p_el[beg + i];
+      V3 p = elem_ip_point(m, el);
+      a[r][0] = 1.0;
+      a[r][1] = p.v[0];
+      a[r][2] = p.v[1];
+      if (NT == 4) a[r][NT - 1] = p.v[2];
+#pragma unroll
+      for (int c = 0; c < NC; ++c) b[r][c] = ip[(size_t)el * NC + c];
+    } else {
+#pragma unroll
+      for (int j = 0; j < NT; ++j) a[r][j] = 0;
+#pragma unroll
+      for (int c = 0; c < NC; ++c) b[r][c] = 0;
+    }
+  }
+  // Householder QR without pivoting; rank test as mth::get_reflector
+  // (column residual norm below 1e-10 absolute = rank deficient).
+#pragma unroll
+  for (int k = 0; k < NT; ++k) {
+    double s = 0;
+#pragma unroll
+    for (int r = 0; r < RPL; ++r) {
+      int i = lane + 32 * r;
+      if (i >= k) s += a[r][k] * a[r][k];
+    }
+    double cn = sqrt(warp_sum(s));
+    if (cn < 1e-10) {  // uniform across the warp
+      if (lane == 0) {
+        int slot = atomicAdd(xl.count, 1);
+        if (slot < xl.cap) xl.items[slot] = v;
+      }
+      return;
+    }
+    double akk = __shfl_sync(0xffffffffu, a[0][k], k);
+    double vv[RPL];
+    double s2 = 0;
+#pragma unroll
+    for (int r = 0; r < RPL; ++r) {
+      int i = lane + 32 * r;
+      vv[r] = (i >= k) ? a[r][k] : 0.0;
+      if (i == k) vv[r] += ((akk < 0) ? -1 : 1) * cn;
+      s2 += vv[r] * vv[r];
+    }
+    double rn = sqrt(warp_sum(s2));
+#pragma unroll
+    for (int r = 0; r < RPL; ++r) vv[r] /= rn;
+#pragma unroll
+    for (int j = k; j < NT; ++j) {
+      double d = 0;
+#pragma unroll
+      for (int r = 0; r < RPL; ++r) d += a[r][j] * vv[r];
+      d = warp_sum(d);
+#pragma unroll
+      for (int r = 0; r < RPL; ++r) a[r][j] -= 2 * d * vv[r];
+    }
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+      double d = 0;
+#pragma unroll
+      for (int r = 0; r < RPL; ++r) d += b[r][c] * vv[r];
+      d = warp_sum(d);
+#pragma unroll
+      for (int r = 0; r < RPL; ++r) b[r][c] -= 2 * d * vv[r];
+    }
+  }
+  // R (NT x NT) sits in lanes 0..NT-1 of slot 0.
+  double R[NT][NT], y[NT][NC];
+#pragma unroll
+  for (int i = 0; i < NT; ++i) {
+#pragma unroll
+    for (int j = 0; j < NT; ++j) R[i][j] = __shfl_sync(0xffffffffu, a[0][j], i);
+#pragma unroll
+    for (int c = 0; c < NC; ++c) y[i][c] = __shfl_sync(0xffffffffu, b[0][c], i);
+  }
+  V3 xv = load_xyz(m.xyz, v);
+  double terms[4] = {1.0, xv.v[0], xv.v[1], xv.v[2]};
+#pragma unroll
+  for (int c = 0; c < NC; ++c) {
+    double x[NT];
+#pragma unroll
+    for (int ii = 0; ii < NT; ++ii) {
+      int i = NT - ii - 1;
+      double t = y[i][c];
+#pragma unroll
+      for (int j = i + 1; j < NT; ++j) t -= R[i][j] * x[j];
+      x[i] = t / R[i][i];
+    }
+    double sres = 0;
+#pragma unroll
+    for (int j = 0; j < NT; ++j) sres += x[j] * terms[j];
+    if (lane == c) rec[(size_t)v * NC + c] = sres;
+  }
+}
+
+// ---------------------------------------------------------------------
+// Patch growth (spr/sprRecoverField.cc:155-386) for listed vertices: one
+// warp per vertex, element set in shared memory, rows in a global slab.
+// ---------------------------------------------------------------------
+__device__ bool hash_insert(int* hs, int key) {
+  unsigned h = ((unsigned)key * 2654435761u) & (kExpandHash - 1);
+  for (int probe = 0; probe < kExpandHash; ++probe) {
+    int prev = atomicCAS(&hs[h], -1, key);
+    if (prev == -1) return true;
+    if (prev == key) return false;
+    h = (h + 1) & (kExpandHash - 1);
+  }
+  return false;
+}
+
+__device__ void warp_sort_set(int* S, int n, int* tmp) {
+  const int lane = threadIdx.x & 31;
+  for (int i = lane; i < n; i += 32) {
+    int x = S[i], rank = 0;
+    for (int j = 0; j < n; ++j) rank += (S[j] < x);
+    tmp[rank] = x;
+  }
+  __syncwarp();
+  for (int i = lane; i < n; i += 32) S[i] = tmp[i];
+  __syncwarp();
+}
+
+// QR fit over the element set S (sorted).  Returns false if rank deficient.
+// rows: n x (NT + nc + 1) doubles; the last column holds the reflector.
+__device__ bool slab_fit(const DevMesh& m, const int* S, int n, const double* __restrict__ ip, int nc,
+                         double* rows, int v, double* rec) {
+  const int lane = threadIdx.x & 31;
+  const int NT = m.dim == 3 ? 4 : 3;
+  const int W = NT + nc;
+  const int LD = W + 1;
+  if (n < NT) return false;
+  for (int i = lane; i < n; i += 32) {
+    int el = S[i];
+    V3 p = elem_ip_point(m, el);
+    double* rw = rows + (size_t)i * LD;
+    rw[0] = 1.0; rw[1] = p.v[0]; rw[2] = p.v[1];
+    if (NT == 4) rw[3] = p.v[2];
+    for (int c = 0; c < nc; ++c) rw[NT + c] = ip[(size_t)el * nc + c];
+  }
+  __syncwarp();
+  for (int k = 0; k < NT; ++k) {
+    double s = 0;
+    for (int i = k + lane; i < n; i += 32) s += rows[(size_t)i * LD + k] * rows[(size_t)i * LD + k];
+    double cn = sqrt(warp_sum(s));
+    if (cn < 1e-10) return false;  // uniform across the warp
+    double akk = rows[(size_t)k * LD + k];
+    double s2 = 0;
+    for (int i = k + lane; i < n; i += 32) {
+      double vi = rows[(size_t)i * LD + k];
+      if (i == k) vi += ((akk < 0) ? -1 : 1) * cn;
+      rows[(size_t)i * LD + W] = vi;
+      s2 += vi * vi;
+    }
+    double rn = sqrt(warp_sum(s2));
+    for (int i = k + lane; i < n; i += 32) rows[(size_t)i * LD + W] /= rn;
+    __syncwarp();
+    for (int j = k; j < W; ++j) {
+      double d = 0;
+      for (int i = k + lane; i < n; i += 32) d += rows[(size_t)i * LD + j] * rows[(size_t)i * LD + W];
+      d = warp_sum(d);
+      for (int i = k + lane; i < n; i += 32) rows[(size_t)i * LD + j] -= 2 * d * rows[(size_t)i * LD + W];
+      __syncwarp();
+    }
+  }
+  V3 xv = load_xyz(m.xyz, v);
+  double terms[4] = {1.0, xv.v[0], xv.v[1], xv.v[2]};
+  for (int c = 0; c < nc; ++c) {
+    double x[4];
+    for (int ii = 0; ii < NT; ++ii) {
+      int i = NT - ii - 1;
+      double t = rows[(size_t)i * LD + NT + c];
+      for (int j = i + 1; j < NT; ++j) t -= rows[(size_t)i * LD + j] * x[j];
+      x[i] = t / rows[(size_t)i * LD + i];
+    }
+    double sres = 0;
+    for (int j = 0; j < NT; ++j) sres += x[j] * terms[j];
+    if (lane == 0) rec[(size_t)v * nc + c] = sres;
+  }
+  __syncwarp();
+  return true;
+}
+
+__global__ void __launch_bounds__(32) k_expand(DevMesh m, const double* __restrict__ ip, int nc,
+                                               double* __restrict__ rec, const int* __restrict__ items,
+                                               const int* __restrict__ n_items_ptr, int cap, double* slab,
+                                               DevStatus* st) {
+  __shared__ int S[kExpandMaxElems];
+  __shared__ int old[kExpandMaxElems];
+  __shared__ int tmp[kExpandMaxElems];
+  __shared__ int hs[kExpandHash];
+  __shared__ int nS;
+  const int lane = threadIdx.x;
+  const int NT = m.dim == 3 ? 4 : 3;
+  double* rows = slab + (size_t)blockIdx.x * kExpandMaxElems * (NT + nc + 1);
+  int n_items = *n_items_ptr;
+  if (n_items > cap) {
+    if (lane == 0 && blockIdx.x == 0) set_status(st, SPRG_EPATCH, -1);
+    n_items = cap;
+  }
+  for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
+    const int v = items[it];
+    for (int i = lane; i < kExpandHash; i += 32) hs[i] = -1;
+    if (lane == 0) nS = 0;
+    __syncwarp();
+    bool overflow = false;
+    for (int k = m.p_off[v] + lane; k < m.p_off[v + 1]; k += 32) {
+      int f = m.p_el[k];
+      if (hash_insert(hs, f)) {
+        int slot = atomicAdd(&nS, 1);
+        if (slot < kExpandMaxElems) S[slot] = f; else overflow = true;
+      }
+    }
+    __syncwarp();
+    bool done = false, failed = false;
+    for (int round = 0; round < 64 && !done && !failed; ++round) {
+      overflow = __any_sync(0xffffffffu, overflow);
+      if (overflow || nS > kExpandMaxElems) { failed = true; break; }
+      int n0 = nS;
+      warp_sort_set(S, n0, tmp);
+      if (slab_fit(m, S, n0, ip, nc, rows, v, rec)) { done = true; break; }
+      for (int i = lane; i < n0; i += 32) old[i] = S[i];
+      __syncwarp();
+      for (int sd = m.dim - 1; sd >= 0 && !done; --sd) {
+        for (int i = lane; i < n0; i += 32) {
+          int e = old[i];
+          const int* ev = m.ev + (size_t)e * m.nn;
+          for (int a = 0; a < m.nn; ++a) {
+            int w = ev[a];
+            for (int k = m.p_off[w]; k < m.p_off[w + 1]; ++k) {
+              int f = m.p_el[k];
+              const int* fv = m.ev + (size_t)f * m.nn;
+              int shared = 0;
+              for (int p = 0; p < m.nn; ++p)
+                for (int q = 0; q < m.nn; ++q) shared += (ev[p] == fv[q]);
+              if (shared >= sd + 1 && hash_insert(hs, f)) {
+                int slot = atomicAdd(&nS, 1);
+                if (slot < kExpandMaxElems) S[slot] = f; else overflow = true;
+              }
+            }
+          }
+        }
+        __syncwarp();
+        overflow = __any_sync(0xffffffffu, overflow);
+        if (overflow || nS > kExpandMaxElems) { failed = true; break; }
+        int n1 = nS;
+        warp_sort_set(S, n1, tmp);
+        if (slab_fit(m, S, n1, ip, nc, rows, v, rec)) { done = true; break; }
+      }
+      if (!done && !failed && !(nS > n0)) failed = true;  // "all hope is lost"
+    }
+    if (!done && lane == 0) set_status(st, SPRG_EPATCH, v);
+    __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------------
+// Element error terms (SelfProduct / ElementError, spr/sprEstimateError.cc:98-170)
+// ---------------------------------------------------------------------
+__device__ __forceinline__ double block_sum(double x, double* sh) {
+  x = warp_sum(x);
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  __syncthreads();
+  if (lane == 0) sh[w] = x;
+  __syncthreads();
+  double t = 0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t += sh[i];
+  return t;
+}
+
+__global__ void __launch_bounds__(kBlock) k_error(DevMesh m, const double* __restrict__ ip, int nc,
+                                                  const double* __restrict__ rec, double* __restrict__ err,
+                                                  double* __restrict__ partials, double g_exponent) {
+  __shared__ double sh[kBlock / 32];
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  double self_term = 0, g_term = 0;
+  if (e < m.T) {
+    const int* ev = m.ev + (size_t)e * m.nn;
+    V3 x[4];
+    for (int a = 0; a < m.nn; ++a) x[a] = load_xyz(m.xyz, ev[a]);
+    M3 J = ref::jacobian(x, m.nn, m.dim);
+    double dV = ref::jacobian_det(J, m.dim);
+    double w = ref::ip_weight(m.dim);
+    double N[4];
+    ref::ip_shape_values(m.dim, N);
+    double v2[9], v1[9];
+    for (int k = 0; k < nc; ++k) v2[k] = 0;
+    for (int a = 0; a < m.nn; ++a)
+      for (int k = 0; k < nc; ++k) v2[k] += rec[(size_t)ev[a] * nc + k] * N[a];
+    double vv = 0;
+    for (int k = 0; k < nc; ++k) vv += v2[k] * v2[k];
+    self_term = vv * w * dV;
+    for (int k = 0; k < nc; ++k) v1[k] = ip[(size_t)e * nc + k];
+    for (int k = 0; k < nc; ++k) v1[k] -= v2[k];
+    double dd = 0;
+    for (int k = 0; k < nc; ++k) dd += v1[k] * v1[k];
+    double sum = 0;
+    sum += dd * w * dV;
+    err[e] = sum;
+    g_term = pow(sqrt(sum), g_exponent);
+  }
+  double s1 = block_sum(self_term, sh);
+  double s2 = block_sum(g_term, sh);
+  if (threadIdx.x == 0) {
+    partials[2 * blockIdx.x] = s1;
+    partials[2 * blockIdx.x + 1] = s2;
+  }
+}
+
+// one block: fixed-order reduction of the partials, then the size factor
+__global__ void __launch_bounds__(kBlock) k_size_factor(const double* __restrict__ partials, int nb, int mode,
+                                                        double adapt_ratio, double target, int dim,
+                                                        double* out3) {
+  __shared__ double sh[kBlock / 32];
+  double a = 0, g = 0;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+    a += partials[2 * i];
+    g += partials[2 * i + 1];
+  }
+  double snorm = block_sum(a, sh);
+  double gsum = block_sum(g, sh);
+  if (threadIdx.x == 0) {
+    double p = 1, d = dim, sf;
+    if (mode == 0) {
+      double esn = sqrt(snorm);
+      double aa = adapt_ratio * adapt_ratio * esn * esn;
+      double b = aa / gsum;
+      sf = pow(b, 1.0 / (2.0 * p));
+    } else {
+      sf = pow((gsum / target), (1.0 / dim));
+    }
+    (void)d;
+    out3[0] = snorm;
+    out3[1] = gsum;
+    out3[2] = sf;
+  }
+}
+
+// apf::measure of a linear edge (N1 rule, w = 2)
+__device__ __forceinline__ double edge_measure(const V3& x0, const V3& x1) {
+  V3 x[2] = {x0, x1};
+  M3 J = ref::jacobian(x, 2, 1);
+  double dV = ref::jacobian_det(J, 1);
+  double r = 0;
+  r += 2 * dV;
+  return r;
+}
+
+__constant__ int c_tet_edges[6][2] = {{0, 1}, {1, 2}, {2, 0}, {0, 3}, {1, 3}, {2, 3}};
+__constant__ int c_tri_edges[3][2] = {{0, 1}, {1, 2}, {2, 0}};
+
+__global__ void __launch_bounds__(kBlock) k_esize(DevMesh m, const double* __restrict__ err,
+                                                  const double* __restrict__ out3, int mode, double alpha,
+                                                  double beta, double* __restrict__ esize) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= m.T) return;
+  const int* ev = m.ev + (size_t)e * m.nn;
+  V3 x[4];
+  for (int a = 0; a < m.nn; ++a) x[a] = load_xyz(m.xyz, ev[a]);
+  double h = 0;
+  for (int i = 0; i < m.ne_el; ++i) {
+    int p = m.dim == 3 ? c_tet_edges[i][0] : c_tri_edges[i][0];
+    int q = m.dim == 3 ? c_tet_edges[i][1] : c_tri_edges[i][1];
+    double l = edge_measure(x[p], x[q]);
+    h = (h < l) ? l : h;
+  }
+  double sf = out3[2];
+  double pp = 1, d = m.dim;
+  if (mode == 0) {
+    double errorNorm = pow(sqrt(err[e]), -(2 / (2 * pp + d)));
+    esize[e] = h * errorNorm * sf;
+  } else {
+    double theta_e = sqrt(err[e]);
+    double r = pow(theta_e, ((-2.0) / (2.0 * 1 + m.dim)));
+    double h_new = sf * r * h;
+    if (h_new < alpha * h) h_new = alpha * h;
+    if (h_new > beta * h) h_new = beta * h;
+    esize[e] = h_new;
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k_average(DevMesh m, const double* __restrict__ esize,
+                                                    double* __restrict__ size) {
+  int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= m.V) return;
+  int b = m.a_off[v], e = m.a_off[v + 1];
+  double s = 0;
+  for (int k = b; k < e; ++k) s += esize[m.a_el[k]];
+  s /= (double)(size_t)(e - b);
+  size[v] = s;
+}
+
+// MetricSizeField::measure, 2-point Gauss (ma/maSize.cc:158-214)
+__device__ __forceinline__ double metric_length(const V3& x0, const V3& x1, const double* hv, const double* Rv) {
+  V3 x[2] = {x0, x1};
+  M3 J = ref::jacobian(x, 2, 1);
+  const double gp[2] = {0.577350269189626, -0.577350269189626};
+  double measurement = 0;
+#pragma unroll
+  for (int p = 0; p < 2; ++p) {
+    double N[2];
+    ref::edge_shape_values(gp[p], N);
+    M3 Q = ref::get_transform(hv, Rv, N, 2);
+    double dV2 = ref::jacobian_det(ref::mul(J, Q), 1);
+    measurement += 1 * dV2;
+  }
+  return measurement;
+}
+
+__device__ __forceinline__ void identity9(double* R) {
+  for (int k = 0; k < 9; ++k) R[k] = (k % 4 == 0) ? 1.0 : 0.0;
+}
+
+__global__ void __launch_bounds__(kBlock) k_measure_iso(DevMesh m, const double* __restrict__ size,
+                                                        double* __restrict__ L) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= m.E) return;
+  int a = m.edv[2 * (size_t)e], b = m.edv[2 * (size_t)e + 1];
+  double hv[6], Rv[18];
+  double sa = size[a], sb = size[b];
+  hv[0] = hv[1] = hv[2] = sa;
+  hv[3] = hv[4] = hv[5] = sb;
+  identity9(Rv);
+  identity9(Rv + 9);
+  L[e] = metric_length(load_xyz(m.xyz, a), load_xyz(m.xyz, b), hv, Rv);
+}
+
+__global__ void __launch_bounds__(kBlock) k_measure_aniso(DevMesh m, const double* __restrict__ sizes,
+                                                          const double* __restrict__ frames,
+                                                          double* __restrict__ L) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= m.E) return;
+  int vv[2] = {m.edv[2 * (size_t)e], m.edv[2 * (size_t)e + 1]};
+  double hv[6], Rv[18];
+  for (int a = 0; a < 2; ++a) {
+    for (int k = 0; k < 3; ++k) hv[3 * a + k] = sizes[3 * (size_t)vv[a] + k];
+    for (int k = 0; k < 9; ++k) Rv[9 * a + k] = frames[9 * (size_t)vv[a] + k];
+  }
+  L[e] = metric_length(load_xyz(m.xyz, vv[0]), load_xyz(m.xyz, vv[1]), hv, Rv);
+}
+
+// ma::markEntities (ma/maAdapt.cc:293-324)
+__global__ void __launch_bounds__(kBlock) k_mark(int E, const double* __restrict__ L, int which,
+                                                 int* __restrict__ flags, unsigned long long* count,
+                                                 DevStatus* st) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  int trueFlag = which == 0 ? SPRG_SPLIT : SPRG_COLLAPSE;
+  int setFalse = which == 0 ? SPRG_NEED_NOT_SPLIT : SPRG_NEED_NOT_COLLAPSE;
+  int allFalse = which == 0 ? (SPRG_DONT_SPLIT | SPRG_NEED_NOT_SPLIT) : (SPRG_DONT_COLLAPSE | SPRG_NEED_NOT_COLLAPSE);
+  int marked = 0;
+  if (e < E) {
+    int f = flags[e];
+    if (f & trueFlag) {
+      set_status(st, SPRG_EFLAGS, e);
+    } else if (!(allFalse & f)) {
+      double l = L[e];
+      bool pred = which == 0 ? (l > 1.5) : (l < .5);
+      if (pred) { f |= trueFlag; marked = 1; }
+      else f |= setFalse;
+      flags[e] = f;
+    }
+  }
+  unsigned b = __ballot_sync(0xffffffffu, marked);
+  if ((threadIdx.x & 31) == 0 && b) atomicAdd(count, (unsigned long long)__popc(b));
+}
+
+// ShouldSplit / ShouldCollapse predicates as the device edge-mark bitmap
+__global__ void __launch_bounds__(kBlock) k_mark_bits(int E, const double* __restrict__ L, uint32_t* __restrict__ split,
+                                                      uint32_t* __restrict__ collapse) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  bool s = false, c = false;
+  if (e < E) {
+    double l = L[e];
+    s = l > 1.5;
+    c = l < .5;
+  }
+  unsigned bs = __ballot_sync(0xffffffffu, s), bc = __ballot_sync(0xffffffffu, c);
+  if ((threadIdx.x & 31) == 0 && e < E) {
+    split[e >> 5] = bs;
+    collapse[e >> 5] = bc;
+  }
+}
+
+// markEntities semantics (ma/maAdapt.cc:293-324) applied from a predicate bitmap
+__global__ void __launch_bounds__(kBlock) k_apply_bits(int E, const uint32_t* __restrict__ bits, int which,
+                                                       int* __restrict__ flags, unsigned long long* count,
+                                                       DevStatus* st) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  int trueFlag = which == 0 ? SPRG_SPLIT : SPRG_COLLAPSE;
+  int setFalse = which == 0 ? SPRG_NEED_NOT_SPLIT : SPRG_NEED_NOT_COLLAPSE;
+  int allFalse = which == 0 ? (SPRG_DONT_SPLIT | SPRG_NEED_NOT_SPLIT) : (SPRG_DONT_COLLAPSE | SPRG_NEED_NOT_COLLAPSE);
+  int marked = 0;
+  if (e < E) {
+    int f = flags[e];
+    if (f & trueFlag) {
+      set_status(st, SPRG_EFLAGS, e);
+    } else if (!(allFalse & f)) {
+      if ((bits[e >> 5] >> (e & 31)) & 1u) { f |= trueFlag; marked = 1; }
+      else f |= setFalse;
+      flags[e] = f;
+    }
+  }
+  unsigned b = __ballot_sync(0xffffffffu, marked);
+  if ((threadIdx.x & 31) == 0 && b) atomicAdd(count, (unsigned long long)__popc(b));
+}
+
+// measureTetQuality / measureTriQuality, useMax = true (ma/maQuality.cc:83-167)
+__device__ __forceinline__ double q_measure(const V3* x, int nn, int edim, const M3& Q) {
+  M3 J = ref::jacobian(x, nn, edim);
+  double w = edim == 3 ? 1.0 / 6.0 : (edim == 2 ? 1.0 / 2.0 : 2.0);
+  double dV2 = ref::jacobian_det(ref::mul(J, Q), edim);
+  double measurement = 0;
+  measurement += w * dV2;
+  return measurement;
+}
+
+__global__ void __launch_bounds__(kBlock) k_quality(DevMesh m, const double* __restrict__ size,
+                                                    const double* __restrict__ sizes,
+                                                    const double* __restrict__ frames, double* __restrict__ q) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= m.T) return;
+  const int* ev = m.ev + (size_t)e * m.nn;
+  M3 Q;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) Q.m[i][j] = 0;
+  double maxJ = -1.0;
+  for (int i = 0; i < m.nn; ++i) {
+    int v = ev[i];
+    double hv[3], Rv[9], N[1] = {1.0};
+    if (size) { hv[0] = hv[1] = hv[2] = size[v]; identity9(Rv); }
+    else {
+      for (int k = 0; k < 3; ++k) hv[k] = sizes[3 * (size_t)v + k];
+      for (int k = 0; k < 9; ++k) Rv[k] = frames[9 * (size_t)v + k];
+    }
+    M3 cQ = ref::get_transform(hv, Rv, N, 1);
+    double cJ = ref::jacobian_det(cQ, m.dim);
+    if (cJ > maxJ) { maxJ = cJ; Q = cQ; }
+  }
+  V3 x[4];
+  for (int a = 0; a < m.nn; ++a) x[a] = load_xyz(m.xyz, ev[a]);
+  double s = 0;
+  for (int i = 0; i < m.ne_el; ++i) {
+    int p = m.dim == 3 ? c_tet_edges[i][0] : c_tri_edges[i][0];
+    int r = m.dim == 3 ? c_tet_edges[i][1] : c_tri_edges[i][1];
+    V3 xe[2] = {x[p], x[r]};
+    double l = q_measure(xe, 2, 1, Q);
+    s += l * l;
+  }
+  double Vm = q_measure(x, m.nn, m.dim, Q);
+  double res;
+  if (m.dim == 3) {
+    if (Vm < 0) res = -15552 * (Vm * Vm) / (s * s * s);
+    else res = 15552 * (Vm * Vm) / (s * s * s);
+  } else {
+    res = 48 * (Vm * Vm) / (s * s);
+  }
+  q[e] = res;
+}
+
+// ---------------------------------------------------------------------
+// adjacency construction
+// ---------------------------------------------------------------------
+__global__ void k_count_v2e(DevMesh m, int* cnt) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= m.T) return;
+  for (int a = 0; a < m.nn; ++a) atomicAdd(&cnt[m.ev[(size_t)e * m.nn + a]], 1);
+}
+__global__ void k_fill_v2e(DevMesh m, const int* off, int* cursor, int* el) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= m.T) return;
+  for (int a = 0; a < m.nn; ++a) {
+    int v = m.ev[(size_t)e * m.nn + a];
+    int pos = off[v] + atomicAdd(&cursor[v], 1);
+    el[pos] = e;
+  }
+}
+// short segments: insertion sort by one thread per segment
+__global__ void k_sort_segments(int V, const int* off, int* el) {
+  int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= V) return;
+  int b = off[v], e = off[v + 1];
+  for (int i = b + 1; i < e; ++i) {
+    int x = el[i], j = i - 1;
+    while (j >= b && el[j] > x) { el[j + 1] = el[j]; --j; }
+    el[j + 1] = x;
+  }
+}
+__global__ void k_xyz_f32(DevMesh m, float* xyz32) {
+  int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= m.V) return;
+  float4 p = make_float4((float)m.xyz[3 * (size_t)v], (float)m.xyz[3 * (size_t)v + 1],
+                         (float)m.xyz[3 * (size_t)v + 2], 0.f);
+  reinterpret_cast<float4*>(xyz32)[v] = p;
+}
+
+inline int nblk(long n, int b = kBlock) { return (int)((n + b - 1) / b); }
+
+}  // namespace
+
+// ----------------------------------------------------------------------
+// launchers
+// ----------------------------------------------------------------------
+void launch_grad_ip_f64(const DevMesh& m, const double* f, int ncin, double* ip, cudaStream_t s) {
+  if (m.T) k_grad_ip<<<nblk(m.T), kBlock, 0, s>>>(m, f, ncin, ip);
+}
+
+void launch_recover_f64(const DevMesh& m, const double* ip, int nc, double* rec, ExpandList xl, DevStatus* st,
+                        cudaStream_t s) {
+  (void)st;
+  if (!m.V) return;
+  int grid = nblk((long)m.V * 32);
+  if (m.dim == 3) {
+    if (nc == 3) k_recover<4, 3, 2><<<grid, kBlock, 0, s>>>(m, ip, rec, xl);
+    else k_recover<4, 9, 1><<<grid, kBlock, 0, s>>>(m, ip, rec, xl);
+  } else {
+    if (nc == 3) k_recover<3, 3, 2><<<grid, kBlock, 0, s>>>(m, ip, rec, xl);
+    else k_recover<3, 9, 1><<<grid, kBlock, 0, s>>>(m, ip, rec, xl);
+  }
+}
+
+int expand_max_elems() { return kExpandMaxElems; }
+
+int expand_grid() { return kExpandGrid; }
+
+void launch_expand_f64(const DevMesh& m, const double* ip, int nc, double* rec, ExpandList xl, double* slab,
+                       DevStatus* st, cudaStream_t s) {
+  k_expand<<<kExpandGrid, 32, 0, s>>>(m, ip, nc, rec, xl.items, xl.count, xl.cap, slab, st);
+}
+
+int error_blocks(int T) { return nblk(T); }
+
+void launch_error_f64(const DevMesh& m, const double* ip, int nc, const double* rec, double* err,
+                      double* partials, int n_blocks, double g_exponent, cudaStream_t s) {
+  if (n_blocks) k_error<<<n_blocks, kBlock, 0, s>>>(m, ip, nc, rec, err, partials, g_exponent);
+}
+
+void launch_size_factor(const double* partials, int n_blocks, int mode, double adapt_ratio, double target, int dim,
+                        double* out3, cudaStream_t s) {
+  k_size_factor<<<1, kBlock, 0, s>>>(partials, n_blocks, mode, adapt_ratio, target, dim, out3);
+}
+
+void launch_esize_f64(const DevMesh& m, const double* err, const double* out3, int mode, double alpha, double beta,
+                      double* esize, cudaStream_t s) {
+  if (m.T) k_esize<<<nblk(m.T), kBlock, 0, s>>>(m, err, out3, mode, alpha, beta, esize);
+}
+
+void launch_average(const DevMesh& m, const double* esize, double* size, cudaStream_t s) {
+  if (m.V) k_average<<<nblk(m.V), kBlock, 0, s>>>(m, esize, size);
+}
+
+void launch_measure_iso_f64(const DevMesh& m, const double* size, double* L, cudaStream_t s) {
+  if (m.E) k_measure_iso<<<nblk(m.E), kBlock, 0, s>>>(m, size, L);
+}
+
+void launch_measure_aniso_f64(const DevMesh& m, const double* sizes, const double* frames, double* L,
+                              cudaStream_t s) {
+  if (m.E) k_measure_aniso<<<nblk(m.E), kBlock, 0, s>>>(m, sizes, frames, L);
+}
+
+void launch_mark(int E, const double* L, int which, int* flags, unsigned long long* count, DevStatus* st,
+                 cudaStream_t s) {
+  if (E) k_mark<<<nblk(E), kBlock, 0, s>>>(E, L, which, flags, count, st);
+}
+
+void launch_mark_bits(int E, const double* L, uint32_t* split, uint32_t* collapse, cudaStream_t s) {
+  if (E) k_mark_bits<<<nblk(E), kBlock, 0, s>>>(E, L, split, collapse);
+}
+
+void launch_apply_bits(int E, const uint32_t* bits, int which, int* flags, unsigned long long* count, DevStatus* st,
+                       cudaStream_t s) {
+  if (E) k_apply_bits<<<nblk(E), kBlock, 0, s>>>(E, bits, which, flags, count, st);
+}
+
+void launch_quality_f64(const DevMesh& m, const double* size, const double* sizes, const double* frames, double* q,
+                        cudaStream_t s) {
+  if (m.T) k_quality<<<nblk(m.T), kBlock, 0, s>>>(m, size, sizes, frames, q);
+}
+
+void launch_build_v2e(const DevMesh& m, int* off, int* el, int* tmp, cudaStream_t s) {
+  cudaMemsetAsync(tmp, 0, sizeof(int) * (size_t)m.V, s);
+  cudaMemsetAsync(off, 0, sizeof(int) * ((size_t)m.V + 1), s);
+  if (m.T) k_count_v2e<<<nblk(m.T), kBlock, 0, s>>>(m, off);
+  // exclusive scan of the V+1 counts (last is 0) -> offsets
+  size_t bytes = 0;
+  cub::DeviceScan::ExclusiveSum(nullptr, bytes, off, off, m.V + 1, s);
+  void* scratch = nullptr;
+  cudaMallocAsync(&scratch, bytes, s);
+  cub::DeviceScan::ExclusiveSum(scratch, bytes, off, off, m.V + 1, s);
+  cudaFreeAsync(scratch, s);
+  if (m.T) k_fill_v2e<<<nblk(m.T), kBlock, 0, s>>>(m, off, tmp, el);
+}
+
+void launch_sort_segments(int V, const int* off, int* el, cudaStream_t s) {
+  if (V) k_sort_segments<<<nblk(V), kBlock, 0, s>>>(V, off, el);
+}
+
+void launch_xyz_to_f32(const DevMesh& m, float* xyz32, cudaStream_t s) {
+  if (m.V) k_xyz_f32<<<nblk(m.V), kBlock, 0, s>>>(m, xyz32);
+}
+
+}  // namespace sprg

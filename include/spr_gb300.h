@@ -1,0 +1,198 @@
+/*
+ * spr_gb300.h -- C ABI of the GB300-native estimate-and-mark pass.
+ *
+ * The entry points replace, one for one, the PUMI (SCOREC/core) calls of the
+ * estimate-and-mark path.  Each declaration names the reference interface it
+ * stands in for (paths relative to the SCOREC/core tree).  A C++ shim on the
+ * reference side flattens an apf::Mesh2 into a
+ * sprg_mesh_view, calls these functions, and writes the results back into
+ * the apf fields and the "ma_flags" tag, so callers keep the unchanged
+ * spr::/ma:: signatures.
+ *
+ * Conventions
+ *  - All arrays are in MDS index order: entity i of a dimension is the i-th
+ *    entity visited by apf::Mesh::begin/iterate on that dimension.
+ *  - Host pointers everywhere (the library copies to and from the device),
+ *    except in the *_resident functions, which keep data in device memory.
+ *  - Calls are synchronous: outputs are complete when a call returns.
+ *  - Every function returns SPRG_OK (0) or a nonzero SPRG_E* code and never
+ *    aborts; sprg_last_error() describes the last failure.  The reference
+ *    aborts instead (PCU_ALWAYS_ASSERT, apf::fail); the shim maps nonzero
+ *    codes back to apf::fail to keep those semantics.
+ *  - One host thread per context.  Contexts are independent.
+ */
+#ifndef SPR_GB300_H
+#define SPR_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPRG_OK 0
+#define SPRG_EINVAL 1   /* bad argument, unsupported mesh or element type */
+#define SPRG_EPATCH 2   /* SPR patch cannot be completed (spr/sprRecoverField.cc:383) */
+#define SPRG_EFLAGS 3   /* edge already carries the true flag (ma/maAdapt.cc:304) */
+#define SPRG_ENOMEM 4   /* device or host allocation failed */
+#define SPRG_ECUDA 5    /* CUDA runtime error */
+#define SPRG_ESTATE 6   /* call order: an input the call needs is not resident */
+
+/* precision modes */
+#define SPRG_FP64 0  /* FP64 throughout, the reference's arithmetic */
+#define SPRG_FP32 1  /* FP32 patch fits and sweeps, FP64 guard (see sprg_guard_info) */
+
+/* markEntities flag bits (ma/maAdapt.h:17-37) */
+#define SPRG_SPLIT (1 << 0)
+#define SPRG_DONT_SPLIT (1 << 1)
+#define SPRG_COLLAPSE (1 << 2)
+#define SPRG_DONT_COLLAPSE (1 << 3)
+#define SPRG_NEED_NOT_SPLIT (1 << 17)
+#define SPRG_NEED_NOT_COLLAPSE (1 << 18)
+
+/* which marking pass */
+#define SPRG_MARK_SPLIT 0    /* ma::markEdgesToSplit    (ma/maRefine.cc:395) */
+#define SPRG_MARK_COLLAPSE 1 /* ma::markEdgesToCollapse (ma/maCoarsen.cc:287) */
+
+/* Flattened linear simplex mesh (tets in 3D, triangles in 2D).
+   Replaces traversal of apf::Mesh / MDS (mds/apfMDS.cc:300-342). */
+typedef struct sprg_mesh_view {
+  int dim;                       /* 3 (tets) or 2 (triangles) */
+  int64_t n_verts;
+  int64_t n_elems;
+  int64_t n_edges;
+  const double* coords;          /* n_verts x 3: apf::Mesh::getPoint */
+  const int32_t* elem_verts;     /* n_elems x (dim+1): getDownward(e, 0) order */
+  const int32_t* edge_verts;     /* n_edges x 2: getDownward(edge, 0) */
+  /* Optional (both NULL or both set): vertex-to-element adjacency in
+     getAdjacent(v, dim) order (mds/mds.c:666 get_up).  It fixes the
+     summation order of the vertex size average (spr/sprEstimateError.cc:255)
+     so results are bitwise those of the reference.  When NULL the library
+     builds it in ascending element order. */
+  const int32_t* vert_elem_offsets; /* n_verts + 1 */
+  const int32_t* vert_elems;
+} sprg_mesh_view;
+
+typedef struct sprg_ctx sprg_ctx;
+
+/* Statistics of the last size-field computation. */
+typedef struct sprg_size_info {
+  double eps_star_norm2;   /* SelfProduct integral, sum over elements (spr/sprEstimateError.cc:98) */
+  double error_sum;        /* Error integral G (spr/sprEstimateError.cc:171) */
+  double size_factor;      /* spr/sprEstimateError.cc:205-217 */
+  int64_t n_expanded;      /* patches that needed growth (spr/sprRecoverField.cc:365) */
+  int64_t n_fp64_refits;   /* FP32 mode: patches refit in FP64 (condition estimate > 1e6) */
+  int64_t n_guard_edges;   /* FP32 mode: edges re-measured in FP64 near 0.5 / 1.5 */
+} sprg_size_info;
+
+/* ---- context: flatten + upload (the MDS-to-device flattener) ---------- */
+
+/* Uploads the mesh to device `device` and builds the device adjacency.
+   Replaces the per-call apf::Mesh traversal of every function below. */
+int sprg_create(const sprg_mesh_view* mesh, int device, sprg_ctx** out);
+int sprg_destroy(sprg_ctx* ctx);
+const char* sprg_last_error(const sprg_ctx* ctx);
+/* SPRG_FP64 (default) or SPRG_FP32. */
+int sprg_set_precision(sprg_ctx* ctx, int precision);
+/* Run on this CUDA stream (cudaStream_t, NULL = the context's own). */
+int sprg_set_stream(sprg_ctx* ctx, void* stream);
+
+/* ---- spr ------------------------------------------------------------- */
+
+/* spr::getGradIPField(f, name, order) (spr/spr.h:33, spr/sprGetGradIPField.cc:15).
+   order must be 1.  ncomp_in 1 (SCALAR f -> VECTOR ip field, 3 per element)
+   or 3 (VECTOR f -> MATRIX ip field, 9 per element, row-major).
+   f: n_verts x ncomp_in.  ip_out: n_elems x (3*ncomp_in), may be NULL (the
+   ip field stays resident for the calls below). */
+int sprg_get_grad_ip_field(sprg_ctx* ctx, const double* f, int ncomp_in, int order, double* ip_out);
+
+/* spr::recoverField(ip_field) (spr/spr.h:39, spr/sprRecoverField.cc:419).
+   ip: n_elems x ncomp, or NULL to use the resident ip field.
+   out: n_verts x ncomp ("spr_<name>" Lagrange-1 field), may be NULL. */
+int sprg_recover_field(sprg_ctx* ctx, const double* ip, int ncomp, double* out);
+
+/* spr::getSPRSizeField(eps, adapt_ratio, pcu) (spr/spr.h:47, spr/sprEstimateError.cc:311).
+   ip: as above.  size_out: n_verts ("size" Lagrange-1 field), may be NULL
+   (stays resident for ma measure / mark / quality).  info may be NULL. */
+int sprg_get_spr_size_field(sprg_ctx* ctx, const double* ip, int ncomp, double adapt_ratio,
+                            double* size_out, sprg_size_info* info);
+
+/* spr::getTargetSPRSizeField(eps, target, pcu, alpha, beta)
+   (spr/spr.h:56, spr/sprEstimateTargetError.cc:241). */
+int sprg_get_target_spr_size_field(sprg_ctx* ctx, const double* ip, int ncomp, size_t target,
+                                   double alpha, double beta, double* size_out, sprg_size_info* info);
+
+/* ---- ma --------------------------------------------------------------- */
+
+/* ma::makeSizeField(m, size) + MetricSizeField::measure on every edge
+   (ma/maSize.cc:649, 208).  size: n_verts, or NULL for the resident size
+   field.  lengths: n_edges, may be NULL (lengths stay resident). */
+int sprg_measure_edges(sprg_ctx* ctx, const double* size, double* lengths);
+
+/* ma::makeSizeField(m, sizes, frames, false) + measure (ma/maSize.cc:618,
+   AnisoSizeField ma/maSize.cc:364-412).  sizes: n_verts x 3; frames:
+   n_verts x 9 row-major (principal directions in columns). */
+int sprg_measure_edges_aniso(sprg_ctx* ctx, const double* sizes, const double* frames, double* lengths);
+
+/* ma::markEdgesToSplit / ma::markEdgesToCollapse through ma::markEntities
+   (ma/maAdapt.cc:293) on the resident lengths.  flags: n_edges int words of
+   the "ma_flags" tag (0 where the tag is absent), updated in place.
+   count: marked edges (all owned on one part). */
+int sprg_mark_edges(sprg_ctx* ctx, int which, int32_t* flags, long* count);
+
+/* ma::measureTetQuality / ma::measureTriQuality with useMax = true
+   (ma/maShape.h:24-26, ma/maQuality.cc:110-167) for every element, under the
+   isotropic size field `size` (NULL = resident) or, when sizes/frames are
+   given, the anisotropic one.  q: n_elems. */
+int sprg_measure_quality(sprg_ctx* ctx, const double* size, const double* sizes, const double* frames,
+                         double* q);
+
+/* ---- the whole pass ---------------------------------------------------- */
+
+/* getGradIPField(u,"grad",1) -> getSPRSizeField(grad, adapt_ratio) ->
+   makeSizeField(m, size) -> markEdgesToCollapse -> markEdgesToSplit, on a
+   scalar P1 field u (n_verts).  flags: n_edges, updated in place (may be
+   NULL).  size_out may be NULL.  Counts may be NULL. */
+int sprg_estimate_and_mark(sprg_ctx* ctx, const double* u, double adapt_ratio, double* size_out,
+                           int32_t* flags, long* n_split, long* n_collapse, sprg_size_info* info);
+
+/* Device-resident form of the pass: d_u is a device pointer (n_verts
+   doubles); the result is the device edge-mark bitmap, one bit per edge in
+   ceil(n_edges/32) uint32 words each: split bit = (length > 1.5), collapse
+   bit = (length < 0.5), the ShouldSplit / ShouldCollapse predicates
+   (ma/maRefine.cc:382, ma/maCoarsen.cc:275).  Nothing crosses the host
+   boundary; asynchronous on the context stream.  sprg_apply_marks turns the
+   bitmaps into "ma_flags" words with markEntities semantics. */
+int sprg_estimate_and_mark_resident(sprg_ctx* ctx, const double* d_u, double adapt_ratio, uint32_t* d_split_bits,
+                                    uint32_t* d_collapse_bits);
+
+/* Host write-back of the device edge-mark bitmaps into "ma_flags" words
+   with markEntities semantics (ma/maAdapt.cc:293-324): collapse pass, then
+   split pass (the order ma::adapt runs them, ma/ma.cc:33-36).  Either
+   bitmap may be NULL to skip its pass.  Returns SPRG_EFLAGS, leaving flags
+   unchanged, if an edge already carries a pass's true flag. */
+int sprg_apply_marks(int64_t n_edges, const uint32_t* split_bits, const uint32_t* collapse_bits, int32_t* flags,
+                     long* n_split, long* n_collapse);
+
+/* Number of kernel launches issued by the last call (instrumentation). */
+int64_t sprg_last_launch_count(const sprg_ctx* ctx);
+
+/* ---- box meshes --------------------------------------------------------- */
+
+/* Entity counts of apf::makeMdsBox(nx, ny, nz, wx, wy, wz, true)
+   (mds/apfBox.cc:330); nz = 0 gives the 2D triangle box. */
+int sprg_box_counts(int nx, int ny, int nz, int64_t* n_verts, int64_t* n_elems, int64_t* n_edges);
+
+/* Flattened apf::makeMdsBox(nx, ny, nz, wx, wy, wz, true): coordinates,
+   element vertices and edge vertices in exactly the MDS numbering and
+   downward order that BoxBuilder (mds/apfBox.cc:68-328) and
+   apf::buildElement (apf/apfMesh2.cc:72) produce.  Arrays are caller
+   allocated with the sizes from sprg_box_counts. */
+int sprg_box_fill(int nx, int ny, int nz, double wx, double wy, double wz,
+                  double* coords, int32_t* elem_verts, int32_t* edge_verts);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
