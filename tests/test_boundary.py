@@ -68,8 +68,8 @@ def test_oracle_adjacency_is_mds_get_up_order(oracle_lib):
     first), their faces (newest first), then tets, as mds get_up does."""
     o = oracle_lib.OracleMesh.box(1, 1, 1)
     off, adj = o.v2e_off, o.v2e
-    # vertex 0 touches all six Kuhn tets; vertex 6 too; the other corners fewer
-    assert off[1] - off[0] == 6 and off[7] - off[6] == 6
+    # the ends of the cube diagonal (grid vertices 0 and 7) touch all six Kuhn tets
+    assert off[1] - off[0] == 6 and off[8] - off[7] == 6
     for v in range(8):
         s = adj[off[v]:off[v + 1]]
         assert len(set(s.tolist())) == len(s)
