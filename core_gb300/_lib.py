@@ -37,7 +37,7 @@ EXPORTS = [
     "sprg_get_target_spr_size_field", "sprg_measure_edges", "sprg_measure_edges_aniso",
     "sprg_mark_edges", "sprg_measure_quality", "sprg_estimate_and_mark",
     "sprg_estimate_and_mark_resident", "sprg_apply_marks", "sprg_last_launch_count",
-    "sprg_box_counts", "sprg_box_fill",
+    "sprg_box_counts", "sprg_box_fill", "sprg_profile_enable", "sprg_profile_flush", "sprg_profile_report",
 ]
 
 
@@ -110,6 +110,10 @@ def load():
     lib.sprg_estimate_and_mark_resident.argtypes = [P, P, D, P, P]
     lib.sprg_apply_marks.argtypes = [ctypes.c_int64, P, P, P, ctypes.POINTER(ctypes.c_long),
                                      ctypes.POINTER(ctypes.c_long)]
+    lib.sprg_profile_enable.argtypes = [P, I]
+    lib.sprg_profile_flush.argtypes = [P]
+    lib.sprg_profile_report.argtypes = [P, I]
+    lib.sprg_profile_report.restype = ctypes.c_char_p
     lib.sprg_last_launch_count.argtypes = [P]
     lib.sprg_last_launch_count.restype = ctypes.c_int64
     lib.sprg_box_counts.argtypes = [I, I, I, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),

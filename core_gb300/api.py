@@ -64,6 +64,16 @@ class Context:
     def set_stream(self, stream_handle):
         self._check(self._lib.sprg_set_stream(self.h, ctypes.c_void_p(stream_handle)))
 
+    def profile(self, on=True):
+        """Per-kernel CUDA-event timing on the context stream."""
+        self._check(self._lib.sprg_profile_enable(self.h, 1 if on else 0))
+
+    def profile_report(self, reset=True):
+        """{kernel: (launches, total_ms)} since the last reset."""
+        import json
+        raw = json.loads(self._lib.sprg_profile_report(self.h, 1 if reset else 0).decode())
+        return {k: (int(v[0]), float(v[1])) for k, v in raw.items()}
+
     @property
     def last_launch_count(self):
         return int(self._lib.sprg_last_launch_count(self.h))

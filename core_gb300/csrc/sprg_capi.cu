@@ -5,6 +5,7 @@
 
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -35,6 +36,13 @@ struct sprg_ctx {
   std::string err_msg;
   int64_t launches = 0;
   sprg_size_info last_info{};
+  // per-kernel CUDA-event timing (sprg_profile_*)
+  bool prof = false;
+  std::vector<cudaEvent_t> ev_pool;
+  size_t ev_used = 0;
+  std::vector<std::pair<std::string, size_t>> pending;  // name, index of start event
+  std::map<std::string, std::pair<int64_t, double>> prof_acc;
+  std::string prof_json;
 };
 
 namespace {
@@ -116,12 +124,32 @@ int set_device(sprg_ctx* c) {
   return SPRG_OK;
 }
 
+// ---- per-kernel timing ----------------------------------------------------
+// When profiling is on, every kernel launch of the pass is bracketed by two
+// events from a preallocated pool, recorded on the launching stream.
+void prof_begin(sprg_ctx* c, const char* name) {
+  if (!c->prof) return;
+  if (c->ev_used + 2 > c->ev_pool.size()) return;  // pool exhausted: stop recording
+  cudaEventRecord(c->ev_pool[c->ev_used], c->stream);
+  c->pending.emplace_back(name, c->ev_used);
+  c->ev_used += 2;
+}
+void prof_end(sprg_ctx* c) {
+  if (!c->prof || c->pending.empty()) return;
+  size_t i = c->pending.back().second;
+  if (i + 1 < c->ev_pool.size()) cudaEventRecord(c->ev_pool[i + 1], c->stream);
+}
+#define PB(name) prof_begin(c, name)
+#define PE() prof_end(c)
+
 // ---- pipeline steps on resident buffers -------------------------------
 
 int step_grad(sprg_ctx* c, int ncin) {
   DevMesh& m = c->m;
   ENSURE(c->ip, sizeof(double) * (size_t)m.T * 3 * ncin);
+  PB("grad_ip_f64");
   launch_grad_ip_f64(m, P<double>(c->f), ncin, P<double>(c->ip), c->stream);
+  PE();
   c->launches += 1;
   c->ip_nc = 3 * ncin;
   c->ip_valid = true;
@@ -137,13 +165,17 @@ int step_recover(sprg_ctx* c) {
   ENSURE(c->slab, sizeof(double) * (size_t)expand_grid() * expand_max_elems() * (4 + nc + 1));
   CK(cudaMemsetAsync(c->xcount.p, 0, sizeof(int), c->stream));
   ExpandList xl{P<int>(c->xitems), P<int>(c->xcount), m.V};
+  PB("recover_f64");
   launch_recover_f64(m, P<double>(c->ip), nc, P<double>(c->rec), xl, P<DevStatus>(c->status), c->stream);
+  PE();
   c->launches += 1;
   int rc = check_launch(c, "recover");
   if (rc) return rc;
   // patches that need growth: the reference growth order, on the device
+  PB("expand_f64");
   launch_expand_f64(m, P<double>(c->ip), nc, P<double>(c->rec), xl, P<double>(c->slab), P<DevStatus>(c->status),
                     c->stream);
+  PE();
   c->launches += 1;
   return check_launch(c, "expand");
 }
@@ -159,11 +191,19 @@ int step_size(sprg_ctx* c, int mode, double adapt_ratio, double target, double a
   ENSURE(c->out3, sizeof(double) * 4);
   double p = 1, d = m.dim;
   double gexp = (2 * d) / (2 * p + d);
+  PB("error_f64");
   launch_error_f64(m, P<double>(c->ip), nc, P<double>(c->rec), P<double>(c->err), P<double>(c->partials), nb, gexp,
                    c->stream);
+  PE();
+  PB("size_factor");
   launch_size_factor(P<double>(c->partials), nb, mode, adapt_ratio, target, m.dim, P<double>(c->out3), c->stream);
+  PE();
+  PB("esize_f64");
   launch_esize_f64(m, P<double>(c->err), P<double>(c->out3), mode, alpha, beta, P<double>(c->esize), c->stream);
+  PE();
+  PB("average_f64");
   launch_average(m, P<double>(c->esize), P<double>(c->size), c->stream);
+  PE();
   c->launches += 4;
   c->size_valid = true;
   return check_launch(c, "size field");
@@ -172,7 +212,9 @@ int step_size(sprg_ctx* c, int mode, double adapt_ratio, double target, double a
 int step_measure_iso(sprg_ctx* c) {
   DevMesh& m = c->m;
   ENSURE(c->L, sizeof(double) * (size_t)m.E);
+  PB("measure_f64");
   launch_measure_iso_f64(m, P<double>(c->size), P<double>(c->L), c->stream);
+  PE();
   c->launches += 1;
   c->L_valid = true;
   return check_launch(c, "measure");
@@ -308,6 +350,7 @@ int sprg_destroy(sprg_ctx* c) {
                     &c->size,  &c->L,       &c->flags, &c->q,    &c->sizes3,  &c->frames9, &c->partials,
                     &c->out3,  &c->status,  &c->count, &c->xitems, &c->xcount, &c->slab, &c->bits};
   for (DevBuf* b : bufs) release(*b);
+  for (auto& e : c->ev_pool) cudaEventDestroy(e);
   if (c->own) cudaStreamDestroy(c->own);
   delete c;
   return SPRG_OK;
@@ -522,7 +565,9 @@ static int pass_resident(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uin
   if ((rc = reset_status(c)) || (rc = step_grad(c, 1)) || (rc = step_recover(c)) ||
       (rc = step_size(c, 0, adapt_ratio, 0, 0, 0)) || (rc = step_measure_iso(c)))
     return rc;
+  PB("mark_bits");
   launch_mark_bits(c->m.E, P<double>(c->L), d_split, d_collapse, c->stream);
+  PE();
   c->launches += 1;
   return check_launch(c, "mark bits");
 }
@@ -571,6 +616,55 @@ int sprg_estimate_and_mark(sprg_ctx* c, const double* u, double adapt_ratio, dou
   if (n_split) *n_split = (long)nspl;
   if (n_collapse) *n_collapse = (long)ncol;
   return fill_info(c, info);
+}
+
+int sprg_profile_enable(sprg_ctx* c, int on) {
+  if (!c) return SPRG_EINVAL;
+  int rc = set_device(c);
+  if (rc) return rc;
+  if (on && c->ev_pool.empty()) {
+    c->ev_pool.resize(8192);
+    for (auto& e : c->ev_pool) CK(cudaEventCreate(&e));
+  }
+  c->prof = on != 0;
+  return SPRG_OK;
+}
+
+int sprg_profile_flush(sprg_ctx* c) {
+  if (!c) return SPRG_EINVAL;
+  int rc = set_device(c);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(c->stream));
+  for (auto& p : c->pending) {
+    float ms = 0;
+    if (p.second + 1 < c->ev_pool.size() &&
+        cudaEventElapsedTime(&ms, c->ev_pool[p.second], c->ev_pool[p.second + 1]) == cudaSuccess) {
+      auto& a = c->prof_acc[p.first];
+      a.first += 1;
+      a.second += ms;
+    }
+  }
+  c->pending.clear();
+  c->ev_used = 0;
+  return SPRG_OK;
+}
+
+const char* sprg_profile_report(sprg_ctx* c, int reset) {
+  if (!c) return "{}";
+  sprg_profile_flush(c);
+  std::string j = "{";
+  bool first = true;
+  for (auto& kv : c->prof_acc) {
+    char buf[160];
+    snprintf(buf, sizeof buf, "%s\"%s\": [%lld, %.6f]", first ? "" : ", ", kv.first.c_str(),
+             (long long)kv.second.first, kv.second.second);
+    j += buf;
+    first = false;
+  }
+  j += "}";
+  c->prof_json = j;
+  if (reset) c->prof_acc.clear();
+  return c->prof_json.c_str();
 }
 
 int sprg_apply_marks(int64_t n_edges, const uint32_t* split_bits, const uint32_t* collapse_bits, int32_t* flags,

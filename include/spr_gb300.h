@@ -175,6 +175,13 @@ int sprg_estimate_and_mark_resident(sprg_ctx* ctx, const double* d_u, double ada
 int sprg_apply_marks(int64_t n_edges, const uint32_t* split_bits, const uint32_t* collapse_bits, int32_t* flags,
                      long* n_split, long* n_collapse);
 
+/* Per-kernel timing: when enabled, each kernel launch is bracketed by CUDA
+   events on the context stream.  sprg_profile_report returns a JSON object
+   {"kernel": [launches, total_ms], ...} accumulated since the last reset. */
+int sprg_profile_enable(sprg_ctx* ctx, int on);
+int sprg_profile_flush(sprg_ctx* ctx);
+const char* sprg_profile_report(sprg_ctx* ctx, int reset);
+
 /* Number of kernel launches issued by the last call (instrumentation). */
 int64_t sprg_last_launch_count(const sprg_ctx* ctx);
 
