@@ -38,17 +38,18 @@ def parse():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
     p.add_argument("--n", type=int, default=160, help="box cells per side (160 -> 24.6M tets)")
-    p.add_argument("--adapt-ratio", type=float, default=0.1)
+    p.add_argument("--adapt-ratio", type=float, default=0.008,
+                   help="getSPRSizeField adapt ratio (0.008 gives a balanced split/collapse mix at 160^3)")
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     return p.parse_args()
 
 
-def workload_desc(n, precision):
+def workload_desc(n, precision, adapt_ratio=0.008):
     V, T, E = (n + 1) ** 3, 6 * n ** 3, 3 * n * (n + 1) ** 2 + 3 * n ** 2 * (n + 1) + n ** 3
     return {"workload": f"{n}^3 jittered unit box, {T} tets, {V} vertices, {E} edges; u = 4 Gaussian bumps "
-                        f"+ linear ramp (seed 4); interior jitter +-0.2h (seed 4); getSPRSizeField adapt_ratio 0.1; "
+                        f"+ linear ramp (seed 4); interior jitter +-0.2h (seed 4); getSPRSizeField adapt_ratio {adapt_ratio}; "
                         f"split/collapse bitmaps", "precision": precision, "n_verts": V, "n_elems": T, "n_edges": E,
             "l2": "inputs larger than L2 (working set > 129 MB)"}
 
@@ -133,22 +134,23 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 # CPU arms
 # ---------------------------------------------------------------------------
-def cpu_port_run(budget_s, threads, n_sample=None):
+def cpu_port_run(budget_s, threads, n_sample=None, ratio=0.008):
     """Times the oracle port of the reference path on the host cores on a
     bounded sample of the same workload family.  Returns (vertices/s, desc)."""
     import oracle
     from core_gb300 import workload
     used = oracle.set_threads(threads)
     n = n_sample or 48
+    ratio = ratio * n / 160.0  # same lengths-to-size regime as the 160^3 workload
     m = workload.box(n, jitter=0.2, seed=4)
     u = workload.bump_field(m.coords, seed=4)
     o = oracle.OracleMesh.box(n, n, n)
     o.set_coords(m.coords)
-    o.estimate_and_mark(u, 0.1)  # warm
+    o.estimate_and_mark(u, ratio)  # warm
     t0 = time.perf_counter()
     passes = 0
     while True:
-        rc = o.estimate_and_mark(u, 0.1)[0]
+        rc = o.estimate_and_mark(u, ratio)[0]
         assert rc == 0
         passes += 1
         el = time.perf_counter() - t0
@@ -168,14 +170,14 @@ def reference_arm(args):
     desc = None
     budget = max(1.0, min(20.0, 60.0 / max(1, args.steps + args.warmup)))
     for i in range(args.warmup + args.steps):
-        v, desc = cpu_port_run(budget, threads)
+        v, desc = cpu_port_run(budget, threads, ratio=args.adapt_ratio)
         if i >= args.warmup:
             steps.append(v)
     value = float(np.mean(steps))
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-           "config": workload_desc(args.n, "fp64"),
+           "config": workload_desc(args.n, "fp64", args.adapt_ratio),
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": desc["cores"], "kind": "port",
                             "sample": desc["sample"]},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -208,7 +210,11 @@ def gpu_arm(args):
     ctx = cg.Context(m, device=local, precision=args.precision)
     torch.cuda.synchronize(dev)
     t_flatten = time.perf_counter() - t0
-    stream = torch.cuda.current_stream(dev)
+    # an explicit stream: the library launches on it and the timing events are
+    # recorded on it (the legacy default stream's handle is 0, which the
+    # library reads as "use the context's own stream")
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
     d_u = torch.from_numpy(u).to(dev)
     nw = (E + 31) // 32
@@ -303,14 +309,14 @@ def gpu_arm(args):
     cpu = None
     if not args.no_cpu_baseline:
         try:
-            v, desc = cpu_port_run(args.cpu_seconds, os.cpu_count() or 1)
+            v, desc = cpu_port_run(args.cpu_seconds, os.cpu_count() or 1, ratio=args.adapt_ratio)
             cpu = {"value": v, "unit": UNIT, "cores": desc["cores"], "kind": "port", "sample": desc["sample"]}
         except Exception as e:  # the baseline is reported, never the target
             cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": f"unavailable: {e}"}
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32",
-           "data": "synthetic", "config": workload_desc(args.n, args.precision), "roofline": roof,
+           "data": "synthetic", "config": workload_desc(args.n, args.precision, args.adapt_ratio), "roofline": roof,
            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches_per_step * args.steps),
            "clocks": clk, "phases": phases,
            "setup_s": {"mesh_build": round(t_mesh, 3), "flatten_upload": round(t_flatten, 3)}}

@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "spr_gb300.h"
+#include "sprg_fast.h"
 #include "sprg_internal.h"
 
 using namespace sprg;
@@ -33,6 +34,10 @@ struct sprg_ctx {
   bool ip_valid = false, size_valid = false, L_valid = false;
   // scratch
   DevBuf partials, out3, status, count, xitems, xcount, slab, bits;
+  // FP32 path buffers
+  DevBuf vrec, rec32, q32, size32, fcnt, guard;
+  static constexpr int kGuardCap = 1 << 20;
+  static constexpr float kGuardRel = 1e-4f;
   std::string err_msg;
   int64_t launches = 0;
   sprg_size_info last_info{};
@@ -173,8 +178,8 @@ int step_recover(sprg_ctx* c) {
   if (rc) return rc;
   // patches that need growth: the reference growth order, on the device
   PB("expand_f64");
-  launch_expand_f64(m, P<double>(c->ip), nc, P<double>(c->rec), xl, P<double>(c->slab), P<DevStatus>(c->status),
-                    c->stream);
+  launch_expand_f64(m, P<double>(c->ip), nullptr, nc, P<double>(c->rec), xl, P<double>(c->slab),
+                    P<DevStatus>(c->status), c->stream);
   PE();
   c->launches += 1;
   return check_launch(c, "expand");
@@ -229,6 +234,15 @@ int fill_info(sprg_ctx* c, sprg_size_info* info) {
   c->last_info.error_sum = o3[1];
   c->last_info.size_factor = o3[2];
   c->last_info.n_expanded = xc;
+  c->last_info.n_fp64_refits = 0;
+  c->last_info.n_guard_edges = 0;
+  if (c->precision == SPRG_FP32 && c->fcnt.p) {
+    int fc[2] = {0, 0};
+    CK(cudaMemcpy(fc, c->fcnt.p, sizeof fc, cudaMemcpyDeviceToHost));
+    c->last_info.n_fp64_refits = fc[0];
+    c->last_info.n_guard_edges = fc[1];
+    c->last_info.n_expanded = xc - fc[0];
+  }
   if (info) *info = c->last_info;
   return SPRG_OK;
 }
@@ -348,7 +362,8 @@ int sprg_destroy(sprg_ctx* c) {
   DevBuf* bufs[] = {&c->xyz,   &c->xyz32,   &c->ev,   &c->edv,   &c->poff,    &c->pel,    &c->aoff,
                     &c->ael,   &c->tmp,     &c->f,    &c->ip,    &c->rec,     &c->err,    &c->esize,
                     &c->size,  &c->L,       &c->flags, &c->q,    &c->sizes3,  &c->frames9, &c->partials,
-                    &c->out3,  &c->status,  &c->count, &c->xitems, &c->xcount, &c->slab, &c->bits};
+                    &c->out3,  &c->status,  &c->count, &c->xitems, &c->xcount, &c->slab, &c->bits,
+                    &c->vrec,  &c->rec32,   &c->q32,  &c->size32, &c->fcnt,   &c->guard};
   for (DevBuf* b : bufs) release(*b);
   for (auto& e : c->ev_pool) cudaEventDestroy(e);
   if (c->own) cudaStreamDestroy(c->own);
@@ -360,7 +375,9 @@ const char* sprg_last_error(const sprg_ctx* c) { return c ? c->err_msg.c_str() :
 
 int sprg_set_precision(sprg_ctx* c, int precision) {
   if (!c) return SPRG_EINVAL;
-  if (precision != SPRG_FP64) return fail(c, SPRG_EINVAL, "unsupported precision");
+  if (precision != SPRG_FP64 && precision != SPRG_FP32) return fail(c, SPRG_EINVAL, "unknown precision");
+  if (precision == SPRG_FP32 && c->m.dim != 3)
+    return fail(c, SPRG_EINVAL, "the FP32 path covers tet meshes; use SPRG_FP64 for triangles");
   c->precision = precision;
   return SPRG_OK;
 }
@@ -560,8 +577,65 @@ int sprg_measure_quality(sprg_ctx* c, const double* size, const double* sizes, c
   return sync_and_status(c);
 }
 
+// FP32 pass: packed double-float records, FP32 fits and sweeps, FP64
+// reference path for ill-conditioned or growing patches (sprg_kernels_f32.cu).
+static int pass_fast(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_t* d_collapse) {
+  DevMesh& m = c->m;
+  int rc;
+  int nb = fast_error_blocks(m.T);
+  ENSURE(c->vrec, 32 * (size_t)m.V);
+  ENSURE(c->rec32, 16 * (size_t)m.V);
+  ENSURE(c->q32, 4 * (size_t)m.T);
+  ENSURE(c->size32, 4 * (size_t)m.V);
+  ENSURE(c->rec, 24 * (size_t)m.V);
+  ENSURE(c->xitems, sizeof(int) * (size_t)m.V);
+  ENSURE(c->xcount, sizeof(int));
+  ENSURE(c->slab, sizeof(double) * (size_t)expand_grid() * expand_max_elems() * (4 + 3 + 1));
+  ENSURE(c->fcnt, 4 * sizeof(int));
+  ENSURE(c->guard, sizeof(int) * (size_t)sprg_ctx::kGuardCap);
+  ENSURE(c->partials, sizeof(double) * 2 * (size_t)(nb > 0 ? nb : 1));
+  ENSURE(c->out3, sizeof(double) * 4);
+  if ((rc = reset_status(c))) return rc;
+  CK(cudaMemsetAsync(c->xcount.p, 0, sizeof(int), c->stream));
+  CK(cudaMemsetAsync(c->fcnt.p, 0, 4 * sizeof(int), c->stream));
+  ExpandList xl{P<int>(c->xitems), P<int>(c->xcount), m.V};
+  float4* vrec = P<float4>(c->vrec);
+  float4* rec32 = P<float4>(c->rec32);
+  PB("prep_f32");
+  fast_prep(m, P<double>(c->f), vrec, c->stream);
+  PE();
+  PB("recover_f32");
+  fast_recover(m, vrec, rec32, xl, P<int>(c->fcnt), c->stream);
+  PE();
+  PB("expand_f64");
+  launch_expand_f64(m, nullptr, P<double>(c->f), 3, P<double>(c->rec), xl, P<double>(c->slab),
+                    P<DevStatus>(c->status), c->stream);
+  PE();
+  PB("merge_f64");
+  fast_merge_ref(xl, P<double>(c->rec), rec32, c->stream);
+  PE();
+  PB("error_f32");
+  fast_error(m, vrec, rec32, P<float>(c->q32), P<double>(c->partials), nb, c->stream);
+  PE();
+  PB("size_factor");
+  launch_size_factor(P<double>(c->partials), nb, 0, adapt_ratio, 0, m.dim, P<double>(c->out3), c->stream);
+  PE();
+  PB("average_f32");
+  fast_average(m, P<float>(c->q32), P<double>(c->out3), P<float>(c->size32), c->stream);
+  PE();
+  PB("measure_f32");
+  fast_measure(m, vrec, P<float>(c->size32), d_split, d_collapse, nullptr, P<int>(c->guard), P<int>(c->fcnt) + 1,
+               sprg_ctx::kGuardCap, sprg_ctx::kGuardRel, c->stream);
+  PE();
+  c->launches += 8;
+  c->size_valid = false;  // the FP64 size buffer is filled on demand
+  c->L_valid = false;
+  return check_launch(c, "fast pass");
+}
+
 static int pass_resident(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_t* d_collapse) {
   int rc;
+  if (c->precision == SPRG_FP32) return pass_fast(c, adapt_ratio, d_split, d_collapse);
   if ((rc = reset_status(c)) || (rc = step_grad(c, 1)) || (rc = step_recover(c)) ||
       (rc = step_size(c, 0, adapt_ratio, 0, 0, 0)) || (rc = step_measure_iso(c)))
     return rc;
@@ -608,6 +682,12 @@ int sprg_estimate_and_mark(sprg_ctx* c, const double* u, double adapt_ratio, dou
   CK(cudaMemcpyAsync(&ncol, c->count.p, sizeof ncol, cudaMemcpyDeviceToHost, c->stream));
   if ((rc = apply_bits(c, SPRG_MARK_SPLIT, sb, P<int>(c->flags)))) return rc;
   CK(cudaMemcpyAsync(&nspl, c->count.p, sizeof nspl, cudaMemcpyDeviceToHost, c->stream));
+  if (c->precision == SPRG_FP32) {
+    ENSURE(c->size, sizeof(double) * (size_t)m.V);
+    fast_size_to_f64(m.V, P<float>(c->size32), P<double>(c->size), c->stream);
+    c->launches += 1;
+    c->size_valid = true;
+  }
   if (size_out)
     CK(cudaMemcpyAsync(size_out, c->size.p, sizeof(double) * (size_t)m.V, cudaMemcpyDeviceToHost, c->stream));
   rc = sync_and_status(c);

@@ -46,8 +46,10 @@ void launch_recover_f64(const DevMesh& m, const double* ip, int nc, double* rec,
 // Patches on the expansion list: grow as the reference does, then fit.
 // The list length is read on the device (no host round trip).
 // slab: expand_grid() * expand_max_elems() * (4 + nc + 1) doubles.
-void launch_expand_f64(const DevMesh& m, const double* ip, int nc, double* rec, ExpandList xl, double* slab,
-                       DevStatus* st, cudaStream_t s);
+// ip may be NULL: the scalar field u's element gradients are computed in
+// place (FP32 path, which keeps no ip field).
+void launch_expand_f64(const DevMesh& m, const double* ip, const double* u, int nc, double* rec, ExpandList xl,
+                       double* slab, DevStatus* st, cudaStream_t s);
 int expand_max_elems();
 int expand_grid();
 // Per-element error terms + deterministic block partials (2 per block).

@@ -53,6 +53,21 @@ __device__ __forceinline__ V3 elem_ip_point(const DevMesh& m, int e) {
   return p;
 }
 
+// gradient of a scalar P1 field at the order-1 integration point of e
+// (ScalarElement::grad, apf/apfScalarElement.cc:18)
+__device__ __forceinline__ V3 elem_grad_scalar(const DevMesh& m, int e, const double* __restrict__ f) {
+  const int* ev = m.ev + (size_t)e * m.nn;
+  V3 x[4];
+  for (int a = 0; a < m.nn; ++a) x[a] = load_xyz(m.xyz, ev[a]);
+  M3 J = ref::jacobian(x, m.nn, m.dim);
+  M3 jinv = ref::jacobian_inverse(J, m.dim);
+  V3 lg[4];
+  ref::shape_grads(m.dim, lg);
+  V3 g = ref::scale(ref::mulv(jinv, lg[0]), f[ev[0]]);
+  for (int a = 1; a < m.nn; ++a) g = ref::add(g, ref::scale(ref::mulv(jinv, lg[a]), f[ev[a]]));
+  return g;
+}
+
 // ---------------------------------------------------------------------
 // spr::getGradIPField
 // ---------------------------------------------------------------------
@@ -235,8 +250,8 @@ __device__ void warp_sort_set(int* S, int n, int* tmp) {
 
 // QR fit over the element set S (sorted).  Returns false if rank deficient.
 // rows: n x (NT + nc + 1) doubles; the last column holds the reflector.
-__device__ bool slab_fit(const DevMesh& m, const int* S, int n, const double* __restrict__ ip, int nc,
-                         double* rows, int v, double* rec) {
+__device__ bool slab_fit(const DevMesh& m, const int* S, int n, const double* __restrict__ ip,
+                         const double* __restrict__ u, int nc, double* rows, int v, double* rec) {
   const int lane = threadIdx.x & 31;
   const int NT = m.dim == 3 ? 4 : 3;
   const int W = NT + nc;
@@ -248,7 +263,12 @@ __device__ bool slab_fit(const DevMesh& m, const int* S, int n, const double* __
     double* rw = rows + (size_t)i * LD;
     rw[0] = 1.0; rw[1] = p.v[0]; rw[2] = p.v[1];
     if (NT == 4) rw[3] = p.v[2];
-    for (int c = 0; c < nc; ++c) rw[NT + c] = ip[(size_t)el * nc + c];
+    if (ip) {
+      for (int c = 0; c < nc; ++c) rw[NT + c] = ip[(size_t)el * nc + c];
+    } else {  // no resident ip field: the gradient of the scalar field u
+      V3 g = elem_grad_scalar(m, el, u);
+      for (int c = 0; c < 3; ++c) rw[NT + c] = g.v[c];
+    }
   }
   __syncwarp();
   for (int k = 0; k < NT; ++k) {
@@ -293,7 +313,8 @@ __device__ bool slab_fit(const DevMesh& m, const int* S, int n, const double* __
   return true;
 }
 
-__global__ void __launch_bounds__(32) k_expand(DevMesh m, const double* __restrict__ ip, int nc,
+__global__ void __launch_bounds__(32) k_expand(DevMesh m, const double* __restrict__ ip,
+                                               const double* __restrict__ u, int nc,
                                                double* __restrict__ rec, const int* __restrict__ items,
                                                const int* __restrict__ n_items_ptr, int cap, double* slab,
                                                DevStatus* st) {
@@ -330,7 +351,7 @@ __global__ void __launch_bounds__(32) k_expand(DevMesh m, const double* __restri
       if (overflow || nS > kExpandMaxElems) { failed = true; break; }
       int n0 = nS;
       warp_sort_set(S, n0, tmp);
-      if (slab_fit(m, S, n0, ip, nc, rows, v, rec)) { done = true; break; }
+      if (slab_fit(m, S, n0, ip, u, nc, rows, v, rec)) { done = true; break; }
       for (int i = lane; i < n0; i += 32) old[i] = S[i];
       __syncwarp();
       for (int sd = m.dim - 1; sd >= 0 && !done; --sd) {
@@ -357,7 +378,7 @@ __global__ void __launch_bounds__(32) k_expand(DevMesh m, const double* __restri
         if (overflow || nS > kExpandMaxElems) { failed = true; break; }
         int n1 = nS;
         warp_sort_set(S, n1, tmp);
-        if (slab_fit(m, S, n1, ip, nc, rows, v, rec)) { done = true; break; }
+        if (slab_fit(m, S, n1, ip, u, nc, rows, v, rec)) { done = true; break; }
       }
       if (!done && !failed && !(nS > n0)) failed = true;  // "all hope is lost"
     }
@@ -735,9 +756,9 @@ int expand_max_elems() { return kExpandMaxElems; }
 
 int expand_grid() { return kExpandGrid; }
 
-void launch_expand_f64(const DevMesh& m, const double* ip, int nc, double* rec, ExpandList xl, double* slab,
-                       DevStatus* st, cudaStream_t s) {
-  k_expand<<<kExpandGrid, 32, 0, s>>>(m, ip, nc, rec, xl.items, xl.count, xl.cap, slab, st);
+void launch_expand_f64(const DevMesh& m, const double* ip, const double* u, int nc, double* rec, ExpandList xl,
+                       double* slab, DevStatus* st, cudaStream_t s) {
+  k_expand<<<kExpandGrid, 32, 0, s>>>(m, ip, u, nc, rec, xl.items, xl.count, xl.cap, slab, st);
 }
 
 int error_blocks(int T) { return nblk(T); }

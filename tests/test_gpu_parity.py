@@ -236,7 +236,8 @@ def test_resident_bitmaps_and_determinism(gpu_lib, oracle_lib):
     d_u = torch.from_numpy(u).cuda()
     bits = torch.zeros(2 * nw, dtype=torch.int32, device="cuda")
     with cg.Context(m) as ctx:
-        stream = torch.cuda.current_stream()
+        stream = torch.cuda.Stream()
+        torch.cuda.set_stream(stream)
         ctx.set_stream(stream.cuda_stream)
         outs = []
         for _ in range(2):
