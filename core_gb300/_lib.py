@@ -38,7 +38,9 @@ EXPORTS = [
     "sprg_mark_edges", "sprg_measure_quality", "sprg_estimate_and_mark",
     "sprg_estimate_and_mark_resident", "sprg_apply_marks", "sprg_last_launch_count",
     "sprg_box_counts", "sprg_box_fill", "sprg_profile_enable", "sprg_profile_flush", "sprg_profile_report",
+    "sprg_spr_size_from_recovered_noalloc",
 ]
+NOALLOC_MAX_ELEMS = 1 << 20
 
 
 class SprgError(RuntimeError):
@@ -114,6 +116,8 @@ def load():
     lib.sprg_profile_flush.argtypes = [P]
     lib.sprg_profile_report.argtypes = [P, I]
     lib.sprg_profile_report.restype = ctypes.c_char_p
+    lib.sprg_spr_size_from_recovered_noalloc.argtypes = [I, ctypes.c_int64, ctypes.c_int64, P, P, P, P, P, I, P, D,
+                                                         P, ctypes.POINTER(D), P]
     lib.sprg_last_launch_count.argtypes = [P]
     lib.sprg_last_launch_count.restype = ctypes.c_int64
     lib.sprg_box_counts.argtypes = [I, I, I, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),

@@ -24,6 +24,7 @@ UNITS = {
     "sprg_kernels_f64.cu": ["-fmad=false"],
     "sprg_kernels_f32.cu": [],
     "sprg_capi.cu": [],
+    "sprg_noalloc.cu": [],
     "sprg_box.cpp": ["-x", "cu"],
 }
 

@@ -185,6 +185,32 @@ const char* sprg_profile_report(sprg_ctx* ctx, int reset);
 /* Number of kernel launches issued by the last call (instrumentation). */
 int64_t sprg_last_launch_count(const sprg_ctx* ctx);
 
+/* ---- size field without device allocation ------------------------------- */
+
+/* No counterpart in the reference.  The size-field stage of
+   getSPRSizeField (element errors, size factor, element sizes, vertex
+   average) for callers that cannot allocate device memory: a code whose
+   memory manager owns the device heap, or a thread that cannot take the
+   synchronisation a cudaMalloc/cudaFree may imply.  All pointers except
+   size_factor_out are device pointers supplied by the caller: the mesh
+   (coordinates, element vertices, vertex-to-element adjacency whose order
+   fixes the averaging order), the integration-point field d_ip (n_elems x
+   ncomp) and the recovered field d_rec (n_verts x ncomp, e.g. from
+   sprg_recover_field); the result d_size has n_verts doubles.  The call
+   allocates nothing: its scratch is a fixed file-scope device array sized for
+   SPRG_NOALLOC_MAX_ELEMS elements (about 17 MB, held by every GPU that loads
+   the library until exit); larger meshes are rejected with SPRG_EINVAL.  The
+   first call on a device resolves that array's address (do it before any
+   stream capture).  Calls share the array: calls that overlap on the GPU
+   race.  Enqueued on `stream` (cudaStream_t, NULL = legacy default); when
+   size_factor_out (host) is given, the call waits and stores the size factor. */
+#define SPRG_NOALLOC_MAX_ELEMS (1 << 20)
+int sprg_spr_size_from_recovered_noalloc(int dim, int64_t n_verts, int64_t n_elems, const double* d_coords,
+                                         const int32_t* d_elem_verts, const int32_t* d_vert_elem_offsets,
+                                         const int32_t* d_vert_elems, const double* d_ip, int ncomp,
+                                         const double* d_rec, double adapt_ratio, double* d_size,
+                                         double* size_factor_out, void* stream);
+
 /* ---- box meshes --------------------------------------------------------- */
 
 /* Entity counts of apf::makeMdsBox(nx, ny, nz, wx, wy, wz, true)
