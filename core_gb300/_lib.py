@@ -38,7 +38,7 @@ EXPORTS = [
     "sprg_mark_edges", "sprg_measure_quality", "sprg_estimate_and_mark",
     "sprg_estimate_and_mark_resident", "sprg_apply_marks", "sprg_last_launch_count",
     "sprg_box_counts", "sprg_box_fill", "sprg_profile_enable", "sprg_profile_flush", "sprg_profile_report",
-    "sprg_spr_size_from_recovered_noalloc",
+    "sprg_spr_size_from_recovered_noalloc", "sprg_debug_read",
 ]
 NOALLOC_MAX_ELEMS = 1 << 20
 
@@ -71,6 +71,7 @@ class SizeInfo(ctypes.Structure):
         ("n_expanded", ctypes.c_int64),
         ("n_fp64_refits", ctypes.c_int64),
         ("n_guard_edges", ctypes.c_int64),
+        ("n_guard_unresolved", ctypes.c_int64),
     ]
 
     def as_dict(self):
@@ -118,6 +119,7 @@ def load():
     lib.sprg_profile_report.restype = ctypes.c_char_p
     lib.sprg_spr_size_from_recovered_noalloc.argtypes = [I, ctypes.c_int64, ctypes.c_int64, P, P, P, P, P, I, P, D,
                                                          P, ctypes.POINTER(D), P]
+    lib.sprg_debug_read.argtypes = [P, ctypes.c_char_p, P, ctypes.c_size_t]
     lib.sprg_last_launch_count.argtypes = [P]
     lib.sprg_last_launch_count.restype = ctypes.c_int64
     lib.sprg_box_counts.argtypes = [I, I, I, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),

@@ -74,6 +74,12 @@ class Context:
         raw = json.loads(self._lib.sprg_profile_report(self.h, 1 if reset else 0).decode())
         return {k: (int(v[0]), float(v[1])) for k, v in raw.items()}
 
+    def debug_read(self, name, dtype, count):
+        """Copy of a named internal device buffer (instrumentation)."""
+        out = np.empty(count, dtype)
+        self._check(self._lib.sprg_debug_read(self.h, name.encode(), out.ctypes.data, out.nbytes))
+        return out
+
     @property
     def last_launch_count(self):
         return int(self._lib.sprg_last_launch_count(self.h))

@@ -35,9 +35,9 @@ struct sprg_ctx {
   // scratch
   DevBuf partials, out3, status, count, xitems, xcount, slab, bits;
   // FP32 path buffers
-  DevBuf vrec, rec32, q32, size32, fcnt, guard;
+  DevBuf vrec, rec32, q32, size32, fcnt, guard, tetd;
   static constexpr int kGuardCap = 1 << 20;
-  static constexpr float kGuardRel = 1e-4f;
+  static constexpr float kGuardRel = 2e-6f;
   std::string err_msg;
   int64_t launches = 0;
   sprg_size_info last_info{};
@@ -236,11 +236,13 @@ int fill_info(sprg_ctx* c, sprg_size_info* info) {
   c->last_info.n_expanded = xc;
   c->last_info.n_fp64_refits = 0;
   c->last_info.n_guard_edges = 0;
+  c->last_info.n_guard_unresolved = 0;
   if (c->precision == SPRG_FP32 && c->fcnt.p) {
-    int fc[2] = {0, 0};
+    int fc[3] = {0, 0, 0};
     CK(cudaMemcpy(fc, c->fcnt.p, sizeof fc, cudaMemcpyDeviceToHost));
     c->last_info.n_fp64_refits = fc[0];
     c->last_info.n_guard_edges = fc[1];
+    c->last_info.n_guard_unresolved = fc[2];
     c->last_info.n_expanded = xc - fc[0];
   }
   if (info) *info = c->last_info;
@@ -363,7 +365,7 @@ int sprg_destroy(sprg_ctx* c) {
                     &c->ael,   &c->tmp,     &c->f,    &c->ip,    &c->rec,     &c->err,    &c->esize,
                     &c->size,  &c->L,       &c->flags, &c->q,    &c->sizes3,  &c->frames9, &c->partials,
                     &c->out3,  &c->status,  &c->count, &c->xitems, &c->xcount, &c->slab, &c->bits,
-                    &c->vrec,  &c->rec32,   &c->q32,  &c->size32, &c->fcnt,   &c->guard};
+                    &c->vrec,  &c->rec32,   &c->q32,  &c->size32, &c->fcnt,   &c->guard, &c->tetd};
   for (DevBuf* b : bufs) release(*b);
   for (auto& e : c->ev_pool) cudaEventDestroy(e);
   if (c->own) cudaStreamDestroy(c->own);
@@ -584,7 +586,8 @@ static int pass_fast(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_
   int rc;
   int nb = fast_error_blocks(m.T);
   ENSURE(c->vrec, 32 * (size_t)m.V);
-  ENSURE(c->rec32, 16 * (size_t)m.V);
+  ENSURE(c->rec32, 32 * (size_t)m.V);
+  ENSURE(c->tetd, 64 * (size_t)m.T);
   ENSURE(c->q32, 4 * (size_t)m.T);
   ENSURE(c->size32, 4 * (size_t)m.V);
   ENSURE(c->rec, 24 * (size_t)m.V);
@@ -604,8 +607,11 @@ static int pass_fast(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_
   PB("prep_f32");
   fast_prep(m, P<double>(c->f), vrec, c->stream);
   PE();
+  PB("tet_f32");
+  fast_tet(m, vrec, P<float4>(c->tetd), c->stream);
+  PE();
   PB("recover_f32");
-  fast_recover(m, vrec, rec32, xl, P<int>(c->fcnt), c->stream);
+  fast_recover(m, vrec, P<float4>(c->tetd), rec32, xl, P<int>(c->fcnt), c->stream);
   PE();
   PB("expand_f64");
   launch_expand_f64(m, nullptr, P<double>(c->f), 3, P<double>(c->rec), xl, P<double>(c->slab),
@@ -615,7 +621,7 @@ static int pass_fast(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_
   fast_merge_ref(xl, P<double>(c->rec), rec32, c->stream);
   PE();
   PB("error_f32");
-  fast_error(m, vrec, rec32, P<float>(c->q32), P<double>(c->partials), nb, c->stream);
+  fast_error(m, P<float4>(c->tetd), rec32, P<float>(c->q32), P<double>(c->partials), nb, c->stream);
   PE();
   PB("size_factor");
   launch_size_factor(P<double>(c->partials), nb, 0, adapt_ratio, 0, m.dim, P<double>(c->out3), c->stream);
@@ -627,7 +633,11 @@ static int pass_fast(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_
   fast_measure(m, vrec, P<float>(c->size32), d_split, d_collapse, nullptr, P<int>(c->guard), P<int>(c->fcnt) + 1,
                sprg_ctx::kGuardCap, sprg_ctx::kGuardRel, c->stream);
   PE();
-  c->launches += 8;
+  PB("guard_f64");
+  launch_guard_f64(m, P<double>(c->f), P<double>(c->out3), P<int>(c->guard), P<int>(c->fcnt) + 1,
+                   sprg_ctx::kGuardCap, d_split, d_collapse, P<int>(c->fcnt) + 2, c->stream);
+  PE();
+  c->launches += 10;
   c->size_valid = false;  // the FP64 size buffer is filled on demand
   c->L_valid = false;
   return check_launch(c, "fast pass");
@@ -696,6 +706,26 @@ int sprg_estimate_and_mark(sprg_ctx* c, const double* u, double adapt_ratio, dou
   if (n_split) *n_split = (long)nspl;
   if (n_collapse) *n_collapse = (long)ncol;
   return fill_info(c, info);
+}
+
+int sprg_debug_read(sprg_ctx* c, const char* name, void* host, size_t bytes) {
+  if (!c || !name || !host) return SPRG_EINVAL;
+  int rc = set_device(c);
+  if (rc) return rc;
+  struct { const char* n; DevBuf* b; } table[] = {
+      {"ip", &c->ip},       {"rec", &c->rec},     {"err", &c->err},       {"esize", &c->esize},
+      {"size", &c->size},   {"L", &c->L},         {"vrec", &c->vrec},     {"rec32", &c->rec32},
+      {"q32", &c->q32},     {"size32", &c->size32}, {"tetd", &c->tetd},   {"out3", &c->out3},
+      {"fcnt", &c->fcnt},   {"guard", &c->guard}, {"xitems", &c->xitems}, {"xcount", &c->xcount}};
+  for (auto& e : table) {
+    if (strcmp(e.n, name) != 0) continue;
+    if (!e.b->p) return fail(c, SPRG_ESTATE, std::string("buffer not allocated: ") + name);
+    if (bytes > e.b->bytes) bytes = e.b->bytes;
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaMemcpy(host, e.b->p, bytes, cudaMemcpyDeviceToHost));
+    return SPRG_OK;
+  }
+  return fail(c, SPRG_EINVAL, std::string("unknown buffer: ") + name);
 }
 
 int sprg_profile_enable(sprg_ctx* c, int on) {

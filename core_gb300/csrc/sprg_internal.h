@@ -72,6 +72,9 @@ void launch_mark_bits(int E, const double* L, uint32_t* split, uint32_t* collaps
 // markEntities semantics from a predicate bitmap
 void launch_apply_bits(int E, const uint32_t* bits, int which, int* flags, unsigned long long* count,
                        DevStatus* st, cudaStream_t s);
+// FP64 guard band of the FP32 path: re-decide the listed edges' bits
+void launch_guard_f64(const DevMesh& m, const double* u, const double* out3, const int* items, const int* count,
+                      int cap, uint32_t* split, uint32_t* collapse, int* unresolved, cudaStream_t s);
 void launch_quality_f64(const DevMesh& m, const double* size, const double* sizes, const double* frames,
                         double* q, cudaStream_t s);
 

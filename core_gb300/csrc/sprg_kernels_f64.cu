@@ -24,6 +24,7 @@ constexpr int kBlock = 256;
 constexpr int kExpandMaxElems = 1024;
 constexpr int kExpandHash = 4096;
 constexpr int kExpandGrid = 304;  // 2 resident single-warp blocks per SM
+constexpr int kExpandSmemRows = 96;  // patches up to this size keep their QR rows in shared memory
 
 __device__ __forceinline__ void set_status(DevStatus* st, int code, int where) {
   if (atomicCAS(&st->code, 0, code) == 0) st->where = where;
@@ -170,9 +171,9 @@ __global__ void __launch_bounds__(kBlock) k_recover(DevMesh m, const double* __r
       if (i == k) vv[r] += ((akk < 0) ? -1 : 1) * cn;
       s2 += vv[r] * vv[r];
     }
-    double rn = sqrt(warp_sum(s2));
+    double rinv = 1.0 / sqrt(warp_sum(s2));
 #pragma unroll
-    for (int r = 0; r < RPL; ++r) vv[r] /= rn;
+    for (int r = 0; r < RPL; ++r) vv[r] *= rinv;
 #pragma unroll
     for (int j = k; j < NT; ++j) {
       double d = 0;
@@ -323,9 +324,10 @@ __global__ void __launch_bounds__(32) k_expand(DevMesh m, const double* __restri
   __shared__ int tmp[kExpandMaxElems];
   __shared__ int hs[kExpandHash];
   __shared__ int nS;
+  __shared__ double srows[kExpandSmemRows * 8];
   const int lane = threadIdx.x;
   const int NT = m.dim == 3 ? 4 : 3;
-  double* rows = slab + (size_t)blockIdx.x * kExpandMaxElems * (NT + nc + 1);
+  double* grows = slab + (size_t)blockIdx.x * kExpandMaxElems * (NT + nc + 1);
   int n_items = *n_items_ptr;
   if (n_items > cap) {
     if (lane == 0 && blockIdx.x == 0) set_status(st, SPRG_EPATCH, -1);
@@ -351,6 +353,7 @@ __global__ void __launch_bounds__(32) k_expand(DevMesh m, const double* __restri
       if (overflow || nS > kExpandMaxElems) { failed = true; break; }
       int n0 = nS;
       warp_sort_set(S, n0, tmp);
+      double* rows = (n0 * (NT + nc + 1) <= kExpandSmemRows * 8) ? srows : grows;
       if (slab_fit(m, S, n0, ip, u, nc, rows, v, rec)) { done = true; break; }
       for (int i = lane; i < n0; i += 32) old[i] = S[i];
       __syncwarp();
@@ -378,7 +381,8 @@ __global__ void __launch_bounds__(32) k_expand(DevMesh m, const double* __restri
         if (overflow || nS > kExpandMaxElems) { failed = true; break; }
         int n1 = nS;
         warp_sort_set(S, n1, tmp);
-        if (slab_fit(m, S, n1, ip, u, nc, rows, v, rec)) { done = true; break; }
+        double* rows1 = (n1 * (NT + nc + 1) <= kExpandSmemRows * 8) ? srows : grows;
+        if (slab_fit(m, S, n1, ip, u, nc, rows1, v, rec)) { done = true; break; }
       }
       if (!done && !failed && !(nS > n0)) failed = true;  // "all hope is lost"
     }
@@ -691,6 +695,231 @@ __global__ void __launch_bounds__(kBlock) k_quality(DevMesh m, const double* __r
   q[e] = res;
 }
 
+
+// ---------------------------------------------------------------------
+// FP64 guard band of the FP32 path: for each listed edge, recompute the
+// sizes of both end vertices in FP64 (patch fits of every vertex of their
+// elements, element errors and sizes, the vertex averages) and re-decide the
+// edge's split/collapse bits.  One 128-thread block per edge; every tet of
+// the patches involved has its FP64 gradient and integration point computed
+// once into shared memory.
+// ---------------------------------------------------------------------
+constexpr int kGuardThreads = 128;
+constexpr int kGuardMaxTets = 96;    // elements around one end vertex
+constexpr int kGuardMaxVerts = 96;   // distinct vertices of those elements
+constexpr int kGuardMaxPatch = 512;  // distinct elements of their patches
+constexpr int kGuardVHash = 256;
+constexpr int kGuardTHash = 1024;
+
+// FP64 gradient of the scalar field and integration point of tet t
+// (cofactor inverse; FP64 accuracy, not the reference's rounding)
+__device__ __forceinline__ void tet_grad_ip_f64(const DevMesh& m, int t, const double* __restrict__ u, double* g,
+                                                double* p) {
+  const int* ev = m.ev + (size_t)t * 4;
+  V3 x0 = load_xyz(m.xyz, ev[0]), x1 = load_xyz(m.xyz, ev[1]), x2 = load_xyz(m.xyz, ev[2]),
+     x3 = load_xyz(m.xyz, ev[3]);
+  double u0 = u[ev[0]];
+  V3 e1 = ref::sub(x1, x0), e2 = ref::sub(x2, x0), e3 = ref::sub(x3, x0);
+  double d1 = u[ev[1]] - u0, d2 = u[ev[2]] - u0, d3 = u[ev[3]] - u0;
+  V3 c1 = ref::cross(e2, e3), c2 = ref::cross(e3, e1), c3 = ref::cross(e1, e2);
+  double inv = 1.0 / ref::dot(e1, c1);
+  for (int k = 0; k < 3; ++k) {
+    g[k] = (c1.v[k] * d1 + c2.v[k] * d2 + c3.v[k] * d3) * inv;
+    p[k] = 0.25 * (((x0.v[k] + x1.v[k]) + x2.v[k]) + x3.v[k]);
+  }
+}
+
+__device__ __forceinline__ int hash_find_insert(int* keys, int cap, int key, int* count, int max, int* list) {
+  unsigned h = ((unsigned)key * 2654435761u) & (cap - 1);
+  for (int probe = 0; probe < cap; ++probe) {
+    int prev = atomicCAS(&keys[2 * h], -1, key);
+    if (prev == -1) {
+      int slot = atomicAdd(count, 1);
+      if (slot < max) list[slot] = key;
+      keys[2 * h + 1] = slot;
+      return slot;
+    }
+    if (prev == key) return -2;  // present; slot published by the inserter
+    h = (h + 1) & (cap - 1);
+  }
+  return -1;
+}
+
+__device__ __forceinline__ int hash_lookup(const int* keys, int cap, int key) {
+  unsigned h = ((unsigned)key * 2654435761u) & (cap - 1);
+  for (int probe = 0; probe < cap; ++probe) {
+    int k = keys[2 * h];
+    if (k == key) return keys[2 * h + 1];
+    if (k == -1) return -1;
+    h = (h + 1) & (cap - 1);
+  }
+  return -1;
+}
+
+__global__ void __launch_bounds__(kGuardThreads) k_guard(DevMesh m, const double* __restrict__ u,
+                                                         const double* __restrict__ out3,
+                                                         const int* __restrict__ items,
+                                                         const int* __restrict__ count, int cap,
+                                                         uint32_t* split, uint32_t* collapse, int* unresolved) {
+  __shared__ int ends[2][kGuardMaxTets];
+  __shared__ int nends[2];
+  __shared__ int verts[kGuardMaxVerts];
+  __shared__ int nverts;
+  __shared__ int vhash[2 * kGuardVHash];
+  __shared__ int tets[kGuardMaxPatch];
+  __shared__ int ntets;
+  __shared__ int thash[2 * kGuardTHash];
+  __shared__ double tg[kGuardMaxPatch][3];
+  __shared__ double tp[kGuardMaxPatch][3];
+  __shared__ double recv[kGuardMaxVerts][3];
+  __shared__ double esz[2][kGuardMaxTets];
+  __shared__ int bad;
+  const int n = min(*count, cap);
+  const double sf = out3[2];
+  const int lane = threadIdx.x & 31;
+  for (int it = blockIdx.x; it < n; it += gridDim.x) {
+    const int e = items[it];
+    const int ab[2] = {m.edv[2 * (size_t)e], m.edv[2 * (size_t)e + 1]};
+    if (threadIdx.x == 0) {
+      nverts = 0;
+      ntets = 0;
+      bad = 0;
+      for (int s = 0; s < 2; ++s) {
+        int c = m.a_off[ab[s] + 1] - m.a_off[ab[s]];
+        if (c > kGuardMaxTets) { bad = 1; c = 0; }
+        nends[s] = c;
+      }
+    }
+    for (int i = threadIdx.x; i < 2 * kGuardVHash; i += blockDim.x) vhash[i] = -1;
+    for (int i = threadIdx.x; i < 2 * kGuardTHash; i += blockDim.x) thash[i] = -1;
+    __syncthreads();
+    for (int s = 0; s < 2; ++s)
+      for (int i = threadIdx.x; i < nends[s]; i += blockDim.x) ends[s][i] = m.a_el[m.a_off[ab[s]] + i];
+    __syncthreads();
+    // distinct vertices W of the elements around a and b
+    for (int s = 0; s < 2; ++s)
+      for (int i = threadIdx.x; i < nends[s] * 4; i += blockDim.x)
+        if (hash_find_insert(vhash, kGuardVHash, m.ev[(size_t)ends[s][i >> 2] * 4 + (i & 3)], &nverts,
+                             kGuardMaxVerts, verts) == -1)
+          bad = 1;
+    __syncthreads();
+    const int nv = nverts;
+    if (nv > kGuardMaxVerts) bad = 1;
+    // distinct elements of the patches of W
+    for (int i = threadIdx.x; i < min(nv, kGuardMaxVerts); i += blockDim.x) {
+      int w = verts[i];
+      for (int k = m.p_off[w]; k < m.p_off[w + 1]; ++k)
+        if (hash_find_insert(thash, kGuardTHash, m.p_el[k], &ntets, kGuardMaxPatch, tets) == -1) bad = 1;
+    }
+    __syncthreads();
+    const int nt = ntets;
+    if (nt > kGuardMaxPatch) bad = 1;
+    __syncthreads();
+    if (!bad) {
+      for (int i = threadIdx.x; i < nt; i += blockDim.x) tet_grad_ip_f64(m, tets[i], u, tg[i], tp[i]);
+      __syncthreads();
+      // patch fits: one warp per vertex of W, lanes over its patch
+      for (int wi = threadIdx.x >> 5; wi < nv; wi += kGuardThreads / 32) {
+        int w = verts[wi];
+        int beg = m.p_off[w], cnt = m.p_off[w + 1] - beg;
+        V3 xw = load_xyz(m.xyz, w);
+        double a[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0}, r[4][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        int s0 = hash_lookup(thash, kGuardTHash, m.p_el[beg]);
+        double hs0 = 0;
+        {  // scale: distance to the first patch element's integration point
+          double dx = tp[s0][0] - xw.v[0], dy = tp[s0][1] - xw.v[1], dz = tp[s0][2] - xw.v[2];
+          hs0 = sqrt(dx * dx + dy * dy + dz * dz);
+        }
+        double inv_h = 1.0 / hs0;
+        for (int k = lane; k < cnt; k += 32) {
+          int sl = hash_lookup(thash, kGuardTHash, m.p_el[beg + k]);
+          double sx = (tp[sl][0] - xw.v[0]) * inv_h, sy = (tp[sl][1] - xw.v[1]) * inv_h,
+                 sz = (tp[sl][2] - xw.v[2]) * inv_h;
+          a[0] += 1; a[1] += sx; a[2] += sy; a[3] += sz;
+          a[4] += sx * sx; a[5] += sx * sy; a[6] += sx * sz; a[7] += sy * sy; a[8] += sy * sz; a[9] += sz * sz;
+          for (int c = 0; c < 3; ++c) {
+            double g = tg[sl][c];
+            r[0][c] += g; r[1][c] += sx * g; r[2][c] += sy * g; r[3][c] += sz * g;
+          }
+        }
+        for (int i = 0; i < 10; ++i) a[i] = warp_sum(a[i]);
+        for (int i = 0; i < 4; ++i)
+          for (int c = 0; c < 3; ++c) r[i][c] = warp_sum(r[i][c]);
+        if (lane == 0) {
+          double l00 = sqrt(a[0]);
+          double l10 = a[1] / l00, l20 = a[2] / l00, l30 = a[3] / l00;
+          double d1 = a[4] - l10 * l10;
+          double l11 = sqrt(fmax(d1, 0.0));
+          double l21 = (a[5] - l20 * l10) / l11, l31 = (a[6] - l30 * l10) / l11;
+          double d2 = a[7] - l20 * l20 - l21 * l21;
+          double l22 = sqrt(fmax(d2, 0.0));
+          double l32 = (a[8] - l30 * l20 - l31 * l21) / l22;
+          double d3 = a[9] - l30 * l30 - l31 * l31 - l32 * l32;
+          double l33 = sqrt(fmax(d3, 0.0));
+          double pmin = fmin(fmin(d1, d2), fmin(d3, a[0])), pmax = fmax(fmax(d1, d2), fmax(d3, a[0]));
+          if (cnt < 4 || !(pmin > 0) || !(pmax <= 1e10 * pmin)) {
+            bad = 1;
+          } else {
+            for (int c = 0; c < 3; ++c) {
+              double y0 = r[0][c] / l00;
+              double y1 = (r[1][c] - l10 * y0) / l11;
+              double y2 = (r[2][c] - l20 * y0 - l21 * y1) / l22;
+              double y3 = (r[3][c] - l30 * y0 - l31 * y1 - l32 * y2) / l33;
+              double z3 = y3 / l33;
+              double z2 = (y2 - l32 * z3) / l22;
+              double z1 = (y1 - l21 * z2 - l31 * z3) / l11;
+              recv[wi][c] = (y0 - l10 * z1 - l20 * z2 - l30 * z3) / l00;
+            }
+          }
+        }
+      }
+      __syncthreads();
+      // element sizes around a and b
+      for (int s = 0; s < 2; ++s)
+        for (int i = threadIdx.x; i < nends[s]; i += blockDim.x) {
+          int t = ends[s][i];
+          const int* ev = m.ev + (size_t)t * 4;
+          int sl = hash_lookup(thash, kGuardTHash, t);
+          V3 x[4];
+          double v2[3] = {0, 0, 0};
+          for (int k = 0; k < 4; ++k) {
+            x[k] = load_xyz(m.xyz, ev[k]);
+            int vi = hash_lookup(vhash, kGuardVHash, ev[k]);
+            for (int c = 0; c < 3; ++c) v2[c] += recv[vi][c] * 0.25;
+          }
+          double dV = ref::dot(ref::sub(x[1], x[0]), ref::cross(ref::sub(x[2], x[0]), ref::sub(x[3], x[0])));
+          double dd = 0;
+          for (int c = 0; c < 3; ++c) dd += (tg[sl][c] - v2[c]) * (tg[sl][c] - v2[c]);
+          double sum = dd * (1.0 / 6.0) * dV;
+          double h = 0;
+          for (int k = 0; k < 6; ++k) h = fmax(h, ref::len(ref::sub(x[c_tet_edges[k][1]], x[c_tet_edges[k][0]])));
+          esz[s][i] = h * pow(sum, -0.2) * sf;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      if (bad) {
+        atomicAdd(unresolved, 1);
+      } else {
+        double sz[2];
+        for (int s = 0; s < 2; ++s) {
+          double acc = 0;
+          for (int i = 0; i < nends[s]; ++i) acc += esz[s][i];
+          sz[s] = acc / (double)nends[s];
+        }
+        double hv[6] = {sz[0], sz[0], sz[0], sz[1], sz[1], sz[1]}, Rv[18];
+        identity9(Rv);
+        identity9(Rv + 9);
+        double L = metric_length(load_xyz(m.xyz, ab[0]), load_xyz(m.xyz, ab[1]), hv, Rv);
+        uint32_t bit = 1u << (e & 31);
+        if (L > 1.5) atomicOr(&split[e >> 5], bit); else atomicAnd(&split[e >> 5], ~bit);
+        if (L < .5) atomicOr(&collapse[e >> 5], bit); else atomicAnd(&collapse[e >> 5], ~bit);
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // ---------------------------------------------------------------------
 // adjacency construction
 // ---------------------------------------------------------------------
@@ -742,12 +971,14 @@ void launch_recover_f64(const DevMesh& m, const double* ip, int nc, double* rec,
                         cudaStream_t s) {
   (void)st;
   if (!m.V) return;
+  // one row per lane: patches of up to 32 elements (every interior patch of
+  // a structured tet or triangle mesh); larger ones take the slab path
   int grid = nblk((long)m.V * 32);
   if (m.dim == 3) {
-    if (nc == 3) k_recover<4, 3, 2><<<grid, kBlock, 0, s>>>(m, ip, rec, xl);
+    if (nc == 3) k_recover<4, 3, 1><<<grid, kBlock, 0, s>>>(m, ip, rec, xl);
     else k_recover<4, 9, 1><<<grid, kBlock, 0, s>>>(m, ip, rec, xl);
   } else {
-    if (nc == 3) k_recover<3, 3, 2><<<grid, kBlock, 0, s>>>(m, ip, rec, xl);
+    if (nc == 3) k_recover<3, 3, 1><<<grid, kBlock, 0, s>>>(m, ip, rec, xl);
     else k_recover<3, 9, 1><<<grid, kBlock, 0, s>>>(m, ip, rec, xl);
   }
 }
@@ -808,6 +1039,11 @@ void launch_apply_bits(int E, const uint32_t* bits, int which, int* flags, unsig
 void launch_quality_f64(const DevMesh& m, const double* size, const double* sizes, const double* frames, double* q,
                         cudaStream_t s) {
   if (m.T) k_quality<<<nblk(m.T), kBlock, 0, s>>>(m, size, sizes, frames, q);
+}
+
+void launch_guard_f64(const DevMesh& m, const double* u, const double* out3, const int* items, const int* count,
+                      int cap, uint32_t* split, uint32_t* collapse, int* unresolved, cudaStream_t s) {
+  k_guard<<<1216, kGuardThreads, 0, s>>>(m, u, out3, items, count, cap, split, collapse, unresolved);
 }
 
 void launch_build_v2e(const DevMesh& m, int* off, int* el, int* tmp, cudaStream_t s) {

@@ -41,7 +41,7 @@ extern "C" {
 
 /* precision modes */
 #define SPRG_FP64 0  /* FP64 throughout, the reference's arithmetic */
-#define SPRG_FP32 1  /* FP32 patch fits and sweeps, FP64 guard (see sprg_guard_info) */
+#define SPRG_FP32 1  /* FP32 fits and sweeps with compensated residuals, FP64 guard band (tets) */
 
 /* markEntities flag bits (ma/maAdapt.h:17-37) */
 #define SPRG_SPLIT (1 << 0)
@@ -83,7 +83,8 @@ typedef struct sprg_size_info {
   double size_factor;      /* spr/sprEstimateError.cc:205-217 */
   int64_t n_expanded;      /* patches that needed growth (spr/sprRecoverField.cc:365) */
   int64_t n_fp64_refits;   /* FP32 mode: patches refit in FP64 (condition estimate > 1e6) */
-  int64_t n_guard_edges;   /* FP32 mode: edges re-measured in FP64 near 0.5 / 1.5 */
+  int64_t n_guard_edges;   /* FP32 mode: edges within 2e-6 of 0.5 / 1.5, re-decided in FP64 */
+  int64_t n_guard_unresolved; /* FP32 mode: guard edges left to the FP32 decision (patch growth needed) */
 } sprg_size_info;
 
 /* ---- context: flatten + upload (the MDS-to-device flattener) ---------- */
@@ -181,6 +182,11 @@ int sprg_apply_marks(int64_t n_edges, const uint32_t* split_bits, const uint32_t
 int sprg_profile_enable(sprg_ctx* ctx, int on);
 int sprg_profile_flush(sprg_ctx* ctx);
 const char* sprg_profile_report(sprg_ctx* ctx, int reset);
+
+/* Copies up to `bytes` of a named internal device buffer to the host
+   (instrumentation for accuracy studies; e.g. "size", "err", "q32",
+   "size32", "rec32", "tetd", "out3"). */
+int sprg_debug_read(sprg_ctx* ctx, const char* name, void* host, size_t bytes);
 
 /* Number of kernel launches issued by the last call (instrumentation). */
 int64_t sprg_last_launch_count(const sprg_ctx* ctx);
