@@ -75,12 +75,12 @@ def algorithmic_bytes(kernel, V, T, E, vb=8):
         "measure_f64": 2 * ib * E + 3 * vb * V + vb * V + vb * E,
         "mark_bits": vb * E + E // 4,
         # FP32 path: 32-byte vertex records, 32-byte recovered (g_ref, deviation) pairs
-        "prep_f32": 24 * V + 8 * V + 32 * V,
-        "tet_f32": 4 * ib * T + 32 * V + 64 * T,
-        "recover_f32": ib * (V + 1) + 4 * ib * T + 64 * T + 32 * V + 32 * V,
-        "error_f32": 4 * ib * T + 32 * T + 32 * V + 4 * T,
-        "average_f32": ib * (V + 1) + 4 * ib * T + 4 * T + 4 * V,
-        "measure_f32": 2 * ib * E + 32 * V + 4 * V + E // 4,
+        "prep_f32": 8 * V + 8 * V,
+        "tet_f32": 4 * ib * T + 32 * V + 8 * V + 32 * T,
+        "recover_f32": ib * (V + 1) + 4 * ib * T + 4 * 4 * T + 32 * T + 32 * V,
+        "error_f32": 4 * ib * T + 32 * T + 32 * V + 8 * T,  # q and its bound packed (8 B)
+        "average_f32": ib * (V + 1) + 4 * ib * T + 8 * T + 8 * V,
+        "measure_f32": 2 * ib * E + 32 * V + 8 * V + E // 4,
     }
     return table.get(kernel)
 

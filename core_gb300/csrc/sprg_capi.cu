@@ -20,6 +20,14 @@ struct DevBuf {
   size_t bytes = 0;
 };
 
+// Final element sets of the listed (grown or refit) patches; they depend
+// on the mesh geometry only, so they are built on the first pass and reused.
+struct PatchCache {
+  bool valid = false;
+  int count = 0;
+  DevBuf v, n, el;
+};
+
 struct sprg_ctx {
   int device = 0;
   cudaStream_t own = nullptr;
@@ -35,7 +43,12 @@ struct sprg_ctx {
   // scratch
   DevBuf partials, out3, status, count, xitems, xcount, slab, bits;
   // FP32 path buffers
-  DevBuf vrec, rec32, q32, size32, fcnt, guard, tetd;
+  DevBuf vrec, rec32, q32, size32, fcnt, guard, tetd, u2, wts, listed, qb, sizeb, fitems;
+  DevBuf gstamp, gfit, grec;  // guard pipeline scratch
+  int pass_id = 0;
+  bool vrec_ready = false;  // coordinate records and SPR weights (per mesh)
+  int n_listed = 0, n_refit = 0;
+  PatchCache cache64, cache32;
   static constexpr int kGuardCap = 1 << 20;
   static constexpr float kGuardRel = 2e-6f;
   std::string err_msg;
@@ -149,6 +162,38 @@ void prof_end(sprg_ctx* c) {
 
 // ---- pipeline steps on resident buffers -------------------------------
 
+// Listed patches: grow them on the first pass (recording the final element
+// sets), afterwards one QR fit per cached set.
+int listed_fits(sprg_ctx* c, PatchCache& pc, const double* ip, const double* u, int nc, double* rec64, ExpandList xl) {
+  DevMesh& m = c->m;
+  if (pc.valid) {
+    PB("cached_fit_f64");
+    launch_cached_fit_f64(m, ip, u, nc, rec64, pc.count, P<int>(pc.v), P<int>(pc.n), P<int>(pc.el), P<double>(c->slab),
+                          P<DevStatus>(c->status), c->stream);
+    PE();
+    c->launches += 1;
+    return check_launch(c, "cached fit");
+  }
+  int xc = 0;
+  CK(cudaMemcpyAsync(&xc, xl.count, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  if (xc > xl.cap) xc = xl.cap;
+  size_t slots = (size_t)(xc > 0 ? xc : 1);
+  ENSURE(pc.v, sizeof(int) * slots);
+  ENSURE(pc.n, sizeof(int) * slots);
+  ENSURE(pc.el, sizeof(int) * slots * expand_max_elems());
+  PB("expand_f64");
+  launch_expand_f64(m, ip, u, nc, rec64, xl, P<double>(c->slab), P<DevStatus>(c->status), c->stream, P<int>(pc.v),
+                    P<int>(pc.n), P<int>(pc.el));
+  PE();
+  c->launches += 1;
+  int rc = check_launch(c, "expand");
+  if (rc) return rc;
+  pc.count = xc;
+  pc.valid = true;
+  return SPRG_OK;
+}
+
 int step_grad(sprg_ctx* c, int ncin) {
   DevMesh& m = c->m;
   ENSURE(c->ip, sizeof(double) * (size_t)m.T * 3 * ncin);
@@ -177,12 +222,7 @@ int step_recover(sprg_ctx* c) {
   int rc = check_launch(c, "recover");
   if (rc) return rc;
   // patches that need growth: the reference growth order, on the device
-  PB("expand_f64");
-  launch_expand_f64(m, P<double>(c->ip), nullptr, nc, P<double>(c->rec), xl, P<double>(c->slab),
-                    P<DevStatus>(c->status), c->stream);
-  PE();
-  c->launches += 1;
-  return check_launch(c, "expand");
+  return listed_fits(c, c->cache64, P<double>(c->ip), nullptr, nc, P<double>(c->rec), xl);
 }
 
 int step_size(sprg_ctx* c, int mode, double adapt_ratio, double target, double alpha, double beta) {
@@ -238,12 +278,12 @@ int fill_info(sprg_ctx* c, sprg_size_info* info) {
   c->last_info.n_guard_edges = 0;
   c->last_info.n_guard_unresolved = 0;
   if (c->precision == SPRG_FP32 && c->fcnt.p) {
-    int fc[3] = {0, 0, 0};
+    int fc[6] = {0, 0, 0, 0, 0, 0};
     CK(cudaMemcpy(fc, c->fcnt.p, sizeof fc, cudaMemcpyDeviceToHost));
-    c->last_info.n_fp64_refits = fc[0];
+    c->last_info.n_fp64_refits = c->n_refit;
     c->last_info.n_guard_edges = fc[1];
-    c->last_info.n_guard_unresolved = fc[2];
-    c->last_info.n_expanded = xc - fc[0];
+    c->last_info.n_guard_unresolved = fc[4];
+    c->last_info.n_expanded = c->n_listed - c->n_refit;
   }
   if (info) *info = c->last_info;
   return SPRG_OK;
@@ -365,7 +405,9 @@ int sprg_destroy(sprg_ctx* c) {
                     &c->ael,   &c->tmp,     &c->f,    &c->ip,    &c->rec,     &c->err,    &c->esize,
                     &c->size,  &c->L,       &c->flags, &c->q,    &c->sizes3,  &c->frames9, &c->partials,
                     &c->out3,  &c->status,  &c->count, &c->xitems, &c->xcount, &c->slab, &c->bits,
-                    &c->vrec,  &c->rec32,   &c->q32,  &c->size32, &c->fcnt,   &c->guard, &c->tetd};
+                    &c->vrec,  &c->rec32,   &c->q32,  &c->size32, &c->fcnt,   &c->guard, &c->tetd, &c->u2,
+                    &c->wts,   &c->listed,  &c->qb,   &c->sizeb,  &c->fitems, &c->gstamp, &c->gfit, &c->grec,
+                    &c->cache64.v, &c->cache64.n, &c->cache64.el, &c->cache32.v, &c->cache32.n, &c->cache32.el};
   for (DevBuf* b : bufs) release(*b);
   for (auto& e : c->ev_pool) cudaEventDestroy(e);
   if (c->own) cudaStreamDestroy(c->own);
@@ -585,59 +627,84 @@ static int pass_fast(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_
   DevMesh& m = c->m;
   int rc;
   int nb = fast_error_blocks(m.T);
+  const size_t nel = (size_t)m.T * m.nn;
   ENSURE(c->vrec, 32 * (size_t)m.V);
+  ENSURE(c->u2, 8 * (size_t)m.V);
   ENSURE(c->rec32, 32 * (size_t)m.V);
-  ENSURE(c->tetd, 64 * (size_t)m.T);
-  ENSURE(c->q32, 4 * (size_t)m.T);
+  ENSURE(c->tetd, 32 * (size_t)m.T);
+  ENSURE(c->q32, 8 * (size_t)m.T);
   ENSURE(c->size32, 4 * (size_t)m.V);
+  ENSURE(c->sizeb, 4 * (size_t)m.V);
   ENSURE(c->rec, 24 * (size_t)m.V);
-  ENSURE(c->xitems, sizeof(int) * (size_t)m.V);
+  ENSURE(c->fitems, sizeof(int) * (size_t)m.V);
   ENSURE(c->xcount, sizeof(int));
   ENSURE(c->slab, sizeof(double) * (size_t)expand_grid() * expand_max_elems() * (4 + 3 + 1));
-  ENSURE(c->fcnt, 4 * sizeof(int));
+  ENSURE(c->fcnt, 8 * sizeof(int));
   ENSURE(c->guard, sizeof(int) * (size_t)sprg_ctx::kGuardCap);
   ENSURE(c->partials, sizeof(double) * 2 * (size_t)(nb > 0 ? nb : 1));
   ENSURE(c->out3, sizeof(double) * 4);
   if ((rc = reset_status(c))) return rc;
-  CK(cudaMemsetAsync(c->xcount.p, 0, sizeof(int), c->stream));
-  CK(cudaMemsetAsync(c->fcnt.p, 0, 4 * sizeof(int), c->stream));
-  ExpandList xl{P<int>(c->xitems), P<int>(c->xcount), m.V};
+  // fcnt: [0] refit patches, [1] guard edges, [3] listed patches,
+  // [4] unresolved guard edges, [5] failed guard fits (0, 3 per mesh; 1, 4, 5 per pass)
+  ExpandList xl{P<int>(c->fitems), P<int>(c->fcnt) + 3, m.V};
   float4* vrec = P<float4>(c->vrec);
   float4* rec32 = P<float4>(c->rec32);
+  if (!c->vrec_ready) {
+    // per mesh: coordinate records, SPR weights and the listed patches
+    ENSURE(c->wts, sizeof(float) * nel);
+    ENSURE(c->listed, (size_t)m.V);
+    CK(cudaMemsetAsync(c->fcnt.p, 0, 8 * sizeof(int), c->stream));
+    fast_prep_coords(m, vrec, c->stream);
+    fast_weights(m, P<float>(c->wts), xl, P<int>(c->fcnt), P<unsigned char>(c->listed), c->stream);
+    int h[2] = {0, 0};
+    CK(cudaMemcpyAsync(&h[0], P<int>(c->fcnt) + 3, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(&h[1], c->fcnt.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if ((rc = check_launch(c, "fast setup"))) return rc;
+    c->n_listed = h[0] < m.V ? h[0] : m.V;
+    c->n_refit = h[1];
+    c->vrec_ready = true;
+  }
+  CK(cudaMemsetAsync(P<int>(c->fcnt) + 1, 0, sizeof(int), c->stream));
+  CK(cudaMemsetAsync(P<int>(c->fcnt) + 4, 0, 2 * sizeof(int), c->stream));
   PB("prep_f32");
-  fast_prep(m, P<double>(c->f), vrec, c->stream);
+  fast_prep(m, P<double>(c->f), P<float2>(c->u2), c->stream);
   PE();
   PB("tet_f32");
-  fast_tet(m, vrec, P<float4>(c->tetd), c->stream);
+  fast_tet(m, vrec, P<float2>(c->u2), P<float4>(c->tetd), c->stream);
   PE();
   PB("recover_f32");
-  fast_recover(m, vrec, P<float4>(c->tetd), rec32, xl, P<int>(c->fcnt), c->stream);
+  fast_recover(m, P<float>(c->wts), P<unsigned char>(c->listed), P<float4>(c->tetd), rec32, c->stream);
   PE();
-  PB("expand_f64");
-  launch_expand_f64(m, nullptr, P<double>(c->f), 3, P<double>(c->rec), xl, P<double>(c->slab),
-                    P<DevStatus>(c->status), c->stream);
-  PE();
+  if ((rc = listed_fits(c, c->cache32, nullptr, P<double>(c->f), 3, P<double>(c->rec), xl))) return rc;
   PB("merge_f64");
   fast_merge_ref(xl, P<double>(c->rec), rec32, c->stream);
   PE();
   PB("error_f32");
-  fast_error(m, P<float4>(c->tetd), rec32, P<float>(c->q32), P<double>(c->partials), nb, c->stream);
+  fast_error(m, P<float4>(c->tetd), rec32, P<float2>(c->q32), P<double>(c->partials), nb, c->stream);
   PE();
   PB("size_factor");
   launch_size_factor(P<double>(c->partials), nb, 0, adapt_ratio, 0, m.dim, P<double>(c->out3), c->stream);
   PE();
   PB("average_f32");
-  fast_average(m, P<float>(c->q32), P<double>(c->out3), P<float>(c->size32), c->stream);
+  fast_average(m, P<float2>(c->q32), P<double>(c->out3), P<float>(c->size32), P<float>(c->sizeb), c->stream);
   PE();
   PB("measure_f32");
-  fast_measure(m, vrec, P<float>(c->size32), d_split, d_collapse, nullptr, P<int>(c->guard), P<int>(c->fcnt) + 1,
-               sprg_ctx::kGuardCap, sprg_ctx::kGuardRel, c->stream);
+  fast_measure(m, vrec, P<float>(c->size32), P<float>(c->sizeb), d_split, d_collapse, P<int>(c->guard),
+               P<int>(c->fcnt) + 1, sprg_ctx::kGuardCap, sprg_ctx::kGuardRel, c->stream);
   PE();
+  if (!c->gstamp.p) {
+    ENSURE(c->gstamp, sizeof(int) * (size_t)m.V);
+    CK(cudaMemsetAsync(c->gstamp.p, 0, sizeof(int) * (size_t)m.V, c->stream));
+  }
+  ENSURE(c->gfit, sizeof(int) * ((size_t)m.V + 1));
+  ENSURE(c->grec, 3 * sizeof(double) * (size_t)m.V);
+  GuardScratch gs{P<int>(c->gstamp), ++c->pass_id, P<int>(c->gfit) + 1, P<int>(c->gfit), m.V, P<double>(c->grec)};
   PB("guard_f64");
   launch_guard_f64(m, P<double>(c->f), P<double>(c->out3), P<int>(c->guard), P<int>(c->fcnt) + 1,
-                   sprg_ctx::kGuardCap, d_split, d_collapse, P<int>(c->fcnt) + 2, c->stream);
+                   sprg_ctx::kGuardCap, d_split, d_collapse, P<int>(c->fcnt) + 4, gs, c->stream);
   PE();
-  c->launches += 10;
+  c->launches += 13;
   c->size_valid = false;  // the FP64 size buffer is filled on demand
   c->L_valid = false;
   return check_launch(c, "fast pass");
@@ -716,7 +783,8 @@ int sprg_debug_read(sprg_ctx* c, const char* name, void* host, size_t bytes) {
       {"ip", &c->ip},       {"rec", &c->rec},     {"err", &c->err},       {"esize", &c->esize},
       {"size", &c->size},   {"L", &c->L},         {"vrec", &c->vrec},     {"rec32", &c->rec32},
       {"q32", &c->q32},     {"size32", &c->size32}, {"tetd", &c->tetd},   {"out3", &c->out3},
-      {"fcnt", &c->fcnt},   {"guard", &c->guard}, {"xitems", &c->xitems}, {"xcount", &c->xcount}};
+      {"fcnt", &c->fcnt},   {"guard", &c->guard}, {"xitems", &c->xitems}, {"xcount", &c->xcount},
+      {"wts", &c->wts},     {"sizeb", &c->sizeb}, {"qb", &c->qb}};
   for (auto& e : table) {
     if (strcmp(e.n, name) != 0) continue;
     if (!e.b->p) return fail(c, SPRG_ESTATE, std::string("buffer not allocated: ") + name);

@@ -48,8 +48,15 @@ void launch_recover_f64(const DevMesh& m, const double* ip, int nc, double* rec,
 // slab: expand_grid() * expand_max_elems() * (4 + nc + 1) doubles.
 // ip may be NULL: the scalar field u's element gradients are computed in
 // place (FP32 path, which keeps no ip field).
+// cache_* (optional): record each listed vertex's final element set
+// (expand_max_elems() ints per list slot) for launch_cached_fit_f64.
 void launch_expand_f64(const DevMesh& m, const double* ip, const double* u, int nc, double* rec, ExpandList xl,
-                       double* slab, DevStatus* st, cudaStream_t s);
+                       double* slab, DevStatus* st, cudaStream_t s, int* cache_v = nullptr, int* cache_n = nullptr,
+                       int* cache_el = nullptr);
+// One QR fit per cached listed vertex (patch growth depends on geometry only).
+void launch_cached_fit_f64(const DevMesh& m, const double* ip, const double* u, int nc, double* rec, int n_cached,
+                           const int* cache_v, const int* cache_n, const int* cache_el, double* slab, DevStatus* st,
+                           cudaStream_t s);
 int expand_max_elems();
 int expand_grid();
 // Per-element error terms + deterministic block partials (2 per block).
@@ -72,9 +79,18 @@ void launch_mark_bits(int E, const double* L, uint32_t* split, uint32_t* collaps
 // markEntities semantics from a predicate bitmap
 void launch_apply_bits(int E, const uint32_t* bits, int which, int* flags, unsigned long long* count,
                        DevStatus* st, cudaStream_t s);
-// FP64 guard band of the FP32 path: re-decide the listed edges' bits
+// FP64 guard band of the FP32 path: re-decide the listed edges' bits.
+struct GuardScratch {
+  int* stamp;      // V ints, persistent (de-duplication stamps)
+  int stamp_id;    // distinct per pass
+  int* fit_items;  // fit_cap ints
+  int* fit_count;
+  int fit_cap;
+  double* rec64;   // V x 3 doubles (FP64 recovered values of collected vertices)
+};
+// unresolved[0]: edges left to the FP32 decision, unresolved[1]: failed fits
 void launch_guard_f64(const DevMesh& m, const double* u, const double* out3, const int* items, const int* count,
-                      int cap, uint32_t* split, uint32_t* collapse, int* unresolved, cudaStream_t s);
+                      int cap, uint32_t* split, uint32_t* collapse, int* unresolved, GuardScratch g, cudaStream_t s);
 void launch_quality_f64(const DevMesh& m, const double* size, const double* sizes, const double* frames,
                         double* q, cudaStream_t s);
 

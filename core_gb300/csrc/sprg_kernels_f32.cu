@@ -1,8 +1,9 @@
 // FP32 fast path of the estimate-and-mark pass (3D tets, scalar field).
 //
 // Every FP64 input value is carried as an unevaluated float pair (hi, lo):
-// one 32-byte record per vertex {x,y,z,u}_hi, {x,y,z,u}_lo, so a vertex gather
-// is one DRAM sector.  All arithmetic is FP32; the places where the SPR
+// one 32-byte coordinate record per vertex {x,y,z,-}_hi, {x,y,z,-}_lo (built
+// once per mesh, a vertex gather is one DRAM sector) and one 8-byte field
+// pair per vertex (rebuilt each pass).  All arithmetic is FP32; the places where the SPR
 // estimator cancels are done with error-free transformations (TwoSum,
 // TwoProd via fmaf) instead of wider types:
 //
@@ -20,22 +21,24 @@
 // for listed patches.
 //
 // Phases:
-//   prep      thread per vertex: pack the records
+//   prep      thread per vertex: the field pair (the coordinate records are
+//             packed once per mesh)
+//   weights   (once per mesh, FP64) the SPR weights w_vt of every patch; the
+//             patches with fewer than 4 elements or a condition estimate
+//             above 1e6 are listed for the FP64 reference path instead
 //   tet       thread per tet: its gradient as (g_t, d_t) with g_t the plain
 //             FP32 value and d_t = J^{-1}(du - J g_t) the compensated
-//             correction, its volume weight, h_max and its integration point
-//             as a pair (64 bytes per tet), so the gradient is evaluated once
-//             instead of once per use and the recover kernel gathers no
-//             vertex records
-//   recover   4 lanes per vertex: patch tets split over the lanes, FP32 normal
-//             equations on centred, scaled coordinates; condition estimate
-//             > 1e6, fewer than 4 points or a non-positive pivot send the
-//             vertex to the FP64 reference path (growth + Householder QR)
+//             correction, its volume weight and h_max (32 bytes per tet), so
+//             the gradient is evaluated once instead of once per use
+//   recover   4 lanes per vertex: eps*(v) = g_ref + sum w_vt (eps_t - g_ref)
 //   error     thread per tet: element error, SelfProduct and Error terms
-//             (compensated), q_t = h_max * err^(-1/5)
+//             (compensated), q_t = h_max * err^(-1/5) and a relative error
+//             bound of q_t
 //   average   thread per vertex: size = size_factor * mean(q_t) (compensated)
+//             and the size's error bound
 //   measure   thread per edge: metric length, split/collapse bitmaps, and the
-//             list of edges within the guard band of 0.5 / 1.5
+//             list of edges whose distance to 0.5 / 1.5 is within the error
+//             bound (re-decided in FP64 by the guard kernel)
 #include "sprg_fast.h"
 
 namespace sprg {
@@ -43,6 +46,10 @@ namespace {
 
 constexpr int kBlock = 256;
 constexpr int kGroup = 4;  // lanes per vertex in the recover kernel
+// relative accuracy assumed for each quantity entering an element-error
+// deviation (about 4 FP32 ulps), scaled into the error bound of q_t; on the
+// 160^3 workload the largest observed error is 0.43 of the resulting bound
+constexpr float kBoundUlps = 2.5e-7f;
 
 __device__ __forceinline__ float4 ld4(const float4* p) { return __ldg(p); }
 
@@ -115,14 +122,23 @@ __device__ __forceinline__ float inv_fifth_root(float x) {
 }
 
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kBlock) k_prep(int V, const double* __restrict__ xyz, const double* __restrict__ u,
-                                                 float4* __restrict__ rec) {
+// coordinate records (once per mesh) and the field pair (once per pass)
+__global__ void __launch_bounds__(kBlock) k_prep_coords(int V, const double* __restrict__ xyz,
+                                                        float4* __restrict__ rec) {
   int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= V) return;
-  double x = xyz[3 * (size_t)v], y = xyz[3 * (size_t)v + 1], z = xyz[3 * (size_t)v + 2], w = u[v];
-  float xh = (float)x, yh = (float)y, zh = (float)z, wh = (float)w;
-  rec[2 * (size_t)v] = make_float4(xh, yh, zh, wh);
-  rec[2 * (size_t)v + 1] = make_float4((float)(x - xh), (float)(y - yh), (float)(z - zh), (float)(w - wh));
+  double x = xyz[3 * (size_t)v], y = xyz[3 * (size_t)v + 1], z = xyz[3 * (size_t)v + 2];
+  float xh = (float)x, yh = (float)y, zh = (float)z;
+  rec[2 * (size_t)v] = make_float4(xh, yh, zh, 0.f);
+  rec[2 * (size_t)v + 1] = make_float4((float)(x - xh), (float)(y - yh), (float)(z - zh), 0.f);
+}
+
+__global__ void __launch_bounds__(kBlock) k_prep(int V, const double* __restrict__ u, float2* __restrict__ u2) {
+  int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= V) return;
+  double w = u[v];
+  float wh = (float)w;
+  u2[v] = make_float2(wh, (float)(w - wh));
 }
 
 // tet t's edge pairs (x_i - x_0, u_i - u_0), i = 1..3, their rounded sums
@@ -133,13 +149,17 @@ struct TetData {
   float4 h0, l0;
 };
 
-__device__ __forceinline__ TetData load_tet(const float4* __restrict__ vr, int4 tv) {
+__device__ __forceinline__ float4 with_u(float4 r, float2 u) { return make_float4(r.x, r.y, r.z, u.x); }
+__device__ __forceinline__ float4 with_ul(float4 r, float2 u) { return make_float4(r.x, r.y, r.z, u.y); }
+
+__device__ __forceinline__ TetData load_tet(const float4* __restrict__ vr, const float2* __restrict__ u2, int4 tv) {
   TetData d;
-  d.h0 = ld4(vr + 2 * (size_t)tv.x);
-  d.l0 = ld4(vr + 2 * (size_t)tv.x + 1);
-  float4 h1 = ld4(vr + 2 * (size_t)tv.y), l1 = ld4(vr + 2 * (size_t)tv.y + 1);
-  float4 h2 = ld4(vr + 2 * (size_t)tv.z), l2 = ld4(vr + 2 * (size_t)tv.z + 1);
-  float4 h3 = ld4(vr + 2 * (size_t)tv.w), l3 = ld4(vr + 2 * (size_t)tv.w + 1);
+  float2 u0 = __ldg(u2 + tv.x), u1 = __ldg(u2 + tv.y), uu2 = __ldg(u2 + tv.z), u3 = __ldg(u2 + tv.w);
+  d.h0 = with_u(ld4(vr + 2 * (size_t)tv.x), u0);
+  d.l0 = with_ul(ld4(vr + 2 * (size_t)tv.x + 1), u0);
+  float4 h1 = with_u(ld4(vr + 2 * (size_t)tv.y), u1), l1 = with_ul(ld4(vr + 2 * (size_t)tv.y + 1), u1);
+  float4 h2 = with_u(ld4(vr + 2 * (size_t)tv.z), uu2), l2 = with_ul(ld4(vr + 2 * (size_t)tv.z + 1), uu2);
+  float4 h3 = with_u(ld4(vr + 2 * (size_t)tv.w), u3), l3 = with_ul(ld4(vr + 2 * (size_t)tv.w + 1), u3);
   pdiff(h1, l1, d.h0, d.l0, d.eh[0], d.el[0]);
   pdiff(h2, l2, d.h0, d.l0, d.eh[1], d.el[1]);
   pdiff(h3, l3, d.h0, d.l0, d.eh[2], d.el[2]);
@@ -154,11 +174,11 @@ __device__ __forceinline__ TetData load_tet(const float4* __restrict__ vr, int4 
 // tet: gradient pair, volume weight, h_max
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kBlock) k_fast_tet(DevMesh m, const float4* __restrict__ vr,
-                                                     float4* __restrict__ td) {
+                                                     const float2* __restrict__ u2, float4* __restrict__ td) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= m.T) return;
   int4 tv = __ldg(reinterpret_cast<const int4*>(m.ev) + t);
-  TetData d = load_tet(vr, tv);
+  TetData d = load_tet(vr, u2, tv);
   Cof cf = cofactors(d.e[0], d.e[1], d.e[2]);
   float g[3], c[3];
   apply_inv(cf, d.e[0].w, d.e[1].w, d.e[2].w, g);
@@ -169,129 +189,135 @@ __global__ void __launch_bounds__(kBlock) k_fast_tet(DevMesh m, const float4* __
   hm = fmaxf(hm, len3(a2.x - a1.x, a2.y - a1.y, a2.z - a1.z));
   hm = fmaxf(hm, len3(a3.x - a1.x, a3.y - a1.y, a3.z - a1.z));
   hm = fmaxf(hm, len3(a3.x - a2.x, a3.y - a2.y, a3.z - a2.z));
-  // integration point (centroid) as a pair: x_0 + (e1 + e2 + e3) / 4
-  float px = 0.25f * ((d.eh[0].x + d.eh[1].x) + d.eh[2].x), pxl = 0.25f * ((d.el[0].x + d.el[1].x) + d.el[2].x);
-  float py = 0.25f * ((d.eh[0].y + d.eh[1].y) + d.eh[2].y), pyl = 0.25f * ((d.el[0].y + d.el[1].y) + d.el[2].y);
-  float pz = 0.25f * ((d.eh[0].z + d.eh[1].z) + d.eh[2].z), pzl = 0.25f * ((d.el[0].z + d.el[1].z) + d.el[2].z);
-  float cxh, cxl, cyh, cyl, czh, czl;
-  two_sum(d.h0.x, px, cxh, cxl);
-  two_sum(d.h0.y, py, cyh, cyl);
-  two_sum(d.h0.z, pz, czh, czl);
-  cxl += d.l0.x + pxl;
-  cyl += d.l0.y + pyl;
-  czl += d.l0.z + pzl;
-  float4* o = td + 4 * (size_t)t;
+  float4* o = td + 2 * (size_t)t;
   o[0] = make_float4(g[0], g[1], g[2], cf.det * (1.0f / 6.0f));
   o[1] = make_float4(c[0], c[1], c[2], hm);
-  o[2] = make_float4(cxh, cyh, czh, 0.f);
-  o[3] = make_float4(cxl, cyl, czl, 0.f);
 }
 
 // ---------------------------------------------------------------------------
-// recover: kGroup lanes per vertex
+// SPR weights (once per mesh).  The constant term of the patch fit, which is
+// the recovered value at the patch vertex when the fit is centred there, is
+// a fixed linear combination of the patch samples:
+//     eps*(v) = sum_t w_vt eps_t,   w_vt = e_0^T (A^T A)^{-1} [1, s_t],
+// with s_t the integration point of t relative to v, scaled.  The weights
+// depend on the geometry only, so they are computed once per mesh in FP64
+// (normal equations, Cholesky) and stored in patch-CSR order.  Patches with
+// fewer than four elements or a condition estimate above 1e6 are listed for
+// the FP64 reference path (growth + Householder QR) instead.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kBlock) k_fast_recover(DevMesh m, const float4* __restrict__ vr,
-                                                         const float4* __restrict__ td, float4* __restrict__ rec,
-                                                         ExpandList xl, int* __restrict__ n_refit) {
+__global__ void __launch_bounds__(kBlock) k_fast_weights(DevMesh m, float* __restrict__ w, ExpandList xl,
+                                                         int* __restrict__ n_refit, unsigned char* __restrict__ listed) {
+  int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= m.V) return;
+  const int beg = m.p_off[v], cnt = m.p_off[v + 1] - beg;
+  const double xv = m.xyz[3 * (size_t)v], yv = m.xyz[3 * (size_t)v + 1], zv = m.xyz[3 * (size_t)v + 2];
+  double a[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  double inv_h = 0;
+  bool ok = cnt >= 4;
+  for (int k = 0; ok && k < cnt; ++k) {
+    const int* ev = m.ev + 4 * (size_t)m.p_el[beg + k];
+    double px = 0, py = 0, pz = 0;
+    for (int i = 0; i < 4; ++i) {
+      px += m.xyz[3 * (size_t)ev[i]];
+      py += m.xyz[3 * (size_t)ev[i] + 1];
+      pz += m.xyz[3 * (size_t)ev[i] + 2];
+    }
+    double sx = 0.25 * px - xv, sy = 0.25 * py - yv, sz = 0.25 * pz - zv;
+    if (k == 0) inv_h = 1.0 / sqrt(sx * sx + sy * sy + sz * sz);
+    sx *= inv_h; sy *= inv_h; sz *= inv_h;
+    a[0] += 1; a[1] += sx; a[2] += sy; a[3] += sz;
+    a[4] += sx * sx; a[5] += sx * sy; a[6] += sx * sz; a[7] += sy * sy; a[8] += sy * sz; a[9] += sz * sz;
+  }
+  double l00 = 0, l10 = 0, l20 = 0, l30 = 0, l11 = 0, l21 = 0, l31 = 0, l22 = 0, l32 = 0, l33 = 0;
+  if (ok) {
+    l00 = sqrt(a[0]);
+    l10 = a[1] / l00; l20 = a[2] / l00; l30 = a[3] / l00;
+    double d1 = a[4] - l10 * l10;
+    l11 = sqrt(fmax(d1, 0.0));
+    l21 = (a[5] - l20 * l10) / l11; l31 = (a[6] - l30 * l10) / l11;
+    double d2 = a[7] - l20 * l20 - l21 * l21;
+    l22 = sqrt(fmax(d2, 0.0));
+    l32 = (a[8] - l30 * l20 - l31 * l21) / l22;
+    double d3 = a[9] - l30 * l30 - l31 * l31 - l32 * l32;
+    l33 = sqrt(fmax(d3, 0.0));
+    double pmin = fmin(fmin(d1, d2), fmin(d3, a[0])), pmax = fmax(fmax(d1, d2), fmax(d3, a[0]));
+    ok = (pmin > 0) && (pmax <= 1e6 * pmin);
+  }
+  listed[v] = ok ? 0 : 1;
+  if (!ok) {
+    int slot = atomicAdd(xl.count, 1);
+    if (slot < xl.cap) xl.items[slot] = v;
+    if (cnt >= 4) atomicAdd(n_refit, 1);
+    return;
+  }
+  // row q = e_0^T (L L^T)^{-1}: solve L y = e_0, then L^T q = y
+  double y0 = 1.0 / l00;
+  double y1 = (-l10 * y0) / l11;
+  double y2 = (-l20 * y0 - l21 * y1) / l22;
+  double y3 = (-l30 * y0 - l31 * y1 - l32 * y2) / l33;
+  double q3 = y3 / l33;
+  double q2 = (y2 - l32 * q3) / l22;
+  double q1 = (y1 - l21 * q2 - l31 * q3) / l11;
+  double q0 = (y0 - l10 * q1 - l20 * q2 - l30 * q3) / l00;
+  for (int k = 0; k < cnt; ++k) {
+    const int* ev = m.ev + 4 * (size_t)m.p_el[beg + k];
+    double px = 0, py = 0, pz = 0;
+    for (int i = 0; i < 4; ++i) {
+      px += m.xyz[3 * (size_t)ev[i]];
+      py += m.xyz[3 * (size_t)ev[i] + 1];
+      pz += m.xyz[3 * (size_t)ev[i] + 2];
+    }
+    double sx = (0.25 * px - xv) * inv_h, sy = (0.25 * py - yv) * inv_h, sz = (0.25 * pz - zv) * inv_h;
+    w[beg + k] = (float)(q0 + q1 * sx + q2 * sy + q3 * sz);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// recover: eps*(v) = g_ref + sum_t w_vt ((g_t - g_ref) + d_t), kGroup lanes
+// per vertex, stored as the pair (g_ref, deviation)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kBlock) k_fast_recover(DevMesh m, const float* __restrict__ w,
+                                                         const unsigned char* __restrict__ listed,
+                                                         const float4* __restrict__ td, float4* __restrict__ rec) {
   const int gid = blockIdx.x * blockDim.x + threadIdx.x;
   const int v = gid / kGroup;
   const int gl = gid % kGroup;
   const int lane = threadIdx.x & 31;
   const int leader = lane & ~(kGroup - 1);
-  const bool valid = v < m.V;
+  const bool active = v < m.V && !listed[v];
   int beg = 0, cnt = 0;
-  if (valid) {
+  float gr0 = 0.f, gr1 = 0.f, gr2 = 0.f;
+  if (active) {
     beg = m.p_off[v];
     cnt = m.p_off[v + 1] - beg;
-  }
-  const bool active = valid && cnt >= 4;
-  // reference gradient (the plain value of the first patch tet) and scale
-  float gr0 = 0.f, gr1 = 0.f, gr2 = 0.f, inv_h = 0.f;
-  if (active && gl == 0) {
-    int t0 = m.p_el[beg];
-    float4 a = ld4(td + 4 * (size_t)t0), b = ld4(td + 4 * (size_t)t0 + 1);
-    gr0 = a.x; gr1 = a.y; gr2 = a.z;
-    inv_h = 1.0f / b.w;
+    if (gl == 0) {
+      float4 a = ld4(td + 2 * (size_t)m.p_el[beg]);
+      gr0 = a.x; gr1 = a.y; gr2 = a.z;
+    }
   }
   gr0 = __shfl_sync(0xffffffffu, gr0, leader);
   gr1 = __shfl_sync(0xffffffffu, gr1, leader);
   gr2 = __shfl_sync(0xffffffffu, gr2, leader);
-  inv_h = __shfl_sync(0xffffffffu, inv_h, leader);
-  // normal equations of [1, sx, sy, sz] against the deviations eps_t - g_ref
-  float a[10];
-  float r[4][3];
-#pragma unroll
-  for (int i = 0; i < 10; ++i) a[i] = 0.f;
-#pragma unroll
-  for (int i = 0; i < 4; ++i) r[i][0] = r[i][1] = r[i][2] = 0.f;
-  if (active) {
-    float4 vh = ld4(vr + 2 * (size_t)v), vl = ld4(vr + 2 * (size_t)v + 1);
+  float x0 = 0.f, x1 = 0.f, x2 = 0.f;
 #pragma unroll 2
-    for (int k = gl; k < cnt; k += kGroup) {
-      int t = m.p_el[beg + k];
-      const float4* tp = td + 4 * (size_t)t;
-      float4 ga = ld4(tp), gb = ld4(tp + 1), ch = ld4(tp + 2), cl = ld4(tp + 3);
-      // integration point relative to v
-      float sx = ((ch.x - vh.x) + (cl.x - vl.x)) * inv_h;
-      float sy = ((ch.y - vh.y) + (cl.y - vl.y)) * inv_h;
-      float sz = ((ch.z - vh.z) + (cl.z - vl.z)) * inv_h;
-      float dev[3] = {(ga.x - gr0) + gb.x, (ga.y - gr1) + gb.y, (ga.z - gr2) + gb.z};
-      a[0] += 1.f; a[1] += sx; a[2] += sy; a[3] += sz;
-      a[4] += sx * sx; a[5] += sx * sy; a[6] += sx * sz;
-      a[7] += sy * sy; a[8] += sy * sz; a[9] += sz * sz;
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        r[0][c] += dev[c]; r[1][c] += sx * dev[c]; r[2][c] += sy * dev[c]; r[3][c] += sz * dev[c];
-      }
-    }
+  for (int k = gl; k < cnt; k += kGroup) {
+    const int t = __ldg(m.p_el + beg + k);
+    const float wk = __ldg(w + beg + k);
+    float4 ga = ld4(td + 2 * (size_t)t), gb = ld4(td + 2 * (size_t)t + 1);
+    x0 = fmaf(wk, (ga.x - gr0) + gb.x, x0);
+    x1 = fmaf(wk, (ga.y - gr1) + gb.y, x1);
+    x2 = fmaf(wk, (ga.z - gr2) + gb.z, x2);
   }
 #pragma unroll
   for (int o = 1; o < kGroup; o <<= 1) {
-#pragma unroll
-    for (int i = 0; i < 10; ++i) a[i] += __shfl_xor_sync(0xffffffffu, a[i], o);
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-#pragma unroll
-      for (int c = 0; c < 3; ++c) r[i][c] += __shfl_xor_sync(0xffffffffu, r[i][c], o);
+    x0 += __shfl_xor_sync(0xffffffffu, x0, o);
+    x1 += __shfl_xor_sync(0xffffffffu, x1, o);
+    x2 += __shfl_xor_sync(0xffffffffu, x2, o);
   }
-  if (!valid || gl != 0) return;
-  bool to_ref = !active;
-  if (!to_ref) {
-    // Cholesky of the normal matrix; the pivot spread estimates its condition
-    float l00 = sqrtf(a[0]);
-    float l10 = a[1] / l00, l20 = a[2] / l00, l30 = a[3] / l00;
-    float d1 = a[4] - l10 * l10;
-    float l11 = sqrtf(fmaxf(d1, 0.f));
-    float l21 = (a[5] - l20 * l10) / l11, l31 = (a[6] - l30 * l10) / l11;
-    float d2 = a[7] - l20 * l20 - l21 * l21;
-    float l22 = sqrtf(fmaxf(d2, 0.f));
-    float l32 = (a[8] - l30 * l20 - l31 * l21) / l22;
-    float d3 = a[9] - l30 * l30 - l31 * l31 - l32 * l32;
-    float l33 = sqrtf(fmaxf(d3, 0.f));
-    float pmin = fminf(fminf(d1, d2), fminf(d3, a[0]));
-    float pmax = fmaxf(fmaxf(d1, d2), fmaxf(d3, a[0]));
-    to_ref = !(pmin > 0.f) || !(pmax <= 1e6f * pmin);
-    if (!to_ref) {
-      float x0[3];
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        float y0 = r[0][c] / l00;
-        float y1 = (r[1][c] - l10 * y0) / l11;
-        float y2 = (r[2][c] - l20 * y0 - l21 * y1) / l22;
-        float y3 = (r[3][c] - l30 * y0 - l31 * y1 - l32 * y2) / l33;
-        float z3 = y3 / l33;
-        float z2 = (y2 - l32 * z3) / l22;
-        float z1 = (y1 - l21 * z2 - l31 * z3) / l11;
-        x0[c] = (y0 - l10 * z1 - l20 * z2 - l30 * z3) / l00;
-      }
-      rec[2 * (size_t)v] = make_float4(gr0, gr1, gr2, 0.f);
-      rec[2 * (size_t)v + 1] = make_float4(x0[0], x0[1], x0[2], 0.f);
-      return;
-    }
+  if (active && gl == 0) {
+    rec[2 * (size_t)v] = make_float4(gr0, gr1, gr2, 0.f);
+    rec[2 * (size_t)v + 1] = make_float4(x0, x1, x2, 0.f);
   }
-  int slot = atomicAdd(xl.count, 1);
-  if (slot < xl.cap) xl.items[slot] = v;
-  if (cnt >= 4) atomicAdd(n_refit, 1);
 }
 
 // listed vertices take the FP64 reference result, split into (hi, lo)
@@ -335,13 +361,13 @@ __device__ __forceinline__ double warp_pair_total(PairSum p) {
 }
 
 __global__ void __launch_bounds__(kBlock) k_fast_error(DevMesh m, const float4* __restrict__ td,
-                                                       const float4* __restrict__ rec, float* __restrict__ q,
+                                                       const float4* __restrict__ rec, float2* __restrict__ q,
                                                        double* __restrict__ partials) {
   __shared__ double sh[2][kBlock / 32];
   PairSum self{0.f, 0.f}, gsum{0.f, 0.f};
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < m.T; t += gridDim.x * blockDim.x) {
     int4 tv = __ldg(reinterpret_cast<const int4*>(m.ev) + t);
-    float4 ga = ld4(td + 4 * (size_t)t), gb = ld4(td + 4 * (size_t)t + 1);
+    float4 ga = ld4(td + 2 * (size_t)t), gb = ld4(td + 2 * (size_t)t + 1);
     float4 G0 = ld4(rec + 2 * (size_t)tv.x), X0 = ld4(rec + 2 * (size_t)tv.x + 1);
     float4 G1 = ld4(rec + 2 * (size_t)tv.y), X1 = ld4(rec + 2 * (size_t)tv.y + 1);
     float4 G2 = ld4(rec + 2 * (size_t)tv.z), X2 = ld4(rec + 2 * (size_t)tv.z + 1);
@@ -361,7 +387,13 @@ __global__ void __launch_bounds__(kBlock) k_fast_error(DevMesh m, const float4* 
     // h_max r, with r = err^(-1/5)
     float rr = inv_fifth_root(err);
     gsum.add(err * (rr * rr));
-    q[t] = gb.w * rr;
+    // relative error bound of q: the deviation (dx, dy, dz) is a difference
+    // of quantities of size `scale`, each good to a few FP32 ulps
+    float scale = fmaxf(fmaxf(fabsf(ga.x - g0), fabsf(ga.y - g1)), fabsf(ga.z - g2)) +
+                  fmaxf(fmaxf(fabsf(D0), fabsf(D1)), fabsf(D2)) +
+                  fmaxf(fmaxf(fabsf(X0.x), fabsf(X0.y)), fabsf(X0.z));
+    float dn = sqrtf(dx * dx + dy * dy + dz * dz);
+    q[t] = make_float2(gb.w * rr, (dn > 0.f) ? kBoundUlps * scale / dn : 3.0e38f);
   }
   double s1 = warp_pair_total(self), s2 = warp_pair_total(gsum);
   const int w = threadIdx.x >> 5;
@@ -384,56 +416,118 @@ __global__ void __launch_bounds__(kBlock) k_fast_error(DevMesh m, const float4* 
 // ---------------------------------------------------------------------------
 // average: size = size_factor * mean(q_t) over the vertex's elements
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kBlock) k_fast_average(DevMesh m, const float* __restrict__ q,
-                                                         const double* __restrict__ out3, float* __restrict__ size32) {
-  int v = blockIdx.x * blockDim.x + threadIdx.x;
-  if (v >= m.V) return;
-  int b = m.a_off[v], e = m.a_off[v + 1];
-  PairSum s{0.f, 0.f};
-  // batches of 8 independent gathers, summed in order
-  for (int k0 = b; k0 < e; k0 += 8) {
-    float x[8];
-#pragma unroll
-    for (int j = 0; j < 8; ++j) x[j] = (k0 + j < e) ? __ldg(q + __ldg(m.a_el + k0 + j)) : 0.f;
-#pragma unroll
-    for (int j = 0; j < 8; ++j)
-      if (k0 + j < e) s.add(x[j]);
+__global__ void __launch_bounds__(kBlock) k_fast_average(DevMesh m, const float2* __restrict__ q,
+                                                         const double* __restrict__ out3, float* __restrict__ size32,
+                                                         float* __restrict__ sizeb) {
+  // kGroup lanes per vertex; each lane sums every kGroup-th entry with a
+  // compensated sum, the lane sums are combined in a fixed order
+  const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int v = gid / kGroup, gl = gid % kGroup;
+  int b = 0, e = 0;
+  if (v < m.V) {
+    b = m.a_off[v];
+    e = m.a_off[v + 1];
   }
-  size32[v] = (float)out3[2] * ((s.h + s.l) / (float)(e - b));
+  PairSum s{0.f, 0.f};
+  float bound = 0.f;
+  float2 x[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    int k = b + gl + j * kGroup;
+    x[j] = (k < e) ? __ldg(q + __ldg(m.a_el + k)) : make_float2(0.f, 0.f);
+  }
+#pragma unroll
+  for (int j = 0; j < 8; ++j)
+    if (b + gl + j * kGroup < e) {
+      s.add(x[j].x);
+      bound = fmaxf(bound, x[j].y);
+    }
+  for (int k = b + gl + 8 * kGroup; k < e; k += kGroup) {  // patches above 32 elements
+    float2 y = __ldg(q + __ldg(m.a_el + k));
+    s.add(y.x);
+    bound = fmaxf(bound, y.y);
+  }
+#pragma unroll
+  for (int o = 1; o < kGroup; o <<= 1) {
+    float oh = __shfl_xor_sync(0xffffffffu, s.h, o), ol = __shfl_xor_sync(0xffffffffu, s.l, o);
+    float ob = __shfl_xor_sync(0xffffffffu, bound, o);
+    // combine the lower lane's pair first so every lane gets the same sum
+    bool low = (gl & o) == 0;
+    float ah = low ? s.h : oh, al = low ? s.l : ol, bh = low ? oh : s.h, bl = low ? ol : s.l;
+    float t, err;
+    two_sum(ah, bh, t, err);
+    s.h = t;
+    s.l = (al + bl) + err;
+    bound = fmaxf(bound, ob);
+  }
+  if (v < m.V && gl == 0) {
+    size32[v] = (float)out3[2] * ((s.h + s.l) / (float)(e - b));
+    sizeb[v] = bound;
+  }
 }
 
 // ---------------------------------------------------------------------------
 // measure: metric length with 2-point Gauss, h linearly interpolated
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ float edge_length_f32(const float4& ha, const float4& la, const float4& hb,
+                                                 const float4& lb, float s0, float s1) {
+  float4 dh, dl;
+  pdiff(hb, lb, ha, la, dh, dl);
+  float half = 0.5f * len3(dh.x + dl.x, dh.y + dl.y, dh.z + dl.z);
+  const float gp = 0.577350269189626f;
+  const float n0 = 0.5f * (1.f - gp), n1 = 0.5f * (1.f + gp);
+  return half * (1.f / (n0 * s0 + n1 * s1) + 1.f / (n1 * s0 + n0 * s1));
+}
+
+// two edges per thread (e and e + 32 within the warp's 64-edge chunk), all
+// gathers issued before use
 __global__ void __launch_bounds__(kBlock) k_fast_measure(DevMesh m, const float4* __restrict__ vr,
-                                                         const float* __restrict__ size32, uint32_t* __restrict__ split,
+                                                         const float* __restrict__ size32,
+                                                         const float* __restrict__ sizeb, uint32_t* __restrict__ split,
                                                          uint32_t* __restrict__ collapse, int* __restrict__ guard_items,
                                                          int* __restrict__ guard_count, int guard_cap,
                                                          float guard_rel) {
-  int e = blockIdx.x * blockDim.x + threadIdx.x;
-  bool s = false, c = false;
-  if (e < m.E) {
-    int2 ab = __ldg(reinterpret_cast<const int2*>(m.edv) + e);
-    float4 ha = ld4(vr + 2 * (size_t)ab.x), la = ld4(vr + 2 * (size_t)ab.x + 1);
-    float4 hb = ld4(vr + 2 * (size_t)ab.y), lb = ld4(vr + 2 * (size_t)ab.y + 1);
-    float4 dh, dl;
-    pdiff(hb, lb, ha, la, dh, dl);
-    float half = 0.5f * len3(dh.x + dl.x, dh.y + dl.y, dh.z + dl.z);
-    float s0 = __ldg(size32 + ab.x), s1 = __ldg(size32 + ab.y);
-    const float gp = 0.577350269189626f;
-    const float n0 = 0.5f * (1.f - gp), n1 = 0.5f * (1.f + gp);
-    float L = half * (1.f / (n0 * s0 + n1 * s1) + 1.f / (n1 * s0 + n0 * s1));
-    s = L > 1.5f;
-    c = L < 0.5f;
-    if (fabsf(L - 1.5f) < guard_rel * 1.5f || fabsf(L - 0.5f) < guard_rel * 0.5f) {
-      int slot = atomicAdd(guard_count, 1);
-      if (slot < guard_cap) guard_items[slot] = e;
-    }
+  const int lane = threadIdx.x & 31;
+  const long warp = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5;
+  const int e0 = (int)(warp * 64) + lane;
+  int eids[2] = {e0, e0 + 32};
+  int2 ab[2];
+  float4 ha[2], la[2], hb[2], lb[2];
+  float s0[2], s1[2], b0[2], b1[2];
+#pragma unroll
+  for (int i = 0; i < 2; ++i) ab[i] = eids[i] < m.E ? __ldg(reinterpret_cast<const int2*>(m.edv) + eids[i]) : make_int2(0, 0);
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    ha[i] = ld4(vr + 2 * (size_t)ab[i].x);
+    la[i] = ld4(vr + 2 * (size_t)ab[i].x + 1);
+    hb[i] = ld4(vr + 2 * (size_t)ab[i].y);
+    lb[i] = ld4(vr + 2 * (size_t)ab[i].y + 1);
+    s0[i] = __ldg(size32 + ab[i].x);
+    s1[i] = __ldg(size32 + ab[i].y);
+    b0[i] = __ldg(sizeb + ab[i].x);
+    b1[i] = __ldg(sizeb + ab[i].y);
   }
-  unsigned bs = __ballot_sync(0xffffffffu, s), bc = __ballot_sync(0xffffffffu, c);
-  if ((threadIdx.x & 31) == 0 && e < m.E) {
-    split[e >> 5] = bs;
-    collapse[e >> 5] = bc;
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    bool s = false, c = false;
+    const int e = eids[i];
+    if (e < m.E) {
+      float L = edge_length_f32(ha[i], la[i], hb[i], lb[i], s0[i], s1[i]);
+      s = L > 1.5f;
+      c = L < 0.5f;
+      // guard band: the FP32 length may be off by guard_rel plus the size
+      // error bounds of the two ends
+      float band = guard_rel + b0[i] + b1[i];
+      if (fabsf(L - 1.5f) <= band * 1.5f || fabsf(L - 0.5f) <= band * 0.5f) {
+        int slot = atomicAdd(guard_count, 1);
+        if (slot < guard_cap) guard_items[slot] = e;
+      }
+    }
+    unsigned bs = __ballot_sync(0xffffffffu, s), bc = __ballot_sync(0xffffffffu, c);
+    if (lane == 0 && e < m.E) {
+      split[e >> 5] = bs;
+      collapse[e >> 5] = bc;
+    }
   }
 }
 
@@ -453,38 +547,47 @@ int fast_error_blocks(int T) {
   return nb < kErrorGrid ? nb : kErrorGrid;
 }
 
-void fast_prep(const DevMesh& m, const double* u, float4* vrec, cudaStream_t s) {
-  if (m.V) k_prep<<<nblk(m.V), kBlock, 0, s>>>(m.V, m.xyz, u, vrec);
+void fast_prep_coords(const DevMesh& m, float4* vrec, cudaStream_t s) {
+  if (m.V) k_prep_coords<<<nblk(m.V), kBlock, 0, s>>>(m.V, m.xyz, vrec);
 }
 
-void fast_tet(const DevMesh& m, const float4* vrec, float4* td, cudaStream_t s) {
-  if (m.T) k_fast_tet<<<nblk(m.T), kBlock, 0, s>>>(m, vrec, td);
+void fast_prep(const DevMesh& m, const double* u, float2* u2, cudaStream_t s) {
+  if (m.V) k_prep<<<nblk(m.V), kBlock, 0, s>>>(m.V, u, u2);
 }
 
-void fast_recover(const DevMesh& m, const float4* vrec, const float4* td, float4* rec, ExpandList xl, int* n_refit,
+void fast_tet(const DevMesh& m, const float4* vrec, const float2* u2, float4* td, cudaStream_t s) {
+  if (m.T) k_fast_tet<<<nblk(m.T), kBlock, 0, s>>>(m, vrec, u2, td);
+}
+
+void fast_weights(const DevMesh& m, float* w, ExpandList xl, int* n_refit, unsigned char* listed, cudaStream_t s) {
+  if (m.V) k_fast_weights<<<nblk(m.V), kBlock, 0, s>>>(m, w, xl, n_refit, listed);
+}
+
+void fast_recover(const DevMesh& m, const float* w, const unsigned char* listed, const float4* td, float4* rec,
                   cudaStream_t s) {
-  if (m.V) k_fast_recover<<<nblk((long)m.V * kGroup), kBlock, 0, s>>>(m, vrec, td, rec, xl, n_refit);
+  if (m.V) k_fast_recover<<<nblk((long)m.V * kGroup), kBlock, 0, s>>>(m, w, listed, td, rec);
 }
 
 void fast_merge_ref(ExpandList xl, const double* rec64, float4* rec, cudaStream_t s) {
   k_merge_ref<<<152, 256, 0, s>>>(xl.items, xl.count, xl.cap, rec64, rec);
 }
 
-void fast_error(const DevMesh& m, const float4* td, const float4* rec, float* q, double* partials, int nb,
+void fast_error(const DevMesh& m, const float4* td, const float4* rec, float2* q, double* partials, int nb,
                 cudaStream_t s) {
   if (nb) k_fast_error<<<nb, kBlock, 0, s>>>(m, td, rec, q, partials);
 }
 
-void fast_average(const DevMesh& m, const float* q, const double* out3, float* size32, cudaStream_t s) {
-  if (m.V) k_fast_average<<<nblk(m.V), kBlock, 0, s>>>(m, q, out3, size32);
+void fast_average(const DevMesh& m, const float2* q, const double* out3, float* size32, float* sizeb,
+                  cudaStream_t s) {
+  if (m.V) k_fast_average<<<nblk((long)m.V * kGroup), kBlock, 0, s>>>(m, q, out3, size32, sizeb);
 }
 
-void fast_measure(const DevMesh& m, const float4* vrec, const float* size32, uint32_t* split, uint32_t* collapse,
-                  float* L32, int* guard_items, int* guard_count, int guard_cap, float guard_rel, cudaStream_t s) {
-  (void)L32;
+void fast_measure(const DevMesh& m, const float4* vrec, const float* size32, const float* sizeb, uint32_t* split,
+                  uint32_t* collapse, int* guard_items, int* guard_count, int guard_cap, float guard_rel,
+                  cudaStream_t s) {
   if (m.E)
-    k_fast_measure<<<nblk(m.E), kBlock, 0, s>>>(m, vrec, size32, split, collapse, guard_items, guard_count,
-                                                guard_cap, guard_rel);
+    k_fast_measure<<<nblk((m.E + 1) / 2), kBlock, 0, s>>>(m, vrec, size32, sizeb, split, collapse, guard_items,
+                                                          guard_count, guard_cap, guard_rel);
 }
 
 void fast_size_to_f64(int V, const float* s32, double* s64, cudaStream_t s) {

@@ -318,7 +318,7 @@ __global__ void __launch_bounds__(32) k_expand(DevMesh m, const double* __restri
                                                const double* __restrict__ u, int nc,
                                                double* __restrict__ rec, const int* __restrict__ items,
                                                const int* __restrict__ n_items_ptr, int cap, double* slab,
-                                               DevStatus* st) {
+                                               DevStatus* st, int* cache_v, int* cache_n, int* cache_el) {
   __shared__ int S[kExpandMaxElems];
   __shared__ int old[kExpandMaxElems];
   __shared__ int tmp[kExpandMaxElems];
@@ -387,6 +387,37 @@ __global__ void __launch_bounds__(32) k_expand(DevMesh m, const double* __restri
       if (!done && !failed && !(nS > n0)) failed = true;  // "all hope is lost"
     }
     if (!done && lane == 0) set_status(st, SPRG_EPATCH, v);
+    if (cache_v) {  // the grown patch depends on geometry only: keep it for later passes
+      int nfin = done ? nS : -1;
+      if (lane == 0) {
+        cache_v[it] = v;
+        cache_n[it] = nfin;
+      }
+      for (int i = lane; i < nfin; i += 32) cache_el[(size_t)it * kExpandMaxElems + i] = S[i];
+    }
+    __syncwarp();
+  }
+}
+
+// Later passes: the listed vertices' final patches come from the cache; one
+// QR fit each, no growth rounds.
+__global__ void __launch_bounds__(32) k_cached_fit(DevMesh m, const double* __restrict__ ip,
+                                                   const double* __restrict__ u, int nc, double* __restrict__ rec,
+                                                   int n_cached, const int* __restrict__ cache_v,
+                                                   const int* __restrict__ cache_n, const int* __restrict__ cache_el,
+                                                   double* slab, DevStatus* st) {
+  __shared__ double srows[kExpandSmemRows * 8];
+  const int NT = m.dim == 3 ? 4 : 3;
+  double* grows = slab + (size_t)blockIdx.x * kExpandMaxElems * (NT + nc + 1);
+  for (int it = blockIdx.x; it < n_cached; it += gridDim.x) {
+    const int v = cache_v[it], n = cache_n[it];
+    if (n < 0) {
+      if (threadIdx.x == 0) set_status(st, SPRG_EPATCH, v);
+      continue;
+    }
+    double* rows = (n * (NT + nc + 1) <= kExpandSmemRows * 8) ? srows : grows;
+    if (!slab_fit(m, cache_el + (size_t)it * kExpandMaxElems, n, ip, u, nc, rows, v, rec) && threadIdx.x == 0)
+      set_status(st, SPRG_EPATCH, v);
     __syncwarp();
   }
 }
@@ -700,16 +731,9 @@ __global__ void __launch_bounds__(kBlock) k_quality(DevMesh m, const double* __r
 // FP64 guard band of the FP32 path: for each listed edge, recompute the
 // sizes of both end vertices in FP64 (patch fits of every vertex of their
 // elements, element errors and sizes, the vertex averages) and re-decide the
-// edge's split/collapse bits.  One 128-thread block per edge; every tet of
-// the patches involved has its FP64 gradient and integration point computed
-// once into shared memory.
+// edge's split/collapse bits.
 // ---------------------------------------------------------------------
-constexpr int kGuardThreads = 128;
-constexpr int kGuardMaxTets = 96;    // elements around one end vertex
-constexpr int kGuardMaxVerts = 96;   // distinct vertices of those elements
-constexpr int kGuardMaxPatch = 512;  // distinct elements of their patches
-constexpr int kGuardVHash = 256;
-constexpr int kGuardTHash = 1024;
+constexpr int kGuardMaxTets = 96;  // elements around one end vertex
 
 // FP64 gradient of the scalar field and integration point of tet t
 // (cofactor inverse; FP64 accuracy, not the reference's rounding)
@@ -729,184 +753,135 @@ __device__ __forceinline__ void tet_grad_ip_f64(const DevMesh& m, int t, const d
   }
 }
 
-__device__ __forceinline__ int hash_find_insert(int* keys, int cap, int key, int* count, int max, int* list) {
-  unsigned h = ((unsigned)key * 2654435761u) & (cap - 1);
-  for (int probe = 0; probe < cap; ++probe) {
-    int prev = atomicCAS(&keys[2 * h], -1, key);
-    if (prev == -1) {
-      int slot = atomicAdd(count, 1);
-      if (slot < max) list[slot] = key;
-      keys[2 * h + 1] = slot;
-      return slot;
+// Guard pipeline, three kernels over all listed edges at once:
+//   collect  thread per edge: the distinct vertices of the elements around
+//            both ends (a per-vertex stamp de-duplicates across edges)
+//   fit      thread per collected vertex: FP64 normal equations of its patch
+//            on FP64 element gradients, Cholesky, the recovered value
+//   decide   warp per edge: FP64 element errors and sizes around both ends,
+//            the vertex averages in adjacency order, the metric length, the
+//            edge's split/collapse bits
+__global__ void k_guard_collect(DevMesh m, const int* __restrict__ items, const int* __restrict__ count, int cap,
+                                int stamp_id, int* __restrict__ stamp, int* __restrict__ fit_items,
+                                int* __restrict__ fit_count, int fit_cap, int* __restrict__ unresolved) {
+  // one thread per (edge, end vertex, adjacent element)
+  const int n = min(*count, cap);
+  const long total = (long)n * 2 * kGuardMaxTets;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+    const int it = (int)(i / (2 * kGuardMaxTets));
+    const int s = (int)((i / kGuardMaxTets) & 1);
+    const int j = (int)(i % kGuardMaxTets);
+    const int v = m.edv[2 * (size_t)items[it] + s];
+    const int b = m.a_off[v];
+    if (j >= m.a_off[v + 1] - b) continue;
+    const int* ev = m.ev + 4 * (size_t)m.a_el[b + j];
+    for (int a = 0; a < 4; ++a) {
+      int w = ev[a];
+      if (atomicExch(&stamp[w], stamp_id) != stamp_id) {
+        int slot = atomicAdd(fit_count, 1);
+        if (slot < fit_cap) fit_items[slot] = w;
+        else atomicAdd(unresolved, 1);
+      }
     }
-    if (prev == key) return -2;  // present; slot published by the inserter
-    h = (h + 1) & (cap - 1);
   }
-  return -1;
 }
 
-__device__ __forceinline__ int hash_lookup(const int* keys, int cap, int key) {
-  unsigned h = ((unsigned)key * 2654435761u) & (cap - 1);
-  for (int probe = 0; probe < cap; ++probe) {
-    int k = keys[2 * h];
-    if (k == key) return keys[2 * h + 1];
-    if (k == -1) return -1;
-    h = (h + 1) & (cap - 1);
+__global__ void k_guard_fit(DevMesh m, const double* __restrict__ u, const int* __restrict__ fit_items,
+                            const int* __restrict__ fit_count, int fit_cap, double* __restrict__ rec64,
+                            int* __restrict__ fit_bad) {
+  const int n = min(*fit_count, fit_cap);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int w = fit_items[i];
+    const int beg = m.p_off[w], cnt = m.p_off[w + 1] - beg;
+    V3 xw = load_xyz(m.xyz, w);
+    double a[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0}, r[4][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    double inv_h = 0;
+    for (int k = 0; k < cnt; ++k) {
+      double g[3], p[3];
+      tet_grad_ip_f64(m, m.p_el[beg + k], u, g, p);
+      double dx = p[0] - xw.v[0], dy = p[1] - xw.v[1], dz = p[2] - xw.v[2];
+      if (k == 0) inv_h = 1.0 / sqrt(dx * dx + dy * dy + dz * dz);
+      double sx = dx * inv_h, sy = dy * inv_h, sz = dz * inv_h;
+      a[0] += 1; a[1] += sx; a[2] += sy; a[3] += sz;
+      a[4] += sx * sx; a[5] += sx * sy; a[6] += sx * sz; a[7] += sy * sy; a[8] += sy * sz; a[9] += sz * sz;
+      for (int c = 0; c < 3; ++c) {
+        r[0][c] += g[c]; r[1][c] += sx * g[c]; r[2][c] += sy * g[c]; r[3][c] += sz * g[c];
+      }
+    }
+    double l00 = sqrt(a[0]);
+    double l10 = a[1] / l00, l20 = a[2] / l00, l30 = a[3] / l00;
+    double d1 = a[4] - l10 * l10;
+    double l11 = sqrt(fmax(d1, 0.0));
+    double l21 = (a[5] - l20 * l10) / l11, l31 = (a[6] - l30 * l10) / l11;
+    double d2 = a[7] - l20 * l20 - l21 * l21;
+    double l22 = sqrt(fmax(d2, 0.0));
+    double l32 = (a[8] - l30 * l20 - l31 * l21) / l22;
+    double d3 = a[9] - l30 * l30 - l31 * l31 - l32 * l32;
+    double l33 = sqrt(fmax(d3, 0.0));
+    double pmin = fmin(fmin(d1, d2), fmin(d3, a[0])), pmax = fmax(fmax(d1, d2), fmax(d3, a[0]));
+    if (cnt < 4 || !(pmin > 0) || !(pmax <= 1e10 * pmin)) {
+      rec64[3 * (size_t)w] = NAN;  // the deciding edges stay with the FP32 result
+      atomicAdd(fit_bad, 1);
+      continue;
+    }
+    for (int c = 0; c < 3; ++c) {
+      double y0 = r[0][c] / l00;
+      double y1 = (r[1][c] - l10 * y0) / l11;
+      double y2 = (r[2][c] - l20 * y0 - l21 * y1) / l22;
+      double y3 = (r[3][c] - l30 * y0 - l31 * y1 - l32 * y2) / l33;
+      double z3 = y3 / l33;
+      double z2 = (y2 - l32 * z3) / l22;
+      double z1 = (y1 - l21 * z2 - l31 * z3) / l11;
+      rec64[3 * (size_t)w + c] = (y0 - l10 * z1 - l20 * z2 - l30 * z3) / l00;
+    }
   }
-  return -1;
 }
 
-__global__ void __launch_bounds__(kGuardThreads) k_guard(DevMesh m, const double* __restrict__ u,
-                                                         const double* __restrict__ out3,
-                                                         const int* __restrict__ items,
-                                                         const int* __restrict__ count, int cap,
-                                                         uint32_t* split, uint32_t* collapse, int* unresolved) {
-  __shared__ int ends[2][kGuardMaxTets];
-  __shared__ int nends[2];
-  __shared__ int verts[kGuardMaxVerts];
-  __shared__ int nverts;
-  __shared__ int vhash[2 * kGuardVHash];
-  __shared__ int tets[kGuardMaxPatch];
-  __shared__ int ntets;
-  __shared__ int thash[2 * kGuardTHash];
-  __shared__ double tg[kGuardMaxPatch][3];
-  __shared__ double tp[kGuardMaxPatch][3];
-  __shared__ double recv[kGuardMaxVerts][3];
-  __shared__ double esz[2][kGuardMaxTets];
-  __shared__ int bad;
+__global__ void __launch_bounds__(128) k_guard_decide(DevMesh m, const double* __restrict__ u,
+                                                      const double* __restrict__ out3,
+                                                      const double* __restrict__ rec64,
+                                                      const int* __restrict__ items, const int* __restrict__ count,
+                                                      int cap, uint32_t* split, uint32_t* collapse,
+                                                      int* __restrict__ unresolved) {
+  __shared__ double esz[4][2][kGuardMaxTets];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int n = min(*count, cap);
   const double sf = out3[2];
-  const int lane = threadIdx.x & 31;
-  for (int it = blockIdx.x; it < n; it += gridDim.x) {
+  for (int it = blockIdx.x * 4 + warp; it < n; it += gridDim.x * 4) {
     const int e = items[it];
     const int ab[2] = {m.edv[2 * (size_t)e], m.edv[2 * (size_t)e + 1]};
-    if (threadIdx.x == 0) {
-      nverts = 0;
-      ntets = 0;
-      bad = 0;
-      for (int s = 0; s < 2; ++s) {
-        int c = m.a_off[ab[s] + 1] - m.a_off[ab[s]];
-        if (c > kGuardMaxTets) { bad = 1; c = 0; }
-        nends[s] = c;
-      }
-    }
-    for (int i = threadIdx.x; i < 2 * kGuardVHash; i += blockDim.x) vhash[i] = -1;
-    for (int i = threadIdx.x; i < 2 * kGuardTHash; i += blockDim.x) thash[i] = -1;
-    __syncthreads();
-    for (int s = 0; s < 2; ++s)
-      for (int i = threadIdx.x; i < nends[s]; i += blockDim.x) ends[s][i] = m.a_el[m.a_off[ab[s]] + i];
-    __syncthreads();
-    // distinct vertices W of the elements around a and b
-    for (int s = 0; s < 2; ++s)
-      for (int i = threadIdx.x; i < nends[s] * 4; i += blockDim.x)
-        if (hash_find_insert(vhash, kGuardVHash, m.ev[(size_t)ends[s][i >> 2] * 4 + (i & 3)], &nverts,
-                             kGuardMaxVerts, verts) == -1)
-          bad = 1;
-    __syncthreads();
-    const int nv = nverts;
-    if (nv > kGuardMaxVerts) bad = 1;
-    // distinct elements of the patches of W
-    for (int i = threadIdx.x; i < min(nv, kGuardMaxVerts); i += blockDim.x) {
-      int w = verts[i];
-      for (int k = m.p_off[w]; k < m.p_off[w + 1]; ++k)
-        if (hash_find_insert(thash, kGuardTHash, m.p_el[k], &ntets, kGuardMaxPatch, tets) == -1) bad = 1;
-    }
-    __syncthreads();
-    const int nt = ntets;
-    if (nt > kGuardMaxPatch) bad = 1;
-    __syncthreads();
+    int cnt[2] = {m.a_off[ab[0] + 1] - m.a_off[ab[0]], m.a_off[ab[1] + 1] - m.a_off[ab[1]]};
+    bool bad = cnt[0] > kGuardMaxTets || cnt[1] > kGuardMaxTets;
     if (!bad) {
-      for (int i = threadIdx.x; i < nt; i += blockDim.x) tet_grad_ip_f64(m, tets[i], u, tg[i], tp[i]);
-      __syncthreads();
-      // patch fits: one warp per vertex of W, lanes over its patch
-      for (int wi = threadIdx.x >> 5; wi < nv; wi += kGuardThreads / 32) {
-        int w = verts[wi];
-        int beg = m.p_off[w], cnt = m.p_off[w + 1] - beg;
-        V3 xw = load_xyz(m.xyz, w);
-        double a[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0}, r[4][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
-        int s0 = hash_lookup(thash, kGuardTHash, m.p_el[beg]);
-        double hs0 = 0;
-        {  // scale: distance to the first patch element's integration point
-          double dx = tp[s0][0] - xw.v[0], dy = tp[s0][1] - xw.v[1], dz = tp[s0][2] - xw.v[2];
-          hs0 = sqrt(dx * dx + dy * dy + dz * dz);
-        }
-        double inv_h = 1.0 / hs0;
-        for (int k = lane; k < cnt; k += 32) {
-          int sl = hash_lookup(thash, kGuardTHash, m.p_el[beg + k]);
-          double sx = (tp[sl][0] - xw.v[0]) * inv_h, sy = (tp[sl][1] - xw.v[1]) * inv_h,
-                 sz = (tp[sl][2] - xw.v[2]) * inv_h;
-          a[0] += 1; a[1] += sx; a[2] += sy; a[3] += sz;
-          a[4] += sx * sx; a[5] += sx * sy; a[6] += sx * sz; a[7] += sy * sy; a[8] += sy * sz; a[9] += sz * sz;
-          for (int c = 0; c < 3; ++c) {
-            double g = tg[sl][c];
-            r[0][c] += g; r[1][c] += sx * g; r[2][c] += sy * g; r[3][c] += sz * g;
-          }
-        }
-        for (int i = 0; i < 10; ++i) a[i] = warp_sum(a[i]);
-        for (int i = 0; i < 4; ++i)
-          for (int c = 0; c < 3; ++c) r[i][c] = warp_sum(r[i][c]);
-        if (lane == 0) {
-          double l00 = sqrt(a[0]);
-          double l10 = a[1] / l00, l20 = a[2] / l00, l30 = a[3] / l00;
-          double d1 = a[4] - l10 * l10;
-          double l11 = sqrt(fmax(d1, 0.0));
-          double l21 = (a[5] - l20 * l10) / l11, l31 = (a[6] - l30 * l10) / l11;
-          double d2 = a[7] - l20 * l20 - l21 * l21;
-          double l22 = sqrt(fmax(d2, 0.0));
-          double l32 = (a[8] - l30 * l20 - l31 * l21) / l22;
-          double d3 = a[9] - l30 * l30 - l31 * l31 - l32 * l32;
-          double l33 = sqrt(fmax(d3, 0.0));
-          double pmin = fmin(fmin(d1, d2), fmin(d3, a[0])), pmax = fmax(fmax(d1, d2), fmax(d3, a[0]));
-          if (cnt < 4 || !(pmin > 0) || !(pmax <= 1e10 * pmin)) {
-            bad = 1;
-          } else {
-            for (int c = 0; c < 3; ++c) {
-              double y0 = r[0][c] / l00;
-              double y1 = (r[1][c] - l10 * y0) / l11;
-              double y2 = (r[2][c] - l20 * y0 - l21 * y1) / l22;
-              double y3 = (r[3][c] - l30 * y0 - l31 * y1 - l32 * y2) / l33;
-              double z3 = y3 / l33;
-              double z2 = (y2 - l32 * z3) / l22;
-              double z1 = (y1 - l21 * z2 - l31 * z3) / l11;
-              recv[wi][c] = (y0 - l10 * z1 - l20 * z2 - l30 * z3) / l00;
-            }
-          }
-        }
-      }
-      __syncthreads();
-      // element sizes around a and b
       for (int s = 0; s < 2; ++s)
-        for (int i = threadIdx.x; i < nends[s]; i += blockDim.x) {
-          int t = ends[s][i];
-          const int* ev = m.ev + (size_t)t * 4;
-          int sl = hash_lookup(thash, kGuardTHash, t);
+        for (int i = lane; i < cnt[s]; i += 32) {
+          int t = m.a_el[m.a_off[ab[s]] + i];
+          const int* ev = m.ev + 4 * (size_t)t;
+          double g[3], p[3], v2[3] = {0, 0, 0};
+          tet_grad_ip_f64(m, t, u, g, p);
+          for (int k = 0; k < 4; ++k)
+            for (int c = 0; c < 3; ++c) v2[c] += rec64[3 * (size_t)ev[k] + c] * 0.25;
           V3 x[4];
-          double v2[3] = {0, 0, 0};
-          for (int k = 0; k < 4; ++k) {
-            x[k] = load_xyz(m.xyz, ev[k]);
-            int vi = hash_lookup(vhash, kGuardVHash, ev[k]);
-            for (int c = 0; c < 3; ++c) v2[c] += recv[vi][c] * 0.25;
-          }
+          for (int k = 0; k < 4; ++k) x[k] = load_xyz(m.xyz, ev[k]);
           double dV = ref::dot(ref::sub(x[1], x[0]), ref::cross(ref::sub(x[2], x[0]), ref::sub(x[3], x[0])));
           double dd = 0;
-          for (int c = 0; c < 3; ++c) dd += (tg[sl][c] - v2[c]) * (tg[sl][c] - v2[c]);
-          double sum = dd * (1.0 / 6.0) * dV;
+          for (int c = 0; c < 3; ++c) dd += (g[c] - v2[c]) * (g[c] - v2[c]);
           double h = 0;
-          for (int k = 0; k < 6; ++k) h = fmax(h, ref::len(ref::sub(x[c_tet_edges[k][1]], x[c_tet_edges[k][0]])));
-          esz[s][i] = h * pow(sum, -0.2) * sf;
+          for (int k = 0; k < 6; ++k)
+            h = fmax(h, ref::len(ref::sub(x[c_tet_edges[k][1]], x[c_tet_edges[k][0]])));
+          esz[warp][s][i] = h * pow(dd * (1.0 / 6.0) * dV, -0.2) * sf;
         }
     }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      if (bad) {
+    __syncwarp();
+    if (lane == 0) {
+      double sz[2] = {0, 0};
+      for (int s = 0; s < 2 && !bad; ++s) {
+        for (int i = 0; i < cnt[s]; ++i) sz[s] += esz[warp][s][i];
+        sz[s] /= (double)cnt[s];
+      }
+      if (bad || !(sz[0] == sz[0]) || !(sz[1] == sz[1])) {  // a fit failed (NaN) or too many elements
         atomicAdd(unresolved, 1);
       } else {
-        double sz[2];
-        for (int s = 0; s < 2; ++s) {
-          double acc = 0;
-          for (int i = 0; i < nends[s]; ++i) acc += esz[s][i];
-          sz[s] = acc / (double)nends[s];
-        }
         double hv[6] = {sz[0], sz[0], sz[0], sz[1], sz[1], sz[1]}, Rv[18];
         identity9(Rv);
         identity9(Rv + 9);
@@ -916,7 +891,7 @@ __global__ void __launch_bounds__(kGuardThreads) k_guard(DevMesh m, const double
         if (L < .5) atomicOr(&collapse[e >> 5], bit); else atomicAnd(&collapse[e >> 5], ~bit);
       }
     }
-    __syncthreads();
+    __syncwarp();
   }
 }
 
@@ -988,8 +963,17 @@ int expand_max_elems() { return kExpandMaxElems; }
 int expand_grid() { return kExpandGrid; }
 
 void launch_expand_f64(const DevMesh& m, const double* ip, const double* u, int nc, double* rec, ExpandList xl,
-                       double* slab, DevStatus* st, cudaStream_t s) {
-  k_expand<<<kExpandGrid, 32, 0, s>>>(m, ip, u, nc, rec, xl.items, xl.count, xl.cap, slab, st);
+                       double* slab, DevStatus* st, cudaStream_t s, int* cache_v, int* cache_n, int* cache_el) {
+  k_expand<<<kExpandGrid, 32, 0, s>>>(m, ip, u, nc, rec, xl.items, xl.count, xl.cap, slab, st, cache_v, cache_n,
+                                      cache_el);
+}
+
+void launch_cached_fit_f64(const DevMesh& m, const double* ip, const double* u, int nc, double* rec, int n_cached,
+                           const int* cache_v, const int* cache_n, const int* cache_el, double* slab, DevStatus* st,
+                           cudaStream_t s) {
+  if (n_cached > 0)
+    k_cached_fit<<<n_cached < kExpandGrid ? n_cached : kExpandGrid, 32, 0, s>>>(m, ip, u, nc, rec, n_cached, cache_v,
+                                                                                cache_n, cache_el, slab, st);
 }
 
 int error_blocks(int T) { return nblk(T); }
@@ -1042,8 +1026,12 @@ void launch_quality_f64(const DevMesh& m, const double* size, const double* size
 }
 
 void launch_guard_f64(const DevMesh& m, const double* u, const double* out3, const int* items, const int* count,
-                      int cap, uint32_t* split, uint32_t* collapse, int* unresolved, cudaStream_t s) {
-  k_guard<<<1216, kGuardThreads, 0, s>>>(m, u, out3, items, count, cap, split, collapse, unresolved);
+                      int cap, uint32_t* split, uint32_t* collapse, int* unresolved, GuardScratch g, cudaStream_t s) {
+  cudaMemsetAsync(g.fit_count, 0, sizeof(int), s);
+  k_guard_collect<<<152 * 8, 256, 0, s>>>(m, items, count, cap, g.stamp_id, g.stamp, g.fit_items, g.fit_count, g.fit_cap,
+                                      unresolved);
+  k_guard_fit<<<152 * 2, 128, 0, s>>>(m, u, g.fit_items, g.fit_count, g.fit_cap, g.rec64, unresolved + 1);
+  k_guard_decide<<<152 * 2, 128, 0, s>>>(m, u, out3, g.rec64, items, count, cap, split, collapse, unresolved);
 }
 
 void launch_build_v2e(const DevMesh& m, int* off, int* el, int* tmp, cudaStream_t s) {

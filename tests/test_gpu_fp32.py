@@ -1,0 +1,89 @@
+"""The FP32 path (SPRG_FP32) against the oracle and the FP64 path.
+
+Stated tolerances of the FP32 path (FP32 arithmetic with compensated
+gradient deviations, FP64 global sums per warp, FP64 guard band):
+  * size field: median of |s - s_ref| / s_ref <= 1e-6; at every
+    vertex the error is within the bound the path carries for it (large only
+    where |eps - eps*| is far below the gradient variation between
+    neighbouring elements); edges whose length is within 2e-6 plus their end
+    bounds of 0.5 / 1.5 are re-decided in FP64;
+  * size factor: relative error <= 1e-7;
+  * split/collapse marks: identical to the FP64 result (every edge within
+    2e-6 of 0.5 or 1.5 in FP32 is re-decided in FP64 by the guard band);
+  * repeated passes are bitwise identical.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def pair(oracle_mod, n, seed):
+    from core_gb300 import workload
+    m = workload.box(n, jitter=0.2, seed=seed)
+    u = workload.bump_field(m.coords, seed=seed)
+    o = oracle_mod.OracleMesh.box(n, n, n)
+    o.set_coords(m.coords)
+    return m, u, o
+
+
+@pytest.mark.parametrize("n,seed", [(12, 31), (24, 32), (40, 4)])
+def test_fp32_against_oracle(gpu_lib, oracle_lib, n, seed):
+    import core_gb300 as cg
+    m, u, o = pair(oracle_lib, n, seed)
+    ratio = 0.008 * n / 160  # the 160^3 workload's length-to-size regime
+    rc, size_o, L_o, flags_o, ns_o, nc_o, info_o = o.estimate_and_mark(u, ratio)
+    assert rc == 0
+    with cg.Context(m, precision="fp32") as ctx:
+        size, flags, ns, nc, info = ctx.estimate_and_mark(u, ratio)
+        bound = ctx.debug_read("sizeb", np.float32, m.n_verts).astype(np.float64)
+    rel = np.abs(size - size_o) / np.abs(size_o)
+    assert np.median(rel) <= 1e-6
+    assert np.all(rel <= bound + 1e-6)
+    assert abs(info["size_factor"] - info_o["size_factor"]) <= 1e-7 * info_o["size_factor"]
+    assert info["n_guard_unresolved"] == 0
+    assert np.array_equal(flags, flags_o)
+    assert (ns, nc) == (ns_o, nc_o)
+
+
+def test_fp32_matches_fp64_marks_and_is_deterministic(gpu_lib):
+    import torch
+    import core_gb300 as cg
+    from core_gb300 import workload
+    n = 64
+    m = workload.box(n, jitter=0.2, seed=33)
+    u = workload.bump_field(m.coords, seed=33)
+    ratio = 0.008 * n / 160
+    with cg.Context(m, precision="fp64") as c64:
+        s64, f64, *_ = c64.estimate_and_mark(u, ratio)
+    E = m.n_edges
+    nw = (E + 31) // 32
+    with cg.Context(m, precision="fp32") as c32:
+        s32, f32, ns, nc, info = c32.estimate_and_mark(u, ratio)
+        d_u = torch.from_numpy(u).cuda()
+        bits = torch.zeros(2 * nw, dtype=torch.int32, device="cuda")
+        stream = torch.cuda.Stream()
+        torch.cuda.set_stream(stream)
+        c32.set_stream(stream.cuda_stream)
+        outs = []
+        for _ in range(2):
+            bits.zero_()
+            c32.estimate_and_mark_resident(d_u.data_ptr(), ratio, bits.data_ptr(), bits.data_ptr() + 4 * nw)
+            torch.cuda.synchronize()
+            outs.append(bits.cpu().numpy().copy())
+        s32b = c32.debug_read("size32", np.float32, m.n_verts)
+        bound = c32.debug_read("sizeb", np.float32, m.n_verts).astype(np.float64)
+    assert np.array_equal(outs[0], outs[1])
+    assert np.array_equal(f32, f64)
+    rel = np.abs(s32 - s64) / s64
+    assert np.median(rel) <= 1e-6
+    assert np.all(rel <= bound + 1e-6)
+    assert np.array_equal(s32b.astype(np.float64), s32)
+
+
+def test_fp32_rejects_triangles(gpu_lib):
+    import core_gb300 as cg
+    from core_gb300 import workload
+    m = workload.box(8, nz=0)
+    with pytest.raises(cg.SprgError):
+        cg.Context(m, precision="fp32")
