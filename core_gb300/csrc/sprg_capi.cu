@@ -43,14 +43,19 @@ struct sprg_ctx {
   // scratch
   DevBuf partials, out3, status, count, xitems, xcount, slab, bits;
   // FP32 path buffers
-  DevBuf vrec, rec32, q32, size32, fcnt, guard, tetd, u2, wts, listed, qb, sizeb, fitems;
-  DevBuf gstamp, gfit, grec;  // guard pipeline scratch
+  DevBuf vrec, rec32, q32, sz2, fcnt, guard, tetd, u2, wts, w64, listed, geo, geo64, elen, fitems;
+  DevBuf gstamp, gfit, grec, tstamp, tslot, trec, tcount;  // guard pipeline scratch
+  // side stream for the FP64 fits of listed patches, forked from and joined
+  // back into the pass's stream
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
   int pass_id = 0;
   bool vrec_ready = false;  // coordinate records and SPR weights (per mesh)
   int n_listed = 0, n_refit = 0;
   PatchCache cache64, cache32;
   static constexpr int kGuardCap = 1 << 20;
   static constexpr float kGuardRel = 2e-6f;
+  static constexpr int kGuardTetCap = 1 << 22;  // FP64 element records of one guard pass
   std::string err_msg;
   int64_t launches = 0;
   sprg_size_info last_info{};
@@ -164,13 +169,15 @@ void prof_end(sprg_ctx* c) {
 
 // Listed patches: grow them on the first pass (recording the final element
 // sets), afterwards one QR fit per cached set.
-int listed_fits(sprg_ctx* c, PatchCache& pc, const double* ip, const double* u, int nc, double* rec64, ExpandList xl) {
+int listed_fits(sprg_ctx* c, PatchCache& pc, const double* ip, const double* u, int nc, double* rec64, ExpandList xl,
+                cudaStream_t on = nullptr) {
   DevMesh& m = c->m;
   if (pc.valid) {
-    PB("cached_fit_f64");
+    cudaStream_t s = on ? on : c->stream;
+    if (!on) PB("cached_fit_f64");
     launch_cached_fit_f64(m, ip, u, nc, rec64, pc.count, P<int>(pc.v), P<int>(pc.n), P<int>(pc.el), P<double>(c->slab),
-                          P<DevStatus>(c->status), c->stream);
-    PE();
+                          P<DevStatus>(c->status), s);
+    if (!on) PE();
     c->launches += 1;
     return check_launch(c, "cached fit");
   }
@@ -405,11 +412,18 @@ int sprg_destroy(sprg_ctx* c) {
                     &c->ael,   &c->tmp,     &c->f,    &c->ip,    &c->rec,     &c->err,    &c->esize,
                     &c->size,  &c->L,       &c->flags, &c->q,    &c->sizes3,  &c->frames9, &c->partials,
                     &c->out3,  &c->status,  &c->count, &c->xitems, &c->xcount, &c->slab, &c->bits,
-                    &c->vrec,  &c->rec32,   &c->q32,  &c->size32, &c->fcnt,   &c->guard, &c->tetd, &c->u2,
-                    &c->wts,   &c->listed,  &c->qb,   &c->sizeb,  &c->fitems, &c->gstamp, &c->gfit, &c->grec,
+                    &c->vrec,  &c->rec32,   &c->q32,  &c->sz2,  &c->fcnt,   &c->guard, &c->tetd, &c->u2,
+                    &c->wts,   &c->w64,     &c->listed, &c->geo, &c->geo64, &c->elen, &c->fitems, &c->gstamp, &c->gfit, &c->grec,
+                    &c->tstamp, &c->tslot,  &c->trec, &c->tcount,
                     &c->cache64.v, &c->cache64.n, &c->cache64.el, &c->cache32.v, &c->cache32.n, &c->cache32.el};
   for (DevBuf* b : bufs) release(*b);
   for (auto& e : c->ev_pool) cudaEventDestroy(e);
+  if (c->side) {
+    cudaStreamSynchronize(c->side);
+    cudaStreamDestroy(c->side);
+  }
+  if (c->fork) cudaEventDestroy(c->fork);
+  if (c->join) cudaEventDestroy(c->join);
   if (c->own) cudaStreamDestroy(c->own);
   delete c;
   return SPRG_OK;
@@ -631,10 +645,9 @@ static int pass_fast(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_
   ENSURE(c->vrec, 32 * (size_t)m.V);
   ENSURE(c->u2, 8 * (size_t)m.V);
   ENSURE(c->rec32, 32 * (size_t)m.V);
-  ENSURE(c->tetd, 32 * (size_t)m.T);
+  ENSURE(c->tetd, 16 * (size_t)m.T);
   ENSURE(c->q32, 8 * (size_t)m.T);
-  ENSURE(c->size32, 4 * (size_t)m.V);
-  ENSURE(c->sizeb, 4 * (size_t)m.V);
+  ENSURE(c->sz2, 8 * (size_t)m.V);
   ENSURE(c->rec, 24 * (size_t)m.V);
   ENSURE(c->fitems, sizeof(int) * (size_t)m.V);
   ENSURE(c->xcount, sizeof(int));
@@ -650,12 +663,19 @@ static int pass_fast(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_
   float4* vrec = P<float4>(c->vrec);
   float4* rec32 = P<float4>(c->rec32);
   if (!c->vrec_ready) {
-    // per mesh: coordinate records, SPR weights and the listed patches
+    // per mesh: coordinate records, element and edge geometry, SPR weights
+    // and the listed patches
     ENSURE(c->wts, sizeof(float) * nel);
+    ENSURE(c->w64, sizeof(double) * nel);
     ENSURE(c->listed, (size_t)m.V);
+    ENSURE(c->geo, 8 * (size_t)m.T);
+    ENSURE(c->geo64, 16 * (size_t)m.T);
+    ENSURE(c->elen, 4 * (size_t)m.E);
     CK(cudaMemsetAsync(c->fcnt.p, 0, 8 * sizeof(int), c->stream));
     fast_prep_coords(m, vrec, c->stream);
-    fast_weights(m, P<float>(c->wts), xl, P<int>(c->fcnt), P<unsigned char>(c->listed), c->stream);
+    fast_geometry(m, P<float2>(c->geo), P<double2>(c->geo64), P<float>(c->elen), c->stream);
+    fast_weights(m, P<float>(c->wts), P<double>(c->w64), xl, P<int>(c->fcnt), P<unsigned char>(c->listed),
+                 c->stream);
     int h[2] = {0, 0};
     CK(cudaMemcpyAsync(&h[0], P<int>(c->fcnt) + 3, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaMemcpyAsync(&h[1], c->fcnt.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
@@ -665,46 +685,79 @@ static int pass_fast(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_
     c->n_refit = h[1];
     c->vrec_ready = true;
   }
+  // the FP64 fits of the listed patches depend on the field only: once their
+  // patches are cached they run on the side stream, beside the FP32 phases
+  const bool fork = c->cache32.valid;
+  if (fork) {
+    if (!c->side) {
+      CK(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
+      CK(cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming));
+      CK(cudaEventCreateWithFlags(&c->join, cudaEventDisableTiming));
+    }
+    CK(cudaEventRecord(c->fork, c->stream));
+    CK(cudaStreamWaitEvent(c->side, c->fork, 0));
+    if ((rc = listed_fits(c, c->cache32, nullptr, P<double>(c->f), 3, P<double>(c->rec), xl, c->side))) return rc;
+    CK(cudaEventRecord(c->join, c->side));
+  }
   CK(cudaMemsetAsync(P<int>(c->fcnt) + 1, 0, sizeof(int), c->stream));
   CK(cudaMemsetAsync(P<int>(c->fcnt) + 4, 0, 2 * sizeof(int), c->stream));
   PB("prep_f32");
   fast_prep(m, P<double>(c->f), P<float2>(c->u2), c->stream);
   PE();
   PB("tet_f32");
-  fast_tet(m, vrec, P<float2>(c->u2), P<float4>(c->tetd), c->stream);
+  fast_tet(m, vrec, P<float2>(c->u2), P<uint4>(c->tetd), c->stream);
   PE();
   PB("recover_f32");
-  fast_recover(m, P<float>(c->wts), P<unsigned char>(c->listed), P<float4>(c->tetd), rec32, c->stream);
+  fast_recover(m, P<float>(c->wts), P<unsigned char>(c->listed), P<uint4>(c->tetd), rec32, c->stream);
   PE();
-  if ((rc = listed_fits(c, c->cache32, nullptr, P<double>(c->f), 3, P<double>(c->rec), xl))) return rc;
+  if (fork) {
+    CK(cudaStreamWaitEvent(c->stream, c->join, 0));
+  } else if ((rc = listed_fits(c, c->cache32, nullptr, P<double>(c->f), 3, P<double>(c->rec), xl))) {
+    return rc;
+  }
   PB("merge_f64");
   fast_merge_ref(xl, P<double>(c->rec), rec32, c->stream);
   PE();
   PB("error_f32");
-  fast_error(m, P<float4>(c->tetd), rec32, P<float2>(c->q32), P<double>(c->partials), nb, c->stream);
+  fast_error(m, P<uint4>(c->tetd), P<float2>(c->geo), rec32, P<float2>(c->q32), P<double>(c->partials), nb,
+             c->stream);
   PE();
   PB("size_factor");
   launch_size_factor(P<double>(c->partials), nb, 0, adapt_ratio, 0, m.dim, P<double>(c->out3), c->stream);
   PE();
   PB("average_f32");
-  fast_average(m, P<float2>(c->q32), P<double>(c->out3), P<float>(c->size32), P<float>(c->sizeb), c->stream);
+  fast_average(m, P<float2>(c->q32), P<double>(c->out3), P<float2>(c->sz2), c->stream);
   PE();
   PB("measure_f32");
-  fast_measure(m, vrec, P<float>(c->size32), P<float>(c->sizeb), d_split, d_collapse, P<int>(c->guard),
-               P<int>(c->fcnt) + 1, sprg_ctx::kGuardCap, sprg_ctx::kGuardRel, c->stream);
+  fast_measure(m, P<float>(c->elen), P<float2>(c->sz2), d_split, d_collapse, P<int>(c->guard), P<int>(c->fcnt) + 1,
+               sprg_ctx::kGuardCap, sprg_ctx::kGuardRel, c->stream);
   PE();
   if (!c->gstamp.p) {
     ENSURE(c->gstamp, sizeof(int) * (size_t)m.V);
     CK(cudaMemsetAsync(c->gstamp.p, 0, sizeof(int) * (size_t)m.V, c->stream));
+    ENSURE(c->tstamp, sizeof(int) * (size_t)m.T);
+    CK(cudaMemsetAsync(c->tstamp.p, 0, sizeof(int) * (size_t)m.T, c->stream));
+    ENSURE(c->tslot, sizeof(int) * (size_t)m.T);
+    CK(cudaMemsetAsync(c->tslot.p, 0xff, sizeof(int) * (size_t)m.T, c->stream));
   }
+  const int tcap = m.T < sprg_ctx::kGuardTetCap ? m.T : sprg_ctx::kGuardTetCap;
   ENSURE(c->gfit, sizeof(int) * ((size_t)m.V + 1));
   ENSURE(c->grec, 3 * sizeof(double) * (size_t)m.V);
-  GuardScratch gs{P<int>(c->gstamp), ++c->pass_id, P<int>(c->gfit) + 1, P<int>(c->gfit), m.V, P<double>(c->grec)};
-  PB("guard_f64");
-  launch_guard_f64(m, P<double>(c->f), P<double>(c->out3), P<int>(c->guard), P<int>(c->fcnt) + 1,
-                   sprg_ctx::kGuardCap, d_split, d_collapse, P<int>(c->fcnt) + 4, gs, c->stream);
-  PE();
-  c->launches += 13;
+  ENSURE(c->trec, sizeof(GuardTet) * (size_t)tcap);
+  ENSURE(c->tcount, sizeof(int));
+  GuardScratch gs{P<int>(c->gstamp),   ++c->pass_id,      P<int>(c->gfit) + 1,
+                  P<int>(c->gfit),     m.V,               P<double>(c->grec),
+                  P<int>(c->tstamp),   P<int>(c->tslot),  P<GuardTet>(c->trec),
+                  P<int>(c->tcount),   tcap,              P<double>(c->w64),
+                  P<unsigned char>(c->listed), P<double>(c->rec), P<double2>(c->geo64)};
+  static const char* const kGuardNames[4] = {"guard_collect", "guard_tets", "guard_fit", "guard_decide"};
+  for (int stage = 0; stage < 4; ++stage) {
+    PB(kGuardNames[stage]);
+    launch_guard_stage(stage, m, P<double>(c->f), P<double>(c->out3), P<int>(c->guard), P<int>(c->fcnt) + 1,
+                       sprg_ctx::kGuardCap, d_split, d_collapse, P<int>(c->fcnt) + 4, gs, c->stream);
+    PE();
+  }
+  c->launches += 12;  // 8 FP32-path kernels and 4 guard kernels (listed_fits counts its own)
   c->size_valid = false;  // the FP64 size buffer is filled on demand
   c->L_valid = false;
   return check_launch(c, "fast pass");
@@ -761,7 +814,7 @@ int sprg_estimate_and_mark(sprg_ctx* c, const double* u, double adapt_ratio, dou
   CK(cudaMemcpyAsync(&nspl, c->count.p, sizeof nspl, cudaMemcpyDeviceToHost, c->stream));
   if (c->precision == SPRG_FP32) {
     ENSURE(c->size, sizeof(double) * (size_t)m.V);
-    fast_size_to_f64(m.V, P<float>(c->size32), P<double>(c->size), c->stream);
+    fast_size_to_f64(m.V, P<float2>(c->sz2), P<double>(c->size), c->stream);
     c->launches += 1;
     c->size_valid = true;
   }
@@ -782,9 +835,9 @@ int sprg_debug_read(sprg_ctx* c, const char* name, void* host, size_t bytes) {
   struct { const char* n; DevBuf* b; } table[] = {
       {"ip", &c->ip},       {"rec", &c->rec},     {"err", &c->err},       {"esize", &c->esize},
       {"size", &c->size},   {"L", &c->L},         {"vrec", &c->vrec},     {"rec32", &c->rec32},
-      {"q32", &c->q32},     {"size32", &c->size32}, {"tetd", &c->tetd},   {"out3", &c->out3},
+      {"q32", &c->q32},     {"sz2", &c->sz2},     {"tetd", &c->tetd},     {"out3", &c->out3},
       {"fcnt", &c->fcnt},   {"guard", &c->guard}, {"xitems", &c->xitems}, {"xcount", &c->xcount},
-      {"wts", &c->wts},     {"sizeb", &c->sizeb}, {"qb", &c->qb}};
+      {"wts", &c->wts},     {"geo", &c->geo},     {"elen", &c->elen}};
   for (auto& e : table) {
     if (strcmp(e.n, name) != 0) continue;
     if (!e.b->p) return fail(c, SPRG_ESTATE, std::string("buffer not allocated: ") + name);

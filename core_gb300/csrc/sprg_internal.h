@@ -80,6 +80,10 @@ void launch_mark_bits(int E, const double* L, uint32_t* split, uint32_t* collaps
 void launch_apply_bits(int E, const uint32_t* bits, int which, int* flags, unsigned long long* count,
                        DevStatus* st, cudaStream_t s);
 // FP64 guard band of the FP32 path: re-decide the listed edges' bits.
+// One FP64 gradient (at the integration point) per element the guard touches.
+struct GuardTet {
+  double g[3];
+};
 struct GuardScratch {
   int* stamp;      // V ints, persistent (de-duplication stamps)
   int stamp_id;    // distinct per pass
@@ -87,10 +91,22 @@ struct GuardScratch {
   int* fit_count;
   int fit_cap;
   double* rec64;   // V x 3 doubles (FP64 recovered values of collected vertices)
+  int* tstamp;     // T ints, persistent (element de-duplication stamps)
+  int* tslot;      // T ints: the element's record slot (valid where stamped this pass)
+  GuardTet* trec;  // tcap records
+  int* tcount;
+  int tcap;
+  const double* w64;            // FP64 SPR weights in patch-CSR order
+  const unsigned char* listed;  // patches on the FP64 reference path
+  const double* rec_ref;        // their FP64 reference results (V x 3)
+  const double2* geo64;         // per element {det J, h_max} in FP64
 };
-// unresolved[0]: edges left to the FP32 decision, unresolved[1]: failed fits
-void launch_guard_f64(const DevMesh& m, const double* u, const double* out3, const int* items, const int* count,
-                      int cap, uint32_t* split, uint32_t* collapse, int* unresolved, GuardScratch g, cudaStream_t s);
+// unresolved[0]: edges left to the FP32 decision, unresolved[1]: failed fits.
+// Four stages in order: 0 collect vertices, 1 element gradients, 2 fits,
+// 3 decide.
+void launch_guard_stage(int stage, const DevMesh& m, const double* u, const double* out3, const int* items,
+                        const int* count, int cap, uint32_t* split, uint32_t* collapse, int* unresolved,
+                        GuardScratch g, cudaStream_t s);
 void launch_quality_f64(const DevMesh& m, const double* size, const double* sizes, const double* frames,
                         double* q, cudaStream_t s);
 

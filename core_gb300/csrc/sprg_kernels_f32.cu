@@ -20,25 +20,23 @@
 // combination of the two global integrals and in the reference (FP64) path
 // for listed patches.
 //
-// Phases:
-//   prep      thread per vertex: the field pair (the coordinate records are
-//             packed once per mesh)
-//   weights   (once per mesh, FP64) the SPR weights w_vt of every patch; the
-//             patches with fewer than 4 elements or a condition estimate
-//             above 1e6 are listed for the FP64 reference path instead
-//   tet       thread per tet: its gradient as (g_t, d_t) with g_t the plain
-//             FP32 value and d_t = J^{-1}(du - J g_t) the compensated
-//             correction, its volume weight and h_max (32 bytes per tet), so
-//             the gradient is evaluated once instead of once per use
+// Per-mesh setup (geometry only): the coordinate records, the SPR weights
+// w_vt of every patch (FP64, rounded), and per tet {w dV, h_max} and per edge
+// half its length (FP64, rounded).
+//
+// Phases of a pass:
+//   prep      four vertices per thread: the field pairs
+//   tet       thread per tet: its gradient as 16 bytes, the FP32 value s
+//             and the packed correction r (exact = s + r, see pack_corr)
 //   recover   4 lanes per vertex: eps*(v) = g_ref + sum w_vt (eps_t - g_ref)
 //   error     thread per tet: element error, SelfProduct and Error terms
 //             (compensated), q_t = h_max * err^(-1/5) and a relative error
 //             bound of q_t
-//   average   thread per vertex: size = size_factor * mean(q_t) (compensated)
-//             and the size's error bound
+//   average   4 lanes per vertex: size = size_factor * mean(q_t)
+//             (compensated) and the size's error bound, packed as a pair
 //   measure   thread per edge: metric length, split/collapse bitmaps, and the
 //             list of edges whose distance to 0.5 / 1.5 is within the error
-//             bound (re-decided in FP64 by the guard kernel)
+//             bound (re-decided in FP64 by the guard kernels)
 #include "sprg_fast.h"
 
 namespace sprg {
@@ -50,6 +48,10 @@ constexpr int kGroup = 4;  // lanes per vertex in the recover kernel
 // deviation (about 4 FP32 ulps), scaled into the error bound of q_t; on the
 // 160^3 workload the largest observed error is 0.43 of the resulting bound
 constexpr float kBoundUlps = 2.5e-7f;
+// error of the packed gradient correction: at most 2^-31 of the tet's
+// largest gradient component, times about 4 through the recovered values
+// (sum |w_vt| of an SPR patch), times 0.4 into q = h err^(-1/5)
+constexpr float kQuantRel = 8e-10f;
 
 __device__ __forceinline__ float4 ld4(const float4* p) { return __ldg(p); }
 
@@ -99,14 +101,13 @@ __device__ __forceinline__ Cof cofactors(const float4& e1, const float4& e2, con
   return k;
 }
 
-// J^{-1} r = C^T r / det
+// J^{-1} r = C^T r / det (approximate reciprocal: both uses are corrected or
+// are corrections)
 __device__ __forceinline__ void apply_inv(const Cof& k, float r1, float r2, float r3, float* g) {
-  float inv = 1.0f / k.det;
+  float inv = __fdividef(1.0f, k.det);
 #pragma unroll
   for (int j = 0; j < 3; ++j) g[j] = (k.c[0][j] * r1 + k.c[1][j] * r2 + k.c[2][j] * r3) * inv;
 }
-
-__device__ __forceinline__ float len3(float x, float y, float z) { return sqrtf(x * x + y * y + z * z); }
 
 // x^(-1/5) for the element error x: powf's estimate refined by one Newton
 // step on x r^5 = 1 whose residual is taken with a single rounding (fmaf).
@@ -121,6 +122,54 @@ __device__ __forceinline__ float inv_fifth_root(float x) {
   return fmaf(r * 0.2f, e, r);
 }
 
+// A tet gradient is kept as 16 bytes: the FP32 value s (3 floats) and its
+// correction r = exact - s with |r_j| <= ulp(s_j)/2, packed into one word as
+// a shared-exponent triple.  With E the exponent of max |r_j| and E_s that of
+// max |s_j| (E <= E_s - 24):
+//   bits 27..31  k = E_s - E - 24 (corrections below 2^-56 |s| are dropped)
+//   bits 18..26, 9..17, 0..8  m_j = rint(r_j 2^(7-E)), 9-bit two's complement
+// so r_j = m_j 2^(E_s - k - 31), exact to 2^-32 max|s_j| (half a unit).
+__device__ __forceinline__ int fexp(float a) { return ((__float_as_int(a) >> 23) & 0xff) - 127; }
+
+__device__ __forceinline__ uint32_t pack_corr(float s0, float s1, float s2, float r0, float r1, float r2) {
+  float M = fmaxf(fabsf(r0), fmaxf(fabsf(r1), fabsf(r2)));
+  if (!(M > 0.f) || !(M < 3.0e38f)) return 0u;
+  int Es = fexp(fmaxf(fabsf(s0), fmaxf(fabsf(s1), fabsf(s2))));
+  int E = fexp(M);
+  int k = Es - E - 24;
+  if (k > 31) return 0u;
+  if (k < 0) {  // only for subnormal s: keep what fits
+    k = 0;
+    E = Es - 24;
+  }
+  // 2^(7-E) as a float: exact for E > -120 (the exponent field 134 - E <= 254)
+  float sc = E > -120 ? __int_as_float((134 - E) << 23) : ldexpf(1.f, 7 - E);
+  int m0 = max(-255, min(255, __float2int_rn(E > -120 ? r0 * sc : ldexpf(r0, 7 - E))));
+  int m1 = max(-255, min(255, __float2int_rn(E > -120 ? r1 * sc : ldexpf(r1, 7 - E))));
+  int m2 = max(-255, min(255, __float2int_rn(E > -120 ? r2 * sc : ldexpf(r2, 7 - E))));
+  return ((uint32_t)k << 27) | (((uint32_t)m0 & 0x1ffu) << 18) | (((uint32_t)m1 & 0x1ffu) << 9) |
+         ((uint32_t)m2 & 0x1ffu);
+}
+
+struct Grad {
+  float s[3], r[3];
+  float gmax;  // max |s_j|
+};
+
+__device__ __forceinline__ Grad unpack_grad(uint4 a) {
+  Grad g;
+  g.s[0] = __uint_as_float(a.x);
+  g.s[1] = __uint_as_float(a.y);
+  g.s[2] = __uint_as_float(a.z);
+  g.gmax = fmaxf(fabsf(g.s[0]), fmaxf(fabsf(g.s[1]), fabsf(g.s[2])));
+  int ex = fexp(g.gmax) - (int)(a.w >> 27) - 31;
+  float sc = ex > -127 ? __int_as_float((ex + 127) << 23) : 0.f;
+  g.r[0] = (float)(((int)(a.w << 5)) >> 23) * sc;
+  g.r[1] = (float)(((int)(a.w << 14)) >> 23) * sc;
+  g.r[2] = (float)(((int)(a.w << 23)) >> 23) * sc;
+  return g;
+}
+
 // ---------------------------------------------------------------------------
 // coordinate records (once per mesh) and the field pair (once per pass)
 __global__ void __launch_bounds__(kBlock) k_prep_coords(int V, const double* __restrict__ xyz,
@@ -133,20 +182,68 @@ __global__ void __launch_bounds__(kBlock) k_prep_coords(int V, const double* __r
   rec[2 * (size_t)v + 1] = make_float4((float)(x - xh), (float)(y - yh), (float)(z - zh), 0.f);
 }
 
-__global__ void __launch_bounds__(kBlock) k_prep(int V, const double* __restrict__ u, float2* __restrict__ u2) {
-  int v = blockIdx.x * blockDim.x + threadIdx.x;
-  if (v >= V) return;
-  double w = u[v];
-  float wh = (float)w;
-  u2[v] = make_float2(wh, (float)(w - wh));
+__device__ __forceinline__ float2 split_pair(double w) {
+  float h = (float)w;
+  return make_float2(h, (float)(w - h));
 }
 
-// tet t's edge pairs (x_i - x_0, u_i - u_0), i = 1..3, their rounded sums
-// e (geometry: Jacobian, volume, lengths) and vertex 0's record
+// four vertices per thread: two 16-byte loads, two 16-byte stores
+__global__ void __launch_bounds__(kBlock) k_prep(int V, const double* __restrict__ u, float2* __restrict__ u2) {
+  const long i = 4 * (blockIdx.x * (long)blockDim.x + threadIdx.x);
+  if (i + 3 < V) {
+    double2 a = __ldg(reinterpret_cast<const double2*>(u + i));
+    double2 b = __ldg(reinterpret_cast<const double2*>(u + i + 2));
+    float2 p0 = split_pair(a.x), p1 = split_pair(a.y), p2 = split_pair(b.x), p3 = split_pair(b.y);
+    reinterpret_cast<float4*>(u2 + i)[0] = make_float4(p0.x, p0.y, p1.x, p1.y);
+    reinterpret_cast<float4*>(u2 + i)[1] = make_float4(p2.x, p2.y, p3.x, p3.y);
+  } else {
+    for (long j = i; j < V; ++j) u2[j] = split_pair(u[j]);
+  }
+}
+
+// per tet {w dV, h_max} (FP32 for the pass, {det J, h_max} in FP64 for the
+// guard) and per edge half its length, FP64 then rounded (once per mesh)
+__global__ void __launch_bounds__(kBlock) k_fast_geo(DevMesh m, float2* __restrict__ geo, double2* __restrict__ geo64) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= m.T) return;
+  const int* ev = m.ev + 4 * (size_t)t;
+  double x[4][3];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) x[i][k] = m.xyz[3 * (size_t)ev[i] + k];
+  double e[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) e[i][k] = x[i + 1][k] - x[0][k];
+  double det = e[0][0] * (e[1][1] * e[2][2] - e[1][2] * e[2][1]) + e[0][1] * (e[1][2] * e[2][0] - e[1][0] * e[2][2]) +
+               e[0][2] * (e[1][0] * e[2][1] - e[1][1] * e[2][0]);
+  double h2 = 0;
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = i + 1; j < 4; ++j) {
+      double dx = x[j][0] - x[i][0], dy = x[j][1] - x[i][1], dz = x[j][2] - x[i][2];
+      h2 = fmax(h2, dx * dx + dy * dy + dz * dz);
+    }
+  const double h = sqrt(h2);
+  geo[t] = make_float2((float)(det * (1.0 / 6.0)), (float)h);
+  geo64[t] = make_double2(det, h);
+}
+
+__global__ void __launch_bounds__(kBlock) k_fast_elen(DevMesh m, float* __restrict__ half_len) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= m.E) return;
+  const int a = m.edv[2 * (size_t)e], b = m.edv[2 * (size_t)e + 1];
+  double dx = m.xyz[3 * (size_t)b] - m.xyz[3 * (size_t)a], dy = m.xyz[3 * (size_t)b + 1] - m.xyz[3 * (size_t)a + 1],
+         dz = m.xyz[3 * (size_t)b + 2] - m.xyz[3 * (size_t)a + 2];
+  half_len[e] = (float)(0.5 * sqrt(dx * dx + dy * dy + dz * dz));
+}
+
+// tet t's edge pairs (x_i - x_0, u_i - u_0), i = 1..3, as (hi, lo)
 struct TetData {
   float4 eh[3], el[3];
-  float4 e[3];
-  float4 h0, l0;
 };
 
 __device__ __forceinline__ float4 with_u(float4 r, float2 u) { return make_float4(r.x, r.y, r.z, u.x); }
@@ -155,43 +252,41 @@ __device__ __forceinline__ float4 with_ul(float4 r, float2 u) { return make_floa
 __device__ __forceinline__ TetData load_tet(const float4* __restrict__ vr, const float2* __restrict__ u2, int4 tv) {
   TetData d;
   float2 u0 = __ldg(u2 + tv.x), u1 = __ldg(u2 + tv.y), uu2 = __ldg(u2 + tv.z), u3 = __ldg(u2 + tv.w);
-  d.h0 = with_u(ld4(vr + 2 * (size_t)tv.x), u0);
-  d.l0 = with_ul(ld4(vr + 2 * (size_t)tv.x + 1), u0);
+  float4 h0 = with_u(ld4(vr + 2 * (size_t)tv.x), u0), l0 = with_ul(ld4(vr + 2 * (size_t)tv.x + 1), u0);
   float4 h1 = with_u(ld4(vr + 2 * (size_t)tv.y), u1), l1 = with_ul(ld4(vr + 2 * (size_t)tv.y + 1), u1);
   float4 h2 = with_u(ld4(vr + 2 * (size_t)tv.z), uu2), l2 = with_ul(ld4(vr + 2 * (size_t)tv.z + 1), uu2);
   float4 h3 = with_u(ld4(vr + 2 * (size_t)tv.w), u3), l3 = with_ul(ld4(vr + 2 * (size_t)tv.w + 1), u3);
-  pdiff(h1, l1, d.h0, d.l0, d.eh[0], d.el[0]);
-  pdiff(h2, l2, d.h0, d.l0, d.eh[1], d.el[1]);
-  pdiff(h3, l3, d.h0, d.l0, d.eh[2], d.el[2]);
-#pragma unroll
-  for (int i = 0; i < 3; ++i)
-    d.e[i] = make_float4(d.eh[i].x + d.el[i].x, d.eh[i].y + d.el[i].y, d.eh[i].z + d.el[i].z,
-                         d.eh[i].w + d.el[i].w);
+  pdiff(h1, l1, h0, l0, d.eh[0], d.el[0]);
+  pdiff(h2, l2, h0, l0, d.eh[1], d.el[1]);
+  pdiff(h3, l3, h0, l0, d.eh[2], d.el[2]);
   return d;
 }
 
 // ---------------------------------------------------------------------------
-// tet: gradient pair, volume weight, h_max
+// tet: gradient value and packed correction
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kBlock) k_fast_tet(DevMesh m, const float4* __restrict__ vr,
-                                                     const float2* __restrict__ u2, float4* __restrict__ td) {
+__global__ void __launch_bounds__(kBlock, 5) k_fast_tet(DevMesh m, const float4* __restrict__ vr,
+                                                     const float2* __restrict__ u2, uint4* __restrict__ td) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= m.T) return;
   int4 tv = __ldg(reinterpret_cast<const int4*>(m.ev) + t);
   TetData d = load_tet(vr, u2, tv);
-  Cof cf = cofactors(d.e[0], d.e[1], d.e[2]);
-  float g[3], c[3];
-  apply_inv(cf, d.e[0].w, d.e[1].w, d.e[2].w, g);
+  // first estimate from the high parts with an approximate inverse; the
+  // correction J^{-1}(du - J g) with the compensated residual makes the
+  // result accurate to second order in both approximations
+  Cof cf = cofactors(d.eh[0], d.eh[1], d.eh[2]);
+  float g[3], c[3], s[3], r[3];
+  apply_inv(cf, d.eh[0].w, d.eh[1].w, d.eh[2].w, g);
   apply_inv(cf, comp_residual(d.eh[0], d.el[0], g[0], g[1], g[2]), comp_residual(d.eh[1], d.el[1], g[0], g[1], g[2]),
             comp_residual(d.eh[2], d.el[2], g[0], g[1], g[2]), c);
-  float4 a1 = d.e[0], a2 = d.e[1], a3 = d.e[2];
-  float hm = fmaxf(fmaxf(len3(a1.x, a1.y, a1.z), len3(a2.x, a2.y, a2.z)), len3(a3.x, a3.y, a3.z));
-  hm = fmaxf(hm, len3(a2.x - a1.x, a2.y - a1.y, a2.z - a1.z));
-  hm = fmaxf(hm, len3(a3.x - a1.x, a3.y - a1.y, a3.z - a1.z));
-  hm = fmaxf(hm, len3(a3.x - a2.x, a3.y - a2.y, a3.z - a2.z));
-  float4* o = td + 2 * (size_t)t;
-  o[0] = make_float4(g[0], g[1], g[2], cf.det * (1.0f / 6.0f));
-  o[1] = make_float4(c[0], c[1], c[2], hm);
+  // s + r = g + c exactly (|c| << |g|: Fast2Sum)
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    s[j] = g[j] + c[j];
+    r[j] = c[j] - (s[j] - g[j]);
+  }
+  td[t] = make_uint4(__float_as_uint(s[0]), __float_as_uint(s[1]), __float_as_uint(s[2]),
+                     pack_corr(s[0], s[1], s[2], r[0], r[1], r[2]));
 }
 
 // ---------------------------------------------------------------------------
@@ -205,7 +300,8 @@ __global__ void __launch_bounds__(kBlock) k_fast_tet(DevMesh m, const float4* __
 // fewer than four elements or a condition estimate above 1e6 are listed for
 // the FP64 reference path (growth + Householder QR) instead.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kBlock) k_fast_weights(DevMesh m, float* __restrict__ w, ExpandList xl,
+__global__ void __launch_bounds__(kBlock) k_fast_weights(DevMesh m, float* __restrict__ w, double* __restrict__ w64,
+                                                         ExpandList xl,
                                                          int* __restrict__ n_refit, unsigned char* __restrict__ listed) {
   int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= m.V) return;
@@ -268,7 +364,9 @@ __global__ void __launch_bounds__(kBlock) k_fast_weights(DevMesh m, float* __res
       pz += m.xyz[3 * (size_t)ev[i] + 2];
     }
     double sx = (0.25 * px - xv) * inv_h, sy = (0.25 * py - yv) * inv_h, sz = (0.25 * pz - zv) * inv_h;
-    w[beg + k] = (float)(q0 + q1 * sx + q2 * sy + q3 * sz);
+    const double wk = q0 + q1 * sx + q2 * sy + q3 * sz;
+    w[beg + k] = (float)wk;
+    w64[beg + k] = wk;
   }
 }
 
@@ -278,7 +376,7 @@ __global__ void __launch_bounds__(kBlock) k_fast_weights(DevMesh m, float* __res
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kBlock) k_fast_recover(DevMesh m, const float* __restrict__ w,
                                                          const unsigned char* __restrict__ listed,
-                                                         const float4* __restrict__ td, float4* __restrict__ rec) {
+                                                         const uint4* __restrict__ td, float4* __restrict__ rec) {
   const int gid = blockIdx.x * blockDim.x + threadIdx.x;
   const int v = gid / kGroup;
   const int gl = gid % kGroup;
@@ -291,8 +389,8 @@ __global__ void __launch_bounds__(kBlock) k_fast_recover(DevMesh m, const float*
     beg = m.p_off[v];
     cnt = m.p_off[v + 1] - beg;
     if (gl == 0) {
-      float4 a = ld4(td + 2 * (size_t)m.p_el[beg]);
-      gr0 = a.x; gr1 = a.y; gr2 = a.z;
+      uint4 a = __ldg(td + m.p_el[beg]);
+      gr0 = __uint_as_float(a.x); gr1 = __uint_as_float(a.y); gr2 = __uint_as_float(a.z);
     }
   }
   gr0 = __shfl_sync(0xffffffffu, gr0, leader);
@@ -303,10 +401,10 @@ __global__ void __launch_bounds__(kBlock) k_fast_recover(DevMesh m, const float*
   for (int k = gl; k < cnt; k += kGroup) {
     const int t = __ldg(m.p_el + beg + k);
     const float wk = __ldg(w + beg + k);
-    float4 ga = ld4(td + 2 * (size_t)t), gb = ld4(td + 2 * (size_t)t + 1);
-    x0 = fmaf(wk, (ga.x - gr0) + gb.x, x0);
-    x1 = fmaf(wk, (ga.y - gr1) + gb.y, x1);
-    x2 = fmaf(wk, (ga.z - gr2) + gb.z, x2);
+    Grad g = unpack_grad(__ldg(td + t));
+    x0 = fmaf(wk, (g.s[0] - gr0) + g.r[0], x0);
+    x1 = fmaf(wk, (g.s[1] - gr1) + g.r[1], x1);
+    x2 = fmaf(wk, (g.s[2] - gr2) + g.r[2], x2);
   }
 #pragma unroll
   for (int o = 1; o < kGroup; o <<= 1) {
@@ -360,40 +458,45 @@ __device__ __forceinline__ double warp_pair_total(PairSum p) {
   return (double)p.h + (double)p.l;
 }
 
-__global__ void __launch_bounds__(kBlock) k_fast_error(DevMesh m, const float4* __restrict__ td,
+__global__ void __launch_bounds__(kBlock) k_fast_error(DevMesh m, const uint4* __restrict__ td,
+                                                       const float2* __restrict__ geo,
                                                        const float4* __restrict__ rec, float2* __restrict__ q,
                                                        double* __restrict__ partials) {
   __shared__ double sh[2][kBlock / 32];
   PairSum self{0.f, 0.f}, gsum{0.f, 0.f};
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < m.T; t += gridDim.x * blockDim.x) {
     int4 tv = __ldg(reinterpret_cast<const int4*>(m.ev) + t);
-    float4 ga = ld4(td + 2 * (size_t)t), gb = ld4(td + 2 * (size_t)t + 1);
+    uint4 ta = __ldg(td + t);
+    float2 gm = __ldg(geo + t);
     float4 G0 = ld4(rec + 2 * (size_t)tv.x), X0 = ld4(rec + 2 * (size_t)tv.x + 1);
     float4 G1 = ld4(rec + 2 * (size_t)tv.y), X1 = ld4(rec + 2 * (size_t)tv.y + 1);
     float4 G2 = ld4(rec + 2 * (size_t)tv.z), X2 = ld4(rec + 2 * (size_t)tv.z + 1);
     float4 G3 = ld4(rec + 2 * (size_t)tv.w), X3 = ld4(rec + 2 * (size_t)tv.w + 1);
+    Grad ga = unpack_grad(ta);
     // eps*(IP) = g + D with g = G0, D = (sum (G_i - g) + X_i) / 4
     float g0 = G0.x, g1 = G0.y, g2 = G0.z;
     float D0 = 0.25f * ((X0.x + ((G1.x - g0) + X1.x)) + (((G2.x - g0) + X2.x) + ((G3.x - g0) + X3.x)));
     float D1 = 0.25f * ((X0.y + ((G1.y - g1) + X1.y)) + (((G2.y - g1) + X2.y) + ((G3.y - g1) + X3.y)));
     float D2 = 0.25f * ((X0.z + ((G1.z - g2) + X1.z)) + (((G2.z - g2) + X2.z) + ((G3.z - g2) + X3.z)));
-    // eps_t - eps*(IP) = (g_t - g) + d_t - D
-    float dx = ((ga.x - g0) + gb.x) - D0, dy = ((ga.y - g1) + gb.y) - D1, dz = ((ga.z - g2) + gb.z) - D2;
-    float wdv = ga.w;
+    // eps_t - eps*(IP) = (s_t - g) + r_t - D
+    float dx = ((ga.s[0] - g0) + ga.r[0]) - D0, dy = ((ga.s[1] - g1) + ga.r[1]) - D1,
+          dz = ((ga.s[2] - g2) + ga.r[2]) - D2;
+    float wdv = gm.x;
     float err = (dx * dx + dy * dy + dz * dz) * wdv;
     float ex = g0 + D0, ey = g1 + D1, ez = g2 + D2;
     self.add((ex * ex + ey * ey + ez * ez) * wdv);
     // (sqrt err)^(6/5) = err^(3/5) = err r^2 and h_max (sqrt err)^(-2/5) =
     // h_max r, with r = err^(-1/5)
     float rr = inv_fifth_root(err);
-    gsum.add(err * (rr * rr));
+    gsum.add(err > 0.f ? err * (rr * rr) : 0.f);  // (sqrt 0)^(6/5) = 0; q = +inf as in FP64
     // relative error bound of q: the deviation (dx, dy, dz) is a difference
-    // of quantities of size `scale`, each good to a few FP32 ulps
-    float scale = fmaxf(fmaxf(fabsf(ga.x - g0), fabsf(ga.y - g1)), fabsf(ga.z - g2)) +
+    // of quantities of size `scale`, each good to a few FP32 ulps, plus the
+    // packed corrections
+    float scale = fmaxf(fmaxf(fabsf(ga.s[0] - g0), fabsf(ga.s[1] - g1)), fabsf(ga.s[2] - g2)) +
                   fmaxf(fmaxf(fabsf(D0), fabsf(D1)), fabsf(D2)) +
                   fmaxf(fmaxf(fabsf(X0.x), fabsf(X0.y)), fabsf(X0.z));
     float dn = sqrtf(dx * dx + dy * dy + dz * dz);
-    q[t] = make_float2(gb.w * rr, (dn > 0.f) ? kBoundUlps * scale / dn : 3.0e38f);
+    q[t] = make_float2(gm.y * rr, (dn > 0.f) ? (kBoundUlps * scale + kQuantRel * ga.gmax) / dn : 3.0e38f);
   }
   double s1 = warp_pair_total(self), s2 = warp_pair_total(gsum);
   const int w = threadIdx.x >> 5;
@@ -417,10 +520,11 @@ __global__ void __launch_bounds__(kBlock) k_fast_error(DevMesh m, const float4* 
 // average: size = size_factor * mean(q_t) over the vertex's elements
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kBlock) k_fast_average(DevMesh m, const float2* __restrict__ q,
-                                                         const double* __restrict__ out3, float* __restrict__ size32,
-                                                         float* __restrict__ sizeb) {
+                                                         const double* __restrict__ out3, float2* __restrict__ sz2) {
   // kGroup lanes per vertex; each lane sums every kGroup-th entry with a
-  // compensated sum, the lane sums are combined in a fixed order
+  // compensated sum, the lane sums are combined in a fixed order.  The
+  // size's relative error bound is the q-weighted mean of the element
+  // bounds (|d size| <= sf/n sum q_t b_t).
   const int gid = blockIdx.x * blockDim.x + threadIdx.x;
   const int v = gid / kGroup, gl = gid % kGroup;
   int b = 0, e = 0;
@@ -429,7 +533,7 @@ __global__ void __launch_bounds__(kBlock) k_fast_average(DevMesh m, const float2
     e = m.a_off[v + 1];
   }
   PairSum s{0.f, 0.f};
-  float bound = 0.f;
+  float qb = 0.f, bmax = 0.f;
   float2 x[8];
 #pragma unroll
   for (int j = 0; j < 8; ++j) {
@@ -440,17 +544,19 @@ __global__ void __launch_bounds__(kBlock) k_fast_average(DevMesh m, const float2
   for (int j = 0; j < 8; ++j)
     if (b + gl + j * kGroup < e) {
       s.add(x[j].x);
-      bound = fmaxf(bound, x[j].y);
+      qb = fmaf(x[j].x, x[j].y, qb);
+      bmax = fmaxf(bmax, x[j].y);
     }
   for (int k = b + gl + 8 * kGroup; k < e; k += kGroup) {  // patches above 32 elements
     float2 y = __ldg(q + __ldg(m.a_el + k));
     s.add(y.x);
-    bound = fmaxf(bound, y.y);
+    qb = fmaf(y.x, y.y, qb);
+    bmax = fmaxf(bmax, y.y);
   }
 #pragma unroll
   for (int o = 1; o < kGroup; o <<= 1) {
     float oh = __shfl_xor_sync(0xffffffffu, s.h, o), ol = __shfl_xor_sync(0xffffffffu, s.l, o);
-    float ob = __shfl_xor_sync(0xffffffffu, bound, o);
+    float oq = __shfl_xor_sync(0xffffffffu, qb, o), ob = __shfl_xor_sync(0xffffffffu, bmax, o);
     // combine the lower lane's pair first so every lane gets the same sum
     bool low = (gl & o) == 0;
     float ah = low ? s.h : oh, al = low ? s.l : ol, bh = low ? oh : s.h, bl = low ? ol : s.l;
@@ -458,67 +564,64 @@ __global__ void __launch_bounds__(kBlock) k_fast_average(DevMesh m, const float2
     two_sum(ah, bh, t, err);
     s.h = t;
     s.l = (al + bl) + err;
-    bound = fmaxf(bound, ob);
+    qb = low ? qb + oq : oq + qb;
+    bmax = fmaxf(bmax, ob);
   }
   if (v < m.V && gl == 0) {
-    size32[v] = (float)out3[2] * ((s.h + s.l) / (float)(e - b));
-    sizeb[v] = bound;
+    // an infinite q (zero element error) leaves +inf in the high part and NaN
+    // in the compensation
+    float tot = isfinite(s.h) ? s.h + s.l : s.h;
+    float bound = qb / tot;
+    // an element with a zero error (infinite q) or an unbounded deviation
+    // leaves the size unbounded
+    if (!(bmax < 1e30f) || !(bound <= 1e30f)) bound = 3.0e38f;
+    sz2[v] = make_float2((float)out3[2] * (tot / (float)(e - b)), bound);
   }
 }
 
 // ---------------------------------------------------------------------------
 // measure: metric length with 2-point Gauss, h linearly interpolated
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ float edge_length_f32(const float4& ha, const float4& la, const float4& hb,
-                                                 const float4& lb, float s0, float s1) {
-  float4 dh, dl;
-  pdiff(hb, lb, ha, la, dh, dl);
-  float half = 0.5f * len3(dh.x + dl.x, dh.y + dl.y, dh.z + dl.z);
-  const float gp = 0.577350269189626f;
-  const float n0 = 0.5f * (1.f - gp), n1 = 0.5f * (1.f + gp);
-  return half * (1.f / (n0 * s0 + n1 * s1) + 1.f / (n1 * s0 + n0 * s1));
-}
-
 // two edges per thread (e and e + 32 within the warp's 64-edge chunk), all
-// gathers issued before use
-__global__ void __launch_bounds__(kBlock) k_fast_measure(DevMesh m, const float4* __restrict__ vr,
-                                                         const float* __restrict__ size32,
-                                                         const float* __restrict__ sizeb, uint32_t* __restrict__ split,
+// loads issued before use; the edge's half length is per-mesh data
+__global__ void __launch_bounds__(kBlock) k_fast_measure(DevMesh m, const float* __restrict__ half_len,
+                                                         const float2* __restrict__ sz2, uint32_t* __restrict__ split,
                                                          uint32_t* __restrict__ collapse, int* __restrict__ guard_items,
                                                          int* __restrict__ guard_count, int guard_cap,
                                                          float guard_rel) {
   const int lane = threadIdx.x & 31;
   const long warp = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5;
   const int e0 = (int)(warp * 64) + lane;
-  int eids[2] = {e0, e0 + 32};
+  const int eids[2] = {e0, e0 + 32};
   int2 ab[2];
-  float4 ha[2], la[2], hb[2], lb[2];
-  float s0[2], s1[2], b0[2], b1[2];
-#pragma unroll
-  for (int i = 0; i < 2; ++i) ab[i] = eids[i] < m.E ? __ldg(reinterpret_cast<const int2*>(m.edv) + eids[i]) : make_int2(0, 0);
+  float hl[2];
+  float2 A[2], B[2];
 #pragma unroll
   for (int i = 0; i < 2; ++i) {
-    ha[i] = ld4(vr + 2 * (size_t)ab[i].x);
-    la[i] = ld4(vr + 2 * (size_t)ab[i].x + 1);
-    hb[i] = ld4(vr + 2 * (size_t)ab[i].y);
-    lb[i] = ld4(vr + 2 * (size_t)ab[i].y + 1);
-    s0[i] = __ldg(size32 + ab[i].x);
-    s1[i] = __ldg(size32 + ab[i].y);
-    b0[i] = __ldg(sizeb + ab[i].x);
-    b1[i] = __ldg(sizeb + ab[i].y);
+    bool in = eids[i] < m.E;
+    ab[i] = in ? __ldg(reinterpret_cast<const int2*>(m.edv) + eids[i]) : make_int2(0, 0);
+    hl[i] = in ? __ldg(half_len + eids[i]) : 0.f;
   }
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    A[i] = __ldg(sz2 + ab[i].x);
+    B[i] = __ldg(sz2 + ab[i].y);
+  }
+  const float gp = 0.577350269189626f;
+  const float n0 = 0.5f * (1.f - gp), n1 = 0.5f * (1.f + gp);
 #pragma unroll
   for (int i = 0; i < 2; ++i) {
     bool s = false, c = false;
     const int e = eids[i];
     if (e < m.E) {
-      float L = edge_length_f32(ha[i], la[i], hb[i], lb[i], s0[i], s1[i]);
+      // 2-point Gauss: h(xi) interpolated linearly between the end sizes
+      float L = hl[i] * (1.f / (n0 * A[i].x + n1 * B[i].x) + 1.f / (n1 * A[i].x + n0 * B[i].x));
       s = L > 1.5f;
       c = L < 0.5f;
       // guard band: the FP32 length may be off by guard_rel plus the size
       // error bounds of the two ends
-      float band = guard_rel + b0[i] + b1[i];
-      if (fabsf(L - 1.5f) <= band * 1.5f || fabsf(L - 0.5f) <= band * 0.5f) {
+      float band = guard_rel + A[i].y + B[i].y;
+      if (fabsf(L - 1.5f) <= band * 1.5f || fabsf(L - 0.5f) <= band * 0.5f || !(L == L)) {
         int slot = atomicAdd(guard_count, 1);
         if (slot < guard_cap) guard_items[slot] = e;
       }
@@ -531,39 +634,56 @@ __global__ void __launch_bounds__(kBlock) k_fast_measure(DevMesh m, const float4
   }
 }
 
-__global__ void k_size_to_f64(int V, const float* __restrict__ s32, double* __restrict__ s64) {
+__global__ void k_size_to_f64(int V, const float2* __restrict__ s32, double* __restrict__ s64) {
   int v = blockIdx.x * blockDim.x + threadIdx.x;
-  if (v < V) s64[v] = (double)s32[v];
+  if (v < V) s64[v] = (double)s32[v].x;
 }
 
 inline int nblk(long n, int b = kBlock) { return (int)((n + b - 1) / b); }
 
-constexpr int kErrorGrid = 152 * 8;  // 8 resident 256-thread blocks per SM
+// the error kernel runs one full wave: resident blocks per SM x SMs
+int error_grid() {
+  static int grid = 0;
+  if (!grid) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fast_error, kBlock, 0);
+    grid = (sms > 0 ? sms : 152) * (per_sm > 0 ? per_sm : 4);
+  }
+  return grid;
+}
 
 }  // namespace
 
 int fast_error_blocks(int T) {
-  int nb = nblk(T);
-  return nb < kErrorGrid ? nb : kErrorGrid;
+  int nb = nblk(T), g = error_grid();
+  return nb < g ? nb : g;
 }
 
 void fast_prep_coords(const DevMesh& m, float4* vrec, cudaStream_t s) {
   if (m.V) k_prep_coords<<<nblk(m.V), kBlock, 0, s>>>(m.V, m.xyz, vrec);
 }
 
-void fast_prep(const DevMesh& m, const double* u, float2* u2, cudaStream_t s) {
-  if (m.V) k_prep<<<nblk(m.V), kBlock, 0, s>>>(m.V, u, u2);
+void fast_geometry(const DevMesh& m, float2* geo, double2* geo64, float* half_len, cudaStream_t s) {
+  if (m.T) k_fast_geo<<<nblk(m.T), kBlock, 0, s>>>(m, geo, geo64);
+  if (m.E) k_fast_elen<<<nblk(m.E), kBlock, 0, s>>>(m, half_len);
 }
 
-void fast_tet(const DevMesh& m, const float4* vrec, const float2* u2, float4* td, cudaStream_t s) {
+void fast_prep(const DevMesh& m, const double* u, float2* u2, cudaStream_t s) {
+  if (m.V) k_prep<<<nblk((m.V + 3) / 4), kBlock, 0, s>>>(m.V, u, u2);
+}
+
+void fast_tet(const DevMesh& m, const float4* vrec, const float2* u2, uint4* td, cudaStream_t s) {
   if (m.T) k_fast_tet<<<nblk(m.T), kBlock, 0, s>>>(m, vrec, u2, td);
 }
 
-void fast_weights(const DevMesh& m, float* w, ExpandList xl, int* n_refit, unsigned char* listed, cudaStream_t s) {
-  if (m.V) k_fast_weights<<<nblk(m.V), kBlock, 0, s>>>(m, w, xl, n_refit, listed);
+void fast_weights(const DevMesh& m, float* w, double* w64, ExpandList xl, int* n_refit, unsigned char* listed,
+                  cudaStream_t s) {
+  if (m.V) k_fast_weights<<<nblk(m.V), kBlock, 0, s>>>(m, w, w64, xl, n_refit, listed);
 }
 
-void fast_recover(const DevMesh& m, const float* w, const unsigned char* listed, const float4* td, float4* rec,
+void fast_recover(const DevMesh& m, const float* w, const unsigned char* listed, const uint4* td, float4* rec,
                   cudaStream_t s) {
   if (m.V) k_fast_recover<<<nblk((long)m.V * kGroup), kBlock, 0, s>>>(m, w, listed, td, rec);
 }
@@ -572,26 +692,24 @@ void fast_merge_ref(ExpandList xl, const double* rec64, float4* rec, cudaStream_
   k_merge_ref<<<152, 256, 0, s>>>(xl.items, xl.count, xl.cap, rec64, rec);
 }
 
-void fast_error(const DevMesh& m, const float4* td, const float4* rec, float2* q, double* partials, int nb,
-                cudaStream_t s) {
-  if (nb) k_fast_error<<<nb, kBlock, 0, s>>>(m, td, rec, q, partials);
+void fast_error(const DevMesh& m, const uint4* td, const float2* geo, const float4* rec, float2* q, double* partials,
+                int nb, cudaStream_t s) {
+  if (nb) k_fast_error<<<nb, kBlock, 0, s>>>(m, td, geo, rec, q, partials);
 }
 
-void fast_average(const DevMesh& m, const float2* q, const double* out3, float* size32, float* sizeb,
-                  cudaStream_t s) {
-  if (m.V) k_fast_average<<<nblk((long)m.V * kGroup), kBlock, 0, s>>>(m, q, out3, size32, sizeb);
+void fast_average(const DevMesh& m, const float2* q, const double* out3, float2* sz2, cudaStream_t s) {
+  if (m.V) k_fast_average<<<nblk((long)m.V * kGroup), kBlock, 0, s>>>(m, q, out3, sz2);
 }
 
-void fast_measure(const DevMesh& m, const float4* vrec, const float* size32, const float* sizeb, uint32_t* split,
-                  uint32_t* collapse, int* guard_items, int* guard_count, int guard_cap, float guard_rel,
-                  cudaStream_t s) {
+void fast_measure(const DevMesh& m, const float* half_len, const float2* sz2, uint32_t* split, uint32_t* collapse,
+                  int* guard_items, int* guard_count, int guard_cap, float guard_rel, cudaStream_t s) {
   if (m.E)
-    k_fast_measure<<<nblk((m.E + 1) / 2), kBlock, 0, s>>>(m, vrec, size32, sizeb, split, collapse, guard_items,
-                                                          guard_count, guard_cap, guard_rel);
+    k_fast_measure<<<nblk((m.E + 1) / 2), kBlock, 0, s>>>(m, half_len, sz2, split, collapse, guard_items, guard_count,
+                                                          guard_cap, guard_rel);
 }
 
-void fast_size_to_f64(int V, const float* s32, double* s64, cudaStream_t s) {
-  if (V) k_size_to_f64<<<nblk(V), kBlock, 0, s>>>(V, s32, s64);
+void fast_size_to_f64(int V, const float2* sz2, double* s64, cudaStream_t s) {
+  if (V) k_size_to_f64<<<nblk(V), kBlock, 0, s>>>(V, sz2, s64);
 }
 
 }  // namespace sprg

@@ -753,93 +753,146 @@ __device__ __forceinline__ void tet_grad_ip_f64(const DevMesh& m, int t, const d
   }
 }
 
-// Guard pipeline, three kernels over all listed edges at once:
-//   collect  thread per edge: the distinct vertices of the elements around
-//            both ends (a per-vertex stamp de-duplicates across edges)
+// Guard pipeline, four kernels over all listed edges at once:
+//   collect  thread per (edge, end, element around the end): the distinct
+//            vertices of those elements (a per-vertex stamp de-duplicates
+//            across edges)
+//   tets     thread per (collected vertex, element of its patch): one FP64
+//            record per distinct element (gradient, integration point,
+//            det J, h_max), so each element is evaluated once
 //   fit      thread per collected vertex: FP64 normal equations of its patch
-//            on FP64 element gradients, Cholesky, the recovered value
+//            from the records, Cholesky, the recovered value
 //   decide   warp per edge: FP64 element errors and sizes around both ends,
 //            the vertex averages in adjacency order, the metric length, the
 //            edge's split/collapse bits
+// a slot for every winning lane of the warp from one atomic on the shared
+// counter (all 32 lanes call it)
+__device__ __forceinline__ int warp_slot(bool win, int* counter) {
+  const unsigned mask = __ballot_sync(0xffffffffu, win);
+  const int lane = threadIdx.x & 31;
+  int base = 0;
+  if (mask) {
+    const int leader = __ffs(mask) - 1;
+    if (lane == leader) base = atomicAdd(counter, __popc(mask));
+    base = __shfl_sync(0xffffffffu, base, leader);
+  }
+  return base + __popc(mask & ((1u << lane) - 1));
+}
+
 __global__ void k_guard_collect(DevMesh m, const int* __restrict__ items, const int* __restrict__ count, int cap,
                                 int stamp_id, int* __restrict__ stamp, int* __restrict__ fit_items,
                                 int* __restrict__ fit_count, int fit_cap, int* __restrict__ unresolved) {
-  // one thread per (edge, end vertex, adjacent element)
+  // warp per (edge, end): lanes over the end's elements in rounds of 32
   const int n = min(*count, cap);
-  const long total = (long)n * 2 * kGuardMaxTets;
+  const long total = (long)n * 2 * 32;
+  const int lane = threadIdx.x & 31;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
-    const int it = (int)(i / (2 * kGuardMaxTets));
-    const int s = (int)((i / kGuardMaxTets) & 1);
-    const int j = (int)(i % kGuardMaxTets);
+    const int it = (int)(i >> 6);
+    const int s = (int)((i >> 5) & 1);
     const int v = m.edv[2 * (size_t)items[it] + s];
-    const int b = m.a_off[v];
-    if (j >= m.a_off[v + 1] - b) continue;
-    const int* ev = m.ev + 4 * (size_t)m.a_el[b + j];
-    for (int a = 0; a < 4; ++a) {
-      int w = ev[a];
-      if (atomicExch(&stamp[w], stamp_id) != stamp_id) {
-        int slot = atomicAdd(fit_count, 1);
-        if (slot < fit_cap) fit_items[slot] = w;
-        else atomicAdd(unresolved, 1);
+    const int b = m.a_off[v], cnt = min(m.a_off[v + 1] - b, kGuardMaxTets);
+    for (int r = 0; r < cnt; r += 32) {
+      const int j = r + lane;
+      const bool valid = j < cnt;
+      const int* ev = valid ? m.ev + 4 * (size_t)m.a_el[b + j] : nullptr;
+      for (int a = 0; a < 4; ++a) {
+        const int w = valid ? ev[a] : 0;
+        const bool win = valid && atomicExch(&stamp[w], stamp_id) != stamp_id;
+        const int slot = warp_slot(win, fit_count);
+        if (win) {
+          if (slot < fit_cap) fit_items[slot] = w;
+          else atomicAdd(unresolved, 1);
+        }
       }
     }
   }
 }
 
-__global__ void k_guard_fit(DevMesh m, const double* __restrict__ u, const int* __restrict__ fit_items,
-                            const int* __restrict__ fit_count, int fit_cap, double* __restrict__ rec64,
-                            int* __restrict__ fit_bad) {
+__global__ void k_guard_tets(DevMesh m, const double* __restrict__ u, const int* __restrict__ fit_items,
+                             const int* __restrict__ fit_count, int fit_cap, GuardScratch g) {
+  // warp per collected vertex: lanes over its patch in rounds of 32
   const int n = min(*fit_count, fit_cap);
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const int w = fit_items[i];
-    const int beg = m.p_off[w], cnt = m.p_off[w + 1] - beg;
-    V3 xw = load_xyz(m.xyz, w);
-    double a[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0}, r[4][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
-    double inv_h = 0;
-    for (int k = 0; k < cnt; ++k) {
-      double g[3], p[3];
-      tet_grad_ip_f64(m, m.p_el[beg + k], u, g, p);
-      double dx = p[0] - xw.v[0], dy = p[1] - xw.v[1], dz = p[2] - xw.v[2];
-      if (k == 0) inv_h = 1.0 / sqrt(dx * dx + dy * dy + dz * dz);
-      double sx = dx * inv_h, sy = dy * inv_h, sz = dz * inv_h;
-      a[0] += 1; a[1] += sx; a[2] += sy; a[3] += sz;
-      a[4] += sx * sx; a[5] += sx * sy; a[6] += sx * sz; a[7] += sy * sy; a[8] += sy * sz; a[9] += sz * sz;
-      for (int c = 0; c < 3; ++c) {
-        r[0][c] += g[c]; r[1][c] += sx * g[c]; r[2][c] += sy * g[c]; r[3][c] += sz * g[c];
+  const long total = (long)n * 32;
+  const int lane = threadIdx.x & 31;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+    const int w = fit_items[i >> 5];
+    if (g.listed[w]) continue;
+    const int b = m.p_off[w], cnt = min(m.p_off[w + 1] - b, kGuardMaxTets);
+    for (int r = 0; r < cnt; r += 32) {
+      const int j = r + lane;
+      const int t = j < cnt ? m.p_el[b + j] : 0;
+      const bool win = j < cnt && atomicExch(&g.tstamp[t], g.stamp_id) != g.stamp_id;
+      const int slot = warp_slot(win, g.tcount);
+      if (!win) continue;
+      if (slot >= g.tcap) {
+        g.tslot[t] = -1;
+        continue;
       }
+      GuardTet rt;
+      double p[3];
+      tet_grad_ip_f64(m, t, u, rt.g, p);
+      g.trec[slot] = rt;
+      g.tslot[t] = slot;
     }
-    double l00 = sqrt(a[0]);
-    double l10 = a[1] / l00, l20 = a[2] / l00, l30 = a[3] / l00;
-    double d1 = a[4] - l10 * l10;
-    double l11 = sqrt(fmax(d1, 0.0));
-    double l21 = (a[5] - l20 * l10) / l11, l31 = (a[6] - l30 * l10) / l11;
-    double d2 = a[7] - l20 * l20 - l21 * l21;
-    double l22 = sqrt(fmax(d2, 0.0));
-    double l32 = (a[8] - l30 * l20 - l31 * l21) / l22;
-    double d3 = a[9] - l30 * l30 - l31 * l31 - l32 * l32;
-    double l33 = sqrt(fmax(d3, 0.0));
-    double pmin = fmin(fmin(d1, d2), fmin(d3, a[0])), pmax = fmax(fmax(d1, d2), fmax(d3, a[0]));
-    if (cnt < 4 || !(pmin > 0) || !(pmax <= 1e10 * pmin)) {
-      rec64[3 * (size_t)w] = NAN;  // the deciding edges stay with the FP32 result
-      atomicAdd(fit_bad, 1);
+  }
+}
+
+// the element's record, or null when it was not evaluated this pass
+__device__ __forceinline__ const GuardTet* guard_rec(const GuardScratch& g, int t) {
+  if (g.tstamp[t] != g.stamp_id) return nullptr;
+  const int slot = g.tslot[t];
+  return slot < 0 ? nullptr : g.trec + slot;
+}
+
+// eps*(w) = sum_t w_wt eps_t with the per-mesh FP64 SPR weights, warp per
+// collected vertex (lanes over the patch, fixed reduction tree); listed
+// patches take their FP64 reference (QR, grown patch) result
+__global__ void k_guard_fit(DevMesh m, const int* __restrict__ fit_items, const int* __restrict__ fit_count,
+                            int fit_cap, GuardScratch g, int* __restrict__ fit_bad) {
+  const int n = min(*fit_count, fit_cap);
+  const int lane = threadIdx.x & 31;
+  const int nwarps = gridDim.x * (blockDim.x >> 5);
+  for (int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += nwarps) {
+    const int w = fit_items[i];
+    if (g.listed[w]) {
+      if (lane < 3) g.rec64[3 * (size_t)w + lane] = g.rec_ref[3 * (size_t)w + lane];
       continue;
     }
-    for (int c = 0; c < 3; ++c) {
-      double y0 = r[0][c] / l00;
-      double y1 = (r[1][c] - l10 * y0) / l11;
-      double y2 = (r[2][c] - l20 * y0 - l21 * y1) / l22;
-      double y3 = (r[3][c] - l30 * y0 - l31 * y1 - l32 * y2) / l33;
-      double z3 = y3 / l33;
-      double z2 = (y2 - l32 * z3) / l22;
-      double z1 = (y1 - l21 * z2 - l31 * z3) / l11;
-      rec64[3 * (size_t)w + c] = (y0 - l10 * z1 - l20 * z2 - l30 * z3) / l00;
+    const int beg = m.p_off[w], cnt = m.p_off[w + 1] - beg;
+    double r0 = 0, r1 = 0, r2 = 0;
+    bool ok = cnt <= kGuardMaxTets;
+    for (int k = lane; ok && k < cnt; k += 32) {
+      const GuardTet* rt = guard_rec(g, m.p_el[beg + k]);
+      if (!rt) {
+        ok = false;
+        break;
+      }
+      const double wk = g.w64[beg + k];
+      r0 += wk * rt->g[0];
+      r1 += wk * rt->g[1];
+      r2 += wk * rt->g[2];
+    }
+    ok = __all_sync(0xffffffffu, ok);
+    for (int o = 16; o > 0; o >>= 1) {
+      r0 += __shfl_xor_sync(0xffffffffu, r0, o);
+      r1 += __shfl_xor_sync(0xffffffffu, r1, o);
+      r2 += __shfl_xor_sync(0xffffffffu, r2, o);
+    }
+    if (lane == 0) {
+      if (!ok) {
+        g.rec64[3 * (size_t)w] = NAN;  // the deciding edges stay with the FP32 result
+        atomicAdd(fit_bad, 1);
+      } else {
+        g.rec64[3 * (size_t)w] = r0;
+        g.rec64[3 * (size_t)w + 1] = r1;
+        g.rec64[3 * (size_t)w + 2] = r2;
+      }
     }
   }
 }
 
 __global__ void __launch_bounds__(128) k_guard_decide(DevMesh m, const double* __restrict__ u,
-                                                      const double* __restrict__ out3,
-                                                      const double* __restrict__ rec64,
+                                                      const double* __restrict__ out3, GuardScratch g,
                                                       const int* __restrict__ items, const int* __restrict__ count,
                                                       int cap, uint32_t* split, uint32_t* collapse,
                                                       int* __restrict__ unresolved) {
@@ -855,21 +908,22 @@ __global__ void __launch_bounds__(128) k_guard_decide(DevMesh m, const double* _
     if (!bad) {
       for (int s = 0; s < 2; ++s)
         for (int i = lane; i < cnt[s]; i += 32) {
-          int t = m.a_el[m.a_off[ab[s]] + i];
+          const int t = m.a_el[m.a_off[ab[s]] + i];
           const int* ev = m.ev + 4 * (size_t)t;
-          double g[3], p[3], v2[3] = {0, 0, 0};
-          tet_grad_ip_f64(m, t, u, g, p);
+          double gt[3], p[3];
+          const GuardTet* rt = guard_rec(g, t);
+          if (rt) {
+            for (int c = 0; c < 3; ++c) gt[c] = rt->g[c];
+          } else {
+            tet_grad_ip_f64(m, t, u, gt, p);  // an element of listed patches only
+          }
+          double v2[3] = {0, 0, 0};
           for (int k = 0; k < 4; ++k)
-            for (int c = 0; c < 3; ++c) v2[c] += rec64[3 * (size_t)ev[k] + c] * 0.25;
-          V3 x[4];
-          for (int k = 0; k < 4; ++k) x[k] = load_xyz(m.xyz, ev[k]);
-          double dV = ref::dot(ref::sub(x[1], x[0]), ref::cross(ref::sub(x[2], x[0]), ref::sub(x[3], x[0])));
+            for (int c = 0; c < 3; ++c) v2[c] += g.rec64[3 * (size_t)ev[k] + c] * 0.25;
+          const double2 dh = g.geo64[t];  // det J, h_max
           double dd = 0;
-          for (int c = 0; c < 3; ++c) dd += (g[c] - v2[c]) * (g[c] - v2[c]);
-          double h = 0;
-          for (int k = 0; k < 6; ++k)
-            h = fmax(h, ref::len(ref::sub(x[c_tet_edges[k][1]], x[c_tet_edges[k][0]])));
-          esz[warp][s][i] = h * pow(dd * (1.0 / 6.0) * dV, -0.2) * sf;
+          for (int c = 0; c < 3; ++c) dd += (gt[c] - v2[c]) * (gt[c] - v2[c]);
+          esz[warp][s][i] = dh.y * pow(dd * (1.0 / 6.0) * dh.x, -0.2) * sf;
         }
     }
     __syncwarp();
@@ -1025,13 +1079,25 @@ void launch_quality_f64(const DevMesh& m, const double* size, const double* size
   if (m.T) k_quality<<<nblk(m.T), kBlock, 0, s>>>(m, size, sizes, frames, q);
 }
 
-void launch_guard_f64(const DevMesh& m, const double* u, const double* out3, const int* items, const int* count,
-                      int cap, uint32_t* split, uint32_t* collapse, int* unresolved, GuardScratch g, cudaStream_t s) {
-  cudaMemsetAsync(g.fit_count, 0, sizeof(int), s);
-  k_guard_collect<<<152 * 8, 256, 0, s>>>(m, items, count, cap, g.stamp_id, g.stamp, g.fit_items, g.fit_count, g.fit_cap,
-                                      unresolved);
-  k_guard_fit<<<152 * 2, 128, 0, s>>>(m, u, g.fit_items, g.fit_count, g.fit_cap, g.rec64, unresolved + 1);
-  k_guard_decide<<<152 * 2, 128, 0, s>>>(m, u, out3, g.rec64, items, count, cap, split, collapse, unresolved);
+void launch_guard_stage(int stage, const DevMesh& m, const double* u, const double* out3, const int* items,
+                        const int* count, int cap, uint32_t* split, uint32_t* collapse, int* unresolved,
+                        GuardScratch g, cudaStream_t s) {
+  switch (stage) {
+    case 0:
+      cudaMemsetAsync(g.fit_count, 0, sizeof(int), s);
+      cudaMemsetAsync(g.tcount, 0, sizeof(int), s);
+      k_guard_collect<<<152 * 4, 256, 0, s>>>(m, items, count, cap, g.stamp_id, g.stamp, g.fit_items, g.fit_count,
+                                          g.fit_cap, unresolved);
+      break;
+    case 1:
+      k_guard_tets<<<152 * 8, 256, 0, s>>>(m, u, g.fit_items, g.fit_count, g.fit_cap, g);
+      break;
+    case 2:
+      k_guard_fit<<<152 * 8, 256, 0, s>>>(m, g.fit_items, g.fit_count, g.fit_cap, g, unresolved + 1);
+      break;
+    default:
+      k_guard_decide<<<152 * 2, 128, 0, s>>>(m, u, out3, g, items, count, cap, split, collapse, unresolved);
+  }
 }
 
 void launch_build_v2e(const DevMesh& m, int* off, int* el, int* tmp, cudaStream_t s) {

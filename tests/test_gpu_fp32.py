@@ -3,19 +3,34 @@
 Stated tolerances of the FP32 path (FP32 arithmetic with compensated
 gradient deviations, FP64 global sums per warp, FP64 guard band):
   * size field: median of |s - s_ref| / s_ref <= 1e-6; at every
-    vertex the error is within the bound the path carries for it (large only
-    where |eps - eps*| is far below the gradient variation between
-    neighbouring elements); edges whose length is within 2e-6 plus their end
-    bounds of 0.5 / 1.5 are re-decided in FP64;
+    vertex the error is within the bound the path carries for it (the
+    q-weighted mean of its elements' bounds, large only where |eps - eps*| is
+    far below the gradient variation between neighbouring elements); edges
+    whose length is within 2e-6 plus their end bounds of 0.5 / 1.5 are
+    re-decided in FP64;
   * size factor: relative error <= 1e-7;
   * split/collapse marks: identical to the FP64 result (every edge within
     2e-6 of 0.5 or 1.5 in FP32 is re-decided in FP64 by the guard band);
   * repeated passes are bitwise identical.
+Where the field is linear to within rounding over a patch, the element errors
+are rounding noise in both precisions and so are the sizes: FP32 may give
++inf (a zero error, as the reference gives for err = 0) where FP64 gives a
+large finite value.  Those vertices carry an unbounded error bound (their
+edges are re-decided in FP64) and are compared through the marks only.
 """
 import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
+
+
+def check_sizes(size, ref, bound):
+    fin = np.isfinite(size) & np.isfinite(ref)
+    rel = np.abs(size[fin] - ref[fin]) / np.abs(ref[fin])
+    assert np.median(rel) <= 1e-6
+    assert np.all(rel <= bound[fin] + 1e-6)
+    assert np.all(bound[~np.isfinite(size)] >= 1e30)
+    assert np.mean(fin) > 0.99
 
 
 def pair(oracle_mod, n, seed):
@@ -36,10 +51,8 @@ def test_fp32_against_oracle(gpu_lib, oracle_lib, n, seed):
     assert rc == 0
     with cg.Context(m, precision="fp32") as ctx:
         size, flags, ns, nc, info = ctx.estimate_and_mark(u, ratio)
-        bound = ctx.debug_read("sizeb", np.float32, m.n_verts).astype(np.float64)
-    rel = np.abs(size - size_o) / np.abs(size_o)
-    assert np.median(rel) <= 1e-6
-    assert np.all(rel <= bound + 1e-6)
+        bound = ctx.debug_read("sz2", np.float32, 2 * m.n_verts)[1::2].astype(np.float64)
+    check_sizes(size, size_o, bound)
     assert abs(info["size_factor"] - info_o["size_factor"]) <= 1e-7 * info_o["size_factor"]
     assert info["n_guard_unresolved"] == 0
     assert np.array_equal(flags, flags_o)
@@ -71,14 +84,13 @@ def test_fp32_matches_fp64_marks_and_is_deterministic(gpu_lib):
             c32.estimate_and_mark_resident(d_u.data_ptr(), ratio, bits.data_ptr(), bits.data_ptr() + 4 * nw)
             torch.cuda.synchronize()
             outs.append(bits.cpu().numpy().copy())
-        s32b = c32.debug_read("size32", np.float32, m.n_verts)
-        bound = c32.debug_read("sizeb", np.float32, m.n_verts).astype(np.float64)
+        sz2 = c32.debug_read("sz2", np.float32, 2 * m.n_verts)
+        s32b, bound = sz2[0::2], sz2[1::2].astype(np.float64)
     assert np.array_equal(outs[0], outs[1])
     assert np.array_equal(f32, f64)
-    rel = np.abs(s32 - s64) / s64
-    assert np.median(rel) <= 1e-6
-    assert np.all(rel <= bound + 1e-6)
-    assert np.array_equal(s32b.astype(np.float64), s32)
+    check_sizes(s32, s64, bound)
+    assert np.array_equal(s32b.astype(np.float64), s32, equal_nan=True)
+    assert not np.any(np.isnan(s32))
 
 
 def test_fp32_rejects_triangles(gpu_lib):
