@@ -85,13 +85,14 @@ def algorithmic_bytes(kernel, V, T, E, vb=8):
         "average_f64": ib * (V + 1) + 4 * ib * T + vb * T + vb * V,
         "measure_f64": 2 * ib * E + 3 * vb * V + vb * V + vb * E,
         "mark_bits": vb * E + E // 4,
-        # FP32 path: 32-byte vertex records, 32-byte recovered (g_ref, deviation) pairs
-        "prep_f32": 8 * V + 8 * V,
-        "tet_f32": 4 * ib * T + 32 * V + 8 * V + 32 * T,
-        "recover_f32": ib * (V + 1) + 4 * ib * T + 4 * 4 * T + 32 * T + 32 * V,
-        "error_f32": 4 * ib * T + 32 * T + 32 * V + 8 * T,  # q and its bound packed (8 B)
+        # FP32 path: 32-byte vertex records (coordinates + field pair), 16-byte
+        # packed element gradients and recovered values, per-mesh geometry
+        "prep_f32": 8 * V + 32 * V + 32 * V,
+        "tet_f32": 4 * ib * T + 32 * V + 16 * T,
+        "recover_f32": ib * (V + 1) + 4 * ib * T + 4 * 4 * T + 16 * T + 16 * V,
+        "error_f32": 4 * ib * T + 16 * T + 8 * T + 16 * V + 8 * T,
         "average_f32": ib * (V + 1) + 4 * ib * T + 8 * T + 8 * V,
-        "measure_f32": 2 * ib * E + 32 * V + 8 * V + E // 4,
+        "measure_f32": 2 * ib * E + 4 * E + 8 * V + E // 4,
     }
     return table.get(kernel)
 

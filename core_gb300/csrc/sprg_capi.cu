@@ -43,7 +43,7 @@ struct sprg_ctx {
   // scratch
   DevBuf partials, out3, status, count, xitems, xcount, slab, bits;
   // FP32 path buffers
-  DevBuf vrec, rec32, q32, sz2, fcnt, guard, tetd, u2, wts, w64, listed, geo, geo64, elen, fitems;
+  DevBuf crec, vrec, rec32, q32, sz2, fcnt, guard, tetd, wts, w64, listed, geo, geo64, elen, fitems;
   DevBuf gstamp, gfit, grec, tstamp, tslot, trec, tcount;  // guard pipeline scratch
   // side stream for the FP64 fits of listed patches, forked from and joined
   // back into the pass's stream
@@ -412,7 +412,7 @@ int sprg_destroy(sprg_ctx* c) {
                     &c->ael,   &c->tmp,     &c->f,    &c->ip,    &c->rec,     &c->err,    &c->esize,
                     &c->size,  &c->L,       &c->flags, &c->q,    &c->sizes3,  &c->frames9, &c->partials,
                     &c->out3,  &c->status,  &c->count, &c->xitems, &c->xcount, &c->slab, &c->bits,
-                    &c->vrec,  &c->rec32,   &c->q32,  &c->sz2,  &c->fcnt,   &c->guard, &c->tetd, &c->u2,
+                    &c->crec,  &c->vrec,    &c->rec32, &c->q32, &c->sz2,  &c->fcnt,   &c->guard, &c->tetd,
                     &c->wts,   &c->w64,     &c->listed, &c->geo, &c->geo64, &c->elen, &c->fitems, &c->gstamp, &c->gfit, &c->grec,
                     &c->tstamp, &c->tslot,  &c->trec, &c->tcount,
                     &c->cache64.v, &c->cache64.n, &c->cache64.el, &c->cache32.v, &c->cache32.n, &c->cache32.el};
@@ -642,9 +642,9 @@ static int pass_fast(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_
   int rc;
   int nb = fast_error_blocks(m.T);
   const size_t nel = (size_t)m.T * m.nn;
+  ENSURE(c->crec, 32 * (size_t)m.V);
   ENSURE(c->vrec, 32 * (size_t)m.V);
-  ENSURE(c->u2, 8 * (size_t)m.V);
-  ENSURE(c->rec32, 32 * (size_t)m.V);
+  ENSURE(c->rec32, 16 * (size_t)m.V);
   ENSURE(c->tetd, 16 * (size_t)m.T);
   ENSURE(c->q32, 8 * (size_t)m.T);
   ENSURE(c->sz2, 8 * (size_t)m.V);
@@ -661,7 +661,7 @@ static int pass_fast(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_
   // [4] unresolved guard edges, [5] failed guard fits (0, 3 per mesh; 1, 4, 5 per pass)
   ExpandList xl{P<int>(c->fitems), P<int>(c->fcnt) + 3, m.V};
   float4* vrec = P<float4>(c->vrec);
-  float4* rec32 = P<float4>(c->rec32);
+  uint4* rec32 = P<uint4>(c->rec32);
   if (!c->vrec_ready) {
     // per mesh: coordinate records, element and edge geometry, SPR weights
     // and the listed patches
@@ -672,7 +672,7 @@ static int pass_fast(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_
     ENSURE(c->geo64, 16 * (size_t)m.T);
     ENSURE(c->elen, 4 * (size_t)m.E);
     CK(cudaMemsetAsync(c->fcnt.p, 0, 8 * sizeof(int), c->stream));
-    fast_prep_coords(m, vrec, c->stream);
+    fast_prep_coords(m, P<float4>(c->crec), c->stream);
     fast_geometry(m, P<float2>(c->geo), P<double2>(c->geo64), P<float>(c->elen), c->stream);
     fast_weights(m, P<float>(c->wts), P<double>(c->w64), xl, P<int>(c->fcnt), P<unsigned char>(c->listed),
                  c->stream);
@@ -702,10 +702,10 @@ static int pass_fast(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_
   CK(cudaMemsetAsync(P<int>(c->fcnt) + 1, 0, sizeof(int), c->stream));
   CK(cudaMemsetAsync(P<int>(c->fcnt) + 4, 0, 2 * sizeof(int), c->stream));
   PB("prep_f32");
-  fast_prep(m, P<double>(c->f), P<float2>(c->u2), c->stream);
+  fast_prep(m, P<double>(c->f), P<float4>(c->crec), vrec, c->stream);
   PE();
   PB("tet_f32");
-  fast_tet(m, vrec, P<float2>(c->u2), P<uint4>(c->tetd), c->stream);
+  fast_tet(m, vrec, P<uint4>(c->tetd), c->stream);
   PE();
   PB("recover_f32");
   fast_recover(m, P<float>(c->wts), P<unsigned char>(c->listed), P<uint4>(c->tetd), rec32, c->stream);

@@ -10,19 +10,20 @@ void fast_prep_coords(const DevMesh& m, float4* vrec, cudaStream_t s);
 // once per mesh: per tet {w dV, h_max} (FP32) and {det J, h_max} (FP64), per
 // edge half its length
 void fast_geometry(const DevMesh& m, float2* geo, double2* geo64, float* half_len, cudaStream_t s);
-// field pair (u_hi, u_lo) per vertex
-void fast_prep(const DevMesh& m, const double* u, float2* u2, cudaStream_t s);
+// the pass's vertex records: coordinate records with the field pair (u_hi, u_lo)
+void fast_prep(const DevMesh& m, const double* u, const float4* crec, float4* vrec, cudaStream_t s);
 // per tet: gradient value (3 floats) and packed correction (1 word)
-void fast_tet(const DevMesh& m, const float4* vrec, const float2* u2, uint4* td, cudaStream_t s);
+void fast_tet(const DevMesh& m, const float4* vrec, uint4* td, cudaStream_t s);
 // once per mesh: SPR weights in patch-CSR order (FP32 for the pass, FP64 for
 // the guard), listed patches
 void fast_weights(const DevMesh& m, float* w, double* w64, ExpandList xl, int* n_refit, unsigned char* listed,
                   cudaStream_t s);
-void fast_recover(const DevMesh& m, const float* w, const unsigned char* listed, const uint4* td, float4* rec,
+// recovered value per vertex as value + packed remainder (16 bytes)
+void fast_recover(const DevMesh& m, const float* w, const unsigned char* listed, const uint4* td, uint4* rec,
                   cudaStream_t s);
-void fast_merge_ref(ExpandList xl, const double* rec64, float4* rec32, cudaStream_t s);
+void fast_merge_ref(ExpandList xl, const double* rec64, uint4* rec32, cudaStream_t s);
 // q: (h_max err^(-1/5), its relative error bound) per tet
-void fast_error(const DevMesh& m, const uint4* td, const float2* geo, const float4* rec, float2* q, double* partials,
+void fast_error(const DevMesh& m, const uint4* td, const float2* geo, const uint4* rec, float2* q, double* partials,
                 int nb, cudaStream_t s);
 // sz2: (size, its relative error bound) per vertex
 void fast_average(const DevMesh& m, const float2* q, const double* out3, float2* sz2, cudaStream_t s);

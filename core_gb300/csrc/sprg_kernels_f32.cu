@@ -48,10 +48,11 @@ constexpr int kGroup = 4;  // lanes per vertex in the recover kernel
 // deviation (about 4 FP32 ulps), scaled into the error bound of q_t; on the
 // 160^3 workload the largest observed error is 0.43 of the resulting bound
 constexpr float kBoundUlps = 2.5e-7f;
-// error of the packed gradient correction: at most 2^-31 of the tet's
-// largest gradient component, times about 4 through the recovered values
-// (sum |w_vt| of an SPR patch), times 0.4 into q = h err^(-1/5)
-constexpr float kQuantRel = 8e-10f;
+// error of the packed corrections: at most 2^-31 of the largest gradient
+// component per tet, times about 4 through the recovered values (sum |w_vt|
+// of an SPR patch), plus the recovered values' own packing, times 0.4 into
+// q = h err^(-1/5)
+constexpr float kQuantRel = 1e-9f;
 
 __device__ __forceinline__ float4 ld4(const float4* p) { return __ldg(p); }
 
@@ -182,23 +183,36 @@ __global__ void __launch_bounds__(kBlock) k_prep_coords(int V, const double* __r
   rec[2 * (size_t)v + 1] = make_float4((float)(x - xh), (float)(y - yh), (float)(z - zh), 0.f);
 }
 
+// w = hi + lo with hi = w truncated to 24 significant bits and lo the rest
+// rounded to 24 bits (w to 2^-48 relative), by integer operations: a split
+// with FP64 arithmetic would run on the FP64 pipe, which bounds this kernel.
+// Magnitudes outside [2^-74, 2^128) (zero, tiny, huge, inf, NaN) take the
+// FP64 conversion.
 __device__ __forceinline__ float2 split_pair(double w) {
-  float h = (float)w;
+  const unsigned long long b = (unsigned long long)__double_as_longlong(w);
+  const int e = (int)((b >> 52) & 0x7ff);  // biased exponent
+  if (e >= 949 && e <= 1150) {
+    const unsigned sign = (unsigned)(b >> 63) << 31;
+    const unsigned hb = sign | ((unsigned)(e - 896) << 23) | (unsigned)((b >> 29) & 0x7fffffu);
+    const float lo = (float)(unsigned)(b & 0x1fffffffu) * __uint_as_float((unsigned)(e - 948) << 23);
+    return make_float2(__uint_as_float(hb), sign ? -lo : lo);
+  }
+  const float h = (float)w;
   return make_float2(h, (float)(w - h));
 }
 
-// four vertices per thread: two 16-byte loads, two 16-byte stores
-__global__ void __launch_bounds__(kBlock) k_prep(int V, const double* __restrict__ u, float2* __restrict__ u2) {
-  const long i = 4 * (blockIdx.x * (long)blockDim.x + threadIdx.x);
-  if (i + 3 < V) {
-    double2 a = __ldg(reinterpret_cast<const double2*>(u + i));
-    double2 b = __ldg(reinterpret_cast<const double2*>(u + i + 2));
-    float2 p0 = split_pair(a.x), p1 = split_pair(a.y), p2 = split_pair(b.x), p3 = split_pair(b.y);
-    reinterpret_cast<float4*>(u2 + i)[0] = make_float4(p0.x, p0.y, p1.x, p1.y);
-    reinterpret_cast<float4*>(u2 + i)[1] = make_float4(p2.x, p2.y, p3.x, p3.y);
-  } else {
-    for (long j = i; j < V; ++j) u2[j] = split_pair(u[j]);
-  }
+// the pass's vertex records: the per-mesh coordinate records with the field
+// pair in the fourth slots, {x,y,z,u}_hi, {x,y,z,u}_lo (one sector per vertex)
+__global__ void __launch_bounds__(kBlock) k_prep(int V, const double* __restrict__ u, const float4* __restrict__ crec,
+                                                 float4* __restrict__ vrec) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= V) return;
+  const float2 p = split_pair(__ldg(u + v));
+  float4 h = ld4(crec + 2 * (size_t)v), l = ld4(crec + 2 * (size_t)v + 1);
+  h.w = p.x;
+  l.w = p.y;
+  vrec[2 * (size_t)v] = h;
+  vrec[2 * (size_t)v + 1] = l;
 }
 
 // per tet {w dV, h_max} (FP32 for the pass, {det J, h_max} in FP64 for the
@@ -246,16 +260,12 @@ struct TetData {
   float4 eh[3], el[3];
 };
 
-__device__ __forceinline__ float4 with_u(float4 r, float2 u) { return make_float4(r.x, r.y, r.z, u.x); }
-__device__ __forceinline__ float4 with_ul(float4 r, float2 u) { return make_float4(r.x, r.y, r.z, u.y); }
-
-__device__ __forceinline__ TetData load_tet(const float4* __restrict__ vr, const float2* __restrict__ u2, int4 tv) {
+__device__ __forceinline__ TetData load_tet(const float4* __restrict__ vr, int4 tv) {
   TetData d;
-  float2 u0 = __ldg(u2 + tv.x), u1 = __ldg(u2 + tv.y), uu2 = __ldg(u2 + tv.z), u3 = __ldg(u2 + tv.w);
-  float4 h0 = with_u(ld4(vr + 2 * (size_t)tv.x), u0), l0 = with_ul(ld4(vr + 2 * (size_t)tv.x + 1), u0);
-  float4 h1 = with_u(ld4(vr + 2 * (size_t)tv.y), u1), l1 = with_ul(ld4(vr + 2 * (size_t)tv.y + 1), u1);
-  float4 h2 = with_u(ld4(vr + 2 * (size_t)tv.z), uu2), l2 = with_ul(ld4(vr + 2 * (size_t)tv.z + 1), uu2);
-  float4 h3 = with_u(ld4(vr + 2 * (size_t)tv.w), u3), l3 = with_ul(ld4(vr + 2 * (size_t)tv.w + 1), u3);
+  const float4 h0 = ld4(vr + 2 * (size_t)tv.x), l0 = ld4(vr + 2 * (size_t)tv.x + 1);
+  const float4 h1 = ld4(vr + 2 * (size_t)tv.y), l1 = ld4(vr + 2 * (size_t)tv.y + 1);
+  const float4 h2 = ld4(vr + 2 * (size_t)tv.z), l2 = ld4(vr + 2 * (size_t)tv.z + 1);
+  const float4 h3 = ld4(vr + 2 * (size_t)tv.w), l3 = ld4(vr + 2 * (size_t)tv.w + 1);
   pdiff(h1, l1, h0, l0, d.eh[0], d.el[0]);
   pdiff(h2, l2, h0, l0, d.eh[1], d.el[1]);
   pdiff(h3, l3, h0, l0, d.eh[2], d.el[2]);
@@ -266,11 +276,11 @@ __device__ __forceinline__ TetData load_tet(const float4* __restrict__ vr, const
 // tet: gradient value and packed correction
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kBlock, 5) k_fast_tet(DevMesh m, const float4* __restrict__ vr,
-                                                     const float2* __restrict__ u2, uint4* __restrict__ td) {
+                                                        uint4* __restrict__ td) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= m.T) return;
   int4 tv = __ldg(reinterpret_cast<const int4*>(m.ev) + t);
-  TetData d = load_tet(vr, u2, tv);
+  TetData d = load_tet(vr, tv);
   // first estimate from the high parts with an approximate inverse; the
   // correction J^{-1}(du - J g) with the compensated residual makes the
   // result accurate to second order in both approximations
@@ -376,7 +386,7 @@ __global__ void __launch_bounds__(kBlock) k_fast_weights(DevMesh m, float* __res
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kBlock) k_fast_recover(DevMesh m, const float* __restrict__ w,
                                                          const unsigned char* __restrict__ listed,
-                                                         const uint4* __restrict__ td, float4* __restrict__ rec) {
+                                                         const uint4* __restrict__ td, uint4* __restrict__ rec) {
   const int gid = blockIdx.x * blockDim.x + threadIdx.x;
   const int v = gid / kGroup;
   const int gl = gid % kGroup;
@@ -413,21 +423,26 @@ __global__ void __launch_bounds__(kBlock) k_fast_recover(DevMesh m, const float*
     x2 += __shfl_xor_sync(0xffffffffu, x2, o);
   }
   if (active && gl == 0) {
-    rec[2 * (size_t)v] = make_float4(gr0, gr1, gr2, 0.f);
-    rec[2 * (size_t)v + 1] = make_float4(x0, x1, x2, 0.f);
+    // eps*(v) = g_ref + x exactly as s + r (TwoSum), stored like a tet gradient
+    float s0, s1, s2, r0, r1, r2;
+    two_sum(gr0, x0, s0, r0);
+    two_sum(gr1, x1, s1, r1);
+    two_sum(gr2, x2, s2, r2);
+    rec[v] = make_uint4(__float_as_uint(s0), __float_as_uint(s1), __float_as_uint(s2),
+                        pack_corr(s0, s1, s2, r0, r1, r2));
   }
 }
 
-// listed vertices take the FP64 reference result, split into (hi, lo)
+// listed vertices take the FP64 reference result, as value + packed remainder
 __global__ void k_merge_ref(const int* __restrict__ items, const int* __restrict__ count, int cap,
-                            const double* __restrict__ rec64, float4* __restrict__ rec) {
+                            const double* __restrict__ rec64, uint4* __restrict__ rec) {
   int n = min(*count, cap);
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     int v = items[i];
     double a = rec64[3 * (size_t)v], b = rec64[3 * (size_t)v + 1], c = rec64[3 * (size_t)v + 2];
     float ah = (float)a, bh = (float)b, ch = (float)c;
-    rec[2 * (size_t)v] = make_float4(ah, bh, ch, 0.f);
-    rec[2 * (size_t)v + 1] = make_float4((float)(a - ah), (float)(b - bh), (float)(c - ch), 0.f);
+    rec[v] = make_uint4(__float_as_uint(ah), __float_as_uint(bh), __float_as_uint(ch),
+                        pack_corr(ah, bh, ch, (float)(a - ah), (float)(b - bh), (float)(c - ch)));
   }
 }
 
@@ -460,7 +475,7 @@ __device__ __forceinline__ double warp_pair_total(PairSum p) {
 
 __global__ void __launch_bounds__(kBlock) k_fast_error(DevMesh m, const uint4* __restrict__ td,
                                                        const float2* __restrict__ geo,
-                                                       const float4* __restrict__ rec, float2* __restrict__ q,
+                                                       const uint4* __restrict__ rec, float2* __restrict__ q,
                                                        double* __restrict__ partials) {
   __shared__ double sh[2][kBlock / 32];
   PairSum self{0.f, 0.f}, gsum{0.f, 0.f};
@@ -468,16 +483,14 @@ __global__ void __launch_bounds__(kBlock) k_fast_error(DevMesh m, const uint4* _
     int4 tv = __ldg(reinterpret_cast<const int4*>(m.ev) + t);
     uint4 ta = __ldg(td + t);
     float2 gm = __ldg(geo + t);
-    float4 G0 = ld4(rec + 2 * (size_t)tv.x), X0 = ld4(rec + 2 * (size_t)tv.x + 1);
-    float4 G1 = ld4(rec + 2 * (size_t)tv.y), X1 = ld4(rec + 2 * (size_t)tv.y + 1);
-    float4 G2 = ld4(rec + 2 * (size_t)tv.z), X2 = ld4(rec + 2 * (size_t)tv.z + 1);
-    float4 G3 = ld4(rec + 2 * (size_t)tv.w), X3 = ld4(rec + 2 * (size_t)tv.w + 1);
+    const uint4 R0 = __ldg(rec + tv.x), R1 = __ldg(rec + tv.y), R2 = __ldg(rec + tv.z), R3 = __ldg(rec + tv.w);
     Grad ga = unpack_grad(ta);
-    // eps*(IP) = g + D with g = G0, D = (sum (G_i - g) + X_i) / 4
-    float g0 = G0.x, g1 = G0.y, g2 = G0.z;
-    float D0 = 0.25f * ((X0.x + ((G1.x - g0) + X1.x)) + (((G2.x - g0) + X2.x) + ((G3.x - g0) + X3.x)));
-    float D1 = 0.25f * ((X0.y + ((G1.y - g1) + X1.y)) + (((G2.y - g1) + X2.y) + ((G3.y - g1) + X3.y)));
-    float D2 = 0.25f * ((X0.z + ((G1.z - g2) + X1.z)) + (((G2.z - g2) + X2.z) + ((G3.z - g2) + X3.z)));
+    const Grad E0 = unpack_grad(R0), E1 = unpack_grad(R1), E2 = unpack_grad(R2), E3 = unpack_grad(R3);
+    // eps*(IP) = g + D with g = s of vertex 0, D = sum ((s_i - g) + r_i) / 4
+    const float g0 = E0.s[0], g1 = E0.s[1], g2 = E0.s[2];
+    float D0 = 0.25f * ((E0.r[0] + ((E1.s[0] - g0) + E1.r[0])) + (((E2.s[0] - g0) + E2.r[0]) + ((E3.s[0] - g0) + E3.r[0])));
+    float D1 = 0.25f * ((E0.r[1] + ((E1.s[1] - g1) + E1.r[1])) + (((E2.s[1] - g1) + E2.r[1]) + ((E3.s[1] - g1) + E3.r[1])));
+    float D2 = 0.25f * ((E0.r[2] + ((E1.s[2] - g2) + E1.r[2])) + (((E2.s[2] - g2) + E2.r[2]) + ((E3.s[2] - g2) + E3.r[2])));
     // eps_t - eps*(IP) = (s_t - g) + r_t - D
     float dx = ((ga.s[0] - g0) + ga.r[0]) - D0, dy = ((ga.s[1] - g1) + ga.r[1]) - D1,
           dz = ((ga.s[2] - g2) + ga.r[2]) - D2;
@@ -493,8 +506,7 @@ __global__ void __launch_bounds__(kBlock) k_fast_error(DevMesh m, const uint4* _
     // of quantities of size `scale`, each good to a few FP32 ulps, plus the
     // packed corrections
     float scale = fmaxf(fmaxf(fabsf(ga.s[0] - g0), fabsf(ga.s[1] - g1)), fabsf(ga.s[2] - g2)) +
-                  fmaxf(fmaxf(fabsf(D0), fabsf(D1)), fabsf(D2)) +
-                  fmaxf(fmaxf(fabsf(X0.x), fabsf(X0.y)), fabsf(X0.z));
+                  fmaxf(fmaxf(fabsf(D0), fabsf(D1)), fabsf(D2));
     float dn = sqrtf(dx * dx + dy * dy + dz * dz);
     q[t] = make_float2(gm.y * rr, (dn > 0.f) ? (kBoundUlps * scale + kQuantRel * ga.gmax) / dn : 3.0e38f);
   }
@@ -670,12 +682,12 @@ void fast_geometry(const DevMesh& m, float2* geo, double2* geo64, float* half_le
   if (m.E) k_fast_elen<<<nblk(m.E), kBlock, 0, s>>>(m, half_len);
 }
 
-void fast_prep(const DevMesh& m, const double* u, float2* u2, cudaStream_t s) {
-  if (m.V) k_prep<<<nblk((m.V + 3) / 4), kBlock, 0, s>>>(m.V, u, u2);
+void fast_prep(const DevMesh& m, const double* u, const float4* crec, float4* vrec, cudaStream_t s) {
+  if (m.V) k_prep<<<nblk(m.V), kBlock, 0, s>>>(m.V, u, crec, vrec);
 }
 
-void fast_tet(const DevMesh& m, const float4* vrec, const float2* u2, uint4* td, cudaStream_t s) {
-  if (m.T) k_fast_tet<<<nblk(m.T), kBlock, 0, s>>>(m, vrec, u2, td);
+void fast_tet(const DevMesh& m, const float4* vrec, uint4* td, cudaStream_t s) {
+  if (m.T) k_fast_tet<<<nblk(m.T), kBlock, 0, s>>>(m, vrec, td);
 }
 
 void fast_weights(const DevMesh& m, float* w, double* w64, ExpandList xl, int* n_refit, unsigned char* listed,
@@ -683,16 +695,16 @@ void fast_weights(const DevMesh& m, float* w, double* w64, ExpandList xl, int* n
   if (m.V) k_fast_weights<<<nblk(m.V), kBlock, 0, s>>>(m, w, w64, xl, n_refit, listed);
 }
 
-void fast_recover(const DevMesh& m, const float* w, const unsigned char* listed, const uint4* td, float4* rec,
+void fast_recover(const DevMesh& m, const float* w, const unsigned char* listed, const uint4* td, uint4* rec,
                   cudaStream_t s) {
   if (m.V) k_fast_recover<<<nblk((long)m.V * kGroup), kBlock, 0, s>>>(m, w, listed, td, rec);
 }
 
-void fast_merge_ref(ExpandList xl, const double* rec64, float4* rec, cudaStream_t s) {
+void fast_merge_ref(ExpandList xl, const double* rec64, uint4* rec, cudaStream_t s) {
   k_merge_ref<<<152, 256, 0, s>>>(xl.items, xl.count, xl.cap, rec64, rec);
 }
 
-void fast_error(const DevMesh& m, const uint4* td, const float2* geo, const float4* rec, float2* q, double* partials,
+void fast_error(const DevMesh& m, const uint4* td, const float2* geo, const uint4* rec, float2* q, double* partials,
                 int nb, cudaStream_t s) {
   if (nb) k_fast_error<<<nb, kBlock, 0, s>>>(m, td, geo, rec, q, partials);
 }
