@@ -20,6 +20,10 @@ ERROR_NAMES = {1: "EINVAL", 2: "EPATCH", 3: "EFLAGS", 4: "ENOMEM", 5: "ECUDA", 6
 
 SPRG_FP64 = 0
 SPRG_FP32 = 1
+SPRG_LEARNED = 2
+MLP_PARAMS = 12611
+MLP_INPUTS = 128
+MLP_AUX = 5
 
 SPLIT = 1 << 0
 DONT_SPLIT = 1 << 1
@@ -39,6 +43,8 @@ EXPORTS = [
     "sprg_estimate_and_mark_resident", "sprg_apply_marks", "sprg_last_launch_count",
     "sprg_box_counts", "sprg_box_fill", "sprg_profile_enable", "sprg_profile_flush", "sprg_profile_report",
     "sprg_spr_size_from_recovered_noalloc", "sprg_debug_read",
+    "sprg_set_mlp_params", "sprg_set_learned_options", "sprg_learned_features", "sprg_mlp_scratch_bytes",
+    "sprg_mlp_forward", "sprg_mlp_grad", "sprg_mlp_adam",
 ]
 NOALLOC_MAX_ELEMS = 1 << 20
 
@@ -72,6 +78,7 @@ class SizeInfo(ctypes.Structure):
         ("n_fp64_refits", ctypes.c_int64),
         ("n_guard_edges", ctypes.c_int64),
         ("n_guard_unresolved", ctypes.c_int64),
+        ("n_learned_fallback", ctypes.c_int64),
     ]
 
     def as_dict(self):
@@ -113,6 +120,15 @@ def load():
     lib.sprg_estimate_and_mark_resident.argtypes = [P, P, D, P, P]
     lib.sprg_apply_marks.argtypes = [ctypes.c_int64, P, P, P, ctypes.POINTER(ctypes.c_long),
                                      ctypes.POINTER(ctypes.c_long)]
+    F = ctypes.c_float
+    lib.sprg_set_mlp_params.argtypes = [P, P, I]
+    lib.sprg_set_learned_options.argtypes = [P, I, D]
+    lib.sprg_learned_features.argtypes = [P, P, P, P]
+    lib.sprg_mlp_scratch_bytes.argtypes = [I]
+    lib.sprg_mlp_scratch_bytes.restype = ctypes.c_size_t
+    lib.sprg_mlp_forward.argtypes = [P, P, I, P, P, P]
+    lib.sprg_mlp_grad.argtypes = [P, P, P, I, P, P, P, P]
+    lib.sprg_mlp_adam.argtypes = [P, P, P, P, F, F, F, F, I, P]
     lib.sprg_profile_enable.argtypes = [P, I]
     lib.sprg_profile_flush.argtypes = [P]
     lib.sprg_profile_report.argtypes = [P, I]

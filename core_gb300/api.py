@@ -57,9 +57,29 @@ class Context:
         check(rc, self.h)
 
     def set_precision(self, precision):
-        code = {"fp64": _lib.SPRG_FP64, "fp32": _lib.SPRG_FP32}[precision]
+        code = {"fp64": _lib.SPRG_FP64, "fp32": _lib.SPRG_FP32, "learned": _lib.SPRG_LEARNED}[precision]
         self._check(self._lib.sprg_set_precision(self.h, code))
         self.precision = precision
+        if precision == "learned" and not getattr(self, "_mlp_set", False):
+            from . import learned
+            self.set_mlp_params(learned.default_params())
+
+    # ---- learned form ----------------------------------------------------
+    def set_mlp_params(self, params):
+        """FP32 parameter vector (W1, b1, W2, b2, W3, b3; see learned.py)."""
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        if p.size != _lib.MLP_PARAMS:
+            raise ValueError(f"expected {_lib.MLP_PARAMS} parameters, got {p.size}")
+        self._check(self._lib.sprg_set_mlp_params(self.h, p.ctypes.data, p.size))
+        self._mlp_set = True
+
+    def set_learned_options(self, use_mlp=True, z_max=8.0):
+        self._check(self._lib.sprg_set_learned_options(self.h, 1 if use_mlp else 0, float(z_max)))
+
+    def learned_features(self, d_u, d_x, d_aux):
+        """Network inputs for a device field (V doubles): d_x [V][128] BF16,
+        d_aux [V][5] FP32 (device pointers)."""
+        self._check(self._lib.sprg_learned_features(self.h, d_u, d_x, d_aux))
 
     def set_stream(self, stream_handle):
         self._check(self._lib.sprg_set_stream(self.h, ctypes.c_void_p(stream_handle)))

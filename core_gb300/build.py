@@ -25,6 +25,7 @@ UNITS = {
     "sprg_kernels_f32.cu": [],
     "sprg_capi.cu": [],
     "sprg_noalloc.cu": [],
+    "sprg_learned.cu": [],
     "sprg_box.cpp": ["-x", "cu"],
 }
 

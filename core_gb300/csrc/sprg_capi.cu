@@ -11,6 +11,7 @@
 
 #include "spr_gb300.h"
 #include "sprg_fast.h"
+#include "sprg_learned.h"
 #include "sprg_internal.h"
 
 using namespace sprg;
@@ -45,6 +46,11 @@ struct sprg_ctx {
   // FP32 path buffers
   DevBuf crec, vrec, rec32, q32, sz2, fcnt, guard, tetd, wts, w64, listed, geo, geo64, elen, fitems;
   DevBuf gstamp, gfit, grec, tstamp, tslot, trec, tcount;  // guard pipeline scratch
+  // learned form
+  DevBuf vvoff, vv, vtile, vr16, rec16, ql, sizel, fbitems, fbcount, mlp_packed, mlp_err, mlp_tmp;
+  bool vv_ready = false, have_mlp = false;
+  int use_mlp = 1;
+  float z_max = 8.f;
   // side stream for the FP64 fits of listed patches, forked from and joined
   // back into the pass's stream
   cudaStream_t side = nullptr;
@@ -284,6 +290,16 @@ int fill_info(sprg_ctx* c, sprg_size_info* info) {
   c->last_info.n_fp64_refits = 0;
   c->last_info.n_guard_edges = 0;
   c->last_info.n_guard_unresolved = 0;
+  c->last_info.n_learned_fallback = 0;
+  if (c->precision == SPRG_LEARNED && c->fbcount.p) {
+    int fb = 0, me = 0;
+    CK(cudaMemcpy(&fb, c->fbcount.p, sizeof fb, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&me, c->mlp_err.p, sizeof me, cudaMemcpyDeviceToHost));
+    if (me) return fail(c, SPRG_ECUDA, "learned form: a tensor-core wait ran out of time");
+    c->last_info.n_learned_fallback = fb;
+    c->last_info.n_fp64_refits = c->n_refit;
+    c->last_info.n_expanded = c->n_listed - c->n_refit;
+  }
   if (c->precision == SPRG_FP32 && c->fcnt.p) {
     int fc[6] = {0, 0, 0, 0, 0, 0};
     CK(cudaMemcpy(fc, c->fcnt.p, sizeof fc, cudaMemcpyDeviceToHost));
@@ -414,7 +430,8 @@ int sprg_destroy(sprg_ctx* c) {
                     &c->out3,  &c->status,  &c->count, &c->xitems, &c->xcount, &c->slab, &c->bits,
                     &c->crec,  &c->vrec,    &c->rec32, &c->q32, &c->sz2,  &c->fcnt,   &c->guard, &c->tetd,
                     &c->wts,   &c->w64,     &c->listed, &c->geo, &c->geo64, &c->elen, &c->fitems, &c->gstamp, &c->gfit, &c->grec,
-                    &c->tstamp, &c->tslot,  &c->trec, &c->tcount,
+                    &c->tstamp, &c->tslot,  &c->trec, &c->tcount, &c->vvoff, &c->vv, &c->vtile, &c->vr16, &c->rec16,
+                    &c->ql,    &c->sizel,   &c->fbitems, &c->fbcount, &c->mlp_packed, &c->mlp_err, &c->mlp_tmp,
                     &c->cache64.v, &c->cache64.n, &c->cache64.el, &c->cache32.v, &c->cache32.n, &c->cache32.el};
   for (DevBuf* b : bufs) release(*b);
   for (auto& e : c->ev_pool) cudaEventDestroy(e);
@@ -433,9 +450,10 @@ const char* sprg_last_error(const sprg_ctx* c) { return c ? c->err_msg.c_str() :
 
 int sprg_set_precision(sprg_ctx* c, int precision) {
   if (!c) return SPRG_EINVAL;
-  if (precision != SPRG_FP64 && precision != SPRG_FP32) return fail(c, SPRG_EINVAL, "unknown precision");
-  if (precision == SPRG_FP32 && c->m.dim != 3)
-    return fail(c, SPRG_EINVAL, "the FP32 path covers tet meshes; use SPRG_FP64 for triangles");
+  if (precision != SPRG_FP64 && precision != SPRG_FP32 && precision != SPRG_LEARNED)
+    return fail(c, SPRG_EINVAL, "unknown precision");
+  if (precision != SPRG_FP64 && c->m.dim != 3)
+    return fail(c, SPRG_EINVAL, "the FP32 and learned forms cover tet meshes; use SPRG_FP64 for triangles");
   c->precision = precision;
   return SPRG_OK;
 }
@@ -635,6 +653,63 @@ int sprg_measure_quality(sprg_ctx* c, const double* size, const double* sizes, c
   return sync_and_status(c);
 }
 
+// per mesh (FP32 and learned forms): coordinate records, element and edge
+// geometry, SPR weights and the listed patches
+static int fast_setup(sprg_ctx* c, ExpandList xl) {
+  if (c->vrec_ready) return SPRG_OK;
+  DevMesh& m = c->m;
+  int rc;
+  const size_t nel = (size_t)m.T * m.nn;
+  ENSURE(c->crec, 32 * (size_t)m.V);
+  ENSURE(c->wts, sizeof(float) * nel);
+  ENSURE(c->w64, sizeof(double) * nel);
+  ENSURE(c->listed, (size_t)m.V);
+  ENSURE(c->geo, 8 * (size_t)m.T);
+  ENSURE(c->geo64, 16 * (size_t)m.T);
+  ENSURE(c->elen, 4 * (size_t)m.E);
+  CK(cudaMemsetAsync(c->fcnt.p, 0, 8 * sizeof(int), c->stream));
+  fast_prep_coords(m, P<float4>(c->crec), c->stream);
+  fast_geometry(m, P<float2>(c->geo), P<double2>(c->geo64), P<float>(c->elen), c->stream);
+  fast_weights(m, P<float>(c->wts), P<double>(c->w64), xl, P<int>(c->fcnt), P<unsigned char>(c->listed), c->stream);
+  int h[2] = {0, 0};
+  CK(cudaMemcpyAsync(&h[0], P<int>(c->fcnt) + 3, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaMemcpyAsync(&h[1], c->fcnt.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  if ((rc = check_launch(c, "fast setup"))) return rc;
+  c->n_listed = h[0] < m.V ? h[0] : m.V;
+  c->n_refit = h[1];
+  c->vrec_ready = true;
+  return SPRG_OK;
+}
+
+// the listed patches' FP64 fits: the first pass grows the patches (and
+// caches them) in order; later passes run the cached fits on the side
+// stream, joined by the caller before the results are used
+static int listed_fork(sprg_ctx* c, ExpandList xl, bool* forked) {
+  *forked = false;
+  if (!c->cache32.valid) return SPRG_OK;
+  if (!c->side) {
+    CK(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&c->join, cudaEventDisableTiming));
+  }
+  CK(cudaEventRecord(c->fork, c->stream));
+  CK(cudaStreamWaitEvent(c->side, c->fork, 0));
+  int rc = listed_fits(c, c->cache32, nullptr, P<double>(c->f), 3, P<double>(c->rec), xl, c->side);
+  if (rc) return rc;
+  CK(cudaEventRecord(c->join, c->side));
+  *forked = true;
+  return SPRG_OK;
+}
+
+static int listed_join(sprg_ctx* c, ExpandList xl, bool forked) {
+  if (forked) {
+    CK(cudaStreamWaitEvent(c->stream, c->join, 0));
+    return SPRG_OK;
+  }
+  return listed_fits(c, c->cache32, nullptr, P<double>(c->f), 3, P<double>(c->rec), xl);
+}
+
 // FP32 pass: packed double-float records, FP32 fits and sweeps, FP64
 // reference path for ill-conditioned or growing patches (sprg_kernels_f32.cu).
 static int pass_fast(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_t* d_collapse) {
@@ -642,7 +717,6 @@ static int pass_fast(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_
   int rc;
   int nb = fast_error_blocks(m.T);
   const size_t nel = (size_t)m.T * m.nn;
-  ENSURE(c->crec, 32 * (size_t)m.V);
   ENSURE(c->vrec, 32 * (size_t)m.V);
   ENSURE(c->rec32, 16 * (size_t)m.V);
   ENSURE(c->tetd, 16 * (size_t)m.T);
@@ -662,43 +736,11 @@ static int pass_fast(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_
   ExpandList xl{P<int>(c->fitems), P<int>(c->fcnt) + 3, m.V};
   float4* vrec = P<float4>(c->vrec);
   uint4* rec32 = P<uint4>(c->rec32);
-  if (!c->vrec_ready) {
-    // per mesh: coordinate records, element and edge geometry, SPR weights
-    // and the listed patches
-    ENSURE(c->wts, sizeof(float) * nel);
-    ENSURE(c->w64, sizeof(double) * nel);
-    ENSURE(c->listed, (size_t)m.V);
-    ENSURE(c->geo, 8 * (size_t)m.T);
-    ENSURE(c->geo64, 16 * (size_t)m.T);
-    ENSURE(c->elen, 4 * (size_t)m.E);
-    CK(cudaMemsetAsync(c->fcnt.p, 0, 8 * sizeof(int), c->stream));
-    fast_prep_coords(m, P<float4>(c->crec), c->stream);
-    fast_geometry(m, P<float2>(c->geo), P<double2>(c->geo64), P<float>(c->elen), c->stream);
-    fast_weights(m, P<float>(c->wts), P<double>(c->w64), xl, P<int>(c->fcnt), P<unsigned char>(c->listed),
-                 c->stream);
-    int h[2] = {0, 0};
-    CK(cudaMemcpyAsync(&h[0], P<int>(c->fcnt) + 3, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaMemcpyAsync(&h[1], c->fcnt.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaStreamSynchronize(c->stream));
-    if ((rc = check_launch(c, "fast setup"))) return rc;
-    c->n_listed = h[0] < m.V ? h[0] : m.V;
-    c->n_refit = h[1];
-    c->vrec_ready = true;
-  }
+  if ((rc = fast_setup(c, xl))) return rc;
   // the FP64 fits of the listed patches depend on the field only: once their
   // patches are cached they run on the side stream, beside the FP32 phases
-  const bool fork = c->cache32.valid;
-  if (fork) {
-    if (!c->side) {
-      CK(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
-      CK(cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming));
-      CK(cudaEventCreateWithFlags(&c->join, cudaEventDisableTiming));
-    }
-    CK(cudaEventRecord(c->fork, c->stream));
-    CK(cudaStreamWaitEvent(c->side, c->fork, 0));
-    if ((rc = listed_fits(c, c->cache32, nullptr, P<double>(c->f), 3, P<double>(c->rec), xl, c->side))) return rc;
-    CK(cudaEventRecord(c->join, c->side));
-  }
+  bool fork = false;
+  if ((rc = listed_fork(c, xl, &fork))) return rc;
   CK(cudaMemsetAsync(P<int>(c->fcnt) + 1, 0, sizeof(int), c->stream));
   CK(cudaMemsetAsync(P<int>(c->fcnt) + 4, 0, 2 * sizeof(int), c->stream));
   PB("prep_f32");
@@ -710,11 +752,7 @@ static int pass_fast(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_
   PB("recover_f32");
   fast_recover(m, P<float>(c->wts), P<unsigned char>(c->listed), P<uint4>(c->tetd), rec32, c->stream);
   PE();
-  if (fork) {
-    CK(cudaStreamWaitEvent(c->stream, c->join, 0));
-  } else if ((rc = listed_fits(c, c->cache32, nullptr, P<double>(c->f), 3, P<double>(c->rec), xl))) {
-    return rc;
-  }
+  if ((rc = listed_join(c, xl, fork))) return rc;
   PB("merge_f64");
   fast_merge_ref(xl, P<double>(c->rec), rec32, c->stream);
   PE();
@@ -763,9 +801,81 @@ static int pass_fast(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_
   return check_launch(c, "fast pass");
 }
 
+// Learned pass: network recovery with plain-SPR fallback, FP32 sweeps
+// (sprg_learned.cu).
+static int pass_learned(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_t* d_collapse) {
+  DevMesh& m = c->m;
+  int rc;
+  if (!c->have_mlp) return fail(c, SPRG_ESTATE, "learned form: no network parameters (sprg_set_mlp_params)");
+  const int nb = learned_error_blocks(m.T);
+  ENSURE(c->rec, 24 * (size_t)m.V);
+  ENSURE(c->fitems, sizeof(int) * (size_t)m.V);
+  ENSURE(c->xcount, sizeof(int));
+  ENSURE(c->slab, sizeof(double) * (size_t)expand_grid() * expand_max_elems() * (4 + 3 + 1));
+  ENSURE(c->fcnt, 8 * sizeof(int));
+  ENSURE(c->partials, sizeof(double) * 2 * (size_t)(nb > 0 ? nb : 1));
+  ENSURE(c->out3, sizeof(double) * 4);
+  ENSURE(c->vr16, 16 * (size_t)m.V);
+  ENSURE(c->rec16, 32 * (size_t)m.V);
+  ENSURE(c->ql, 4 * (size_t)m.T);
+  ENSURE(c->sizel, 4 * (size_t)m.V);
+  ENSURE(c->fbitems, sizeof(int) * (size_t)m.V);
+  ENSURE(c->fbcount, sizeof(int));
+  ENSURE(c->mlp_err, sizeof(int));
+  if ((rc = reset_status(c))) return rc;
+  ExpandList xl{P<int>(c->fitems), P<int>(c->fcnt) + 3, m.V};
+  if ((rc = fast_setup(c, xl))) return rc;
+  if (!c->vv_ready) {
+    ENSURE(c->vvoff, sizeof(int) * ((size_t)m.V + 1));
+    ENSURE(c->vv, sizeof(int) * 2 * (size_t)m.E);
+    ENSURE(c->tmp, sizeof(int) * (size_t)m.V);
+    ENSURE(c->vtile, ((size_t)m.V + 127) / 128);
+    learned_build_v2v(m, P<int>(c->vvoff), P<int>(c->vv), P<int>(c->tmp), P<unsigned char>(c->vtile), c->stream);
+    CK(cudaMemsetAsync(c->mlp_err.p, 0, sizeof(int), c->stream));
+    if ((rc = check_launch(c, "vertex adjacency"))) return rc;
+    c->vv_ready = true;
+  }
+  bool fork = false;
+  if ((rc = listed_fork(c, xl, &fork))) return rc;
+  LearnMesh lm{P<int>(c->vvoff), P<int>(c->vv), P<unsigned char>(c->listed), P<unsigned char>(c->vtile)};
+  float4* vr = P<float4>(c->vr16);
+  float4* rec = P<float4>(c->rec16);
+  CK(cudaMemsetAsync(c->fbcount.p, 0, sizeof(int), c->stream));
+  PB("prep_l");
+  learned_prep(m, P<double>(c->f), vr, c->stream);
+  PE();
+  PB("mlp_l");
+  learned_infer(m, lm, vr, P<double>(c->f), c->mlp_packed.p, rec, P<int>(c->fbitems), P<int>(c->fbcount), c->z_max,
+                c->use_mlp,
+                P<int>(c->mlp_err), c->stream);
+  PE();
+  if ((rc = listed_join(c, xl, fork))) return rc;
+  PB("fallback_l");
+  learned_fallback(m, lm, vr, P<double>(c->f), P<float>(c->wts), P<double>(c->rec), P<int>(c->fbitems),
+                   P<int>(c->fbcount), m.V, rec, c->stream);
+  PE();
+  PB("error_l");
+  learned_error(m, rec, P<float2>(c->geo), P<float>(c->ql), P<double>(c->partials), nb, c->stream);
+  PE();
+  PB("size_factor");
+  launch_size_factor(P<double>(c->partials), nb, 0, adapt_ratio, 0, m.dim, P<double>(c->out3), c->stream);
+  PE();
+  PB("average_l");
+  learned_average(m, P<float>(c->ql), P<double>(c->out3), P<float>(c->sizel), c->stream);
+  PE();
+  PB("measure_l");
+  learned_measure(m, P<float>(c->elen), P<float>(c->sizel), d_split, d_collapse, c->stream);
+  PE();
+  c->launches += 7;  // prep, network, fallback, error, size factor, average, measure
+  c->size_valid = false;
+  c->L_valid = false;
+  return check_launch(c, "learned pass");
+}
+
 static int pass_resident(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_t* d_collapse) {
   int rc;
   if (c->precision == SPRG_FP32) return pass_fast(c, adapt_ratio, d_split, d_collapse);
+  if (c->precision == SPRG_LEARNED) return pass_learned(c, adapt_ratio, d_split, d_collapse);
   if ((rc = reset_status(c)) || (rc = step_grad(c, 1)) || (rc = step_recover(c)) ||
       (rc = step_size(c, 0, adapt_ratio, 0, 0, 0)) || (rc = step_measure_iso(c)))
     return rc;
@@ -817,6 +927,11 @@ int sprg_estimate_and_mark(sprg_ctx* c, const double* u, double adapt_ratio, dou
     fast_size_to_f64(m.V, P<float2>(c->sz2), P<double>(c->size), c->stream);
     c->launches += 1;
     c->size_valid = true;
+  } else if (c->precision == SPRG_LEARNED) {
+    ENSURE(c->size, sizeof(double) * (size_t)m.V);
+    learned_size_to_f64(m.V, P<float>(c->sizel), P<double>(c->size), c->stream);
+    c->launches += 1;
+    c->size_valid = true;
   }
   if (size_out)
     CK(cudaMemcpyAsync(size_out, c->size.p, sizeof(double) * (size_t)m.V, cudaMemcpyDeviceToHost, c->stream));
@@ -837,7 +952,9 @@ int sprg_debug_read(sprg_ctx* c, const char* name, void* host, size_t bytes) {
       {"size", &c->size},   {"L", &c->L},         {"vrec", &c->vrec},     {"rec32", &c->rec32},
       {"q32", &c->q32},     {"sz2", &c->sz2},     {"tetd", &c->tetd},     {"out3", &c->out3},
       {"fcnt", &c->fcnt},   {"guard", &c->guard}, {"xitems", &c->xitems}, {"xcount", &c->xcount},
-      {"wts", &c->wts},     {"geo", &c->geo},     {"elen", &c->elen}};
+      {"wts", &c->wts},     {"geo", &c->geo},     {"elen", &c->elen},     {"rec16", &c->rec16},
+      {"sizel", &c->sizel}, {"ql", &c->ql},       {"vr16", &c->vr16},     {"fbitems", &c->fbitems},
+      {"fbcount", &c->fbcount}, {"listed", &c->listed}};
   for (auto& e : table) {
     if (strcmp(e.n, name) != 0) continue;
     if (!e.b->p) return fail(c, SPRG_ESTATE, std::string("buffer not allocated: ") + name);
@@ -924,6 +1041,79 @@ int sprg_apply_marks(int64_t n_edges, const uint32_t* split_bits, const uint32_t
   if (n_collapse) *n_collapse = counts[0];
   if (n_split) *n_split = counts[1];
   return SPRG_OK;
+}
+
+int sprg_set_mlp_params(sprg_ctx* c, const float* params, int n_params) {
+  if (!c || !params || n_params != kMlpParams) return SPRG_EINVAL;
+  int rc = set_device(c);
+  if (rc) return rc;
+  ENSURE(c->mlp_tmp, sizeof(float) * kMlpParams);
+  ENSURE(c->mlp_packed, kMlpPackedBytes);
+  CK(cudaMemcpyAsync(c->mlp_tmp.p, params, sizeof(float) * kMlpParams, cudaMemcpyHostToDevice, c->stream));
+  learned_pack(P<float>(c->mlp_tmp), c->mlp_packed.p, c->stream);
+  CK(cudaStreamSynchronize(c->stream));
+  if ((rc = check_launch(c, "pack network parameters"))) return rc;
+  c->have_mlp = true;
+  return SPRG_OK;
+}
+
+int sprg_set_learned_options(sprg_ctx* c, int use_mlp, double z_max) {
+  if (!c || !(z_max > 0)) return SPRG_EINVAL;
+  c->use_mlp = use_mlp ? 1 : 0;
+  c->z_max = (float)z_max;
+  return SPRG_OK;
+}
+
+int sprg_learned_features(sprg_ctx* c, const double* d_u, uint16_t* d_x, float* d_aux) {
+  if (!c || !d_u || !d_x || !d_aux) return SPRG_EINVAL;
+  if (c->m.dim != 3) return fail(c, SPRG_EINVAL, "the learned form covers tet meshes");
+  int rc = set_device(c);
+  if (rc) return rc;
+  DevMesh& m = c->m;
+  ENSURE(c->fitems, sizeof(int) * (size_t)m.V);
+  ENSURE(c->fcnt, 8 * sizeof(int));
+  ENSURE(c->vr16, 16 * (size_t)m.V);
+  ExpandList xl{P<int>(c->fitems), P<int>(c->fcnt) + 3, m.V};
+  if ((rc = fast_setup(c, xl))) return rc;
+  if (!c->vv_ready) {
+    ENSURE(c->vvoff, sizeof(int) * ((size_t)m.V + 1));
+    ENSURE(c->vv, sizeof(int) * 2 * (size_t)m.E);
+    ENSURE(c->tmp, sizeof(int) * (size_t)m.V);
+    ENSURE(c->mlp_err, sizeof(int));
+    ENSURE(c->vtile, ((size_t)m.V + 127) / 128);
+    learned_build_v2v(m, P<int>(c->vvoff), P<int>(c->vv), P<int>(c->tmp), P<unsigned char>(c->vtile), c->stream);
+    CK(cudaMemsetAsync(c->mlp_err.p, 0, sizeof(int), c->stream));
+    c->vv_ready = true;
+  }
+  LearnMesh lm{P<int>(c->vvoff), P<int>(c->vv), P<unsigned char>(c->listed), P<unsigned char>(c->vtile)};
+  learned_prep(m, d_u, P<float4>(c->vr16), c->stream);
+  learned_features(m, lm, P<float4>(c->vr16), d_x, d_aux, c->stream);
+  CK(cudaStreamSynchronize(c->stream));
+  return check_launch(c, "learned features");
+}
+
+size_t sprg_mlp_scratch_bytes(int n) { return n > 0 ? mlp_scratch_bytes(n) : 0; }
+
+int sprg_mlp_forward(const float* d_params, const uint16_t* d_x, int n, float* d_out, void* d_scratch, void* stream) {
+  if (!d_params || !d_x || !d_out || n <= 0 || !d_scratch) return SPRG_EINVAL;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  mlp_run(0, d_params, d_x, nullptr, n, d_out, nullptr, nullptr, d_scratch, s);
+  return cudaGetLastError() == cudaSuccess ? SPRG_OK : SPRG_ECUDA;
+}
+
+int sprg_mlp_grad(const float* d_params, const uint16_t* d_x, const float* d_y, int n, float* d_grad, float* d_loss,
+                  void* d_scratch, void* stream) {
+  if (!d_params || !d_x || !d_y || !d_grad || n <= 0 || !d_scratch) return SPRG_EINVAL;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  mlp_run(1, d_params, d_x, d_y, n, nullptr, d_grad, d_loss, d_scratch, s);
+  return cudaGetLastError() == cudaSuccess ? SPRG_OK : SPRG_ECUDA;
+}
+
+int sprg_mlp_adam(float* d_params, float* d_m1, float* d_m2, const float* d_grad, float lr, float beta1, float beta2,
+                  float eps, int step, void* stream) {
+  if (!d_params || !d_m1 || !d_m2 || !d_grad || step < 1) return SPRG_EINVAL;
+  mlp_adam(d_params, d_m1, d_m2, d_grad, lr, beta1, beta2, eps, step, static_cast<cudaStream_t>(stream));
+  return cudaGetLastError() == cudaSuccess ? SPRG_OK : SPRG_ECUDA;
 }
 
 }  // extern "C"

@@ -1,0 +1,1149 @@
+// Learned form of the estimate-and-mark pass (3D tets, scalar field).
+//
+// Per vertex v with neighbour vertices j (edge CSR, ascending ids, <= 32):
+//   d_j = x_j - x_v,  r_v = max |d_j|
+//   g_c = argmin_g sum_j (u_j - u_v - g . d_j)^2          (cheap gradient)
+//   rho_j = u_j - u_v - g_c . d_j,  s_v = rms_j(rho_j)
+//   features (slot j): (d_j / r_v, rho_j / s_v), zero in empty slots
+//   eps*(v) = g_c + z * s_v / r_v,  z = MLP(features)
+// SPR is linear in u and reproduces linear fields exactly, as g_c does, so
+// eps* - g_c is a linear function of rho for a given patch geometry; the
+// normalisation makes the prediction homogeneous of degree one in rho and
+// invariant to translating and scaling the patch.  The network is
+// 128 -> 64 -> 64 -> 3 with GELU (erf form), BF16 weights and activations and
+// FP32 accumulation, evaluated on the tensor cores (tcgen05.mma, accumulators
+// in tensor memory, operands in shared memory).  Plain SPR is the fallback:
+// vertices with fewer than 4 or more than 32 neighbours, listed patches (FP64
+// reference path), a degenerate least-squares system, or a network output
+// beyond the trained range (|z| > z_max, the residual guard).
+//
+// The sweeps around it run in plain FP32 (the learned form is stated to 1e-2
+// in size): element gradients are recomputed from the 16-byte vertex records
+// where they are needed, and no per-element gradient array is stored.
+#include <cuda_bf16.h>
+#include <cub/cub.cuh>
+
+#include "sprg_learned.h"
+
+namespace sprg {
+namespace {
+
+constexpr int kBlock = 256;
+inline int nblk(long n, int b = kBlock) { return (int)((n + b - 1) / b); }
+
+// ---------------------------------------------------------------------------
+// vertex -> vertex CSR (once per mesh)
+// ---------------------------------------------------------------------------
+__global__ void k_v2v_count(int E, const int* __restrict__ edv, int* __restrict__ cnt) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= E) return;
+  atomicAdd(&cnt[edv[2 * (size_t)e]], 1);
+  atomicAdd(&cnt[edv[2 * (size_t)e + 1]], 1);
+}
+
+__global__ void k_v2v_fill(int E, const int* __restrict__ edv, const int* __restrict__ off, int* __restrict__ cur,
+                           int* __restrict__ nb) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= E) return;
+  const int a = edv[2 * (size_t)e], b = edv[2 * (size_t)e + 1];
+  nb[off[a] + atomicAdd(&cur[a], 1)] = b;
+  nb[off[b] + atomicAdd(&cur[b], 1)] = a;
+}
+
+// per 128-vertex tile: 1 when every vertex has at most 16 neighbours
+__global__ void k_tile_half(int V, const int* __restrict__ off, unsigned char* __restrict__ half) {
+  const int tile = blockIdx.x;
+  const int v = tile * 128 + threadIdx.x;
+  const int cnt = v < V ? off[v + 1] - off[v] : 0;
+  const int any = __syncthreads_or(cnt > kMlpSlots / 2);
+  if (threadIdx.x == 0) half[tile] = any ? 0 : 1;
+}
+
+__global__ void k_v2v_sort(int V, const int* __restrict__ off, int* __restrict__ nb) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= V) return;
+  const int b = off[v], e = off[v + 1];
+  for (int i = b + 1; i < e; ++i) {
+    int x = nb[i], j = i - 1;
+    while (j >= b && nb[j] > x) {
+      nb[j + 1] = nb[j];
+      --j;
+    }
+    nb[j + 1] = x;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// vertex records {x, y, z, u} in FP32; u truncated to 24 bits by integer
+// operations (an FP64 conversion would run on the FP64 pipe)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float trunc_f32(double w) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(w);
+  const int e = (int)((b >> 52) & 0x7ff);
+  if (e >= 897 && e <= 1150)
+    return __uint_as_float(((unsigned)(b >> 63) << 31) | ((unsigned)(e - 896) << 23) |
+                           (unsigned)((b >> 29) & 0x7fffffu));
+  return (float)w;
+}
+
+// the remainder u - trunc_f32(u) rounded to FP32 (integer operations)
+__device__ __forceinline__ float trunc_lo(double w) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(w);
+  const int e = (int)((b >> 52) & 0x7ff);
+  if (e >= 949 && e <= 1150) {
+    const float lo = (float)(unsigned)(b & 0x1fffffffu) * __uint_as_float((unsigned)(e - 948) << 23);
+    return (b >> 63) ? -lo : lo;
+  }
+  return e < 949 ? (float)(w - (double)trunc_f32(w)) : 0.f;
+}
+
+__global__ void __launch_bounds__(kBlock) k_lprep(int V, const double* __restrict__ u, const float4* __restrict__ xyz32,
+                                                  float4* __restrict__ vr) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= V) return;
+  float4 p = __ldg(xyz32 + v);
+  p.w = trunc_f32(__ldg(u + v));
+  vr[v] = p;
+}
+
+// ---------------------------------------------------------------------------
+// features: four consecutive lanes per vertex (q = lane & 3 takes slots
+// q, q + 4, ...); every lane of the warp calls
+// ---------------------------------------------------------------------------
+// neighbour centroid offset (in units of r_v) above which a patch counts as
+// one-sided and takes plain SPR: the network is trained on, and answers,
+// interior patches only
+constexpr float kOneSided = 0.3f;
+
+template <int NS>
+struct VFeat {
+  float4 f[NS];
+  float gc[3];
+  float scl;
+  int flag;
+};
+
+__device__ __forceinline__ float quad_sum(float x) {
+  x += __shfl_xor_sync(0xffffffffu, x, 1);
+  return x + __shfl_xor_sync(0xffffffffu, x, 2);
+}
+
+// NS slots per lane: 8 covers 32 neighbours, 4 covers 16 (vertices with more
+// take the fallback: their slot count n is 0)
+template <int NS>
+__device__ __forceinline__ VFeat<NS> vertex_features(const LearnMesh& lm, const float4* __restrict__ vr, int V, int v,
+                                                     int q) {
+  VFeat<NS> o;
+  const bool valid = v < V;
+  int b = 0, cnt = 0;
+  float4 xv = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (valid) {
+    b = lm.vv_off[v];
+    cnt = lm.vv_off[v + 1] - b;
+    xv = __ldg(vr + v);
+  }
+  bool flag = !valid || cnt < 4 || cnt > 4 * NS || (valid && lm.listed[v]);
+  const int n = cnt <= 4 * NS ? cnt : 0;
+  int id[NS];
+#pragma unroll
+  for (int i = 0; i < NS; ++i) {
+    const int j = q + 4 * i;
+    id[i] = j < n ? __ldg(lm.vv + b + j) : -1;
+  }
+  float dx[NS], dy[NS], dz[NS], du[NS];
+#pragma unroll
+  for (int i = 0; i < NS; ++i) {
+    const float4 p = id[i] >= 0 ? __ldg(vr + id[i]) : xv;
+    dx[i] = p.x - xv.x;
+    dy[i] = p.y - xv.y;
+    dz[i] = p.z - xv.z;
+    du[i] = p.w - xv.w;
+  }
+  float a00 = 0.f, a01 = 0.f, a02 = 0.f, a11 = 0.f, a12 = 0.f, a22 = 0.f, b0 = 0.f, b1 = 0.f, b2 = 0.f, r2 = 0.f;
+  float mx = 0.f, my = 0.f, mz = 0.f;
+#pragma unroll
+  for (int i = 0; i < NS; ++i) {
+    mx += dx[i];
+    my += dy[i];
+    mz += dz[i];
+    a00 = fmaf(dx[i], dx[i], a00);
+    a01 = fmaf(dx[i], dy[i], a01);
+    a02 = fmaf(dx[i], dz[i], a02);
+    a11 = fmaf(dy[i], dy[i], a11);
+    a12 = fmaf(dy[i], dz[i], a12);
+    a22 = fmaf(dz[i], dz[i], a22);
+    b0 = fmaf(dx[i], du[i], b0);
+    b1 = fmaf(dy[i], du[i], b1);
+    b2 = fmaf(dz[i], du[i], b2);
+    r2 = fmaxf(r2, dx[i] * dx[i] + dy[i] * dy[i] + dz[i] * dz[i]);
+  }
+  a00 = quad_sum(a00); a01 = quad_sum(a01); a02 = quad_sum(a02);
+  a11 = quad_sum(a11); a12 = quad_sum(a12); a22 = quad_sum(a22);
+  b0 = quad_sum(b0); b1 = quad_sum(b1); b2 = quad_sum(b2);
+  mx = quad_sum(mx); my = quad_sum(my); mz = quad_sum(mz);
+  r2 = fmaxf(r2, __shfl_xor_sync(0xffffffffu, r2, 1));
+  r2 = fmaxf(r2, __shfl_xor_sync(0xffffffffu, r2, 2));
+  // hardware reciprocal square roots and divides: the features are rounded
+  // to BF16
+  const float ir = r2 > 0.f ? rsqrtf(r2) : 0.f, ir2 = ir * ir;
+  // normalised normal equations (A / r^2) g' = b / r, g_c = g' / r
+  a00 *= ir2; a01 *= ir2; a02 *= ir2; a11 *= ir2; a12 *= ir2; a22 *= ir2;
+  b0 *= ir; b1 *= ir; b2 *= ir;
+  const float c00 = a11 * a22 - a12 * a12, c01 = a02 * a12 - a01 * a22, c02 = a01 * a12 - a02 * a11;
+  const float c11 = a00 * a22 - a02 * a02, c12 = a01 * a02 - a00 * a12, c22 = a00 * a11 - a01 * a01;
+  const float det = a00 * c00 + a01 * c01 + a02 * c02;
+  const float tr = a00 + a11 + a22;
+  if (!(det > 1e-6f * tr * tr * tr)) flag = true;
+  // one-sided patches (boundary vertices): neighbour centroid far from v
+  const float nn = (float)(n > 0 ? n : 1);
+  if ((mx * mx + my * my + mz * mz) * ir2 > kOneSided * kOneSided * nn * nn) flag = true;
+  const float idet = det > 0.f ? __fdividef(ir, det) : 0.f;
+  const float g0 = (c00 * b0 + c01 * b1 + c02 * b2) * idet;
+  const float g1 = (c01 * b0 + c11 * b1 + c12 * b2) * idet;
+  const float g2 = (c02 * b0 + c12 * b1 + c22 * b2) * idet;
+  float rho[NS], s2 = 0.f;
+#pragma unroll
+  for (int i = 0; i < NS; ++i) {
+    rho[i] = id[i] >= 0 ? du[i] - (g0 * dx[i] + g1 * dy[i] + g2 * dz[i]) : 0.f;
+    s2 = fmaf(rho[i], rho[i], s2);
+  }
+  s2 = quad_sum(s2) * __fdividef(1.f, (float)(n > 0 ? n : 1));
+  const float is = s2 > 0.f ? rsqrtf(s2) : 0.f;
+  const float s = s2 * is;
+#pragma unroll
+  for (int i = 0; i < NS; ++i)
+    o.f[i] = id[i] >= 0 ? make_float4(dx[i] * ir, dy[i] * ir, dz[i] * ir, rho[i] * is) : make_float4(0.f, 0.f, 0.f, 0.f);
+  o.gc[0] = g0;
+  o.gc[1] = g1;
+  o.gc[2] = g2;
+  o.scl = s * ir;
+  o.flag = flag ? 1 : 0;
+  return o;
+}
+
+__device__ __forceinline__ uint2 pack4_bf16(float4 a) {
+  __nv_bfloat162 lo = __floats2bfloat162_rn(a.x, a.y), hi = __floats2bfloat162_rn(a.z, a.w);
+  return make_uint2(*reinterpret_cast<uint32_t*>(&lo), *reinterpret_cast<uint32_t*>(&hi));
+}
+
+__global__ void __launch_bounds__(kBlock) k_lfeatures(int V, LearnMesh lm, const float4* __restrict__ vr,
+                                                      uint2* __restrict__ x, float* __restrict__ aux) {
+  const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int v = gid >> 2, q = gid & 3;
+  VFeat<8> f = vertex_features<8>(lm, vr, V, v, q);
+  if (v >= V) return;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) x[(size_t)v * kMlpSlots + q + 4 * i] = pack4_bf16(f.f[i]);
+  if (q == 0) {
+    float* a = aux + (size_t)v * kMlpAux;
+    a[0] = f.gc[0];
+    a[1] = f.gc[1];
+    a[2] = f.gc[2];
+    a[3] = f.scl;
+    a[4] = (float)f.flag;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// tensor-core inference (tcgen05)
+//
+// Operands are BF16 in shared memory in the K-major layout without swizzle:
+// 8-row x 16-byte core matrices, core matrix (row / 8, k / 8) at
+// ((row / 8) * (K / 8) + k / 8) * 128 bytes, so adjacent core matrices along
+// K are 128 bytes apart (leading byte offset) and adjacent 8-row groups
+// K * 16 bytes apart (stride byte offset).  One MMA covers K = 16.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int tile_off(int row, int k, int K) {
+  return (((row >> 3) * (K >> 3) + (k >> 3)) << 6) + ((row & 7) << 3) + (k & 7);
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// shared memory matrix descriptor: start address, leading / stride byte
+// offsets (16-byte units), descriptor version 1, no swizzle
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((saddr & 0x3ffffu) >> 4) | ((uint64_t)((lbo >> 4) & 0x3fffu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3fffu) << 32) | (1ull << 46);
+}
+
+// instruction descriptor, kind::f16: D FP32, A and B BF16, both K-major
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void tmem_alloc(uint32_t* dst, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst)), "r"(ncols)
+               : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish() {
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void mma_bf16(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc)
+      : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+// bounded wait on the barrier's phase; false when the limit ran out
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int max_iter) {
+  const uint32_t addr = smem_u32(bar);
+  for (int i = 0; i < max_iter; ++i) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(done)
+        : "r"(addr), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+// 32 lanes x 16 consecutive FP32 columns: thread i gets lane (base + i)
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
+                 "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]),
+                 "+r"(r[15])::"memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.f + erff(x * 0.70710678118654752f)); }
+
+// normal CDF for the inference epilogues, gelu(x) = x Phi(x): a table of
+// Phi(x_i) = (1 + erff(x_i / sqrt 2)) / 2 (computed by each block),
+// x_i = -6 + i / 128, stored as (Phi(x_i), Phi(x_i+1) - Phi(x_i)) and
+// interpolated linearly; clamping at the ends gives Phi = 0 or 1 there
+// (|error| < 1e-9).  |x Phi - gelu| < 1e-5 for |x| < 6 and < 6e-9 |x| beyond,
+// far below the BF16 rounding of the stored activation.
+constexpr int kGeluN = 12 * 128;
+__device__ __forceinline__ float gelu_tab(const float2* __restrict__ tab, float x) {
+  const float t = fminf(fmaxf(fmaf(x, 128.f, 768.f), 0.f), (float)kGeluN - 0.001f);
+  // floor by the 1.5 * 2^23 rounding constant (t - 0.5 rounded to an
+  // integer; a tie gives t itself, which interpolates to the same value)
+  const float r = (t - 0.5f) + 12582912.f;
+  const float2 y = tab[__float_as_int(r) - 0x4B400000];
+  return x * fmaf(t - (r - 12582912.f), y.y, y.x);
+}
+__device__ __forceinline__ float phi(float x) { return 0.5f * (1.f + erff(x * 0.70710678118654752f)); }
+
+// shared-memory layout of the inference kernel (bytes); the first
+// kMlpPackedBytes are the packed parameters, copied as one block
+constexpr int kSmW1 = 0;
+constexpr int kSmW2 = kSmW1 + 2 * kMlpHidden * kMlpIn;
+constexpr int kSmW3 = kSmW2 + 2 * kMlpHidden * kMlpHidden;
+constexpr int kSmBias = kSmW3 + 2 * 16 * kMlpHidden;  // b1 [64], b2 [64], b3 [16] FP32
+constexpr int kSmA1 = 27 * 1024;                       // 128 x 128 BF16
+constexpr int kSmA2 = kSmA1 + 2 * 128 * kMlpIn;       // 128 x 64 BF16
+constexpr int kSmAux = kSmA2 + 2 * 128 * kMlpHidden;  // g_c [128][3], scale [128], flag [128]
+constexpr int kSmBar = kSmAux + 128 * 5 * 4;
+constexpr int kSmGelu = kSmBar + 64;                   // kGeluN float2
+constexpr int kSmInfer = kSmGelu + 8 * kGeluN;
+static_assert(kSmBias + 4 * 144 == kMlpPackedBytes, "packed parameter layout");
+static_assert(kSmA1 >= kMlpPackedBytes, "operand tiles after the parameters");
+constexpr int kInferThreads = 512;
+constexpr int kTmemCols = 128;  // D1 / D2 in columns 0..63, D3 in 64..79
+
+// hidden layer epilogue: bias + GELU of a 128 x 64 accumulator into the next
+// layer's A operand; warp w reads lanes 32 (w % 4) .. + 31, columns
+// 16 (w / 4) .. + 15
+__device__ __forceinline__ void hidden_epilogue(uint32_t tbase, const float* __restrict__ bias,
+                                                const float2* __restrict__ tab, __nv_bfloat16* __restrict__ A,
+                                                int warp, int lane) {
+  const int lq = warp & 3, cg = warp >> 2;
+  float z[16];
+  tmem_ld16(tbase + ((uint32_t)(32 * lq) << 16) + 16 * cg, z);
+  const int row = 32 * lq + lane;
+  uint32_t h[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    __nv_bfloat162 p = __floats2bfloat162_rn(gelu_tab(tab, z[2 * i] + bias[16 * cg + 2 * i]),
+                                             gelu_tab(tab, z[2 * i + 1] + bias[16 * cg + 2 * i + 1]));
+    h[i] = *reinterpret_cast<uint32_t*>(&p);
+  }
+  *reinterpret_cast<uint4*>(A + tile_off(row, 16 * cg, kMlpHidden)) = make_uint4(h[0], h[1], h[2], h[3]);
+  *reinterpret_cast<uint4*>(A + tile_off(row, 16 * cg + 8, kMlpHidden)) = make_uint4(h[4], h[5], h[6], h[7]);
+}
+
+__device__ __forceinline__ int warp_slot(bool win, int* counter) {
+  const unsigned mask = __ballot_sync(0xffffffffu, win);
+  const int lane = threadIdx.x & 31;
+  int base = 0;
+  if (mask) {
+    const int leader = __ffs(mask) - 1;
+    if (lane == leader) base = atomicAdd(counter, __popc(mask));
+    base = __shfl_sync(0xffffffffu, base, leader);
+  }
+  return base + __popc(mask & ((1u << lane) - 1));
+}
+
+constexpr int kWaitLimit = 1 << 22;
+
+__global__ void __launch_bounds__(kInferThreads, 2)
+    k_mlp_infer(int V, LearnMesh lm, const float4* __restrict__ vr, const double* __restrict__ u,
+                const uint4* __restrict__ packed,
+                float4* __restrict__ rec16, int* __restrict__ fb_items, int* __restrict__ fb_count, float z_max,
+                int use_mlp, int* __restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const float* bias = reinterpret_cast<const float*>(sm + kSmBias);
+  __nv_bfloat16* A1 = reinterpret_cast<__nv_bfloat16*>(sm + kSmA1);
+  __nv_bfloat16* A2 = reinterpret_cast<__nv_bfloat16*>(sm + kSmA2);
+  float* gcs = reinterpret_cast<float*>(sm + kSmAux);
+  float* scls = gcs + 3 * 128;
+  int* flags = reinterpret_cast<int*>(scls + 128);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + kSmBar);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + kSmBar + 8);
+  float2* gtab = reinterpret_cast<float2*>(sm + kSmGelu);
+
+  for (int i = tid; i < kMlpPackedBytes / 16; i += blockDim.x) reinterpret_cast<uint4*>(sm)[i] = packed[i];
+  for (int i = tid; i < kGeluN; i += blockDim.x)
+    gtab[i] = make_float2(phi(-6.f + (float)i / 128.f), phi(-6.f + (float)(i + 1) / 128.f) - phi(-6.f + (float)i / 128.f));
+  if (warp == 0) {
+    tmem_alloc(tslot, kTmemCols);
+    tmem_relinquish();
+  }
+  if (tid == 0) mbar_init(bar, 1);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tbase = *tslot;
+  const uint32_t sA1 = smem_u32(A1), sA2 = smem_u32(A2), sW1 = smem_u32(sm + kSmW1), sW2 = smem_u32(sm + kSmW2),
+                 sW3 = smem_u32(sm + kSmW3);
+  constexpr uint32_t id64 = idesc_bf16(128, 64), id16 = idesc_bf16(128, 16);
+  uint32_t phase = 0;
+  bool ok = true;
+  const int ntiles = (V + 127) / 128;
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    // tiles whose vertices all have at most 16 neighbours (slots 16..31
+    // empty) multiply only the first 64 inputs: layer 1 with K = 64
+    const int half = lm.tile_half[tile];
+    // features, four lanes per vertex
+    {
+      const int r = tid >> 2, q = tid & 3;
+      if (half) {
+        VFeat<4> f = vertex_features<4>(lm, vr, V, tile * 128 + r, q);
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+          *reinterpret_cast<uint2*>(A1 + tile_off(r, 4 * (q + 4 * i), kMlpIn)) = pack4_bf16(f.f[i]);
+        if (q == 0) {
+          gcs[3 * r] = f.gc[0];
+          gcs[3 * r + 1] = f.gc[1];
+          gcs[3 * r + 2] = f.gc[2];
+          scls[r] = f.scl;
+          flags[r] = f.flag;
+        }
+      } else {
+        VFeat<8> f = vertex_features<8>(lm, vr, V, tile * 128 + r, q);
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+          *reinterpret_cast<uint2*>(A1 + tile_off(r, 4 * (q + 4 * i), kMlpIn)) = pack4_bf16(f.f[i]);
+        if (q == 0) {
+          gcs[3 * r] = f.gc[0];
+          gcs[3 * r + 1] = f.gc[1];
+          gcs[3 * r + 2] = f.gc[2];
+          scls[r] = f.scl;
+          flags[r] = f.flag;
+        }
+      }
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    // layer 1: D[0:64) = A1 W1^T
+    if (tid == 0) {
+      tc_fence_after();
+      const int nk = half ? kMlpIn / 32 : kMlpIn / 16;
+      for (int k = 0; k < nk; ++k)
+        mma_bf16(tbase, sdesc(sA1 + 256 * k, 128, 16 * kMlpIn), sdesc(sW1 + 256 * k, 128, 16 * kMlpIn), id64, k > 0);
+      mma_commit(bar);
+    }
+    ok = __syncthreads_and(tid == 0 ? mbar_wait(bar, phase, kWaitLimit) : true);
+    phase ^= 1;
+    if (!ok) break;
+    tc_fence_after();
+    hidden_epilogue(tbase, bias, gtab, A2, warp, lane);
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    // layer 2: D[0:64) = H1 W2^T
+    if (tid == 0) {
+      tc_fence_after();
+#pragma unroll
+      for (int k = 0; k < kMlpHidden / 16; ++k)
+        mma_bf16(tbase, sdesc(sA2 + 256 * k, 128, 16 * kMlpHidden), sdesc(sW2 + 256 * k, 128, 16 * kMlpHidden), id64,
+                 k > 0);
+      mma_commit(bar);
+    }
+    ok = __syncthreads_and(tid == 0 ? mbar_wait(bar, phase, kWaitLimit) : true);
+    phase ^= 1;
+    if (!ok) break;
+    tc_fence_after();
+    hidden_epilogue(tbase, bias + kMlpHidden, gtab, A2, warp, lane);
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    // layer 3: D[64:80) = H2 W3^T (rows 3..15 of W3 are zero)
+    if (tid == 0) {
+      tc_fence_after();
+#pragma unroll
+      for (int k = 0; k < kMlpHidden / 16; ++k)
+        mma_bf16(tbase + 64, sdesc(sA2 + 256 * k, 128, 16 * kMlpHidden), sdesc(sW3 + 256 * k, 128, 16 * kMlpHidden),
+                 id16, k > 0);
+      mma_commit(bar);
+    }
+    ok = __syncthreads_and(tid == 0 ? mbar_wait(bar, phase, kWaitLimit) : true);
+    phase ^= 1;
+    if (!ok) break;
+    tc_fence_after();
+    if (warp < 4) {
+      float z[16];
+      tmem_ld16(tbase + ((uint32_t)(32 * warp) << 16) + 64, z);
+      const int r = 32 * warp + lane, v = tile * 128 + r;
+      const float* b3 = bias + 2 * kMlpHidden;
+      float z0 = z[0] + b3[0], z1 = z[1] + b3[1], z2 = z[2] + b3[2];
+      const bool in = v < V;
+      const bool fb = in && (flags[r] || !(fabsf(z0) <= z_max && fabsf(z1) <= z_max && fabsf(z2) <= z_max));
+      if (!use_mlp) z0 = z1 = z2 = 0.f;
+      if (in && !fb) {
+        const float s = scls[r];
+        rec16[2 * (size_t)v] = __ldg(vr + v);
+        rec16[2 * (size_t)v + 1] = make_float4(fmaf(z0, s, gcs[3 * r]), fmaf(z1, s, gcs[3 * r + 1]),
+                                               fmaf(z2, s, gcs[3 * r + 2]), trunc_lo(__ldg(u + v)));
+      }
+      const int slot = warp_slot(fb, fb_count);
+      if (fb && slot < V) fb_items[slot] = v;
+    }
+    tc_fence_before();
+    __syncthreads();
+  }
+  if (!ok) {
+    // a wait ran out: let the MMAs in flight finish (bounded) before freeing
+    mbar_wait(bar, phase ^ 1, kWaitLimit);
+    if (tid == 0) atomicExch(err, 1);
+  }
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0) tmem_dealloc(tbase, kTmemCols);
+}
+
+// pack FP32 master parameters: W1 (64 x 128), W2 (64 x 64), W3 (16 x 64, rows
+// 3..15 zero) as BF16 K-major tiles, then b1, b2, b3 (padded to 16) in FP32
+__global__ void k_mlp_pack(const float* __restrict__ P, unsigned char* __restrict__ out) {
+  __nv_bfloat16* W1 = reinterpret_cast<__nv_bfloat16*>(out + kSmW1);
+  __nv_bfloat16* W2 = reinterpret_cast<__nv_bfloat16*>(out + kSmW2);
+  __nv_bfloat16* W3 = reinterpret_cast<__nv_bfloat16*>(out + kSmW3);
+  float* bias = reinterpret_cast<float*>(out + kSmBias);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < kMlpHidden * kMlpIn; i += gridDim.x * blockDim.x) {
+    const int n = i / kMlpIn, k = i % kMlpIn;
+    W1[tile_off(n, k, kMlpIn)] = __float2bfloat16_rn(P[kMlpW1 + i]);
+  }
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < kMlpHidden * kMlpHidden; i += gridDim.x * blockDim.x) {
+    const int n = i / kMlpHidden, k = i % kMlpHidden;
+    W2[tile_off(n, k, kMlpHidden)] = __float2bfloat16_rn(P[kMlpW2 + i]);
+  }
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 16 * kMlpHidden; i += gridDim.x * blockDim.x) {
+    const int n = i / kMlpHidden, k = i % kMlpHidden;
+    W3[tile_off(n, k, kMlpHidden)] = __float2bfloat16_rn(n < kMlpOut ? P[kMlpW3 + i] : 0.f);
+  }
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 144; i += gridDim.x * blockDim.x)
+    bias[i] = i < 64 ? P[kMlpB1 + i] : i < 128 ? P[kMlpB2 + i - 64] : (i - 128 < kMlpOut ? P[kMlpB3 + i - 128] : 0.f);
+}
+
+// ---------------------------------------------------------------------------
+// plain SPR fallback and the FP32 sweeps
+// ---------------------------------------------------------------------------
+// element gradient from the records: the field differences carry the low
+// words (hi_i - hi_0 is exact for nearby values), so they are good to
+// ~2^-48 of u instead of 2^-24
+__device__ __forceinline__ float3 tet_grad_rec(const float4& p0, const float4& p1, const float4& p2,
+                                              const float4& p3, float l0, float l1, float l2, float l3) {
+  const float e1x = p1.x - p0.x, e1y = p1.y - p0.y, e1z = p1.z - p0.z, d1 = (p1.w - p0.w) + (l1 - l0);
+  const float e2x = p2.x - p0.x, e2y = p2.y - p0.y, e2z = p2.z - p0.z, d2 = (p2.w - p0.w) + (l2 - l0);
+  const float e3x = p3.x - p0.x, e3y = p3.y - p0.y, e3z = p3.z - p0.z, d3 = (p3.w - p0.w) + (l3 - l0);
+  // cofactor rows c1 = e2 x e3, c2 = e3 x e1, c3 = e1 x e2
+  const float c1x = e2y * e3z - e2z * e3y, c1y = e2z * e3x - e2x * e3z, c1z = e2x * e3y - e2y * e3x;
+  const float c2x = e3y * e1z - e3z * e1y, c2y = e3z * e1x - e3x * e1z, c2z = e3x * e1y - e3y * e1x;
+  const float c3x = e1y * e2z - e1z * e2y, c3y = e1z * e2x - e1x * e2z, c3z = e1x * e2y - e1y * e2x;
+  const float inv = __fdividef(1.f, e1x * c1x + e1y * c1y + e1z * c1z);
+  return make_float3((c1x * d1 + c2x * d2 + c3x * d3) * inv, (c1y * d1 + c2y * d2 + c3y * d3) * inv,
+                     (c1z * d1 + c2z * d2 + c3z * d3) * inv);
+}
+
+// fallback: warp per vertex
+__global__ void k_lfallback(DevMesh m, LearnMesh lm, const float4* __restrict__ vr, const double* __restrict__ u,
+                            const float* __restrict__ w,
+                            const double* __restrict__ rec64, const int* __restrict__ items,
+                            const int* __restrict__ count, int cap, float4* __restrict__ rec16) {
+  const int n = min(*count, cap);
+  const int lane = threadIdx.x & 31;
+  const int nw = gridDim.x * (blockDim.x >> 5);
+  for (int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += nw) {
+    const int v = items[i];
+    if (lm.listed[v]) {
+      if (lane == 0) {
+        rec16[2 * (size_t)v] = __ldg(vr + v);
+        rec16[2 * (size_t)v + 1] = make_float4((float)rec64[3 * (size_t)v], (float)rec64[3 * (size_t)v + 1],
+                                               (float)rec64[3 * (size_t)v + 2], trunc_lo(u[v]));
+      }
+      continue;
+    }
+    const int beg = m.p_off[v], cnt = m.p_off[v + 1] - beg;
+    float x0 = 0.f, x1 = 0.f, x2 = 0.f;
+    for (int k = lane; k < cnt; k += 32) {
+      const int t = m.p_el[beg + k];
+      const int4 tv = __ldg(reinterpret_cast<const int4*>(m.ev) + t);
+      // field differences with the low words (as in the error kernel)
+      const float3 g = tet_grad_rec(__ldg(vr + tv.x), __ldg(vr + tv.y), __ldg(vr + tv.z), __ldg(vr + tv.w),
+                                    trunc_lo(u[tv.x]), trunc_lo(u[tv.y]), trunc_lo(u[tv.z]), trunc_lo(u[tv.w]));
+      const float wk = w[beg + k];
+      x0 = fmaf(wk, g.x, x0);
+      x1 = fmaf(wk, g.y, x1);
+      x2 = fmaf(wk, g.z, x2);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      x0 += __shfl_xor_sync(0xffffffffu, x0, o);
+      x1 += __shfl_xor_sync(0xffffffffu, x1, o);
+      x2 += __shfl_xor_sync(0xffffffffu, x2, o);
+    }
+    if (lane == 0) {
+      rec16[2 * (size_t)v] = __ldg(vr + v);
+      rec16[2 * (size_t)v + 1] = make_float4(x0, x1, x2, trunc_lo(u[v]));
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// error, average, measure in plain FP32
+// ---------------------------------------------------------------------------
+// two elements per iteration, all loads issued before use; w dV and h_max
+// are the per-mesh element geometry
+__global__ void __launch_bounds__(kBlock) k_lerror(DevMesh m, const float4* __restrict__ rec,
+                                                   const float2* __restrict__ geo, float* __restrict__ q,
+                                                   double* __restrict__ partials) {
+  __shared__ double sh[2][kBlock / 32];
+  float self = 0.f, gsum = 0.f;
+  const int stride = gridDim.x * blockDim.x;
+  for (int t0 = blockIdx.x * blockDim.x + threadIdx.x; t0 < m.T; t0 += 2 * stride) {
+    const int ts[2] = {t0, t0 + stride};
+    int4 tv[2];
+    float2 gm[2];
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+      const bool in = ts[i] < m.T;
+      tv[i] = in ? __ldg(reinterpret_cast<const int4*>(m.ev) + ts[i]) : make_int4(0, 0, 0, 0);
+      gm[i] = in ? __ldg(geo + ts[i]) : make_float2(0.f, 0.f);
+    }
+    // one 32-byte record per vertex: {x, y, z, u_hi}, {eps*, u_lo}
+    float4 P[2][4], E[2][4];
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+      const int vs[4] = {tv[i].x, tv[i].y, tv[i].z, tv[i].w};
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        P[i][k] = __ldg(rec + 2 * (size_t)vs[k]);
+        E[i][k] = __ldg(rec + 2 * (size_t)vs[k] + 1);
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+      if (ts[i] >= m.T) continue;
+      const float3 g =
+          tet_grad_rec(P[i][0], P[i][1], P[i][2], P[i][3], E[i][0].w, E[i][1].w, E[i][2].w, E[i][3].w);
+      const float ex = 0.25f * ((E[i][0].x + E[i][1].x) + (E[i][2].x + E[i][3].x));
+      const float ey = 0.25f * ((E[i][0].y + E[i][1].y) + (E[i][2].y + E[i][3].y));
+      const float ez = 0.25f * ((E[i][0].z + E[i][1].z) + (E[i][2].z + E[i][3].z));
+      const float dx = g.x - ex, dy = g.y - ey, dz = g.z - ez;
+      const float wdv = gm[i].x;
+      const float err = (dx * dx + dy * dy + dz * dz) * wdv;
+      self = fmaf(ex * ex + ey * ey + ez * ez, wdv, self);
+      // err^(-1/5) through the hardware log2 / exp2 (the learned form is
+      // stated to 1e-2; these are good to a few 1e-7)
+      const float rr = err > 0.f ? exp2f(-0.2f * __log2f(err)) : __int_as_float(0x7f800000);
+      gsum += err > 0.f ? err * (rr * rr) : 0.f;
+      q[ts[i]] = gm[i].y * rr;
+    }
+  }
+  double s1 = self, s2 = gsum;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+    s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+  }
+  const int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) {
+    sh[0][w] = s1;
+    sh[1][w] = s2;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0, b = 0;
+    for (int i = 0; i < kBlock / 32; ++i) {
+      a += sh[0][i];
+      b += sh[1][i];
+    }
+    partials[2 * blockIdx.x] = a;
+    partials[2 * blockIdx.x + 1] = b;
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k_laverage(DevMesh m, const float* __restrict__ q,
+                                                     const double* __restrict__ out3, float* __restrict__ size) {
+  const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int v = gid >> 2, gl = gid & 3;
+  int b = 0, e = 0;
+  if (v < m.V) {
+    b = m.a_off[v];
+    e = m.a_off[v + 1];
+  }
+  float x[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const int k = b + gl + 4 * j;
+    x[j] = k < e ? __ldg(q + __ldg(m.a_el + k)) : 0.f;
+  }
+  float s = 0.f;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) s += x[j];
+  for (int k = b + gl + 32; k < e; k += 4) s += __ldg(q + __ldg(m.a_el + k));
+  s += __shfl_xor_sync(0xffffffffu, s, 1);
+  s += __shfl_xor_sync(0xffffffffu, s, 2);
+  if (v < m.V && gl == 0) size[v] = (float)out3[2] * (s / (float)(e - b));
+}
+
+__global__ void __launch_bounds__(kBlock) k_lmeasure(DevMesh m, const float* __restrict__ half_len,
+                                                     const float* __restrict__ size, uint32_t* __restrict__ split,
+                                                     uint32_t* __restrict__ collapse) {
+  const int lane = threadIdx.x & 31;
+  const long warp = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5;
+  const int e0 = (int)(warp * 64) + lane;
+  const int eids[2] = {e0, e0 + 32};
+  int2 ab[2];
+  float hl[2], A[2], B[2];
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    const bool in = eids[i] < m.E;
+    ab[i] = in ? __ldg(reinterpret_cast<const int2*>(m.edv) + eids[i]) : make_int2(0, 0);
+    hl[i] = in ? __ldg(half_len + eids[i]) : 0.f;
+  }
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    A[i] = __ldg(size + ab[i].x);
+    B[i] = __ldg(size + ab[i].y);
+  }
+  const float gp = 0.577350269189626f;
+  const float n0 = 0.5f * (1.f - gp), n1 = 0.5f * (1.f + gp);
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    const int e = eids[i];
+    bool s = false, c = false;
+    if (e < m.E) {
+      const float L = hl[i] * (1.f / (n0 * A[i] + n1 * B[i]) + 1.f / (n1 * A[i] + n0 * B[i]));
+      s = L > 1.5f;
+      c = L < 0.5f;
+    }
+    const unsigned bs = __ballot_sync(0xffffffffu, s), bc = __ballot_sync(0xffffffffu, c);
+    if (lane == 0 && e < m.E) {
+      split[e >> 5] = bs;
+      collapse[e >> 5] = bc;
+    }
+  }
+}
+
+__global__ void k_lsize_f64(int V, const float* __restrict__ s32, double* __restrict__ s64) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v < V) s64[v] = (double)s32[v];
+}
+
+// ---------------------------------------------------------------------------
+// training: 64 samples per block, forward and backward in shared memory,
+// per-block gradient partials reduced in a fixed order
+// ---------------------------------------------------------------------------
+constexpr int kTB = 64;
+constexpr int kZP = kMlpHidden + 1;  // padded FP32 row
+constexpr int kTrOffW1 = 0;
+constexpr int kTrOffW2 = kTrOffW1 + 2 * kMlpHidden * kMlpIn;
+constexpr int kTrOffW3 = kTrOffW2 + 2 * kMlpHidden * kMlpHidden;
+constexpr int kTrOffB = kTrOffW3 + 2 * kMlpOut * kMlpHidden;
+constexpr int kTrOffX = kTrOffB + 4 * 160;
+constexpr int kTrOffZ1 = kTrOffX + 2 * kTB * kMlpIn;
+constexpr int kTrOffZ2 = kTrOffZ1 + 4 * kTB * kZP;
+constexpr int kTrOffH1 = kTrOffZ2 + 4 * kTB * kZP;
+constexpr int kTrOffH2 = kTrOffH1 + 2 * kTB * kMlpHidden;
+constexpr int kTrOffY = kTrOffH2 + 2 * kTB * kMlpHidden;
+constexpr int kTrOffL = kTrOffY + 4 * kTB * 4;
+constexpr int kTrSmem = kTrOffL + 4 * kTB * kMlpOut;
+
+__device__ __forceinline__ float gelu_grad(float x) {
+  return 0.5f * (1.f + erff(x * 0.70710678118654752f)) + x * 0.39894228040143268f * expf(-0.5f * x * x);
+}
+
+__global__ void __launch_bounds__(256) k_mlp_train(int mode, const float* __restrict__ P,
+                                                   const __nv_bfloat16* __restrict__ X, const float* __restrict__ Yt,
+                                                   int n, float* __restrict__ out, float* __restrict__ gpart,
+                                                   float* __restrict__ lpart) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  __nv_bfloat16* W1 = reinterpret_cast<__nv_bfloat16*>(sm + kTrOffW1);
+  __nv_bfloat16* W2 = reinterpret_cast<__nv_bfloat16*>(sm + kTrOffW2);
+  __nv_bfloat16* W3 = reinterpret_cast<__nv_bfloat16*>(sm + kTrOffW3);
+  float* b1 = reinterpret_cast<float*>(sm + kTrOffB);
+  float* b2 = b1 + kMlpHidden;
+  float* b3 = b2 + kMlpHidden;
+  __nv_bfloat16* Xs = reinterpret_cast<__nv_bfloat16*>(sm + kTrOffX);
+  float* Z1 = reinterpret_cast<float*>(sm + kTrOffZ1);
+  float* Z2 = reinterpret_cast<float*>(sm + kTrOffZ2);
+  __nv_bfloat16* H1 = reinterpret_cast<__nv_bfloat16*>(sm + kTrOffH1);
+  __nv_bfloat16* H2 = reinterpret_cast<__nv_bfloat16*>(sm + kTrOffH2);
+  float* Yo = reinterpret_cast<float*>(sm + kTrOffY);    // [64][4]: dY
+  float* Lsq = reinterpret_cast<float*>(sm + kTrOffL);   // [64 * 3]: squared errors
+  const int tid = threadIdx.x;
+  const int s0 = blockIdx.x * kTB;
+  for (int i = tid; i < kMlpHidden * kMlpIn; i += 256) W1[i] = __float2bfloat16_rn(P[kMlpW1 + i]);
+  for (int i = tid; i < kMlpHidden * kMlpHidden; i += 256) W2[i] = __float2bfloat16_rn(P[kMlpW2 + i]);
+  for (int i = tid; i < kMlpOut * kMlpHidden; i += 256) W3[i] = __float2bfloat16_rn(P[kMlpW3 + i]);
+  if (tid < kMlpHidden) {
+    b1[tid] = P[kMlpB1 + tid];
+    b2[tid] = P[kMlpB2 + tid];
+  }
+  if (tid < kMlpOut) b3[tid] = P[kMlpB3 + tid];
+  for (int i = tid; i < kTB * kMlpIn; i += 256) {
+    const int s = i / kMlpIn;
+    Xs[i] = s0 + s < n ? X[(size_t)s0 * kMlpIn + i] : __float2bfloat16_rn(0.f);
+  }
+  __syncthreads();
+  // thread tile: samples 4 sr .. 4 sr + 3, neurons nc + 16 j
+  const int sr = tid >> 4, nc = tid & 15;
+  {
+    float acc[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) acc[a][j] = b1[nc + 16 * j];
+    for (int k = 0; k < kMlpIn; ++k) {
+      float xv[4], wv[4];
+#pragma unroll
+      for (int a = 0; a < 4; ++a) xv[a] = __bfloat162float(Xs[(4 * sr + a) * kMlpIn + k]);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) wv[j] = __bfloat162float(W1[(nc + 16 * j) * kMlpIn + k]);
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[a][j] = fmaf(xv[a], wv[j], acc[a][j]);
+    }
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int s = 4 * sr + a, c = nc + 16 * j;
+        Z1[s * kZP + c] = acc[a][j];
+        H1[s * kMlpHidden + c] = __float2bfloat16_rn(gelu(acc[a][j]));
+      }
+  }
+  __syncthreads();
+  {
+    float acc[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) acc[a][j] = b2[nc + 16 * j];
+    for (int k = 0; k < kMlpHidden; ++k) {
+      float xv[4], wv[4];
+#pragma unroll
+      for (int a = 0; a < 4; ++a) xv[a] = __bfloat162float(H1[(4 * sr + a) * kMlpHidden + k]);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) wv[j] = __bfloat162float(W2[(nc + 16 * j) * kMlpHidden + k]);
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[a][j] = fmaf(xv[a], wv[j], acc[a][j]);
+    }
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int s = 4 * sr + a, c = nc + 16 * j;
+        Z2[s * kZP + c] = acc[a][j];
+        H2[s * kMlpHidden + c] = __float2bfloat16_rn(gelu(acc[a][j]));
+      }
+  }
+  __syncthreads();
+  if (tid < kTB * kMlpOut) {
+    const int s = tid / kMlpOut, o = tid % kMlpOut;
+    float z = b3[o];
+    for (int k = 0; k < kMlpHidden; ++k)
+      z = fmaf(__bfloat162float(H2[s * kMlpHidden + k]), __bfloat162float(W3[o * kMlpHidden + k]), z);
+    const bool in = s0 + s < n;
+    if (mode == 0) {
+      if (in) out[(size_t)(s0 + s) * kMlpOut + o] = z;
+    } else {
+      const float d = in ? z - Yt[(size_t)(s0 + s) * kMlpOut + o] : 0.f;
+      Yo[s * 4 + o] = 2.f * d / (float)(kMlpOut * n);  // d(mean squared error) / dz
+      Lsq[tid] = d * d;
+    }
+  }
+  if (mode == 0) return;
+  __syncthreads();
+  float* g = gpart + (size_t)blockIdx.x * kMlpParams;
+  // output layer: dW3 = dY^T H2, db3 = sum dY
+  if (tid < kMlpOut * kMlpHidden) {
+    const int o = tid / kMlpHidden, k = tid % kMlpHidden;
+    float a = 0.f;
+    for (int s = 0; s < kTB; ++s) a = fmaf(Yo[s * 4 + o], __bfloat162float(H2[s * kMlpHidden + k]), a);
+    g[kMlpW3 + tid] = a;
+  }
+  if (tid < kMlpOut) {
+    float a = 0.f;
+    for (int s = 0; s < kTB; ++s) a += Yo[s * 4 + tid];
+    g[kMlpB3 + tid] = a;
+  }
+  if (tid == 0) {
+    float a = 0.f;
+    for (int i = 0; i < kTB * kMlpOut; ++i) a += Lsq[i];
+    lpart[blockIdx.x] = a;
+  }
+  // dZ2 = (dY W3) * gelu'(Z2), in place (each thread its own entries)
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int s = 4 * sr + a, c = nc + 16 * j;
+      float dh = 0.f;
+#pragma unroll
+      for (int o = 0; o < kMlpOut; ++o) dh = fmaf(Yo[s * 4 + o], __bfloat162float(W3[o * kMlpHidden + c]), dh);
+      Z2[s * kZP + c] = dh * gelu_grad(Z2[s * kZP + c]);
+    }
+  __syncthreads();
+  // dW2 = dZ2^T H1 (rows 4 sr + a, columns nc + 16 j), db2 = sum dZ2
+  {
+    float acc[4][4] = {};
+    for (int s = 0; s < kTB; ++s) {
+      float dz[4], h[4];
+#pragma unroll
+      for (int a = 0; a < 4; ++a) dz[a] = Z2[s * kZP + 4 * sr + a];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) h[j] = __bfloat162float(H1[s * kMlpHidden + nc + 16 * j]);
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[a][j] = fmaf(dz[a], h[j], acc[a][j]);
+    }
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) g[kMlpW2 + (4 * sr + a) * kMlpHidden + nc + 16 * j] = acc[a][j];
+  }
+  if (tid < kMlpHidden) {
+    float a = 0.f;
+    for (int s = 0; s < kTB; ++s) a += Z2[s * kZP + tid];
+    g[kMlpB2 + tid] = a;
+  }
+  // dZ1 = (dZ2 W2) * gelu'(Z1), in place after every thread has its values
+  {
+    float dz1[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int s = 4 * sr + a, c = nc + 16 * j;
+        float dh = 0.f;
+        for (int k = 0; k < kMlpHidden; ++k)
+          dh = fmaf(Z2[s * kZP + k], __bfloat162float(W2[k * kMlpHidden + c]), dh);
+        dz1[a][j] = dh * gelu_grad(Z1[s * kZP + c]);
+      }
+    __syncthreads();
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) Z1[(4 * sr + a) * kZP + nc + 16 * j] = dz1[a][j];
+  }
+  __syncthreads();
+  // dW1 = dZ1^T X (rows 4 sr + a, columns nc + 16 j, j < 8), db1 = sum dZ1
+  {
+    float acc[4][8] = {};
+    for (int s = 0; s < kTB; ++s) {
+      float dz[4], x[8];
+#pragma unroll
+      for (int a = 0; a < 4; ++a) dz[a] = Z1[s * kZP + 4 * sr + a];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) x[j] = __bfloat162float(Xs[s * kMlpIn + nc + 16 * j]);
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[a][j] = fmaf(dz[a], x[j], acc[a][j]);
+    }
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int j = 0; j < 8; ++j) g[kMlpW1 + (4 * sr + a) * kMlpIn + nc + 16 * j] = acc[a][j];
+  }
+  if (tid < kMlpHidden) {
+    float a = 0.f;
+    for (int s = 0; s < kTB; ++s) a += Z1[s * kZP + tid];
+    g[kMlpB1 + tid] = a;
+  }
+}
+
+__global__ void k_mlp_reduce(const float* __restrict__ gpart, const float* __restrict__ lpart, int nb,
+                             float* __restrict__ grad, float* __restrict__ loss) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p < kMlpParams) {
+    float a = 0.f;
+    for (int b = 0; b < nb; ++b) a += gpart[(size_t)b * kMlpParams + p];
+    grad[p] = a;
+  }
+  if (p == 0 && loss) {
+    float a = 0.f;
+    for (int b = 0; b < nb; ++b) a += lpart[b];
+    *loss = a;
+  }
+}
+
+__global__ void k_mlp_adam(float* __restrict__ P, float* __restrict__ m1, float* __restrict__ m2,
+                           const float* __restrict__ g, float lr, float beta1, float beta2, float eps, int step) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= kMlpParams) return;
+  const float gp = g[p];
+  const float a = beta1 * m1[p] + (1.f - beta1) * gp;
+  const float b = beta2 * m2[p] + (1.f - beta2) * gp * gp;
+  m1[p] = a;
+  m2[p] = b;
+  const float ah = a / (1.f - powf(beta1, (float)step)), bh = b / (1.f - powf(beta2, (float)step));
+  P[p] -= lr * ah / (sqrtf(bh) + eps);
+}
+
+int infer_grid() {
+  static int grid = 0;
+  if (!grid) {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmInfer);
+    cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mlp_infer, kInferThreads, kSmInfer);
+    // two blocks per SM fit (64 registers x 512 threads, ~90 KB of shared
+    // memory, 128 tensor-memory columns each)
+    grid = (sms > 0 ? sms : 152) * (per > 1 ? per : 2);
+  }
+  return grid;
+}
+
+constexpr int kLErrorGrid = 152 * 8;
+
+}  // namespace
+
+void learned_build_v2v(const DevMesh& m, int* off, int* nb, int* tmp, unsigned char* tile_half, cudaStream_t s) {
+  cudaMemsetAsync(off, 0, sizeof(int) * ((size_t)m.V + 1), s);
+  cudaMemsetAsync(tmp, 0, sizeof(int) * (size_t)m.V, s);
+  if (m.E) k_v2v_count<<<nblk(m.E), kBlock, 0, s>>>(m.E, m.edv, off);
+  size_t bytes = 0;
+  cub::DeviceScan::ExclusiveSum(nullptr, bytes, off, off, m.V + 1, s);
+  void* scratch = nullptr;
+  cudaMallocAsync(&scratch, bytes, s);
+  cub::DeviceScan::ExclusiveSum(scratch, bytes, off, off, m.V + 1, s);
+  cudaFreeAsync(scratch, s);
+  if (m.E) k_v2v_fill<<<nblk(m.E), kBlock, 0, s>>>(m.E, m.edv, off, tmp, nb);
+  if (m.V) k_v2v_sort<<<nblk(m.V), kBlock, 0, s>>>(m.V, off, nb);
+  if (m.V) k_tile_half<<<(m.V + 127) / 128, 128, 0, s>>>(m.V, off, tile_half);
+}
+
+void learned_prep(const DevMesh& m, const double* u, float4* vr16, cudaStream_t s) {
+  if (m.V) k_lprep<<<nblk(m.V), kBlock, 0, s>>>(m.V, u, reinterpret_cast<const float4*>(m.xyz32), vr16);
+}
+
+void learned_features(const DevMesh& m, const LearnMesh& lm, const float4* vr16, uint16_t* x, float* aux,
+                      cudaStream_t s) {
+  if (m.V) k_lfeatures<<<nblk(4L * m.V), kBlock, 0, s>>>(m.V, lm, vr16, reinterpret_cast<uint2*>(x), aux);
+}
+
+void learned_pack(const float* params, void* packed, cudaStream_t s) {
+  k_mlp_pack<<<32, 256, 0, s>>>(params, static_cast<unsigned char*>(packed));
+}
+
+void learned_infer(const DevMesh& m, const LearnMesh& lm, const float4* vr16, const double* u, const void* packed,
+                   float4* rec16, int* fb_items, int* fb_count, float z_max, int use_mlp, int* err, cudaStream_t s) {
+  if (!m.V) return;
+  const int ntiles = (m.V + 127) / 128;
+  int grid = infer_grid();
+  if (grid > ntiles) grid = ntiles;
+  k_mlp_infer<<<grid, kInferThreads, kSmInfer, s>>>(m.V, lm, vr16, u, static_cast<const uint4*>(packed), rec16, fb_items,
+                                                    fb_count, z_max, use_mlp, err);
+}
+
+void learned_fallback(const DevMesh& m, const LearnMesh& lm, const float4* vr16, const double* u, const float* w,
+                      const double* rec64, const int* fb_items, const int* fb_count, int fb_cap, float4* rec16,
+                      cudaStream_t s) {
+  k_lfallback<<<152 * 4, 256, 0, s>>>(m, lm, vr16, u, w, rec64, fb_items, fb_count, fb_cap, rec16);
+}
+
+int learned_error_blocks(int T) {
+  int nb = nblk(T);
+  return nb < kLErrorGrid ? nb : kLErrorGrid;
+}
+
+void learned_error(const DevMesh& m, const float4* rec, const float2* geo, float* q, double* partials, int nb,
+                   cudaStream_t s) {
+  if (nb) k_lerror<<<nb, kBlock, 0, s>>>(m, rec, geo, q, partials);
+}
+
+void learned_average(const DevMesh& m, const float* q, const double* out3, float* size, cudaStream_t s) {
+  if (m.V) k_laverage<<<nblk(4L * m.V), kBlock, 0, s>>>(m, q, out3, size);
+}
+
+void learned_measure(const DevMesh& m, const float* half_len, const float* size, uint32_t* split, uint32_t* collapse,
+                     cudaStream_t s) {
+  if (m.E) k_lmeasure<<<nblk((m.E + 1) / 2), kBlock, 0, s>>>(m, half_len, size, split, collapse);
+}
+
+void learned_size_to_f64(int V, const float* s32, double* s64, cudaStream_t s) {
+  if (V) k_lsize_f64<<<nblk(V), kBlock, 0, s>>>(V, s32, s64);
+}
+
+size_t mlp_scratch_bytes(int n) {
+  const size_t nb = (size_t)nblk(n, kTB);
+  return 4 * (nb * kMlpParams + nb);
+}
+
+void mlp_run(int mode, const float* params, const uint16_t* x, const float* y, int n, float* out, float* grad,
+             float* loss, void* scratch, cudaStream_t s) {
+  if (n <= 0) return;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize, kTrSmem);
+    attr = true;
+  }
+  const int nb = nblk(n, kTB);
+  float* gpart = static_cast<float*>(scratch);
+  float* lpart = gpart + (size_t)nb * kMlpParams;
+  k_mlp_train<<<nb, 256, kTrSmem, s>>>(mode, params, reinterpret_cast<const __nv_bfloat16*>(x), y, n, out, gpart,
+                                       lpart);
+  if (mode == 1) k_mlp_reduce<<<nblk(kMlpParams), kBlock, 0, s>>>(gpart, lpart, nb, grad, loss);
+}
+
+void mlp_adam(float* params, float* m1, float* m2, const float* grad, float lr, float beta1, float beta2, float eps,
+              int step, cudaStream_t s) {
+  k_mlp_adam<<<nblk(kMlpParams), kBlock, 0, s>>>(params, m1, m2, grad, lr, beta1, beta2, eps, step);
+}
+
+}  // namespace sprg

@@ -42,6 +42,7 @@ extern "C" {
 /* precision modes */
 #define SPRG_FP64 0  /* FP64 throughout, the reference's arithmetic */
 #define SPRG_FP32 1  /* FP32 fits and sweeps with compensated residuals, FP64 guard band (tets) */
+#define SPRG_LEARNED 2 /* MLP-predicted recovery with SPR fallback, FP32 sweeps (tets, size to 1e-2) */
 
 /* markEntities flag bits (ma/maAdapt.h:17-37) */
 #define SPRG_SPLIT (1 << 0)
@@ -85,6 +86,7 @@ typedef struct sprg_size_info {
   int64_t n_fp64_refits;   /* FP32 mode: patches refit in FP64 (condition estimate > 1e6) */
   int64_t n_guard_edges;   /* FP32 mode: edges within 2e-6 of 0.5 / 1.5, re-decided in FP64 */
   int64_t n_guard_unresolved; /* FP32 mode: guard edges left to the FP32 decision (patch growth needed) */
+  int64_t n_learned_fallback; /* learned mode: vertices recovered by plain SPR instead of the network */
 } sprg_size_info;
 
 /* ---- context: flatten + upload (the MDS-to-device flattener) ---------- */
@@ -94,7 +96,7 @@ typedef struct sprg_size_info {
 int sprg_create(const sprg_mesh_view* mesh, int device, sprg_ctx** out);
 int sprg_destroy(sprg_ctx* ctx);
 const char* sprg_last_error(const sprg_ctx* ctx);
-/* SPRG_FP64 (default) or SPRG_FP32. */
+/* SPRG_FP64 (default), SPRG_FP32 or SPRG_LEARNED. */
 int sprg_set_precision(sprg_ctx* ctx, int precision);
 /* Run on this CUDA stream (cudaStream_t, NULL = the context's own). */
 int sprg_set_stream(sprg_ctx* ctx, void* stream);
@@ -230,6 +232,39 @@ int sprg_box_counts(int nx, int ny, int nz, int64_t* n_verts, int64_t* n_elems, 
    allocated with the sizes from sprg_box_counts. */
 int sprg_box_fill(int nx, int ny, int nz, double wx, double wy, double wz,
                   double* coords, int32_t* elem_verts, int32_t* edge_verts);
+
+/* ---- learned form (SPRG_LEARNED); no reference counterpart ------------
+   eps*(v) = g_c + z * s_v / r_v with g_c the least-squares gradient of the
+   vertex's neighbours, z an MLP (4 x 32 inputs -> 64 -> 64 -> 3, GELU, BF16
+   weights and activations, FP32 accumulation) of the normalised neighbour
+   offsets and residuals.  Plain SPR recovers the vertices the network does
+   not answer (see sprg_set_learned_options).  Parameters: FP32 vector of
+   SPRG_MLP_PARAMS values, W1 [64][128], b1 [64], W2 [64][64], b2 [64],
+   W3 [3][64], b3 [3] (weights [output][input]). */
+#define SPRG_MLP_PARAMS 12611
+#define SPRG_MLP_INPUTS 128
+#define SPRG_MLP_AUX 5
+int sprg_set_mlp_params(sprg_ctx* ctx, const float* params, int n_params);
+/* use_mlp = 0: g_c alone (the method without the network); z_max: vertices
+   whose output has a component beyond it take plain SPR (default 8). */
+int sprg_set_learned_options(sprg_ctx* ctx, int use_mlp, double z_max);
+/* Network inputs of every vertex for field d_u (device, V doubles): d_x
+   [V][128] BF16 (row-major), d_aux [V][5] FP32 = g_c (3), s_v / r_v, and 1 where
+   the vertex takes plain SPR.  Training-data generation. */
+int sprg_learned_features(sprg_ctx* ctx, const double* d_u, uint16_t* d_x, float* d_aux);
+
+/* ---- MLP training kernels (device pointers, stream = cudaStream_t) ----- */
+/* scratch bytes for n samples */
+size_t sprg_mlp_scratch_bytes(int n);
+/* d_out [n][3] = MLP(d_x) with BF16 weights and activations */
+int sprg_mlp_forward(const float* d_params, const uint16_t* d_x, int n, float* d_out, void* d_scratch, void* stream);
+/* gradient of the mean squared error against d_y [n][3] (d_grad, SPRG_MLP_PARAMS)
+   and the sum of squared errors (d_loss, 1 float) */
+int sprg_mlp_grad(const float* d_params, const uint16_t* d_x, const float* d_y, int n, float* d_grad, float* d_loss,
+                  void* d_scratch, void* stream);
+/* one Adam step (step counts from 1) */
+int sprg_mlp_adam(float* d_params, float* d_m1, float* d_m2, const float* d_grad, float lr, float beta1, float beta2,
+                  float eps, int step, void* stream);
 
 #ifdef __cplusplus
 }
