@@ -44,7 +44,8 @@ EXPORTS = [
     "sprg_box_counts", "sprg_box_fill", "sprg_profile_enable", "sprg_profile_flush", "sprg_profile_report",
     "sprg_spr_size_from_recovered_noalloc", "sprg_debug_read",
     "sprg_set_mlp_params", "sprg_set_learned_options", "sprg_learned_features", "sprg_mlp_scratch_bytes",
-    "sprg_mlp_forward", "sprg_mlp_grad", "sprg_mlp_adam",
+    "sprg_mlp_forward", "sprg_mlp_grad", "sprg_mlp_adam", "sprg_hessian_metric",
+    "sprg_aniso_estimate_and_mark_resident",
 ]
 NOALLOC_MAX_ELEMS = 1 << 20
 
@@ -121,6 +122,8 @@ def load():
     lib.sprg_apply_marks.argtypes = [ctypes.c_int64, P, P, P, ctypes.POINTER(ctypes.c_long),
                                      ctypes.POINTER(ctypes.c_long)]
     F = ctypes.c_float
+    lib.sprg_hessian_metric.argtypes = [P, P, D, D, D, P, P]
+    lib.sprg_aniso_estimate_and_mark_resident.argtypes = [P, P, D, D, D, P, P, P]
     lib.sprg_set_mlp_params.argtypes = [P, P, I]
     lib.sprg_set_learned_options.argtypes = [P, I, D]
     lib.sprg_learned_features.argtypes = [P, P, P, P]

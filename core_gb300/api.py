@@ -200,6 +200,21 @@ class Context:
                                                      ctypes.byref(info)))
         return size, flags, ns.value, nc.value, info.as_dict()
 
+    def hessian_metric(self, hessian, eps, h_min, h_max):
+        """(sizes V x 3, frames V x 9) from a nodal Hessian V x 9."""
+        V = self.mesh.n_verts
+        H = _f64(hessian, (V, 9))
+        sizes = np.empty((V, 3))
+        frames = np.empty((V, 9))
+        self._check(self._lib.sprg_hessian_metric(self.h, H.ctypes.data, float(eps), float(h_min), float(h_max),
+                                                  sizes.ctypes.data, frames.ctypes.data))
+        return sizes, frames
+
+    def aniso_estimate_and_mark_resident(self, d_u, eps, h_min, h_max, d_split_bits, d_collapse_bits, d_quality=None):
+        """The anisotropic pass on device pointers (FP64)."""
+        self._check(self._lib.sprg_aniso_estimate_and_mark_resident(
+            self.h, d_u, float(eps), float(h_min), float(h_max), d_split_bits, d_collapse_bits, d_quality))
+
     def estimate_and_mark_resident(self, d_u, adapt_ratio, d_split_bits, d_collapse_bits):
         """Device-pointer form (ints are raw device addresses); asynchronous."""
         self._check(self._lib.sprg_estimate_and_mark_resident(self.h, ctypes.c_void_p(d_u), float(adapt_ratio),

@@ -47,6 +47,7 @@ struct sprg_ctx {
   DevBuf crec, vrec, rec32, q32, sz2, fcnt, guard, tetd, wts, w64, listed, geo, geo64, elen, fitems;
   DevBuf gstamp, gfit, grec, tstamp, tslot, trec, tcount;  // guard pipeline scratch
   // learned form
+  DevBuf hess;  // nodal Hessian upload (sprg_hessian_metric)
   DevBuf vvoff, vv, vtile, vr16, rec16, ql, sizel, fbitems, fbcount, mlp_packed, mlp_err, mlp_tmp;
   bool vv_ready = false, have_mlp = false;
   int use_mlp = 1;
@@ -430,7 +431,7 @@ int sprg_destroy(sprg_ctx* c) {
                     &c->out3,  &c->status,  &c->count, &c->xitems, &c->xcount, &c->slab, &c->bits,
                     &c->crec,  &c->vrec,    &c->rec32, &c->q32, &c->sz2,  &c->fcnt,   &c->guard, &c->tetd,
                     &c->wts,   &c->w64,     &c->listed, &c->geo, &c->geo64, &c->elen, &c->fitems, &c->gstamp, &c->gfit, &c->grec,
-                    &c->tstamp, &c->tslot,  &c->trec, &c->tcount, &c->vvoff, &c->vv, &c->vtile, &c->vr16, &c->rec16,
+                    &c->tstamp, &c->tslot,  &c->trec, &c->tcount, &c->hess, &c->vvoff, &c->vv, &c->vtile, &c->vr16, &c->rec16,
                     &c->ql,    &c->sizel,   &c->fbitems, &c->fbcount, &c->mlp_packed, &c->mlp_err, &c->mlp_tmp,
                     &c->cache64.v, &c->cache64.n, &c->cache64.el, &c->cache32.v, &c->cache32.n, &c->cache32.el};
   for (DevBuf* b : bufs) release(*b);
@@ -1114,6 +1115,67 @@ int sprg_mlp_adam(float* d_params, float* d_m1, float* d_m2, const float* d_grad
   if (!d_params || !d_m1 || !d_m2 || !d_grad || step < 1) return SPRG_EINVAL;
   mlp_adam(d_params, d_m1, d_m2, d_grad, lr, beta1, beta2, eps, step, static_cast<cudaStream_t>(stream));
   return cudaGetLastError() == cudaSuccess ? SPRG_OK : SPRG_ECUDA;
+}
+
+int sprg_hessian_metric(sprg_ctx* c, const double* hessian, double eps, double h_min, double h_max,
+                        double* sizes_out, double* frames_out) {
+  if (!c || !hessian || !sizes_out || !frames_out) return SPRG_EINVAL;
+  if (!(eps > 0) || !(h_min > 0) || !(h_max >= h_min)) return fail(c, SPRG_EINVAL, "need eps > 0, 0 < h_min <= h_max");
+  int rc = set_device(c);
+  if (rc) return rc;
+  c->launches = 0;
+  DevMesh& m = c->m;
+  ENSURE(c->hess, sizeof(double) * 9 * (size_t)m.V);
+  ENSURE(c->sizes3, sizeof(double) * 3 * (size_t)m.V);
+  ENSURE(c->frames9, sizeof(double) * 9 * (size_t)m.V);
+  CK(cudaMemcpyAsync(c->hess.p, hessian, sizeof(double) * 9 * (size_t)m.V, cudaMemcpyHostToDevice, c->stream));
+  launch_hessian_metric(m, P<double>(c->hess), eps, h_min, h_max, P<double>(c->sizes3), P<double>(c->frames9),
+                        c->stream);
+  c->launches += 1;
+  if ((rc = check_launch(c, "hessian metric"))) return rc;
+  CK(cudaMemcpyAsync(sizes_out, c->sizes3.p, sizeof(double) * 3 * (size_t)m.V, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaMemcpyAsync(frames_out, c->frames9.p, sizeof(double) * 9 * (size_t)m.V, cudaMemcpyDeviceToHost, c->stream));
+  return sync_and_status(c);
+}
+
+int sprg_aniso_estimate_and_mark_resident(sprg_ctx* c, const double* d_u, double eps, double h_min, double h_max,
+                                          uint32_t* d_split_bits, uint32_t* d_collapse_bits, double* d_quality) {
+  if (!c || !d_u || !d_split_bits || !d_collapse_bits) return SPRG_EINVAL;
+  if (!(eps > 0) || !(h_min > 0) || !(h_max >= h_min)) return fail(c, SPRG_EINVAL, "need eps > 0, 0 < h_min <= h_max");
+  int rc = set_device(c);
+  if (rc) return rc;
+  c->launches = 0;
+  DevMesh& m = c->m;
+  ENSURE(c->f, sizeof(double) * 3 * (size_t)m.V);
+  ENSURE(c->sizes3, sizeof(double) * 3 * (size_t)m.V);
+  ENSURE(c->frames9, sizeof(double) * 9 * (size_t)m.V);
+  ENSURE(c->L, sizeof(double) * (size_t)m.E);
+  if ((rc = reset_status(c))) return rc;
+  CK(cudaMemcpyAsync(c->f.p, d_u, sizeof(double) * (size_t)m.V, cudaMemcpyDeviceToDevice, c->stream));
+  // recovered gradient, then the recovered gradient of it (nodal Hessian)
+  if ((rc = step_grad(c, 1)) || (rc = step_recover(c))) return rc;
+  CK(cudaMemcpyAsync(c->f.p, c->rec.p, sizeof(double) * 3 * (size_t)m.V, cudaMemcpyDeviceToDevice, c->stream));
+  if ((rc = step_grad(c, 3)) || (rc = step_recover(c))) return rc;
+  PB("hessian_metric");
+  launch_hessian_metric(m, P<double>(c->rec), eps, h_min, h_max, P<double>(c->sizes3), P<double>(c->frames9),
+                        c->stream);
+  PE();
+  PB("measure_aniso_f64");
+  launch_measure_aniso_f64(m, P<double>(c->sizes3), P<double>(c->frames9), P<double>(c->L), c->stream);
+  PE();
+  PB("mark_bits");
+  launch_mark_bits(m.E, P<double>(c->L), d_split_bits, d_collapse_bits, c->stream);
+  PE();
+  c->launches += 3;
+  if (d_quality) {
+    PB("quality_f64");
+    launch_quality_f64(m, nullptr, P<double>(c->sizes3), P<double>(c->frames9), d_quality, c->stream);
+    PE();
+    c->launches += 1;
+  }
+  c->L_valid = true;
+  c->size_valid = false;
+  return check_launch(c, "aniso pass");
 }
 
 }  // extern "C"

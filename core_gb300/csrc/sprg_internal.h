@@ -109,6 +109,9 @@ void launch_guard_stage(int stage, const DevMesh& m, const double* u, const doub
                         GuardScratch g, cudaStream_t s);
 void launch_quality_f64(const DevMesh& m, const double* size, const double* sizes, const double* frames,
                         double* q, cudaStream_t s);
+// anisotropic metric (sizes V x 3, frames V x 9) from a nodal Hessian (V x 9)
+void launch_hessian_metric(const DevMesh& m, const double* H, double eps, double hmin, double hmax, double* sizes,
+                           double* frames, cudaStream_t s);
 
 // ---- adjacency builders (sprg_kernels_f64.cu) ---------------------------
 // Ascending vertex->element CSR via counting sort on the device.

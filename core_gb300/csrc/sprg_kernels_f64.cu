@@ -950,6 +950,128 @@ __global__ void __launch_bounds__(128) k_guard_decide(DevMesh m, const double* _
 }
 
 // ---------------------------------------------------------------------
+// anisotropic metric from a nodal Hessian (the 2D anisotropic workload's
+// size and frame fields): eigen-decompose the symmetric part, order the
+// principal directions by |lambda| descending, sign each direction so its
+// largest component is positive (2D: first direction's x >= 0, second its
+// +90 degree rotation), h_i = clamp(sqrt(eps / |lambda_i|), h_min, h_max);
+// frames row-major with the directions as columns (AnisoSizeField's R).
+// ---------------------------------------------------------------------
+__device__ void sym_eigen3(double A[3][3], double lam[3], double Vm[3][3]) {
+  // cyclic Jacobi, fixed sweep count (deterministic)
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) Vm[i][j] = i == j ? 1.0 : 0.0;
+  for (int sweep = 0; sweep < 8; ++sweep) {
+    for (int p = 0; p < 2; ++p)
+      for (int q = p + 1; q < 3; ++q) {
+        const double apq = A[p][q];
+        if (apq == 0.0) continue;
+        const double theta = (A[q][q] - A[p][p]) / (2.0 * apq);
+        const double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+        const double c = 1.0 / sqrt(t * t + 1.0), sn = t * c;
+        for (int k = 0; k < 3; ++k) {
+          const double akp = A[k][p], akq = A[k][q];
+          A[k][p] = c * akp - sn * akq;
+          A[k][q] = sn * akp + c * akq;
+        }
+        for (int k = 0; k < 3; ++k) {
+          const double apk = A[p][k], aqk = A[q][k];
+          A[p][k] = c * apk - sn * aqk;
+          A[q][k] = sn * apk + c * aqk;
+        }
+        for (int k = 0; k < 3; ++k) {
+          const double vkp = Vm[k][p], vkq = Vm[k][q];
+          Vm[k][p] = c * vkp - sn * vkq;
+          Vm[k][q] = sn * vkp + c * vkq;
+        }
+      }
+  }
+  for (int i = 0; i < 3; ++i) lam[i] = A[i][i];
+}
+
+__device__ __forceinline__ double metric_size(double lam, double eps, double hmin, double hmax) {
+  const double a = fabs(lam);
+  if (!(a > 0)) return hmax;
+  return fmin(fmax(sqrt(eps / a), hmin), hmax);
+}
+
+__global__ void k_hessian_metric(int V, int dim, const double* __restrict__ H, double eps, double hmin, double hmax,
+                                 double* __restrict__ sizes, double* __restrict__ frames) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= V) return;
+  const double* h = H + 9 * (size_t)v;
+  double R[3][3], hs[3];
+  if (dim == 2) {
+    const double a = h[0], b = 0.5 * (h[1] + h[3]), c = h[4];
+    const double mid = 0.5 * (a + c), hd = 0.5 * (a - c);
+    const double d = sqrt(hd * hd + b * b);
+    double l1 = mid + d, l2 = mid - d;
+    double x, y;
+    if (b == 0.0) {
+      x = a >= c ? 1.0 : 0.0;
+      y = a >= c ? 0.0 : 1.0;
+    } else if (a >= c) {
+      x = l1 - c;
+      y = b;
+    } else {
+      x = b;
+      y = l1 - a;
+    }
+    const double n = sqrt(x * x + y * y);
+    x /= n;
+    y /= n;
+    if (fabs(l2) > fabs(l1)) {  // the second direction is (-y, x)
+      const double tl = l1;
+      l1 = l2;
+      l2 = tl;
+      const double tx = x;
+      x = -y;
+      y = tx;
+    }
+    if (x < 0 || (x == 0 && y < 0)) {
+      x = -x;
+      y = -y;
+    }
+    R[0][0] = x; R[0][1] = -y; R[0][2] = 0;
+    R[1][0] = y; R[1][1] = x;  R[1][2] = 0;
+    R[2][0] = 0; R[2][1] = 0;  R[2][2] = 1;
+    hs[0] = metric_size(l1, eps, hmin, hmax);
+    hs[1] = metric_size(l2, eps, hmin, hmax);
+    hs[2] = hmax;
+  } else {
+    double A[3][3], lam[3], Vm[3][3];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) A[i][j] = 0.5 * (h[3 * i + j] + h[3 * j + i]);
+    sym_eigen3(A, lam, Vm);
+    int o[3] = {0, 1, 2};
+    for (int i = 0; i < 3; ++i)
+      for (int j = i + 1; j < 3; ++j)
+        if (fabs(lam[o[j]]) > fabs(lam[o[i]])) {
+          const int t = o[i];
+          o[i] = o[j];
+          o[j] = t;
+        }
+    for (int k = 0; k < 2; ++k) {
+      double col[3] = {Vm[0][o[k]], Vm[1][o[k]], Vm[2][o[k]]};
+      int im = 0;
+      for (int i = 1; i < 3; ++i)
+        if (fabs(col[i]) > fabs(col[im])) im = i;
+      const double sg = col[im] < 0 ? -1.0 : 1.0;
+      for (int i = 0; i < 3; ++i) R[i][k] = sg * col[i];
+      hs[k] = metric_size(lam[o[k]], eps, hmin, hmax);
+    }
+    // third direction: right-handed completion
+    R[0][2] = R[1][0] * R[2][1] - R[2][0] * R[1][1];
+    R[1][2] = R[2][0] * R[0][1] - R[0][0] * R[2][1];
+    R[2][2] = R[0][0] * R[1][1] - R[1][0] * R[0][1];
+    hs[2] = metric_size(lam[o[2]], eps, hmin, hmax);
+  }
+  for (int k = 0; k < 3; ++k) sizes[3 * (size_t)v + k] = hs[k];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) frames[9 * (size_t)v + 3 * i + j] = R[i][j];
+}
+
+// ---------------------------------------------------------------------
 // adjacency construction
 // ---------------------------------------------------------------------
 __global__ void k_count_v2e(DevMesh m, int* cnt) {
@@ -1098,6 +1220,11 @@ void launch_guard_stage(int stage, const DevMesh& m, const double* u, const doub
     default:
       k_guard_decide<<<152 * 2, 128, 0, s>>>(m, u, out3, g, items, count, cap, split, collapse, unresolved);
   }
+}
+
+void launch_hessian_metric(const DevMesh& m, const double* H, double eps, double hmin, double hmax, double* sizes,
+                           double* frames, cudaStream_t s) {
+  if (m.V) k_hessian_metric<<<nblk(m.V), kBlock, 0, s>>>(m.V, m.dim, H, eps, hmin, hmax, sizes, frames);
 }
 
 void launch_build_v2e(const DevMesh& m, int* off, int* el, int* tmp, cudaStream_t s) {

@@ -60,6 +60,20 @@ def boundary_layer_field(coords):
     return np.tanh((y - 0.5) / 1e-3) + 0.1 * np.sin(8 * np.pi * x)
 
 
+def aniso2d_params(n):
+    """Metric constants of the 2D anisotropic workload on an n x n square:
+    eps = 63 (2/n)^2 (twice the cell size where |u_xx| = 0.1 (8 pi)^2),
+    h_min = 1 / (4 n), h_max = 0.05."""
+    return 63.0 * (2.0 / n) ** 2, 1.0 / (4 * n), 0.05
+
+
+def aniso2d(n, seed=5):
+    """(mesh, u, (eps, h_min, h_max)): n x n square, interior jitter +-0.15h,
+    boundary-layer field."""
+    m = box(n, nz=0, jitter=0.15, seed=seed)
+    return m, boundary_layer_field(m.coords), aniso2d_params(n)
+
+
 def config(name):
     """(mesh, field, adapt_ratio) of a named workload."""
     if name == "box8":

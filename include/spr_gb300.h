@@ -151,6 +151,18 @@ int sprg_mark_edges(sprg_ctx* ctx, int which, int32_t* flags, long* count);
 int sprg_measure_quality(sprg_ctx* ctx, const double* size, const double* sizes, const double* frames,
                          double* q);
 
+/* Anisotropic metric from a nodal Hessian (V x 9 row-major, e.g. the
+   recovered field of the gradient of the recovered gradient): sizes (V x 3)
+   h_i = clamp(sqrt(eps / |lambda_i|), h_min, h_max) and frames (V x 9,
+   row-major, principal directions as columns, ordered by |lambda|
+   descending, each signed so its largest component is positive; in 2D the
+   second direction is the first turned by +90 degrees and the third is z with
+   h_max).  The metric the 2D anisotropic workload feeds to
+   ma::makeSizeField(m, sizes, frames, false) (ma/maSize.cc:618); the
+   reference's drivers build it with apf::eigen (apf/apfMatrix.cc:68). */
+int sprg_hessian_metric(sprg_ctx* ctx, const double* hessian, double eps, double h_min, double h_max,
+                        double* sizes_out, double* frames_out);
+
 /* ---- the whole pass ---------------------------------------------------- */
 
 /* getGradIPField(u,"grad",1) -> getSPRSizeField(grad, adapt_ratio) ->
@@ -169,6 +181,14 @@ int sprg_estimate_and_mark(sprg_ctx* ctx, const double* u, double adapt_ratio, d
    bitmaps into "ma_flags" words with markEntities semantics. */
 int sprg_estimate_and_mark_resident(sprg_ctx* ctx, const double* d_u, double adapt_ratio, uint32_t* d_split_bits,
                                     uint32_t* d_collapse_bits);
+/* The anisotropic pass on device buffers (FP64, any precision setting):
+   getGradIPField(u) -> recoverField -> getGradIPField of the recovered
+   gradient -> recoverField (nodal Hessian) -> sprg_hessian_metric ->
+   AnisoSizeField measure (ma/maSize.cc:364-412) -> split/collapse bitmaps
+   -> element quality under the metric (d_quality, n_elems doubles, may be
+   NULL).  d_u: V doubles. */
+int sprg_aniso_estimate_and_mark_resident(sprg_ctx* ctx, const double* d_u, double eps, double h_min, double h_max,
+                                          uint32_t* d_split_bits, uint32_t* d_collapse_bits, double* d_quality);
 
 /* Host write-back of the device edge-mark bitmaps into "ma_flags" words
    with markEntities semantics (ma/maAdapt.cc:293-324): collapse pass, then
