@@ -45,7 +45,7 @@ EXPORTS = [
     "sprg_spr_size_from_recovered_noalloc", "sprg_debug_read",
     "sprg_set_mlp_params", "sprg_set_learned_options", "sprg_learned_features", "sprg_mlp_scratch_bytes",
     "sprg_mlp_forward", "sprg_mlp_grad", "sprg_mlp_adam", "sprg_hessian_metric",
-    "sprg_aniso_estimate_and_mark_resident",
+    "sprg_aniso_estimate_and_mark_resident", "sprg_set_batch", "sprg_batch_info",
 ]
 NOALLOC_MAX_ELEMS = 1 << 20
 
@@ -123,6 +123,8 @@ def load():
                                      ctypes.POINTER(ctypes.c_long)]
     F = ctypes.c_float
     lib.sprg_hessian_metric.argtypes = [P, P, D, D, D, P, P]
+    lib.sprg_set_batch.argtypes = [P, I, P, P, P]
+    lib.sprg_batch_info.argtypes = [P, P]
     lib.sprg_aniso_estimate_and_mark_resident.argtypes = [P, P, D, D, D, P, P, P]
     lib.sprg_set_mlp_params.argtypes = [P, P, I]
     lib.sprg_set_learned_options.argtypes = [P, I, D]

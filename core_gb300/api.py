@@ -200,6 +200,22 @@ class Context:
                                                      ctypes.byref(info)))
         return size, flags, ns.value, nc.value, info.as_dict()
 
+    # ---- batch of meshes ---------------------------------------------------
+    def set_batch(self, vert_offsets, elem_offsets, adapt_ratios):
+        """Treat the context's mesh as a disjoint union of meshes (prefix
+        offsets of length n + 1) with per-mesh adapt ratios."""
+        vo = np.ascontiguousarray(vert_offsets, np.int64)
+        eo = np.ascontiguousarray(elem_offsets, np.int64)
+        r = np.ascontiguousarray(adapt_ratios, np.float64)
+        self._check(self._lib.sprg_set_batch(self.h, int(r.size), vo.ctypes.data, eo.ctypes.data, r.ctypes.data))
+        self._batch_n = int(r.size)
+
+    def batch_info(self):
+        """(n, 3): eps_star_norm2, error_sum, size_factor per mesh."""
+        out = np.empty((self._batch_n, 3))
+        self._check(self._lib.sprg_batch_info(self.h, out.ctypes.data))
+        return out
+
     def hessian_metric(self, hessian, eps, h_min, h_max):
         """(sizes V x 3, frames V x 9) from a nodal Hessian V x 9."""
         V = self.mesh.n_verts

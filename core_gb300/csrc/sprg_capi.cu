@@ -48,6 +48,10 @@ struct sprg_ctx {
   DevBuf gstamp, gfit, grec, tstamp, tslot, trec, tcount;  // guard pipeline scratch
   // learned form
   DevBuf hess;  // nodal Hessian upload (sprg_hessian_metric)
+  // batch of independent meshes (sprg_set_batch)
+  int batch_n = 0, batch_nseg = 0;
+  DevBuf bvoff, bseg, bsegoff, bratios;
+  static constexpr int kSegTets = 2048;  // elements per error segment (8 per thread)
   DevBuf vvoff, vv, vtile, vr16, rec16, ql, sizel, fbitems, fbcount, mlp_packed, mlp_err, mlp_tmp;
   bool vv_ready = false, have_mlp = false;
   int use_mlp = 1;
@@ -431,7 +435,7 @@ int sprg_destroy(sprg_ctx* c) {
                     &c->out3,  &c->status,  &c->count, &c->xitems, &c->xcount, &c->slab, &c->bits,
                     &c->crec,  &c->vrec,    &c->rec32, &c->q32, &c->sz2,  &c->fcnt,   &c->guard, &c->tetd,
                     &c->wts,   &c->w64,     &c->listed, &c->geo, &c->geo64, &c->elen, &c->fitems, &c->gstamp, &c->gfit, &c->grec,
-                    &c->tstamp, &c->tslot,  &c->trec, &c->tcount, &c->hess, &c->vvoff, &c->vv, &c->vtile, &c->vr16, &c->rec16,
+                    &c->tstamp, &c->tslot,  &c->trec, &c->tcount, &c->hess, &c->bvoff, &c->bseg, &c->bsegoff, &c->bratios, &c->vvoff, &c->vv, &c->vtile, &c->vr16, &c->rec16,
                     &c->ql,    &c->sizel,   &c->fbitems, &c->fbcount, &c->mlp_packed, &c->mlp_err, &c->mlp_tmp,
                     &c->cache64.v, &c->cache64.n, &c->cache64.el, &c->cache32.v, &c->cache32.n, &c->cache32.el};
   for (DevBuf* b : bufs) release(*b);
@@ -654,6 +658,11 @@ int sprg_measure_quality(sprg_ctx* c, const double* size, const double* sizes, c
   return sync_and_status(c);
 }
 
+static BatchView batch_view(sprg_ctx* c) {
+  if (!c->batch_n) return BatchView{0, nullptr, nullptr, nullptr, nullptr};
+  return BatchView{c->batch_n, P<int>(c->bvoff), P<int2>(c->bseg), P<int>(c->bsegoff), P<double>(c->bratios)};
+}
+
 // per mesh (FP32 and learned forms): coordinate records, element and edge
 // geometry, SPR weights and the listed patches
 static int fast_setup(sprg_ctx* c, ExpandList xl) {
@@ -716,7 +725,8 @@ static int listed_join(sprg_ctx* c, ExpandList xl, bool forked) {
 static int pass_fast(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_t* d_collapse) {
   DevMesh& m = c->m;
   int rc;
-  int nb = fast_error_blocks(m.T);
+  const BatchView bv = batch_view(c);
+  const int nb = bv.n ? c->batch_nseg : fast_error_blocks(m.T);
   const size_t nel = (size_t)m.T * m.nn;
   ENSURE(c->vrec, 32 * (size_t)m.V);
   ENSURE(c->rec32, 16 * (size_t)m.V);
@@ -730,7 +740,7 @@ static int pass_fast(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_
   ENSURE(c->fcnt, 8 * sizeof(int));
   ENSURE(c->guard, sizeof(int) * (size_t)sprg_ctx::kGuardCap);
   ENSURE(c->partials, sizeof(double) * 2 * (size_t)(nb > 0 ? nb : 1));
-  ENSURE(c->out3, sizeof(double) * 4);
+  ENSURE(c->out3, sizeof(double) * 4 * (size_t)(bv.n > 0 ? bv.n : 1));
   if ((rc = reset_status(c))) return rc;
   // fcnt: [0] refit patches, [1] guard edges, [3] listed patches,
   // [4] unresolved guard edges, [5] failed guard fits (0, 3 per mesh; 1, 4, 5 per pass)
@@ -759,13 +769,16 @@ static int pass_fast(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_
   PE();
   PB("error_f32");
   fast_error(m, P<uint4>(c->tetd), P<float2>(c->geo), rec32, P<float2>(c->q32), P<double>(c->partials), nb,
-             c->stream);
+             bv.n ? P<int2>(c->bseg) : nullptr, c->stream);
   PE();
   PB("size_factor");
-  launch_size_factor(P<double>(c->partials), nb, 0, adapt_ratio, 0, m.dim, P<double>(c->out3), c->stream);
+  if (bv.n)
+    launch_size_factor_batch(P<double>(c->partials), bv, m.dim, P<double>(c->out3), c->stream);
+  else
+    launch_size_factor(P<double>(c->partials), nb, 0, adapt_ratio, 0, m.dim, P<double>(c->out3), c->stream);
   PE();
   PB("average_f32");
-  fast_average(m, P<float2>(c->q32), P<double>(c->out3), P<float2>(c->sz2), c->stream);
+  fast_average(m, P<float2>(c->q32), P<double>(c->out3), P<float2>(c->sz2), bv, c->stream);
   PE();
   PB("measure_f32");
   fast_measure(m, P<float>(c->elen), P<float2>(c->sz2), d_split, d_collapse, P<int>(c->guard), P<int>(c->fcnt) + 1,
@@ -793,7 +806,7 @@ static int pass_fast(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_
   for (int stage = 0; stage < 4; ++stage) {
     PB(kGuardNames[stage]);
     launch_guard_stage(stage, m, P<double>(c->f), P<double>(c->out3), P<int>(c->guard), P<int>(c->fcnt) + 1,
-                       sprg_ctx::kGuardCap, d_split, d_collapse, P<int>(c->fcnt) + 4, gs, c->stream);
+                       sprg_ctx::kGuardCap, d_split, d_collapse, P<int>(c->fcnt) + 4, gs, bv, c->stream);
     PE();
   }
   c->launches += 12;  // 8 FP32-path kernels and 4 guard kernels (listed_fits counts its own)
@@ -875,6 +888,8 @@ static int pass_learned(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint
 
 static int pass_resident(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_t* d_collapse) {
   int rc;
+  if (c->batch_n && c->precision != SPRG_FP32)
+    return fail(c, SPRG_EINVAL, "a batch of meshes runs in SPRG_FP32 (per-mesh size factors)");
   if (c->precision == SPRG_FP32) return pass_fast(c, adapt_ratio, d_split, d_collapse);
   if (c->precision == SPRG_LEARNED) return pass_learned(c, adapt_ratio, d_split, d_collapse);
   if ((rc = reset_status(c)) || (rc = step_grad(c, 1)) || (rc = step_recover(c)) ||
@@ -1176,6 +1191,60 @@ int sprg_aniso_estimate_and_mark_resident(sprg_ctx* c, const double* d_u, double
   c->L_valid = true;
   c->size_valid = false;
   return check_launch(c, "aniso pass");
+}
+
+int sprg_set_batch(sprg_ctx* c, int n_meshes, const int64_t* vert_offsets, const int64_t* elem_offsets,
+                   const double* adapt_ratios) {
+  if (!c) return SPRG_EINVAL;
+  int rc = set_device(c);
+  if (rc) return rc;
+  if (n_meshes == 0) {
+    c->batch_n = 0;
+    return SPRG_OK;
+  }
+  if (n_meshes < 0 || !vert_offsets || !elem_offsets || !adapt_ratios) return SPRG_EINVAL;
+  const DevMesh& m = c->m;
+  if (vert_offsets[0] != 0 || elem_offsets[0] != 0 || vert_offsets[n_meshes] != m.V || elem_offsets[n_meshes] != m.T)
+    return fail(c, SPRG_EINVAL, "batch offsets must start at 0 and end at the vertex / element counts");
+  std::vector<int> voff(n_meshes + 1), segoff(n_meshes + 1);
+  std::vector<int2> seg;
+  for (int k = 0; k < n_meshes; ++k) {
+    if (vert_offsets[k + 1] <= vert_offsets[k] || elem_offsets[k + 1] <= elem_offsets[k])
+      return fail(c, SPRG_EINVAL, "batch offsets must increase");
+    if (!(adapt_ratios[k] > 0)) return fail(c, SPRG_EINVAL, "adapt ratios must be positive");
+    voff[k] = (int)vert_offsets[k];
+    segoff[k] = (int)seg.size();
+    for (int64_t t = elem_offsets[k]; t < elem_offsets[k + 1]; t += sprg_ctx::kSegTets) {
+      int64_t e = t + sprg_ctx::kSegTets;
+      if (e > elem_offsets[k + 1]) e = elem_offsets[k + 1];
+      seg.push_back(make_int2((int)t, (int)e));
+    }
+  }
+  voff[n_meshes] = m.V;
+  segoff[n_meshes] = (int)seg.size();
+  ENSURE(c->bvoff, sizeof(int) * voff.size());
+  ENSURE(c->bsegoff, sizeof(int) * segoff.size());
+  ENSURE(c->bseg, sizeof(int2) * seg.size());
+  ENSURE(c->bratios, sizeof(double) * n_meshes);
+  CK(cudaMemcpy(c->bvoff.p, voff.data(), sizeof(int) * voff.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(c->bsegoff.p, segoff.data(), sizeof(int) * segoff.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(c->bseg.p, seg.data(), sizeof(int2) * seg.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(c->bratios.p, adapt_ratios, sizeof(double) * n_meshes, cudaMemcpyHostToDevice));
+  c->batch_n = n_meshes;
+  c->batch_nseg = (int)seg.size();
+  return SPRG_OK;
+}
+
+int sprg_batch_info(sprg_ctx* c, double* out) {
+  if (!c || !out || !c->batch_n || !c->out3.p) return SPRG_EINVAL;
+  int rc = set_device(c);
+  if (rc) return rc;
+  std::vector<double> o4(4 * (size_t)c->batch_n);
+  CK(cudaStreamSynchronize(c->stream));
+  CK(cudaMemcpy(o4.data(), c->out3.p, sizeof(double) * o4.size(), cudaMemcpyDeviceToHost));
+  for (int k = 0; k < c->batch_n; ++k)
+    for (int j = 0; j < 3; ++j) out[3 * (size_t)k + j] = o4[4 * (size_t)k + j];
+  return SPRG_OK;
 }
 
 }  // extern "C"

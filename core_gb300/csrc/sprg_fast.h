@@ -23,10 +23,11 @@ void fast_recover(const DevMesh& m, const float* w, const unsigned char* listed,
                   cudaStream_t s);
 void fast_merge_ref(ExpandList xl, const double* rec64, uint4* rec32, cudaStream_t s);
 // q: (h_max err^(-1/5), its relative error bound) per tet
+// seg (batch): one element range per block, nb = number of segments
 void fast_error(const DevMesh& m, const uint4* td, const float2* geo, const uint4* rec, float2* q, double* partials,
-                int nb, cudaStream_t s);
+                int nb, const int2* seg, cudaStream_t s);
 // sz2: (size, its relative error bound) per vertex
-void fast_average(const DevMesh& m, const float2* q, const double* out3, float2* sz2, cudaStream_t s);
+void fast_average(const DevMesh& m, const float2* q, const double* out3, float2* sz2, BatchView bv, cudaStream_t s);
 void fast_measure(const DevMesh& m, const float* half_len, const float2* sz2, uint32_t* split, uint32_t* collapse,
                   int* guard_items, int* guard_count, int guard_cap, float guard_rel, cudaStream_t s);
 void fast_size_to_f64(int V, const float2* sz2, double* s64, cudaStream_t s);

@@ -25,6 +25,35 @@ struct DevMesh {
   const int* a_el;
 };
 
+// A batch of independent meshes flattened into one context (disjoint union,
+// entity ids offset per mesh).  n = 0: a single mesh.  Per mesh k:
+// vertices [voff[k], voff[k+1]); error-kernel segments [segoff[k],
+// segoff[k+1]) of seg (element ranges that never cross a mesh); the size
+// factor of mesh k at out3[4 k + 2].
+struct BatchView {
+  int n;
+  const int* voff;
+  const int2* seg;
+  const int* segoff;
+  const double* ratios;
+};
+
+// mesh of vertex v (binary search over the vertex offsets)
+__device__ __forceinline__ int batch_mesh(const BatchView& b, int v) {
+  int lo = 0, hi = b.n;  // voff[lo] <= v < voff[hi]
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (__ldg(b.voff + mid) <= v) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// the size factor that applies at vertex v
+__device__ __forceinline__ double batch_sf(const BatchView& b, const double* out3, int v) {
+  return b.n ? out3[4 * batch_mesh(b, v) + 2] : out3[2];
+}
+
 // Device status word written by kernels (first error wins).
 struct DevStatus {
   int code;        // SPRG_OK or SPRG_E*
@@ -106,7 +135,9 @@ struct GuardScratch {
 // 3 decide.
 void launch_guard_stage(int stage, const DevMesh& m, const double* u, const double* out3, const int* items,
                         const int* count, int cap, uint32_t* split, uint32_t* collapse, int* unresolved,
-                        GuardScratch g, cudaStream_t s);
+                        GuardScratch g, BatchView bv, cudaStream_t s);
+// per-mesh size factors of a batch (SPR mode) from segment partials
+void launch_size_factor_batch(const double* partials, BatchView bv, int dim, double* out4, cudaStream_t s);
 void launch_quality_f64(const DevMesh& m, const double* size, const double* sizes, const double* frames,
                         double* q, cudaStream_t s);
 // anisotropic metric (sizes V x 3, frames V x 9) from a nodal Hessian (V x 9)

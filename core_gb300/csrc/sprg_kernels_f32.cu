@@ -473,13 +473,22 @@ __device__ __forceinline__ double warp_pair_total(PairSum p) {
   return (double)p.h + (double)p.l;
 }
 
+// grid-stride over all elements, or (batch) block b over the element range
+// seg[b] of one mesh, so each block's partials belong to one mesh
 __global__ void __launch_bounds__(kBlock) k_fast_error(DevMesh m, const uint4* __restrict__ td,
                                                        const float2* __restrict__ geo,
                                                        const uint4* __restrict__ rec, float2* __restrict__ q,
-                                                       double* __restrict__ partials) {
+                                                       double* __restrict__ partials, const int2* __restrict__ seg) {
   __shared__ double sh[2][kBlock / 32];
   PairSum self{0.f, 0.f}, gsum{0.f, 0.f};
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < m.T; t += gridDim.x * blockDim.x) {
+  int t_beg = blockIdx.x * blockDim.x + threadIdx.x, t_end = m.T, t_step = gridDim.x * blockDim.x;
+  if (seg) {
+    const int2 r = seg[blockIdx.x];
+    t_beg = r.x + threadIdx.x;
+    t_end = r.y;
+    t_step = blockDim.x;
+  }
+  for (int t = t_beg; t < t_end; t += t_step) {
     int4 tv = __ldg(reinterpret_cast<const int4*>(m.ev) + t);
     uint4 ta = __ldg(td + t);
     float2 gm = __ldg(geo + t);
@@ -532,7 +541,8 @@ __global__ void __launch_bounds__(kBlock) k_fast_error(DevMesh m, const uint4* _
 // average: size = size_factor * mean(q_t) over the vertex's elements
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kBlock) k_fast_average(DevMesh m, const float2* __restrict__ q,
-                                                         const double* __restrict__ out3, float2* __restrict__ sz2) {
+                                                         const double* __restrict__ out3, float2* __restrict__ sz2,
+                                                         BatchView bv) {
   // kGroup lanes per vertex; each lane sums every kGroup-th entry with a
   // compensated sum, the lane sums are combined in a fixed order.  The
   // size's relative error bound is the q-weighted mean of the element
@@ -587,7 +597,7 @@ __global__ void __launch_bounds__(kBlock) k_fast_average(DevMesh m, const float2
     // an element with a zero error (infinite q) or an unbounded deviation
     // leaves the size unbounded
     if (!(bmax < 1e30f) || !(bound <= 1e30f)) bound = 3.0e38f;
-    sz2[v] = make_float2((float)out3[2] * (tot / (float)(e - b)), bound);
+    sz2[v] = make_float2((float)batch_sf(bv, out3, v) * (tot / (float)(e - b)), bound);
   }
 }
 
@@ -705,12 +715,12 @@ void fast_merge_ref(ExpandList xl, const double* rec64, uint4* rec, cudaStream_t
 }
 
 void fast_error(const DevMesh& m, const uint4* td, const float2* geo, const uint4* rec, float2* q, double* partials,
-                int nb, cudaStream_t s) {
-  if (nb) k_fast_error<<<nb, kBlock, 0, s>>>(m, td, geo, rec, q, partials);
+                int nb, const int2* seg, cudaStream_t s) {
+  if (nb) k_fast_error<<<nb, kBlock, 0, s>>>(m, td, geo, rec, q, partials, seg);
 }
 
-void fast_average(const DevMesh& m, const float2* q, const double* out3, float2* sz2, cudaStream_t s) {
-  if (m.V) k_fast_average<<<nblk((long)m.V * kGroup), kBlock, 0, s>>>(m, q, out3, sz2);
+void fast_average(const DevMesh& m, const float2* q, const double* out3, float2* sz2, BatchView bv, cudaStream_t s) {
+  if (m.V) k_fast_average<<<nblk((long)m.V * kGroup), kBlock, 0, s>>>(m, q, out3, sz2, bv);
 }
 
 void fast_measure(const DevMesh& m, const float* half_len, const float2* sz2, uint32_t* split, uint32_t* collapse,

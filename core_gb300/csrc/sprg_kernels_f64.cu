@@ -505,6 +505,28 @@ __global__ void __launch_bounds__(kBlock) k_size_factor(const double* __restrict
   }
 }
 
+// one block per mesh of a batch: its segments' partials in a fixed order
+__global__ void __launch_bounds__(kBlock) k_size_factor_batch(const double* __restrict__ partials, BatchView bv,
+                                                              double* __restrict__ out4) {
+  __shared__ double sh[kBlock / 32];
+  const int k = blockIdx.x;
+  double a = 0, g = 0;
+  for (int i = bv.segoff[k] + threadIdx.x; i < bv.segoff[k + 1]; i += blockDim.x) {
+    a += partials[2 * i];
+    g += partials[2 * i + 1];
+  }
+  double snorm = block_sum(a, sh);
+  double gsum = block_sum(g, sh);
+  if (threadIdx.x == 0) {
+    const double r = bv.ratios[k];
+    const double esn = sqrt(snorm);
+    out4[4 * k] = snorm;
+    out4[4 * k + 1] = gsum;
+    out4[4 * k + 2] = pow(r * r * esn * esn / gsum, 0.5);
+    out4[4 * k + 3] = 0;
+  }
+}
+
 // apf::measure of a linear edge (N1 rule, w = 2)
 __device__ __forceinline__ double edge_measure(const V3& x0, const V3& x1) {
   V3 x[2] = {x0, x1};
@@ -895,14 +917,14 @@ __global__ void __launch_bounds__(128) k_guard_decide(DevMesh m, const double* _
                                                       const double* __restrict__ out3, GuardScratch g,
                                                       const int* __restrict__ items, const int* __restrict__ count,
                                                       int cap, uint32_t* split, uint32_t* collapse,
-                                                      int* __restrict__ unresolved) {
+                                                      int* __restrict__ unresolved, BatchView bv) {
   __shared__ double esz[4][2][kGuardMaxTets];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int n = min(*count, cap);
-  const double sf = out3[2];
   for (int it = blockIdx.x * 4 + warp; it < n; it += gridDim.x * 4) {
     const int e = items[it];
     const int ab[2] = {m.edv[2 * (size_t)e], m.edv[2 * (size_t)e + 1]};
+    const double sf = batch_sf(bv, out3, ab[0]);
     int cnt[2] = {m.a_off[ab[0] + 1] - m.a_off[ab[0]], m.a_off[ab[1] + 1] - m.a_off[ab[1]]};
     bool bad = cnt[0] > kGuardMaxTets || cnt[1] > kGuardMaxTets;
     if (!bad) {
@@ -1164,6 +1186,11 @@ void launch_size_factor(const double* partials, int n_blocks, int mode, double a
   k_size_factor<<<1, kBlock, 0, s>>>(partials, n_blocks, mode, adapt_ratio, target, dim, out3);
 }
 
+void launch_size_factor_batch(const double* partials, BatchView bv, int dim, double* out4, cudaStream_t s) {
+  (void)dim;  // p = 1: size_factor = (ratio^2 |eps*|^2 / G)^(1/2) in 2D and 3D
+  if (bv.n) k_size_factor_batch<<<bv.n, kBlock, 0, s>>>(partials, bv, out4);
+}
+
 void launch_esize_f64(const DevMesh& m, const double* err, const double* out3, int mode, double alpha, double beta,
                       double* esize, cudaStream_t s) {
   if (m.T) k_esize<<<nblk(m.T), kBlock, 0, s>>>(m, err, out3, mode, alpha, beta, esize);
@@ -1203,7 +1230,7 @@ void launch_quality_f64(const DevMesh& m, const double* size, const double* size
 
 void launch_guard_stage(int stage, const DevMesh& m, const double* u, const double* out3, const int* items,
                         const int* count, int cap, uint32_t* split, uint32_t* collapse, int* unresolved,
-                        GuardScratch g, cudaStream_t s) {
+                        GuardScratch g, BatchView bv, cudaStream_t s) {
   switch (stage) {
     case 0:
       cudaMemsetAsync(g.fit_count, 0, sizeof(int), s);
@@ -1218,7 +1245,7 @@ void launch_guard_stage(int stage, const DevMesh& m, const double* u, const doub
       k_guard_fit<<<152 * 8, 256, 0, s>>>(m, g.fit_items, g.fit_count, g.fit_cap, g, unresolved + 1);
       break;
     default:
-      k_guard_decide<<<152 * 2, 128, 0, s>>>(m, u, out3, g, items, count, cap, split, collapse, unresolved);
+      k_guard_decide<<<152 * 2, 128, 0, s>>>(m, u, out3, g, items, count, cap, split, collapse, unresolved, bv);
   }
 }
 

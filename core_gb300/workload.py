@@ -74,6 +74,28 @@ def aniso2d(n, seed=5):
     return m, boundary_layer_field(m.coords), aniso2d_params(n)
 
 
+def batch_boxes(n_meshes, seed=3, lo=4, hi=40, jitter=0.0):
+    """The batched workload: n_meshes unit tet boxes with n per side
+    log-uniform in [lo, hi] (seeded), each with its own field of 1-8 Gaussian
+    bumps (batched_field), flattened into one disjoint union.  Returns
+    (mesh, u, vert_offsets, elem_offsets, edge_offsets, ns)."""
+    from .mesh import Mesh
+    rng = np.random.Generator(np.random.PCG64(seed))
+    ns = np.rint(np.exp(rng.uniform(np.log(lo), np.log(hi), n_meshes))).astype(int)
+    parts, us = [], []
+    for k, n in enumerate(ns):
+        m = box(int(n), jitter=jitter, seed=seed * 1_000_003 + k)
+        parts.append(m)
+        us.append(batched_field(m.coords, seed * 1_000_003 + k))
+    voff = np.concatenate([[0], np.cumsum([p.n_verts for p in parts])]).astype(np.int64)
+    eoff = np.concatenate([[0], np.cumsum([p.n_elems for p in parts])]).astype(np.int64)
+    doff = np.concatenate([[0], np.cumsum([p.n_edges for p in parts])]).astype(np.int64)
+    coords = np.concatenate([p.coords for p in parts])
+    ev = np.concatenate([p.elem_verts + np.int32(voff[k]) for k, p in enumerate(parts)])
+    ed = np.concatenate([p.edge_verts + np.int32(voff[k]) for k, p in enumerate(parts)])
+    return Mesh(3, coords, ev, ed), np.concatenate(us), voff, eoff, doff, ns
+
+
 def config(name):
     """(mesh, field, adapt_ratio) of a named workload."""
     if name == "box8":

@@ -253,6 +253,20 @@ int sprg_box_counts(int nx, int ny, int nz, int64_t* n_verts, int64_t* n_elems, 
 int sprg_box_fill(int nx, int ny, int nz, double wx, double wy, double wz,
                   double* coords, int32_t* elem_verts, int32_t* edge_verts);
 
+/* ---- batch of independent meshes; no reference counterpart ------------
+   The context's mesh is the disjoint union of n_meshes meshes (entity ids
+   of mesh k offset by the sizes of meshes 0..k-1; vert_offsets and
+   elem_offsets hold n_meshes + 1 prefix sums).  The pass (SPRG_FP32) then
+   computes each mesh's own SelfProduct / Error integrals and size factor
+   with its own adapt ratio, as calling spr::getSPRSizeField once per mesh
+   does; the adapt_ratio argument of the pass is ignored.  n_meshes = 0
+   returns to a single mesh. */
+int sprg_set_batch(sprg_ctx* ctx, int n_meshes, const int64_t* vert_offsets, const int64_t* elem_offsets,
+                   const double* adapt_ratios);
+/* per mesh of the last batch pass: eps_star_norm2, error_sum, size_factor
+   (out: 3 n_meshes doubles) */
+int sprg_batch_info(sprg_ctx* ctx, double* out);
+
 /* ---- learned form (SPRG_LEARNED); no reference counterpart ------------
    eps*(v) = g_c + z * s_v / r_v with g_c the least-squares gradient of the
    vertex's neighbours, z an MLP (4 x 32 inputs -> 64 -> 64 -> 3, GELU, BF16

@@ -46,6 +46,11 @@ def metric_2d(H, eps, hmin, hmax):
 
 
 def _jacobi(A):
+    with np.errstate(over="ignore"):  # theta^2 may overflow: t = 0, as on the device
+        return _jacobi_sweeps(A)
+
+
+def _jacobi_sweeps(A):
     A = A.copy()
     Vm = np.eye(3)
     for _ in range(8):

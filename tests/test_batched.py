@@ -1,0 +1,52 @@
+"""The batched workload: many uneven boxes in one context (disjoint union),
+per-mesh size factors, FP32 with the FP64 guard band.
+
+Each mesh of the batch gets the marks of its own FP64 pass (identical) and
+its own size factor (within 1e-7 relative of the FP64 one), and the batch
+pass is bitwise repeatable.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_batch_matches_per_mesh_passes(gpu_lib):
+    import core_gb300 as cg
+    from core_gb300 import workload
+    from core_gb300.mesh import Mesh
+    m, u, voff, eoff, doff, ns = workload.batch_boxes(24, seed=7, lo=4, hi=12)
+    K = len(ns)
+    ratios = np.full(K, 0.1)
+    with cg.Context(m, precision="fp32") as c:
+        c.set_batch(voff, eoff, ratios)
+        size, flags, ns_, nc_, info = c.estimate_and_mark(u, 0.0 + 1.0)
+        per = c.batch_info()
+        size2, flags2, *_ = c.estimate_and_mark(u, 1.0)
+    assert np.array_equal(flags, flags2) and np.array_equal(size, size2)
+    for k in range(K):
+        mk = Mesh(3, m.coords[voff[k]:voff[k + 1]], m.elem_verts[eoff[k]:eoff[k + 1]] - voff[k],
+                  m.edge_verts[doff[k]:doff[k + 1]] - voff[k])
+        with cg.Context(mk, precision="fp64") as c64:
+            s64, f64, *_, i64 = c64.estimate_and_mark(u[voff[k]:voff[k + 1]], ratios[k])
+        assert np.array_equal(flags[doff[k]:doff[k + 1]], f64), k
+        assert abs(per[k, 2] - i64["size_factor"]) <= 1e-7 * i64["size_factor"]
+        sk = size[voff[k]:voff[k + 1]]
+        fin = np.isfinite(sk) & np.isfinite(s64)
+        rel = np.abs(sk[fin] - s64[fin]) / s64[fin]
+        assert np.median(rel) <= 1e-6
+
+
+def test_batch_rejects_bad_offsets(gpu_lib):
+    import core_gb300 as cg
+    from core_gb300 import workload
+    m, u, voff, eoff, doff, ns = workload.batch_boxes(3, seed=1, lo=4, hi=5)
+    with cg.Context(m, precision="fp32") as c:
+        bad = voff.copy()
+        bad[-1] -= 1
+        with pytest.raises(cg.SprgError):
+            c.set_batch(bad, eoff, np.full(3, 0.1))
+    with cg.Context(m, precision="fp64") as c:
+        c.set_batch(voff, eoff, np.full(3, 0.1))
+        with pytest.raises(cg.SprgError):
+            c.estimate_and_mark(u, 0.1)
