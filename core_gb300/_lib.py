@@ -45,7 +45,8 @@ EXPORTS = [
     "sprg_spr_size_from_recovered_noalloc", "sprg_debug_read",
     "sprg_set_mlp_params", "sprg_set_learned_options", "sprg_learned_features", "sprg_mlp_scratch_bytes",
     "sprg_mlp_forward", "sprg_mlp_grad", "sprg_mlp_adam", "sprg_hessian_metric",
-    "sprg_aniso_estimate_and_mark_resident", "sprg_set_batch", "sprg_batch_info",
+    "sprg_aniso_estimate_and_mark_resident", "sprg_set_batch", "sprg_batch_info", "sprg_set_autotune",
+    "sprg_tuning_report", "sprg_graph_capture", "sprg_graph_replay", "sprg_set_tiling",
 ]
 NOALLOC_MAX_ELEMS = 1 << 20
 
@@ -124,6 +125,12 @@ def load():
     F = ctypes.c_float
     lib.sprg_hessian_metric.argtypes = [P, P, D, D, D, P, P]
     lib.sprg_set_batch.argtypes = [P, I, P, P, P]
+    lib.sprg_set_autotune.argtypes = [P, I]
+    lib.sprg_set_tiling.argtypes = [P, P, I, I]
+    lib.sprg_tuning_report.argtypes = [P]
+    lib.sprg_tuning_report.restype = ctypes.c_char_p
+    lib.sprg_graph_capture.argtypes = [P, P, D, P, P]
+    lib.sprg_graph_replay.argtypes = [P]
     lib.sprg_batch_info.argtypes = [P, P]
     lib.sprg_aniso_estimate_and_mark_resident.argtypes = [P, P, D, D, D, P, P, P]
     lib.sprg_set_mlp_params.argtypes = [P, P, I]

@@ -200,6 +200,25 @@ class Context:
                                                      ctypes.byref(info)))
         return size, flags, ns.value, nc.value, info.as_dict()
 
+    # ---- launch shape and graphs ---------------------------------------------
+    def set_autotune(self, on=True):
+        self._check(self._lib.sprg_set_autotune(self.h, 1 if on else 0))
+
+    def set_tiling(self, lanes, tile_verts=256, blocks_per_sm=8):
+        l = np.ascontiguousarray(lanes, np.int32)
+        self._check(self._lib.sprg_set_tiling(self.h, l.ctypes.data, int(tile_verts), int(blocks_per_sm)))
+
+    def tuning_report(self):
+        import json
+        return json.loads(self._lib.sprg_tuning_report(self.h).decode())
+
+    def graph_capture(self, d_u, adapt_ratio, d_split_bits, d_collapse_bits):
+        """Capture the resident pass into a CUDA graph (needs set_stream)."""
+        self._check(self._lib.sprg_graph_capture(self.h, d_u, float(adapt_ratio), d_split_bits, d_collapse_bits))
+
+    def graph_replay(self):
+        self._check(self._lib.sprg_graph_replay(self.h))
+
     # ---- batch of meshes ---------------------------------------------------
     def set_batch(self, vert_offsets, elem_offsets, adapt_ratios):
         """Treat the context's mesh as a disjoint union of meshes (prefix

@@ -7,6 +7,7 @@
 #include <cstring>
 #include <map>
 #include <string>
+#include <algorithm>
 #include <vector>
 
 #include "spr_gb300.h"
@@ -52,6 +53,15 @@ struct sprg_ctx {
   int batch_n = 0, batch_nseg = 0;
   DevBuf bvoff, bseg, bsegoff, bratios;
   static constexpr int kSegTets = 2048;  // elements per error segment (8 per thread)
+  // binned recover: patch-size bins, tiles, tuned configuration
+  DevBuf pcls, bverts, btiles, bnext;
+  bool bins_ready = false, tuned = false, autotune = true;
+  int bin_count[4] = {0, 0, 0, 0};
+  int bin_lanes[4] = {4, 4, 4, 4};
+  int tile_verts = 256, grid_per_sm = 8, n_tiles = 0, n_sms = 152;
+  std::string tune_json;
+  // CUDA graph of the resident pass (sprg_graph_capture / sprg_graph_replay)
+  cudaGraphExec_t graph_exec = nullptr;
   DevBuf vvoff, vv, vtile, vr16, rec16, ql, sizel, fbitems, fbcount, mlp_packed, mlp_err, mlp_tmp;
   bool vv_ready = false, have_mlp = false;
   int use_mlp = 1;
@@ -435,7 +445,7 @@ int sprg_destroy(sprg_ctx* c) {
                     &c->out3,  &c->status,  &c->count, &c->xitems, &c->xcount, &c->slab, &c->bits,
                     &c->crec,  &c->vrec,    &c->rec32, &c->q32, &c->sz2,  &c->fcnt,   &c->guard, &c->tetd,
                     &c->wts,   &c->w64,     &c->listed, &c->geo, &c->geo64, &c->elen, &c->fitems, &c->gstamp, &c->gfit, &c->grec,
-                    &c->tstamp, &c->tslot,  &c->trec, &c->tcount, &c->hess, &c->bvoff, &c->bseg, &c->bsegoff, &c->bratios, &c->vvoff, &c->vv, &c->vtile, &c->vr16, &c->rec16,
+                    &c->tstamp, &c->tslot,  &c->trec, &c->tcount, &c->hess, &c->pcls, &c->bverts, &c->btiles, &c->bnext, &c->bvoff, &c->bseg, &c->bsegoff, &c->bratios, &c->vvoff, &c->vv, &c->vtile, &c->vr16, &c->rec16,
                     &c->ql,    &c->sizel,   &c->fbitems, &c->fbcount, &c->mlp_packed, &c->mlp_err, &c->mlp_tmp,
                     &c->cache64.v, &c->cache64.n, &c->cache64.el, &c->cache32.v, &c->cache32.n, &c->cache32.el};
   for (DevBuf* b : bufs) release(*b);
@@ -444,6 +454,7 @@ int sprg_destroy(sprg_ctx* c) {
     cudaStreamSynchronize(c->side);
     cudaStreamDestroy(c->side);
   }
+  if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
   if (c->fork) cudaEventDestroy(c->fork);
   if (c->join) cudaEventDestroy(c->join);
   if (c->own) cudaStreamDestroy(c->own);
@@ -720,6 +731,146 @@ static int listed_join(sprg_ctx* c, ExpandList xl, bool forked) {
   return listed_fits(c, c->cache32, nullptr, P<double>(c->f), 3, P<double>(c->rec), xl);
 }
 
+// patch-size bins of the non-listed vertices (stable: ascending ids within a
+// bin), once per mesh
+static int build_bins(sprg_ctx* c) {
+  if (c->bins_ready) return SPRG_OK;
+  DevMesh& m = c->m;
+  ENSURE(c->pcls, (size_t)m.V);
+  ENSURE(c->bverts, sizeof(int) * (size_t)m.V);
+  ENSURE(c->bnext, sizeof(int));
+  fast_patch_class(m, P<unsigned char>(c->listed), P<unsigned char>(c->pcls), c->stream);
+  std::vector<unsigned char> cls(m.V);
+  CK(cudaMemcpyAsync(cls.data(), c->pcls.p, (size_t)m.V, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  std::vector<int> order;
+  order.reserve(m.V);
+  for (int b = 0; b < 4; ++b) {
+    const size_t before = order.size();
+    for (int v = 0; v < m.V; ++v)
+      if (cls[v] == b) order.push_back(v);
+    c->bin_count[b] = (int)(order.size() - before);
+  }
+  CK(cudaMemcpy(c->bverts.p, order.data(), sizeof(int) * order.size(), cudaMemcpyHostToDevice));
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&c->n_sms, cudaDevAttrMultiProcessorCount, dev));
+  c->bins_ready = true;
+  return SPRG_OK;
+}
+
+// tiles (first, count, lanes, bin) of the current configuration; `only` >= 0
+// keeps one bin (autotuning)
+static int build_tiles(sprg_ctx* c, int only = -1) {
+  std::vector<int4> tiles;
+  int first = 0;
+  for (int b = 0; b < 4; ++b) {
+    for (int i = 0; i < c->bin_count[b]; i += c->tile_verts) {
+      const int n = std::min(c->tile_verts, c->bin_count[b] - i);
+      if (only < 0 || only == b) tiles.push_back(make_int4(first + i, n, c->bin_lanes[b], b));
+    }
+    first += c->bin_count[b];
+  }
+  ENSURE(c->btiles, sizeof(int4) * (tiles.empty() ? 1 : tiles.size()));
+  if (!tiles.empty())
+    CK(cudaMemcpy(c->btiles.p, tiles.data(), sizeof(int4) * tiles.size(), cudaMemcpyHostToDevice));
+  c->n_tiles = (int)tiles.size();
+  return SPRG_OK;
+}
+
+static void run_tiles(sprg_ctx* c, uint4* rec32) {
+  fast_recover_tiles(c->m, P<float>(c->wts), P<uint4>(c->tetd), rec32, P<int>(c->bverts), P<int4>(c->btiles),
+                     c->n_tiles, P<int>(c->bnext), c->n_sms * c->grid_per_sm, c->stream);
+}
+
+// CUDA-event time of the binned recover under the current configuration
+static float time_tiles(sprg_ctx* c, uint4* rec32, int only) {
+  if (build_tiles(c, only)) return 1e30f;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  for (int r = 0; r < 3; ++r) {
+    cudaEventRecord(e0, c->stream);
+    run_tiles(c, rec32);
+    cudaEventRecord(e1, c->stream);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best) best = ms;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return best;
+}
+
+// Autotuner (first pass, element gradients in place): coordinate descent
+// over lanes per bin {1, 2, 4}, tile size {64, 256, 1024} vertices and
+// blocks per SM {4, 8, 16}; every configuration gives bitwise the same
+// result, so the choice only changes time.  The choice and the timings are
+// kept for sprg_tuning_report.
+static int autotune(sprg_ctx* c, uint4* rec32) {
+  std::string log = "[";
+  auto note = [&](const char* what, int val, float ms) {
+    if (log.size() > 1) log += ",";
+    log += "{\"" + std::string(what) + "\":" + std::to_string(val) + ",\"ms\":" + std::to_string(ms) + "}";
+  };
+  for (int b = 0; b < 4; ++b) {
+    if (!c->bin_count[b]) continue;
+    int best_l = c->bin_lanes[b];
+    float best = 1e30f;
+    for (int l : {1, 2, 4}) {
+      c->bin_lanes[b] = l;
+      const float ms = time_tiles(c, rec32, b);
+      note(("lanes_bin" + std::to_string(b)).c_str(), l, ms);
+      if (ms < best) {
+        best = ms;
+        best_l = l;
+      }
+    }
+    c->bin_lanes[b] = best_l;
+  }
+  {
+    int best_t = c->tile_verts;
+    float best = 1e30f;
+    for (int t : {64, 256, 1024}) {
+      c->tile_verts = t;
+      const float ms = time_tiles(c, rec32, -1);
+      note("tile_verts", t, ms);
+      if (ms < best) {
+        best = ms;
+        best_t = t;
+      }
+    }
+    c->tile_verts = best_t;
+  }
+  {
+    int best_g = c->grid_per_sm;
+    float best = 1e30f;
+    for (int g : {4, 8, 16}) {
+      c->grid_per_sm = g;
+      const float ms = time_tiles(c, rec32, -1);
+      note("blocks_per_sm", g, ms);
+      if (ms < best) {
+        best = ms;
+        best_g = g;
+      }
+    }
+    c->grid_per_sm = best_g;
+  }
+  log += "]";
+  int rc = build_tiles(c);
+  if (rc) return rc;
+  c->tune_json = "{\"bins\":[" + std::to_string(c->bin_count[0]) + "," + std::to_string(c->bin_count[1]) + "," +
+                 std::to_string(c->bin_count[2]) + "," + std::to_string(c->bin_count[3]) + "],\"lanes\":[" +
+                 std::to_string(c->bin_lanes[0]) + "," + std::to_string(c->bin_lanes[1]) + "," +
+                 std::to_string(c->bin_lanes[2]) + "," + std::to_string(c->bin_lanes[3]) +
+                 "],\"tile_verts\":" + std::to_string(c->tile_verts) +
+                 ",\"blocks_per_sm\":" + std::to_string(c->grid_per_sm) + ",\"timings\":" + log + "}";
+  c->tuned = true;
+  return check_launch(c, "autotune");
+}
+
 // FP32 pass: packed double-float records, FP32 fits and sweeps, FP64
 // reference path for ill-conditioned or growing patches (sprg_kernels_f32.cu).
 static int pass_fast(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_t* d_collapse) {
@@ -760,8 +911,13 @@ static int pass_fast(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_
   PB("tet_f32");
   fast_tet(m, vrec, P<uint4>(c->tetd), c->stream);
   PE();
+  if (!c->bins_ready) {
+    if ((rc = build_bins(c))) return rc;
+    if ((rc = build_tiles(c))) return rc;
+  }
+  if (c->autotune && !c->tuned && (rc = autotune(c, rec32))) return rc;
   PB("recover_f32");
-  fast_recover(m, P<float>(c->wts), P<unsigned char>(c->listed), P<uint4>(c->tetd), rec32, c->stream);
+  run_tiles(c, rec32);
   PE();
   if ((rc = listed_join(c, xl, fork))) return rc;
   PB("merge_f64");
@@ -1245,6 +1401,81 @@ int sprg_batch_info(sprg_ctx* c, double* out) {
   for (int k = 0; k < c->batch_n; ++k)
     for (int j = 0; j < 3; ++j) out[3 * (size_t)k + j] = o4[4 * (size_t)k + j];
   return SPRG_OK;
+}
+
+int sprg_set_autotune(sprg_ctx* c, int on) {
+  if (!c) return SPRG_EINVAL;
+  c->autotune = on != 0;
+  return SPRG_OK;
+}
+
+const char* sprg_tuning_report(sprg_ctx* c) {
+  if (!c) return "";
+  if (c->tune_json.empty()) {
+    c->tune_json = "{\"bins\":[" + std::to_string(c->bin_count[0]) + "," + std::to_string(c->bin_count[1]) + "," +
+                   std::to_string(c->bin_count[2]) + "," + std::to_string(c->bin_count[3]) + "],\"lanes\":[" +
+                   std::to_string(c->bin_lanes[0]) + "," + std::to_string(c->bin_lanes[1]) + "," +
+                   std::to_string(c->bin_lanes[2]) + "," + std::to_string(c->bin_lanes[3]) +
+                   "],\"tile_verts\":" + std::to_string(c->tile_verts) +
+                   ",\"blocks_per_sm\":" + std::to_string(c->grid_per_sm) + ",\"tuned\":false}";
+  }
+  return c->tune_json.c_str();
+}
+
+int sprg_graph_capture(sprg_ctx* c, const double* d_u, double adapt_ratio, uint32_t* d_split_bits,
+                       uint32_t* d_collapse_bits) {
+  if (!c || !d_u || !d_split_bits || !d_collapse_bits) return SPRG_EINVAL;
+  int rc = set_device(c);
+  if (rc) return rc;
+  if (c->stream == c->own || c->stream == nullptr)
+    return fail(c, SPRG_ESTATE, "graph capture needs a caller stream (sprg_set_stream)");
+  // one ordinary pass first: buffers, per-mesh setup, patch cache and tuning
+  if ((rc = sprg_estimate_and_mark_resident(c, d_u, adapt_ratio, d_split_bits, d_collapse_bits))) return rc;
+  CK(cudaStreamSynchronize(c->stream));
+  const bool prof = c->prof;
+  c->prof = false;
+  if (c->graph_exec) {
+    cudaGraphExecDestroy(c->graph_exec);
+    c->graph_exec = nullptr;
+  }
+  CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  rc = sprg_estimate_and_mark_resident(c, d_u, adapt_ratio, d_split_bits, d_collapse_bits);
+  cudaGraph_t graph = nullptr;
+  cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
+  c->prof = prof;
+  if (rc) {
+    if (graph) cudaGraphDestroy(graph);
+    return rc;
+  }
+  if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamEndCapture");
+  e = cudaGraphInstantiate(&c->graph_exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return cuda_fail(c, e, "cudaGraphInstantiate");
+  return SPRG_OK;
+}
+
+int sprg_graph_replay(sprg_ctx* c) {
+  if (!c) return SPRG_EINVAL;
+  if (!c->graph_exec) return fail(c, SPRG_ESTATE, "no captured graph (sprg_graph_capture)");
+  int rc = set_device(c);
+  if (rc) return rc;
+  CK(cudaGraphLaunch(c->graph_exec, c->stream));
+  return SPRG_OK;
+}
+
+int sprg_set_tiling(sprg_ctx* c, const int* lanes, int tile_verts, int blocks_per_sm) {
+  if (!c || !lanes || tile_verts <= 0 || blocks_per_sm <= 0) return SPRG_EINVAL;
+  for (int b = 0; b < 4; ++b)
+    if (lanes[b] != 1 && lanes[b] != 2 && lanes[b] != 4) return fail(c, SPRG_EINVAL, "lanes per vertex: 1, 2 or 4");
+  int rc = set_device(c);
+  if (rc) return rc;
+  for (int b = 0; b < 4; ++b) c->bin_lanes[b] = lanes[b];
+  c->tile_verts = tile_verts;
+  c->grid_per_sm = blocks_per_sm;
+  c->autotune = false;
+  c->tuned = true;
+  c->tune_json.clear();
+  return c->bins_ready ? build_tiles(c) : SPRG_OK;
 }
 
 }  // extern "C"

@@ -19,9 +19,13 @@ void fast_tet(const DevMesh& m, const float4* vrec, uint4* td, cudaStream_t s);
 void fast_weights(const DevMesh& m, float* w, double* w64, ExpandList xl, int* n_refit, unsigned char* listed,
                   cudaStream_t s);
 // recovered value per vertex as value + packed remainder (16 bytes)
-void fast_recover(const DevMesh& m, const float* w, const unsigned char* listed, const uint4* td, uint4* rec,
-                  cudaStream_t s);
 void fast_merge_ref(ExpandList xl, const double* rec64, uint4* rec32, cudaStream_t s);
+// patch-size class per vertex: 0 (<= 8 elements), 1 (<= 16), 2 (<= 32), 3, 4 = listed
+void fast_patch_class(const DevMesh& m, const unsigned char* listed, unsigned char* cls, cudaStream_t s);
+// binned recover: tiles (first, count, lanes in {1, 2, 4}, bin) over verts, taken
+// from a counter by a persistent grid; every tiling gives the same bits
+void fast_recover_tiles(const DevMesh& m, const float* w, const uint4* td, uint4* rec, const int* verts,
+                        const int4* tiles, int n_tiles, int* next, int grid, cudaStream_t s);
 // q: (h_max err^(-1/5), its relative error bound) per tet
 // seg (batch): one element range per block, nb = number of segments
 void fast_error(const DevMesh& m, const uint4* td, const float2* geo, const uint4* rec, float2* q, double* partials,

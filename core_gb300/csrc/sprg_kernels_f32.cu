@@ -43,7 +43,7 @@ namespace sprg {
 namespace {
 
 constexpr int kBlock = 256;
-constexpr int kGroup = 4;  // lanes per vertex in the recover kernel
+constexpr int kGroup = 4;  // lanes per vertex in the average kernel
 // relative accuracy assumed for each quantity entering an element-error
 // deviation (about 4 FP32 ulps), scaled into the error bound of q_t; on the
 // 160^3 workload the largest observed error is 0.43 of the resulting bound
@@ -381,56 +381,110 @@ __global__ void __launch_bounds__(kBlock) k_fast_weights(DevMesh m, float* __res
 }
 
 // ---------------------------------------------------------------------------
-// recover: eps*(v) = g_ref + sum_t w_vt ((g_t - g_ref) + d_t), kGroup lanes
-// per vertex, stored as the pair (g_ref, deviation)
+// recover: eps*(v) = g_ref + sum_t w_vt ((s_t - g_ref) + r_t), stored as the
+// value + packed remainder pair.  Vertices are binned by patch size; one
+// persistent grid takes tiles (first, count, lanes, bin) from a counter and
+// gives a tile's vertices `lanes` lanes each.  Lane l sums the elements
+// k = l, l + L, ... of the patch into the class sums x_{k mod 4} (each in
+// increasing k) and the classes are combined as (x0 + x1) + (x2 + x3): the
+// same operations for every lane count, so every tiling gives bitwise the
+// same result.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kBlock) k_fast_recover(DevMesh m, const float* __restrict__ w,
-                                                         const unsigned char* __restrict__ listed,
-                                                         const uint4* __restrict__ td, uint4* __restrict__ rec) {
-  const int gid = blockIdx.x * blockDim.x + threadIdx.x;
-  const int v = gid / kGroup;
-  const int gl = gid % kGroup;
-  const int lane = threadIdx.x & 31;
-  const int leader = lane & ~(kGroup - 1);
-  const bool active = v < m.V && !listed[v];
-  int beg = 0, cnt = 0;
-  float gr0 = 0.f, gr1 = 0.f, gr2 = 0.f;
-  if (active) {
-    beg = m.p_off[v];
-    cnt = m.p_off[v + 1] - beg;
-    if (gl == 0) {
-      uint4 a = __ldg(td + m.p_el[beg]);
-      gr0 = __uint_as_float(a.x); gr1 = __uint_as_float(a.y); gr2 = __uint_as_float(a.z);
+template <int L>
+__device__ __forceinline__ void recover_tile(const DevMesh& m, const float* __restrict__ w,
+                                             const uint4* __restrict__ td, uint4* __restrict__ rec,
+                                             const int* __restrict__ verts, int first, int count) {
+  constexpr int NX = 4 / L;
+  const int gl = threadIdx.x % L, slot = threadIdx.x / L;
+  const int lane = threadIdx.x & 31, leader = lane & ~(L - 1);
+  for (int i0 = 0; i0 < count; i0 += blockDim.x / L) {
+    const int i = i0 + slot;
+    const bool active = i < count;
+    const int v = active ? __ldg(verts + first + i) : 0;
+    int beg = 0, cnt = 0;
+    float gr0 = 0.f, gr1 = 0.f, gr2 = 0.f;
+    if (active) {
+      beg = m.p_off[v];
+      cnt = m.p_off[v + 1] - beg;
+      if (gl == 0) {
+        const uint4 a = __ldg(td + m.p_el[beg]);
+        gr0 = __uint_as_float(a.x); gr1 = __uint_as_float(a.y); gr2 = __uint_as_float(a.z);
+      }
+    }
+    if (L > 1) {
+      gr0 = __shfl_sync(0xffffffffu, gr0, leader);
+      gr1 = __shfl_sync(0xffffffffu, gr1, leader);
+      gr2 = __shfl_sync(0xffffffffu, gr2, leader);
+    }
+    float x[NX][3];
+#pragma unroll
+    for (int c = 0; c < NX; ++c) x[c][0] = x[c][1] = x[c][2] = 0.f;
+    for (int k = gl; k < cnt; k += L) {
+      const int t = __ldg(m.p_el + beg + k);
+      const float wk = __ldg(w + beg + k);
+      const Grad g = unpack_grad(__ldg(td + t));
+      const int c = (k & 3) / L;
+#pragma unroll
+      for (int cc = 0; cc < NX; ++cc)
+        if (cc == c) {
+          x[cc][0] = fmaf(wk, (g.s[0] - gr0) + g.r[0], x[cc][0]);
+          x[cc][1] = fmaf(wk, (g.s[1] - gr1) + g.r[1], x[cc][1]);
+          x[cc][2] = fmaf(wk, (g.s[2] - gr2) + g.r[2], x[cc][2]);
+        }
+    }
+    float tot[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      if (L == 4) {
+        float a = x[0][d];
+        a += __shfl_xor_sync(0xffffffffu, a, 1);
+        a += __shfl_xor_sync(0xffffffffu, a, 2);
+        tot[d] = a;
+      } else if (L == 2) {
+        const float a = x[0][d] + __shfl_xor_sync(0xffffffffu, x[0][d], 1);
+        const float b = x[NX - 1][d] + __shfl_xor_sync(0xffffffffu, x[NX - 1][d], 1);
+        tot[d] = a + b;
+      } else {
+        tot[d] = (x[0][d] + x[NX > 1 ? 1 : 0][d]) + (x[NX > 2 ? 2 : 0][d] + x[NX > 3 ? 3 : 0][d]);
+      }
+    }
+    if (active && gl == 0) {
+      float s0, s1, s2, r0, r1, r2;
+      two_sum(gr0, tot[0], s0, r0);
+      two_sum(gr1, tot[1], s1, r1);
+      two_sum(gr2, tot[2], s2, r2);
+      rec[v] = make_uint4(__float_as_uint(s0), __float_as_uint(s1), __float_as_uint(s2),
+                          pack_corr(s0, s1, s2, r0, r1, r2));
     }
   }
-  gr0 = __shfl_sync(0xffffffffu, gr0, leader);
-  gr1 = __shfl_sync(0xffffffffu, gr1, leader);
-  gr2 = __shfl_sync(0xffffffffu, gr2, leader);
-  float x0 = 0.f, x1 = 0.f, x2 = 0.f;
-#pragma unroll 2
-  for (int k = gl; k < cnt; k += kGroup) {
-    const int t = __ldg(m.p_el + beg + k);
-    const float wk = __ldg(w + beg + k);
-    Grad g = unpack_grad(__ldg(td + t));
-    x0 = fmaf(wk, (g.s[0] - gr0) + g.r[0], x0);
-    x1 = fmaf(wk, (g.s[1] - gr1) + g.r[1], x1);
-    x2 = fmaf(wk, (g.s[2] - gr2) + g.r[2], x2);
+}
+
+__global__ void __launch_bounds__(kBlock) k_fast_recover_tiles(DevMesh m, const float* __restrict__ w,
+                                                               const uint4* __restrict__ td, uint4* __restrict__ rec,
+                                                               const int* __restrict__ verts,
+                                                               const int4* __restrict__ tiles, int n_tiles,
+                                                               int* __restrict__ next) {
+  __shared__ int cur;
+  for (;;) {
+    if (threadIdx.x == 0) cur = atomicAdd(next, 1);
+    __syncthreads();
+    const int t = cur;
+    __syncthreads();
+    if (t >= n_tiles) return;
+    const int4 tile = tiles[t];  // (first, count, lanes, bin)
+    if (tile.z == 1) recover_tile<1>(m, w, td, rec, verts, tile.x, tile.y);
+    else if (tile.z == 2) recover_tile<2>(m, w, td, rec, verts, tile.x, tile.y);
+    else recover_tile<4>(m, w, td, rec, verts, tile.x, tile.y);
   }
-#pragma unroll
-  for (int o = 1; o < kGroup; o <<= 1) {
-    x0 += __shfl_xor_sync(0xffffffffu, x0, o);
-    x1 += __shfl_xor_sync(0xffffffffu, x1, o);
-    x2 += __shfl_xor_sync(0xffffffffu, x2, o);
-  }
-  if (active && gl == 0) {
-    // eps*(v) = g_ref + x exactly as s + r (TwoSum), stored like a tet gradient
-    float s0, s1, s2, r0, r1, r2;
-    two_sum(gr0, x0, s0, r0);
-    two_sum(gr1, x1, s1, r1);
-    two_sum(gr2, x2, s2, r2);
-    rec[v] = make_uint4(__float_as_uint(s0), __float_as_uint(s1), __float_as_uint(s2),
-                        pack_corr(s0, s1, s2, r0, r1, r2));
-  }
+}
+
+// patch-size class of a vertex: <= 8, <= 16, <= 32, more elements
+__device__ __forceinline__ int patch_class(int cnt) { return cnt <= 8 ? 0 : cnt <= 16 ? 1 : cnt <= 32 ? 2 : 3; }
+
+__global__ void k_patch_class(DevMesh m, const unsigned char* __restrict__ listed, unsigned char* __restrict__ cls) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= m.V) return;
+  cls[v] = listed[v] ? 4 : (unsigned char)patch_class(m.p_off[v + 1] - m.p_off[v]);
 }
 
 // listed vertices take the FP64 reference result, as value + packed remainder
@@ -705,9 +759,15 @@ void fast_weights(const DevMesh& m, float* w, double* w64, ExpandList xl, int* n
   if (m.V) k_fast_weights<<<nblk(m.V), kBlock, 0, s>>>(m, w, w64, xl, n_refit, listed);
 }
 
-void fast_recover(const DevMesh& m, const float* w, const unsigned char* listed, const uint4* td, uint4* rec,
-                  cudaStream_t s) {
-  if (m.V) k_fast_recover<<<nblk((long)m.V * kGroup), kBlock, 0, s>>>(m, w, listed, td, rec);
+
+void fast_patch_class(const DevMesh& m, const unsigned char* listed, unsigned char* cls, cudaStream_t s) {
+  if (m.V) k_patch_class<<<nblk(m.V), kBlock, 0, s>>>(m, listed, cls);
+}
+
+void fast_recover_tiles(const DevMesh& m, const float* w, const uint4* td, uint4* rec, const int* verts,
+                        const int4* tiles, int n_tiles, int* next, int grid, cudaStream_t s) {
+  cudaMemsetAsync(next, 0, sizeof(int), s);
+  if (n_tiles) k_fast_recover_tiles<<<grid, kBlock, 0, s>>>(m, w, td, rec, verts, tiles, n_tiles, next);
 }
 
 void fast_merge_ref(ExpandList xl, const double* rec64, uint4* rec, cudaStream_t s) {

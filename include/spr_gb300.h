@@ -267,6 +267,26 @@ int sprg_set_batch(sprg_ctx* ctx, int n_meshes, const int64_t* vert_offsets, con
    (out: 3 n_meshes doubles) */
 int sprg_batch_info(sprg_ctx* ctx, double* out);
 
+/* ---- launch shape and graphs; no reference counterpart ----------------
+   The FP32 recovery runs over patch-size bins (<= 8, <= 16, <= 32, more
+   elements) in one persistent launch; on the first pass of a mesh an
+   autotuner times lanes per bin, tile size and blocks per SM on the real
+   data (every choice gives bitwise the same result).  on = 0 keeps the
+   default configuration. */
+int sprg_set_autotune(sprg_ctx* ctx, int on);
+/* fix the binned recovery's configuration (lanes per bin in {1, 2, 4}, tile
+   size in vertices, blocks per SM); turns the autotuner off */
+int sprg_set_tiling(sprg_ctx* ctx, const int* lanes, int tile_verts, int blocks_per_sm);
+/* JSON: bin sizes, chosen configuration, the autotuner's timings */
+const char* sprg_tuning_report(sprg_ctx* ctx);
+/* Capture the resident pass (sprg_estimate_and_mark_resident with these
+   device buffers) into a CUDA graph, after one ordinary pass; needs a caller
+   stream (sprg_set_stream).  sprg_graph_replay relaunches it on that stream:
+   the caller refreshes d_u in place between replays. */
+int sprg_graph_capture(sprg_ctx* ctx, const double* d_u, double adapt_ratio, uint32_t* d_split_bits,
+                       uint32_t* d_collapse_bits);
+int sprg_graph_replay(sprg_ctx* ctx);
+
 /* ---- learned form (SPRG_LEARNED); no reference counterpart ------------
    eps*(v) = g_c + z * s_v / r_v with g_c the least-squares gradient of the
    vertex's neighbours, z an MLP (4 x 32 inputs -> 64 -> 64 -> 3, GELU, BF16

@@ -50,3 +50,58 @@ def test_batch_rejects_bad_offsets(gpu_lib):
         c.set_batch(voff, eoff, np.full(3, 0.1))
         with pytest.raises(cg.SprgError):
             c.estimate_and_mark(u, 0.1)
+
+
+def test_tilings_give_identical_bits(gpu_lib):
+    import core_gb300 as cg
+    from core_gb300 import workload
+    m, u, voff, eoff, doff, ns = workload.batch_boxes(16, seed=9, lo=4, hi=24, jitter=0.2)
+    ratios = np.full(len(ns), 0.05)
+    runs = []
+    report = None
+    for cfg in [None, ([4, 4, 4, 4], 256, 8), ([1, 1, 1, 1], 64, 4), ([2, 1, 4, 2], 1024, 16)]:
+        with cg.Context(m, precision="fp32") as c:
+            c.set_batch(voff, eoff, ratios)
+            if cfg is not None:
+                c.set_tiling(*cfg)
+            size, flags, *_ = c.estimate_and_mark(u, 1.0)
+            if cfg is None:
+                report = c.tuning_report()
+        runs.append((size, flags))
+    for size, flags in runs[1:]:
+        assert np.array_equal(size, runs[0][0], equal_nan=True) and np.array_equal(flags, runs[0][1])
+    assert sum(report["bins"]) > 0 and len(report["lanes"]) == 4 and report["timings"]
+    assert set(report["lanes"]) <= {1, 2, 4}
+
+
+def test_graph_replay_matches_direct_passes(gpu_lib):
+    import torch
+    import core_gb300 as cg
+    from core_gb300 import workload
+    m = workload.box(20, jitter=0.2, seed=3)
+    u1 = workload.bump_field(m.coords, seed=3)
+    u2 = workload.bump_field(m.coords, seed=5)
+    E = m.n_edges
+    nw = (E + 31) // 32
+    with cg.Context(m, precision="fp32") as c:
+        stream = torch.cuda.Stream()
+        torch.cuda.set_stream(stream)
+        c.set_stream(stream.cuda_stream)
+        d_u = torch.from_numpy(u1).cuda()
+        bits = torch.zeros(2 * nw, dtype=torch.int32, device="cuda")
+        ps, pc = bits.data_ptr(), bits.data_ptr() + 4 * nw
+        direct = []
+        for uu in (u1, u2):
+            d_u.copy_(torch.from_numpy(uu))
+            bits.zero_()
+            c.estimate_and_mark_resident(d_u.data_ptr(), 0.001, ps, pc)
+            torch.cuda.synchronize()
+            direct.append(bits.cpu().numpy().copy())
+        d_u.copy_(torch.from_numpy(u1))
+        c.graph_capture(d_u.data_ptr(), 0.001, ps, pc)
+        for uu, want in zip((u1, u2, u1), (direct[0], direct[1], direct[0])):
+            d_u.copy_(torch.from_numpy(uu))
+            bits.zero_()
+            c.graph_replay()
+            torch.cuda.synchronize()
+            assert np.array_equal(bits.cpu().numpy(), want)
