@@ -39,7 +39,12 @@ def parse():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--precision", default="fp32", choices=["fp64", "fp32"])
+    p.add_argument("--precision", default="fp32", choices=["fp64", "fp32", "learned"],
+                   help="form of the headline line: plain FP32 (exact marks), FP64, or learned")
+    p.add_argument("--workload", default="jbox", choices=["jbox", "batched", "aniso2d"],
+                   help="jbox: 160^3 jittered box (the headline); batched: 4096 uneven boxes; "
+                        "aniso2d: 4096^2 anisotropic square")
+    p.add_argument("--no-compare", action="store_true", help="skip the learned / FP64 comparison blocks")
     p.add_argument("--n", type=int, default=160, help="box cells per side (160 -> 24.6M tets)")
     p.add_argument("--adapt-ratio", type=float, default=0.008,
                    help="getSPRSizeField adapt ratio (0.008 gives a balanced split/collapse mix at 160^3)")
@@ -93,6 +98,13 @@ def algorithmic_bytes(kernel, V, T, E, vb=8):
         "error_f32": 4 * ib * T + 16 * T + 8 * T + 16 * V + 8 * T,
         "average_f32": ib * (V + 1) + 4 * ib * T + 8 * T + 8 * V,
         "measure_f32": 2 * ib * E + 4 * E + 8 * V + E // 4,
+        # learned form: 16-byte vertex records in, 32-byte records out of the
+        # network kernel, FP32 element errors
+        "prep_l": 8 * V + 16 * V + 16 * V,
+        "mlp_l": ib * (V + 1) + 2 * ib * E + 16 * V + 32 * V,
+        "error_l": 4 * ib * T + 32 * V + 8 * T + 4 * T,
+        "average_l": ib * (V + 1) + 4 * ib * T + 4 * T + 4 * V,
+        "measure_l": 2 * ib * E + 4 * E + 4 * V + E // 4,
     }
     return table.get(kernel)
 
@@ -210,6 +222,46 @@ def reference_arm(args):
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
+def time_form(m, u, precision, ratio, steps, dev, s64=None, f64=None):
+    """Resident pass of one form on the same mesh: ms per pass (CUDA events
+    on the launching stream, after warm-up) and, given the FP64 sizes and
+    flags, the size error and mark agreement of its host-API result."""
+    import torch
+    import core_gb300 as cg
+    E = m.n_edges
+    nw = (E + 31) // 32
+    with cg.Context(m, device=dev.index or 0, precision=precision) as c:
+        st = torch.cuda.Stream(dev)
+        c.set_stream(st.cuda_stream)
+        d_u = torch.from_numpy(u).to(dev)
+        bits = torch.zeros(2 * nw, dtype=torch.int32, device=dev)
+        ps, pc = bits.data_ptr(), bits.data_ptr() + 4 * nw
+        for _ in range(3):
+            c.estimate_and_mark_resident(d_u.data_ptr(), ratio, ps, pc)
+        torch.cuda.synchronize(dev)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(steps):
+            c.estimate_and_mark_resident(d_u.data_ptr(), ratio, ps, pc)
+        e1.record(st)
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1) / steps
+        out = {"ms_per_step": ms, "value": m.n_verts / (ms / 1e3), "unit": UNIT, "gpu_launches_per_step":
+               int(c.last_launch_count)}
+        if s64 is not None:
+            c.set_stream(0)
+            s, f, _, _, info = c.estimate_and_mark(u, ratio)
+            fin = np.isfinite(s) & np.isfinite(s64)
+            rel = np.abs(s[fin] - s64[fin]) / np.abs(s64[fin])
+            out.update({"size_rel_err_median": float(np.median(rel)), "size_rel_err_p99": float(np.percentile(rel, 99)),
+                        "size_rel_err_max": float(rel.max()), "mark_agreement": float(np.mean(f == f64)),
+                        "marks_identical": bool(np.array_equal(f, f64))})
+            if precision == "learned":
+                out["fallback_vertices"] = int(info["n_learned_fallback"])
+    return out
+
+
 def gpu_arm(args):
     import torch
     import torch.distributed as dist
@@ -297,17 +349,27 @@ def gpu_arm(args):
 
     # accuracy of the FP32 result against the FP64 path, outside the timed region
     acc = None
-    if args.precision == "fp32" and not args.no_accuracy and rank == 0:
-        ctx.set_stream(0)
-        s32, f32, *_ = ctx.estimate_and_mark(u, args.adapt_ratio)
+    compare = None
+    if rank == 0 and not (args.no_accuracy and args.no_compare):
         with cg.Context(m, device=local, precision="fp64") as c64:
             s64, f64, *_ = c64.estimate_and_mark(u, args.adapt_ratio)
-        rel = np.abs(s32 - s64) / np.abs(s64)
+    if args.precision != "fp64" and not args.no_accuracy and rank == 0:
+        ctx.set_stream(0)
+        s32, f32, *_ = ctx.estimate_and_mark(u, args.adapt_ratio)
+        fin = np.isfinite(s32) & np.isfinite(s64)
+        rel = np.abs(s32[fin] - s64[fin]) / np.abs(s64[fin])
         acc = {"size_rel_err_max": float(rel.max()), "size_rel_err_p99": float(np.percentile(rel, 99)),
                "size_rel_err_median": float(np.median(rel)), "mark_agreement": float(np.mean(f32 == f64)),
                "marks_identical": bool(np.array_equal(f32, f64)),
                "against": "FP64 path (equal to the oracle within 1e-10 relative)"}
         ctx.set_stream(stream.cuda_stream)
+    if rank == 0 and not args.no_compare:
+        # the learned-vs-plain comparison of the metric, and the FP64 path
+        compare = {}
+        for form in ("fp32", "learned", "fp64"):
+            if form == args.precision:
+                continue
+            compare[form] = time_form(m, u, form, args.adapt_ratio, args.steps if form != "fp64" else 3, dev, s64, f64)
 
     if rank != 0:
         ctx.close()
@@ -332,10 +394,21 @@ def gpu_arm(args):
         vb = 8 if args.precision == "fp64" else 4
         byts = algorithmic_bytes(dom, V, T, E, vb)
         traffic = None
+        if dom == "mlp_l":
+            # the network kernel is a contraction: tensor FLOPs per vertex
+            # (K = 64 first layer for <= 16 neighbours: 64x64 + 64x64 + 16x64 MACs)
+            flops = 2.0 * (64 * 64 + 64 * 64 + 16 * 64) * V
+            tf = peaks.get("bf16_tflops") or 1900.0
+            ach = flops / (avg / 1e3) / 1e12
+            roof = {"bound": "tensor", "kernel": dom, "achieved": ach, "peak": tf, "unit": "TFLOP/s",
+                    "frac": ach / tf, "traffic": None, "algorithmic_flops": flops, "avg_ms": avg,
+                    "peak_source": "measured (MEASURED_PEAKS.json bf16_tflops)" if peaks.get("bf16_tflops")
+                    else "fallback 1900 TFLOP/s"}
+            byts = None
         tf = os.path.join(ROOT, "profiles", "traffic.json")
         if os.path.exists(tf):
             traffic = json.load(open(tf)).get(f"{dom}@{args.n}")
-        if byts:
+        if byts and dom != "mlp_l":
             ach = byts / (avg / 1e3) / 1e9
             roof = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": hbm, "unit": "GB/s",
                     "frac": ach / hbm, "traffic": traffic, "algorithmic_bytes": byts, "avg_ms": avg,
@@ -350,11 +423,12 @@ def gpu_arm(args):
             cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": f"unavailable: {e}"}
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
-           "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32",
+           "scaling": "weak", "vs_baseline": None,
+           "dtype": {"fp64": "f64", "fp32": "f32", "learned": "bf16/f32"}[args.precision],
            "data": "synthetic", "config": dict(workload_desc(args.n, args.precision, args.adapt_ratio),
                                                  form="plain " + args.precision.upper()), "roofline": roof,
            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches_per_step * args.steps),
-           "clocks": clk, "phases": phases, "accuracy": acc,
+           "clocks": clk, "phases": phases, "accuracy": acc, "forms": compare,
            "pass_roofline": {"algorithmic_bytes": pass_bytes(V, T, E),
                              "achieved": pass_bytes(V, T, E) / (ms_max / args.steps / 1e3) / 1e9, "peak": hbm,
                              "unit": "GB/s",
@@ -366,10 +440,114 @@ def gpu_arm(args):
         dist.destroy_process_group()
 
 
+def gpu_batched(args):
+    """The batched workload: 4096 uneven boxes (n log-uniform in [4, 40],
+    1-8 bumps each) in one context, FP32 with the FP64 guard, autotuned
+    binned recovery, the pass replayed from a CUDA graph."""
+    import torch
+    import core_gb300 as cg
+    from core_gb300 import workload
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    t0 = time.perf_counter()
+    m, u, voff, eoff, doff, ns = workload.batch_boxes(4096, seed=3)
+    t_mesh = time.perf_counter() - t0
+    V, T, E = m.n_verts, m.n_elems, m.n_edges
+    nw = (E + 31) // 32
+    with cg.Context(m, precision="fp32") as c:
+        c.set_batch(voff, eoff, np.full(len(ns), 0.1))
+        st = torch.cuda.Stream(dev)
+        torch.cuda.set_stream(st)
+        c.set_stream(st.cuda_stream)
+        d_u = torch.from_numpy(u).to(dev)
+        bits = torch.zeros(2 * nw, dtype=torch.int32, device=dev)
+        ps, pc = bits.data_ptr(), bits.data_ptr() + 4 * nw
+        c.graph_capture(d_u.data_ptr(), 1.0, ps, pc)
+        for _ in range(args.warmup):
+            c.graph_replay()
+        clocks = ClockSampler(0)
+        clocks.start()
+        time.sleep(0.3)
+        torch.cuda.synchronize(dev)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(args.steps):
+            c.graph_replay()
+        e1.record(st)
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1) / args.steps
+        clk = clocks.stop()
+        tune = c.tuning_report()
+        c.set_stream(0)
+        _, _, _, _, info = c.estimate_and_mark(u, 1.0)
+    out = {"metric": METRIC, "value": V / (ms / 1e3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": f"4096 unit tet boxes, n per side log-uniform in [4, 40] (seed 3), 1-8 Gaussian "
+                                  f"bumps each; {V} vertices, {T} tets, {E} edges; adapt ratio 0.1 per mesh",
+                      "form": "plain FP32, batched, CUDA graph", "l2": "inputs larger than L2"},
+           "tuning": tune, "guard_edges": int(info["n_guard_edges"]), "clocks": clk,
+           "setup_s": {"mesh_build": round(t_mesh, 2)}}
+    print(json.dumps(out), flush=True)
+
+
+def gpu_aniso2d(args):
+    """The 2D anisotropic workload: 4096^2 square (33.5M triangles), nodal
+    Hessian by two SPR recoveries, metric, AnisoSizeField measure, marks and
+    quality, FP64."""
+    import torch
+    import core_gb300 as cg
+    from core_gb300 import workload
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    n = 4096
+    m, u, (eps, hmin, hmax) = workload.aniso2d(n)
+    V, T, E = m.n_verts, m.n_elems, m.n_edges
+    nw = (E + 31) // 32
+    with cg.Context(m) as c:
+        st = torch.cuda.Stream(dev)
+        torch.cuda.set_stream(st)
+        c.set_stream(st.cuda_stream)
+        d_u = torch.from_numpy(u).to(dev)
+        bits = torch.zeros(2 * nw, dtype=torch.int32, device=dev)
+        q = torch.zeros(T, dtype=torch.float64, device=dev)
+        run = lambda: c.aniso_estimate_and_mark_resident(d_u.data_ptr(), eps, hmin, hmax, bits.data_ptr(),
+                                                          bits.data_ptr() + 4 * nw, q.data_ptr())
+        for _ in range(max(1, args.warmup)):
+            run()
+        torch.cuda.synchronize(dev)
+        c.profile(True)
+        c.profile_report(True)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        steps = min(args.steps, 3)
+        e0.record(st)
+        for _ in range(steps):
+            run()
+        e1.record(st)
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1) / steps
+        prof = c.profile_report(True)
+    out = {"metric": METRIC, "value": V / (ms / 1e3), "unit": UNIT, "n_gpus": 1, "steps": steps,
+           "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": f"{n}^2 unit square, {T} triangles, {V} vertices, {E} edges, interior jitter "
+                                  f"+-0.15h (seed 5); u = tanh((y-0.5)/1e-3) + 0.1 sin(8 pi x); Hessian by two SPR "
+                                  f"recoveries, metric eps {eps:.3g}, h in [{hmin:.3g}, {hmax:.3g}]; AnisoSizeField "
+                                  f"measure, marks, quality", "form": "FP64"},
+           "phases": {k: {"launches": nl, "total_ms": t, "avg_ms": t / max(nl, 1)} for k, (nl, t) in prof.items()}}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         reference_arm(args)
+    elif args.workload == "batched":
+        gpu_batched(args)
+    elif args.workload == "aniso2d":
+        gpu_aniso2d(args)
     else:
         gpu_arm(args)
 
