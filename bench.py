@@ -222,6 +222,20 @@ def reference_arm(args):
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
+def job_throughput(ms_local, units_per_rank, steps, world, device=None):
+    """Whole-job throughput of `world` independent replicas: the slowest
+    rank's time (all-reduce MAX) for world x units x steps.  Returns
+    (ms_max, units per second)."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([ms_local], dtype=torch.float64, device=device)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dist.barrier()
+    ms_max = float(t.item())
+    return ms_max, world * units_per_rank * steps / (ms_max / 1e3)
+
+
 def time_form(m, u, precision, ratio, steps, dev, s64=None, f64=None):
     """Resident pass of one form on the same mesh: ms per pass (CUDA events
     on the launching stream, after warm-up) and, given the FP64 sizes and
@@ -320,12 +334,7 @@ def gpu_arm(args):
     clk = clocks.stop()
     prof = ctx.profile_report(reset=True)
     ctx.profile(False)
-    t = torch.tensor([ms_total], dtype=torch.float64, device=dev)
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dist.barrier()
-    ms_max = float(t.item())
-    value = world * V * args.steps / (ms_max / 1e3)
+    ms_max, value = job_throughput(ms_total, V, args.steps, world, dev)
 
     # e2e through the host API: pinned u in, flags + size out, every step
     e2e = None

@@ -99,3 +99,22 @@ def test_fp32_rejects_triangles(gpu_lib):
     m = workload.box(8, nz=0)
     with pytest.raises(cg.SprgError):
         cg.Context(m, precision="fp32")
+
+
+def test_fp32_marks_bit_exact_at_128cube(gpu_lib):
+    """The 128^3 parity workload: FP32 fits and sweeps with the FP64 guard
+    give the FP64 path's marks bit for bit."""
+    import core_gb300 as cg
+    from core_gb300 import workload
+    m = workload.box(128, jitter=0.2, seed=2)
+    u = workload.bump_field(m.coords, seed=2)
+    ratio = 0.008 * 128 / 160
+    with cg.Context(m, precision="fp64") as c64:
+        s64, f64, ns64, nc64, _ = c64.estimate_and_mark(u, ratio)
+    with cg.Context(m, precision="fp32") as c32:
+        s32, f32, ns32, nc32, info = c32.estimate_and_mark(u, ratio)
+    assert np.array_equal(f32, f64) and (ns32, nc32) == (ns64, nc64)
+    assert ns64 > 0 and nc64 > 0
+    assert info["n_guard_unresolved"] == 0
+    fin = np.isfinite(s32) & np.isfinite(s64)
+    assert np.median(np.abs(s32[fin] - s64[fin]) / s64[fin]) <= 1e-6
