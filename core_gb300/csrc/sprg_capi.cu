@@ -64,6 +64,7 @@ struct sprg_ctx {
   cudaGraphExec_t graph_exec = nullptr;
   DevBuf vvoff, vv, vtile, vr16, rec16, ql, sizel, fbitems, fbcount, mlp_packed, mlp_err, mlp_tmp;
   bool vv_ready = false, have_mlp = false;
+  int max_degree = 0;
   int use_mlp = 1;
   float z_max = 8.f;
   // side stream for the FP64 fits of listed patches, forked from and joined
@@ -1000,7 +1001,10 @@ static int pass_learned(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint
     ENSURE(c->vv, sizeof(int) * 2 * (size_t)m.E);
     ENSURE(c->tmp, sizeof(int) * (size_t)m.V);
     ENSURE(c->vtile, ((size_t)m.V + 127) / 128);
-    learned_build_v2v(m, P<int>(c->vvoff), P<int>(c->vv), P<int>(c->tmp), P<unsigned char>(c->vtile), c->stream);
+    learned_build_v2v(m, P<int>(c->vvoff), P<int>(c->vv), P<int>(c->tmp), P<unsigned char>(c->vtile),
+                      P<int>(c->fcnt) + 6, c->stream);
+    CK(cudaMemcpyAsync(&c->max_degree, P<int>(c->fcnt) + 6, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
     CK(cudaMemsetAsync(c->mlp_err.p, 0, sizeof(int), c->stream));
     if ((rc = check_launch(c, "vertex adjacency"))) return rc;
     c->vv_ready = true;
@@ -1016,7 +1020,7 @@ static int pass_learned(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint
   PE();
   PB("mlp_l");
   learned_infer(m, lm, vr, P<double>(c->f), c->mlp_packed.p, rec, P<int>(c->fbitems), P<int>(c->fbcount), c->z_max,
-                c->use_mlp,
+                c->use_mlp, c->max_degree,
                 P<int>(c->mlp_err), c->stream);
   PE();
   if ((rc = listed_join(c, xl, fork))) return rc;
@@ -1253,7 +1257,10 @@ int sprg_learned_features(sprg_ctx* c, const double* d_u, uint16_t* d_x, float* 
     ENSURE(c->tmp, sizeof(int) * (size_t)m.V);
     ENSURE(c->mlp_err, sizeof(int));
     ENSURE(c->vtile, ((size_t)m.V + 127) / 128);
-    learned_build_v2v(m, P<int>(c->vvoff), P<int>(c->vv), P<int>(c->tmp), P<unsigned char>(c->vtile), c->stream);
+    learned_build_v2v(m, P<int>(c->vvoff), P<int>(c->vv), P<int>(c->tmp), P<unsigned char>(c->vtile),
+                      P<int>(c->fcnt) + 6, c->stream);
+    CK(cudaMemcpyAsync(&c->max_degree, P<int>(c->fcnt) + 6, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
     CK(cudaMemsetAsync(c->mlp_err.p, 0, sizeof(int), c->stream));
     c->vv_ready = true;
   }

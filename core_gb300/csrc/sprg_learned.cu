@@ -20,6 +20,7 @@
 // The sweeps around it run in plain FP32 (the learned form is stated to 1e-2
 // in size): element gradients are recomputed from the 16-byte vertex records
 // where they are needed, and no per-element gradient array is stored.
+#include <algorithm>
 #include <cuda_bf16.h>
 #include <cub/cub.cuh>
 
@@ -51,12 +52,14 @@ __global__ void k_v2v_fill(int E, const int* __restrict__ edv, const int* __rest
 }
 
 // per 128-vertex tile: 1 when every vertex has at most 16 neighbours
-__global__ void k_tile_half(int V, const int* __restrict__ off, unsigned char* __restrict__ half) {
+__global__ void k_tile_half(int V, const int* __restrict__ off, unsigned char* __restrict__ half,
+                            int* __restrict__ max_deg) {
   const int tile = blockIdx.x;
   const int v = tile * 128 + threadIdx.x;
   const int cnt = v < V ? off[v + 1] - off[v] : 0;
   const int any = __syncthreads_or(cnt > kMlpSlots / 2);
   if (threadIdx.x == 0) half[tile] = any ? 0 : 1;
+  if (cnt > 0) atomicMax(max_deg, cnt);
 }
 
 __global__ void k_v2v_sort(int V, const int* __restrict__ off, int* __restrict__ nb) {
@@ -348,42 +351,56 @@ __device__ __forceinline__ float gelu_tab(const float2* __restrict__ tab, float 
 }
 __device__ __forceinline__ float phi(float x) { return 0.5f * (1.f + erff(x * 0.70710678118654752f)); }
 
-// shared-memory layout of the inference kernel (bytes); the first
-// kMlpPackedBytes are the packed parameters, copied as one block
+// packed parameters at the start of the kernel's shared memory (bytes)
 constexpr int kSmW1 = 0;
 constexpr int kSmW2 = kSmW1 + 2 * kMlpHidden * kMlpIn;
 constexpr int kSmW3 = kSmW2 + 2 * kMlpHidden * kMlpHidden;
 constexpr int kSmBias = kSmW3 + 2 * 16 * kMlpHidden;  // b1 [64], b2 [64], b3 [16] FP32
-constexpr int kSmA1 = 27 * 1024;                       // 128 x 128 BF16
-constexpr int kSmA2 = kSmA1 + 2 * 128 * kMlpIn;       // 128 x 64 BF16
-constexpr int kSmAux = kSmA2 + 2 * 128 * kMlpHidden;  // g_c [128][3], scale [128], flag [128]
-constexpr int kSmBar = kSmAux + 128 * 5 * 4;
-constexpr int kSmGelu = kSmBar + 64;                   // kGeluN float2
-constexpr int kSmInfer = kSmGelu + 8 * kGeluN;
 static_assert(kSmBias + 4 * 144 == kMlpPackedBytes, "packed parameter layout");
-static_assert(kSmA1 >= kMlpPackedBytes, "operand tiles after the parameters");
-constexpr int kInferThreads = 512;
-constexpr int kTmemCols = 128;  // D1 / D2 in columns 0..63, D3 in 64..79
 
-// hidden layer epilogue: bias + GELU of a 128 x 64 accumulator into the next
-// layer's A operand; warp w reads lanes 32 (w % 4) .. + 31, columns
-// 16 (w / 4) .. + 15
+// Inference shared memory for tiles of at most KMAX inputs: parameters, two
+// feature tiles (double buffer between producer and consumer warps), the
+// hidden tile, two auxiliary records, barriers, the CDF table.
+template <int KMAX>
+struct InferSmem {
+  static constexpr int kA1 = 27 * 1024;
+  static constexpr int kA1Bytes = 2 * 128 * KMAX;
+  static constexpr int kA2 = kA1 + 2 * kA1Bytes;
+  static constexpr int kAux = kA2 + 2 * 128 * kMlpHidden;
+  static constexpr int kAuxBytes = 128 * 5 * 4 + 16;  // g_c [128][3], scale [128], flag [128], K flag
+  static constexpr int kBar = kAux + 2 * kAuxBytes;   // mma, full[2], empty[2] (8 B each), tmem slot
+  static constexpr int kGelu = kBar + 64;
+  static constexpr int kTotal = kGelu + 8 * kGeluN;
+  static_assert(kA1 >= kMlpPackedBytes, "operand tiles after the parameters");
+};
+
+constexpr int kInferThreads = 512;  // warps 0-7 consume, warps 8-15 produce
+constexpr int kConsumers = 256;
+constexpr int kTmemCols = 128;      // D1 / D2 in columns 0..63, D3 in 64..79
+
+// hidden layer epilogue by the 8 consumer warps: bias + GELU of a 128 x 64
+// accumulator into the next layer's A operand; warp w reads lanes
+// 32 (w % 4) .. + 31 and columns 32 (w / 4) .. + 31
 __device__ __forceinline__ void hidden_epilogue(uint32_t tbase, const float* __restrict__ bias,
                                                 const float2* __restrict__ tab, __nv_bfloat16* __restrict__ A,
                                                 int warp, int lane) {
-  const int lq = warp & 3, cg = warp >> 2;
-  float z[16];
-  tmem_ld16(tbase + ((uint32_t)(32 * lq) << 16) + 16 * cg, z);
+  const int lq = warp & 3, ch = warp >> 2;
   const int row = 32 * lq + lane;
-  uint32_t h[8];
 #pragma unroll
-  for (int i = 0; i < 8; ++i) {
-    __nv_bfloat162 p = __floats2bfloat162_rn(gelu_tab(tab, z[2 * i] + bias[16 * cg + 2 * i]),
-                                             gelu_tab(tab, z[2 * i + 1] + bias[16 * cg + 2 * i + 1]));
-    h[i] = *reinterpret_cast<uint32_t*>(&p);
+  for (int half = 0; half < 2; ++half) {
+    const int c0 = 32 * ch + 16 * half;
+    float z[16];
+    tmem_ld16(tbase + ((uint32_t)(32 * lq) << 16) + c0, z);
+    uint32_t h[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      __nv_bfloat162 p = __floats2bfloat162_rn(gelu_tab(tab, z[2 * i] + bias[c0 + 2 * i]),
+                                               gelu_tab(tab, z[2 * i + 1] + bias[c0 + 2 * i + 1]));
+      h[i] = *reinterpret_cast<uint32_t*>(&p);
+    }
+    *reinterpret_cast<uint4*>(A + tile_off(row, c0, kMlpHidden)) = make_uint4(h[0], h[1], h[2], h[3]);
+    *reinterpret_cast<uint4*>(A + tile_off(row, c0 + 8, kMlpHidden)) = make_uint4(h[4], h[5], h[6], h[7]);
   }
-  *reinterpret_cast<uint4*>(A + tile_off(row, 16 * cg, kMlpHidden)) = make_uint4(h[0], h[1], h[2], h[3]);
-  *reinterpret_cast<uint4*>(A + tile_off(row, 16 * cg + 8, kMlpHidden)) = make_uint4(h[4], h[5], h[6], h[7]);
 }
 
 __device__ __forceinline__ int warp_slot(bool win, int* counter) {
@@ -398,24 +415,43 @@ __device__ __forceinline__ int warp_slot(bool win, int* counter) {
   return base + __popc(mask & ((1u << lane) - 1));
 }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// named barrier `id` over n threads, AND of v
+__device__ __forceinline__ bool bar_and(int id, int n, bool v) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 q, %1, 0;\n\tbar.red.and.pred p, %2, %3, q;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(r)
+      : "r"((uint32_t)v), "r"(id), "r"(n)
+      : "memory");
+  return r != 0;
+}
+
 constexpr int kWaitLimit = 1 << 22;
 
-__global__ void __launch_bounds__(kInferThreads, 2)
+// Warp-specialised persistent inference.  Producers (warps 8-15) compute the
+// features of a block's k-th tile into buffer k % 2 and arrive on full[b];
+// consumers (warps 0-7) wait on full[b], issue the three layers (thread 0)
+// and run the epilogues, then arrive on empty[b], which the producers wait on
+// before refilling the buffer.  Every wait is bounded; a wait that runs out
+// sets *err and both groups leave their loops.
+template <int KMAX>
+__global__ void __launch_bounds__(kInferThreads, KMAX == 64 ? 2 : 1)
     k_mlp_infer(int V, LearnMesh lm, const float4* __restrict__ vr, const double* __restrict__ u,
-                const uint4* __restrict__ packed,
-                float4* __restrict__ rec16, int* __restrict__ fb_items, int* __restrict__ fb_count, float z_max,
-                int use_mlp, int* __restrict__ err) {
+                const uint4* __restrict__ packed, float4* __restrict__ rec16, int* __restrict__ fb_items,
+                int* __restrict__ fb_count, float z_max, int use_mlp, int* __restrict__ err) {
+  using S = InferSmem<KMAX>;
   extern __shared__ __align__(1024) unsigned char sm[];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const float* bias = reinterpret_cast<const float*>(sm + kSmBias);
-  __nv_bfloat16* A1 = reinterpret_cast<__nv_bfloat16*>(sm + kSmA1);
-  __nv_bfloat16* A2 = reinterpret_cast<__nv_bfloat16*>(sm + kSmA2);
-  float* gcs = reinterpret_cast<float*>(sm + kSmAux);
-  float* scls = gcs + 3 * 128;
-  int* flags = reinterpret_cast<int*>(scls + 128);
-  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + kSmBar);
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + kSmBar + 8);
-  float2* gtab = reinterpret_cast<float2*>(sm + kSmGelu);
+  __nv_bfloat16* A2 = reinterpret_cast<__nv_bfloat16*>(sm + S::kA2);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sm + S::kBar);  // [0] mma, [1..2] full, [3..4] empty
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + S::kBar + 40);
+  float2* gtab = reinterpret_cast<float2*>(sm + S::kGelu);
 
   for (int i = tid; i < kMlpPackedBytes / 16; i += blockDim.x) reinterpret_cast<uint4*>(sm)[i] = packed[i];
   for (int i = tid; i < kGeluN; i += blockDim.x)
@@ -424,125 +460,152 @@ __global__ void __launch_bounds__(kInferThreads, 2)
     tmem_alloc(tslot, kTmemCols);
     tmem_relinquish();
   }
-  if (tid == 0) mbar_init(bar, 1);
+  if (tid == 0) {
+    mbar_init(bars, 1);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(bars + 1 + b, kInferThreads - kConsumers);
+      mbar_init(bars + 3 + b, kConsumers);
+    }
+  }
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tbase = *tslot;
-  const uint32_t sA1 = smem_u32(A1), sA2 = smem_u32(A2), sW1 = smem_u32(sm + kSmW1), sW2 = smem_u32(sm + kSmW2),
-                 sW3 = smem_u32(sm + kSmW3);
-  constexpr uint32_t id64 = idesc_bf16(128, 64), id16 = idesc_bf16(128, 16);
-  uint32_t phase = 0;
-  bool ok = true;
   const int ntiles = (V + 127) / 128;
-  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    // tiles whose vertices all have at most 16 neighbours (slots 16..31
-    // empty) multiply only the first 64 inputs: layer 1 with K = 64
-    const int half = lm.tile_half[tile];
-    // features, four lanes per vertex
-    {
-      const int r = tid >> 2, q = tid & 3;
-      if (half) {
-        VFeat<4> f = vertex_features<4>(lm, vr, V, tile * 128 + r, q);
+  bool ok = true;
+
+  if (warp >= 8) {
+    // ---- producers: 256 threads, four lanes per vertex, two passes of 64
+    const int ptid = tid - kConsumers;
+    for (int k = 0;; ++k) {
+      const int tile = blockIdx.x + k * gridDim.x;
+      if (tile >= ntiles) break;
+      const int b = k & 1;
+      if (k >= 2 && !mbar_wait(bars + 3 + b, ((k - 2) >> 1) & 1, kWaitLimit)) {
+        ok = false;
+        break;
+      }
+      __nv_bfloat16* A1 = reinterpret_cast<__nv_bfloat16*>(sm + S::kA1 + b * S::kA1Bytes);
+      float* gcs = reinterpret_cast<float*>(sm + S::kAux + b * S::kAuxBytes);
+      float* scls = gcs + 3 * 128;
+      int* flags = reinterpret_cast<int*>(scls + 128);
+      int* kflag = flags + 128;
+      const int half = KMAX == 64 ? 1 : lm.tile_half[tile];
+      for (int pass = 0; pass < 2; ++pass) {
+        const int r = 64 * pass + (ptid >> 2), q = ptid & 3;
+        if (half) {
+          VFeat<4> f = vertex_features<4>(lm, vr, V, tile * 128 + r, q);
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
-          *reinterpret_cast<uint2*>(A1 + tile_off(r, 4 * (q + 4 * i), kMlpIn)) = pack4_bf16(f.f[i]);
-        if (q == 0) {
-          gcs[3 * r] = f.gc[0];
-          gcs[3 * r + 1] = f.gc[1];
-          gcs[3 * r + 2] = f.gc[2];
-          scls[r] = f.scl;
-          flags[r] = f.flag;
-        }
-      } else {
-        VFeat<8> f = vertex_features<8>(lm, vr, V, tile * 128 + r, q);
+          for (int i = 0; i < 4; ++i)
+            *reinterpret_cast<uint2*>(A1 + tile_off(r, 4 * (q + 4 * i), KMAX)) = pack4_bf16(f.f[i]);
+          if (q == 0) {
+            gcs[3 * r] = f.gc[0]; gcs[3 * r + 1] = f.gc[1]; gcs[3 * r + 2] = f.gc[2];
+            scls[r] = f.scl;
+            flags[r] = f.flag;
+          }
+        } else if (KMAX == 128) {
+          VFeat<8> f = vertex_features<8>(lm, vr, V, tile * 128 + r, q);
 #pragma unroll
-        for (int i = 0; i < 8; ++i)
-          *reinterpret_cast<uint2*>(A1 + tile_off(r, 4 * (q + 4 * i), kMlpIn)) = pack4_bf16(f.f[i]);
-        if (q == 0) {
-          gcs[3 * r] = f.gc[0];
-          gcs[3 * r + 1] = f.gc[1];
-          gcs[3 * r + 2] = f.gc[2];
-          scls[r] = f.scl;
-          flags[r] = f.flag;
+          for (int i = 0; i < 8; ++i)
+            *reinterpret_cast<uint2*>(A1 + tile_off(r, 4 * (q + 4 * i), KMAX)) = pack4_bf16(f.f[i]);
+          if (q == 0) {
+            gcs[3 * r] = f.gc[0]; gcs[3 * r + 1] = f.gc[1]; gcs[3 * r + 2] = f.gc[2];
+            scls[r] = f.scl;
+            flags[r] = f.flag;
+          }
         }
       }
+      if (ptid == 0) *kflag = half;
+      fence_async_smem();
+      mbar_arrive(bars + 1 + b);
     }
-    fence_async_smem();
-    tc_fence_before();
-    __syncthreads();
-    // layer 1: D[0:64) = A1 W1^T
-    if (tid == 0) {
+  } else {
+    // ---- consumers: 256 threads; thread 0 issues the MMAs
+    const uint32_t sA2 = smem_u32(A2), sW1 = smem_u32(sm + kSmW1), sW2 = smem_u32(sm + kSmW2),
+                   sW3 = smem_u32(sm + kSmW3);
+    constexpr uint32_t id64 = idesc_bf16(128, 64), id16 = idesc_bf16(128, 16);
+    uint32_t mph = 0;
+    for (int k = 0;; ++k) {
+      const int tile = blockIdx.x + k * gridDim.x;
+      if (tile >= ntiles) break;
+      const int b = k & 1;
+      ok = bar_and(1, kConsumers, mbar_wait(bars + 1 + b, (k >> 1) & 1, kWaitLimit));
+      if (!ok) break;
+      const float* gcs = reinterpret_cast<const float*>(sm + S::kAux + b * S::kAuxBytes);
+      const float* scls = gcs + 3 * 128;
+      const int* flags = reinterpret_cast<const int*>(scls + 128);
+      const int half = flags[128];
+      const uint32_t sA1 = smem_u32(sm + S::kA1 + b * S::kA1Bytes);
       tc_fence_after();
-      const int nk = half ? kMlpIn / 32 : kMlpIn / 16;
-      for (int k = 0; k < nk; ++k)
-        mma_bf16(tbase, sdesc(sA1 + 256 * k, 128, 16 * kMlpIn), sdesc(sW1 + 256 * k, 128, 16 * kMlpIn), id64, k > 0);
-      mma_commit(bar);
-    }
-    ok = __syncthreads_and(tid == 0 ? mbar_wait(bar, phase, kWaitLimit) : true);
-    phase ^= 1;
-    if (!ok) break;
-    tc_fence_after();
-    hidden_epilogue(tbase, bias, gtab, A2, warp, lane);
-    fence_async_smem();
-    tc_fence_before();
-    __syncthreads();
-    // layer 2: D[0:64) = H1 W2^T
-    if (tid == 0) {
-      tc_fence_after();
-#pragma unroll
-      for (int k = 0; k < kMlpHidden / 16; ++k)
-        mma_bf16(tbase, sdesc(sA2 + 256 * k, 128, 16 * kMlpHidden), sdesc(sW2 + 256 * k, 128, 16 * kMlpHidden), id64,
-                 k > 0);
-      mma_commit(bar);
-    }
-    ok = __syncthreads_and(tid == 0 ? mbar_wait(bar, phase, kWaitLimit) : true);
-    phase ^= 1;
-    if (!ok) break;
-    tc_fence_after();
-    hidden_epilogue(tbase, bias + kMlpHidden, gtab, A2, warp, lane);
-    fence_async_smem();
-    tc_fence_before();
-    __syncthreads();
-    // layer 3: D[64:80) = H2 W3^T (rows 3..15 of W3 are zero)
-    if (tid == 0) {
-      tc_fence_after();
-#pragma unroll
-      for (int k = 0; k < kMlpHidden / 16; ++k)
-        mma_bf16(tbase + 64, sdesc(sA2 + 256 * k, 128, 16 * kMlpHidden), sdesc(sW3 + 256 * k, 128, 16 * kMlpHidden),
-                 id16, k > 0);
-      mma_commit(bar);
-    }
-    ok = __syncthreads_and(tid == 0 ? mbar_wait(bar, phase, kWaitLimit) : true);
-    phase ^= 1;
-    if (!ok) break;
-    tc_fence_after();
-    if (warp < 4) {
-      float z[16];
-      tmem_ld16(tbase + ((uint32_t)(32 * warp) << 16) + 64, z);
-      const int r = 32 * warp + lane, v = tile * 128 + r;
-      const float* b3 = bias + 2 * kMlpHidden;
-      float z0 = z[0] + b3[0], z1 = z[1] + b3[1], z2 = z[2] + b3[2];
-      const bool in = v < V;
-      const bool fb = in && (flags[r] || !(fabsf(z0) <= z_max && fabsf(z1) <= z_max && fabsf(z2) <= z_max));
-      if (!use_mlp) z0 = z1 = z2 = 0.f;
-      if (in && !fb) {
-        const float s = scls[r];
-        rec16[2 * (size_t)v] = __ldg(vr + v);
-        rec16[2 * (size_t)v + 1] = make_float4(fmaf(z0, s, gcs[3 * r]), fmaf(z1, s, gcs[3 * r + 1]),
-                                               fmaf(z2, s, gcs[3 * r + 2]), trunc_lo(__ldg(u + v)));
+      // layer 1: D[0:64) = A1 W1^T (K = 64 for tiles of <= 16 neighbours)
+      if (tid == 0) {
+        const int nk = half ? 4 : KMAX / 16;
+        for (int kk = 0; kk < nk; ++kk)
+          mma_bf16(tbase, sdesc(sA1 + 256 * kk, 128, 16 * KMAX), sdesc(sW1 + 256 * kk, 128, 16 * kMlpIn), id64,
+                   kk > 0);
+        mma_commit(bars);
       }
-      const int slot = warp_slot(fb, fb_count);
-      if (fb && slot < V) fb_items[slot] = v;
+      ok = bar_and(1, kConsumers, tid == 0 ? mbar_wait(bars, mph, kWaitLimit) : true);
+      mph ^= 1;
+      if (!ok) break;
+      tc_fence_after();
+      hidden_epilogue(tbase, bias, gtab, A2, warp, lane);
+      fence_async_smem();
+      tc_fence_before();
+      bar_and(1, kConsumers, true);
+      // layer 2: D[0:64) = H1 W2^T
+      if (tid == 0) {
+        tc_fence_after();
+        for (int kk = 0; kk < kMlpHidden / 16; ++kk)
+          mma_bf16(tbase, sdesc(sA2 + 256 * kk, 128, 16 * kMlpHidden), sdesc(sW2 + 256 * kk, 128, 16 * kMlpHidden),
+                   id64, kk > 0);
+        mma_commit(bars);
+      }
+      ok = bar_and(1, kConsumers, tid == 0 ? mbar_wait(bars, mph, kWaitLimit) : true);
+      mph ^= 1;
+      if (!ok) break;
+      tc_fence_after();
+      hidden_epilogue(tbase, bias + kMlpHidden, gtab, A2, warp, lane);
+      fence_async_smem();
+      tc_fence_before();
+      bar_and(1, kConsumers, true);
+      // layer 3: D[64:80) = H2 W3^T (rows 3..15 of W3 are zero)
+      if (tid == 0) {
+        tc_fence_after();
+        for (int kk = 0; kk < kMlpHidden / 16; ++kk)
+          mma_bf16(tbase + 64, sdesc(sA2 + 256 * kk, 128, 16 * kMlpHidden),
+                   sdesc(sW3 + 256 * kk, 128, 16 * kMlpHidden), id16, kk > 0);
+        mma_commit(bars);
+      }
+      ok = bar_and(1, kConsumers, tid == 0 ? mbar_wait(bars, mph, kWaitLimit) : true);
+      mph ^= 1;
+      if (!ok) break;
+      tc_fence_after();
+      if (warp < 4) {
+        float z[16];
+        tmem_ld16(tbase + ((uint32_t)(32 * warp) << 16) + 64, z);
+        const int r = 32 * warp + lane, v = tile * 128 + r;
+        const float* b3 = bias + 2 * kMlpHidden;
+        float z0 = z[0] + b3[0], z1 = z[1] + b3[1], z2 = z[2] + b3[2];
+        const bool in = v < V;
+        const bool fb = in && (flags[r] || !(fabsf(z0) <= z_max && fabsf(z1) <= z_max && fabsf(z2) <= z_max));
+        if (!use_mlp) z0 = z1 = z2 = 0.f;
+        if (in && !fb) {
+          const float s = scls[r];
+          rec16[2 * (size_t)v] = __ldg(vr + v);
+          rec16[2 * (size_t)v + 1] = make_float4(fmaf(z0, s, gcs[3 * r]), fmaf(z1, s, gcs[3 * r + 1]),
+                                                 fmaf(z2, s, gcs[3 * r + 2]), trunc_lo(__ldg(u + v)));
+        }
+        const int slot = warp_slot(fb, fb_count);
+        if (fb && slot < V) fb_items[slot] = v;
+      }
+      // buffer b (features and auxiliary record) is free again
+      tc_fence_before();
+      mbar_arrive(bars + 3 + b);
     }
-    tc_fence_before();
-    __syncthreads();
+    if (!ok) mbar_wait(bars, mph, kWaitLimit);  // MMAs in flight finish before the memory is freed
   }
-  if (!ok) {
-    // a wait ran out: let the MMAs in flight finish (bounded) before freeing
-    mbar_wait(bar, phase ^ 1, kWaitLimit);
-    if (tid == 0) atomicExch(err, 1);
-  }
+  if (!ok) atomicExch(err, 1);
   __syncthreads();
   tc_fence_after();
   if (warp == 0) tmem_dealloc(tbase, kTmemCols);
@@ -1033,18 +1096,20 @@ __global__ void k_mlp_adam(float* __restrict__ P, float* __restrict__ m1, float*
   P[p] -= lr * ah / (sqrtf(bh) + eps);
 }
 
+template <int KMAX>
 int infer_grid() {
   static int grid = 0;
   if (!grid) {
     int dev = 0, sms = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmInfer);
-    cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mlp_infer, kInferThreads, kSmInfer);
-    // two blocks per SM fit (64 registers x 512 threads, ~90 KB of shared
-    // memory, 128 tensor-memory columns each)
-    grid = (sms > 0 ? sms : 152) * (per > 1 ? per : 2);
+    cudaFuncSetAttribute(k_mlp_infer<KMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize, InferSmem<KMAX>::kTotal);
+    cudaFuncSetAttribute(k_mlp_infer<KMAX>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mlp_infer<KMAX>, kInferThreads, InferSmem<KMAX>::kTotal);
+    // KMAX = 64: two blocks per SM (64 registers x 512 threads, ~92 KB of
+    // shared memory, 128 tensor-memory columns each)
+    grid = (sms > 0 ? sms : 152) * (per > 0 ? per : 1);
+    if (KMAX == 64 && per < 2) grid = (sms > 0 ? sms : 152) * 2;
   }
   return grid;
 }
@@ -1053,7 +1118,8 @@ constexpr int kLErrorGrid = 152 * 8;
 
 }  // namespace
 
-void learned_build_v2v(const DevMesh& m, int* off, int* nb, int* tmp, unsigned char* tile_half, cudaStream_t s) {
+void learned_build_v2v(const DevMesh& m, int* off, int* nb, int* tmp, unsigned char* tile_half, int* max_deg,
+                       cudaStream_t s) {
   cudaMemsetAsync(off, 0, sizeof(int) * ((size_t)m.V + 1), s);
   cudaMemsetAsync(tmp, 0, sizeof(int) * (size_t)m.V, s);
   if (m.E) k_v2v_count<<<nblk(m.E), kBlock, 0, s>>>(m.E, m.edv, off);
@@ -1065,7 +1131,8 @@ void learned_build_v2v(const DevMesh& m, int* off, int* nb, int* tmp, unsigned c
   cudaFreeAsync(scratch, s);
   if (m.E) k_v2v_fill<<<nblk(m.E), kBlock, 0, s>>>(m.E, m.edv, off, tmp, nb);
   if (m.V) k_v2v_sort<<<nblk(m.V), kBlock, 0, s>>>(m.V, off, nb);
-  if (m.V) k_tile_half<<<(m.V + 127) / 128, 128, 0, s>>>(m.V, off, tile_half);
+  cudaMemsetAsync(max_deg, 0, sizeof(int), s);
+  if (m.V) k_tile_half<<<(m.V + 127) / 128, 128, 0, s>>>(m.V, off, tile_half, max_deg);
 }
 
 void learned_prep(const DevMesh& m, const double* u, float4* vr16, cudaStream_t s) {
@@ -1082,13 +1149,19 @@ void learned_pack(const float* params, void* packed, cudaStream_t s) {
 }
 
 void learned_infer(const DevMesh& m, const LearnMesh& lm, const float4* vr16, const double* u, const void* packed,
-                   float4* rec16, int* fb_items, int* fb_count, float z_max, int use_mlp, int* err, cudaStream_t s) {
+                   float4* rec16, int* fb_items, int* fb_count, float z_max, int use_mlp, int max_degree, int* err,
+                   cudaStream_t s) {
   if (!m.V) return;
   const int ntiles = (m.V + 127) / 128;
-  int grid = infer_grid();
-  if (grid > ntiles) grid = ntiles;
-  k_mlp_infer<<<grid, kInferThreads, kSmInfer, s>>>(m.V, lm, vr16, u, static_cast<const uint4*>(packed), rec16, fb_items,
-                                                    fb_count, z_max, use_mlp, err);
+  if (max_degree <= kMlpSlots / 2) {
+    const int grid = std::min(infer_grid<64>(), ntiles);
+    k_mlp_infer<64><<<grid, kInferThreads, InferSmem<64>::kTotal, s>>>(
+        m.V, lm, vr16, u, static_cast<const uint4*>(packed), rec16, fb_items, fb_count, z_max, use_mlp, err);
+  } else {
+    const int grid = std::min(infer_grid<128>(), ntiles);
+    k_mlp_infer<128><<<grid, kInferThreads, InferSmem<128>::kTotal, s>>>(
+        m.V, lm, vr16, u, static_cast<const uint4*>(packed), rec16, fb_items, fb_count, z_max, use_mlp, err);
+  }
 }
 
 void learned_fallback(const DevMesh& m, const LearnMesh& lm, const float4* vr16, const double* u, const float* w,

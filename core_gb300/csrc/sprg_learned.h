@@ -34,9 +34,10 @@ struct LearnMesh {
   const unsigned char* tile_half;   // per 128-vertex tile: all degrees <= 16
 };
 
-// vertex -> vertex CSR from the edge list (off: V + 1, nb: 2E, tmp: V ints)
-// and the per-tile degree flags (ceil(V / 128) bytes)
-void learned_build_v2v(const DevMesh& m, int* off, int* nb, int* tmp, unsigned char* tile_half, cudaStream_t s);
+// vertex -> vertex CSR from the edge list (off: V + 1, nb: 2E, tmp: V ints),
+// the per-tile degree flags (ceil(V / 128) bytes) and the largest degree
+void learned_build_v2v(const DevMesh& m, int* off, int* nb, int* tmp, unsigned char* tile_half, int* max_deg,
+                       cudaStream_t s);
 // FP32 vertex records {x, y, z, u}
 void learned_prep(const DevMesh& m, const double* u, float4* vr16, cudaStream_t s);
 // features for training: x [V][128] BF16 (row-major), aux [V][5]
@@ -48,8 +49,10 @@ void learned_pack(const float* params, void* packed, cudaStream_t s);
 // {x, y, z, u_hi}, {eps*, u_lo}) for the vertices the
 // network answers, the rest appended to fb_items (fb_count); use_mlp = 0
 // gives the cheap gradient alone.  err: set when a wait timed out.
+// max_degree <= 16 selects the K = 64 kernel (two blocks per SM)
 void learned_infer(const DevMesh& m, const LearnMesh& lm, const float4* vr16, const double* u, const void* packed,
-                   float4* rec16, int* fb_items, int* fb_count, float z_max, int use_mlp, int* err, cudaStream_t s);
+                   float4* rec16, int* fb_items, int* fb_count, float z_max, int use_mlp, int max_degree, int* err,
+                   cudaStream_t s);
 // plain SPR for the fallback vertices (FP32 weights, FP32 element gradients;
 // listed patches take rec64, their FP64 reference result)
 void learned_fallback(const DevMesh& m, const LearnMesh& lm, const float4* vr16, const double* u, const float* w,
