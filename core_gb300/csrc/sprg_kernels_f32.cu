@@ -12,7 +12,7 @@
 //  * a tet gradient is formed relative to a reference gradient g as
 //    J^{-1} (du - J g), with the residual du - J g evaluated by compensated
 //    dot products, so only the small deviation carries FP32 rounding;
-//  * the recovered field is stored as (g_ref, deviation) per vertex, and the
+//  * the recovered value is stored as a value + packed remainder pair, and the
 //    element error |eps - eps*|^2 is taken from those deviations.
 //
 // That keeps the element errors (and so the sizes) at ~1e-7 relative even
@@ -543,35 +543,44 @@ __global__ void __launch_bounds__(kBlock) k_fast_error(DevMesh m, const uint4* _
     t_step = blockDim.x;
   }
   for (int t = t_beg; t < t_end; t += t_step) {
-    int4 tv = __ldg(reinterpret_cast<const int4*>(m.ev) + t);
-    uint4 ta = __ldg(td + t);
-    float2 gm = __ldg(geo + t);
-    const uint4 R0 = __ldg(rec + tv.x), R1 = __ldg(rec + tv.y), R2 = __ldg(rec + tv.z), R3 = __ldg(rec + tv.w);
-    Grad ga = unpack_grad(ta);
-    const Grad E0 = unpack_grad(R0), E1 = unpack_grad(R1), E2 = unpack_grad(R2), E3 = unpack_grad(R3);
-    // eps*(IP) = g + D with g = s of vertex 0, D = sum ((s_i - g) + r_i) / 4
-    const float g0 = E0.s[0], g1 = E0.s[1], g2 = E0.s[2];
-    float D0 = 0.25f * ((E0.r[0] + ((E1.s[0] - g0) + E1.r[0])) + (((E2.s[0] - g0) + E2.r[0]) + ((E3.s[0] - g0) + E3.r[0])));
-    float D1 = 0.25f * ((E0.r[1] + ((E1.s[1] - g1) + E1.r[1])) + (((E2.s[1] - g1) + E2.r[1]) + ((E3.s[1] - g1) + E3.r[1])));
-    float D2 = 0.25f * ((E0.r[2] + ((E1.s[2] - g2) + E1.r[2])) + (((E2.s[2] - g2) + E2.r[2]) + ((E3.s[2] - g2) + E3.r[2])));
-    // eps_t - eps*(IP) = (s_t - g) + r_t - D
-    float dx = ((ga.s[0] - g0) + ga.r[0]) - D0, dy = ((ga.s[1] - g1) + ga.r[1]) - D1,
-          dz = ((ga.s[2] - g2) + ga.r[2]) - D2;
-    float wdv = gm.x;
-    float err = (dx * dx + dy * dy + dz * dz) * wdv;
-    float ex = g0 + D0, ey = g1 + D1, ez = g2 + D2;
-    self.add((ex * ex + ey * ey + ez * ez) * wdv);
-    // (sqrt err)^(6/5) = err^(3/5) = err r^2 and h_max (sqrt err)^(-2/5) =
-    // h_max r, with r = err^(-1/5)
-    float rr = inv_fifth_root(err);
-    gsum.add(err > 0.f ? err * (rr * rr) : 0.f);  // (sqrt 0)^(6/5) = 0; q = +inf as in FP64
-    // relative error bound of q: the deviation (dx, dy, dz) is a difference
-    // of quantities of size `scale`, each good to a few FP32 ulps, plus the
-    // packed corrections
-    float scale = fmaxf(fmaxf(fabsf(ga.s[0] - g0), fabsf(ga.s[1] - g1)), fabsf(ga.s[2] - g2)) +
-                  fmaxf(fmaxf(fabsf(D0), fabsf(D1)), fabsf(D2));
-    float dn = sqrtf(dx * dx + dy * dy + dz * dz);
-    q[t] = make_float2(gm.y * rr, (dn > 0.f) ? (kBoundUlps * scale + kQuantRel * ga.gmax) / dn : 3.0e38f);
+    {
+      const int4 tv = __ldg(reinterpret_cast<const int4*>(m.ev) + t);
+      const uint4 ta = __ldg(td + t);
+      const float2 gm = __ldg(geo + t);
+      const uint4 R0 = __ldg(rec + tv.x), R1 = __ldg(rec + tv.y), R2 = __ldg(rec + tv.z), R3 = __ldg(rec + tv.w);
+      Grad ga = unpack_grad(ta);
+      const Grad E0 = unpack_grad(R0), E1 = unpack_grad(R1), E2 = unpack_grad(R2), E3 = unpack_grad(R3);
+      // eps*(IP) = g + D with g = s of vertex 0, D = sum ((s_i - g) + r_i) / 4
+      const float g0 = E0.s[0], g1 = E0.s[1], g2 = E0.s[2];
+      float D0 = 0.25f * ((E0.r[0] + ((E1.s[0] - g0) + E1.r[0])) + (((E2.s[0] - g0) + E2.r[0]) + ((E3.s[0] - g0) + E3.r[0])));
+      float D1 = 0.25f * ((E0.r[1] + ((E1.s[1] - g1) + E1.r[1])) + (((E2.s[1] - g1) + E2.r[1]) + ((E3.s[1] - g1) + E3.r[1])));
+      float D2 = 0.25f * ((E0.r[2] + ((E1.s[2] - g2) + E1.r[2])) + (((E2.s[2] - g2) + E2.r[2]) + ((E3.s[2] - g2) + E3.r[2])));
+      // eps_t - eps*(IP) = (s_t - g) + r_t - D
+      float dx = ((ga.s[0] - g0) + ga.r[0]) - D0, dy = ((ga.s[1] - g1) + ga.r[1]) - D1,
+            dz = ((ga.s[2] - g2) + ga.r[2]) - D2;
+      float wdv = gm.x;
+      float err = (dx * dx + dy * dy + dz * dz) * wdv;
+      float ex = g0 + D0, ey = g1 + D1, ez = g2 + D2;
+      self.add((ex * ex + ey * ey + ez * ez) * wdv);
+      // (sqrt err)^(6/5) = err^(3/5) = err r^2 and h_max (sqrt err)^(-2/5) =
+      // h_max r, with r = err^(-1/5)
+      float rr = inv_fifth_root(err);
+      gsum.add(err > 0.f ? err * (rr * rr) : 0.f);  // (sqrt 0)^(6/5) = 0; q = +inf as in FP64
+      // error bound of q: the deviation (dx, dy, dz) is a difference of
+      // quantities of size `scale`, each good to a few FP32 ulps, plus the
+      // packed corrections; delta is 0.4 x that absolute deviation error
+      float scale = fmaxf(fmaxf(fabsf(ga.s[0] - g0), fabsf(ga.s[1] - g1)), fabsf(ga.s[2] - g2)) +
+                    fmaxf(fmaxf(fabsf(D0), fabsf(D1)), fabsf(D2));
+      // (plus a floor for field values below FP32's range, which read as 0)
+      const float delta = kBoundUlps * scale + kQuantRel * ga.gmax + 1e-30f;
+      float dn = sqrtf(dx * dx + dy * dy + dz * dz);
+      // a zero deviation (q = +inf) keeps a lower bound of q instead: the FP64
+      // deviation is at most delta / 0.4, so q >= h_max (w dV (delta / 0.4)^2)^(-1/5)
+      // (stored negated)
+      float b = delta / dn;
+      if (!(dn > 0.f)) b = -(gm.y * inv_fifth_root(wdv * (2.5f * delta) * (2.5f * delta)));
+      q[t] = make_float2(gm.y * rr, b);
+    }
   }
   double s1 = warp_pair_total(self), s2 = warp_pair_total(gsum);
   const int w = threadIdx.x >> 5;
@@ -609,30 +618,34 @@ __global__ void __launch_bounds__(kBlock) k_fast_average(DevMesh m, const float2
     e = m.a_off[v + 1];
   }
   PairSum s{0.f, 0.f};
-  float qb = 0.f, bmax = 0.f;
+  float qb = 0.f, bmax = 0.f, lo = 0.f;
   float2 x[8];
 #pragma unroll
   for (int j = 0; j < 8; ++j) {
     int k = b + gl + j * kGroup;
     x[j] = (k < e) ? __ldg(q + __ldg(m.a_el + k)) : make_float2(0.f, 0.f);
   }
+  // element (q, b): b >= 0 a relative bound; b < 0 for q = +inf, -b a lower
+  // bound of the FP64 q
+  auto take = [&](float2 y) {
+    s.add(y.x);
+    if (y.y >= 0.f) {
+      qb = fmaf(y.x, y.y, qb);
+      bmax = fmaxf(bmax, y.y);
+      lo += y.x * fmaxf(1.f - y.y, 0.f);
+    } else {
+      lo += -y.y;
+    }
+  };
 #pragma unroll
   for (int j = 0; j < 8; ++j)
-    if (b + gl + j * kGroup < e) {
-      s.add(x[j].x);
-      qb = fmaf(x[j].x, x[j].y, qb);
-      bmax = fmaxf(bmax, x[j].y);
-    }
-  for (int k = b + gl + 8 * kGroup; k < e; k += kGroup) {  // patches above 32 elements
-    float2 y = __ldg(q + __ldg(m.a_el + k));
-    s.add(y.x);
-    qb = fmaf(y.x, y.y, qb);
-    bmax = fmaxf(bmax, y.y);
-  }
+    if (b + gl + j * kGroup < e) take(x[j]);
+  for (int k = b + gl + 8 * kGroup; k < e; k += kGroup) take(__ldg(q + __ldg(m.a_el + k)));  // > 32 elements
 #pragma unroll
   for (int o = 1; o < kGroup; o <<= 1) {
     float oh = __shfl_xor_sync(0xffffffffu, s.h, o), ol = __shfl_xor_sync(0xffffffffu, s.l, o);
     float oq = __shfl_xor_sync(0xffffffffu, qb, o), ob = __shfl_xor_sync(0xffffffffu, bmax, o);
+    const float olo = __shfl_xor_sync(0xffffffffu, lo, o);
     // combine the lower lane's pair first so every lane gets the same sum
     bool low = (gl & o) == 0;
     float ah = low ? s.h : oh, al = low ? s.l : ol, bh = low ? oh : s.h, bl = low ? ol : s.l;
@@ -641,17 +654,21 @@ __global__ void __launch_bounds__(kBlock) k_fast_average(DevMesh m, const float2
     s.h = t;
     s.l = (al + bl) + err;
     qb = low ? qb + oq : oq + qb;
+    lo = low ? lo + olo : olo + lo;
     bmax = fmaxf(bmax, ob);
   }
   if (v < m.V && gl == 0) {
     // an infinite q (zero element error) leaves +inf in the high part and NaN
     // in the compensation
     float tot = isfinite(s.h) ? s.h + s.l : s.h;
+    const float sf = (float)batch_sf(bv, out3, v), inv_n = 1.f / (float)(e - b);
     float bound = qb / tot;
-    // an element with a zero error (infinite q) or an unbounded deviation
-    // leaves the size unbounded
     if (!(bmax < 1e30f) || !(bound <= 1e30f)) bound = 3.0e38f;
-    sz2[v] = make_float2((float)batch_sf(bv, out3, v) * (tot / (float)(e - b)), bound);
+    // an element with a zero deviation makes the size +inf (as FP64 does for
+    // a zero error); its record then carries the negated lower bound of the
+    // FP64 size
+    if (!isfinite(tot)) bound = -(sf * (lo * inv_n) * (1.f - 1e-6f));
+    sz2[v] = make_float2(sf * (tot * inv_n), bound);
   }
 }
 
@@ -694,10 +711,22 @@ __global__ void __launch_bounds__(kBlock) k_fast_measure(DevMesh m, const float*
       float L = hl[i] * (1.f / (n0 * A[i].x + n1 * B[i].x) + 1.f / (n1 * A[i].x + n0 * B[i].x));
       s = L > 1.5f;
       c = L < 0.5f;
-      // guard band: the FP32 length may be off by guard_rel plus the size
-      // error bounds of the two ends
-      float band = guard_rel + A[i].y + B[i].y;
-      if (fabsf(L - 1.5f) <= band * 1.5f || fabsf(L - 0.5f) <= band * 0.5f || !(L == L)) {
+      // guard band: the interval of the FP64 length from the ends' size
+      // intervals (relative bounds, or a lower bound for an infinite size),
+      // widened by guard_rel for the FP32 length itself
+      bool near;
+      if (A[i].y >= 0.f && B[i].y >= 0.f) {
+        // finite ends: L moves by at most guard_rel + b_a + b_b relative
+        const float band = guard_rel + A[i].y + B[i].y;
+        near = fabsf(L - 1.5f) <= band * 1.5f || fabsf(L - 0.5f) <= band * 0.5f;
+      } else {
+        // an infinite end: the upper end of L from the sizes' lower bounds
+        const float alo = A[i].y >= 0.f ? A[i].x * fmaxf(1.f - A[i].y, 0.f) : -A[i].y;
+        const float blo = B[i].y >= 0.f ? B[i].x * fmaxf(1.f - B[i].y, 0.f) : -B[i].y;
+        const float Lhi = hl[i] * (1.f / (n0 * alo + n1 * blo) + 1.f / (n1 * alo + n0 * blo)) * (1.f + guard_rel);
+        near = !(Lhi < 0.5f);  // the FP32 length is 0 here: only a collapse can be in doubt
+      }
+      if (near || !(L == L)) {
         int slot = atomicAdd(guard_count, 1);
         if (slot < guard_cap) guard_items[slot] = e;
       }
