@@ -44,6 +44,7 @@ struct sprg_ctx {
   bool ip_valid = false, size_valid = false, L_valid = false;
   // scratch
   DevBuf partials, out3, status, count, xitems, xcount, slab, bits;
+  DevBuf titems, tcountb;  // triangle patches above the thread-per-vertex size
   // FP32 path buffers
   DevBuf crec, vrec, rec32, q32, sz2, fcnt, guard, tetd, wts, w64, listed, geo, geo64, elen, fitems;
   DevBuf gstamp, gfit, grec, tstamp, tslot, trec, tcount;  // guard pipeline scratch
@@ -73,6 +74,7 @@ struct sprg_ctx {
   cudaEvent_t fork = nullptr, join = nullptr;
   int pass_id = 0;
   bool vrec_ready = false;  // coordinate records and SPR weights (per mesh)
+  double frame[4] = {0, 0, 0, 1};  // coordinate records: x' = (x - c) s + 1 in [1, 2]
   int n_listed = 0, n_refit = 0;
   PatchCache cache64, cache32;
   static constexpr int kGuardCap = 1 << 20;
@@ -242,10 +244,14 @@ int step_recover(sprg_ctx* c) {
   ENSURE(c->xitems, sizeof(int) * (size_t)(m.V > 0 ? m.V : 1));
   ENSURE(c->xcount, sizeof(int));
   ENSURE(c->slab, sizeof(double) * (size_t)expand_grid() * expand_max_elems() * (4 + nc + 1));
+  ENSURE(c->titems, sizeof(int) * (size_t)(m.dim == 2 && m.V > 0 ? m.V : 1));
+  ENSURE(c->tcountb, sizeof(int));
   CK(cudaMemsetAsync(c->xcount.p, 0, sizeof(int), c->stream));
+  CK(cudaMemsetAsync(c->tcountb.p, 0, sizeof(int), c->stream));
   ExpandList xl{P<int>(c->xitems), P<int>(c->xcount), m.V};
+  ExpandList big{P<int>(c->titems), P<int>(c->tcountb), m.dim == 2 ? m.V : 0};
   PB("recover_f64");
-  launch_recover_f64(m, P<double>(c->ip), nc, P<double>(c->rec), xl, P<DevStatus>(c->status), c->stream);
+  launch_recover_f64(m, P<double>(c->ip), nc, P<double>(c->rec), xl, big, P<DevStatus>(c->status), c->stream);
   PE();
   c->launches += 1;
   int rc = check_launch(c, "recover");
@@ -396,6 +402,26 @@ int sprg_create(const sprg_mesh_view* mv, int device, sprg_ctx** out) {
   CKC(cudaMemcpyAsync(c->xyz.p, mv->coords, sizeof(double) * 3 * (size_t)m.V, cudaMemcpyHostToDevice, c->stream));
   CKC(cudaMemcpyAsync(c->ev.p, mv->elem_verts, sizeof(int) * nel, cudaMemcpyHostToDevice, c->stream));
   CKC(cudaMemcpyAsync(c->edv.p, mv->edge_verts, sizeof(int) * 2 * (size_t)m.E, cudaMemcpyHostToDevice, c->stream));
+  {
+    // bounding box -> the FP32 records' frame: shift to the lower corner and
+    // scale by a power of two so every coordinate lands in [1, 2]
+    double lo[3] = {mv->coords[0], mv->coords[1], mv->coords[2]}, hi[3] = {lo[0], lo[1], lo[2]};
+    for (int64_t v = 1; v < mv->n_verts; ++v)
+      for (int k = 0; k < 3; ++k) {
+        const double x = mv->coords[3 * v + k];
+        lo[k] = x < lo[k] ? x : lo[k];
+        hi[k] = x > hi[k] ? x : hi[k];
+      }
+    double ext = 0;
+    for (int k = 0; k < 3; ++k) ext = hi[k] - lo[k] > ext ? hi[k] - lo[k] : ext;
+    double s = 1;
+    while (s * ext > 1) s *= 0.5;
+    while (ext > 0 && s * ext <= 0.5) s *= 2;
+    c->frame[0] = lo[0];
+    c->frame[1] = lo[1];
+    c->frame[2] = lo[2];
+    c->frame[3] = s;
+  }
   m.xyz = P<double>(c->xyz);
   m.xyz32 = P<float>(c->xyz32);
   m.ev = P<int>(c->ev);
@@ -443,7 +469,7 @@ int sprg_destroy(sprg_ctx* c) {
   DevBuf* bufs[] = {&c->xyz,   &c->xyz32,   &c->ev,   &c->edv,   &c->poff,    &c->pel,    &c->aoff,
                     &c->ael,   &c->tmp,     &c->f,    &c->ip,    &c->rec,     &c->err,    &c->esize,
                     &c->size,  &c->L,       &c->flags, &c->q,    &c->sizes3,  &c->frames9, &c->partials,
-                    &c->out3,  &c->status,  &c->count, &c->xitems, &c->xcount, &c->slab, &c->bits,
+                    &c->out3,  &c->status,  &c->count, &c->xitems, &c->xcount, &c->slab, &c->bits, &c->titems, &c->tcountb,
                     &c->crec,  &c->vrec,    &c->rec32, &c->q32, &c->sz2,  &c->fcnt,   &c->guard, &c->tetd,
                     &c->wts,   &c->w64,     &c->listed, &c->geo, &c->geo64, &c->elen, &c->fitems, &c->gstamp, &c->gfit, &c->grec,
                     &c->tstamp, &c->tslot,  &c->trec, &c->tcount, &c->hess, &c->pcls, &c->bverts, &c->btiles, &c->bnext, &c->bvoff, &c->bseg, &c->bsegoff, &c->bratios, &c->vvoff, &c->vv, &c->vtile, &c->vr16, &c->rec16,
@@ -690,7 +716,7 @@ static int fast_setup(sprg_ctx* c, ExpandList xl) {
   ENSURE(c->geo64, 16 * (size_t)m.T);
   ENSURE(c->elen, 4 * (size_t)m.E);
   CK(cudaMemsetAsync(c->fcnt.p, 0, 8 * sizeof(int), c->stream));
-  fast_prep_coords(m, P<float4>(c->crec), c->stream);
+  fast_prep_coords(m, c->frame, P<float4>(c->crec), c->stream);
   fast_geometry(m, P<float2>(c->geo), P<double2>(c->geo64), P<float>(c->elen), c->stream);
   fast_weights(m, P<float>(c->wts), P<double>(c->w64), xl, P<int>(c->fcnt), P<unsigned char>(c->listed), c->stream);
   int h[2] = {0, 0};
@@ -910,7 +936,7 @@ static int pass_fast(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_
   fast_prep(m, P<double>(c->f), P<float4>(c->crec), vrec, c->stream);
   PE();
   PB("tet_f32");
-  fast_tet(m, vrec, P<uint4>(c->tetd), c->stream);
+  fast_tet(m, vrec, (float)c->frame[3], P<uint4>(c->tetd), c->stream);
   PE();
   if (!c->bins_ready) {
     if ((rc = build_bins(c))) return rc;

@@ -5,15 +5,18 @@
 namespace sprg {
 
 int fast_error_blocks(int T);
-// packed double-float coordinate records {x,y,z,0}_hi, {x,y,z,0}_lo (2 float4 per vertex)
-void fast_prep_coords(const DevMesh& m, float4* vrec, cudaStream_t s);
+// packed double-float coordinate records {x,y,z,0}_hi, {x,y,z,0}_lo (2 float4 per
+// vertex) of the coordinates mapped into [1, 2]: x' = (x - c) s + 1 with
+// frame = {c_x, c_y, c_z, s}, s a power of two
+void fast_prep_coords(const DevMesh& m, const double* frame, float4* vrec, cudaStream_t s);
 // once per mesh: per tet {w dV, h_max} (FP32) and {det J, h_max} (FP64), per
 // edge half its length
 void fast_geometry(const DevMesh& m, float2* geo, double2* geo64, float* half_len, cudaStream_t s);
 // the pass's vertex records: coordinate records with the field pair (u_hi, u_lo)
 void fast_prep(const DevMesh& m, const double* u, const float4* crec, float4* vrec, cudaStream_t s);
 // per tet: gradient value (3 floats) and packed correction (1 word)
-void fast_tet(const DevMesh& m, const float4* vrec, uint4* td, cudaStream_t s);
+// gscale = the frame's s (gradients in the mesh's coordinates)
+void fast_tet(const DevMesh& m, const float4* vrec, float gscale, uint4* td, cudaStream_t s);
 // once per mesh: SPR weights in patch-CSR order (FP32 for the pass, FP64 for
 // the guard), listed patches
 void fast_weights(const DevMesh& m, float* w, double* w64, ExpandList xl, int* n_refit, unsigned char* listed,

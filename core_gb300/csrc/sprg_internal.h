@@ -70,7 +70,10 @@ struct ExpandList {
 
 // ---- kernel launchers (sprg_kernels_f64.cu) ---------------------------
 void launch_grad_ip_f64(const DevMesh& m, const double* f, int ncin, double* ip, cudaStream_t s);
-void launch_recover_f64(const DevMesh& m, const double* ip, int nc, double* rec, ExpandList xl,
+// xl: patches that need growth; big: triangle patches above the
+// thread-per-vertex size (fitted by the warp path inside this call; its
+// counter must be zero on entry)
+void launch_recover_f64(const DevMesh& m, const double* ip, int nc, double* rec, ExpandList xl, ExpandList big,
                         DevStatus* st, cudaStream_t s);
 // Patches on the expansion list: grow as the reference does, then fit.
 // The list length is read on the device (no host round trip).

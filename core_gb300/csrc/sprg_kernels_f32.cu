@@ -110,13 +110,14 @@ __device__ __forceinline__ void apply_inv(const Cof& k, float r1, float r2, floa
   for (int j = 0; j < 3; ++j) g[j] = (k.c[0][j] * r1 + k.c[1][j] * r2 + k.c[2][j] * r3) * inv;
 }
 
-// x^(-1/5) for the element error x: powf's estimate refined by one Newton
-// step on x r^5 = 1 whose residual is taken with a single rounding (fmaf).
-// powf alone is biased by several ulp for these exponents, which would shift
-// the global error sum and with it every size.
+// x^(-1/5) for the element error x: a hardware log2 / exp2 estimate
+// (relative error below 1e-5 for x in (1e-30, 1e30)) refined by one Newton
+// step on x r^5 = 1 whose residual is taken with a single rounding (fmaf);
+// the step squares the estimate's error, leaving the FP32 rounding of the
+// last operations.  Outside that range powf handles zero, inf and NaN.
 __device__ __forceinline__ float inv_fifth_root(float x) {
-  float r = powf(x, -0.2f);
-  if (!(x > 1e-30f) || !(x < 1e30f)) return r;
+  if (!(x > 1e-30f) || !(x < 1e30f)) return powf(x, -0.2f);
+  float r = exp2f(-0.2f * __log2f(x));
   float r2 = r * r;
   float r5 = r2 * r2 * r;
   float e = fmaf(-x, r5, 1.0f);
@@ -128,28 +129,33 @@ __device__ __forceinline__ float inv_fifth_root(float x) {
 // a shared-exponent triple.  With E the exponent of max |r_j| and E_s that of
 // max |s_j| (E <= E_s - 24):
 //   bits 27..31  k = E_s - E - 24 (corrections below 2^-56 |s| are dropped)
-//   bits 18..26, 9..17, 0..8  m_j = rint(r_j 2^(7-E)), 9-bit two's complement
-// so r_j = m_j 2^(E_s - k - 31), exact to 2^-32 max|s_j| (half a unit).
+//   bits 18..26, 9..17, 0..8  m_j + 256, m_j = rint(r_j 2^(7-E)) in [-255, 255]
+// so r_j = m_j 2^(E_s - k - 31), exact to 2^-32 max|s_j| (half a unit); no
+// correction is k = 31 with m_j = 0 (kNoCorr).  Rounding and the int <-> float
+// steps use the 1.5 * 2^23 constant (integer and FMA pipes) instead of
+// conversion instructions, which run at a quarter rate.
+constexpr uint32_t kNoCorr = (31u << 27) | (256u << 18) | (256u << 9) | 256u;
 __device__ __forceinline__ int fexp(float a) { return ((__float_as_int(a) >> 23) & 0xff) - 127; }
 
 __device__ __forceinline__ uint32_t pack_corr(float s0, float s1, float s2, float r0, float r1, float r2) {
   float M = fmaxf(fabsf(r0), fmaxf(fabsf(r1), fabsf(r2)));
-  if (!(M > 0.f) || !(M < 3.0e38f)) return 0u;
+  if (!(M > 0.f) || !(M < 3.0e38f)) return kNoCorr;
   int Es = fexp(fmaxf(fabsf(s0), fmaxf(fabsf(s1), fabsf(s2))));
   int E = fexp(M);
   int k = Es - E - 24;
-  if (k > 31) return 0u;
+  if (k > 31) return kNoCorr;
   if (k < 0) {  // only for subnormal s: keep what fits
     k = 0;
     E = Es - 24;
   }
   // 2^(7-E) as a float: exact for E > -120 (the exponent field 134 - E <= 254)
   float sc = E > -120 ? __int_as_float((134 - E) << 23) : ldexpf(1.f, 7 - E);
-  int m0 = max(-255, min(255, __float2int_rn(E > -120 ? r0 * sc : ldexpf(r0, 7 - E))));
-  int m1 = max(-255, min(255, __float2int_rn(E > -120 ? r1 * sc : ldexpf(r1, 7 - E))));
-  int m2 = max(-255, min(255, __float2int_rn(E > -120 ? r2 * sc : ldexpf(r2, 7 - E))));
-  return ((uint32_t)k << 27) | (((uint32_t)m0 & 0x1ffu) << 18) | (((uint32_t)m1 & 0x1ffu) << 9) |
-         ((uint32_t)m2 & 0x1ffu);
+  auto q9 = [&](float r) {  // rint(r 2^(7-E)) + 256, clamped to [1, 511]
+    const float x = E > -120 ? r * sc : ldexpf(r, 7 - E);
+    const int mj = __float_as_int(x + 12582912.f) - 0x4B400000;
+    return (uint32_t)(max(-255, min(255, mj)) + 256);
+  };
+  return ((uint32_t)k << 27) | (q9(r0) << 18) | (q9(r1) << 9) | q9(r2);
 }
 
 struct Grad {
@@ -164,20 +170,26 @@ __device__ __forceinline__ Grad unpack_grad(uint4 a) {
   g.s[2] = __uint_as_float(a.z);
   g.gmax = fmaxf(fabsf(g.s[0]), fmaxf(fabsf(g.s[1]), fabsf(g.s[2])));
   int ex = fexp(g.gmax) - (int)(a.w >> 27) - 31;
-  float sc = ex > -127 ? __int_as_float((ex + 127) << 23) : 0.f;
-  g.r[0] = (float)(((int)(a.w << 5)) >> 23) * sc;
-  g.r[1] = (float)(((int)(a.w << 14)) >> 23) * sc;
-  g.r[2] = (float)(((int)(a.w << 23)) >> 23) * sc;
+  const float sc = ex > -127 ? __int_as_float((ex + 127) << 23) : 0.f;
+  // m_j as a float: 1.5 * 2^23 + (m_j + 256) read as a float, minus the offset
+  const float off = 12582912.f + 256.f;
+  g.r[0] = (__int_as_float(0x4B400000 + ((a.w >> 18) & 0x1ffu)) - off) * sc;
+  g.r[1] = (__int_as_float(0x4B400000 + ((a.w >> 9) & 0x1ffu)) - off) * sc;
+  g.r[2] = (__int_as_float(0x4B400000 + (a.w & 0x1ffu)) - off) * sc;
   return g;
 }
 
 // ---------------------------------------------------------------------------
-// coordinate records (once per mesh) and the field pair (once per pass)
-__global__ void __launch_bounds__(kBlock) k_prep_coords(int V, const double* __restrict__ xyz,
-                                                        float4* __restrict__ rec) {
+// coordinate records (once per mesh) and the field pair (once per pass).
+// The coordinates are mapped into [1, 2] (x' = (x - c) s + 1, s a power of
+// two): differences of the high words of two records are then exact (Sterbenz)
+// and gradients scale back exactly (du/dx = s du/dx').
+__global__ void __launch_bounds__(kBlock) k_prep_coords(int V, const double* __restrict__ xyz, double cx, double cy,
+                                                        double cz, double cs, float4* __restrict__ rec) {
   int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= V) return;
-  double x = xyz[3 * (size_t)v], y = xyz[3 * (size_t)v + 1], z = xyz[3 * (size_t)v + 2];
+  double x = (xyz[3 * (size_t)v] - cx) * cs + 1.0, y = (xyz[3 * (size_t)v + 1] - cy) * cs + 1.0,
+         z = (xyz[3 * (size_t)v + 2] - cz) * cs + 1.0;
   float xh = (float)x, yh = (float)y, zh = (float)z;
   rec[2 * (size_t)v] = make_float4(xh, yh, zh, 0.f);
   rec[2 * (size_t)v + 1] = make_float4((float)(x - xh), (float)(y - yh), (float)(z - zh), 0.f);
@@ -260,31 +272,53 @@ struct TetData {
   float4 eh[3], el[3];
 };
 
+// record difference a - b: coordinates in [1, 2], so the high words
+// subtract exactly; the field pair takes a TwoSum
+__device__ __forceinline__ void rdiff(const float4& ah, const float4& al, const float4& bh, const float4& bl,
+                                      float4& dh, float4& dl) {
+  dh.x = ah.x - bh.x; dl.x = al.x - bl.x;
+  dh.y = ah.y - bh.y; dl.y = al.y - bl.y;
+  dh.z = ah.z - bh.z; dl.z = al.z - bl.z;
+  float e;
+  two_sum(ah.w, -bh.w, dh.w, e);
+  dl.w = (al.w - bl.w) + e;
+}
+
 __device__ __forceinline__ TetData load_tet(const float4* __restrict__ vr, int4 tv) {
   TetData d;
   const float4 h0 = ld4(vr + 2 * (size_t)tv.x), l0 = ld4(vr + 2 * (size_t)tv.x + 1);
   const float4 h1 = ld4(vr + 2 * (size_t)tv.y), l1 = ld4(vr + 2 * (size_t)tv.y + 1);
   const float4 h2 = ld4(vr + 2 * (size_t)tv.z), l2 = ld4(vr + 2 * (size_t)tv.z + 1);
   const float4 h3 = ld4(vr + 2 * (size_t)tv.w), l3 = ld4(vr + 2 * (size_t)tv.w + 1);
-  pdiff(h1, l1, h0, l0, d.eh[0], d.el[0]);
-  pdiff(h2, l2, h0, l0, d.eh[1], d.el[1]);
-  pdiff(h3, l3, h0, l0, d.eh[2], d.el[2]);
+  rdiff(h1, l1, h0, l0, d.eh[0], d.el[0]);
+  rdiff(h2, l2, h0, l0, d.eh[1], d.el[1]);
+  rdiff(h3, l3, h0, l0, d.eh[2], d.el[2]);
   return d;
 }
 
 // ---------------------------------------------------------------------------
 // tet: gradient value and packed correction
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kBlock, 5) k_fast_tet(DevMesh m, const float4* __restrict__ vr,
+__global__ void __launch_bounds__(kBlock, 5) k_fast_tet(DevMesh m, const float4* __restrict__ vr, float gscale,
                                                         uint4* __restrict__ td) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= m.T) return;
   int4 tv = __ldg(reinterpret_cast<const int4*>(m.ev) + t);
   TetData d = load_tet(vr, tv);
-  // first estimate from the high parts with an approximate inverse; the
-  // correction J^{-1}(du - J g) with the compensated residual makes the
-  // result accurate to second order in both approximations
-  Cof cf = cofactors(d.eh[0], d.eh[1], d.eh[2]);
+  // first estimate with an approximate inverse of the rounded edge matrix
+  // (hi + lo: the high words alone, exact differences of [1, 2] values, are
+  // off by up to 2^-23 absolute, which squared through the correction would
+  // exceed the accuracy the error bound assumes); the correction
+  // J^{-1}(du - J g) with the compensated residual makes the result accurate
+  // to second order in both approximations
+  Cof cf;
+  {
+    float4 er[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+      er[i] = make_float4(d.eh[i].x + d.el[i].x, d.eh[i].y + d.el[i].y, d.eh[i].z + d.el[i].z, 0.f);
+    cf = cofactors(er[0], er[1], er[2]);
+  }
   float g[3], c[3], s[3], r[3];
   apply_inv(cf, d.eh[0].w, d.eh[1].w, d.eh[2].w, g);
   apply_inv(cf, comp_residual(d.eh[0], d.el[0], g[0], g[1], g[2]), comp_residual(d.eh[1], d.el[1], g[0], g[1], g[2]),
@@ -295,8 +329,11 @@ __global__ void __launch_bounds__(kBlock, 5) k_fast_tet(DevMesh m, const float4*
     s[j] = g[j] + c[j];
     r[j] = c[j] - (s[j] - g[j]);
   }
-  td[t] = make_uint4(__float_as_uint(s[0]), __float_as_uint(s[1]), __float_as_uint(s[2]),
-                     pack_corr(s[0], s[1], s[2], r[0], r[1], r[2]));
+  // back to the mesh's coordinates: the correction word is relative to the
+  // largest |s_j|, so scaling s by a power of two scales r with it
+  const uint32_t corr = pack_corr(s[0], s[1], s[2], r[0], r[1], r[2]);
+  td[t] = make_uint4(__float_as_uint(s[0] * gscale), __float_as_uint(s[1] * gscale),
+                     __float_as_uint(s[2] * gscale), corr);
 }
 
 // ---------------------------------------------------------------------------
@@ -766,8 +803,8 @@ int fast_error_blocks(int T) {
   return nb < g ? nb : g;
 }
 
-void fast_prep_coords(const DevMesh& m, float4* vrec, cudaStream_t s) {
-  if (m.V) k_prep_coords<<<nblk(m.V), kBlock, 0, s>>>(m.V, m.xyz, vrec);
+void fast_prep_coords(const DevMesh& m, const double* frame, float4* vrec, cudaStream_t s) {
+  if (m.V) k_prep_coords<<<nblk(m.V), kBlock, 0, s>>>(m.V, m.xyz, frame[0], frame[1], frame[2], frame[3], vrec);
 }
 
 void fast_geometry(const DevMesh& m, float2* geo, double2* geo64, float* half_len, cudaStream_t s) {
@@ -779,8 +816,8 @@ void fast_prep(const DevMesh& m, const double* u, const float4* crec, float4* vr
   if (m.V) k_prep<<<nblk(m.V), kBlock, 0, s>>>(m.V, u, crec, vrec);
 }
 
-void fast_tet(const DevMesh& m, const float4* vrec, uint4* td, cudaStream_t s) {
-  if (m.T) k_fast_tet<<<nblk(m.T), kBlock, 0, s>>>(m, vrec, td);
+void fast_tet(const DevMesh& m, const float4* vrec, float gscale, uint4* td, cudaStream_t s) {
+  if (m.T) k_fast_tet<<<nblk(m.T), kBlock, 0, s>>>(m, vrec, gscale, td);
 }
 
 void fast_weights(const DevMesh& m, float* w, double* w64, ExpandList xl, int* n_refit, unsigned char* listed,

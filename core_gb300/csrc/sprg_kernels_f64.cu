@@ -25,6 +25,7 @@ constexpr int kExpandMaxElems = 1024;
 constexpr int kExpandHash = 4096;
 constexpr int kExpandGrid = 304;  // 2 resident single-warp blocks per SM
 constexpr int kExpandSmemRows = 96;  // patches up to this size keep their QR rows in shared memory
+constexpr int kTriThreadRows = 8;    // triangle patches up to this size take the thread-per-vertex QR
 
 __device__ __forceinline__ void set_status(DevStatus* st, int code, int where) {
   if (atomicCAS(&st->code, 0, code) == 0) st->where = where;
@@ -109,11 +110,9 @@ __global__ void __launch_bounds__(kBlock) k_grad_ip(DevMesh m, const double* __r
 // rows go to the expansion list.
 // ---------------------------------------------------------------------
 template <int NT, int NC, int RPL>
-__global__ void __launch_bounds__(kBlock) k_recover(DevMesh m, const double* __restrict__ ip,
-                                                    double* __restrict__ rec, ExpandList xl) {
-  const int lane = threadIdx.x & 31;
-  const int v = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
-  if (v >= m.V) return;
+__device__ __forceinline__ void recover_vertex_warp(const DevMesh& m, const double* __restrict__ ip,
+                                                    double* __restrict__ rec, const ExpandList& xl, int v,
+                                                    int lane) {
   const int beg = m.p_off[v];
   const int cnt = m.p_off[v + 1] - beg;
   if (cnt < NT || cnt > 32 * RPL) {
@@ -219,6 +218,157 @@ __global__ void __launch_bounds__(kBlock) k_recover(DevMesh m, const double* __r
 #pragma unroll
     for (int j = 0; j < NT; ++j) sres += x[j] * terms[j];
     if (lane == c) rec[(size_t)v * NC + c] = sres;
+  }
+}
+
+template <int NT, int NC, int RPL>
+__global__ void __launch_bounds__(kBlock) k_recover(DevMesh m, const double* __restrict__ ip,
+                                                    double* __restrict__ rec, ExpandList xl) {
+  const int lane = threadIdx.x & 31;
+  const int v = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+  if (v >= m.V) return;
+  recover_vertex_warp<NT, NC, RPL>(m, ip, rec, xl, v, lane);
+}
+
+// the warp path over a vertex list (the patches too large for the thread
+// path); a fixed grid of warps strides over the device-side count
+template <int NT, int NC, int RPL>
+__global__ void __launch_bounds__(kBlock) k_recover_list(DevMesh m, const double* __restrict__ ip,
+                                                         double* __restrict__ rec, ExpandList xl, ExpandList list) {
+  const int lane = threadIdx.x & 31;
+  int n = *list.count;
+  n = n < list.cap ? n : list.cap;
+  const int nw = (int)((gridDim.x * (size_t)blockDim.x) >> 5);
+  for (int w = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5); w < n; w += nw)
+    recover_vertex_warp<NT, NC, RPL>(m, ip, rec, xl, list.items[w], lane);
+}
+
+// ---------------------------------------------------------------------
+// spr::recoverField on triangles -- one thread per vertex for patches of
+// NT..MAXM elements, in the reference's own operation order
+// (mth/mthQR.cc:19-160, spr/sprRecoverField.cc:226-353):
+//   get_reflector      column norm from row k down, the 1e-10 rank test,
+//                      v = column + sgn * norm at k, v /= |v|;
+//   reflect_columns    dot from row k down, a -= (2 dot) v_i;
+//   reflect_rows       Q = I H_1 H_2 H_3: every row of Q evolves on its own,
+//                      so the rows are built one at a time and only their
+//                      first NT entries (the columns y = Q^T b reads) kept;
+//   solveFromQR        y_i = sum over rows in ascending order, back
+//                      substitution, then the fit evaluated at the vertex.
+// Columns left of k, which reflect_columns also updates, are never read
+// again and are skipped.  Compiled without FMA contraction, the results
+// are bitwise those of that sequence.  Patches with fewer than NT elements
+// or rank deficient go to the expansion list, larger ones to `big` (the
+// warp path).
+// ---------------------------------------------------------------------
+template <int NC, int MAXM>
+__global__ void __launch_bounds__(128) k_recover_tri(DevMesh m, const double* __restrict__ ip,
+                                                     double* __restrict__ rec, ExpandList xl, ExpandList big) {
+  constexpr int NT = 3;
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= m.V) return;
+  const int beg = m.p_off[v];
+  const int cnt = m.p_off[v + 1] - beg;
+  if (cnt < NT || cnt > MAXM) {
+    const ExpandList& l = cnt < NT ? xl : big;
+    const int slot = atomicAdd(l.count, 1);
+    if (slot < l.cap) l.items[slot] = v;
+    return;
+  }
+  int el[MAXM];
+  double R[MAXM][NT];
+#pragma unroll
+  for (int i = 0; i < MAXM; ++i) {
+    el[i] = 0;
+    R[i][0] = R[i][1] = R[i][2] = 0;
+    if (i < cnt) {
+      el[i] = m.p_el[beg + i];
+      const V3 p = elem_ip_point(m, el[i]);
+      R[i][0] = 1.0;
+      R[i][1] = p.v[0];
+      R[i][2] = p.v[1];
+    }
+  }
+  double H[NT][MAXM];  // the reflectors
+#pragma unroll
+  for (int k = 0; k < NT; ++k) {
+    double cn = 0;
+#pragma unroll
+    for (int i = k; i < MAXM; ++i)
+      if (i < cnt) cn += R[i][k] * R[i][k];
+    cn = sqrt(cn);
+    if (cn < 1e-10) {
+      const int slot = atomicAdd(xl.count, 1);
+      if (slot < xl.cap) xl.items[slot] = v;
+      return;
+    }
+#pragma unroll
+    for (int i = 0; i < MAXM; ++i) H[k][i] = (i >= k && i < cnt) ? R[i][k] : 0.0;
+    H[k][k] += ((R[k][k] < 0) ? -1 : 1) * cn;
+    double rn = 0;
+#pragma unroll
+    for (int i = k; i < MAXM; ++i)
+      if (i < cnt) rn += H[k][i] * H[k][i];
+    rn = sqrt(rn);
+#pragma unroll
+    for (int i = k; i < MAXM; ++i)
+      if (i < cnt) H[k][i] /= rn;
+#pragma unroll
+    for (int j = k; j < NT; ++j) {
+      double dot = 0;
+#pragma unroll
+      for (int i = k; i < MAXM; ++i)
+        if (i < cnt) dot += R[i][j] * H[k][i];
+#pragma unroll
+      for (int i = k; i < MAXM; ++i)
+        if (i < cnt) R[i][j] -= 2 * dot * H[k][i];
+    }
+  }
+  // the first NT columns of Q, row by row
+  double Qc[MAXM][NT];
+#pragma unroll
+  for (int r = 0; r < MAXM; ++r) {
+    double q[MAXM];
+#pragma unroll
+    for (int j = 0; j < MAXM; ++j) q[j] = (j == r) ? 1.0 : 0.0;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) {
+      double dot = 0;
+#pragma unroll
+      for (int j = k; j < MAXM; ++j)
+        if (j < cnt) dot += q[j] * H[k][j];
+#pragma unroll
+      for (int j = k; j < MAXM; ++j)
+        if (j < cnt) q[j] -= 2 * dot * H[k][j];
+    }
+#pragma unroll
+    for (int i = 0; i < NT; ++i) Qc[r][i] = q[i];
+  }
+  const V3 xv = load_xyz(m.xyz, v);
+#pragma unroll 1
+  for (int c = 0; c < NC; ++c) {
+    double y[NT] = {0, 0, 0};
+#pragma unroll
+    for (int r = 0; r < MAXM; ++r)
+      if (r < cnt) {
+        const double b = ip[(size_t)el[r] * NC + c];
+#pragma unroll
+        for (int i = 0; i < NT; ++i) y[i] += Qc[r][i] * b;
+      }
+    double x[NT];
+#pragma unroll
+    for (int ii = 0; ii < NT; ++ii) {
+      const int i = NT - ii - 1;
+      x[i] = y[i];
+#pragma unroll
+      for (int j = i + 1; j < NT; ++j) x[i] -= R[i][j] * x[j];
+      x[i] /= R[i][i];
+    }
+    double sres = 0;
+    sres += x[0] * 1.0;
+    sres += x[1] * xv.v[0];
+    sres += x[2] * xv.v[1];
+    rec[(size_t)v * NC + c] = sres;
   }
 }
 
@@ -1140,19 +1290,28 @@ void launch_grad_ip_f64(const DevMesh& m, const double* f, int ncin, double* ip,
   if (m.T) k_grad_ip<<<nblk(m.T), kBlock, 0, s>>>(m, f, ncin, ip);
 }
 
-void launch_recover_f64(const DevMesh& m, const double* ip, int nc, double* rec, ExpandList xl, DevStatus* st,
-                        cudaStream_t s) {
+void launch_recover_f64(const DevMesh& m, const double* ip, int nc, double* rec, ExpandList xl, ExpandList big,
+                        DevStatus* st, cudaStream_t s) {
   (void)st;
   if (!m.V) return;
-  // one row per lane: patches of up to 32 elements (every interior patch of
-  // a structured tet or triangle mesh); larger ones take the slab path
-  int grid = nblk((long)m.V * 32);
   if (m.dim == 3) {
+    // one row per lane: patches of up to 32 elements (every interior patch of
+    // a structured tet mesh); larger ones take the slab path
+    int grid = nblk((long)m.V * 32);
     if (nc == 3) k_recover<4, 3, 1><<<grid, kBlock, 0, s>>>(m, ip, rec, xl);
     else k_recover<4, 9, 1><<<grid, kBlock, 0, s>>>(m, ip, rec, xl);
   } else {
-    if (nc == 3) k_recover<3, 3, 1><<<grid, kBlock, 0, s>>>(m, ip, rec, xl);
-    else k_recover<3, 9, 1><<<grid, kBlock, 0, s>>>(m, ip, rec, xl);
+    // triangles: a thread per vertex up to kTriThreadRows patch elements,
+    // then the warp path over the vertices it listed
+    const int grid = (m.V + 127) / 128;
+    const int lgrid = 152 * 8;
+    if (nc == 3) {
+      k_recover_tri<3, kTriThreadRows><<<grid, 128, 0, s>>>(m, ip, rec, xl, big);
+      k_recover_list<3, 3, 1><<<lgrid, kBlock, 0, s>>>(m, ip, rec, xl, big);
+    } else {
+      k_recover_tri<9, kTriThreadRows><<<grid, 128, 0, s>>>(m, ip, rec, xl, big);
+      k_recover_list<3, 9, 1><<<lgrid, kBlock, 0, s>>>(m, ip, rec, xl, big);
+    }
   }
 }
 
