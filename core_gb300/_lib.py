@@ -31,6 +31,11 @@ COLLAPSE = 1 << 2
 DONT_COLLAPSE = 1 << 3
 NEED_NOT_SPLIT = 1 << 17
 NEED_NOT_COLLAPSE = 1 << 18
+BAD_QUALITY = 1 << 5
+OK_QUALITY = 1 << 6
+SIZE_IDENTITY = 0
+SIZE_ISO = 1
+SIZE_ANISO = 2
 MARK_SPLIT = 0
 MARK_COLLAPSE = 1
 
@@ -47,6 +52,8 @@ EXPORTS = [
     "sprg_mlp_forward", "sprg_mlp_grad", "sprg_mlp_adam", "sprg_hessian_metric",
     "sprg_aniso_estimate_and_mark_resident", "sprg_set_batch", "sprg_batch_info", "sprg_set_autotune",
     "sprg_tuning_report", "sprg_graph_capture", "sprg_graph_replay", "sprg_set_tiling",
+    "sprg_measure_vertex_pairs", "sprg_get_maximum_edge_length", "sprg_get_average_edge_length",
+    "sprg_max_iterations_for_length", "sprg_mark_bad_quality", "sprg_get_min_quality",
 ]
 NOALLOC_MAX_ELEMS = 1 << 20
 
@@ -153,6 +160,12 @@ def load():
     lib.sprg_box_counts.argtypes = [I, I, I, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
                                     ctypes.POINTER(ctypes.c_int64)]
     lib.sprg_box_fill.argtypes = [I, I, I, D, D, D, P, P, P]
+    lib.sprg_measure_vertex_pairs.argtypes = [P, I, P, P, P, ctypes.c_int64, P, P]
+    lib.sprg_get_maximum_edge_length.argtypes = [P, I, P, P, P, ctypes.POINTER(D)]
+    lib.sprg_get_average_edge_length.argtypes = [P, ctypes.POINTER(D)]
+    lib.sprg_max_iterations_for_length.argtypes = [D]
+    lib.sprg_mark_bad_quality.argtypes = [P, D, P, ctypes.POINTER(ctypes.c_long)]
+    lib.sprg_get_min_quality.argtypes = [P, ctypes.POINTER(D)]
     _lib = lib
     return lib
 

@@ -185,6 +185,81 @@ class Context:
             None if ff is None else ff.ctypes.data, q.ctypes.data))
         return q
 
+    # -- MA sweeps around the marks -------------------------------------
+    def _size_kind(self, size, sizes, frames, identity):
+        if identity:
+            return _lib.SIZE_IDENTITY, None, None, None
+        if sizes is not None or frames is not None:
+            return (_lib.SIZE_ANISO, None, _f64(sizes).reshape(self.mesh.n_verts, 3),
+                    _f64(frames).reshape(self.mesh.n_verts, 9))
+        return _lib.SIZE_ISO, None if size is None else _f64(size), None, None
+
+    @staticmethod
+    def _ptr(a):
+        return None if a is None else a.ctypes.data
+
+    def measure_vertex_pairs(self, pairs, size=None, sizes=None, frames=None, identity=False):
+        """SizeField::measure of the would-be edges (vertex pairs, n x 2)."""
+        kind, s, ss, ff = self._size_kind(size, sizes, frames, identity)
+        pr = np.ascontiguousarray(pairs, np.int32).reshape(-1, 2)
+        out = np.empty(pr.shape[0], np.float64)
+        self._check(self._lib.sprg_measure_vertex_pairs(self.h, kind, self._ptr(s), self._ptr(ss), self._ptr(ff),
+                                                        pr.shape[0], pr.ctypes.data, out.ctypes.data))
+        return out
+
+    def getMaximumEdgeLength(self, size=None, sizes=None, frames=None, identity=False):
+        """ma::getMaximumEdgeLength(m, sf): identity=True is the reference's sf = 0
+        (IdentitySizeField); otherwise the isotropic (size, None = resident) or
+        anisotropic (sizes, frames) field."""
+        kind, s, ss, ff = self._size_kind(size, sizes, frames, identity)
+        out = ctypes.c_double()
+        self._check(self._lib.sprg_get_maximum_edge_length(self.h, kind, self._ptr(s), self._ptr(ss), self._ptr(ff),
+                                                           ctypes.byref(out)))
+        return out.value
+
+    def getAverageEdgeLength(self):
+        """ma::getAverageEdgeLength(m): mean apf::measure of the edges."""
+        out = ctypes.c_double()
+        self._check(self._lib.sprg_get_average_edge_length(self.h, ctypes.byref(out)))
+        return out.value
+
+    def markBadQuality(self, good_quality, flags):
+        """ma::markBadQuality on the qualities of the last measureQuality; element
+        flags (int32, n_elems) updated in place.  Returns the marked count."""
+        if flags.dtype != np.int32 or not flags.flags["C_CONTIGUOUS"]:
+            raise TypeError("flags must be a contiguous int32 array")
+        n = ctypes.c_long()
+        self._check(self._lib.sprg_mark_bad_quality(self.h, float(good_quality), flags.ctypes.data, ctypes.byref(n)))
+        return n.value
+
+    def getMinQuality(self):
+        """ma::getMinQuality on the qualities of the last measureQuality."""
+        out = ctypes.c_double()
+        self._check(self._lib.sprg_get_min_quality(self.h, ctypes.byref(out)))
+        return out.value
+
+    def collapseSizeCheck(self, keep, edges, adjacent, size=None, sizes=None, frames=None):
+        """ma::collapseSizeCheck (ma/maCoarsen.cc:47-60) for a batch of candidate
+        collapses: collapse i keeps vertex keep[i] and removes the other vertex
+        of edges[i]; adjacent[i] lists the edges the reference passes as
+        `adjacent`.  The new edges run from the kept vertex to the vertex of each
+        adjacent edge opposite the collapsing one; all are measured in one
+        launch.  Returns one bool per collapse (no new edge longer than 1.5)."""
+        ev = self.mesh.edge_verts
+        pairs, owner = [], []
+        for i, (k, e) in enumerate(zip(keep, edges)):
+            a, b = int(ev[e][0]), int(ev[e][1])
+            vc = b if a == k else a
+            for f in adjacent[i]:
+                p, q = int(ev[f][0]), int(ev[f][1])
+                pairs.append((k, q if p == vc else p))
+                owner.append(i)
+        ok = np.ones(len(keep), bool)
+        if pairs:
+            L = self.measure_vertex_pairs(np.array(pairs, np.int32), size, sizes, frames)
+            np.logical_and.at(ok, np.array(owner), ~(L > 1.5))
+        return ok
+
     # -- the whole pass --------------------------------------------------
     def estimate_and_mark(self, u, adapt_ratio, flags=None):
         """getGradIPField -> getSPRSizeField -> makeSizeField -> collapse/split marks.
@@ -274,6 +349,12 @@ class SizeField:
 
     def shouldCollapse(self):
         return self.measure() < 0.5
+
+
+def max_iterations_for_length(max_metric_length):
+    """The maximumIterations ma::configure derives from the maximum metric edge
+    length (updateMaxIterBasedOnSize, ma/maInput.cc:174-190)."""
+    return int(_lib.load().sprg_max_iterations_for_length(float(max_metric_length)))
 
 
 def apply_marks(split_bits, collapse_bits, flags):

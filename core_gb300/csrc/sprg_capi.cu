@@ -3,6 +3,7 @@
 // reference call.  See include/spr_gb300.h for the contract of every entry.
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -41,10 +42,11 @@ struct sprg_ctx {
   // fields
   DevBuf f, ip, rec, err, esize, size, L, flags, q, sizes3, frames9;
   int ip_nc = 0;
-  bool ip_valid = false, size_valid = false, L_valid = false;
+  bool ip_valid = false, size_valid = false, L_valid = false, q_valid = false;
   // scratch
   DevBuf partials, out3, status, count, xitems, xcount, slab, bits;
   DevBuf titems, tcountb;  // triangle patches above the thread-per-vertex size
+  DevBuf Lx, pairs, red, eflags;  // MA sweeps: lengths, vertex pairs, reduction scratch, element flags
   // FP32 path buffers
   DevBuf crec, vrec, rec32, q32, sz2, fcnt, guard, tetd, wts, w64, listed, geo, geo64, elen, fitems;
   DevBuf gstamp, gfit, grec, tstamp, tslot, trec, tcount;  // guard pipeline scratch
@@ -469,7 +471,7 @@ int sprg_destroy(sprg_ctx* c) {
   DevBuf* bufs[] = {&c->xyz,   &c->xyz32,   &c->ev,   &c->edv,   &c->poff,    &c->pel,    &c->aoff,
                     &c->ael,   &c->tmp,     &c->f,    &c->ip,    &c->rec,     &c->err,    &c->esize,
                     &c->size,  &c->L,       &c->flags, &c->q,    &c->sizes3,  &c->frames9, &c->partials,
-                    &c->out3,  &c->status,  &c->count, &c->xitems, &c->xcount, &c->slab, &c->bits, &c->titems, &c->tcountb,
+                    &c->out3,  &c->status,  &c->count, &c->xitems, &c->xcount, &c->slab, &c->bits, &c->titems, &c->tcountb, &c->Lx, &c->pairs, &c->red, &c->eflags,
                     &c->crec,  &c->vrec,    &c->rec32, &c->q32, &c->sz2,  &c->fcnt,   &c->guard, &c->tetd,
                     &c->wts,   &c->w64,     &c->listed, &c->geo, &c->geo64, &c->elen, &c->fitems, &c->gstamp, &c->gfit, &c->grec,
                     &c->tstamp, &c->tslot,  &c->trec, &c->tcount, &c->hess, &c->pcls, &c->bverts, &c->btiles, &c->bnext, &c->bvoff, &c->bseg, &c->bsegoff, &c->bratios, &c->vvoff, &c->vv, &c->vtile, &c->vr16, &c->rec16,
@@ -692,8 +694,159 @@ int sprg_measure_quality(sprg_ctx* c, const double* size, const double* sizes, c
   c->launches += 1;
   rc = check_launch(c, "quality");
   if (rc) return rc;
+  c->q_valid = true;
   CK(cudaMemcpyAsync(q, c->q.p, sizeof(double) * (size_t)m.T, cudaMemcpyDeviceToHost, c->stream));
   return sync_and_status(c);
+}
+
+// ---- MA sweeps around the marks ----------------------------------------
+
+// device inputs of a size field of the given kind (uploads host arrays;
+// an isotropic field without `size` is the resident one)
+static int size_field_inputs(sprg_ctx* c, int kind, const double* size, const double* sizes, const double* frames,
+                             const double** ds, const double** dss, const double** dff) {
+  DevMesh& m = c->m;
+  *ds = *dss = *dff = nullptr;
+  if (kind == SPRG_SIZE_IDENTITY) return SPRG_OK;
+  if (kind == SPRG_SIZE_ISO) {
+    if (size) {
+      ENSURE(c->size, sizeof(double) * (size_t)m.V);
+      CK(cudaMemcpyAsync(c->size.p, size, sizeof(double) * (size_t)m.V, cudaMemcpyHostToDevice, c->stream));
+      c->size_valid = true;
+    } else if (!c->size_valid) {
+      return fail(c, SPRG_ESTATE, "no resident size field");
+    }
+    *ds = P<double>(c->size);
+    return SPRG_OK;
+  }
+  if (kind == SPRG_SIZE_ANISO) {
+    if (!sizes || !frames) return fail(c, SPRG_EINVAL, "an anisotropic size field needs sizes and frames");
+    ENSURE(c->sizes3, sizeof(double) * 3 * (size_t)m.V);
+    ENSURE(c->frames9, sizeof(double) * 9 * (size_t)m.V);
+    CK(cudaMemcpyAsync(c->sizes3.p, sizes, sizeof(double) * 3 * (size_t)m.V, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->frames9.p, frames, sizeof(double) * 9 * (size_t)m.V, cudaMemcpyHostToDevice, c->stream));
+    *dss = P<double>(c->sizes3);
+    *dff = P<double>(c->frames9);
+    return SPRG_OK;
+  }
+  return fail(c, SPRG_EINVAL, "unknown size field kind");
+}
+
+int sprg_measure_vertex_pairs(sprg_ctx* c, int kind, const double* size, const double* sizes, const double* frames,
+                              int64_t n_pairs, const int32_t* pairs, double* lengths) {
+  if (!c || n_pairs < 0 || (n_pairs > 0 && (!pairs || !lengths))) return SPRG_EINVAL;
+  const int V = c->m.V;
+  for (int64_t i = 0; i < 2 * n_pairs; ++i)
+    if (pairs[i] < 0 || pairs[i] >= V) return fail(c, SPRG_EINVAL, "vertex id out of range");
+  int rc = set_device(c);
+  if (rc) return rc;
+  c->launches = 0;
+  const double *ds, *dss, *dff;
+  if ((rc = size_field_inputs(c, kind, size, sizes, frames, &ds, &dss, &dff))) return rc;
+  if (n_pairs == 0) return sync_and_status(c);
+  ENSURE(c->pairs, sizeof(int) * 2 * (size_t)n_pairs);
+  ENSURE(c->Lx, sizeof(double) * (size_t)n_pairs);
+  CK(cudaMemcpyAsync(c->pairs.p, pairs, sizeof(int) * 2 * (size_t)n_pairs, cudaMemcpyHostToDevice, c->stream));
+  launch_measure_pairs(c->m, kind, n_pairs, P<int>(c->pairs), ds, dss, dff, P<double>(c->Lx), c->stream);
+  c->launches += 1;
+  if ((rc = check_launch(c, "measure pairs"))) return rc;
+  CK(cudaMemcpyAsync(lengths, c->Lx.p, sizeof(double) * (size_t)n_pairs, cudaMemcpyDeviceToHost, c->stream));
+  return sync_and_status(c);
+}
+
+int sprg_get_maximum_edge_length(sprg_ctx* c, int kind, const double* size, const double* sizes,
+                                 const double* frames, double* out) {
+  if (!c || !out) return SPRG_EINVAL;
+  int rc = set_device(c);
+  if (rc) return rc;
+  c->launches = 0;
+  DevMesh& m = c->m;
+  const double *ds, *dss, *dff;
+  if ((rc = size_field_inputs(c, kind, size, sizes, frames, &ds, &dss, &dff))) return rc;
+  ENSURE(c->Lx, sizeof(double) * (size_t)(m.E > 0 ? m.E : 1));
+  ENSURE(c->red, sizeof(double) * (size_t)(sum_partials_count() + 4));
+  launch_measure_pairs(m, kind, m.E, nullptr, ds, dss, dff, P<double>(c->Lx), c->stream);
+  launch_max_positive(m.E, P<double>(c->Lx), P<unsigned long long>(c->red), c->stream);
+  c->launches += 2;
+  if ((rc = check_launch(c, "maximum edge length"))) return rc;
+  unsigned long long bits = 0;
+  CK(cudaMemcpyAsync(&bits, c->red.p, sizeof bits, cudaMemcpyDeviceToHost, c->stream));
+  if ((rc = sync_and_status(c))) return rc;
+  double v;
+  std::memcpy(&v, &bits, sizeof v);
+  *out = v;
+  return SPRG_OK;
+}
+
+int sprg_get_average_edge_length(sprg_ctx* c, double* out) {
+  if (!c || !out) return SPRG_EINVAL;
+  int rc = set_device(c);
+  if (rc) return rc;
+  c->launches = 0;
+  DevMesh& m = c->m;
+  ENSURE(c->Lx, sizeof(double) * (size_t)(m.E > 0 ? m.E : 1));
+  ENSURE(c->red, sizeof(double) * (size_t)(sum_partials_count() + 4));
+  launch_measure_pairs(m, SPRG_SIZE_IDENTITY, m.E, nullptr, nullptr, nullptr, nullptr, P<double>(c->Lx), c->stream);
+  double* partials = P<double>(c->red) + 4;
+  launch_sum(m.E, P<double>(c->Lx), partials, P<double>(c->red), c->stream);
+  c->launches += 3;
+  if ((rc = check_launch(c, "average edge length"))) return rc;
+  double sum = 0;
+  CK(cudaMemcpyAsync(&sum, c->red.p, sizeof sum, cudaMemcpyDeviceToHost, c->stream));
+  if ((rc = sync_and_status(c))) return rc;
+  *out = sum / (double)m.E;
+  return SPRG_OK;
+}
+
+int sprg_max_iterations_for_length(double max_metric_length) {
+  const int iter = (int)std::ceil(std::log2(max_metric_length));
+  return iter >= 10 ? 10 : iter + 1;
+}
+
+int sprg_mark_bad_quality(sprg_ctx* c, double good_quality, int32_t* flags, long* count) {
+  if (!c || !flags) return SPRG_EINVAL;
+  if (!c->q_valid) return fail(c, SPRG_ESTATE, "no resident element qualities (call sprg_measure_quality first)");
+  int rc = set_device(c);
+  if (rc) return rc;
+  c->launches = 0;
+  DevMesh& m = c->m;
+  ENSURE(c->eflags, sizeof(int) * (size_t)(m.T > 0 ? m.T : 1));
+  CK(cudaMemcpyAsync(c->eflags.p, flags, sizeof(int) * (size_t)m.T, cudaMemcpyHostToDevice, c->stream));
+  if ((rc = reset_status(c))) return rc;
+  CK(cudaMemsetAsync(c->count.p, 0, sizeof(unsigned long long), c->stream));
+  launch_mark_quality(m.T, P<double>(c->q), good_quality, P<int>(c->eflags), P<unsigned long long>(c->count),
+                      P<DevStatus>(c->status), c->stream);
+  c->launches += 1;
+  if ((rc = check_launch(c, "mark bad quality"))) return rc;
+  unsigned long long n = 0;
+  CK(cudaMemcpyAsync(&n, c->count.p, sizeof n, cudaMemcpyDeviceToHost, c->stream));
+  if ((rc = sync_and_status(c))) return rc;  // flags left untouched on the host on error
+  CK(cudaMemcpy(flags, c->eflags.p, sizeof(int) * (size_t)m.T, cudaMemcpyDeviceToHost));
+  if (count) *count = (long)n;
+  return SPRG_OK;
+}
+
+int sprg_get_min_quality(sprg_ctx* c, double* out) {
+  if (!c || !out) return SPRG_EINVAL;
+  if (!c->q_valid) return fail(c, SPRG_ESTATE, "no resident element qualities (call sprg_measure_quality first)");
+  int rc = set_device(c);
+  if (rc) return rc;
+  c->launches = 0;
+  DevMesh& m = c->m;
+  ENSURE(c->red, sizeof(double) * (size_t)(sum_partials_count() + 4));
+  unsigned long long* key = P<unsigned long long>(c->red);
+  launch_first_min_below(m.T, P<double>(c->q), 1.0, key, key + 1, c->stream);
+  c->launches += 2;
+  if ((rc = check_launch(c, "minimum quality"))) return rc;
+  unsigned long long first = 0;
+  CK(cudaMemcpyAsync(&first, key + 1, sizeof first, cudaMemcpyDeviceToHost, c->stream));
+  if ((rc = sync_and_status(c))) return rc;
+  if (first == ~0ull) {
+    *out = 1.0;  // no element below the reference's starting value
+    return SPRG_OK;
+  }
+  CK(cudaMemcpy(out, P<double>(c->q) + first, sizeof(double), cudaMemcpyDeviceToHost));
+  return SPRG_OK;
 }
 
 static BatchView batch_view(sprg_ctx* c) {

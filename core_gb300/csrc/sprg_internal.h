@@ -111,6 +111,22 @@ void launch_mark_bits(int E, const double* L, uint32_t* split, uint32_t* collaps
 // markEntities semantics from a predicate bitmap
 void launch_apply_bits(int E, const uint32_t* bits, int which, int* flags, unsigned long long* count,
                        DevStatus* st, cudaStream_t s);
+// MA sweeps around the marks.  kind: 0 identity size field, 1 isotropic
+// (size), 2 anisotropic (sizes, frames); pairs: n x 2 vertex ids, or NULL
+// for the mesh's edges (n = E)
+void launch_measure_pairs(const DevMesh& m, int kind, long long n, const int* pairs, const double* size,
+                          const double* sizes, const double* frames, double* L, cudaStream_t s);
+// *out = bits of max(0, the positive values of x) (NaN ignored)
+void launch_max_positive(long long n, const double* x, unsigned long long* out, cudaStream_t s);
+// deterministic sum: partials holds sum_partials_count() doubles
+int sum_partials_count();
+void launch_sum(long long n, const double* x, double* partials, double* out, cudaStream_t s);
+// first index (in *first, all ones if none) holding the minimum of the
+// values below `start`; *key is scratch
+void launch_first_min_below(long long n, const double* x, double start, unsigned long long* key,
+                            unsigned long long* first, cudaStream_t s);
+void launch_mark_quality(int T, const double* q, double good, int* flags, unsigned long long* count, DevStatus* st,
+                         cudaStream_t s);
 // FP64 guard band of the FP32 path: re-decide the listed edges' bits.
 // One FP64 gradient (at the integration point) per element the guard touches.
 struct GuardTet {

@@ -1281,6 +1281,146 @@ __global__ void k_xyz_f32(DevMesh m, float* xyz32) {
 
 inline int nblk(long n, int b = kBlock) { return (int)((n + b - 1) / b); }
 
+// ---------------------------------------------------------------------
+// MA sweeps around the marks (ma/maSize.cc:652-690, ma/maShape.cc:132-169,
+// ma/maCoarsen.cc:36-60)
+// ---------------------------------------------------------------------
+// length of the vertex pair (a, b) under a size field: kind 0 the identity
+// field (apf::measure of the edge, ma/maSize.cc:54-60), 1 the isotropic
+// user field, 2 the anisotropic one -- the same evaluation as the edge
+// measure kernels, for edges that may not exist yet
+__device__ __forceinline__ double pair_length(const DevMesh& m, int kind, int a, int b,
+                                              const double* __restrict__ size, const double* __restrict__ sizes,
+                                              const double* __restrict__ frames) {
+  const V3 xa = load_xyz(m.xyz, a), xb = load_xyz(m.xyz, b);
+  if (kind == 0) return edge_measure(xa, xb);
+  double hv[6], Rv[18];
+  if (kind == 1) {
+    const double sa = size[a], sb = size[b];
+    hv[0] = hv[1] = hv[2] = sa;
+    hv[3] = hv[4] = hv[5] = sb;
+    identity9(Rv);
+    identity9(Rv + 9);
+  } else {
+    const int vv[2] = {a, b};
+    for (int i = 0; i < 2; ++i) {
+      for (int k = 0; k < 3; ++k) hv[3 * i + k] = sizes[3 * (size_t)vv[i] + k];
+      for (int k = 0; k < 9; ++k) Rv[9 * i + k] = frames[9 * (size_t)vv[i] + k];
+    }
+  }
+  return metric_length(xa, xb, hv, Rv);
+}
+
+// pairs == nullptr: the mesh's own edges
+__global__ void __launch_bounds__(kBlock) k_measure_pairs(DevMesh m, int kind, long long n,
+                                                          const int* __restrict__ pairs,
+                                                          const double* __restrict__ size,
+                                                          const double* __restrict__ sizes,
+                                                          const double* __restrict__ frames, double* __restrict__ L) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int* ab = pairs ? pairs + 2 * i : m.edv + 2 * i;
+  L[i] = pair_length(m, kind, ab[0], ab[1], size, sizes, frames);
+}
+
+// getMaximumEdgeLength: the reference keeps `length > maxLength` from 0, so
+// NaN and non-positive lengths never win; positive doubles order like their
+// bit patterns, so the block maxima meet in one 64-bit atomicMax
+__global__ void __launch_bounds__(kBlock) k_max_positive(long long n, const double* __restrict__ x,
+                                                         unsigned long long* __restrict__ out) {
+  double best = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double v = x[i];
+    if (v > best) best = v;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) best = fmax(best, __shfl_xor_sync(0xffffffffu, best, o));
+  if ((threadIdx.x & 31) == 0 && best > 0.0) atomicMax(out, (unsigned long long)__double_as_longlong(best));
+}
+
+// fixed-grid partial sums in a fixed order, then one thread sums the
+// partials: the same bits on every run
+constexpr int kSumBlocks = 1024;
+__global__ void __launch_bounds__(kBlock) k_sum_partials(long long n, const double* __restrict__ x,
+                                                         double* __restrict__ partials) {
+  __shared__ double sh[kBlock / 32];
+  double s = 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    s += x[i];
+  s = warp_sum(s);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0;
+    for (int w = 0; w < kBlock / 32; ++w) t += sh[w];
+    partials[blockIdx.x] = t;
+  }
+}
+__global__ void k_sum_final(int nb, const double* __restrict__ partials, double* __restrict__ out) {
+  double t = 0;
+  for (int b = 0; b < nb; ++b) t += partials[b];
+  *out = t;
+}
+
+// getMinQuality: the reference scans the elements in order and keeps
+// `qual < minqual` from 1, i.e. the first element attaining the minimum
+// below 1 (NaN never wins).  Pass 1 finds the minimum value (-0 and +0
+// alike) through an order-preserving 64-bit key, pass 2 the first index
+// holding it; the result is that element's value.
+__device__ __forceinline__ unsigned long long order_key(double v) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v == 0.0 ? 0.0 : v);
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__global__ void __launch_bounds__(kBlock) k_min_below(long long n, const double* __restrict__ x, double start,
+                                                      unsigned long long* __restrict__ key) {
+  double best = start;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double v = x[i];
+    if (v < best) best = v;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) best = fmin(best, __shfl_xor_sync(0xffffffffu, best, o));
+  if ((threadIdx.x & 31) == 0 && best < start) atomicMin(key, order_key(best));
+}
+__global__ void __launch_bounds__(kBlock) k_first_equal(long long n, const double* __restrict__ x,
+                                                        const unsigned long long* __restrict__ key,
+                                                        unsigned long long* __restrict__ first) {
+  const unsigned long long k = *key;
+  const unsigned long long b = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
+  const double target = __longlong_as_double((long long)b);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    if (x[i] == target) {
+      atomicMin(first, (unsigned long long)i);
+      break;
+    }
+}
+
+// markBadQuality: ma::markEntities over the elements with predicate
+// quality < goodQuality, BAD_QUALITY / OK_QUALITY (ma/maShape.cc:132-136)
+__global__ void __launch_bounds__(kBlock) k_mark_quality(int T, const double* __restrict__ q, double good,
+                                                         int* __restrict__ flags, unsigned long long* count,
+                                                         DevStatus* st) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  int marked = 0;
+  if (e < T) {
+    int f = flags[e];
+    if (f & SPRG_BAD_QUALITY) {
+      set_status(st, SPRG_EFLAGS, e);
+    } else if (!(f & SPRG_OK_QUALITY)) {
+      if (q[e] < good) {
+        f |= SPRG_BAD_QUALITY;
+        marked = 1;
+      } else {
+        f |= SPRG_OK_QUALITY;
+      }
+      flags[e] = f;
+    }
+  }
+  const unsigned b = __ballot_sync(0xffffffffu, marked);
+  if ((threadIdx.x & 31) == 0 && b) atomicAdd(count, (unsigned long long)__popc(b));
+}
+
+
 }  // namespace
 
 // ----------------------------------------------------------------------
@@ -1435,4 +1575,37 @@ void launch_xyz_to_f32(const DevMesh& m, float* xyz32, cudaStream_t s) {
   if (m.V) k_xyz_f32<<<nblk(m.V), kBlock, 0, s>>>(m, xyz32);
 }
 
+
+void launch_measure_pairs(const DevMesh& m, int kind, long long n, const int* pairs, const double* size,
+                          const double* sizes, const double* frames, double* L, cudaStream_t s) {
+  if (n > 0) k_measure_pairs<<<(unsigned)((n + kBlock - 1) / kBlock), kBlock, 0, s>>>(m, kind, n, pairs, size, sizes,
+                                                                                    frames, L);
+}
+
+void launch_max_positive(long long n, const double* x, unsigned long long* out, cudaStream_t s) {
+  cudaMemsetAsync(out, 0, sizeof(unsigned long long), s);
+  if (n > 0) k_max_positive<<<kSumBlocks, kBlock, 0, s>>>(n, x, out);
+}
+
+int sum_partials_count() { return kSumBlocks; }
+
+void launch_sum(long long n, const double* x, double* partials, double* out, cudaStream_t s) {
+  k_sum_partials<<<kSumBlocks, kBlock, 0, s>>>(n, x, partials);
+  k_sum_final<<<1, 1, 0, s>>>(kSumBlocks, partials, out);
+}
+
+void launch_first_min_below(long long n, const double* x, double start, unsigned long long* key,
+                            unsigned long long* first, cudaStream_t s) {
+  cudaMemsetAsync(key, 0xff, sizeof(unsigned long long), s);
+  cudaMemsetAsync(first, 0xff, sizeof(unsigned long long), s);
+  if (n > 0) {
+    k_min_below<<<kSumBlocks, kBlock, 0, s>>>(n, x, start, key);
+    k_first_equal<<<kSumBlocks, kBlock, 0, s>>>(n, x, key, first);
+  }
+}
+
+void launch_mark_quality(int T, const double* q, double good, int* flags, unsigned long long* count, DevStatus* st,
+                         cudaStream_t s) {
+  if (T) k_mark_quality<<<nblk(T), kBlock, 0, s>>>(T, q, good, flags, count, st);
+}
 }  // namespace sprg

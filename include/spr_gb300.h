@@ -51,6 +51,8 @@ extern "C" {
 #define SPRG_DONT_COLLAPSE (1 << 3)
 #define SPRG_NEED_NOT_SPLIT (1 << 17)
 #define SPRG_NEED_NOT_COLLAPSE (1 << 18)
+#define SPRG_BAD_QUALITY (1 << 5)  /* element flags of ma::markBadQuality (ma/maAdapt.h:23-24) */
+#define SPRG_OK_QUALITY (1 << 6)
 
 /* which marking pass */
 #define SPRG_MARK_SPLIT 0    /* ma::markEdgesToSplit    (ma/maRefine.cc:395) */
@@ -150,6 +152,45 @@ int sprg_mark_edges(sprg_ctx* ctx, int which, int32_t* flags, long* count);
    given, the anisotropic one.  q: n_elems. */
 int sprg_measure_quality(sprg_ctx* ctx, const double* size, const double* sizes, const double* frames,
                          double* q);
+
+/* ---- MA sweeps around the marks -------------------------------------------
+   Size field kinds: SPRG_SIZE_IDENTITY is ma::IdentitySizeField (apf::measure
+   of the edge, ma/maSize.cc:49-92); SPRG_SIZE_ISO the isotropic user field
+   (`size`: n_verts, or NULL for the resident one); SPRG_SIZE_ANISO the
+   AnisoSizeField of `sizes` (n_verts x 3) and `frames` (n_verts x 9). */
+#define SPRG_SIZE_IDENTITY 0
+#define SPRG_SIZE_ISO 1
+#define SPRG_SIZE_ANISO 2
+
+/* SizeField::measure of would-be edges given as vertex pairs (pairs: n x 2),
+   e.g. the edges a collapse would create that ma::collapseSizeCheck measures
+   (ma/maCoarsen.cc:47-60).  lengths: n. */
+int sprg_measure_vertex_pairs(sprg_ctx* ctx, int kind, const double* size, const double* sizes, const double* frames,
+                              int64_t n_pairs, const int32_t* pairs, double* lengths);
+
+/* ma::getMaximumEdgeLength(m, sf) (ma/maSize.cc:673-690): the largest edge
+   measure, from 0 (all edges owned on one part). */
+int sprg_get_maximum_edge_length(sprg_ctx* ctx, int kind, const double* size, const double* sizes,
+                                 const double* frames, double* out);
+
+/* ma::getAverageEdgeLength(m) (ma/maSize.cc:652-671): mean apf::measure of
+   the edges (summed in a fixed tree order, not the reference's sequence). */
+int sprg_get_average_edge_length(sprg_ctx* ctx, double* out);
+
+/* The iteration count ma::configure derives from the maximum metric edge
+   length (updateMaxIterBasedOnSize, ma/maInput.cc:174-190):
+   ceil(log2(L)) + 1, at most 10. */
+int sprg_max_iterations_for_length(double max_metric_length);
+
+/* ma::markBadQuality (ma/maShape.cc:132-136): ma::markEntities over the
+   elements with quality < good_quality on the resident qualities of the last
+   sprg_measure_quality; flags: n_elems int words, BAD_QUALITY / OK_QUALITY
+   set in place (SPRG_EFLAGS if an element already carries BAD_QUALITY). */
+int sprg_mark_bad_quality(sprg_ctx* ctx, double good_quality, int32_t* flags, long* count);
+
+/* ma::getMinQuality (ma/maShape.cc:151-169) on the resident qualities: the
+   minimum below 1 (1 if none), the value of the first element holding it. */
+int sprg_get_min_quality(sprg_ctx* ctx, double* out);
 
 /* Anisotropic metric from a nodal Hessian (V x 9 row-major, e.g. the
    recovered field of the gradient of the recovered gradient): sizes (V x 3)

@@ -56,6 +56,15 @@ def load():
     L.orc_qr_decompose.argtypes = [_I, _I, _P, _P, _P, _P]
     L.orc_qr_solve.argtypes = [_I, _I, _P, _P, _P]
     L.orc_set_threads.argtypes = [_I]
+    L.orc_measure_pairs.argtypes = [_P, _I, _P, _P, _P, ctypes.c_long, _P, _P]
+    L.orc_max_edge_length.argtypes = [_P, _I, _P, _P, _P]
+    L.orc_max_edge_length.restype = _D
+    L.orc_average_edge_length.argtypes = [_P]
+    L.orc_average_edge_length.restype = _D
+    L.orc_max_iterations.argtypes = [_D]
+    L.orc_mark_bad_quality.argtypes = [_I, _P, _D, _P, ctypes.POINTER(ctypes.c_long)]
+    L.orc_min_quality.argtypes = [_I, _P]
+    L.orc_min_quality.restype = _D
     _lib = L
     return L
 
@@ -176,6 +185,37 @@ class OracleMesh:
                            None if ff is None else ff.ctypes.data, q.ctypes.data)
         return q
 
+    @staticmethod
+    def _sf(size, sizes, frames, identity):
+        """(kind, size, sizes, frames) arrays of a size field argument set."""
+        c = lambda a: None if a is None else np.ascontiguousarray(a, np.float64)
+        if identity:
+            return 0, None, None, None
+        if sizes is not None:
+            return 2, None, c(sizes), c(frames)
+        return 1, c(size), None, None
+
+    @staticmethod
+    def _p(a):
+        return None if a is None else a.ctypes.data
+
+    def measure_pairs(self, pairs, size=None, sizes=None, frames=None, identity=False):
+        kind, s, ss, ff = self._sf(size, sizes, frames, identity)
+        pr = np.ascontiguousarray(pairs, np.int32).reshape(-1, 2)
+        L = np.empty(pr.shape[0], np.float64)
+        rc = self.L.orc_measure_pairs(self.h, kind, self._p(s), self._p(ss), self._p(ff), pr.shape[0],
+                                      pr.ctypes.data, L.ctypes.data)
+        if rc:
+            raise ValueError("vertex id out of range")
+        return L
+
+    def max_edge_length(self, size=None, sizes=None, frames=None, identity=False):
+        kind, s, ss, ff = self._sf(size, sizes, frames, identity)
+        return self.L.orc_max_edge_length(self.h, kind, self._p(s), self._p(ss), self._p(ff))
+
+    def average_edge_length(self):
+        return self.L.orc_average_edge_length(self.h)
+
     def estimate_and_mark(self, u, adapt_ratio):
         """Returns (rc, size, L, flags, n_split, n_collapse, info)."""
         u = np.ascontiguousarray(u, np.float64)
@@ -188,6 +228,23 @@ class OracleMesh:
                                           L.ctypes.data, flags.ctypes.data, ctypes.byref(ns), ctypes.byref(nc),
                                           ctypes.byref(info))
         return rc, size, L, flags, ns.value, nc.value, info.as_dict()
+
+
+def max_iterations(max_metric_length):
+    return int(load().orc_max_iterations(float(max_metric_length)))
+
+
+def mark_bad_quality(q, good, flags):
+    """markBadQuality on given qualities; returns (rc, count); flags updated in place."""
+    qa = np.ascontiguousarray(q, np.float64)
+    c = ctypes.c_long()
+    rc = load().orc_mark_bad_quality(qa.shape[0], qa.ctypes.data, float(good), flags.ctypes.data, ctypes.byref(c))
+    return rc, c.value
+
+
+def min_quality(q):
+    qa = np.ascontiguousarray(q, np.float64)
+    return load().orc_min_quality(qa.shape[0], qa.ctypes.data)
 
 
 def mark_edges(L, which, flags):

@@ -977,8 +977,10 @@ static void vertex_metric(const double* sizes3, const double* frames9, const dou
    +-0.577350269189626, w = 1 (ma/maSize.cc:158-214, apf/apfIntegrate.cc:41-53).
    Either size1 (IsoUserField: makeSizeField(m, size)) or sizes3 + frames9
    (AnisoSizeField::init: makeSizeField(m, sizes, frames, false)). */
-static double metric_length(const orc_mesh* m, int edge, const double* size1, const double* sizes3, const double* frames9) {
-  const int* ev = m->dn[1] + 2 * (size_t)edge;
+/* MetricSizeField::measure of the vertex pair (a, b) (ma/maSize.cc:158-216) */
+static double pair_metric_length(const orc_mesh* m, int a0, int b0, const double* size1, const double* sizes3,
+                                 const double* frames9) {
+  const int ev[2] = {a0, b0};
   V3 x[2] = {vert_xyz(m, ev[0]), vert_xyz(m, ev[1])};
   double hv[6], Rv[18];
   for (int a = 0; a < 2; ++a) vertex_metric(sizes3, frames9, size1, ev[a], hv + 3 * a, Rv + 9 * a);
@@ -994,6 +996,11 @@ static double metric_length(const orc_mesh* m, int edge, const double* size1, co
     measurement += 1 * dV2;
   }
   return measurement;
+}
+
+static double metric_length(const orc_mesh* m, int edge, const double* size1, const double* sizes3, const double* frames9) {
+  const int* ev = m->dn[1] + 2 * (size_t)edge;
+  return pair_metric_length(m, ev[0], ev[1], size1, sizes3, frames9);
 }
 
 int orc_measure_edges(const orc_mesh* m, const double* size1, const double* sizes3, const double* frames9, double* L) {
@@ -1101,6 +1108,81 @@ int orc_estimate_and_mark(const orc_mesh* m, const double* u, double adapt_ratio
   if (!L_out) free(L);
   if (!flags_out) free(flags);
   return rc;
+}
+
+/* ------------------------------------------------------------------ */
+/* MA sweeps around the marks                                           */
+/* ------------------------------------------------------------------ */
+/* SizeField::measure of a vertex pair; kind 0: IdentitySizeField
+   (apf::measure of the edge, ma/maSize.cc:54-60), 1: isotropic user field,
+   2: anisotropic (sizes3, frames9) */
+static double pair_length(const orc_mesh* m, int kind, int a, int b, const double* size1, const double* sizes3,
+                          const double* frames9) {
+  if (kind == 0) return edge_measure(vert_xyz(m, a), vert_xyz(m, b));
+  return kind == 1 ? pair_metric_length(m, a, b, size1, NULL, NULL) : pair_metric_length(m, a, b, NULL, sizes3, frames9);
+}
+
+int orc_measure_pairs(const orc_mesh* m, int kind, const double* size1, const double* sizes3, const double* frames9,
+                      long n, const int* pairs, double* L) {
+  for (long i = 0; i < n; ++i) {
+    if (pairs[2 * i] < 0 || pairs[2 * i] >= m->n[0] || pairs[2 * i + 1] < 0 || pairs[2 * i + 1] >= m->n[0])
+      return ORC_EINVAL;
+    L[i] = pair_length(m, kind, pairs[2 * i], pairs[2 * i + 1], size1, sizes3, frames9);
+  }
+  return ORC_OK;
+}
+
+/* getMaximumEdgeLength (ma/maSize.cc:673-690) */
+double orc_max_edge_length(const orc_mesh* m, int kind, const double* size1, const double* sizes3,
+                           const double* frames9) {
+  double maxLength = 0.0;
+  for (int e = 0; e < m->n[1]; ++e) {
+    const int* ev = m->dn[1] + 2 * (size_t)e;
+    double length = pair_length(m, kind, ev[0], ev[1], size1, sizes3, frames9);
+    if (length > maxLength) maxLength = length;
+  }
+  return maxLength;
+}
+
+/* getAverageEdgeLength (ma/maSize.cc:652-671) */
+double orc_average_edge_length(const orc_mesh* m) {
+  double length_sum = 0, edge_count = 0;
+  for (int e = 0; e < m->n[1]; ++e) {
+    const int* ev = m->dn[1] + 2 * (size_t)e;
+    length_sum += edge_measure(vert_xyz(m, ev[0]), vert_xyz(m, ev[1]));
+    edge_count += 1.0;
+  }
+  return length_sum / edge_count;
+}
+
+/* updateMaxIterBasedOnSize (ma/maInput.cc:174-190) */
+int orc_max_iterations(double max_metric_length) {
+  int iter = (int)ceil(log2(max_metric_length));
+  return iter >= 10 ? 10 : iter + 1;
+}
+
+/* markBadQuality = markEntities(dim, quality < goodQuality, BAD_QUALITY,
+   OK_QUALITY) (ma/maShape.cc:132-136, ma/maAdapt.cc:293-324) */
+int orc_mark_bad_quality(int T, const double* q, double good, int* flags, long* count) {
+  const int BAD_QUALITY = 1 << 5, OK_QUALITY = 1 << 6;
+  long c = 0;
+  for (int e = 0; e < T; ++e)
+    if (flags[e] & BAD_QUALITY) return ORC_EFLAGS;
+  for (int e = 0; e < T; ++e) {
+    if (OK_QUALITY & flags[e]) continue;
+    if (q[e] < good) { flags[e] |= BAD_QUALITY; ++c; }
+    else flags[e] |= OK_QUALITY;
+  }
+  *count = c;
+  return ORC_OK;
+}
+
+/* getMinQuality (ma/maShape.cc:151-169) */
+double orc_min_quality(int T, const double* q) {
+  double minqual = 1;
+  for (int e = 0; e < T; ++e)
+    if (q[e] < minqual) minqual = q[e];
+  return minqual;
 }
 
 int orc_set_threads(int n) {
