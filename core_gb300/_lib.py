@@ -16,7 +16,8 @@ SPRG_EFLAGS = 3
 SPRG_ENOMEM = 4
 SPRG_ECUDA = 5
 SPRG_ESTATE = 6
-ERROR_NAMES = {1: "EINVAL", 2: "EPATCH", 3: "EFLAGS", 4: "ENOMEM", 5: "ECUDA", 6: "ESTATE"}
+SPRG_EEIGEN = 7
+ERROR_NAMES = {1: "EINVAL", 2: "EPATCH", 3: "EFLAGS", 4: "ENOMEM", 5: "ECUDA", 6: "ESTATE", 7: "EEIGEN"}
 
 SPRG_FP64 = 0
 SPRG_FP32 = 1
@@ -36,6 +37,7 @@ OK_QUALITY = 1 << 6
 SIZE_IDENTITY = 0
 SIZE_ISO = 1
 SIZE_ANISO = 2
+SIZE_LOG_ANISO = 3
 MARK_SPLIT = 0
 MARK_COLLAPSE = 1
 
@@ -54,6 +56,7 @@ EXPORTS = [
     "sprg_tuning_report", "sprg_graph_capture", "sprg_graph_replay", "sprg_set_tiling",
     "sprg_measure_vertex_pairs", "sprg_get_maximum_edge_length", "sprg_get_average_edge_length",
     "sprg_max_iterations_for_length", "sprg_mark_bad_quality", "sprg_get_min_quality",
+    "sprg_measure_edges_log_aniso", "sprg_measure_quality_log_aniso",
 ]
 NOALLOC_MAX_ELEMS = 1 << 20
 
@@ -166,6 +169,8 @@ def load():
     lib.sprg_max_iterations_for_length.argtypes = [D]
     lib.sprg_mark_bad_quality.argtypes = [P, D, P, ctypes.POINTER(ctypes.c_long)]
     lib.sprg_get_min_quality.argtypes = [P, ctypes.POINTER(D)]
+    lib.sprg_measure_edges_log_aniso.argtypes = [P, P, P, P]
+    lib.sprg_measure_quality_log_aniso.argtypes = [P, P, P, P]
     _lib = lib
     return lib
 

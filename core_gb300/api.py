@@ -141,9 +141,9 @@ class Context:
         return out, info.as_dict()
 
     # -- ma -------------------------------------------------------------
-    def makeSizeField(self, size=None, sizes=None, frames=None):
-        """ma::makeSizeField(m, size) or ma::makeSizeField(m, sizes, frames, false)."""
-        return SizeField(self, size, sizes, frames)
+    def makeSizeField(self, size=None, sizes=None, frames=None, logInterpolation=False):
+        """ma::makeSizeField(m, size) or ma::makeSizeField(m, sizes, frames, logInterpolation)."""
+        return SizeField(self, size, sizes, frames, logInterpolation)
 
     def measure_edges(self, size=None):
         out = np.empty(self.mesh.n_edges, np.float64)
@@ -158,6 +158,24 @@ class Context:
         self._check(self._lib.sprg_measure_edges_aniso(self.h, sizes.ctypes.data, frames.ctypes.data,
                                                        out.ctypes.data))
         return out
+
+    def measure_edges_log_aniso(self, sizes, frames):
+        """makeSizeField(m, sizes, frames, true) (LogAnisoSizeField) + measure."""
+        sizes = _f64(sizes)
+        frames = _f64(frames).reshape(self.mesh.n_verts, 9)
+        out = np.empty(self.mesh.n_edges, np.float64)
+        self._check(self._lib.sprg_measure_edges_log_aniso(self.h, sizes.ctypes.data, frames.ctypes.data,
+                                                           out.ctypes.data))
+        return out
+
+    def measureQualityLog(self, sizes, frames):
+        """measureTetQuality / measureTriQuality under the LogAnisoSizeField."""
+        sizes = _f64(sizes)
+        frames = _f64(frames).reshape(self.mesh.n_verts, 9)
+        q = np.empty(self.mesh.n_elems, np.float64)
+        self._check(self._lib.sprg_measure_quality_log_aniso(self.h, sizes.ctypes.data, frames.ctypes.data,
+                                                             q.ctypes.data))
+        return q
 
     def _mark(self, which, flags):
         if flags.dtype != np.int32 or not flags.flags["C_CONTIGUOUS"]:
@@ -186,32 +204,33 @@ class Context:
         return q
 
     # -- MA sweeps around the marks -------------------------------------
-    def _size_kind(self, size, sizes, frames, identity):
+    def _size_kind(self, size, sizes, frames, identity, log=False):
         if identity:
             return _lib.SIZE_IDENTITY, None, None, None
         if sizes is not None or frames is not None:
-            return (_lib.SIZE_ANISO, None, _f64(sizes).reshape(self.mesh.n_verts, 3),
-                    _f64(frames).reshape(self.mesh.n_verts, 9))
+            return (_lib.SIZE_LOG_ANISO if log else _lib.SIZE_ANISO, None,
+                    _f64(sizes).reshape(self.mesh.n_verts, 3), _f64(frames).reshape(self.mesh.n_verts, 9))
         return _lib.SIZE_ISO, None if size is None else _f64(size), None, None
 
     @staticmethod
     def _ptr(a):
         return None if a is None else a.ctypes.data
 
-    def measure_vertex_pairs(self, pairs, size=None, sizes=None, frames=None, identity=False):
-        """SizeField::measure of the would-be edges (vertex pairs, n x 2)."""
-        kind, s, ss, ff = self._size_kind(size, sizes, frames, identity)
+    def measure_vertex_pairs(self, pairs, size=None, sizes=None, frames=None, identity=False, log=False):
+        """SizeField::measure of the would-be edges (vertex pairs, n x 2);
+        log=True selects the log-interpolated anisotropic field."""
+        kind, s, ss, ff = self._size_kind(size, sizes, frames, identity, log)
         pr = np.ascontiguousarray(pairs, np.int32).reshape(-1, 2)
         out = np.empty(pr.shape[0], np.float64)
         self._check(self._lib.sprg_measure_vertex_pairs(self.h, kind, self._ptr(s), self._ptr(ss), self._ptr(ff),
                                                         pr.shape[0], pr.ctypes.data, out.ctypes.data))
         return out
 
-    def getMaximumEdgeLength(self, size=None, sizes=None, frames=None, identity=False):
+    def getMaximumEdgeLength(self, size=None, sizes=None, frames=None, identity=False, log=False):
         """ma::getMaximumEdgeLength(m, sf): identity=True is the reference's sf = 0
         (IdentitySizeField); otherwise the isotropic (size, None = resident) or
-        anisotropic (sizes, frames) field."""
-        kind, s, ss, ff = self._size_kind(size, sizes, frames, identity)
+        anisotropic (sizes, frames; log=True: LogAnisoSizeField) field."""
+        kind, s, ss, ff = self._size_kind(size, sizes, frames, identity, log)
         out = ctypes.c_double()
         self._check(self._lib.sprg_get_maximum_edge_length(self.h, kind, self._ptr(s), self._ptr(ss), self._ptr(ff),
                                                            ctypes.byref(out)))
@@ -333,13 +352,15 @@ class Context:
 
 
 class SizeField:
-    """ma::SizeField over a context (IsoUserField or AnisoSizeField)."""
+    """ma::SizeField over a context (IsoUserField, AnisoSizeField or LogAnisoSizeField)."""
 
-    def __init__(self, ctx, size=None, sizes=None, frames=None):
-        self.ctx, self.size, self.sizes, self.frames = ctx, size, sizes, frames
+    def __init__(self, ctx, size=None, sizes=None, frames=None, log=False):
+        self.ctx, self.size, self.sizes, self.frames, self.log = ctx, size, sizes, frames, log
 
     def measure(self):
         """MetricSizeField::measure of every edge (MDS edge order)."""
+        if self.sizes is not None and self.log:
+            return self.ctx.measure_edges_log_aniso(self.sizes, self.frames)
         if self.sizes is not None:
             return self.ctx.measure_edges_aniso(self.sizes, self.frames)
         return self.ctx.measure_edges(self.size)

@@ -47,6 +47,7 @@ struct sprg_ctx {
   DevBuf partials, out3, status, count, xitems, xcount, slab, bits;
   DevBuf titems, tcountb;  // triangle patches above the thread-per-vertex size
   DevBuf Lx, pairs, red, eflags;  // MA sweeps: lengths, vertex pairs, reduction scratch, element flags
+  DevBuf logm;                    // LogAnisoSizeField: per-vertex log-metrics (V x 9)
   // FP32 path buffers
   DevBuf crec, vrec, rec32, q32, sz2, fcnt, guard, tetd, wts, w64, listed, geo, geo64, elen, fitems;
   DevBuf gstamp, gfit, grec, tstamp, tslot, trec, tcount;  // guard pipeline scratch
@@ -158,7 +159,9 @@ int sync_and_status(sprg_ctx* c) {
                 st.where >= 0 ? "SPR: patch construction failed at vertex " + std::to_string(st.where)
                               : std::string("SPR: expansion list overflow"));
   if (st.code == SPRG_EFLAGS)
-    return fail(c, SPRG_EFLAGS, "markEntities: edge " + std::to_string(st.where) + " already carries the true flag");
+    return fail(c, SPRG_EFLAGS, "markEntities: entity " + std::to_string(st.where) + " already carries the true flag");
+  if (st.code == SPRG_EEIGEN)
+    return fail(c, SPRG_EEIGEN, "eigenQR of a log-metric did not converge (entity " + std::to_string(st.where) + ")");
   if (st.code) return fail(c, st.code, "device status " + std::to_string(st.code));
   return SPRG_OK;
 }
@@ -471,7 +474,7 @@ int sprg_destroy(sprg_ctx* c) {
   DevBuf* bufs[] = {&c->xyz,   &c->xyz32,   &c->ev,   &c->edv,   &c->poff,    &c->pel,    &c->aoff,
                     &c->ael,   &c->tmp,     &c->f,    &c->ip,    &c->rec,     &c->err,    &c->esize,
                     &c->size,  &c->L,       &c->flags, &c->q,    &c->sizes3,  &c->frames9, &c->partials,
-                    &c->out3,  &c->status,  &c->count, &c->xitems, &c->xcount, &c->slab, &c->bits, &c->titems, &c->tcountb, &c->Lx, &c->pairs, &c->red, &c->eflags,
+                    &c->out3,  &c->status,  &c->count, &c->xitems, &c->xcount, &c->slab, &c->bits, &c->titems, &c->tcountb, &c->Lx, &c->pairs, &c->red, &c->eflags, &c->logm,
                     &c->crec,  &c->vrec,    &c->rec32, &c->q32, &c->sz2,  &c->fcnt,   &c->guard, &c->tetd,
                     &c->wts,   &c->w64,     &c->listed, &c->geo, &c->geo64, &c->elen, &c->fitems, &c->gstamp, &c->gfit, &c->grec,
                     &c->tstamp, &c->tslot,  &c->trec, &c->tcount, &c->hess, &c->pcls, &c->bverts, &c->btiles, &c->bnext, &c->bvoff, &c->bseg, &c->bsegoff, &c->bratios, &c->vvoff, &c->vv, &c->vtile, &c->vr16, &c->rec16,
@@ -702,11 +705,12 @@ int sprg_measure_quality(sprg_ctx* c, const double* size, const double* sizes, c
 // ---- MA sweeps around the marks ----------------------------------------
 
 // device inputs of a size field of the given kind (uploads host arrays;
-// an isotropic field without `size` is the resident one)
+// an isotropic field without `size` is the resident one; the log-
+// interpolated field gets its per-vertex log-metrics in *dlm)
 static int size_field_inputs(sprg_ctx* c, int kind, const double* size, const double* sizes, const double* frames,
-                             const double** ds, const double** dss, const double** dff) {
+                             const double** ds, const double** dss, const double** dff, const double** dlm) {
   DevMesh& m = c->m;
-  *ds = *dss = *dff = nullptr;
+  *ds = *dss = *dff = *dlm = nullptr;
   if (kind == SPRG_SIZE_IDENTITY) return SPRG_OK;
   if (kind == SPRG_SIZE_ISO) {
     if (size) {
@@ -719,7 +723,7 @@ static int size_field_inputs(sprg_ctx* c, int kind, const double* size, const do
     *ds = P<double>(c->size);
     return SPRG_OK;
   }
-  if (kind == SPRG_SIZE_ANISO) {
+  if (kind == SPRG_SIZE_ANISO || kind == SPRG_SIZE_LOG_ANISO) {
     if (!sizes || !frames) return fail(c, SPRG_EINVAL, "an anisotropic size field needs sizes and frames");
     ENSURE(c->sizes3, sizeof(double) * 3 * (size_t)m.V);
     ENSURE(c->frames9, sizeof(double) * 9 * (size_t)m.V);
@@ -727,6 +731,12 @@ static int size_field_inputs(sprg_ctx* c, int kind, const double* size, const do
     CK(cudaMemcpyAsync(c->frames9.p, frames, sizeof(double) * 9 * (size_t)m.V, cudaMemcpyHostToDevice, c->stream));
     *dss = P<double>(c->sizes3);
     *dff = P<double>(c->frames9);
+    if (kind == SPRG_SIZE_LOG_ANISO) {
+      ENSURE(c->logm, sizeof(double) * 9 * (size_t)(m.V > 0 ? m.V : 1));
+      launch_log_metric(m.V, *dss, *dff, P<double>(c->logm), c->stream);
+      c->launches += 1;
+      *dlm = P<double>(c->logm);
+    }
     return SPRG_OK;
   }
   return fail(c, SPRG_EINVAL, "unknown size field kind");
@@ -741,13 +751,15 @@ int sprg_measure_vertex_pairs(sprg_ctx* c, int kind, const double* size, const d
   int rc = set_device(c);
   if (rc) return rc;
   c->launches = 0;
-  const double *ds, *dss, *dff;
-  if ((rc = size_field_inputs(c, kind, size, sizes, frames, &ds, &dss, &dff))) return rc;
+  const double *ds, *dss, *dff, *dlm;
+  if ((rc = reset_status(c))) return rc;
+  if ((rc = size_field_inputs(c, kind, size, sizes, frames, &ds, &dss, &dff, &dlm))) return rc;
   if (n_pairs == 0) return sync_and_status(c);
   ENSURE(c->pairs, sizeof(int) * 2 * (size_t)n_pairs);
   ENSURE(c->Lx, sizeof(double) * (size_t)n_pairs);
   CK(cudaMemcpyAsync(c->pairs.p, pairs, sizeof(int) * 2 * (size_t)n_pairs, cudaMemcpyHostToDevice, c->stream));
-  launch_measure_pairs(c->m, kind, n_pairs, P<int>(c->pairs), ds, dss, dff, P<double>(c->Lx), c->stream);
+  launch_measure_pairs(c->m, kind, n_pairs, P<int>(c->pairs), ds, dss, dff, dlm, P<double>(c->Lx),
+                       P<DevStatus>(c->status), c->stream);
   c->launches += 1;
   if ((rc = check_launch(c, "measure pairs"))) return rc;
   CK(cudaMemcpyAsync(lengths, c->Lx.p, sizeof(double) * (size_t)n_pairs, cudaMemcpyDeviceToHost, c->stream));
@@ -761,11 +773,13 @@ int sprg_get_maximum_edge_length(sprg_ctx* c, int kind, const double* size, cons
   if (rc) return rc;
   c->launches = 0;
   DevMesh& m = c->m;
-  const double *ds, *dss, *dff;
-  if ((rc = size_field_inputs(c, kind, size, sizes, frames, &ds, &dss, &dff))) return rc;
+  const double *ds, *dss, *dff, *dlm;
+  if ((rc = reset_status(c))) return rc;
+  if ((rc = size_field_inputs(c, kind, size, sizes, frames, &ds, &dss, &dff, &dlm))) return rc;
   ENSURE(c->Lx, sizeof(double) * (size_t)(m.E > 0 ? m.E : 1));
   ENSURE(c->red, sizeof(double) * (size_t)(sum_partials_count() + 4));
-  launch_measure_pairs(m, kind, m.E, nullptr, ds, dss, dff, P<double>(c->Lx), c->stream);
+  launch_measure_pairs(m, kind, m.E, nullptr, ds, dss, dff, dlm, P<double>(c->Lx), P<DevStatus>(c->status),
+                       c->stream);
   launch_max_positive(m.E, P<double>(c->Lx), P<unsigned long long>(c->red), c->stream);
   c->launches += 2;
   if ((rc = check_launch(c, "maximum edge length"))) return rc;
@@ -786,7 +800,8 @@ int sprg_get_average_edge_length(sprg_ctx* c, double* out) {
   DevMesh& m = c->m;
   ENSURE(c->Lx, sizeof(double) * (size_t)(m.E > 0 ? m.E : 1));
   ENSURE(c->red, sizeof(double) * (size_t)(sum_partials_count() + 4));
-  launch_measure_pairs(m, SPRG_SIZE_IDENTITY, m.E, nullptr, nullptr, nullptr, nullptr, P<double>(c->Lx), c->stream);
+  launch_measure_pairs(m, SPRG_SIZE_IDENTITY, m.E, nullptr, nullptr, nullptr, nullptr, nullptr, P<double>(c->Lx),
+                       nullptr, c->stream);
   double* partials = P<double>(c->red) + 4;
   launch_sum(m.E, P<double>(c->Lx), partials, P<double>(c->red), c->stream);
   c->launches += 3;
@@ -795,6 +810,45 @@ int sprg_get_average_edge_length(sprg_ctx* c, double* out) {
   CK(cudaMemcpyAsync(&sum, c->red.p, sizeof sum, cudaMemcpyDeviceToHost, c->stream));
   if ((rc = sync_and_status(c))) return rc;
   *out = sum / (double)m.E;
+  return SPRG_OK;
+}
+
+int sprg_measure_edges_log_aniso(sprg_ctx* c, const double* sizes, const double* frames, double* lengths) {
+  if (!c || !sizes || !frames) return SPRG_EINVAL;
+  int rc = set_device(c);
+  if (rc) return rc;
+  c->launches = 0;
+  DevMesh& m = c->m;
+  const double *ds, *dss, *dff, *dlm;
+  if ((rc = reset_status(c))) return rc;
+  if ((rc = size_field_inputs(c, SPRG_SIZE_LOG_ANISO, nullptr, sizes, frames, &ds, &dss, &dff, &dlm))) return rc;
+  ENSURE(c->L, sizeof(double) * (size_t)(m.E > 0 ? m.E : 1));
+  launch_measure_pairs(m, SPRG_SIZE_LOG_ANISO, m.E, nullptr, nullptr, nullptr, nullptr, dlm, P<double>(c->L),
+                       P<DevStatus>(c->status), c->stream);
+  c->launches += 1;
+  if ((rc = check_launch(c, "measure log-aniso"))) return rc;
+  if ((rc = sync_and_status(c))) return rc;
+  c->L_valid = true;
+  if (lengths) CK(cudaMemcpy(lengths, c->L.p, sizeof(double) * (size_t)m.E, cudaMemcpyDeviceToHost));
+  return SPRG_OK;
+}
+
+int sprg_measure_quality_log_aniso(sprg_ctx* c, const double* sizes, const double* frames, double* q) {
+  if (!c || !sizes || !frames || !q) return SPRG_EINVAL;
+  int rc = set_device(c);
+  if (rc) return rc;
+  c->launches = 0;
+  DevMesh& m = c->m;
+  const double *ds, *dss, *dff, *dlm;
+  if ((rc = reset_status(c))) return rc;
+  if ((rc = size_field_inputs(c, SPRG_SIZE_LOG_ANISO, nullptr, sizes, frames, &ds, &dss, &dff, &dlm))) return rc;
+  ENSURE(c->q, sizeof(double) * (size_t)(m.T > 0 ? m.T : 1));
+  launch_quality_f64(m, nullptr, nullptr, nullptr, P<double>(c->q), c->stream, dlm, P<DevStatus>(c->status));
+  c->launches += 1;
+  if ((rc = check_launch(c, "quality log-aniso"))) return rc;
+  if ((rc = sync_and_status(c))) return rc;
+  c->q_valid = true;
+  CK(cudaMemcpy(q, c->q.p, sizeof(double) * (size_t)m.T, cudaMemcpyDeviceToHost));
   return SPRG_OK;
 }
 

@@ -112,10 +112,15 @@ void launch_mark_bits(int E, const double* L, uint32_t* split, uint32_t* collaps
 void launch_apply_bits(int E, const uint32_t* bits, int which, int* flags, unsigned long long* count,
                        DevStatus* st, cudaStream_t s);
 // MA sweeps around the marks.  kind: 0 identity size field, 1 isotropic
-// (size), 2 anisotropic (sizes, frames); pairs: n x 2 vertex ids, or NULL
-// for the mesh's edges (n = E)
+// (size), 2 anisotropic (sizes, frames), 3 log-interpolated anisotropic
+// (logm); pairs: n x 2 vertex ids, or NULL for the mesh's edges (n = E);
+// st records SPRG_EEIGEN when an eigen iteration fails
 void launch_measure_pairs(const DevMesh& m, int kind, long long n, const int* pairs, const double* size,
-                          const double* sizes, const double* frames, double* L, cudaStream_t s);
+                          const double* sizes, const double* frames, const double* logm, double* L, DevStatus* st,
+                          cudaStream_t s);
+// LogAnisoSizeField: per-vertex log-metric (V x 9) of sizes and frames; kind
+// 3 of launch_measure_pairs and the logm argument of launch_quality_f64 read it
+void launch_log_metric(int V, const double* sizes, const double* frames, double* logm, cudaStream_t s);
 // *out = bits of max(0, the positive values of x) (NaN ignored)
 void launch_max_positive(long long n, const double* x, unsigned long long* out, cudaStream_t s);
 // deterministic sum: partials holds sum_partials_count() doubles
@@ -158,7 +163,7 @@ void launch_guard_stage(int stage, const DevMesh& m, const double* u, const doub
 // per-mesh size factors of a batch (SPR mode) from segment partials
 void launch_size_factor_batch(const double* partials, BatchView bv, int dim, double* out4, cudaStream_t s);
 void launch_quality_f64(const DevMesh& m, const double* size, const double* sizes, const double* frames,
-                        double* q, cudaStream_t s);
+                        double* q, cudaStream_t s, const double* logm = nullptr, DevStatus* st = nullptr);
 // anisotropic metric (sizes V x 3, frames V x 9) from a nodal Hessian (V x 9)
 void launch_hessian_metric(const DevMesh& m, const double* H, double eps, double hmin, double hmax, double* sizes,
                            double* frames, cudaStream_t s);

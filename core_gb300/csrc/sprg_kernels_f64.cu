@@ -855,9 +855,12 @@ __device__ __forceinline__ double q_measure(const V3* x, int nn, int edim, const
   return measurement;
 }
 
+template <bool LOG>
 __global__ void __launch_bounds__(kBlock) k_quality(DevMesh m, const double* __restrict__ size,
                                                     const double* __restrict__ sizes,
-                                                    const double* __restrict__ frames, double* __restrict__ q) {
+                                                    const double* __restrict__ frames,
+                                                    const double* __restrict__ logm, double* __restrict__ q,
+                                                    DevStatus* st) {
   int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= m.T) return;
   const int* ev = m.ev + (size_t)e * m.nn;
@@ -868,12 +871,19 @@ __global__ void __launch_bounds__(kBlock) k_quality(DevMesh m, const double* __r
   for (int i = 0; i < m.nn; ++i) {
     int v = ev[i];
     double hv[3], Rv[9], N[1] = {1.0};
-    if (size) { hv[0] = hv[1] = hv[2] = size[v]; identity9(Rv); }
-    else {
-      for (int k = 0; k < 3; ++k) hv[k] = sizes[3 * (size_t)v + k];
-      for (int k = 0; k < 9; ++k) Rv[k] = frames[9 * (size_t)v + k];
+    M3 cQ;
+    if (LOG) {  // LogAnisoSizeField: the vertex's own log-metric
+      bool ok = true;
+      cQ = ref::log_transform(logm + 9 * (size_t)v, N, 1, &ok);
+      if (!ok) set_status(st, SPRG_EEIGEN, e);
+    } else {
+      if (size) { hv[0] = hv[1] = hv[2] = size[v]; identity9(Rv); }
+      else {
+        for (int k = 0; k < 3; ++k) hv[k] = sizes[3 * (size_t)v + k];
+        for (int k = 0; k < 9; ++k) Rv[k] = frames[9 * (size_t)v + k];
+      }
+      cQ = ref::get_transform(hv, Rv, N, 1);
     }
-    M3 cQ = ref::get_transform(hv, Rv, N, 1);
     double cJ = ref::jacobian_det(cQ, m.dim);
     if (cJ > maxJ) { maxJ = cJ; Q = cQ; }
   }
@@ -1285,15 +1295,41 @@ inline int nblk(long n, int b = kBlock) { return (int)((n + b - 1) / b); }
 // MA sweeps around the marks (ma/maSize.cc:652-690, ma/maShape.cc:132-169,
 // ma/maCoarsen.cc:36-60)
 // ---------------------------------------------------------------------
+// MetricSizeField::measure under LogAnisoSizeField (ma/maSize.cc:158-216,
+// 508-523): two Gauss points, log-metrics of both ends interpolated
+__device__ __forceinline__ double log_metric_length(const V3& x0, const V3& x1, const double* __restrict__ la,
+                                                    const double* __restrict__ lb, bool* ok) {
+  V3 x[2] = {x0, x1};
+  M3 J = ref::jacobian(x, 2, 1);
+  double Mv[18];
+  for (int k = 0; k < 9; ++k) {
+    Mv[k] = la[k];
+    Mv[9 + k] = lb[k];
+  }
+  const double gp[2] = {0.577350269189626, -0.577350269189626};
+  double measurement = 0;
+  for (int p = 0; p < 2; ++p) {
+    double N[2];
+    ref::edge_shape_values(gp[p], N);
+    M3 Q = ref::log_transform(Mv, N, 2, ok);
+    double dV2 = ref::jacobian_det(ref::mul(J, Q), 1);
+    measurement += 1 * dV2;
+  }
+  return measurement;
+}
+
 // length of the vertex pair (a, b) under a size field: kind 0 the identity
 // field (apf::measure of the edge, ma/maSize.cc:54-60), 1 the isotropic
-// user field, 2 the anisotropic one -- the same evaluation as the edge
-// measure kernels, for edges that may not exist yet
+// user field, 2 the anisotropic one, 3 LogAnisoSizeField (per-vertex
+// log-metrics) -- the same evaluation as the edge measure kernels, for
+// edges that may not exist yet
 __device__ __forceinline__ double pair_length(const DevMesh& m, int kind, int a, int b,
                                               const double* __restrict__ size, const double* __restrict__ sizes,
-                                              const double* __restrict__ frames) {
+                                              const double* __restrict__ frames, const double* __restrict__ logm,
+                                              bool* ok) {
   const V3 xa = load_xyz(m.xyz, a), xb = load_xyz(m.xyz, b);
   if (kind == 0) return edge_measure(xa, xb);
+  if (kind == 3) return log_metric_length(xa, xb, logm + 9 * (size_t)a, logm + 9 * (size_t)b, ok);
   double hv[6], Rv[18];
   if (kind == 1) {
     const double sa = size[a], sb = size[b];
@@ -1316,11 +1352,24 @@ __global__ void __launch_bounds__(kBlock) k_measure_pairs(DevMesh m, int kind, l
                                                           const int* __restrict__ pairs,
                                                           const double* __restrict__ size,
                                                           const double* __restrict__ sizes,
-                                                          const double* __restrict__ frames, double* __restrict__ L) {
+                                                          const double* __restrict__ frames,
+                                                          const double* __restrict__ logm, double* __restrict__ L,
+                                                          DevStatus* st) {
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int* ab = pairs ? pairs + 2 * i : m.edv + 2 * i;
-  L[i] = pair_length(m, kind, ab[0], ab[1], size, sizes, frames);
+  bool ok = true;
+  L[i] = pair_length(m, kind, ab[0], ab[1], size, sizes, frames, logm, &ok);
+  if (!ok) set_status(st, SPRG_EEIGEN, (int)i);
+}
+
+// LogAnisoSizeField::init: per-vertex log-metric from sizes and frames
+__global__ void __launch_bounds__(kBlock) k_log_metric(int V, const double* __restrict__ sizes,
+                                                       const double* __restrict__ frames,
+                                                       double* __restrict__ logm) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= V) return;
+  ref::vertex_logm(sizes + 3 * (size_t)v, frames + 9 * (size_t)v, logm + 9 * (size_t)v);
 }
 
 // getMaximumEdgeLength: the reference keeps `length > maxLength` from 0, so
@@ -1523,8 +1572,10 @@ void launch_apply_bits(int E, const uint32_t* bits, int which, int* flags, unsig
 }
 
 void launch_quality_f64(const DevMesh& m, const double* size, const double* sizes, const double* frames, double* q,
-                        cudaStream_t s) {
-  if (m.T) k_quality<<<nblk(m.T), kBlock, 0, s>>>(m, size, sizes, frames, q);
+                        cudaStream_t s, const double* logm, DevStatus* st) {
+  if (!m.T) return;
+  if (logm) k_quality<true><<<nblk(m.T), kBlock, 0, s>>>(m, size, sizes, frames, logm, q, st);
+  else k_quality<false><<<nblk(m.T), kBlock, 0, s>>>(m, size, sizes, frames, logm, q, st);
 }
 
 void launch_guard_stage(int stage, const DevMesh& m, const double* u, const double* out3, const int* items,
@@ -1577,9 +1628,15 @@ void launch_xyz_to_f32(const DevMesh& m, float* xyz32, cudaStream_t s) {
 
 
 void launch_measure_pairs(const DevMesh& m, int kind, long long n, const int* pairs, const double* size,
-                          const double* sizes, const double* frames, double* L, cudaStream_t s) {
-  if (n > 0) k_measure_pairs<<<(unsigned)((n + kBlock - 1) / kBlock), kBlock, 0, s>>>(m, kind, n, pairs, size, sizes,
-                                                                                    frames, L);
+                          const double* sizes, const double* frames, const double* logm, double* L, DevStatus* st,
+                          cudaStream_t s) {
+  if (n > 0)
+    k_measure_pairs<<<(unsigned)((n + kBlock - 1) / kBlock), kBlock, 0, s>>>(m, kind, n, pairs, size, sizes, frames,
+                                                                            logm, L, st);
+}
+
+void launch_log_metric(int V, const double* sizes, const double* frames, double* logm, cudaStream_t s) {
+  if (V) k_log_metric<<<nblk(V), kBlock, 0, s>>>(V, sizes, frames, logm);
 }
 
 void launch_max_positive(long long n, const double* x, unsigned long long* out, cudaStream_t s) {

@@ -199,5 +199,147 @@ __device__ __forceinline__ M3 get_transform(const double* hv, const double* Rv, 
   return mul(R, S);
 }
 
+// ---- mth::eigenQR on a 3x3 matrix (mth/mthQR.cc:19-297) -------------------
+// get_reflector with offset o (mth/mthQR.cc:19-45)
+__device__ inline bool eig_reflector(const M3& a, double* v, int k, int o) {
+  double cnorm = 0;
+  for (int i = k + o; i < 3; ++i) cnorm += a.m[i][k] * a.m[i][k];
+  cnorm = sqrt(cnorm);
+  if (cnorm < 1e-10) return false;
+  for (int i = 0; i < k + o; ++i) v[i] = 0;
+  for (int i = k + o; i < 3; ++i) v[i] = a.m[i][k];
+  v[k + o] += ((a.m[k + o][k] < 0) ? -1 : 1) * cnorm;
+  double rnorm = 0;
+  for (int i = k + o; i < 3; ++i) rnorm += v[i] * v[i];
+  rnorm = sqrt(rnorm);
+  for (int i = k + o; i < 3; ++i) v[i] /= rnorm;
+  return true;
+}
+// reflect_columns / reflect_rows (mth/mthQR.cc:47-79)
+__device__ inline void eig_reflect_columns(const double* v, M3& a, int k, int o) {
+  for (int j = 0; j < 3; ++j) {
+    double d = 0;
+    for (int i = k + o; i < 3; ++i) d += a.m[i][j] * v[i];
+    for (int i = k + o; i < 3; ++i) a.m[i][j] -= 2 * d * v[i];
+  }
+}
+__device__ inline void eig_reflect_rows(const double* v, M3& q, int k, int o) {
+  for (int i = 0; i < 3; ++i) {
+    double d = 0;
+    for (int j = k + o; j < 3; ++j) d += q.m[i][j] * v[j];
+    for (int j = k + o; j < 3; ++j) q.m[i][j] -= 2 * d * v[j];
+  }
+}
+// mth::multiply (mth/mth_def.h:235-248): c(i,j) = 0, then += a(i,l) b(l,j)
+__device__ inline M3 eig_mul(const M3& a, const M3& b) {
+  M3 c;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      c.m[i][j] = 0;
+      for (int l = 0; l < 3; ++l) c.m[i][j] += a.m[i][l] * b.m[l][j];
+    }
+  return c;
+}
+__device__ inline void eig_identity(M3& q) {
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) q.m[i][j] = (double)(i == j);
+}
+// Hessenberg reduction, then Wilkinson-shifted QR steps with deflation from
+// the bottom (at most max_iters).  Returns 1 when converged, 0 when the
+// iterations ran out, -1 when the shift's denominator vanished (the
+// reference asserts in both failure cases).
+__device__ inline int eigen_qr3(const M3& A, M3& L, M3& Q, int max_iters) {
+  double v[3];
+  eig_identity(Q);
+  M3 h = A;
+  if (eig_reflector(h, v, 0, 1)) {
+    eig_reflect_columns(v, h, 0, 1);
+    eig_reflect_rows(v, h, 0, 1);
+    eig_reflect_rows(v, Q, 0, 1);
+  }
+  int red_m = 3, status = 0;
+  for (int it = 0; it < max_iters; ++it) {
+    bool more = false;
+    while (red_m > 1) {
+      if (fabs(h.m[red_m - 2][red_m - 1]) < 1e-10 && fabs(h.m[red_m - 1][red_m - 2]) < 1e-10) {
+        --red_m;
+      } else {
+        more = true;
+        break;
+      }
+    }
+    if (!more) {
+      status = 1;
+      break;
+    }
+    const double amm1 = h.m[red_m - 2][red_m - 2], am = h.m[red_m - 1][red_m - 1], bmm1 = h.m[red_m - 2][red_m - 1];
+    const double sig = (amm1 - am) / 2;
+    const double denom = (fabs(sig) + sqrt(sig * sig + bmm1 * bmm1));
+    if (!(fabs(denom) > 1e-10)) {
+      status = -1;
+      break;
+    }
+    const double mu = am - ((((sig < 0) ? -1 : 1) * (bmm1 * bmm1)) / denom);
+    for (int i = 0; i < 3; ++i) h.m[i][i] -= mu;
+    M3 qk, rk = h;
+    eig_identity(qk);
+    for (int k = 0; k < 3; ++k)
+      if (eig_reflector(rk, v, k, 0)) {
+        eig_reflect_columns(v, rk, k, 0);
+        eig_reflect_rows(v, qk, k, 0);
+      }
+    h = eig_mul(rk, qk);
+    for (int i = 0; i < 3; ++i) h.m[i][i] -= -mu;
+    Q = eig_mul(Q, qk);
+  }
+  L = h;
+  return status;
+}
+
+// LogAnisoSizeField::init (ma/maSize.cc:472-503): f diag(log(1/h/h)) f^T
+__device__ inline void vertex_logm(const double* h, const double* f9, double* out9) {
+  M3 f, S;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      f.m[i][j] = f9[3 * i + j];
+      S.m[i][j] = 0;
+    }
+  S.m[0][0] = log(1 / h[0] / h[0]);
+  S.m[1][1] = log(1 / h[1] / h[1]);
+  S.m[2][2] = log(1 / h[2] / h[2]);
+  const M3 r = mul(mul(f, S), transpose(f));
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) out9[3 * i + j] = r.m[i][j];
+}
+
+// LogAnisoSizeField::getTransform (ma/maSize.cc:508-523): log-metrics of nn
+// nodes (nn x 9) interpolated by N, apf::eigen (apf/apfMatrix.cc:68-82),
+// orthogonalEigenDecompForSymmetricMatrix (ma/maSize.cc:123-142),
+// Q = R diag(sqrt(exp(v))).  *ok = false when the eigen iteration fails.
+__device__ inline M3 log_transform(const double* Mv, const double* N, int nn, bool* ok) {
+  double M9[9];
+  for (int k = 0; k < 9; ++k) M9[k] = 0;
+  for (int a = 0; a < nn; ++a)
+    for (int k = 0; k < 9; ++k) M9[k] += Mv[9 * a + k] * N[a];
+  M3 A, L, Qe;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) A.m[i][j] = M9[3 * i + j];
+  if (eigen_qr3(A, L, Qe, 100) != 1) *ok = false;
+  // eigenvectors: the columns of Qe, as the rows of RT
+  M3 RT = transpose(Qe);
+  V3 r0 = normalize(row(RT, 0));
+  V3 r1 = sub(row(RT, 1), scale(r0, dot(r0, row(RT, 1))));
+  r1 = normalize(r1);
+  V3 r2 = cross(r0, r1);
+  setrow(RT, 0, r0); setrow(RT, 1, r1); setrow(RT, 2, r2);
+  M3 S;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) S.m[i][j] = 0;
+  S.m[0][0] = sqrt(exp(L.m[0][0]));
+  S.m[1][1] = sqrt(exp(L.m[1][1]));
+  S.m[2][2] = sqrt(exp(L.m[2][2]));
+  return mul(transpose(RT), S);
+}
+
 }  // namespace ref
 }  // namespace sprg

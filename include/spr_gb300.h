@@ -38,6 +38,7 @@ extern "C" {
 #define SPRG_ENOMEM 4   /* device or host allocation failed */
 #define SPRG_ECUDA 5    /* CUDA runtime error */
 #define SPRG_ESTATE 6   /* call order: an input the call needs is not resident */
+#define SPRG_EEIGEN 7   /* mth::eigenQR of a log-metric did not converge (apf/apfMatrix.cc:75 asserts) */
 
 /* precision modes */
 #define SPRG_FP64 0  /* FP64 throughout, the reference's arithmetic */
@@ -140,6 +141,17 @@ int sprg_measure_edges(sprg_ctx* ctx, const double* size, double* lengths);
    n_verts x 9 row-major (principal directions in columns). */
 int sprg_measure_edges_aniso(sprg_ctx* ctx, const double* sizes, const double* frames, double* lengths);
 
+/* ma::makeSizeField(m, sizes, frames, true) + measure: LogAnisoSizeField
+   (ma/maSize.cc:455-580), the log-metrics f diag(log(1/h^2)) f^T of the
+   vertices interpolated and eigen-decomposed (mth::eigenQR) at each Gauss
+   point.  Lengths stay resident for sprg_mark_edges.  SPRG_EEIGEN where the
+   reference's eigen iteration would assert. */
+int sprg_measure_edges_log_aniso(sprg_ctx* ctx, const double* sizes, const double* frames, double* lengths);
+
+/* ma::measureTetQuality / measureTriQuality (useMax = true) under the
+   LogAnisoSizeField of sizes and frames; q resident for the quality sweeps. */
+int sprg_measure_quality_log_aniso(sprg_ctx* ctx, const double* sizes, const double* frames, double* q);
+
 /* ma::markEdgesToSplit / ma::markEdgesToCollapse through ma::markEntities
    (ma/maAdapt.cc:293) on the resident lengths.  flags: n_edges int words of
    the "ma_flags" tag (0 where the tag is absent), updated in place.
@@ -157,10 +169,14 @@ int sprg_measure_quality(sprg_ctx* ctx, const double* size, const double* sizes,
    Size field kinds: SPRG_SIZE_IDENTITY is ma::IdentitySizeField (apf::measure
    of the edge, ma/maSize.cc:49-92); SPRG_SIZE_ISO the isotropic user field
    (`size`: n_verts, or NULL for the resident one); SPRG_SIZE_ANISO the
-   AnisoSizeField of `sizes` (n_verts x 3) and `frames` (n_verts x 9). */
+   AnisoSizeField of `sizes` (n_verts x 3) and `frames` (n_verts x 9)
+   (makeSizeField(m, sizes, frames, false)); SPRG_SIZE_LOG_ANISO the
+   LogAnisoSizeField of the same inputs (makeSizeField(m, sizes, frames,
+   true), ma/maSize.cc:455-580, the default of ma::configure). */
 #define SPRG_SIZE_IDENTITY 0
 #define SPRG_SIZE_ISO 1
 #define SPRG_SIZE_ANISO 2
+#define SPRG_SIZE_LOG_ANISO 3
 
 /* SizeField::measure of would-be edges given as vertex pairs (pairs: n x 2),
    e.g. the edges a collapse would create that ma::collapseSizeCheck measures

@@ -65,6 +65,10 @@ def load():
     L.orc_mark_bad_quality.argtypes = [_I, _P, _D, _P, ctypes.POINTER(ctypes.c_long)]
     L.orc_min_quality.argtypes = [_I, _P]
     L.orc_min_quality.restype = _D
+    L.orc_eigen_qr3.argtypes = [_P, _P, _P, _I]
+    L.orc_log_metric.argtypes = [_P, _P, _P, _P]
+    L.orc_measure_edges_log.argtypes = [_P, _P, _P, _P]
+    L.orc_quality_log.argtypes = [_P, _P, _P, _P]
     _lib = L
     return L
 
@@ -186,21 +190,21 @@ class OracleMesh:
         return q
 
     @staticmethod
-    def _sf(size, sizes, frames, identity):
+    def _sf(size, sizes, frames, identity, log=False):
         """(kind, size, sizes, frames) arrays of a size field argument set."""
         c = lambda a: None if a is None else np.ascontiguousarray(a, np.float64)
         if identity:
             return 0, None, None, None
         if sizes is not None:
-            return 2, None, c(sizes), c(frames)
+            return (3 if log else 2), None, c(sizes), c(frames)
         return 1, c(size), None, None
 
     @staticmethod
     def _p(a):
         return None if a is None else a.ctypes.data
 
-    def measure_pairs(self, pairs, size=None, sizes=None, frames=None, identity=False):
-        kind, s, ss, ff = self._sf(size, sizes, frames, identity)
+    def measure_pairs(self, pairs, size=None, sizes=None, frames=None, identity=False, log=False):
+        kind, s, ss, ff = self._sf(size, sizes, frames, identity, log)
         pr = np.ascontiguousarray(pairs, np.int32).reshape(-1, 2)
         L = np.empty(pr.shape[0], np.float64)
         rc = self.L.orc_measure_pairs(self.h, kind, self._p(s), self._p(ss), self._p(ff), pr.shape[0],
@@ -209,8 +213,28 @@ class OracleMesh:
             raise ValueError("vertex id out of range")
         return L
 
-    def max_edge_length(self, size=None, sizes=None, frames=None, identity=False):
-        kind, s, ss, ff = self._sf(size, sizes, frames, identity)
+    def log_metric(self, sizes, frames):
+        """Per-vertex log-metric f diag(log(1/h^2)) f^T (V x 9)."""
+        out = np.empty((self.V, 9))
+        self.L.orc_log_metric(self.h, np.ascontiguousarray(sizes, np.float64).ctypes.data,
+                              np.ascontiguousarray(frames, np.float64).ctypes.data, out.ctypes.data)
+        return out
+
+    def measure_log(self, sizes, frames):
+        """Edge lengths under makeSizeField(m, sizes, frames, true); (rc, L)."""
+        L = np.empty(self.E)
+        rc = self.L.orc_measure_edges_log(self.h, np.ascontiguousarray(sizes, np.float64).ctypes.data,
+                                          np.ascontiguousarray(frames, np.float64).ctypes.data, L.ctypes.data)
+        return rc, L
+
+    def quality_log(self, sizes, frames):
+        q = np.empty(self.T)
+        rc = self.L.orc_quality_log(self.h, np.ascontiguousarray(sizes, np.float64).ctypes.data,
+                                    np.ascontiguousarray(frames, np.float64).ctypes.data, q.ctypes.data)
+        return rc, q
+
+    def max_edge_length(self, size=None, sizes=None, frames=None, identity=False, log=False):
+        kind, s, ss, ff = self._sf(size, sizes, frames, identity, log)
         return self.L.orc_max_edge_length(self.h, kind, self._p(s), self._p(ss), self._p(ff))
 
     def average_edge_length(self):
@@ -228,6 +252,15 @@ class OracleMesh:
                                           L.ctypes.data, flags.ctypes.data, ctypes.byref(ns), ctypes.byref(nc),
                                           ctypes.byref(info))
         return rc, size, L, flags, ns.value, nc.value, info.as_dict()
+
+
+def eigen_qr3(A, max_iters=100):
+    """mth::eigenQR restated: (converged, L, Q); converged -1 when the
+    Wilkinson shift's denominator vanishes (the reference asserts)."""
+    A9 = np.ascontiguousarray(A, np.float64).reshape(9)
+    L9, Q9 = np.empty(9), np.empty(9)
+    rc = load().orc_eigen_qr3(A9.ctypes.data, L9.ctypes.data, Q9.ctypes.data, int(max_iters))
+    return rc, L9.reshape(3, 3), Q9.reshape(3, 3)
 
 
 def max_iterations(max_metric_length):
@@ -280,4 +313,6 @@ def ref_qr():
     L = ctypes.CDLL(REF_QR_PATH)
     L.ref_qr_decompose.argtypes = [_I, _I, _P, _P, _P]
     L.ref_qr_solve.argtypes = [_I, _I, _P, _P, _P]
+    L.ref_eigen_qr3.argtypes = [_P, _P, _P, _I]
+    L.ref_apf_eigen.argtypes = [_P, _P, _P]
     return L

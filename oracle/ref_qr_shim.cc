@@ -1,10 +1,12 @@
-// ref_qr_shim.cc -- C entry points over the reference's own mth QR
-// (mth/mthQR.cc, compiled from the reference sources by oracle/Makefile
-// into oracle/_ref/).  TEST INFRASTRUCTURE ONLY: used to generate the
-// golden QR fixtures that pin the oracle's restatement of
-// mth::decomposeQR / mth::solveFromQR (mth/mthQR.cc:106-160).
+// ref_qr_shim.cc -- C entry points over the reference's own mth QR and
+// apf::eigen (mth/mthQR.cc, apf/apfMatrix.cc, compiled from the reference
+// sources by oracle/Makefile into oracle/_ref/).  TEST INFRASTRUCTURE ONLY:
+// used to generate the golden fixtures that pin the oracle's restatements of
+// mth::decomposeQR / mth::solveFromQR (mth/mthQR.cc:106-160) and
+// mth::eigenQR / apf::eigen (mth/mthQR.cc:192-297, apf/apfMatrix.cc:68-82).
 #include "mthQR.h"
 #include "mth_def.h"
+#include "apfMatrix.h"
 
 extern "C" {
 
@@ -35,6 +37,32 @@ int ref_qr_solve(int m, int n, const double* A, const double* b, double* x) {
   mth::solveFromQR(q, r, bb, xx);
   for (int j = 0; j < n; ++j) x[j] = xx(j);
   return (int)rank;
+}
+
+// mth::eigenQR on a 3x3 matrix (row-major in and out); returns 1 when it
+// converged within max_iters.
+int ref_eigen_qr3(const double* A9, double* L9, double* Q9, int max_iters) {
+  mth::Matrix<double, 3, 3> a, l, q;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) a(i, j) = A9[3 * i + j];
+  bool ok = mth::eigenQR(a, l, q, (unsigned)max_iters);
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      L9[3 * i + j] = l(i, j);
+      Q9[3 * i + j] = q(i, j);
+    }
+  return ok ? 1 : 0;
+}
+
+// apf::eigen: eigenvectors as rows of vec9, eigenvalues in val3
+void ref_apf_eigen(const double* A9, double* vec9, double* val3) {
+  apf::Matrix3x3 a;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) a[i][j] = A9[3 * i + j];
+  apf::Vector3 vecs[3];
+  apf::eigen(a, vecs, val3);
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) vec9[3 * i + j] = vecs[i][j];
 }
 
 }

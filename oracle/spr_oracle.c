@@ -50,6 +50,7 @@
 #define ORC_EPATCH 2
 #define ORC_EFLAGS 3
 #define ORC_ENOMEM 4
+#define ORC_EEIGEN 5
 
 /* ------------------------------------------------------------------ */
 /* small vector / matrix helpers, in the reference's evaluation order  */
@@ -963,6 +964,142 @@ static M3 get_transform(const double* hv, const double* Rv, const double* N, int
   return m3_mul(R, S);
 }
 
+/* ------------------------------------------------------------------ */
+/* mth::eigenQR for 3x3 (mth/mthQR.cc:19-297) and apf::eigen            */
+/* (apf/apfMatrix.cc:68-82): Hessenberg reduction, Wilkinson-shifted QR */
+/* with deflation from the bottom, at most max_iters steps              */
+/* ------------------------------------------------------------------ */
+typedef struct { double a[3][3]; } Q3;
+
+static void q3_identity(Q3* q) {
+  for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) q->a[i][j] = (double)(i == j);
+}
+/* get_reflector with offset o (mth/mthQR.cc:19-45) */
+static int q3_reflector(const Q3* a, double v[3], int k, int o) {
+  double cnorm = 0;
+  for (int i = k + o; i < 3; ++i) cnorm += a->a[i][k] * a->a[i][k];
+  cnorm = sqrt(cnorm);
+  if (cnorm < 1e-10) return 0;
+  for (int i = 0; i < k + o; ++i) v[i] = 0;
+  for (int i = k + o; i < 3; ++i) v[i] = a->a[i][k];
+  v[k + o] += sgn(a->a[k + o][k]) * cnorm;
+  double rnorm = 0;
+  for (int i = k + o; i < 3; ++i) rnorm += v[i] * v[i];
+  rnorm = sqrt(rnorm);
+  for (int i = k + o; i < 3; ++i) v[i] /= rnorm;
+  return 1;
+}
+/* reflect_columns / reflect_rows (mth/mthQR.cc:47-79) */
+static void q3_reflect_columns(const double v[3], Q3* a, int k, int o) {
+  for (int j = 0; j < 3; ++j) {
+    double dot = 0;
+    for (int i = k + o; i < 3; ++i) dot += a->a[i][j] * v[i];
+    for (int i = k + o; i < 3; ++i) a->a[i][j] -= 2 * dot * v[i];
+  }
+}
+static void q3_reflect_rows(const double v[3], Q3* q, int k, int o) {
+  for (int i = 0; i < 3; ++i) {
+    double dot = 0;
+    for (int j = k + o; j < 3; ++j) dot += q->a[i][j] * v[j];
+    for (int j = k + o; j < 3; ++j) q->a[i][j] -= 2 * dot * v[j];
+  }
+}
+/* mth::multiply (mth/mth_def.h:235-248): c(i,j) = 0, += a(i,l) b(l,j) */
+static void q3_mul(const Q3* a, const Q3* b, Q3* c) {
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      c->a[i][j] = 0;
+      for (int l = 0; l < 3; ++l) c->a[i][j] += a->a[i][l] * b->a[l][j];
+    }
+}
+int orc_eigen_qr3(const double* A9, double* L9, double* Q9, int max_iters) {
+  Q3 a, q, h, rk, qk, tmp;
+  double v[3];
+  for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) a.a[i][j] = A9[3 * i + j];
+  /* reduceToHessenberg (mth/mthQR.cc:192-209) */
+  q3_identity(&q);
+  h = a;
+  if (q3_reflector(&h, v, 0, 1)) {
+    q3_reflect_columns(v, &h, 0, 1);
+    q3_reflect_rows(v, &h, 0, 1);
+    q3_reflect_rows(v, &q, 0, 1);
+  }
+  int red_m = 3, converged = 0;
+  for (int it = 0; it < max_iters; ++it) {
+    /* reduce (mth/mthQR.cc:211-222) */
+    int more = 0;
+    while (red_m > 1) {
+      if (fabs(h.a[red_m - 2][red_m - 1]) < 1e-10 && fabs(h.a[red_m - 1][red_m - 2]) < 1e-10) --red_m;
+      else { more = 1; break; }
+    }
+    if (!more) { converged = 1; break; }
+    /* get_wilkinson_shift (mth/mthQR.cc:224-236) */
+    double amm1 = h.a[red_m - 2][red_m - 2], am = h.a[red_m - 1][red_m - 1], bmm1 = h.a[red_m - 2][red_m - 1];
+    double sig = (amm1 - am) / 2;
+    double denom = (fabs(sig) + sqrt(sig * sig + bmm1 * bmm1));
+    if (!(fabs(denom) > 1e-10)) return -1; /* PCU_ALWAYS_ASSERT */
+    double mu = am - ((sgn(sig) * (bmm1 * bmm1)) / denom);
+    for (int i = 0; i < 3; ++i) h.a[i][i] -= mu;
+    /* decomposeQR (mth/mthQR.cc:106-126) */
+    q3_identity(&qk);
+    rk = h;
+    for (int k = 0; k < 3; ++k)
+      if (q3_reflector(&rk, v, k, 0)) {
+        q3_reflect_columns(v, &rk, k, 0);
+        q3_reflect_rows(v, &qk, k, 0);
+      }
+    q3_mul(&rk, &qk, &h);
+    for (int i = 0; i < 3; ++i) h.a[i][i] -= -mu;
+    q3_mul(&q, &qk, &tmp);
+    q = tmp;
+  }
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) { L9[3 * i + j] = h.a[i][j]; Q9[3 * i + j] = q.a[i][j]; }
+  return converged;
+}
+
+/* LogAnisoSizeField::getTransform (ma/maSize.cc:508-523): logM interpolated
+   over nn nodes (Mv: nn x 9), apf::eigen + orthogonalEigenDecompForSymmetric
+   Matrix (ma/maSize.cc:123-142), Q = R diag(sqrt(exp(v))).  *ok = 0 when the
+   eigen iteration fails (the reference asserts). */
+static M3 log_transform(const double* Mv, const double* N, int nn, int* ok) {
+  double M9[9], L9[9], Q9[9];
+  interp(Mv, nn, 9, N, M9);
+  if (orc_eigen_qr3(M9, L9, Q9, 100) != 1) *ok = 0;
+  double val[3];
+  V3 vec[3];
+  for (int i = 0; i < 3; ++i) val[i] = L9[4 * i];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) vec[j].v[i] = Q9[3 * i + j];
+  V3 r0 = v3_normalize(vec[0]);
+  V3 r1 = v3_sub(vec[1], v3_scale(r0, v3_dot(r0, vec[1])));
+  r1 = v3_normalize(r1);
+  V3 r2 = v3_cross(r0, r1);
+  M3 RT;
+  m3_setrow(&RT, 0, r0); m3_setrow(&RT, 1, r1); m3_setrow(&RT, 2, r2);
+  M3 R = m3_transpose(RT);
+  M3 S;
+  memset(&S, 0, sizeof S);
+  S.m[0][0] = sqrt(exp(val[0])); S.m[1][1] = sqrt(exp(val[1])); S.m[2][2] = sqrt(exp(val[2]));
+  return m3_mul(R, S);
+}
+
+/* LogAnisoSizeField::init (ma/maSize.cc:472-503): logM = f diag(log(1/h/h)) f^T */
+static void vertex_logm(const double* sizes3, const double* frames9, int v, double* out9) {
+  const double* h = sizes3 + 3 * (size_t)v;
+  M3 f, S;
+  for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) f.m[i][j] = frames9[9 * (size_t)v + 3 * i + j];
+  memset(&S, 0, sizeof S);
+  S.m[0][0] = log(1 / h[0] / h[0]); S.m[1][1] = log(1 / h[1] / h[1]); S.m[2][2] = log(1 / h[2] / h[2]);
+  M3 r = m3_mul(m3_mul(f, S), m3_transpose(f));
+  for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) out9[3 * i + j] = r.m[i][j];
+}
+
+int orc_log_metric(const orc_mesh* m, const double* sizes3, const double* frames9, double* logm9) {
+  for (int v = 0; v < m->n[0]; ++v) vertex_logm(sizes3, frames9, v, logm9 + 9 * (size_t)v);
+  return ORC_OK;
+}
+
 static void vertex_metric(const double* sizes3, const double* frames9, const double* size1, int v,
                           double* hv, double* Rv) {
   if (size1) { hv[0] = hv[1] = hv[2] = size1[v]; }
@@ -978,12 +1115,17 @@ static void vertex_metric(const double* sizes3, const double* frames9, const dou
    Either size1 (IsoUserField: makeSizeField(m, size)) or sizes3 + frames9
    (AnisoSizeField::init: makeSizeField(m, sizes, frames, false)). */
 /* MetricSizeField::measure of the vertex pair (a, b) (ma/maSize.cc:158-216) */
-static double pair_metric_length(const orc_mesh* m, int a0, int b0, const double* size1, const double* sizes3,
-                                 const double* frames9) {
+static int g_log_ok = 1; /* cleared when an eigen iteration of a log-metric transform fails */
+
+static double pair_metric_length_mode(const orc_mesh* m, int a0, int b0, const double* size1, const double* sizes3,
+                                      const double* frames9, int logi) {
   const int ev[2] = {a0, b0};
   V3 x[2] = {vert_xyz(m, ev[0]), vert_xyz(m, ev[1])};
-  double hv[6], Rv[18];
-  for (int a = 0; a < 2; ++a) vertex_metric(sizes3, frames9, size1, ev[a], hv + 3 * a, Rv + 9 * a);
+  double hv[6], Rv[18], Mv[18];
+  for (int a = 0; a < 2; ++a) {
+    if (logi) vertex_logm(sizes3, frames9, ev[a], Mv + 9 * a);
+    else vertex_metric(sizes3, frames9, size1, ev[a], hv + 3 * a, Rv + 9 * a);
+  }
   static const double gp[2] = {0.577350269189626, -0.577350269189626};
   M3 J = jacobian(x, 2, 1);
   double measurement = 0;
@@ -991,11 +1133,18 @@ static double pair_metric_length(const orc_mesh* m, int a0, int b0, const double
     V3 xi = {{gp[p], 0, 0}};
     double N[2];
     shape_values(1, xi, N);
-    M3 Q = get_transform(hv, Rv, N, 2);
+    int ok = 1;
+    M3 Q = logi ? log_transform(Mv, N, 2, &ok) : get_transform(hv, Rv, N, 2);
+    if (!ok) g_log_ok = 0;
     double dV2 = jacobian_det(m3_mul(J, Q), 1);
     measurement += 1 * dV2;
   }
   return measurement;
+}
+
+static double pair_metric_length(const orc_mesh* m, int a0, int b0, const double* size1, const double* sizes3,
+                                 const double* frames9) {
+  return pair_metric_length_mode(m, a0, b0, size1, sizes3, frames9, 0);
 }
 
 static double metric_length(const orc_mesh* m, int edge, const double* size1, const double* sizes3, const double* frames9) {
@@ -1043,16 +1192,25 @@ static double q_measure(const V3* x, int nn, int edim, M3 Q) {
 }
 
 /* measureTetQuality / measureTriQuality with useMax = true (ma/maQuality.cc:83-167) */
-static double element_quality(const orc_mesh* m, int e, const double* size1, const double* sizes3, const double* frames9) {
+static double element_quality_mode(const orc_mesh* m, int e, const double* size1, const double* sizes3,
+                                   const double* frames9, int logi) {
   int dim = m->dim, nn = dim + 1;
   const int* ev = m->elem_verts + (size_t)e * nn;
   M3 Q;
   memset(&Q, 0, sizeof Q);
   double maxJ = -1.0;
   for (int i = 0; i < nn; ++i) {
-    double hv[3], Rv[9], N[1] = {1.0};
-    vertex_metric(sizes3, frames9, size1, ev[i], hv, Rv);
-    M3 cQ = get_transform(hv, Rv, N, 1);
+    double hv[3], Rv[9], Mv[9], N[1] = {1.0};
+    M3 cQ;
+    if (logi) {
+      int ok = 1;
+      vertex_logm(sizes3, frames9, ev[i], Mv);
+      cQ = log_transform(Mv, N, 1, &ok);
+      if (!ok) g_log_ok = 0;
+    } else {
+      vertex_metric(sizes3, frames9, size1, ev[i], hv, Rv);
+      cQ = get_transform(hv, Rv, N, 1);
+    }
     double cJ = jacobian_det(cQ, dim);
     if (cJ > maxJ) { maxJ = cJ; Q = cQ; }
   }
@@ -1073,6 +1231,28 @@ static double element_quality(const orc_mesh* m, int e, const double* size1, con
     return 15552 * (Vm * Vm) / (s * s * s);
   }
   return 48 * (Vm * Vm) / (s * s);
+}
+
+static double element_quality(const orc_mesh* m, int e, const double* size1, const double* sizes3, const double* frames9) {
+  return element_quality_mode(m, e, size1, sizes3, frames9, 0);
+}
+
+/* makeSizeField(m, sizes, frames, true) (LogAnisoSizeField, ma/maSize.cc:455-580):
+   metric lengths of every edge and qualities of every element.  Returns
+   ORC_EEIGEN when an eigen iteration fails (the reference asserts). */
+int orc_measure_edges_log(const orc_mesh* m, const double* sizes3, const double* frames9, double* L) {
+  g_log_ok = 1;
+  for (int e = 0; e < m->n[1]; ++e) {
+    const int* ev = m->dn[1] + 2 * (size_t)e;
+    L[e] = pair_metric_length_mode(m, ev[0], ev[1], NULL, sizes3, frames9, 1);
+  }
+  return g_log_ok ? ORC_OK : ORC_EEIGEN;
+}
+
+int orc_quality_log(const orc_mesh* m, const double* sizes3, const double* frames9, double* q) {
+  g_log_ok = 1;
+  for (int e = 0; e < m->n[m->dim]; ++e) q[e] = element_quality_mode(m, e, NULL, sizes3, frames9, 1);
+  return g_log_ok ? ORC_OK : ORC_EEIGEN;
 }
 
 int orc_quality(const orc_mesh* m, const double* size1, const double* sizes3, const double* frames9, double* q) {
@@ -1115,10 +1295,11 @@ int orc_estimate_and_mark(const orc_mesh* m, const double* u, double adapt_ratio
 /* ------------------------------------------------------------------ */
 /* SizeField::measure of a vertex pair; kind 0: IdentitySizeField
    (apf::measure of the edge, ma/maSize.cc:54-60), 1: isotropic user field,
-   2: anisotropic (sizes3, frames9) */
+   2: anisotropic (sizes3, frames9), 3: LogAnisoSizeField of (sizes3, frames9) */
 static double pair_length(const orc_mesh* m, int kind, int a, int b, const double* size1, const double* sizes3,
                           const double* frames9) {
   if (kind == 0) return edge_measure(vert_xyz(m, a), vert_xyz(m, b));
+  if (kind == 3) return pair_metric_length_mode(m, a, b, NULL, sizes3, frames9, 1);
   return kind == 1 ? pair_metric_length(m, a, b, size1, NULL, NULL) : pair_metric_length(m, a, b, NULL, sizes3, frames9);
 }
 

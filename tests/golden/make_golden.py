@@ -8,6 +8,11 @@ reads the reference).
                   (mth/mthQR.cc, compiled from source into oracle/_ref by
                   `make -C oracle ref`) on seeded SPR-shaped patch matrices,
                   including exactly rank-deficient ones.
+  eigen_ref.npz   outputs of the reference's mth::eigenQR (100 iterations)
+                  and apf::eigen (mth/mthQR.cc, apf/apfMatrix.cc compiled
+                  from source into oracle/_ref) on seeded symmetric 3x3
+                  matrices: log-metrics of random sizes and frames, their
+                  edge-midpoint blends, repeated eigenvalues, diagonal ones.
   box8_oracle.npz oracle outputs of the 8^3 sine-field pass (regression
                   fixture of the oracle itself, not a reference output).
 
@@ -59,6 +64,35 @@ def patch_matrices(seed=7):
     return cases
 
 
+def eigen_matrices(seed=9, n=400):
+    """Symmetric 3x3 matrices of the kinds a LogAnisoSizeField decomposes."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    for k in range(n):
+        t = k % 5
+        q, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+        lam = np.log(1.0 / np.exp(rng.uniform(np.log(1e-4), np.log(0.3), 3)) ** 2)
+        if t == 0:
+            A = q @ np.diag(lam) @ q.T
+        elif t == 1:  # blend of two vertex log-metrics (an edge's Gauss point)
+            q2, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+            lam2 = np.log(1.0 / rng.uniform(1e-3, 0.2, 3) ** 2)
+            w = rng.uniform(0, 1)
+            A = w * (q @ np.diag(lam) @ q.T) + (1 - w) * (q2 @ np.diag(lam2) @ q2.T)
+        elif t == 2:  # repeated eigenvalue
+            lam[1] = lam[0]
+            A = q @ np.diag(lam) @ q.T
+        elif t == 3:  # 2D frames: rotation about z
+            th = rng.uniform(0, np.pi)
+            c, s_ = np.cos(th), np.sin(th)
+            f = np.array([[c, -s_, 0], [s_, c, 0], [0, 0, 1.0]])
+            A = f @ np.diag(lam) @ f.T
+        else:
+            A = np.diag(lam)
+        out.append(np.ascontiguousarray(0.5 * (A + A.T)))
+    return out
+
+
 def main(ref):
     import oracle
     os.makedirs(HERE, exist_ok=True)
@@ -87,6 +121,17 @@ def main(ref):
         out[f"rank{i}"] = np.array(rank); out[f"x{i}"] = X
     out["n"] = np.array(len(cases))
     np.savez_compressed(os.path.join(HERE, "qr_ref.npz"), **out)
+
+    mats = eigen_matrices()
+    A = np.array(mats)
+    Ls, Qs, conv, vecs, vals = [], [], [], [], []
+    for M in mats:
+        L9, Q9, v9, w3 = np.empty(9), np.empty(9), np.empty(9), np.empty(3)
+        conv.append(L.ref_eigen_qr3(M.ctypes.data, L9.ctypes.data, Q9.ctypes.data, 100))
+        L.ref_apf_eigen(M.ctypes.data, v9.ctypes.data, w3.ctypes.data)
+        Ls.append(L9.reshape(3, 3)); Qs.append(Q9.reshape(3, 3)); vecs.append(v9.reshape(3, 3)); vals.append(w3)
+    np.savez_compressed(os.path.join(HERE, "eigen_ref.npz"), A=A, L=np.array(Ls), Q=np.array(Qs),
+                        converged=np.array(conv), vecs=np.array(vecs), vals=np.array(vals))
 
     # oracle regression fixture for the 8^3 sine-field pass (config 1)
     from core_gb300 import workload

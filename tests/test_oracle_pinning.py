@@ -79,3 +79,33 @@ def test_config1_recorded_outcome(oracle_lib):
     assert info["n_expanded"] == 8  # 6 too-small + 2 rank-deficient corner patches
     q = m.quality(size)
     assert abs(q.min() - 0.432) < 1e-12 and abs(q.max() - 0.432) < 1e-12
+
+
+def test_eigen_qr_bitwise_against_reference_fixture(oracle_lib):
+    """mth::eigenQR / apf::eigen restated in the oracle equal the reference's
+    compiled outputs bit for bit (tests/golden/eigen_ref.npz), and decompose."""
+    d = np.load(os.path.join(GOLD, "eigen_ref.npz"))
+    for A, L, Q, conv, vecs, vals in zip(d["A"], d["L"], d["Q"], d["converged"], d["vecs"], d["vals"]):
+        rc, Lo, Qo = oracle_lib.eigen_qr3(A)
+        assert rc == conv == 1
+        assert np.array_equal(Lo, L) and np.array_equal(Qo, Q)
+        # apf::eigen: eigenvalues on the diagonal, eigenvectors = columns of Q
+        assert np.array_equal(np.diag(Lo), vals) and np.array_equal(Qo.T, vecs)
+        # off-diagonals below the reference's 1e-10 deflation threshold remain
+        assert np.abs(Qo @ np.diag(vals) @ Qo.T - A).max() <= 1e-9 * max(1.0, np.abs(A).max())
+
+
+def test_eigen_qr_live_reference_build(oracle_lib):
+    L = oracle_lib.ref_qr()
+    if L is None:
+        pytest.skip("oracle/_ref not built (reference tree absent on this host)")
+    rng = np.random.Generator(np.random.PCG64(19))
+    for k in range(300):
+        A = rng.normal(size=(3, 3)) * 10.0 ** rng.uniform(-6, 4)
+        A = np.ascontiguousarray(A + A.T)
+        if k % 7 == 0:
+            A[0, 1] = A[1, 0] = A[0, 2] = A[2, 0] = 0.0
+        L9, Q9 = np.empty(9), np.empty(9)
+        rr = L.ref_eigen_qr3(A.ctypes.data, L9.ctypes.data, Q9.ctypes.data, 100)
+        ro, Lo, Qo = oracle_lib.eigen_qr3(A)
+        assert rr == ro and np.array_equal(L9.reshape(3, 3), Lo) and np.array_equal(Q9.reshape(3, 3), Qo)
