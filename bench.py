@@ -504,7 +504,11 @@ def gpu_batched(args):
 def gpu_aniso2d(args):
     """The 2D anisotropic workload: 4096^2 square (33.5M triangles), nodal
     Hessian by two SPR recoveries, metric, AnisoSizeField measure, marks and
-    quality, FP64."""
+    quality.  Two forms: FP64 throughout (the reference's arithmetic; patch
+    QR in its operation order) and the mixed form (SPRG_FP32: recoveries from
+    cached FP64 patch weights, FP64 metric, FP32 measure with the FP64 guard
+    band, FP32 qualities).  The line is the --precision form (fp32 = mixed);
+    `forms` holds both with the mark comparison."""
     import torch
     import core_gb300 as cg
     from core_gb300 import workload
@@ -514,38 +518,66 @@ def gpu_aniso2d(args):
     m, u, (eps, hmin, hmax) = workload.aniso2d(n)
     V, T, E = m.n_verts, m.n_elems, m.n_edges
     nw = (E + 31) // 32
-    with cg.Context(m) as c:
-        st = torch.cuda.Stream(dev)
-        torch.cuda.set_stream(st)
-        c.set_stream(st.cuda_stream)
-        d_u = torch.from_numpy(u).to(dev)
-        bits = torch.zeros(2 * nw, dtype=torch.int32, device=dev)
-        q = torch.zeros(T, dtype=torch.float64, device=dev)
-        run = lambda: c.aniso_estimate_and_mark_resident(d_u.data_ptr(), eps, hmin, hmax, bits.data_ptr(),
-                                                          bits.data_ptr() + 4 * nw, q.data_ptr())
-        for _ in range(max(1, args.warmup)):
-            run()
-        torch.cuda.synchronize(dev)
-        c.profile(True)
-        c.profile_report(True)
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        steps = min(args.steps, 3)
-        e0.record(st)
-        for _ in range(steps):
-            run()
-        e1.record(st)
-        torch.cuda.synchronize(dev)
-        ms = e0.elapsed_time(e1) / steps
-        prof = c.profile_report(True)
-    out = {"metric": METRIC, "value": V / (ms / 1e3), "unit": UNIT, "n_gpus": 1, "steps": steps,
-           "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+
+    def run_form(precision):
+        with cg.Context(m, precision=precision) as c:
+            st = torch.cuda.Stream(dev)
+            torch.cuda.set_stream(st)
+            c.set_stream(st.cuda_stream)
+            d_u = torch.from_numpy(u).to(dev)
+            bits = torch.zeros(2 * nw, dtype=torch.int32, device=dev)
+            q = torch.zeros(T, dtype=torch.float64, device=dev)
+            run = lambda: c.aniso_estimate_and_mark_resident(d_u.data_ptr(), eps, hmin, hmax, bits.data_ptr(),
+                                                              bits.data_ptr() + 4 * nw, q.data_ptr())
+            for _ in range(max(1, args.warmup)):
+                run()
+            torch.cuda.synchronize(dev)
+            c.profile(True)
+            c.profile_report(True)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            steps = min(args.steps, 5)
+            e0.record(st)
+            for _ in range(steps):
+                run()
+            e1.record(st)
+            torch.cuda.synchronize(dev)
+            ms = e0.elapsed_time(e1) / steps
+            prof = c.profile_report(True)
+            guard = int(c.debug_read("agcount", np.int32, 1)[0]) if precision == "fp32" else 0
+            launches = c.last_launch_count
+            res = (bits.cpu().numpy().view(np.uint32).copy(), q.cpu().numpy())
+        return ms, steps, prof, guard, launches, res
+
+    forms = {}
+    results = {}
+    for prec in ("fp64", "fp32"):
+        ms, steps, prof, guard, launches, res = run_form(prec)
+        results[prec] = res
+        forms[prec] = {"ms_per_step": ms, "value": V / (ms / 1e3), "unit": UNIT, "steps": steps,
+                       "gpu_launches_per_step": launches,
+                       "phases": {k: {"launches": nl, "total_ms": t, "avg_ms": t / max(nl, 1)}
+                                  for k, (nl, t) in prof.items()}}
+        if prec == "fp32":
+            forms[prec]["guard_edges"] = guard
+    b64, q64 = results["fp64"]
+    b32, q32 = results["fp32"]
+    rel = np.abs(q32 - q64) / np.maximum(np.abs(q64), 1e-300)
+    forms["fp32"].update({"marks_identical": bool(np.array_equal(b32, b64)),
+                          "quality_rel_err_max": float(rel.max()), "quality_rel_err_median": float(np.median(rel))})
+    main_form = "fp32" if args.precision == "fp32" else "fp64"
+    f = forms[main_form]
+    out = {"metric": METRIC, "value": f["value"], "unit": UNIT, "n_gpus": 1, "steps": f["steps"],
+           "warmup": args.warmup, "ms_per_step": f["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64/f32" if main_form == "fp32" else "f64", "data": "synthetic",
            "config": {"workload": f"{n}^2 unit square, {T} triangles, {V} vertices, {E} edges, interior jitter "
                                   f"+-0.15h (seed 5); u = tanh((y-0.5)/1e-3) + 0.1 sin(8 pi x); Hessian by two SPR "
                                   f"recoveries, metric eps {eps:.3g}, h in [{hmin:.3g}, {hmax:.3g}]; AnisoSizeField "
-                                  f"measure, marks, quality", "form": "FP64"},
-           "phases": {k: {"launches": nl, "total_ms": t, "avg_ms": t / max(nl, 1)} for k, (nl, t) in prof.items()}}
+                                  f"measure, marks, quality",
+                      "form": "mixed (FP64 recovery and metric, FP32 measure + FP64 guard, FP32 quality)"
+                      if main_form == "fp32" else "FP64"},
+           "gpu_launches": f["gpu_launches_per_step"] * f["steps"],
+           "phases": f["phases"], "forms": forms}
     print(json.dumps(out), flush=True)
 
 

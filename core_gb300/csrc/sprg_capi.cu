@@ -48,6 +48,10 @@ struct sprg_ctx {
   DevBuf titems, tcountb;  // triangle patches above the thread-per-vertex size
   DevBuf Lx, pairs, red, eflags;  // MA sweeps: lengths, vertex pairs, reduction scratch, element flags
   DevBuf logm;                    // LogAnisoSizeField: per-vertex log-metrics (V x 9)
+  // mixed-precision anisotropic pass: triangle patch weights and their
+  // listed vertices (per mesh), FP32 metric records, guarded edges
+  DevBuf tw, twlisted, twitems, twcount, met32, qrec32, agitems, agcount, kidx, kval, klen, rec9;
+  bool tw_ready = false;
   // FP32 path buffers
   DevBuf crec, vrec, rec32, q32, sz2, fcnt, guard, tetd, wts, w64, listed, geo, geo64, elen, fitems;
   DevBuf gstamp, gfit, grec, tstamp, tslot, trec, tcount;  // guard pipeline scratch
@@ -79,7 +83,7 @@ struct sprg_ctx {
   bool vrec_ready = false;  // coordinate records and SPR weights (per mesh)
   double frame[4] = {0, 0, 0, 1};  // coordinate records: x' = (x - c) s + 1 in [1, 2]
   int n_listed = 0, n_refit = 0;
-  PatchCache cache64, cache32;
+  PatchCache cache64, cache32, cache2d;
   static constexpr int kGuardCap = 1 << 20;
   static constexpr float kGuardRel = 2e-6f;
   static constexpr int kGuardTetCap = 1 << 22;  // FP64 element records of one guard pass
@@ -474,7 +478,7 @@ int sprg_destroy(sprg_ctx* c) {
   DevBuf* bufs[] = {&c->xyz,   &c->xyz32,   &c->ev,   &c->edv,   &c->poff,    &c->pel,    &c->aoff,
                     &c->ael,   &c->tmp,     &c->f,    &c->ip,    &c->rec,     &c->err,    &c->esize,
                     &c->size,  &c->L,       &c->flags, &c->q,    &c->sizes3,  &c->frames9, &c->partials,
-                    &c->out3,  &c->status,  &c->count, &c->xitems, &c->xcount, &c->slab, &c->bits, &c->titems, &c->tcountb, &c->Lx, &c->pairs, &c->red, &c->eflags, &c->logm,
+                    &c->out3,  &c->status,  &c->count, &c->xitems, &c->xcount, &c->slab, &c->bits, &c->titems, &c->tcountb, &c->Lx, &c->pairs, &c->red, &c->eflags, &c->logm, &c->tw, &c->twlisted, &c->twitems, &c->twcount, &c->met32, &c->qrec32, &c->kidx, &c->kval, &c->klen, &c->rec9, &c->cache2d.v, &c->cache2d.n, &c->cache2d.el, &c->agitems, &c->agcount,
                     &c->crec,  &c->vrec,    &c->rec32, &c->q32, &c->sz2,  &c->fcnt,   &c->guard, &c->tetd,
                     &c->wts,   &c->w64,     &c->listed, &c->geo, &c->geo64, &c->elen, &c->fitems, &c->gstamp, &c->gfit, &c->grec,
                     &c->tstamp, &c->tslot,  &c->trec, &c->tcount, &c->hess, &c->pcls, &c->bverts, &c->btiles, &c->bnext, &c->bvoff, &c->bseg, &c->bsegoff, &c->bratios, &c->vvoff, &c->vv, &c->vtile, &c->vr16, &c->rec16,
@@ -500,8 +504,8 @@ int sprg_set_precision(sprg_ctx* c, int precision) {
   if (!c) return SPRG_EINVAL;
   if (precision != SPRG_FP64 && precision != SPRG_FP32 && precision != SPRG_LEARNED)
     return fail(c, SPRG_EINVAL, "unknown precision");
-  if (precision != SPRG_FP64 && c->m.dim != 3)
-    return fail(c, SPRG_EINVAL, "the FP32 and learned forms cover tet meshes; use SPRG_FP64 for triangles");
+  if (precision == SPRG_LEARNED && c->m.dim != 3)
+    return fail(c, SPRG_EINVAL, "the learned form covers tet meshes");
   c->precision = precision;
   return SPRG_OK;
 }
@@ -1110,6 +1114,8 @@ static int autotune(sprg_ctx* c, uint4* rec32) {
 static int pass_fast(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_t* d_collapse) {
   DevMesh& m = c->m;
   int rc;
+  if (m.dim != 3)
+    return fail(c, SPRG_EINVAL, "the FP32 isotropic pass covers tet meshes (on triangles SPRG_FP32 is the mixed anisotropic pass)");
   const BatchView bv = batch_view(c);
   const int nb = bv.n ? c->batch_nseg : fast_error_blocks(m.T);
   const size_t nel = (size_t)m.T * m.nn;
@@ -1360,7 +1366,7 @@ int sprg_debug_read(sprg_ctx* c, const char* name, void* host, size_t bytes) {
       {"ip", &c->ip},       {"rec", &c->rec},     {"err", &c->err},       {"esize", &c->esize},
       {"size", &c->size},   {"L", &c->L},         {"vrec", &c->vrec},     {"rec32", &c->rec32},
       {"q32", &c->q32},     {"sz2", &c->sz2},     {"tetd", &c->tetd},     {"out3", &c->out3},
-      {"fcnt", &c->fcnt},   {"guard", &c->guard}, {"xitems", &c->xitems}, {"xcount", &c->xcount},
+      {"fcnt", &c->fcnt},   {"guard", &c->guard}, {"xitems", &c->xitems}, {"xcount", &c->xcount}, {"agcount", &c->agcount}, {"sizes3", &c->sizes3}, {"frames9", &c->frames9}, {"twcount", &c->twcount},
       {"wts", &c->wts},     {"geo", &c->geo},     {"elen", &c->elen},     {"rec16", &c->rec16},
       {"sizel", &c->sizel}, {"ql", &c->ql},       {"vr16", &c->vr16},     {"fbitems", &c->fbitems},
       {"fbcount", &c->fbcount}, {"listed", &c->listed}};
@@ -1549,6 +1555,102 @@ int sprg_hessian_metric(sprg_ctx* c, const double* hessian, double eps, double h
   return sync_and_status(c);
 }
 
+// The mixed-precision pass's nodal Hessian on triangles: per mesh, the
+// patch weights and the recovery-of-gradient operator K (FP64); per pass
+// rec1 = K u and H = K rec1, the listed patches (growth or more than the
+// weights' patch size) by the FP64 slab fits with in-place gradients.
+static int hessian_operator_2d(sprg_ctx* c) {
+  DevMesh& m = c->m;
+  int rc;
+  const int ks = tri_operator_slots();
+  // the list buffers exist before any kernel or list view refers to them
+  ENSURE(c->twitems, sizeof(int) * (size_t)(m.V > 0 ? m.V : 1));
+  ENSURE(c->twcount, sizeof(int));
+  const ExpandList lst{P<int>(c->twitems), P<int>(c->twcount), m.V};
+  if (!c->tw_ready) {
+    ENSURE(c->tw, sizeof(double) * (size_t)m.T * m.nn);
+    ENSURE(c->twlisted, (size_t)(m.V > 0 ? m.V : 1));
+    ENSURE(c->kidx, sizeof(int) * (size_t)m.V * ks);
+    ENSURE(c->kval, sizeof(double) * 3 * (size_t)m.V * ks);
+    ENSURE(c->klen, sizeof(int) * (size_t)(m.V > 0 ? m.V : 1));
+    CK(cudaMemsetAsync(c->twcount.p, 0, sizeof(int), c->stream));
+    PB("tri_weights_f64");
+    launch_tri_weights(m, P<double>(c->tw), P<unsigned char>(c->twlisted), lst, c->stream);
+    PE();
+    PB("tri_operator_f64");
+    launch_tri_operator(m, P<double>(c->tw), P<unsigned char>(c->twlisted), lst, P<int>(c->kidx),
+                        P<double>(c->kval), P<int>(c->klen), c->stream);
+    PE();
+    c->launches += 2;
+    if ((rc = check_launch(c, "triangle operator"))) return rc;
+    c->tw_ready = true;
+  }
+  ENSURE(c->rec, sizeof(double) * 3 * (size_t)m.V);
+  ENSURE(c->rec9, sizeof(double) * 9 * (size_t)m.V);
+  ENSURE(c->slab, sizeof(double) * (size_t)expand_grid() * expand_max_elems() * (4 + 9 + 1));
+  PB("recover_grad_op_f64");
+  launch_apply_operator(m.V, 1, P<unsigned char>(c->twlisted), P<int>(c->kidx), P<double>(c->kval), P<int>(c->klen),
+                        P<double>(c->f), P<double>(c->rec), c->stream);
+  PE();
+  c->launches += 1;
+  if ((rc = listed_fits(c, c->cache2d, nullptr, P<double>(c->f), 3, P<double>(c->rec), lst))) return rc;
+  PB("recover_grad_op_f64");
+  launch_apply_operator(m.V, 3, P<unsigned char>(c->twlisted), P<int>(c->kidx), P<double>(c->kval), P<int>(c->klen),
+                        P<double>(c->rec), P<double>(c->rec9), c->stream);
+  PE();
+  c->launches += 1;
+  return listed_fits(c, c->cache2d, nullptr, P<double>(c->rec), 9, P<double>(c->rec9), lst);
+}
+
+// the mixed-precision anisotropic pass (SPRG_FP32): FP64 nodal Hessian
+// (on triangles through the per-mesh operator) and metric; FP32 edge measure
+// with the FP64 guard band; FP32 qualities
+static int aniso_pass_mixed(sprg_ctx* c, double eps, double h_min, double h_max, uint32_t* d_split_bits,
+                            uint32_t* d_collapse_bits, double* d_quality) {
+  DevMesh& m = c->m;
+  int rc;
+  const double* H;
+  if (m.dim == 2) {
+    if ((rc = hessian_operator_2d(c))) return rc;
+    H = P<double>(c->rec9);
+  } else {  // tets: the FP64 gradients and recoveries
+    if ((rc = step_grad(c, 1)) || (rc = step_recover(c))) return rc;
+    CK(cudaMemcpyAsync(c->f.p, c->rec.p, sizeof(double) * 3 * (size_t)m.V, cudaMemcpyDeviceToDevice, c->stream));
+    if ((rc = step_grad(c, 3)) || (rc = step_recover(c))) return rc;
+    H = P<double>(c->rec);
+  }
+  PB("hessian_metric");
+  launch_hessian_metric(m, H, eps, h_min, h_max, P<double>(c->sizes3), P<double>(c->frames9), c->stream);
+  PE();
+  ENSURE(c->met32, sizeof(float) * 12 * (size_t)(m.V > 0 ? m.V : 1));
+  ENSURE(c->qrec32, (size_t)quality_rec_bytes() * (size_t)(m.V > 0 ? m.V : 1));
+  ENSURE(c->agitems, sizeof(int) * (size_t)(m.E > 0 ? m.E : 1));
+  ENSURE(c->agcount, sizeof(int));
+  CK(cudaMemsetAsync(c->agcount.p, 0, sizeof(int), c->stream));
+  PB("metric_f32");
+  launch_metric_f32(m.V, m.dim, P<double>(c->sizes3), P<double>(c->frames9), P<float>(c->met32), c->qrec32.p,
+                    c->stream);
+  PE();
+  PB("measure_aniso_f32");
+  launch_measure_aniso_f32(m, P<float>(c->met32), d_split_bits, d_collapse_bits, P<int>(c->agitems),
+                           P<int>(c->agcount), m.E, c->stream);
+  PE();
+  PB("guard_measure_f64");
+  launch_measure_guard_f64(m, P<double>(c->sizes3), P<double>(c->frames9), P<int>(c->agitems), P<int>(c->agcount),
+                           m.E, d_split_bits, d_collapse_bits, c->stream);
+  PE();
+  c->launches += 4;
+  if (d_quality) {
+    PB("quality_f32");
+    launch_quality_aniso_f32(m, c->qrec32.p, d_quality, c->stream);
+    PE();
+    c->launches += 1;
+  }
+  c->L_valid = false;  // no FP64 length array in this form
+  c->size_valid = false;
+  return check_launch(c, "mixed aniso pass");
+}
+
 int sprg_aniso_estimate_and_mark_resident(sprg_ctx* c, const double* d_u, double eps, double h_min, double h_max,
                                           uint32_t* d_split_bits, uint32_t* d_collapse_bits, double* d_quality) {
   if (!c || !d_u || !d_split_bits || !d_collapse_bits) return SPRG_EINVAL;
@@ -1563,6 +1665,7 @@ int sprg_aniso_estimate_and_mark_resident(sprg_ctx* c, const double* d_u, double
   ENSURE(c->L, sizeof(double) * (size_t)m.E);
   if ((rc = reset_status(c))) return rc;
   CK(cudaMemcpyAsync(c->f.p, d_u, sizeof(double) * (size_t)m.V, cudaMemcpyDeviceToDevice, c->stream));
+  if (c->precision == SPRG_FP32) return aniso_pass_mixed(c, eps, h_min, h_max, d_split_bits, d_collapse_bits, d_quality);
   // recovered gradient, then the recovered gradient of it (nodal Hessian)
   if ((rc = step_grad(c, 1)) || (rc = step_recover(c))) return rc;
   CK(cudaMemcpyAsync(c->f.p, c->rec.p, sizeof(double) * 3 * (size_t)m.V, cudaMemcpyDeviceToDevice, c->stream));

@@ -78,8 +78,9 @@ void launch_recover_f64(const DevMesh& m, const double* ip, int nc, double* rec,
 // Patches on the expansion list: grow as the reference does, then fit.
 // The list length is read on the device (no host round trip).
 // slab: expand_grid() * expand_max_elems() * (4 + nc + 1) doubles.
-// ip may be NULL: the scalar field u's element gradients are computed in
-// place (FP32 path, which keeps no ip field).
+// ip may be NULL: the element gradients of u are computed in place (nc 3:
+// u scalar; nc 9: u a VECTOR field, V x 3) -- for the forms that keep no ip
+// field.
 // cache_* (optional): record each listed vertex's final element set
 // (expand_max_elems() ints per list slot) for launch_cached_fit_f64.
 void launch_expand_f64(const DevMesh& m, const double* ip, const double* u, int nc, double* rec, ExpandList xl,
@@ -132,6 +133,33 @@ void launch_first_min_below(long long n, const double* x, double start, unsigned
                             unsigned long long* first, cudaStream_t s);
 void launch_mark_quality(int T, const double* q, double good, int* flags, unsigned long long* count, DevStatus* st,
                          cudaStream_t s);
+// Mixed-precision anisotropic pass.  Triangle patch weights (FP64, patch
+// CSR layout) with the listed vertices (weights not covering them) in lst;
+// FP32 metric records (12 floats per
+// vertex: h, frame) and quality records (FP64-selected vertex transforms);
+// FP32 edge measure writing the mark bitmaps and the
+// edges within their error bound of 0.5 / 1.5 (guard); the guard's FP64
+// re-measure fixing those bits; FP32 qualities.
+void launch_tri_weights(const DevMesh& m, double* w, unsigned char* listed, ExpandList lst, cudaStream_t s);
+// qrec: quality_rec_bytes() per vertex
+void launch_metric_f32(int V, int dim, const double* sizes, const double* frames, float* out, void* qrec,
+                       cudaStream_t s);
+int quality_rec_bytes();
+void launch_measure_aniso_f32(const DevMesh& m, const float* met, uint32_t* split, uint32_t* collapse, int* guard,
+                              int* gcount, int gcap, cudaStream_t s);
+void launch_measure_guard_f64(const DevMesh& m, const double* sizes, const double* frames, const int* guard,
+                              const int* gcount, int gcap, uint32_t* split, uint32_t* collapse, cudaStream_t s);
+void launch_quality_aniso_f32(const DevMesh& m, const void* qrec, double* q, cudaStream_t s);
+// Triangle recovery-of-gradient operator (per mesh, FP64): K_va over the
+// patch vertices, tri_operator_slots() slots per vertex (kidx ints, kval 3
+// doubles each, klen counts; patches that are not fans are added to the
+// listed set); applied to a scalar (ncin 1 -> V x 3) or a
+// VECTOR field (ncin 3 -> V x 9) at the covered (not listed) vertices
+int tri_operator_slots();
+void launch_tri_operator(const DevMesh& m, const double* w, unsigned char* listed, ExpandList lst, int* kidx,
+                         double* kval, int* klen, cudaStream_t s);
+void launch_apply_operator(int V, int ncin, const unsigned char* listed, const int* kidx, const double* kval,
+                           const int* klen, const double* f, double* out, cudaStream_t s);
 // FP64 guard band of the FP32 path: re-decide the listed edges' bits.
 // One FP64 gradient (at the integration point) per element the guard touches.
 struct GuardTet {

@@ -70,6 +70,22 @@ __device__ __forceinline__ V3 elem_grad_scalar(const DevMesh& m, int e, const do
   return g;
 }
 
+// gradient of component r of a P1 field stored with stride `stride` (a
+// VECTOR field's row r of the MATRIX ip value), same operation order
+__device__ __forceinline__ V3 elem_grad_component(const DevMesh& m, int e, const double* __restrict__ f, int stride,
+                                                  int r) {
+  const int* ev = m.ev + (size_t)e * m.nn;
+  V3 x[4];
+  for (int a = 0; a < m.nn; ++a) x[a] = load_xyz(m.xyz, ev[a]);
+  M3 J = ref::jacobian(x, m.nn, m.dim);
+  M3 jinv = ref::jacobian_inverse(J, m.dim);
+  V3 lg[4];
+  ref::shape_grads(m.dim, lg);
+  V3 g = ref::scale(ref::mulv(jinv, lg[0]), f[(size_t)ev[0] * stride + r]);
+  for (int a = 1; a < m.nn; ++a) g = ref::add(g, ref::scale(ref::mulv(jinv, lg[a]), f[(size_t)ev[a] * stride + r]));
+  return g;
+}
+
 // ---------------------------------------------------------------------
 // spr::getGradIPField
 // ---------------------------------------------------------------------
@@ -416,9 +432,14 @@ __device__ bool slab_fit(const DevMesh& m, const int* S, int n, const double* __
     if (NT == 4) rw[3] = p.v[2];
     if (ip) {
       for (int c = 0; c < nc; ++c) rw[NT + c] = ip[(size_t)el * nc + c];
-    } else {  // no resident ip field: the gradient of the scalar field u
+    } else if (nc == 3) {  // no resident ip field: the gradient of the scalar field u
       V3 g = elem_grad_scalar(m, el, u);
       for (int c = 0; c < 3; ++c) rw[NT + c] = g.v[c];
+    } else {  // ... or of the VECTOR field u (V x 3): MATRIX rows, row r = grad u_r
+      for (int r = 0; r < 3; ++r) {
+        V3 g = elem_grad_component(m, el, u, 3, r);
+        for (int c = 0; c < 3; ++c) rw[NT + 3 * r + c] = g.v[c];
+      }
     }
   }
   __syncwarp();
@@ -1470,6 +1491,408 @@ __global__ void __launch_bounds__(kBlock) k_mark_quality(int T, const double* __
 }
 
 
+// ---------------------------------------------------------------------
+// Mixed-precision anisotropic pass (SPRG_FP32 on the Hessian-metric
+// workload).  The recoveries use per-mesh FP64 patch weights, the metric
+// stays FP64, the edge measure and the qualities run in FP32: every edge
+// whose FP32 length is within its error bound of 0.5 or 1.5 is re-measured
+// by the FP64 kernel, so the marks equal the FP64 pass's.
+// ---------------------------------------------------------------------
+// SPR weights of a triangle patch: the fitted value at the vertex is a
+// fixed combination of the patch samples, eps*(v) = sum_j w_j b_j with
+// w = Q_c R^-T t (Q_c the first NT columns of Q, t = [1, x_v, y_v]).  The QR
+// is the reference's (as in k_recover_tri); listed: patches the weights do
+// not cover (fewer than NT or more than MAXM elements, rank deficient),
+// which take the FP64 fit paths every pass.
+template <int MAXM>
+__global__ void __launch_bounds__(128) k_tri_weights(DevMesh m, double* __restrict__ w,
+                                                     unsigned char* __restrict__ listed, ExpandList lst) {
+  constexpr int NT = 3;
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= m.V) return;
+  const int beg = m.p_off[v];
+  const int cnt = m.p_off[v + 1] - beg;
+  auto give_up = [&]() {
+    listed[v] = 1;
+    const int slot = atomicAdd(lst.count, 1);
+    if (slot < lst.cap) lst.items[slot] = v;
+  };
+  if (cnt < NT || cnt > MAXM) {
+    give_up();
+    return;
+  }
+  double R[MAXM][NT];
+#pragma unroll
+  for (int i = 0; i < MAXM; ++i) {
+    R[i][0] = R[i][1] = R[i][2] = 0;
+    if (i < cnt) {
+      const V3 p = elem_ip_point(m, m.p_el[beg + i]);
+      R[i][0] = 1.0;
+      R[i][1] = p.v[0];
+      R[i][2] = p.v[1];
+    }
+  }
+  double H[NT][MAXM];
+#pragma unroll
+  for (int k = 0; k < NT; ++k) {
+    double cn = 0;
+#pragma unroll
+    for (int i = k; i < MAXM; ++i)
+      if (i < cnt) cn += R[i][k] * R[i][k];
+    cn = sqrt(cn);
+    if (cn < 1e-10) {
+      give_up();
+      return;
+    }
+#pragma unroll
+    for (int i = 0; i < MAXM; ++i) H[k][i] = (i >= k && i < cnt) ? R[i][k] : 0.0;
+    H[k][k] += ((R[k][k] < 0) ? -1 : 1) * cn;
+    double rn = 0;
+#pragma unroll
+    for (int i = k; i < MAXM; ++i)
+      if (i < cnt) rn += H[k][i] * H[k][i];
+    rn = sqrt(rn);
+#pragma unroll
+    for (int i = k; i < MAXM; ++i)
+      if (i < cnt) H[k][i] /= rn;
+#pragma unroll
+    for (int j = k; j < NT; ++j) {
+      double dot = 0;
+#pragma unroll
+      for (int i = k; i < MAXM; ++i)
+        if (i < cnt) dot += R[i][j] * H[k][i];
+#pragma unroll
+      for (int i = k; i < MAXM; ++i)
+        if (i < cnt) R[i][j] -= 2 * dot * H[k][i];
+    }
+  }
+  // z = R^-T t
+  const V3 xv = load_xyz(m.xyz, v);
+  double z[NT];
+  z[0] = 1.0 / R[0][0];
+  z[1] = (xv.v[0] - R[0][1] * z[0]) / R[1][1];
+  z[2] = (xv.v[1] - R[0][2] * z[0] - R[1][2] * z[1]) / R[2][2];
+#pragma unroll
+  for (int r = 0; r < MAXM; ++r) {
+    if (r >= cnt) break;
+    double q[MAXM];
+#pragma unroll
+    for (int j = 0; j < MAXM; ++j) q[j] = (j == r) ? 1.0 : 0.0;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) {
+      double dot = 0;
+#pragma unroll
+      for (int j = k; j < MAXM; ++j)
+        if (j < cnt) dot += q[j] * H[k][j];
+#pragma unroll
+      for (int j = k; j < MAXM; ++j)
+        if (j < cnt) q[j] -= 2 * dot * H[k][j];
+    }
+    w[beg + r] = q[0] * z[0] + q[1] * z[1] + q[2] * z[2];
+  }
+  listed[v] = 0;
+}
+
+// Per vertex: the FP32 metric record h (3), frame (9, row-major) for the
+// edge measure, and the quality record: the vertex transform Q =
+// orth(R) diag(1/h) and its Jacobian determinant, both evaluated in FP64 by
+// the FP64 quality kernel's arithmetic (so the quality kernel picks the same
+// vertex as the FP64 one), Q then rounded to FP32.
+struct QualityRec {
+  float q[9];
+  float pad;
+  double cj;
+};
+__global__ void __launch_bounds__(kBlock) k_metric_f32(int V, int dim, const double* __restrict__ sizes,
+                                                       const double* __restrict__ frames, float* __restrict__ out,
+                                                       QualityRec* __restrict__ qrec) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= V) return;
+  float* o = out + 12 * (size_t)v;
+  double hv[3], Rv[9];
+  for (int k = 0; k < 3; ++k) {
+    hv[k] = sizes[3 * (size_t)v + k];
+    o[k] = (float)hv[k];
+  }
+  for (int k = 0; k < 9; ++k) {
+    Rv[k] = frames[9 * (size_t)v + k];
+    o[3 + k] = (float)Rv[k];
+  }
+  const double N[1] = {1.0};
+  const M3 Q = ref::get_transform(hv, Rv, N, 1);
+  QualityRec r;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) r.q[3 * i + j] = (float)Q.m[i][j];
+  r.pad = 0.f;
+  r.cj = ref::jacobian_det(Q, dim);
+  qrec[v] = r;
+}
+
+// AnisoSizeField measure in FP32 with a relative error bound.  Per Gauss
+// point: R(xi) interpolated and orthogonalised, dV = |(J.r_j / h_j)_j|.  Each
+// term J.r_j / h_j carries an absolute error of a few units of |J| / h_j
+// times 2^-24, amplified by the orthogonalisation's conditioning (the first
+// column divided by its length |c0|, the second, after the projection, by
+// |r1|); relative to dV that is at most
+// kAnisoUlps 2^-24 (1 + 1/|c0|)(1 + 1/|r1|) sum_j (|J| / h_j) / dV,
+// where the last factor is >= 1 and kAnisoUlps covers the few roundings of
+// each step (inputs, interpolation, normalisations, dot products, sqrt).
+constexpr float kAnisoUlps = 64.f;
+__device__ __forceinline__ float aniso_dv_f32(float Jx, float Jy, float Jz, const float* ma, const float* mb,
+                                              float n0, float n1, float* bound) {
+  float h[3], R[9];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) h[k] = n0 * ma[k] + n1 * mb[k];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) R[k] = n0 * ma[3 + k] + n1 * mb[3 + k];
+  // columns of R
+  float c0x = R[0], c0y = R[3], c0z = R[6];
+  float c1x = R[1], c1y = R[4], c1z = R[7];
+  const float l0 = sqrtf(c0x * c0x + c0y * c0y + c0z * c0z);
+  const float r0x = c0x / l0, r0y = c0y / l0, r0z = c0z / l0;
+  const float d01 = r0x * c1x + r0y * c1y + r0z * c1z;
+  c1x -= r0x * d01; c1y -= r0y * d01; c1z -= r0z * d01;
+  const float l1 = sqrtf(c1x * c1x + c1y * c1y + c1z * c1z);
+  const float r1x = c1x / l1, r1y = c1y / l1, r1z = c1z / l1;
+  const float r2x = r0y * r1z - r0z * r1y, r2y = r0z * r1x - r0x * r1z, r2z = r0x * r1y - r0y * r1x;
+  const float t0 = (Jx * r0x + Jy * r0y + Jz * r0z) / h[0];
+  const float t1 = (Jx * r1x + Jy * r1y + Jz * r1z) / h[1];
+  const float t2 = (Jx * r2x + Jy * r2y + Jz * r2z) / h[2];
+  const float dv = sqrtf(t0 * t0 + t1 * t1 + t2 * t2);
+  const float jn = sqrtf(Jx * Jx + Jy * Jy + Jz * Jz);
+  const float sum = jn / fabsf(h[0]) + jn / fabsf(h[1]) + jn / fabsf(h[2]);
+  const float cond = (1.f + 1.f / l0) * (1.f + 1.f / l1);
+  *bound = fmaxf(*bound, kAnisoUlps * 5.9604645e-8f * cond * sum / dv);
+  return dv;
+}
+
+__global__ void __launch_bounds__(kBlock) k_measure_aniso_f32(DevMesh m, const float* __restrict__ met,
+                                                              uint32_t* __restrict__ split,
+                                                              uint32_t* __restrict__ collapse,
+                                                              int* __restrict__ guard, int* __restrict__ gcount,
+                                                              int gcap) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  bool sp = false, co = false, g = false;
+  if (e < m.E) {
+    const int a = m.edv[2 * (size_t)e], b = m.edv[2 * (size_t)e + 1];
+    // J = x_b / 2 - x_a / 2 in FP64 (the reference's edge Jacobian), then rounded
+    const float Jx = (float)(0.5 * m.xyz[3 * (size_t)b] - 0.5 * m.xyz[3 * (size_t)a]);
+    const float Jy = (float)(0.5 * m.xyz[3 * (size_t)b + 1] - 0.5 * m.xyz[3 * (size_t)a + 1]);
+    const float Jz = (float)(0.5 * m.xyz[3 * (size_t)b + 2] - 0.5 * m.xyz[3 * (size_t)a + 2]);
+    float ma[12], mb[12];
+#pragma unroll
+    for (int k = 0; k < 12; ++k) {
+      ma[k] = met[12 * (size_t)a + k];
+      mb[k] = met[12 * (size_t)b + k];
+    }
+    float bound = 0.f;
+    const float g0 = 0.577350269189626f;
+    const float L = aniso_dv_f32(Jx, Jy, Jz, ma, mb, (1.f - g0) * 0.5f, (1.f + g0) * 0.5f, &bound) +
+                    aniso_dv_f32(Jx, Jy, Jz, ma, mb, (1.f + g0) * 0.5f, (1.f - g0) * 0.5f, &bound);
+    const float lo = L * (1.f - bound), hi = L * (1.f + bound);
+    if (!(bound < 0.25f) || !isfinite(L)) {
+      g = true;
+    } else {
+      if (lo > 1.5f) sp = true;
+      else if (hi > 1.5f) g = true;
+      if (hi < 0.5f) co = true;
+      else if (lo < 0.5f) g = true;
+    }
+  }
+  const unsigned bs = __ballot_sync(0xffffffffu, sp), bc = __ballot_sync(0xffffffffu, co);
+  if ((threadIdx.x & 31) == 0 && e < m.E) {
+    split[e >> 5] = bs;
+    collapse[e >> 5] = bc;
+  }
+  const unsigned bg = __ballot_sync(0xffffffffu, g);
+  if (bg) {
+    const int lane = threadIdx.x & 31;
+    int base = 0;
+    if (lane == __ffs(bg) - 1) base = atomicAdd(gcount, __popc(bg));
+    base = __shfl_sync(0xffffffffu, base, __ffs(bg) - 1);
+    const int slot = base + __popc(bg & ((1u << lane) - 1));
+    if (g && slot < gcap) guard[slot] = e;
+  }
+}
+
+// the guarded edges re-measured by the FP64 kernel's arithmetic
+__global__ void __launch_bounds__(kBlock) k_measure_guard_f64(DevMesh m, const double* __restrict__ sizes,
+                                                              const double* __restrict__ frames,
+                                                              const int* __restrict__ guard,
+                                                              const int* __restrict__ gcount, int gcap,
+                                                              uint32_t* __restrict__ split,
+                                                              uint32_t* __restrict__ collapse) {
+  int n = *gcount;
+  n = n < gcap ? n : gcap;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int e = guard[i];
+    const int vv[2] = {m.edv[2 * (size_t)e], m.edv[2 * (size_t)e + 1]};
+    double hv[6], Rv[18];
+    for (int a = 0; a < 2; ++a) {
+      for (int k = 0; k < 3; ++k) hv[3 * a + k] = sizes[3 * (size_t)vv[a] + k];
+      for (int k = 0; k < 9; ++k) Rv[9 * a + k] = frames[9 * (size_t)vv[a] + k];
+    }
+    const double L = metric_length(load_xyz(m.xyz, vv[0]), load_xyz(m.xyz, vv[1]), hv, Rv);
+    const uint32_t bit = 1u << (e & 31);
+    if (L > 1.5) atomicOr(split + (e >> 5), bit);
+    else atomicAnd(split + (e >> 5), ~bit);
+    if (L < .5) atomicOr(collapse + (e >> 5), bit);
+    else atomicAnd(collapse + (e >> 5), ~bit);
+  }
+}
+
+// mean-ratio quality under the anisotropic metric in FP32 (the vertex
+// transform with the largest determinant, ma/maQuality.cc:83-167)
+__global__ void __launch_bounds__(kBlock) k_quality_aniso_f32(DevMesh m, const QualityRec* __restrict__ qrec,
+                                                              double* __restrict__ q) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= m.T) return;
+  const int* ev = m.ev + (size_t)e * m.nn;
+  // the vertex with the largest FP64 determinant (getMetricWithMaxJacobean,
+  // ma/maQuality.cc:83-108, in the reference's order and comparison)
+  int best = 0;
+  double maxJ = -1.0;
+  for (int i = 0; i < m.nn; ++i) {
+    const double cJ = qrec[ev[i]].cj;
+    if (cJ > maxJ) {
+      maxJ = cJ;
+      best = i;
+    }
+  }
+  float Q[3][3];
+  {
+    const QualityRec r = qrec[ev[best]];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) Q[i][j] = r.q[3 * i + j];
+  }
+  // edge vectors in metric space, (x_r - x_p) Q, from FP64 differences
+  double x[4][3];
+  for (int a = 0; a < m.nn; ++a)
+    for (int k = 0; k < 3; ++k) x[a][k] = m.xyz[3 * (size_t)ev[a] + k];
+  auto mvec = [&](int r, int p, float* t) {
+    float d[3];
+    for (int k = 0; k < 3; ++k) d[k] = (float)(x[r][k] - x[p][k]);
+    for (int c = 0; c < 3; ++c) t[c] = d[0] * Q[0][c] + d[1] * Q[1][c] + d[2] * Q[2][c];
+  };
+  float s = 0.f;
+  for (int i = 0; i < m.ne_el; ++i) {
+    float t[3];
+    mvec(m.dim == 3 ? c_tet_edges[i][1] : c_tri_edges[i][1], m.dim == 3 ? c_tet_edges[i][0] : c_tri_edges[i][0], t);
+    s += t[0] * t[0] + t[1] * t[1] + t[2] * t[2];
+  }
+  float a0[3], a1[3];
+  mvec(1, 0, a0);
+  mvec(2, 0, a1);
+  const float cx = a0[1] * a1[2] - a0[2] * a1[1], cy = a0[2] * a1[0] - a0[0] * a1[2],
+              cz = a0[0] * a1[1] - a0[1] * a1[0];
+  float res;
+  if (m.dim == 3) {
+    float a2[3];
+    mvec(3, 0, a2);
+    const float Vm = (cx * a2[0] + cy * a2[1] + cz * a2[2]) / 6.f;  // det(J Q) / 6
+    res = 15552.f * (Vm * Vm) / (s * s * s);
+    if (Vm < 0) res = -res;
+  } else {
+    const float A = 0.5f * sqrtf(cx * cx + cy * cy + cz * cz);
+    res = 48.f * (A * A) / (s * s);
+  }
+  q[e] = res;
+}
+
+// Recovery composed with the element gradient: on a P1 field f the
+// recovered gradient at a covered vertex is
+//   eps*(v) = sum_t w_vt grad_t f = sum_a K_va f_a,
+// K_va = sum over the patch elements t holding a of w_vt (J_t^-1 grad N_a),
+// a linear operator over the patch's vertices that depends on the geometry
+// only.  It is built once per mesh (FP64) and the two recoveries of the
+// Hessian workload become two sparse products with it.  kOpSlots slots per
+// vertex (a fan of up to kTriThreadRows triangles touches at most
+// kTriThreadRows + 2 vertices); a patch touching more is listed for the
+// FP64 slab fit instead.
+constexpr int kOpSlots = kTriThreadRows + 2;
+__global__ void __launch_bounds__(kBlock) k_tri_operator(DevMesh m, const double* __restrict__ w,
+                                                         unsigned char* __restrict__ listed, ExpandList lst,
+                                                         int* __restrict__ kidx, double* __restrict__ kval,
+                                                         int* __restrict__ klen) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= m.V) return;
+  if (listed[v]) {
+    klen[v] = 0;
+    return;
+  }
+  int ids[kOpSlots];
+  double acc[kOpSlots][3];
+  int n = 0;
+  for (int k = m.p_off[v]; k < m.p_off[v + 1]; ++k) {
+    const int t = m.p_el[k];
+    const double wk = w[k];
+    const int* ev = m.ev + (size_t)t * 3;
+    V3 x[3];
+    for (int a = 0; a < 3; ++a) x[a] = load_xyz(m.xyz, ev[a]);
+    const M3 J = ref::jacobian(x, 3, 2);
+    const M3 jinv = ref::jacobian_inverse(J, 2);
+    V3 lg[4];
+    ref::shape_grads(2, lg);
+    for (int a = 0; a < 3; ++a) {
+      const V3 g = ref::mulv(jinv, lg[a]);
+      int s = 0;
+      while (s < n && ids[s] != ev[a]) ++s;
+      if (s == n) {
+        if (n == kOpSlots) {  // not a fan: the slab fit takes it
+          listed[v] = 1;
+          klen[v] = 0;
+          const int slot = atomicAdd(lst.count, 1);
+          if (slot < lst.cap) lst.items[slot] = v;
+          return;
+        }
+        ids[n] = ev[a];
+        acc[n][0] = acc[n][1] = acc[n][2] = 0;
+        ++n;
+      }
+      for (int c = 0; c < 3; ++c) acc[s][c] += wk * g.v[c];
+    }
+  }
+  klen[v] = n;
+  for (int s = 0; s < n; ++s) {
+    kidx[(size_t)v * kOpSlots + s] = ids[s];
+    for (int c = 0; c < 3; ++c) kval[((size_t)v * kOpSlots + s) * 3 + c] = acc[s][c];
+  }
+}
+
+// out (V x 3 NCIN) = K f (f: V x NCIN) at the covered vertices; row r of a
+// MATRIX value is the recovered gradient of component r
+template <int NCIN>
+__global__ void __launch_bounds__(kBlock) k_apply_operator(int V, const unsigned char* __restrict__ listed,
+                                                           const int* __restrict__ kidx,
+                                                           const double* __restrict__ kval,
+                                                           const int* __restrict__ klen, const double* __restrict__ f,
+                                                           double* __restrict__ out) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= V || listed[v]) return;
+  const int n = klen[v];
+  double acc[NCIN][3];
+#pragma unroll
+  for (int r = 0; r < NCIN; ++r) acc[r][0] = acc[r][1] = acc[r][2] = 0;
+  for (int s = 0; s < n; ++s) {
+    const size_t slot = (size_t)v * kOpSlots + s;
+    const int a = kidx[slot];
+    const double k0 = kval[3 * slot], k1 = kval[3 * slot + 1], k2 = kval[3 * slot + 2];
+#pragma unroll
+    for (int r = 0; r < NCIN; ++r) {
+      const double fa = f[(size_t)a * NCIN + r];
+      acc[r][0] = fma(k0, fa, acc[r][0]);
+      acc[r][1] = fma(k1, fa, acc[r][1]);
+      acc[r][2] = fma(k2, fa, acc[r][2]);
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < NCIN; ++r)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) out[(size_t)v * 3 * NCIN + 3 * r + c] = acc[r][c];
+}
+
 }  // namespace
 
 // ----------------------------------------------------------------------
@@ -1665,4 +2088,43 @@ void launch_mark_quality(int T, const double* q, double good, int* flags, unsign
                          cudaStream_t s) {
   if (T) k_mark_quality<<<nblk(T), kBlock, 0, s>>>(T, q, good, flags, count, st);
 }
+void launch_tri_weights(const DevMesh& m, double* w, unsigned char* listed, ExpandList lst, cudaStream_t s) {
+  if (m.V) k_tri_weights<kTriThreadRows><<<(m.V + 127) / 128, 128, 0, s>>>(m, w, listed, lst);
+}
+
+void launch_metric_f32(int V, int dim, const double* sizes, const double* frames, float* out, void* qrec,
+                       cudaStream_t s) {
+  if (V) k_metric_f32<<<nblk(V), kBlock, 0, s>>>(V, dim, sizes, frames, out, static_cast<QualityRec*>(qrec));
+}
+
+void launch_measure_aniso_f32(const DevMesh& m, const float* met, uint32_t* split, uint32_t* collapse, int* guard,
+                              int* gcount, int gcap, cudaStream_t s) {
+  if (m.E) k_measure_aniso_f32<<<nblk(m.E), kBlock, 0, s>>>(m, met, split, collapse, guard, gcount, gcap);
+}
+
+void launch_measure_guard_f64(const DevMesh& m, const double* sizes, const double* frames, const int* guard,
+                              const int* gcount, int gcap, uint32_t* split, uint32_t* collapse, cudaStream_t s) {
+  k_measure_guard_f64<<<152 * 4, kBlock, 0, s>>>(m, sizes, frames, guard, gcount, gcap, split, collapse);
+}
+
+int quality_rec_bytes() { return (int)sizeof(QualityRec); }
+
+void launch_quality_aniso_f32(const DevMesh& m, const void* qrec, double* q, cudaStream_t s) {
+  if (m.T) k_quality_aniso_f32<<<nblk(m.T), kBlock, 0, s>>>(m, static_cast<const QualityRec*>(qrec), q);
+}
+
+int tri_operator_slots() { return kOpSlots; }
+
+void launch_tri_operator(const DevMesh& m, const double* w, unsigned char* listed, ExpandList lst, int* kidx,
+                         double* kval, int* klen, cudaStream_t s) {
+  if (m.V) k_tri_operator<<<nblk(m.V), kBlock, 0, s>>>(m, w, listed, lst, kidx, kval, klen);
+}
+
+void launch_apply_operator(int V, int ncin, const unsigned char* listed, const int* kidx, const double* kval,
+                           const int* klen, const double* f, double* out, cudaStream_t s) {
+  if (!V) return;
+  if (ncin == 1) k_apply_operator<1><<<nblk(V), kBlock, 0, s>>>(V, listed, kidx, kval, klen, f, out);
+  else k_apply_operator<3><<<nblk(V), kBlock, 0, s>>>(V, listed, kidx, kval, klen, f, out);
+}
+
 }  // namespace sprg

@@ -42,7 +42,9 @@ extern "C" {
 
 /* precision modes */
 #define SPRG_FP64 0  /* FP64 throughout, the reference's arithmetic */
-#define SPRG_FP32 1  /* FP32 fits and sweeps with compensated residuals, FP64 guard band (tets) */
+#define SPRG_FP32 1  /* FP32 fits and sweeps with compensated residuals, FP64 guard band (tets); in the
+                        anisotropic pass: FP64 recoveries (cached triangle patch weights) and metric,
+                        FP32 measure with an FP64 guard band, FP32 qualities */
 #define SPRG_LEARNED 2 /* MLP-predicted recovery with SPR fallback, FP32 sweeps (tets, size to 1e-2) */
 
 /* markEntities flag bits (ma/maAdapt.h:17-37) */

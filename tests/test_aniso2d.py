@@ -112,3 +112,75 @@ def test_aniso_pass_matches_oracle(gpu_lib, oracle_lib):
     assert np.array_equal(split, L_ref > 1.5) and np.array_equal(coll, L_ref < 0.5)
     assert split.any() and coll.any()
     assert np.abs(q - q_ref).max() <= 1e-12
+
+
+def run_aniso(m, u, eps, hmin, hmax, precision):
+    """Resident anisotropic pass; returns (split, collapse, quality, sizes, frames, guarded edges)."""
+    import torch
+    import core_gb300 as cg
+    E, T, V = m.n_edges, m.n_elems, m.n_verts
+    nw = (E + 31) // 32
+    with cg.Context(m) as c:
+        c.set_precision(precision)
+        stream = torch.cuda.Stream()
+        torch.cuda.set_stream(stream)
+        c.set_stream(stream.cuda_stream)
+        d_u = torch.from_numpy(u).cuda()
+        bits = torch.zeros(2 * nw, dtype=torch.int32, device="cuda")
+        q = torch.zeros(T, dtype=torch.float64, device="cuda")
+        for _ in range(2):  # the second pass runs on the per-mesh caches
+            c.aniso_estimate_and_mark_resident(d_u.data_ptr(), eps, hmin, hmax, bits.data_ptr(),
+                                               bits.data_ptr() + 4 * nw, q.data_ptr())
+        torch.cuda.synchronize()
+        sizes = c.debug_read("sizes3", np.float64, 3 * V).reshape(V, 3)
+        frames = c.debug_read("frames9", np.float64, 9 * V).reshape(V, 9)
+        guard = int(c.debug_read("agcount", np.int32, 1)[0]) if precision == "fp32" else 0
+        b = bits.cpu().numpy().view(np.uint32)
+        q = q.cpu().numpy()
+    idx = np.arange(E)
+    split = ((b[:nw][idx >> 5] >> (idx & 31)) & 1).astype(bool)
+    coll = ((b[nw:][idx >> 5] >> (idx & 31)) & 1).astype(bool)
+    return split, coll, q, sizes, frames, guard
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dim", [2, 3])
+def test_mixed_aniso_pass_matches_fp64(gpu_lib, dim):
+    """SPRG_FP32 on the anisotropic pass: recoveries from cached FP64 patch
+    weights (triangles), FP64 metric, FP32 measure with the FP64 guard band,
+    FP32 qualities.  Marks identical to the FP64 pass, the metric tensors
+    within 1e-9 relative (the weights sum the patch in another order than
+    the QR), qualities within 1e-4 relative."""
+    from core_gb300 import workload
+    if dim == 2:
+        m, u, (eps, hmin, hmax) = case(96)
+    else:
+        m = workload.box(12, jitter=0.2, seed=5)
+        u = np.tanh((m.coords[:, 1] - 0.5) / 0.05) + 0.1 * np.sin(4 * np.pi * m.coords[:, 0])
+        eps, hmin, hmax = 0.02, 1.0 / 48, 0.5
+    s64, c64, q64, S64, F64, _ = run_aniso(m, u, eps, hmin, hmax, "fp64")
+    s32, c32, q32, S32, F32, guard = run_aniso(m, u, eps, hmin, hmax, "fp32")
+    assert np.array_equal(s32, s64) and np.array_equal(c32, c64)
+    assert s64.any() and c64.any()
+    # the metric tensors R diag(1/h^2) R^T (frames alone rotate freely where
+    # two sizes coincide)
+    def tensors(S, F):
+        R = F.reshape(-1, 3, 3)
+        return np.einsum("vij,vj,vkj->vik", R, 1.0 / S ** 2, R)
+    M32, M64 = tensors(S32, F32), tensors(S64, F64)
+    scale = np.abs(M64).reshape(len(M64), -1).max(axis=1)
+    assert (np.abs(M32 - M64).reshape(len(M64), -1).max(axis=1) / scale).max() <= 1e-9
+    assert np.abs(q32 - q64).max() <= 1e-4 * np.abs(q64).max()
+    assert np.median(np.abs(q32 - q64) / np.abs(q64)) <= 1e-6
+    assert guard < 0.01 * m.n_edges
+
+
+@pytest.mark.gpu
+def test_isotropic_fp32_pass_rejects_triangles(gpu_lib):
+    import core_gb300 as cg
+    from core_gb300 import _lib as K, workload
+    m = workload.box(8, nz=0, jitter=0.1, seed=1)
+    with cg.Context(m, precision="fp32") as c:
+        with pytest.raises(K.SprgError) as ei:
+            c.estimate_and_mark(workload.bump_field(m.coords, seed=1), 0.1)
+        assert ei.value.code == K.SPRG_EINVAL

@@ -96,12 +96,14 @@ def test_fp32_matches_fp64_marks_and_is_deterministic(gpu_lib):
     assert not np.any(np.isnan(s32))
 
 
-def test_fp32_rejects_triangles(gpu_lib):
+def test_learned_rejects_triangles(gpu_lib):
+    """The learned form covers tets (SPRG_FP32 on triangles is the mixed
+    anisotropic pass, tests/test_aniso2d.py)."""
     import core_gb300 as cg
     from core_gb300 import workload
     m = workload.box(8, nz=0)
     with pytest.raises(cg.SprgError):
-        cg.Context(m, precision="fp32")
+        cg.Context(m, precision="learned")
 
 
 def test_fp32_marks_bit_exact_at_128cube(gpu_lib):
