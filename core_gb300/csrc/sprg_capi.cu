@@ -79,6 +79,9 @@ struct sprg_ctx {
   // back into the pass's stream
   cudaStream_t side = nullptr;
   cudaEvent_t fork = nullptr, join = nullptr;
+  // copy stream of the host entry point: the flags upload runs beside the pass
+  cudaStream_t copy = nullptr;
+  cudaEvent_t copy_fork = nullptr, copy_join = nullptr;
   int pass_id = 0;
   bool vrec_ready = false;  // coordinate records and SPR weights (per mesh)
   double frame[4] = {0, 0, 0, 1};  // coordinate records: x' = (x - c) s + 1 in [1, 2]
@@ -486,6 +489,12 @@ int sprg_destroy(sprg_ctx* c) {
                     &c->cache64.v, &c->cache64.n, &c->cache64.el, &c->cache32.v, &c->cache32.n, &c->cache32.el};
   for (DevBuf* b : bufs) release(*b);
   for (auto& e : c->ev_pool) cudaEventDestroy(e);
+  if (c->copy) {
+    cudaStreamSynchronize(c->copy);
+    cudaStreamDestroy(c->copy);
+    cudaEventDestroy(c->copy_fork);
+    cudaEventDestroy(c->copy_join);
+  }
   if (c->side) {
     cudaStreamSynchronize(c->side);
     cudaStreamDestroy(c->side);
@@ -1324,14 +1333,27 @@ int sprg_estimate_and_mark(sprg_ctx* c, const double* u, double adapt_ratio, dou
   ENSURE(c->f, sizeof(double) * (size_t)m.V);
   ENSURE(c->flags, sizeof(int) * (size_t)m.E);
   CK(cudaMemcpyAsync(c->f.p, u, sizeof(double) * (size_t)m.V, cudaMemcpyHostToDevice, c->stream));
-  if (flags)
-    CK(cudaMemcpyAsync(c->flags.p, flags, sizeof(int) * (size_t)m.E, cudaMemcpyHostToDevice, c->stream));
-  else
+  // the flag words are needed only by the write-back at the end: their
+  // upload runs on the copy stream beside the pass (ordered after this
+  // stream's earlier work, which may still read the buffer)
+  if (flags) {
+    if (!c->copy) {
+      CK(cudaStreamCreateWithFlags(&c->copy, cudaStreamNonBlocking));
+      CK(cudaEventCreateWithFlags(&c->copy_fork, cudaEventDisableTiming));
+      CK(cudaEventCreateWithFlags(&c->copy_join, cudaEventDisableTiming));
+    }
+    CK(cudaEventRecord(c->copy_fork, c->stream));
+    CK(cudaStreamWaitEvent(c->copy, c->copy_fork, 0));
+    CK(cudaMemcpyAsync(c->flags.p, flags, sizeof(int) * (size_t)m.E, cudaMemcpyHostToDevice, c->copy));
+    CK(cudaEventRecord(c->copy_join, c->copy));
+  } else {
     CK(cudaMemsetAsync(c->flags.p, 0, sizeof(int) * (size_t)m.E, c->stream));
+  }
   size_t nw = ((size_t)m.E + 31) / 32;
   ENSURE(c->bits, sizeof(uint32_t) * 2 * nw);
   uint32_t* sb = P<uint32_t>(c->bits);
   if ((rc = pass_resident(c, adapt_ratio, sb, sb + nw))) return rc;
+  if (flags) CK(cudaStreamWaitEvent(c->stream, c->copy_join, 0));
   unsigned long long ncol = 0, nspl = 0;
   if ((rc = apply_bits(c, SPRG_MARK_COLLAPSE, sb + nw, P<int>(c->flags)))) return rc;
   CK(cudaMemcpyAsync(&ncol, c->count.p, sizeof ncol, cudaMemcpyDeviceToHost, c->stream));
