@@ -56,7 +56,7 @@ EXPORTS = [
     "sprg_tuning_report", "sprg_graph_capture", "sprg_graph_replay", "sprg_set_tiling",
     "sprg_measure_vertex_pairs", "sprg_get_maximum_edge_length", "sprg_get_average_edge_length",
     "sprg_max_iterations_for_length", "sprg_mark_bad_quality", "sprg_get_min_quality",
-    "sprg_measure_edges_log_aniso", "sprg_measure_quality_log_aniso",
+    "sprg_measure_edges_log_aniso", "sprg_measure_quality_log_aniso", "sprg_update_mesh",
 ]
 NOALLOC_MAX_ELEMS = 1 << 20
 
@@ -75,6 +75,26 @@ class MeshView(ctypes.Structure):
         ("n_edges", ctypes.c_int64),
         ("coords", ctypes.c_void_p),
         ("elem_verts", ctypes.c_void_p),
+        ("edge_verts", ctypes.c_void_p),
+        ("vert_elem_offsets", ctypes.c_void_p),
+        ("vert_elems", ctypes.c_void_p),
+    ]
+
+
+class MeshDelta(ctypes.Structure):
+    """sprg_mesh_delta: new counts and the rows whose values are new."""
+    _fields_ = [
+        ("n_verts", ctypes.c_int64),
+        ("n_elems", ctypes.c_int64),
+        ("n_edges", ctypes.c_int64),
+        ("n_vert_rows", ctypes.c_int64),
+        ("vert_ids", ctypes.c_void_p),
+        ("coords", ctypes.c_void_p),
+        ("n_elem_rows", ctypes.c_int64),
+        ("elem_ids", ctypes.c_void_p),
+        ("elem_verts", ctypes.c_void_p),
+        ("n_edge_rows", ctypes.c_int64),
+        ("edge_ids", ctypes.c_void_p),
         ("edge_verts", ctypes.c_void_p),
         ("vert_elem_offsets", ctypes.c_void_p),
         ("vert_elems", ctypes.c_void_p),
@@ -170,6 +190,7 @@ def load():
     lib.sprg_mark_bad_quality.argtypes = [P, D, P, ctypes.POINTER(ctypes.c_long)]
     lib.sprg_get_min_quality.argtypes = [P, ctypes.POINTER(D)]
     lib.sprg_measure_edges_log_aniso.argtypes = [P, P, P, P]
+    lib.sprg_update_mesh.argtypes = [P, ctypes.POINTER(MeshDelta)]
     lib.sprg_measure_quality_log_aniso.argtypes = [P, P, P, P]
     _lib = lib
     return lib

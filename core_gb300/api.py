@@ -203,6 +203,36 @@ class Context:
             None if ff is None else ff.ctypes.data, q.ctypes.data))
         return q
 
+    # -- incremental update after host topology changes -----------------
+    def update_mesh(self, new_mesh):
+        """Send the rows of `new_mesh` that differ from the context's mesh
+        (moved vertices, new or rewired elements and edges, the counts) and
+        rebuild the device structures; the context then holds `new_mesh`.
+        Returns the delta's row counts (vertices, elements, edges)."""
+        if new_mesh.dim != self.mesh.dim:
+            raise ValueError("the dimension cannot change")
+        d = mesh_delta(self.mesh, new_mesh)
+        keep = []  # arrays referenced by the ctypes struct stay alive for the call
+
+        def ptr(a):
+            if a is None:
+                return None
+            keep.append(a)
+            return a.ctypes.data
+        off = getattr(new_mesh, "v2e_off", None)
+        el = getattr(new_mesh, "v2e", None)
+        off = None if off is None else np.ascontiguousarray(off, np.int32)
+        el = None if el is None else np.ascontiguousarray(el, np.int32)
+        delta = _lib.MeshDelta(new_mesh.n_verts, new_mesh.n_elems, new_mesh.n_edges,
+                               len(d["vert_ids"]), ptr(d["vert_ids"]), ptr(d["coords"]),
+                               len(d["elem_ids"]), ptr(d["elem_ids"]), ptr(d["elem_verts"]),
+                               len(d["edge_ids"]), ptr(d["edge_ids"]), ptr(d["edge_verts"]),
+                               ptr(off), ptr(el))
+        self._check(self._lib.sprg_update_mesh(self.h, ctypes.byref(delta)))
+        self.mesh = new_mesh
+        self._view = new_mesh.view()
+        return len(d["vert_ids"]), len(d["elem_ids"]), len(d["edge_ids"])
+
     # -- MA sweeps around the marks -------------------------------------
     def _size_kind(self, size, sizes, frames, identity, log=False):
         if identity:
@@ -374,6 +404,24 @@ class SizeField:
 
     def shouldCollapse(self):
         return self.measure() < 0.5
+
+
+def mesh_delta(old, new):
+    """Rows of `new`'s flattened arrays that differ from `old`'s or lie beyond
+    its counts: {vert_ids, coords, elem_ids, elem_verts, edge_ids,
+    edge_verts} (int32 ids, contiguous values)."""
+    def rows(a_old, a_new, dtype):
+        a_old = np.asarray(a_old)
+        a_new = np.ascontiguousarray(a_new, dtype)
+        n_old, n_new = a_old.shape[0], a_new.shape[0]
+        k = min(n_old, n_new)
+        changed = np.nonzero(np.any(a_old[:k].reshape(k, -1) != a_new[:k].reshape(k, -1), axis=1))[0]
+        ids = np.concatenate([changed, np.arange(k, n_new)]).astype(np.int32)
+        return ids, np.ascontiguousarray(a_new[ids])
+    vi, vx = rows(old.coords, new.coords, np.float64)
+    ei, ex = rows(old.elem_verts, new.elem_verts, np.int32)
+    di, dx = rows(old.edge_verts, new.edge_verts, np.int32)
+    return {"vert_ids": vi, "coords": vx, "elem_ids": ei, "elem_verts": ex, "edge_ids": di, "edge_verts": dx}
 
 
 def max_iterations_for_length(max_metric_length):

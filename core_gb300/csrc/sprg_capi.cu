@@ -367,6 +367,37 @@ int upload_ip(sprg_ctx* c, const double* ip, int ncomp) {
 // ======================================================================
 extern "C" {
 
+// the FP32 records' frame from the bounding box: shift to the lower corner
+// and scale by a power of two so every coordinate lands in [1, 2]
+static void set_frame(sprg_ctx* c, const double* lo, const double* hi) {
+  double ext = 0;
+  for (int k = 0; k < 3; ++k) ext = hi[k] - lo[k] > ext ? hi[k] - lo[k] : ext;
+  double s = 1;
+  while (s * ext > 1) s *= 0.5;
+  while (ext > 0 && s * ext <= 0.5) s *= 2;
+  c->frame[0] = lo[0];
+  c->frame[1] = lo[1];
+  c->frame[2] = lo[2];
+  c->frame[3] = s;
+}
+
+// index arrays must stay inside the entity counts: a bad id would reach
+// the kernels as an out-of-range gather
+static bool ids_in_range(const int32_t* a, size_t n, int64_t limit) {
+  for (size_t i = 0; i < n; ++i)
+    if (a[i] < 0 || a[i] >= limit) return false;
+  return true;
+}
+
+// a vertex -> element CSR: offsets from 0 to T nn, non-decreasing, entries
+// element ids
+static bool csr_valid(const int32_t* off, const int32_t* el, int64_t V, int64_t T, int nn) {
+  if (off[0] != 0 || off[V] != T * nn) return false;
+  for (int64_t v = 0; v < V; ++v)
+    if (off[v + 1] < off[v]) return false;
+  return ids_in_range(el, (size_t)(T * nn), T);
+}
+
 int sprg_create(const sprg_mesh_view* mv, int device, sprg_ctx** out) {
   if (!out) return SPRG_EINVAL;
   *out = nullptr;
@@ -376,6 +407,12 @@ int sprg_create(const sprg_mesh_view* mv, int device, sprg_ctx** out) {
   if (mv->n_verts > INT32_MAX || mv->n_edges > INT32_MAX || mv->n_elems * (mv->dim + 1) > INT32_MAX)
     return SPRG_EINVAL;
   if ((mv->vert_elem_offsets == nullptr) != (mv->vert_elems == nullptr)) return SPRG_EINVAL;
+  if (!ids_in_range(mv->elem_verts, (size_t)(mv->n_elems * (mv->dim + 1)), mv->n_verts) ||
+      !ids_in_range(mv->edge_verts, (size_t)(2 * mv->n_edges), mv->n_verts))
+    return SPRG_EINVAL;
+  if (mv->vert_elem_offsets &&
+      !csr_valid(mv->vert_elem_offsets, mv->vert_elems, mv->n_verts, mv->n_elems, mv->dim + 1))
+    return SPRG_EINVAL;
   sprg_ctx* c = new sprg_ctx();
   c->device = device;
   int rc = set_device(c);
@@ -424,15 +461,7 @@ int sprg_create(const sprg_mesh_view* mv, int device, sprg_ctx** out) {
         lo[k] = x < lo[k] ? x : lo[k];
         hi[k] = x > hi[k] ? x : hi[k];
       }
-    double ext = 0;
-    for (int k = 0; k < 3; ++k) ext = hi[k] - lo[k] > ext ? hi[k] - lo[k] : ext;
-    double s = 1;
-    while (s * ext > 1) s *= 0.5;
-    while (ext > 0 && s * ext <= 0.5) s *= 2;
-    c->frame[0] = lo[0];
-    c->frame[1] = lo[1];
-    c->frame[2] = lo[2];
-    c->frame[3] = s;
+    set_frame(c, lo, hi);
   }
   m.xyz = P<double>(c->xyz);
   m.xyz32 = P<float>(c->xyz32);
@@ -471,6 +500,173 @@ int sprg_create(const sprg_mesh_view* mv, int device, sprg_ctx** out) {
 #undef CKC
 #undef ENSUREC
   *out = c;
+  return SPRG_OK;
+}
+
+// every per-mesh result, cache and derived structure, after the mesh changed
+static void invalidate_mesh_state(sprg_ctx* c) {
+  c->ip_valid = c->size_valid = c->L_valid = c->q_valid = false;
+  c->vrec_ready = false;
+  c->bins_ready = false;
+  c->tuned = false;
+  c->tw_ready = false;
+  c->vv_ready = false;
+  c->cache64.valid = c->cache32.valid = c->cache2d.valid = false;
+  c->batch_n = 0;
+  c->batch_nseg = 0;
+  // stamps are zeroed when (re)allocated at the next guard pass
+  release(c->gstamp);
+  release(c->tstamp);
+  if (c->graph_exec) {
+    cudaGraphExecDestroy(c->graph_exec);
+    c->graph_exec = nullptr;
+  }
+}
+
+int sprg_update_mesh(sprg_ctx* c, const sprg_mesh_delta* d) {
+  if (!c || !d) return SPRG_EINVAL;
+  DevMesh& m = c->m;
+  const int nn = m.nn;
+  const int64_t V1 = d->n_verts, T1 = d->n_elems, E1 = d->n_edges;
+  // ---- validation (nothing changes before it passes)
+  if (V1 <= 0 || T1 <= 0 || E1 <= 0 || V1 > INT32_MAX || E1 > INT32_MAX || T1 * nn > INT32_MAX)
+    return fail(c, SPRG_EINVAL, "counts must be positive and fit 32-bit ids");
+  if (d->n_vert_rows < 0 || d->n_elem_rows < 0 || d->n_edge_rows < 0 ||
+      (d->n_vert_rows && (!d->vert_ids || !d->coords)) || (d->n_elem_rows && (!d->elem_ids || !d->elem_verts)) ||
+      (d->n_edge_rows && (!d->edge_ids || !d->edge_verts)))
+    return fail(c, SPRG_EINVAL, "row lists need their ids and values");
+  if ((d->vert_elem_offsets == nullptr) != (d->vert_elems == nullptr))
+    return fail(c, SPRG_EINVAL, "averaging CSR: offsets and elements go together");
+  auto rows_ok = [](int64_t n, const int32_t* ids, int64_t count, int64_t old) {
+    std::vector<char> seen(count > old ? (size_t)(count - old) : 0, 0);
+    for (int64_t r = 0; r < n; ++r) {
+      if (ids[r] < 0 || ids[r] >= count) return false;
+      if (ids[r] >= old) seen[(size_t)(ids[r] - old)] = 1;
+    }
+    for (char x : seen)
+      if (!x) return false;
+    return true;
+  };
+  if (!rows_ok(d->n_vert_rows, d->vert_ids, V1, m.V) || !rows_ok(d->n_elem_rows, d->elem_ids, T1, m.T) ||
+      !rows_ok(d->n_edge_rows, d->edge_ids, E1, m.E))
+    return fail(c, SPRG_EINVAL, "row ids out of range, or new rows not all listed");
+  if (!ids_in_range(d->elem_verts, (size_t)(d->n_elem_rows * nn), V1) ||
+      !ids_in_range(d->edge_verts, (size_t)(2 * d->n_edge_rows), V1))
+    return fail(c, SPRG_EINVAL, "element or edge vertex id out of range");
+  if (d->vert_elem_offsets && !csr_valid(d->vert_elem_offsets, d->vert_elems, V1, T1, nn))
+    return fail(c, SPRG_EINVAL, "averaging CSR does not match the new counts");
+  int rc = set_device(c);
+  if (rc) return rc;
+  c->launches = 0;
+  CK(cudaStreamSynchronize(c->stream));
+  // ---- the new arrays: kept rows copied, listed rows scattered
+  DevBuf nxyz, nev, nedv, ids, vals, bad;
+  auto cleanup = [&]() {
+    release(nxyz); release(nev); release(nedv); release(ids); release(vals); release(bad);
+  };
+#define CKU(call)                                                  \
+  do {                                                             \
+    cudaError_t e_ = (call);                                       \
+    if (e_ != cudaSuccess) { cleanup(); return cuda_fail(c, e_, #call); } \
+  } while (0)
+#define ENSUREU(buf, bytes)                                        \
+  do {                                                             \
+    int rc_ = ensure(c, (buf), (bytes));                           \
+    if (rc_) { cleanup(); return rc_; }                            \
+  } while (0)
+  ENSUREU(nxyz, sizeof(double) * 3 * (size_t)V1);
+  ENSUREU(nev, sizeof(int) * (size_t)(T1 * nn));
+  ENSUREU(nedv, sizeof(int) * 2 * (size_t)E1);
+  const int64_t kv = V1 < m.V ? V1 : m.V, kt = T1 < m.T ? T1 : m.T, ke = E1 < m.E ? E1 : m.E;
+  CKU(cudaMemcpyAsync(nxyz.p, c->xyz.p, sizeof(double) * 3 * (size_t)kv, cudaMemcpyDeviceToDevice, c->stream));
+  CKU(cudaMemcpyAsync(nev.p, c->ev.p, sizeof(int) * (size_t)(kt * nn), cudaMemcpyDeviceToDevice, c->stream));
+  CKU(cudaMemcpyAsync(nedv.p, c->edv.p, sizeof(int) * 2 * (size_t)ke, cudaMemcpyDeviceToDevice, c->stream));
+  const int64_t maxrows = std::max(d->n_vert_rows, std::max(d->n_elem_rows, d->n_edge_rows));
+  ENSUREU(ids, sizeof(int) * (size_t)(maxrows > 0 ? maxrows : 1));
+  ENSUREU(vals, sizeof(double) * 3 * (size_t)(maxrows > 0 ? maxrows : 1) + sizeof(int) * (size_t)(maxrows * nn));
+  ENSUREU(bad, sizeof(unsigned long long));
+  auto scatter_i32 = [&](int64_t n, const int32_t* hid, const int32_t* hval, int width, int* dst) -> int {
+    if (!n) return SPRG_OK;
+    CKU(cudaMemcpyAsync(ids.p, hid, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, c->stream));
+    CKU(cudaMemcpyAsync(vals.p, hval, sizeof(int) * (size_t)(n * width), cudaMemcpyHostToDevice, c->stream));
+    launch_scatter_rows_i32(n, width, P<int>(ids), P<int>(vals), dst, c->stream);
+    CKU(cudaStreamSynchronize(c->stream));  // the staging buffers are reused
+    return SPRG_OK;
+  };
+  if (d->n_vert_rows) {
+    CKU(cudaMemcpyAsync(ids.p, d->vert_ids, sizeof(int) * (size_t)d->n_vert_rows, cudaMemcpyHostToDevice, c->stream));
+    CKU(cudaMemcpyAsync(vals.p, d->coords, sizeof(double) * 3 * (size_t)d->n_vert_rows, cudaMemcpyHostToDevice,
+                        c->stream));
+    launch_scatter_rows_f64(d->n_vert_rows, 3, P<int>(ids), P<double>(vals), P<double>(nxyz), c->stream);
+    CKU(cudaStreamSynchronize(c->stream));
+  }
+  if ((rc = scatter_i32(d->n_elem_rows, d->elem_ids, d->elem_verts, nn, P<int>(nev)))) return rc;
+  if ((rc = scatter_i32(d->n_edge_rows, d->edge_ids, d->edge_verts, 2, P<int>(nedv)))) return rc;
+  // kept rows may name vertices beyond a smaller vertex count
+  CKU(cudaMemsetAsync(bad.p, 0, sizeof(unsigned long long), c->stream));
+  launch_count_out_of_range(T1 * nn, P<int>(nev), (int)V1, P<unsigned long long>(bad), c->stream);
+  launch_count_out_of_range(2 * E1, P<int>(nedv), (int)V1, P<unsigned long long>(bad), c->stream);
+  unsigned long long nbad = 0;
+  CKU(cudaMemcpyAsync(&nbad, bad.p, sizeof nbad, cudaMemcpyDeviceToHost, c->stream));
+  CKU(cudaStreamSynchronize(c->stream));
+  if (nbad) {
+    cleanup();
+    return fail(c, SPRG_EINVAL, "kept elements or edges name vertices beyond the new vertex count");
+  }
+  // ---- swap in, rebuild what derives from the arrays
+  release(c->xyz); release(c->ev); release(c->edv);
+  c->xyz = nxyz; c->ev = nev; c->edv = nedv;
+  nxyz = DevBuf{}; nev = DevBuf{}; nedv = DevBuf{};
+  cleanup();
+#undef CKU
+#undef ENSUREU
+  m.V = (int)V1;
+  m.T = (int)T1;
+  m.E = (int)E1;
+  m.xyz = P<double>(c->xyz);
+  m.ev = P<int>(c->ev);
+  m.edv = P<int>(c->edv);
+  const size_t nel = (size_t)m.T * nn;
+  ENSURE(c->xyz32, sizeof(float) * 4 * (size_t)m.V);
+  m.xyz32 = P<float>(c->xyz32);
+  launch_xyz_to_f32(m, P<float>(c->xyz32), c->stream);
+  ENSURE(c->red, sizeof(double) * (size_t)(sum_partials_count() + 4));
+  launch_bbox(m.V, m.xyz, P<unsigned long long>(c->red), c->stream);
+  unsigned long long keys[6];
+  CK(cudaMemcpyAsync(keys, c->red.p, sizeof keys, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  double lo[3], hi[3];
+  for (int k = 0; k < 3; ++k) {
+    lo[k] = key_to_double(keys[k]);
+    hi[k] = key_to_double(keys[3 + k]);
+  }
+  set_frame(c, lo, hi);
+  ENSURE(c->poff, sizeof(int) * ((size_t)m.V + 1));
+  ENSURE(c->pel, sizeof(int) * nel);
+  ENSURE(c->tmp, sizeof(int) * (size_t)m.V);
+  if (d->vert_elem_offsets) {
+    ENSURE(c->aoff, sizeof(int) * ((size_t)m.V + 1));
+    ENSURE(c->ael, sizeof(int) * nel);
+    CK(cudaMemcpyAsync(c->aoff.p, d->vert_elem_offsets, sizeof(int) * ((size_t)m.V + 1), cudaMemcpyHostToDevice,
+                       c->stream));
+    CK(cudaMemcpyAsync(c->ael.p, d->vert_elems, sizeof(int) * nel, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->poff.p, c->aoff.p, sizeof(int) * ((size_t)m.V + 1), cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->pel.p, c->ael.p, sizeof(int) * nel, cudaMemcpyDeviceToDevice, c->stream));
+    launch_sort_segments(m.V, P<int>(c->poff), P<int>(c->pel), c->stream);
+    m.a_off = P<int>(c->aoff);
+    m.a_el = P<int>(c->ael);
+  } else {
+    launch_build_v2e(m, P<int>(c->poff), P<int>(c->pel), P<int>(c->tmp), c->stream);
+    launch_sort_segments(m.V, P<int>(c->poff), P<int>(c->pel), c->stream);
+    m.a_off = P<int>(c->poff);
+    m.a_el = P<int>(c->pel);
+  }
+  m.p_off = P<int>(c->poff);
+  m.p_el = P<int>(c->pel);
+  c->launches += 5;
+  if ((rc = check_launch(c, "mesh update"))) return rc;
+  CK(cudaStreamSynchronize(c->stream));
+  invalidate_mesh_state(c);
   return SPRG_OK;
 }
 

@@ -160,6 +160,14 @@ void launch_tri_operator(const DevMesh& m, const double* w, unsigned char* liste
                          double* kval, int* klen, cudaStream_t s);
 void launch_apply_operator(int V, int ncin, const unsigned char* listed, const int* kidx, const double* kval,
                            const int* klen, const double* f, double* out, cudaStream_t s);
+// incremental mesh update: dst[ids[r] * width + j] = vals[r * width + j];
+// the coordinates' bounding box as order keys (3 minima, 3 maxima)
+void launch_scatter_rows_f64(long long n, int width, const int* ids, const double* vals, double* dst, cudaStream_t s);
+void launch_scatter_rows_i32(long long n, int width, const int* ids, const int* vals, int* dst, cudaStream_t s);
+void launch_bbox(int V, const double* xyz, unsigned long long* keys, cudaStream_t s);
+// *bad += the number of entries of a outside [0, limit)
+void launch_count_out_of_range(long long n, const int* a, int limit, unsigned long long* bad, cudaStream_t s);
+double key_to_double(unsigned long long k);
 // FP64 guard band of the FP32 path: re-decide the listed edges' bits.
 // One FP64 gradient (at the integration point) per element the guard touches.
 struct GuardTet {

@@ -9,6 +9,7 @@
 // m x m Q), and the two global integrals are summed by a fixed tree instead
 // of sequentially.  Both move results by a few ulps only.
 #include <cub/cub.cuh>
+#include <cstring>
 
 #include "sprg_internal.h"
 #include "sprg_refmath.cuh"
@@ -1893,6 +1894,43 @@ __global__ void __launch_bounds__(kBlock) k_apply_operator(int V, const unsigned
     for (int c = 0; c < 3; ++c) out[(size_t)v * 3 * NCIN + 3 * r + c] = acc[r][c];
 }
 
+// ---------------------------------------------------------------------
+// incremental mesh update: row scatter and the bounding box
+// ---------------------------------------------------------------------
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_scatter_rows(long long n, int width, const int* __restrict__ ids,
+                                                         const T* __restrict__ vals, T* __restrict__ dst) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n * width) return;
+  const long long r = i / width;
+  dst[(size_t)ids[r] * width + (i - r * width)] = vals[i];
+}
+
+// per axis min and max of the coordinates as order-preserving 64-bit keys
+// (keys[0..2] minima, keys[3..5] maxima)
+__global__ void __launch_bounds__(kBlock) k_bbox(int V, const double* __restrict__ xyz,
+                                                 unsigned long long* __restrict__ keys) {
+  unsigned long long lo[3] = {~0ull, ~0ull, ~0ull}, hi[3] = {0, 0, 0};
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x)
+    for (int k = 0; k < 3; ++k) {
+      const unsigned long long key = order_key(xyz[3 * (size_t)v + k]);
+      lo[k] = key < lo[k] ? key : lo[k];
+      hi[k] = key > hi[k] ? key : hi[k];
+    }
+  for (int k = 0; k < 3; ++k) {
+    atomicMin(keys + k, lo[k]);
+    atomicMax(keys + 3 + k, hi[k]);
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k_count_out_of_range(long long n, const int* __restrict__ a, int limit,
+                                                               unsigned long long* __restrict__ bad) {
+  unsigned long long c = 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    c += (a[i] < 0 || a[i] >= limit);
+  if (c) atomicAdd(bad, c);
+}
+
 }  // namespace
 
 // ----------------------------------------------------------------------
@@ -2125,6 +2163,33 @@ void launch_apply_operator(int V, int ncin, const unsigned char* listed, const i
   if (!V) return;
   if (ncin == 1) k_apply_operator<1><<<nblk(V), kBlock, 0, s>>>(V, listed, kidx, kval, klen, f, out);
   else k_apply_operator<3><<<nblk(V), kBlock, 0, s>>>(V, listed, kidx, kval, klen, f, out);
+}
+
+void launch_scatter_rows_f64(long long n, int width, const int* ids, const double* vals, double* dst, cudaStream_t s) {
+  if (n > 0) k_scatter_rows<double><<<(unsigned)((n * width + kBlock - 1) / kBlock), kBlock, 0, s>>>(n, width, ids,
+                                                                                                   vals, dst);
+}
+
+void launch_scatter_rows_i32(long long n, int width, const int* ids, const int* vals, int* dst, cudaStream_t s) {
+  if (n > 0) k_scatter_rows<int><<<(unsigned)((n * width + kBlock - 1) / kBlock), kBlock, 0, s>>>(n, width, ids,
+                                                                                                vals, dst);
+}
+
+void launch_bbox(int V, const double* xyz, unsigned long long* keys, cudaStream_t s) {
+  cudaMemsetAsync(keys, 0xff, 3 * sizeof(unsigned long long), s);
+  cudaMemsetAsync(keys + 3, 0, 3 * sizeof(unsigned long long), s);
+  if (V) k_bbox<<<152 * 4, kBlock, 0, s>>>(V, xyz, keys);
+}
+
+double key_to_double(unsigned long long k) {
+  const unsigned long long b = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
+  double d;
+  memcpy(&d, &b, sizeof d);
+  return d;
+}
+
+void launch_count_out_of_range(long long n, const int* a, int limit, unsigned long long* bad, cudaStream_t s) {
+  if (n > 0) k_count_out_of_range<<<152 * 4, kBlock, 0, s>>>(n, a, limit, bad);
 }
 
 }  // namespace sprg

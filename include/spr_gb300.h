@@ -210,6 +210,31 @@ int sprg_mark_bad_quality(sprg_ctx* ctx, double good_quality, int32_t* flags, lo
    minimum below 1 (1 if none), the value of the first element holding it. */
 int sprg_get_min_quality(sprg_ctx* ctx, double* out);
 
+/* ---- incremental update after host topology changes ------------------------
+   The adapt loop modifies the mesh on the host (refine, coarsen, swap, snap)
+   and re-marks it every iteration (ma/maRefine.cc:420-448,
+   ma/maCoarsen.cc:294-320).  Instead of a new context (a full flatten and
+   upload), the caller sends what changed in the flattened arrays: the new
+   counts and, per entity kind, the rows (ids) whose values are new --
+   moved vertices, new or rewired elements and edges.  Rows below the old
+   count keep their values unless listed; rows from the old count up to the
+   new one must all be listed; rows beyond the new count are dropped (a
+   deleted entity is expressed by moving the last row into its slot).  The
+   vertex-element adjacency, the FP32 records, patch weights, bins, caches
+   and graphs are rebuilt or invalidated on the device; a batch view is
+   cleared.  averaging CSR (optional, both or neither): the reference's
+   getAdjacent order for the size average, as in sprg_mesh_view.
+   Everything is validated before anything changes (SPRG_EINVAL). */
+typedef struct sprg_mesh_delta {
+  int64_t n_verts, n_elems, n_edges;           /* counts after the update */
+  int64_t n_vert_rows;  const int32_t* vert_ids;  const double* coords;      /* n x 3 */
+  int64_t n_elem_rows;  const int32_t* elem_ids;  const int32_t* elem_verts; /* n x (dim + 1) */
+  int64_t n_edge_rows;  const int32_t* edge_ids;  const int32_t* edge_verts; /* n x 2 */
+  const int32_t* vert_elem_offsets;            /* n_verts + 1, optional */
+  const int32_t* vert_elems;                   /* n_elems x (dim + 1), optional */
+} sprg_mesh_delta;
+int sprg_update_mesh(sprg_ctx* ctx, const sprg_mesh_delta* delta);
+
 /* Anisotropic metric from a nodal Hessian (V x 9 row-major, e.g. the
    recovered field of the gradient of the recovered gradient): sizes (V x 3)
    h_i = clamp(sqrt(eps / |lambda_i|), h_min, h_max) and frames (V x 9,
