@@ -27,6 +27,7 @@ UNITS = {
     "sprg_noalloc.cu": [],
     "sprg_learned.cu": [],
     "sprg_box.cpp": ["-x", "cu"],
+    "sprg_smb.cpp": [],
 }
 
 

@@ -89,3 +89,18 @@ def makeMdsBox(nx, ny, nz, wx=1.0, wy=1.0, wz=1.0):
     _lib.check(lib.sprg_box_fill(nx, ny, nz, float(wx), float(wy), float(wz) if nz else 0.0,
                                  coords.ctypes.data, ev.ctypes.data, ed.ctypes.data))
     return Mesh(dim, coords, ev, ed, grid=(nx, ny, nz))
+
+
+def read_smb(path):
+    """One part of an MDS .smb file (simplex meshes) as a flattened Mesh in
+    MDS index order (sprg_smb_read)."""
+    lib = _lib.load()
+    dim = ctypes.c_int()
+    V, T, E = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+    p = str(path).encode()
+    _lib.check(lib.sprg_smb_counts(p, ctypes.byref(dim), ctypes.byref(V), ctypes.byref(T), ctypes.byref(E)))
+    coords = np.empty((V.value, 3), np.float64)
+    ev = np.empty((T.value, dim.value + 1), np.int32)
+    ed = np.empty((E.value, 2), np.int32)
+    _lib.check(lib.sprg_smb_read(p, coords.ctypes.data, ev.ctypes.data, ed.ctypes.data))
+    return Mesh(dim.value, coords, ev, ed)

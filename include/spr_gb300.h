@@ -210,6 +210,20 @@ int sprg_mark_bad_quality(sprg_ctx* ctx, double good_quality, int32_t* flags, lo
    minimum below 1 (1 if none), the value of the first element holding it. */
 int sprg_get_min_quality(sprg_ctx* ctx, double* out);
 
+/* ---- mesh files --------------------------------------------------------------
+   One part of an MDS .smb file (mds/mds_smb.c:547-606, versions 0-6,
+   uncompressed) read into the flattened layout of sprg_mesh_view, in MDS
+   index order: counts and connectivity, coordinates; the sections after the
+   coordinates (parametric coordinates, remote copies, classification, tags,
+   matches, meta) are not read.  Simplex meshes only: files with quads,
+   hexes, prisms or pyramids are refused (SPRG_EINVAL).  Element vertices
+   follow MDS's derivation from the downward adjacency (mds/mds.c:498,
+   627-662), the order getDownward(e, 0) returns.  Host-only calls.
+   sprg_smb_counts: dim and counts; sprg_smb_read: coords (n_verts x 3),
+   elem_verts (n_elems x (dim + 1)), edge_verts (n_edges x 2). */
+int sprg_smb_counts(const char* path, int* dim, int64_t* n_verts, int64_t* n_elems, int64_t* n_edges);
+int sprg_smb_read(const char* path, double* coords, int32_t* elem_verts, int32_t* edge_verts);
+
 /* ---- incremental update after host topology changes ------------------------
    The adapt loop modifies the mesh on the host (refine, coarsen, swap, snap)
    and re-marks it every iteration (ma/maRefine.cc:420-448,

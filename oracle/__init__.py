@@ -117,6 +117,28 @@ class OracleMesh:
     def set_coords(self, xyz):
         self.coords[:] = np.asarray(xyz, np.float64)
 
+    @classmethod
+    def from_down(cls, dim, coords, edges, faces, tets=None):
+        """MDS mesh from downward adjacency: edges (E x 2 vertices), faces
+        (F x 3 edges), tets (T x 4 faces, 3D)."""
+        L = load()
+        x = np.ascontiguousarray(coords, np.float64)
+        e = np.ascontiguousarray(edges, np.int32)
+        f = np.ascontiguousarray(faces, np.int32)
+        t = np.ascontiguousarray(tets if tets is not None else np.zeros((0, 4)), np.int32)
+        h = _P()
+        rc = L.orc_from_down(dim, x.shape[0], x.ctypes.data, e.shape[0], e.ctypes.data, f.shape[0], f.ctypes.data,
+                             t.shape[0], t.ctypes.data, ctypes.byref(h))
+        if rc:
+            raise RuntimeError(f"orc_from_down failed: {rc}")
+        return cls(h)
+
+    def down(self, d):
+        """Stored downward adjacency of dimension d (one dimension down)."""
+        n = self.L.orc_count(self.h, d)
+        deg = {1: 2, 2: 3, 3: 4}[d]
+        return _arr(self.L.orc_down(self.h, d), (n, deg), np.int32).copy()
+
     @property
     def elem_verts(self):
         return _arr(self.L.orc_elem_verts(self.h), (self.T, self.dim + 1), np.int32).copy()

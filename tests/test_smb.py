@@ -1,0 +1,136 @@
+"""The .smb reader (sprg_smb_counts / sprg_smb_read, host-only calls).
+
+Files are written here in the layout of mds/mds_smb.c (big-endian, version
+4: header, counts, downward connectivity, coordinates, parametric
+coordinates, remotes, classification, tags, matches).  Pinning: the
+downward adjacency the oracle's MDS box stores, read back, gives exactly the
+element vertices of the flattened makeMdsBox; with the face lists of every
+tet (and the edge lists of every triangle) shuffled, the element vertices
+equal the oracle's independent restatement of MDS's derivation
+(orc_from_down).  Mixed-element and malformed files are refused."""
+import os
+import struct
+
+import numpy as np
+import pytest
+
+SMB_TYPES = 8  # vertex, edge, triangle, quad, hex, prism, pyramid, tet
+
+
+def write_smb(path, dim, coords, edges, faces, tets=None, version=4, quads=0):
+    V, E, F = len(coords), len(edges), len(faces)
+    T = 0 if tets is None else len(tets)
+    u = lambda a: struct.pack(f">{len(a)}I", *[int(x) for x in a])
+    d = lambda a: struct.pack(f">{len(a)}d", *[float(x) for x in a])
+    counts = [V, E, F, quads, 0, 0, 0, T]
+    out = [u([0, version, dim, 1]), u(counts),
+           u(np.ravel(edges)), u(np.ravel(faces)), u([0] * (4 * quads)), b"", b"", b"",
+           u(np.ravel(tets) if T else []), d(np.ravel(coords))]
+    if version >= 2:
+        out.append(d([0.0] * (2 * V)))
+    out.append(u([0]))                                        # remotes: no peers
+    for n in counts:                                          # classification
+        out.append(u([0] * (2 * n)))
+    out.append(u([0]))                                        # no tags
+    for _ in range(SMB_TYPES):
+        out.append(b"")                                       # (tag sizes: none)
+    for _ in range(SMB_TYPES):
+        out.append(u([0]))                                    # matches: no peers
+    with open(path, "wb") as f:
+        f.write(b"".join(out))
+
+
+@pytest.fixture(scope="module")
+def host_lib():
+    """The library (its .smb calls need no GPU)."""
+    from core_gb300 import build
+    build.build()
+    import core_gb300
+    return core_gb300.load()
+
+
+@pytest.mark.parametrize("n,nz", [(3, 3), (4, 2), (5, 0)])
+def test_box_read_back_matches_makeMdsBox(host_lib, oracle_lib, tmp_path, n, nz):
+    from core_gb300.mesh import makeMdsBox, read_smb
+    o = oracle_lib.OracleMesh.box(n, n, nz)
+    dim = 3 if nz else 2
+    path = tmp_path / "box0.smb"
+    write_smb(path, dim, o.coords, o.down(1), o.down(2), o.down(3) if dim == 3 else None)
+    m = read_smb(path)
+    b = makeMdsBox(n, n, nz)
+    assert m.dim == dim
+    assert np.array_equal(m.coords, b.coords)
+    assert np.array_equal(m.elem_verts, b.elem_verts) and np.array_equal(m.edge_verts, b.edge_verts)
+
+
+@pytest.mark.parametrize("dim", [3, 2])
+def test_shuffled_downward_lists_follow_mds_derivation(host_lib, oracle_lib, tmp_path, dim):
+    from core_gb300.mesh import read_smb
+    o = oracle_lib.OracleMesh.box(4, 3, 2 if dim == 3 else 0)
+    rng = np.random.Generator(np.random.PCG64(3))
+    edges, faces = o.down(1), o.down(2)
+    tets = o.down(3) if dim == 3 else None
+    if dim == 3:
+        tets = np.array([rng.permutation(t) for t in tets], np.int32)
+    faces = np.array([rng.permutation(f) for f in faces], np.int32)
+    edges = np.array([rng.permutation(e) for e in edges], np.int32)
+    path = tmp_path / "shuffled0.smb"
+    write_smb(path, dim, o.coords, edges, faces, tets)
+    m = read_smb(path)
+    ref = oracle_lib.OracleMesh.from_down(dim, o.coords, edges, faces, tets)
+    assert np.array_equal(m.elem_verts, ref.elem_verts)
+    assert np.array_equal(m.edge_verts, edges)
+    # the element vertices are still the elements' vertex sets
+    assert np.array_equal(np.sort(m.elem_verts, axis=1), np.sort(o.elem_verts, axis=1))
+
+
+def test_refused_files(host_lib, oracle_lib, tmp_path):
+    from core_gb300 import _lib as K
+    from core_gb300.mesh import read_smb
+    o = oracle_lib.OracleMesh.box(2, 2, 2)
+    good = tmp_path / "good0.smb"
+    write_smb(good, 3, o.coords, o.down(1), o.down(2), o.down(3))
+    read_smb(good)
+    raw = good.read_bytes()
+    cases = {}
+    cases["truncated"] = raw[: len(raw) // 3]
+    cases["version"] = raw[:4] + struct.pack(">I", 9) + raw[8:]
+    bad_edges = o.down(1).copy()
+    bad_edges[0, 0] = o.V  # a vertex id beyond the count
+    for name, data in cases.items():
+        p = tmp_path / f"{name}0.smb"
+        p.write_bytes(data)
+        with pytest.raises(K.SprgError) as ei:
+            read_smb(p)
+        assert ei.value.code == K.SPRG_EINVAL, name
+    p = tmp_path / "badid0.smb"
+    write_smb(p, 3, o.coords, bad_edges, o.down(2), o.down(3))
+    with pytest.raises(K.SprgError):
+        read_smb(p)
+    p = tmp_path / "mixed0.smb"
+    write_smb(p, 3, o.coords, o.down(1), o.down(2), o.down(3), quads=1)
+    with pytest.raises(K.SprgError):
+        read_smb(p)
+    with pytest.raises(K.SprgError):
+        read_smb(tmp_path / "missing0.smb")
+
+
+@pytest.mark.gpu
+def test_read_mesh_runs_the_pass(gpu_lib, oracle_lib, tmp_path):
+    """A mesh read from a file runs the FP64 pass to the oracle's marks."""
+    import core_gb300 as cg
+    from core_gb300 import workload
+    from core_gb300.mesh import read_smb
+    o = oracle_lib.OracleMesh.box(6, 6, 6)
+    jit = workload.box(6, jitter=0.2, seed=9).coords
+    o.set_coords(jit)
+    path = tmp_path / "jbox0.smb"
+    write_smb(path, 3, o.coords, o.down(1), o.down(2), o.down(3))
+    m = read_smb(path)
+    u = workload.bump_field(m.coords, seed=9)
+    rc, size_o, L_o, flags_o, ns_o, nc_o, _ = o.estimate_and_mark(u, 0.1)
+    assert rc == 0
+    with cg.Context(m) as ctx:
+        size, flags, ns, nc, _ = ctx.estimate_and_mark(u, 0.1)
+    assert np.array_equal(flags, flags_o) and (ns, nc) == (ns_o, nc_o)
+    assert np.abs(size - size_o).max() <= 1e-10 * np.abs(size_o).max()
