@@ -1860,7 +1860,7 @@ static int aniso_pass_mixed(sprg_ctx* c, double eps, double h_min, double h_max,
   c->launches += 4;
   if (d_quality) {
     PB("quality_f32");
-    launch_quality_aniso_f32(m, c->qrec32.p, d_quality, c->stream);
+    launch_quality_aniso_f32(m, c->qrec32.p, P<double>(c->sizes3), P<double>(c->frames9), d_quality, c->stream);
     PE();
     c->launches += 1;
   }

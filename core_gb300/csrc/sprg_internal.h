@@ -136,7 +136,8 @@ void launch_mark_quality(int T, const double* q, double good, int* flags, unsign
 // Mixed-precision anisotropic pass.  Triangle patch weights (FP64, patch
 // CSR layout) with the listed vertices (weights not covering them) in lst;
 // FP32 metric records (12 floats per
-// vertex: h, frame) and quality records (FP64-selected vertex transforms);
+// vertex: h, frame) and quality records (FP32 vertex transforms and
+// determinants; ambiguous choices that matter are decided in FP64);
 // FP32 edge measure writing the mark bitmaps and the
 // edges within their error bound of 0.5 / 1.5 (guard); the guard's FP64
 // re-measure fixing those bits; FP32 qualities.
@@ -149,7 +150,8 @@ void launch_measure_aniso_f32(const DevMesh& m, const float* met, uint32_t* spli
                               int* gcount, int gcap, cudaStream_t s);
 void launch_measure_guard_f64(const DevMesh& m, const double* sizes, const double* frames, const int* guard,
                               const int* gcount, int gcap, uint32_t* split, uint32_t* collapse, cudaStream_t s);
-void launch_quality_aniso_f32(const DevMesh& m, const void* qrec, double* q, cudaStream_t s);
+void launch_quality_aniso_f32(const DevMesh& m, const void* qrec, const double* sizes, const double* frames, double* q,
+                              cudaStream_t s);
 // Triangle recovery-of-gradient operator (per mesh, FP64): K_va over the
 // patch vertices, tri_operator_slots() slots per vertex (kidx ints, kval 3
 // doubles each, klen counts; patches that are not fans are added to the

@@ -1596,36 +1596,52 @@ __global__ void __launch_bounds__(128) k_tri_weights(DevMesh m, double* __restri
 
 // Per vertex: the FP32 metric record h (3), frame (9, row-major) for the
 // edge measure, and the quality record: the vertex transform Q =
-// orth(R) diag(1/h) and its Jacobian determinant, both evaluated in FP64 by
-// the FP64 quality kernel's arithmetic (so the quality kernel picks the same
-// vertex as the FP64 one), Q then rounded to FP32.
+// orth(R) diag(1/h) and its Jacobian determinant in FP32.  The quality
+// kernel picks the vertex with the largest determinant as the reference
+// does; where the FP32 determinants cannot separate the candidates and the
+// candidates give different qualities, it decides with the FP64
+// determinants of the FP64 quality kernel's arithmetic.
 struct QualityRec {
   float q[9];
-  float pad;
-  double cj;
+  float cj;
 };
+__device__ __forceinline__ void transform_f32(const float* h, const float* R, float Q[3][3]) {
+  // orthogonalised frame columns, then Q = R diag(1 / h)
+  float c0x = R[0], c0y = R[3], c0z = R[6], c1x = R[1], c1y = R[4], c1z = R[7];
+  const float l0 = sqrtf(c0x * c0x + c0y * c0y + c0z * c0z);
+  c0x /= l0; c0y /= l0; c0z /= l0;
+  const float d = c0x * c1x + c0y * c1y + c0z * c1z;
+  c1x -= c0x * d; c1y -= c0y * d; c1z -= c0z * d;
+  const float l1 = sqrtf(c1x * c1x + c1y * c1y + c1z * c1z);
+  c1x /= l1; c1y /= l1; c1z /= l1;
+  const float c2x = c0y * c1z - c0z * c1y, c2y = c0z * c1x - c0x * c1z, c2z = c0x * c1y - c0y * c1x;
+  Q[0][0] = c0x / h[0]; Q[0][1] = c1x / h[1]; Q[0][2] = c2x / h[2];
+  Q[1][0] = c0y / h[0]; Q[1][1] = c1y / h[1]; Q[1][2] = c2y / h[2];
+  Q[2][0] = c0z / h[0]; Q[2][1] = c1z / h[1]; Q[2][2] = c2z / h[2];
+}
+__device__ __forceinline__ float det_f32(const float Q[3][3], int dim) {
+  if (dim == 3)
+    return Q[0][0] * (Q[1][1] * Q[2][2] - Q[1][2] * Q[2][1]) - Q[0][1] * (Q[1][0] * Q[2][2] - Q[1][2] * Q[2][0]) +
+           Q[0][2] * (Q[1][0] * Q[2][1] - Q[1][1] * Q[2][0]);
+  const float x = Q[0][1] * Q[1][2] - Q[0][2] * Q[1][1], y = Q[0][2] * Q[1][0] - Q[0][0] * Q[1][2],
+              z = Q[0][0] * Q[1][1] - Q[0][1] * Q[1][0];
+  return sqrtf(x * x + y * y + z * z);  // |row0 x row1|
+}
+
 __global__ void __launch_bounds__(kBlock) k_metric_f32(int V, int dim, const double* __restrict__ sizes,
                                                        const double* __restrict__ frames, float* __restrict__ out,
                                                        QualityRec* __restrict__ qrec) {
   const int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= V) return;
   float* o = out + 12 * (size_t)v;
-  double hv[3], Rv[9];
-  for (int k = 0; k < 3; ++k) {
-    hv[k] = sizes[3 * (size_t)v + k];
-    o[k] = (float)hv[k];
-  }
-  for (int k = 0; k < 9; ++k) {
-    Rv[k] = frames[9 * (size_t)v + k];
-    o[3 + k] = (float)Rv[k];
-  }
-  const double N[1] = {1.0};
-  const M3 Q = ref::get_transform(hv, Rv, N, 1);
+  for (int k = 0; k < 3; ++k) o[k] = (float)sizes[3 * (size_t)v + k];
+  for (int k = 0; k < 9; ++k) o[3 + k] = (float)frames[9 * (size_t)v + k];
+  float Q[3][3];
+  transform_f32(o, o + 3, Q);
   QualityRec r;
   for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j) r.q[3 * i + j] = (float)Q.m[i][j];
-  r.pad = 0.f;
-  r.cj = ref::jacobian_det(Q, dim);
+    for (int j = 0; j < 3; ++j) r.q[3 * i + j] = Q[i][j];
+  r.cj = det_f32(Q, dim);
   qrec[v] = r;
 }
 
@@ -1744,34 +1760,8 @@ __global__ void __launch_bounds__(kBlock) k_measure_guard_f64(DevMesh m, const d
 
 // mean-ratio quality under the anisotropic metric in FP32 (the vertex
 // transform with the largest determinant, ma/maQuality.cc:83-167)
-__global__ void __launch_bounds__(kBlock) k_quality_aniso_f32(DevMesh m, const QualityRec* __restrict__ qrec,
-                                                              double* __restrict__ q) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= m.T) return;
-  const int* ev = m.ev + (size_t)e * m.nn;
-  // the vertex with the largest FP64 determinant (getMetricWithMaxJacobean,
-  // ma/maQuality.cc:83-108, in the reference's order and comparison)
-  int best = 0;
-  double maxJ = -1.0;
-  for (int i = 0; i < m.nn; ++i) {
-    const double cJ = qrec[ev[i]].cj;
-    if (cJ > maxJ) {
-      maxJ = cJ;
-      best = i;
-    }
-  }
-  float Q[3][3];
-  {
-    const QualityRec r = qrec[ev[best]];
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-      for (int j = 0; j < 3; ++j) Q[i][j] = r.q[3 * i + j];
-  }
-  // edge vectors in metric space, (x_r - x_p) Q, from FP64 differences
-  double x[4][3];
-  for (int a = 0; a < m.nn; ++a)
-    for (int k = 0; k < 3; ++k) x[a][k] = m.xyz[3 * (size_t)ev[a] + k];
+// FP32 mean-ratio quality of element e under transform Q
+__device__ __forceinline__ float quality_with_f32(const DevMesh& m, const double (*x)[3], const float Q[3][3]) {
   auto mvec = [&](int r, int p, float* t) {
     float d[3];
     for (int k = 0; k < 3; ++k) d[k] = (float)(x[r][k] - x[p][k]);
@@ -1788,19 +1778,84 @@ __global__ void __launch_bounds__(kBlock) k_quality_aniso_f32(DevMesh m, const Q
   mvec(2, 0, a1);
   const float cx = a0[1] * a1[2] - a0[2] * a1[1], cy = a0[2] * a1[0] - a0[0] * a1[2],
               cz = a0[0] * a1[1] - a0[1] * a1[0];
-  float res;
   if (m.dim == 3) {
     float a2[3];
     mvec(3, 0, a2);
     const float Vm = (cx * a2[0] + cy * a2[1] + cz * a2[2]) / 6.f;  // det(J Q) / 6
-    res = 15552.f * (Vm * Vm) / (s * s * s);
-    if (Vm < 0) res = -res;
-  } else {
-    const float A = 0.5f * sqrtf(cx * cx + cy * cy + cz * cz);
-    res = 48.f * (A * A) / (s * s);
+    const float res = 15552.f * (Vm * Vm) / (s * s * s);
+    return Vm < 0 ? -res : res;
+  }
+  const float A = 0.5f * sqrtf(cx * cx + cy * cy + cz * cz);
+  return 48.f * (A * A) / (s * s);
+}
+
+// relative separation of FP32 determinants taken as certain (their error
+// is a few ulps for the orthonormal frames of the metric), and the
+// relative agreement of the candidates' qualities within which any of them
+// is the reference's value to the FP32 accuracy
+constexpr float kDetTie = 1e-5f, kQualTie = 4e-6f;
+
+__global__ void __launch_bounds__(kBlock) k_quality_aniso_f32(DevMesh m, const QualityRec* __restrict__ qrec,
+                                                              const double* __restrict__ sizes,
+                                                              const double* __restrict__ frames,
+                                                              double* __restrict__ q) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= m.T) return;
+  const int* ev = m.ev + (size_t)e * m.nn;
+  double x[4][3];
+  for (int a = 0; a < m.nn; ++a)
+    for (int k = 0; k < 3; ++k) x[a][k] = m.xyz[3 * (size_t)ev[a] + k];
+  // getMetricWithMaxJacobean (ma/maQuality.cc:83-108): the first vertex with
+  // the largest determinant
+  float cj[4];
+  int best = 0;
+  for (int i = 0; i < m.nn; ++i) {
+    cj[i] = qrec[ev[i]].cj;
+    if (cj[i] > cj[best]) best = i;
+  }
+  unsigned cand = 0;  // vertices the FP32 determinants cannot rule out
+  for (int i = 0; i < m.nn; ++i)
+    if (cj[i] * (1.f + kDetTie) >= cj[best]) cand |= 1u << i;
+  float Q[3][3];
+  auto load_q = [&](int i, float (*T)[3]) {
+    const QualityRec& r = qrec[ev[i]];
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b) T[a][b] = r.q[3 * a + b];
+  };
+  load_q(best, Q);
+  float res = quality_with_f32(m, x, Q);
+  if (cand != (1u << best)) {
+    bool agree = true;
+    for (int i = 0; i < m.nn; ++i) {
+      if (!(cand >> i & 1) || i == best) continue;
+      float T[3][3];
+      load_q(i, T);
+      const float qi = quality_with_f32(m, x, T);
+      if (!(fabsf(qi - res) <= kQualTie * fabsf(res))) agree = false;
+    }
+    if (!agree) {  // the FP64 determinants decide, in the reference's order
+      double maxJ = -1.0;
+      int pick = best;
+      for (int i = 0; i < m.nn; ++i) {
+        double hv[3], Rv[9];
+        for (int k = 0; k < 3; ++k) hv[k] = sizes[3 * (size_t)ev[i] + k];
+        for (int k = 0; k < 9; ++k) Rv[k] = frames[9 * (size_t)ev[i] + k];
+        const double N[1] = {1.0};
+        const double cJ = ref::jacobian_det(ref::get_transform(hv, Rv, N, 1), m.dim);
+        if (cJ > maxJ) {
+          maxJ = cJ;
+          pick = i;
+        }
+      }
+      if (pick != best) {
+        load_q(pick, Q);
+        res = quality_with_f32(m, x, Q);
+      }
+    }
   }
   q[e] = res;
 }
+
 
 // Recovery composed with the element gradient: on a P1 field f the
 // recovered gradient at a covered vertex is
@@ -2147,8 +2202,10 @@ void launch_measure_guard_f64(const DevMesh& m, const double* sizes, const doubl
 
 int quality_rec_bytes() { return (int)sizeof(QualityRec); }
 
-void launch_quality_aniso_f32(const DevMesh& m, const void* qrec, double* q, cudaStream_t s) {
-  if (m.T) k_quality_aniso_f32<<<nblk(m.T), kBlock, 0, s>>>(m, static_cast<const QualityRec*>(qrec), q);
+void launch_quality_aniso_f32(const DevMesh& m, const void* qrec, const double* sizes, const double* frames, double* q,
+                              cudaStream_t s) {
+  if (m.T)
+    k_quality_aniso_f32<<<nblk(m.T), kBlock, 0, s>>>(m, static_cast<const QualityRec*>(qrec), sizes, frames, q);
 }
 
 int tri_operator_slots() { return kOpSlots; }
