@@ -48,6 +48,9 @@ struct sprg_ctx {
   DevBuf titems, tcountb;  // triangle patches above the thread-per-vertex size
   DevBuf Lx, pairs, red, eflags;  // MA sweeps: lengths, vertex pairs, reduction scratch, element flags
   DevBuf logm;                    // LogAnisoSizeField: per-vertex log-metrics (V x 9)
+  // FP64 recovery on tets: per-mesh QR weights and the listed patches
+  DevBuf qw, qwlisted, qwitems, qwcount;
+  bool qw_ready = false;
   // mixed-precision anisotropic pass: triangle patch weights and their
   // listed vertices (per mesh), FP32 metric records, guarded edges
   DevBuf tw, twlisted, twitems, twcount, met32, qrec32, agitems, agcount, kidx, kval, klen, rec9;
@@ -253,9 +256,36 @@ int step_recover(sprg_ctx* c) {
   DevMesh& m = c->m;
   int nc = c->ip_nc;
   ENSURE(c->rec, sizeof(double) * (size_t)m.V * nc);
+  ENSURE(c->slab, sizeof(double) * (size_t)expand_grid() * expand_max_elems() * (4 + nc + 1));
+  if (m.dim == 3) {
+    // tets: the per-mesh FP64 QR weights, a weighted sum per vertex; the
+    // listed patches (growth, size) through the slab fits
+    ENSURE(c->qwitems, sizeof(int) * (size_t)(m.V > 0 ? m.V : 1));
+    ENSURE(c->qwcount, sizeof(int));
+    const ExpandList lst{P<int>(c->qwitems), P<int>(c->qwcount), m.V};
+    if (!c->qw_ready) {
+      ENSURE(c->qw, sizeof(double) * (size_t)m.T * m.nn);
+      ENSURE(c->qwlisted, (size_t)(m.V > 0 ? m.V : 1));
+      CK(cudaMemsetAsync(c->qwcount.p, 0, sizeof(int), c->stream));
+      PB("qr_weights_f64");
+      launch_qr_weights(m, P<double>(c->qw), P<unsigned char>(c->qwlisted), lst, c->stream);
+      PE();
+      c->launches += 1;
+      int rc = check_launch(c, "QR weights");
+      if (rc) return rc;
+      c->qw_ready = true;
+    }
+    PB("recover_f64");
+    launch_recover_w64(m, P<double>(c->ip), nc, P<double>(c->qw), P<unsigned char>(c->qwlisted), P<double>(c->rec),
+                       c->stream);
+    PE();
+    c->launches += 1;
+    int rc = check_launch(c, "recover");
+    if (rc) return rc;
+    return listed_fits(c, c->cache64, P<double>(c->ip), nullptr, nc, P<double>(c->rec), lst);
+  }
   ENSURE(c->xitems, sizeof(int) * (size_t)(m.V > 0 ? m.V : 1));
   ENSURE(c->xcount, sizeof(int));
-  ENSURE(c->slab, sizeof(double) * (size_t)expand_grid() * expand_max_elems() * (4 + nc + 1));
   ENSURE(c->titems, sizeof(int) * (size_t)(m.dim == 2 && m.V > 0 ? m.V : 1));
   ENSURE(c->tcountb, sizeof(int));
   CK(cudaMemsetAsync(c->xcount.p, 0, sizeof(int), c->stream));
@@ -315,8 +345,11 @@ int step_measure_iso(sprg_ctx* c) {
 int fill_info(sprg_ctx* c, sprg_size_info* info) {
   double o3[3];
   CK(cudaMemcpy(o3, c->out3.p, sizeof o3, cudaMemcpyDeviceToHost));
+  // listed patches of the last FP64 recovery (tets: the per-mesh list of
+  // the QR weights; triangles: the pass's expansion list)
   int xc = 0;
-  CK(cudaMemcpy(&xc, c->xcount.p, sizeof xc, cudaMemcpyDeviceToHost));
+  const DevBuf& cnt = c->m.dim == 3 ? c->qwcount : c->xcount;
+  if (cnt.p) CK(cudaMemcpy(&xc, cnt.p, sizeof xc, cudaMemcpyDeviceToHost));
   c->last_info.eps_star_norm2 = o3[0];
   c->last_info.error_sum = o3[1];
   c->last_info.size_factor = o3[2];
@@ -510,6 +543,7 @@ static void invalidate_mesh_state(sprg_ctx* c) {
   c->bins_ready = false;
   c->tuned = false;
   c->tw_ready = false;
+  c->qw_ready = false;
   c->vv_ready = false;
   c->cache64.valid = c->cache32.valid = c->cache2d.valid = false;
   c->batch_n = 0;
@@ -677,7 +711,7 @@ int sprg_destroy(sprg_ctx* c) {
   DevBuf* bufs[] = {&c->xyz,   &c->xyz32,   &c->ev,   &c->edv,   &c->poff,    &c->pel,    &c->aoff,
                     &c->ael,   &c->tmp,     &c->f,    &c->ip,    &c->rec,     &c->err,    &c->esize,
                     &c->size,  &c->L,       &c->flags, &c->q,    &c->sizes3,  &c->frames9, &c->partials,
-                    &c->out3,  &c->status,  &c->count, &c->xitems, &c->xcount, &c->slab, &c->bits, &c->titems, &c->tcountb, &c->Lx, &c->pairs, &c->red, &c->eflags, &c->logm, &c->tw, &c->twlisted, &c->twitems, &c->twcount, &c->met32, &c->qrec32, &c->kidx, &c->kval, &c->klen, &c->rec9, &c->cache2d.v, &c->cache2d.n, &c->cache2d.el, &c->agitems, &c->agcount,
+                    &c->out3,  &c->status,  &c->count, &c->xitems, &c->xcount, &c->slab, &c->bits, &c->titems, &c->tcountb, &c->Lx, &c->pairs, &c->red, &c->eflags, &c->logm, &c->qw, &c->qwlisted, &c->qwitems, &c->qwcount, &c->tw, &c->twlisted, &c->twitems, &c->twcount, &c->met32, &c->qrec32, &c->kidx, &c->kval, &c->klen, &c->rec9, &c->cache2d.v, &c->cache2d.n, &c->cache2d.el, &c->agitems, &c->agcount,
                     &c->crec,  &c->vrec,    &c->rec32, &c->q32, &c->sz2,  &c->fcnt,   &c->guard, &c->tetd,
                     &c->wts,   &c->w64,     &c->listed, &c->geo, &c->geo64, &c->elen, &c->fitems, &c->gstamp, &c->gfit, &c->grec,
                     &c->tstamp, &c->tslot,  &c->trec, &c->tcount, &c->hess, &c->pcls, &c->bverts, &c->btiles, &c->bnext, &c->bvoff, &c->bseg, &c->bsegoff, &c->bratios, &c->vvoff, &c->vv, &c->vtile, &c->vr16, &c->rec16,

@@ -170,6 +170,11 @@ void launch_bbox(int V, const double* xyz, unsigned long long* keys, cudaStream_
 // *bad += the number of entries of a outside [0, limit)
 void launch_count_out_of_range(long long n, const int* a, int limit, unsigned long long* bad, cudaStream_t s);
 double key_to_double(unsigned long long k);
+// FP64 SPR weights of tet patches (per mesh, the reference's QR; listed
+// patches in lst) and the FP64 recovery from them (listed vertices skipped)
+void launch_qr_weights(const DevMesh& m, double* w, unsigned char* listed, ExpandList lst, cudaStream_t s);
+void launch_recover_w64(const DevMesh& m, const double* ip, int nc, const double* w, const unsigned char* listed,
+                        double* rec, cudaStream_t s);
 // FP64 guard band of the FP32 path: re-decide the listed edges' bits.
 // One FP64 gradient (at the integration point) per element the guard touches.
 struct GuardTet {

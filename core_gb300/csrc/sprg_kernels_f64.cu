@@ -1986,6 +1986,118 @@ __global__ void __launch_bounds__(kBlock) k_count_out_of_range(long long n, cons
   if (c) atomicAdd(bad, c);
 }
 
+// ---------------------------------------------------------------------
+// FP64 SPR weights of tet patches (once per mesh): the patch fit evaluated
+// at the vertex is linear in the samples, eps*(v) = sum_j w_j b_j, with
+// w = Q [R^-T t; 0] (t = [1, x_v, y_v, z_v]).  One warp per vertex, a row
+// per lane: the reference's Householder QR and 1e-10 rank test
+// (mth/mthQR.cc:19-126) as in recover_vertex_warp, then R^T z = t solved
+// from R and [z; 0] taken through the reflectors in reverse order.  Every
+// later FP64 recovery of the mesh is a weighted sum per vertex.  Patches
+// with fewer than 4 or more than 32 elements or rank deficient are listed
+// (lst) for the FP64 slab fits.
+// ---------------------------------------------------------------------
+__global__ void __launch_bounds__(kBlock) k_qr_weights(DevMesh m, double* __restrict__ w,
+                                                       unsigned char* __restrict__ listed, ExpandList lst) {
+  constexpr int NT = 4;
+  const int lane = threadIdx.x & 31;
+  const int v = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+  if (v >= m.V) return;
+  const int beg = m.p_off[v];
+  const int cnt = m.p_off[v + 1] - beg;
+  auto give_up = [&]() {
+    if (lane == 0) {
+      listed[v] = 1;
+      const int slot = atomicAdd(lst.count, 1);
+      if (slot < lst.cap) lst.items[slot] = v;
+    }
+  };
+  if (cnt < NT || cnt > 32) {
+    give_up();
+    return;
+  }
+  double a[NT];
+  if (lane < cnt) {
+    const V3 p = elem_ip_point(m, m.p_el[beg + lane]);
+    a[0] = 1.0;
+    a[1] = p.v[0];
+    a[2] = p.v[1];
+    a[3] = p.v[2];
+  } else {
+    a[0] = a[1] = a[2] = a[3] = 0;
+  }
+  double vk[NT];  // this lane's entry of each reflector
+#pragma unroll
+  for (int k = 0; k < NT; ++k) {
+    const double cn = sqrt(warp_sum(lane >= k ? a[k] * a[k] : 0.0));
+    if (cn < 1e-10) {  // uniform across the warp
+      give_up();
+      return;
+    }
+    const double akk = __shfl_sync(0xffffffffu, a[k], k);
+    double vv = lane >= k ? a[k] : 0.0;
+    if (lane == k) vv += ((akk < 0) ? -1 : 1) * cn;
+    const double rn = sqrt(warp_sum(vv * vv));
+    vv /= rn;
+    vk[k] = vv;
+#pragma unroll
+    for (int j = k; j < NT; ++j) {
+      const double d = warp_sum(a[j] * vv);
+      a[j] -= 2 * d * vv;
+    }
+  }
+  // R in lanes 0..3; z = R^-T t by forward substitution
+  double R[NT][NT];
+#pragma unroll
+  for (int i = 0; i < NT; ++i)
+#pragma unroll
+    for (int j = 0; j < NT; ++j) R[i][j] = __shfl_sync(0xffffffffu, a[j], i);
+  const V3 xv = load_xyz(m.xyz, v);
+  const double t[NT] = {1.0, xv.v[0], xv.v[1], xv.v[2]};
+  double z[NT];
+#pragma unroll
+  for (int i = 0; i < NT; ++i) {
+    double acc = t[i];
+#pragma unroll
+    for (int j = 0; j < i; ++j) acc -= R[j][i] * z[j];
+    z[i] = acc / R[i][i];
+  }
+  // y = H_1 H_2 H_3 H_4 [z; 0]: the reflectors from the last to the first
+  double y = 0;
+#pragma unroll
+  for (int i = 0; i < NT; ++i)
+    if (lane == i) y = z[i];
+#pragma unroll
+  for (int k = NT - 1; k >= 0; --k) {
+    const double d = warp_sum(vk[k] * y);
+    y -= 2 * d * vk[k];
+  }
+  if (lane < cnt) w[beg + lane] = y;
+  if (lane == 0) listed[v] = 0;
+}
+
+// FP64 recovery from the weights: thread per vertex, NC components
+template <int NC>
+__global__ void __launch_bounds__(kBlock) k_recover_w64(DevMesh m, const double* __restrict__ ip,
+                                                        const double* __restrict__ w,
+                                                        const unsigned char* __restrict__ listed,
+                                                        double* __restrict__ rec) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= m.V || listed[v]) return;
+  const int beg = m.p_off[v], end = m.p_off[v + 1];
+  double acc[NC];
+#pragma unroll
+  for (int c = 0; c < NC; ++c) acc[c] = 0;
+  for (int k = beg; k < end; ++k) {
+    const double wk = w[k];
+    const double* b = ip + (size_t)m.p_el[k] * NC;
+#pragma unroll
+    for (int c = 0; c < NC; ++c) acc[c] += wk * b[c];
+  }
+#pragma unroll
+  for (int c = 0; c < NC; ++c) rec[(size_t)v * NC + c] = acc[c];
+}
+
 }  // namespace
 
 // ----------------------------------------------------------------------
@@ -2247,6 +2359,17 @@ double key_to_double(unsigned long long k) {
 
 void launch_count_out_of_range(long long n, const int* a, int limit, unsigned long long* bad, cudaStream_t s) {
   if (n > 0) k_count_out_of_range<<<152 * 4, kBlock, 0, s>>>(n, a, limit, bad);
+}
+
+void launch_qr_weights(const DevMesh& m, double* w, unsigned char* listed, ExpandList lst, cudaStream_t s) {
+  if (m.V) k_qr_weights<<<nblk((long)m.V * 32), kBlock, 0, s>>>(m, w, listed, lst);
+}
+
+void launch_recover_w64(const DevMesh& m, const double* ip, int nc, const double* w, const unsigned char* listed,
+                        double* rec, cudaStream_t s) {
+  if (!m.V) return;
+  if (nc == 3) k_recover_w64<3><<<nblk(m.V), kBlock, 0, s>>>(m, ip, w, listed, rec);
+  else k_recover_w64<9><<<nblk(m.V), kBlock, 0, s>>>(m, ip, w, listed, rec);
 }
 
 }  // namespace sprg
