@@ -1,9 +1,7 @@
-// One part of an MDS .smb mesh file read straight into the flattened layout
-// of sprg_mesh_view (mds/mds_smb.c:547-606, the pcu encoding of
-// pcu/pcu_io.c:242-336).
+// MDS .smb mesh files (one part) and the flattened layout of sprg_mesh_view
+// (mds/mds_smb.c:547-637, the pcu encoding of pcu/pcu_io.c:242-336).
 //
-// Layout of the parts read here, all big-endian (uint32 "unsigned",
-// IEEE float64 "double"):
+// Layout, all big-endian (uint32 "unsigned", IEEE float64 "double"):
 //   header     magic, version (<= 6), dim, number of parts
 //   counts     8 unsigned in SMB type order: vertex, edge, triangle, quad,
 //              hex, prism, pyramid, tet
@@ -13,20 +11,31 @@
 //              triangles + 3 quads, pyramid: 1 quad + 4 triangles, tet: 4
 //              triangles), as indices of that type
 //   coordinates 3 doubles per vertex
-// What follows (parametric coordinates from version 2, remote copies,
-// classification, tags, periodic matches, the apf meta section from
-// version 5) does not enter the estimate-and-mark pass and is not read.
+//   then parametric coordinates (version >= 2), remote copies,
+//   classification, tags, periodic matches (version >= 3), the apf meta
+//   section (version >= 5).
 //
-// Only simplex meshes are taken: files with quads, hexes, prisms or
-// pyramids are refused.  Element vertices follow MDS's derivation from the
-// downward adjacency (mds/mds.c:498 common_down, 627-662 convert_down): a
-// tet's edges are the common edges of face pairs (0,1) (0,2) (0,3) (1,3)
-// (1,2) (2,3), its vertices the common vertices of edge pairs (2,0) (0,1)
-// (1,2) (3,4); a triangle's vertices those of its edge pairs (2,0) (0,1)
-// (1,2).
+// Reader: the header, counts, connectivity and coordinates; the rest does
+// not enter the estimate-and-mark pass and is not read.  Only simplex
+// meshes are taken: files with quads, hexes, prisms or pyramids are
+// refused.  Element vertices follow MDS's derivation from the downward
+// adjacency (mds/mds.c:498 common_down, 627-662 convert_down): a tet's
+// edges are the common edges of face pairs (0,1) (0,2) (0,3) (1,3) (1,2)
+// (2,3), its vertices the common vertices of edge pairs (2,0) (0,1) (1,2)
+// (3,4); a triangle's vertices those of its edge pairs (2,0) (0,1) (1,2).
+//
+// Writer: version 4 (no meta section); the flattened edges, the triangles
+// of the elements numbered in order of first appearance (element order,
+// faces in the canonical order (0,1,2) (0,1,3) (1,2,3) (0,2,3) of
+// apf/apfMesh.cc, their edges (0,1) (1,2) (2,0)), so that the derivation
+// above gives back every element's vertex order; every entity classified on
+// the model entity of the mesh's dimension with tag 0 (the flattened mesh
+// carries no geometric classification); one part, no tags, no matches.
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <unordered_map>
+#include <utility>
 #include <vector>
 
 #include "spr_gb300.h"
@@ -65,9 +74,6 @@ struct Reader {
     return true;
   }
 };
-
-// downward degree of each SMB type (one dimension down)
-constexpr int kDownDegree[kTypes] = {0, 2, 3, 4, 6, 5, 5, 4};
 
 struct SmbMesh {
   uint32_t version = 0, dim = 0;
@@ -175,4 +181,145 @@ extern "C" int sprg_smb_read(const char* path, double* coords, int32_t* elem_ver
     }
   }
   return SPRG_OK;
+}
+
+namespace {
+
+struct Writer {
+  FILE* f = nullptr;
+  bool ok = true;
+  explicit Writer(const char* path) { f = std::fopen(path, "wb"); ok = f != nullptr; }
+  ~Writer() {
+    if (f) std::fclose(f);
+  }
+  void u32s(const uint32_t* p, size_t n) {
+    if (!ok || !n) return;
+    std::vector<unsigned char> b(4 * n);
+    for (size_t i = 0; i < n; ++i)
+      for (int k = 0; k < 4; ++k) b[4 * i + k] = (unsigned char)(p[i] >> (24 - 8 * k));
+    ok = std::fwrite(b.data(), 1, b.size(), f) == b.size();
+  }
+  void u32(uint32_t x) { u32s(&x, 1); }
+  void f64s(const double* p, size_t n) {
+    if (!ok || !n) return;
+    std::vector<unsigned char> b(8 * n);
+    for (size_t i = 0; i < n; ++i) {
+      uint64_t u;
+      std::memcpy(&u, p + i, 8);
+      for (int k = 0; k < 8; ++k) b[8 * i + k] = (unsigned char)(u >> (56 - 8 * k));
+    }
+    ok = std::fwrite(b.data(), 1, b.size(), f) == b.size();
+  }
+};
+
+uint64_t pair_key(uint32_t a, uint32_t b) {
+  if (a > b) std::swap(a, b);
+  return (uint64_t)a << 32 | b;
+}
+
+struct FaceKey {
+  uint32_t e[3];
+  bool operator==(const FaceKey& o) const { return e[0] == o.e[0] && e[1] == o.e[1] && e[2] == o.e[2]; }
+};
+struct FaceKeyHash {
+  size_t operator()(const FaceKey& k) const {
+    uint64_t h = k.e[0];
+    h = h * 0x9E3779B97F4A7C15ull ^ k.e[1];
+    h = h * 0x9E3779B97F4A7C15ull ^ k.e[2];
+    return (size_t)(h ^ (h >> 29));
+  }
+};
+
+}  // namespace
+
+extern "C" int sprg_smb_write(const char* path, const sprg_mesh_view* mv) {
+  if (!path || !mv || (mv->dim != 2 && mv->dim != 3) || mv->n_verts <= 0 || mv->n_elems <= 0 || mv->n_edges <= 0 ||
+      !mv->coords || !mv->elem_verts || !mv->edge_verts)
+    return SPRG_EINVAL;
+  if (mv->n_verts >= kMaxEntities || mv->n_edges >= kMaxEntities || mv->n_elems >= kMaxEntities) return SPRG_EINVAL;
+  const uint32_t V = (uint32_t)mv->n_verts, E = (uint32_t)mv->n_edges, T = (uint32_t)mv->n_elems;
+  const int nn = mv->dim + 1;
+  std::unordered_map<uint64_t, uint32_t> edge_of;
+  edge_of.reserve(2 * (size_t)E);
+  std::vector<uint32_t> edges(2 * (size_t)E);
+  for (uint32_t e = 0; e < E; ++e) {
+    const int32_t a = mv->edge_verts[2 * (size_t)e], b = mv->edge_verts[2 * (size_t)e + 1];
+    if (a < 0 || b < 0 || (uint32_t)a >= V || (uint32_t)b >= V || a == b) return SPRG_EINVAL;
+    edges[2 * (size_t)e] = (uint32_t)a;
+    edges[2 * (size_t)e + 1] = (uint32_t)b;
+    if (!edge_of.emplace(pair_key(a, b), e).second) return SPRG_EINVAL;  // duplicate edge
+  }
+  static const int tri_edge[3][2] = {{0, 1}, {1, 2}, {2, 0}};
+  static const int tet_tri[4][3] = {{0, 1, 2}, {0, 1, 3}, {1, 2, 3}, {0, 2, 3}};
+  // triangles: the elements themselves (2D) or the tets' faces (3D)
+  std::vector<uint32_t> tris, tet_faces;
+  auto tri_edges = [&](const uint32_t* v, uint32_t* out) {
+    for (int i = 0; i < 3; ++i) {
+      auto it = edge_of.find(pair_key(v[tri_edge[i][0]], v[tri_edge[i][1]]));
+      if (it == edge_of.end()) return false;
+      out[i] = it->second;
+    }
+    return true;
+  };
+  if (mv->dim == 2) {
+    tris.resize(3 * (size_t)T);
+    for (uint32_t t = 0; t < T; ++t) {
+      uint32_t v[3];
+      for (int i = 0; i < 3; ++i) {
+        const int32_t x = mv->elem_verts[3 * (size_t)t + i];
+        if (x < 0 || (uint32_t)x >= V) return SPRG_EINVAL;
+        v[i] = (uint32_t)x;
+      }
+      if (!tri_edges(v, &tris[3 * (size_t)t])) return SPRG_EINVAL;
+    }
+  } else {
+    std::unordered_map<FaceKey, uint32_t, FaceKeyHash> face_of;  // the face's three edge ids, sorted
+    face_of.reserve(2 * (size_t)T);
+    tet_faces.resize(4 * (size_t)T);
+    for (uint32_t t = 0; t < T; ++t) {
+      uint32_t v[4];
+      for (int i = 0; i < 4; ++i) {
+        const int32_t x = mv->elem_verts[4 * (size_t)t + i];
+        if (x < 0 || (uint32_t)x >= V) return SPRG_EINVAL;
+        v[i] = (uint32_t)x;
+      }
+      for (int f = 0; f < 4; ++f) {
+        const uint32_t fv[3] = {v[tet_tri[f][0]], v[tet_tri[f][1]], v[tet_tri[f][2]]};
+        uint32_t fe[3];
+        if (!tri_edges(fv, fe)) return SPRG_EINVAL;
+        FaceKey k{{fe[0], fe[1], fe[2]}};
+        if (k.e[0] > k.e[1]) std::swap(k.e[0], k.e[1]);
+        if (k.e[1] > k.e[2]) std::swap(k.e[1], k.e[2]);
+        if (k.e[0] > k.e[1]) std::swap(k.e[0], k.e[1]);
+        auto ins = face_of.emplace(k, (uint32_t)(tris.size() / 3));
+        if (ins.second) tris.insert(tris.end(), fe, fe + 3);
+        const uint32_t id = ins.first->second;
+        tet_faces[4 * (size_t)t + f] = id;
+      }
+    }
+  }
+  const uint32_t F = (uint32_t)(tris.size() / 3);
+  const uint32_t Tt = mv->dim == 3 ? T : 0;
+  Writer w(path);
+  const uint32_t counts[kTypes] = {V, E, F, 0, 0, 0, 0, Tt};
+  w.u32(0);  // magic
+  w.u32(4);  // version
+  w.u32((uint32_t)mv->dim);
+  w.u32(1);  // one part
+  w.u32s(counts, kTypes);
+  w.u32s(edges.data(), edges.size());
+  w.u32s(tris.data(), tris.size());
+  w.u32s(tet_faces.data(), tet_faces.size());
+  w.f64s(mv->coords, 3 * (size_t)V);
+  std::vector<double> params(2 * (size_t)V, 0.0);
+  w.f64s(params.data(), params.size());
+  w.u32(0);  // remote copies: no peers
+  for (int t = 0; t < kTypes; ++t) {  // classification: (tag 0, dimension of the mesh)
+    std::vector<uint32_t> cls(2 * (size_t)counts[t]);
+    for (size_t j = 0; j < counts[t]; ++j) cls[2 * j + 1] = (uint32_t)mv->dim;
+    w.u32s(cls.data(), cls.size());
+  }
+  w.u32(0);                                       // no tags (no per-type tag sizes follow)
+  for (int t = 0; t < kTypes; ++t) w.u32(0);      // periodic matches: no peers
+  return w.ok ? SPRG_OK : SPRG_EINVAL;
 }

@@ -104,3 +104,10 @@ def read_smb(path):
     ed = np.empty((E.value, 2), np.int32)
     _lib.check(lib.sprg_smb_read(p, coords.ctypes.data, ev.ctypes.data, ed.ctypes.data))
     return Mesh(dim.value, coords, ev, ed)
+
+
+def write_smb(mesh, path):
+    """Write a flattened Mesh as one part of an MDS .smb file (sprg_smb_write)."""
+    lib = _lib.load()
+    view = mesh.view()
+    _lib.check(lib.sprg_smb_write(str(path).encode(), ctypes.byref(view)))

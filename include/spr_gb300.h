@@ -223,6 +223,13 @@ int sprg_get_min_quality(sprg_ctx* ctx, double* out);
    elem_verts (n_elems x (dim + 1)), edge_verts (n_edges x 2). */
 int sprg_smb_counts(const char* path, int* dim, int64_t* n_verts, int64_t* n_elems, int64_t* n_edges);
 int sprg_smb_read(const char* path, double* coords, int32_t* elem_verts, int32_t* edge_verts);
+/* mds_write_smb for one part (mds/mds_smb.c:617-637): version 4 with the
+   flattened edges, the elements' triangles numbered in order of first
+   appearance (so that the reader's derivation gives back each element's
+   vertex order), zero parametric coordinates, every entity classified on
+   the model entity of the mesh's dimension with tag 0, no remote copies,
+   tags or matches.  The optional averaging CSR of the view is not stored. */
+int sprg_smb_write(const char* path, const sprg_mesh_view* mesh);
 
 /* ---- incremental update after host topology changes ------------------------
    The adapt loop modifies the mesh on the host (refine, coarsen, swap, snap)
