@@ -57,7 +57,7 @@ struct sprg_ctx {
   bool tw_ready = false;
   // FP32 path buffers
   DevBuf crec, vrec, rec32, q32, sz2, fcnt, guard, tetd, wts, w64, listed, geo, geo64, elen, fitems;
-  DevBuf gstamp, gfit, grec, tstamp, tslot, trec, tcount;  // guard pipeline scratch
+  DevBuf gstamp, gfit, grec;  // guard pipeline scratch
   // learned form
   DevBuf hess;  // nodal Hessian upload (sprg_hessian_metric)
   // batch of independent meshes (sprg_set_batch)
@@ -82,9 +82,23 @@ struct sprg_ctx {
   // back into the pass's stream
   cudaStream_t side = nullptr;
   cudaEvent_t fork = nullptr, join = nullptr;
-  // copy stream of the host entry point: the flags upload runs beside the pass
+  // copy stream of the host entry point: the flags upload and (FP32) the size
+  // download run beside the pass
   cudaStream_t copy = nullptr;
   cudaEvent_t copy_fork = nullptr, copy_join = nullptr;
+  cudaEvent_t size_ready = nullptr, size_join = nullptr;
+  bool size_hook = false;  // the FP32 pass records size_ready after the vertex average
+  DevBuf mcount;           // split / collapse counts of the host entry point
+  // pinned staging of the small results read back after a pass (status,
+  // integrals, counters): enqueued on the stream, read after one synchronize
+  struct HostStage {
+    DevStatus st;
+    int xc, fb, me;
+    int fc[6];
+    double o3[3];
+    unsigned long long counts[2];
+  };
+  HostStage* stage = nullptr;
   int pass_id = 0;
   bool vrec_ready = false;  // coordinate records and SPR weights (per mesh)
   double frame[4] = {0, 0, 0, 1};  // coordinate records: x' = (x - c) s + 1 in [1, 2]
@@ -92,7 +106,6 @@ struct sprg_ctx {
   PatchCache cache64, cache32, cache2d;
   static constexpr int kGuardCap = 1 << 20;
   static constexpr float kGuardRel = 2e-6f;
-  static constexpr int kGuardTetCap = 1 << 22;  // FP64 element records of one guard pass
   std::string err_msg;
   int64_t launches = 0;
   sprg_size_info last_info{};
@@ -158,12 +171,25 @@ int check_launch(sprg_ctx* c, const char* what) {
   return SPRG_OK;
 }
 
+int ensure_stage(sprg_ctx* c) {
+  if (c->stage) return SPRG_OK;
+  void* p = nullptr;
+  cudaError_t e = cudaMallocHost(&p, sizeof(sprg_ctx::HostStage));
+  if (e != cudaSuccess) return cuda_fail(c, e, "cudaMallocHost");
+  c->stage = static_cast<sprg_ctx::HostStage*>(p);
+  memset(c->stage, 0, sizeof(sprg_ctx::HostStage));
+  return SPRG_OK;
+}
+
+// the device status word, read back with the stream's other results
 int sync_and_status(sprg_ctx* c) {
-  cudaError_t e = cudaStreamSynchronize(c->stream);
-  if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamSynchronize");
-  DevStatus st;
-  e = cudaMemcpy(&st, c->status.p, sizeof st, cudaMemcpyDeviceToHost);
+  int rc = ensure_stage(c);
+  if (rc) return rc;
+  cudaError_t e = cudaMemcpyAsync(&c->stage->st, c->status.p, sizeof(DevStatus), cudaMemcpyDeviceToHost, c->stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "status readback");
+  e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamSynchronize");
+  const DevStatus st = c->stage->st;
   if (st.code == SPRG_EPATCH)
     return fail(c, SPRG_EPATCH,
                 st.where >= 0 ? "SPR: patch construction failed at vertex " + std::to_string(st.where)
@@ -342,41 +368,58 @@ int step_measure_iso(sprg_ctx* c) {
   return check_launch(c, "measure");
 }
 
-int fill_info(sprg_ctx* c, sprg_size_info* info) {
-  double o3[3];
-  CK(cudaMemcpy(o3, c->out3.p, sizeof o3, cudaMemcpyDeviceToHost));
+// the pass's integrals and counters, copied into the staging block on the
+// stream (read by info_from_stage after the stream is synchronized)
+int enqueue_info(sprg_ctx* c) {
+  int rc = ensure_stage(c);
+  if (rc) return rc;
+  sprg_ctx::HostStage* h = c->stage;
+  CK(cudaMemcpyAsync(h->o3, c->out3.p, sizeof h->o3, cudaMemcpyDeviceToHost, c->stream));
   // listed patches of the last FP64 recovery (tets: the per-mesh list of
   // the QR weights; triangles: the pass's expansion list)
-  int xc = 0;
+  h->xc = 0;
   const DevBuf& cnt = c->m.dim == 3 ? c->qwcount : c->xcount;
-  if (cnt.p) CK(cudaMemcpy(&xc, cnt.p, sizeof xc, cudaMemcpyDeviceToHost));
-  c->last_info.eps_star_norm2 = o3[0];
-  c->last_info.error_sum = o3[1];
-  c->last_info.size_factor = o3[2];
-  c->last_info.n_expanded = xc;
+  if (cnt.p) CK(cudaMemcpyAsync(&h->xc, cnt.p, sizeof h->xc, cudaMemcpyDeviceToHost, c->stream));
+  if (c->precision == SPRG_LEARNED && c->fbcount.p) {
+    CK(cudaMemcpyAsync(&h->fb, c->fbcount.p, sizeof h->fb, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(&h->me, c->mlp_err.p, sizeof h->me, cudaMemcpyDeviceToHost, c->stream));
+  }
+  if (c->precision == SPRG_FP32 && c->fcnt.p)
+    CK(cudaMemcpyAsync(h->fc, c->fcnt.p, sizeof h->fc, cudaMemcpyDeviceToHost, c->stream));
+  return SPRG_OK;
+}
+
+int info_from_stage(sprg_ctx* c, sprg_size_info* info) {
+  const sprg_ctx::HostStage* h = c->stage;
+  c->last_info.eps_star_norm2 = h->o3[0];
+  c->last_info.error_sum = h->o3[1];
+  c->last_info.size_factor = h->o3[2];
+  c->last_info.n_expanded = h->xc;
   c->last_info.n_fp64_refits = 0;
   c->last_info.n_guard_edges = 0;
   c->last_info.n_guard_unresolved = 0;
   c->last_info.n_learned_fallback = 0;
   if (c->precision == SPRG_LEARNED && c->fbcount.p) {
-    int fb = 0, me = 0;
-    CK(cudaMemcpy(&fb, c->fbcount.p, sizeof fb, cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(&me, c->mlp_err.p, sizeof me, cudaMemcpyDeviceToHost));
-    if (me) return fail(c, SPRG_ECUDA, "learned form: a tensor-core wait ran out of time");
-    c->last_info.n_learned_fallback = fb;
+    if (h->me) return fail(c, SPRG_ECUDA, "learned form: a tensor-core wait ran out of time");
+    c->last_info.n_learned_fallback = h->fb;
     c->last_info.n_fp64_refits = c->n_refit;
     c->last_info.n_expanded = c->n_listed - c->n_refit;
   }
   if (c->precision == SPRG_FP32 && c->fcnt.p) {
-    int fc[6] = {0, 0, 0, 0, 0, 0};
-    CK(cudaMemcpy(fc, c->fcnt.p, sizeof fc, cudaMemcpyDeviceToHost));
     c->last_info.n_fp64_refits = c->n_refit;
-    c->last_info.n_guard_edges = fc[1];
-    c->last_info.n_guard_unresolved = fc[4];
+    c->last_info.n_guard_edges = h->fc[1];
+    c->last_info.n_guard_unresolved = h->fc[4];
     c->last_info.n_expanded = c->n_listed - c->n_refit;
   }
   if (info) *info = c->last_info;
   return SPRG_OK;
+}
+
+int fill_info(sprg_ctx* c, sprg_size_info* info) {
+  int rc = enqueue_info(c);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(c->stream));
+  return info_from_stage(c, info);
 }
 
 int upload_ip(sprg_ctx* c, const double* ip, int ncomp) {
@@ -550,7 +593,6 @@ static void invalidate_mesh_state(sprg_ctx* c) {
   c->batch_nseg = 0;
   // stamps are zeroed when (re)allocated at the next guard pass
   release(c->gstamp);
-  release(c->tstamp);
   if (c->graph_exec) {
     cudaGraphExecDestroy(c->graph_exec);
     c->graph_exec = nullptr;
@@ -711,10 +753,10 @@ int sprg_destroy(sprg_ctx* c) {
   DevBuf* bufs[] = {&c->xyz,   &c->xyz32,   &c->ev,   &c->edv,   &c->poff,    &c->pel,    &c->aoff,
                     &c->ael,   &c->tmp,     &c->f,    &c->ip,    &c->rec,     &c->err,    &c->esize,
                     &c->size,  &c->L,       &c->flags, &c->q,    &c->sizes3,  &c->frames9, &c->partials,
-                    &c->out3,  &c->status,  &c->count, &c->xitems, &c->xcount, &c->slab, &c->bits, &c->titems, &c->tcountb, &c->Lx, &c->pairs, &c->red, &c->eflags, &c->logm, &c->qw, &c->qwlisted, &c->qwitems, &c->qwcount, &c->tw, &c->twlisted, &c->twitems, &c->twcount, &c->met32, &c->qrec32, &c->kidx, &c->kval, &c->klen, &c->rec9, &c->cache2d.v, &c->cache2d.n, &c->cache2d.el, &c->agitems, &c->agcount,
+                    &c->out3,  &c->status,  &c->count, &c->mcount, &c->xitems, &c->xcount, &c->slab, &c->bits, &c->titems, &c->tcountb, &c->Lx, &c->pairs, &c->red, &c->eflags, &c->logm, &c->qw, &c->qwlisted, &c->qwitems, &c->qwcount, &c->tw, &c->twlisted, &c->twitems, &c->twcount, &c->met32, &c->qrec32, &c->kidx, &c->kval, &c->klen, &c->rec9, &c->cache2d.v, &c->cache2d.n, &c->cache2d.el, &c->agitems, &c->agcount,
                     &c->crec,  &c->vrec,    &c->rec32, &c->q32, &c->sz2,  &c->fcnt,   &c->guard, &c->tetd,
                     &c->wts,   &c->w64,     &c->listed, &c->geo, &c->geo64, &c->elen, &c->fitems, &c->gstamp, &c->gfit, &c->grec,
-                    &c->tstamp, &c->tslot,  &c->trec, &c->tcount, &c->hess, &c->pcls, &c->bverts, &c->btiles, &c->bnext, &c->bvoff, &c->bseg, &c->bsegoff, &c->bratios, &c->vvoff, &c->vv, &c->vtile, &c->vr16, &c->rec16,
+                    &c->hess, &c->pcls, &c->bverts, &c->btiles, &c->bnext, &c->bvoff, &c->bseg, &c->bsegoff, &c->bratios, &c->vvoff, &c->vv, &c->vtile, &c->vr16, &c->rec16,
                     &c->ql,    &c->sizel,   &c->fbitems, &c->fbcount, &c->mlp_packed, &c->mlp_err, &c->mlp_tmp,
                     &c->cache64.v, &c->cache64.n, &c->cache64.el, &c->cache32.v, &c->cache32.n, &c->cache32.el};
   for (DevBuf* b : bufs) release(*b);
@@ -724,7 +766,10 @@ int sprg_destroy(sprg_ctx* c) {
     cudaStreamDestroy(c->copy);
     cudaEventDestroy(c->copy_fork);
     cudaEventDestroy(c->copy_join);
+    if (c->size_ready) cudaEventDestroy(c->size_ready);
+    if (c->size_join) cudaEventDestroy(c->size_join);
   }
+  if (c->stage) cudaFreeHost(c->stage);
   if (c->side) {
     cudaStreamSynchronize(c->side);
     cudaStreamDestroy(c->side);
@@ -1373,7 +1418,7 @@ static int pass_fast(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_
   ENSURE(c->out3, sizeof(double) * 4 * (size_t)(bv.n > 0 ? bv.n : 1));
   if ((rc = reset_status(c))) return rc;
   // fcnt: [0] refit patches, [1] guard edges, [3] listed patches,
-  // [4] unresolved guard edges, [5] failed guard fits (0, 3 per mesh; 1, 4, 5 per pass)
+  // [4] unresolved guard edges (0, 3 per mesh; 1, 4 per pass)
   ExpandList xl{P<int>(c->fitems), P<int>(c->fcnt) + 3, m.V};
   float4* vrec = P<float4>(c->vrec);
   uint4* rec32 = P<uint4>(c->rec32);
@@ -1383,7 +1428,7 @@ static int pass_fast(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_
   bool fork = false;
   if ((rc = listed_fork(c, xl, &fork))) return rc;
   CK(cudaMemsetAsync(P<int>(c->fcnt) + 1, 0, sizeof(int), c->stream));
-  CK(cudaMemsetAsync(P<int>(c->fcnt) + 4, 0, 2 * sizeof(int), c->stream));
+  CK(cudaMemsetAsync(P<int>(c->fcnt) + 4, 0, sizeof(int), c->stream));
   PB("prep_f32");
   fast_prep(m, P<double>(c->f), P<float4>(c->crec), vrec, c->stream);
   PE();
@@ -1415,6 +1460,7 @@ static int pass_fast(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_
   PB("average_f32");
   fast_average(m, P<float2>(c->q32), P<double>(c->out3), P<float2>(c->sz2), bv, c->stream);
   PE();
+  if (c->size_hook) CK(cudaEventRecord(c->size_ready, c->stream));
   PB("measure_f32");
   fast_measure(m, P<float>(c->elen), P<float2>(c->sz2), d_split, d_collapse, P<int>(c->guard), P<int>(c->fcnt) + 1,
                sprg_ctx::kGuardCap, sprg_ctx::kGuardRel, c->stream);
@@ -1422,29 +1468,20 @@ static int pass_fast(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_
   if (!c->gstamp.p) {
     ENSURE(c->gstamp, sizeof(int) * (size_t)m.V);
     CK(cudaMemsetAsync(c->gstamp.p, 0, sizeof(int) * (size_t)m.V, c->stream));
-    ENSURE(c->tstamp, sizeof(int) * (size_t)m.T);
-    CK(cudaMemsetAsync(c->tstamp.p, 0, sizeof(int) * (size_t)m.T, c->stream));
-    ENSURE(c->tslot, sizeof(int) * (size_t)m.T);
-    CK(cudaMemsetAsync(c->tslot.p, 0xff, sizeof(int) * (size_t)m.T, c->stream));
   }
-  const int tcap = m.T < sprg_ctx::kGuardTetCap ? m.T : sprg_ctx::kGuardTetCap;
   ENSURE(c->gfit, sizeof(int) * ((size_t)m.V + 1));
   ENSURE(c->grec, 3 * sizeof(double) * (size_t)m.V);
-  ENSURE(c->trec, sizeof(GuardTet) * (size_t)tcap);
-  ENSURE(c->tcount, sizeof(int));
-  GuardScratch gs{P<int>(c->gstamp),   ++c->pass_id,      P<int>(c->gfit) + 1,
-                  P<int>(c->gfit),     m.V,               P<double>(c->grec),
-                  P<int>(c->tstamp),   P<int>(c->tslot),  P<GuardTet>(c->trec),
-                  P<int>(c->tcount),   tcap,              P<double>(c->w64),
-                  P<unsigned char>(c->listed), P<double>(c->rec), P<double2>(c->geo64)};
-  static const char* const kGuardNames[4] = {"guard_collect", "guard_tets", "guard_fit", "guard_decide"};
-  for (int stage = 0; stage < 4; ++stage) {
+  GuardScratch gs{P<int>(c->gstamp), ++c->pass_id,      P<int>(c->gfit) + 1,         P<int>(c->gfit),
+                  m.V,               P<double>(c->grec), P<double>(c->w64),           P<unsigned char>(c->listed),
+                  P<double>(c->rec), P<double2>(c->geo64)};
+  static const char* const kGuardNames[kGuardStages] = {"guard_collect", "guard_fit", "guard_decide"};
+  for (int stage = 0; stage < kGuardStages; ++stage) {
     PB(kGuardNames[stage]);
     launch_guard_stage(stage, m, P<double>(c->f), P<double>(c->out3), P<int>(c->guard), P<int>(c->fcnt) + 1,
                        sprg_ctx::kGuardCap, d_split, d_collapse, P<int>(c->fcnt) + 4, gs, bv, c->stream);
     PE();
   }
-  c->launches += 12;  // 8 FP32-path kernels and 4 guard kernels (listed_fits counts its own)
+  c->launches += 8 + kGuardStages;  // FP32-path kernels and guard kernels (listed_fits counts its own)
   c->size_valid = false;  // the FP64 size buffer is filled on demand
   c->L_valid = false;
   return check_launch(c, "fast pass");
@@ -1562,16 +1599,21 @@ int sprg_estimate_and_mark(sprg_ctx* c, const double* u, double adapt_ratio, dou
   DevMesh& m = c->m;
   ENSURE(c->f, sizeof(double) * (size_t)m.V);
   ENSURE(c->flags, sizeof(int) * (size_t)m.E);
+  ENSURE(c->mcount, 2 * sizeof(unsigned long long));
+  if ((rc = ensure_stage(c))) return rc;
+  if (!c->copy) {
+    CK(cudaStreamCreateWithFlags(&c->copy, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&c->copy_fork, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&c->copy_join, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&c->size_ready, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&c->size_join, cudaEventDisableTiming));
+  }
   CK(cudaMemcpyAsync(c->f.p, u, sizeof(double) * (size_t)m.V, cudaMemcpyHostToDevice, c->stream));
   // the flag words are needed only by the write-back at the end: their
-  // upload runs on the copy stream beside the pass (ordered after this
-  // stream's earlier work, which may still read the buffer)
+  // upload runs on the copy stream beside the pass, after the field's upload
+  // (which then has the link to itself) and this stream's earlier work
+  // (which may still read the buffer)
   if (flags) {
-    if (!c->copy) {
-      CK(cudaStreamCreateWithFlags(&c->copy, cudaStreamNonBlocking));
-      CK(cudaEventCreateWithFlags(&c->copy_fork, cudaEventDisableTiming));
-      CK(cudaEventCreateWithFlags(&c->copy_join, cudaEventDisableTiming));
-    }
     CK(cudaEventRecord(c->copy_fork, c->stream));
     CK(cudaStreamWaitEvent(c->copy, c->copy_fork, 0));
     CK(cudaMemcpyAsync(c->flags.p, flags, sizeof(int) * (size_t)m.E, cudaMemcpyHostToDevice, c->copy));
@@ -1582,32 +1624,53 @@ int sprg_estimate_and_mark(sprg_ctx* c, const double* u, double adapt_ratio, dou
   size_t nw = ((size_t)m.E + 31) / 32;
   ENSURE(c->bits, sizeof(uint32_t) * 2 * nw);
   uint32_t* sb = P<uint32_t>(c->bits);
-  if ((rc = pass_resident(c, adapt_ratio, sb, sb + nw))) return rc;
-  if (flags) CK(cudaStreamWaitEvent(c->stream, c->copy_join, 0));
-  unsigned long long ncol = 0, nspl = 0;
-  if ((rc = apply_bits(c, SPRG_MARK_COLLAPSE, sb + nw, P<int>(c->flags)))) return rc;
-  CK(cudaMemcpyAsync(&ncol, c->count.p, sizeof ncol, cudaMemcpyDeviceToHost, c->stream));
-  if ((rc = apply_bits(c, SPRG_MARK_SPLIT, sb, P<int>(c->flags)))) return rc;
-  CK(cudaMemcpyAsync(&nspl, c->count.p, sizeof nspl, cudaMemcpyDeviceToHost, c->stream));
-  if (c->precision == SPRG_FP32) {
-    ENSURE(c->size, sizeof(double) * (size_t)m.V);
-    fast_size_to_f64(m.V, P<float2>(c->sz2), P<double>(c->size), c->stream);
+  // FP32: the size field is final after the vertex average, so its FP64
+  // conversion and download run on the copy stream beside the measure and
+  // the guard
+  const bool early_size = size_out && c->precision == SPRG_FP32;
+  if (early_size) ENSURE(c->size, sizeof(double) * (size_t)m.V);
+  c->size_hook = early_size;
+  rc = pass_resident(c, adapt_ratio, sb, sb + nw);
+  c->size_hook = false;
+  if (rc) return rc;
+  if (early_size) {
+    CK(cudaStreamWaitEvent(c->copy, c->size_ready, 0));
+    fast_size_to_f64(m.V, P<float2>(c->sz2), P<double>(c->size), c->copy);
     c->launches += 1;
-    c->size_valid = true;
-  } else if (c->precision == SPRG_LEARNED) {
-    ENSURE(c->size, sizeof(double) * (size_t)m.V);
-    learned_size_to_f64(m.V, P<float>(c->sizel), P<double>(c->size), c->stream);
-    c->launches += 1;
+    CK(cudaMemcpyAsync(size_out, c->size.p, sizeof(double) * (size_t)m.V, cudaMemcpyDeviceToHost, c->copy));
+    CK(cudaEventRecord(c->size_join, c->copy));
     c->size_valid = true;
   }
-  if (size_out)
-    CK(cudaMemcpyAsync(size_out, c->size.p, sizeof(double) * (size_t)m.V, cudaMemcpyDeviceToHost, c->stream));
-  rc = sync_and_status(c);
-  if (rc) return rc;
-  if (flags) CK(cudaMemcpy(flags, c->flags.p, sizeof(int) * (size_t)m.E, cudaMemcpyDeviceToHost));
-  if (n_split) *n_split = (long)nspl;
-  if (n_collapse) *n_collapse = (long)ncol;
-  return fill_info(c, info);
+  if (flags) CK(cudaStreamWaitEvent(c->stream, c->copy_join, 0));
+  CK(cudaMemsetAsync(c->mcount.p, 0, 2 * sizeof(unsigned long long), c->stream));
+  launch_apply_marks(m.E, sb, sb + nw, P<int>(c->flags), P<unsigned long long>(c->mcount), P<DevStatus>(c->status),
+                     c->stream);
+  c->launches += 1;
+  if ((rc = check_launch(c, "apply marks"))) return rc;
+  if (flags) CK(cudaMemcpyAsync(flags, c->flags.p, sizeof(int) * (size_t)m.E, cudaMemcpyDeviceToHost, c->stream));
+  if (!early_size) {
+    if (c->precision == SPRG_FP32) {
+      ENSURE(c->size, sizeof(double) * (size_t)m.V);
+      fast_size_to_f64(m.V, P<float2>(c->sz2), P<double>(c->size), c->stream);
+      c->launches += 1;
+      c->size_valid = true;
+    } else if (c->precision == SPRG_LEARNED) {
+      ENSURE(c->size, sizeof(double) * (size_t)m.V);
+      learned_size_to_f64(m.V, P<float>(c->sizel), P<double>(c->size), c->stream);
+      c->launches += 1;
+      c->size_valid = true;
+    }
+    if (size_out)
+      CK(cudaMemcpyAsync(size_out, c->size.p, sizeof(double) * (size_t)m.V, cudaMemcpyDeviceToHost, c->stream));
+  } else {
+    CK(cudaStreamWaitEvent(c->stream, c->size_join, 0));
+  }
+  CK(cudaMemcpyAsync(c->stage->counts, c->mcount.p, sizeof c->stage->counts, cudaMemcpyDeviceToHost, c->stream));
+  if ((rc = enqueue_info(c))) return rc;
+  if ((rc = sync_and_status(c))) return rc;
+  if (n_split) *n_split = (long)c->stage->counts[0];
+  if (n_collapse) *n_collapse = (long)c->stage->counts[1];
+  return info_from_stage(c, info);
 }
 
 int sprg_debug_read(sprg_ctx* c, const char* name, void* host, size_t bytes) {

@@ -70,9 +70,10 @@ struct ExpandList {
 
 // ---- kernel launchers (sprg_kernels_f64.cu) ---------------------------
 void launch_grad_ip_f64(const DevMesh& m, const double* f, int ncin, double* ip, cudaStream_t s);
-// xl: patches that need growth; big: triangle patches above the
-// thread-per-vertex size (fitted by the warp path inside this call; its
-// counter must be zero on entry)
+// Triangles (tets recover through launch_qr_weights / launch_recover_w64):
+// xl: patches that need growth; big: patches above the thread-per-vertex
+// size (fitted by the warp path inside this call; its counter must be zero
+// on entry)
 void launch_recover_f64(const DevMesh& m, const double* ip, int nc, double* rec, ExpandList xl, ExpandList big,
                         DevStatus* st, cudaStream_t s);
 // Patches on the expansion list: grow as the reference does, then fit.
@@ -112,6 +113,9 @@ void launch_mark_bits(int E, const double* L, uint32_t* split, uint32_t* collaps
 // markEntities semantics from a predicate bitmap
 void launch_apply_bits(int E, const uint32_t* bits, int which, int* flags, unsigned long long* count,
                        DevStatus* st, cudaStream_t s);
+// the collapse and split passes in one sweep (counts[0] split, counts[1] collapse)
+void launch_apply_marks(int E, const uint32_t* split_bits, const uint32_t* collapse_bits, int* flags,
+                        unsigned long long* counts, DevStatus* st, cudaStream_t s);
 // MA sweeps around the marks.  kind: 0 identity size field, 1 isotropic
 // (size), 2 anisotropic (sizes, frames), 3 log-interpolated anisotropic
 // (logm); pairs: n x 2 vertex ids, or NULL for the mesh's edges (n = E);
@@ -176,10 +180,6 @@ void launch_qr_weights(const DevMesh& m, double* w, unsigned char* listed, Expan
 void launch_recover_w64(const DevMesh& m, const double* ip, int nc, const double* w, const unsigned char* listed,
                         double* rec, cudaStream_t s);
 // FP64 guard band of the FP32 path: re-decide the listed edges' bits.
-// One FP64 gradient (at the integration point) per element the guard touches.
-struct GuardTet {
-  double g[3];
-};
 struct GuardScratch {
   int* stamp;      // V ints, persistent (de-duplication stamps)
   int stamp_id;    // distinct per pass
@@ -187,19 +187,14 @@ struct GuardScratch {
   int* fit_count;
   int fit_cap;
   double* rec64;   // V x 3 doubles (FP64 recovered values of collected vertices)
-  int* tstamp;     // T ints, persistent (element de-duplication stamps)
-  int* tslot;      // T ints: the element's record slot (valid where stamped this pass)
-  GuardTet* trec;  // tcap records
-  int* tcount;
-  int tcap;
   const double* w64;            // FP64 SPR weights in patch-CSR order
   const unsigned char* listed;  // patches on the FP64 reference path
   const double* rec_ref;        // their FP64 reference results (V x 3)
   const double2* geo64;         // per element {det J, h_max} in FP64
 };
-// unresolved[0]: edges left to the FP32 decision, unresolved[1]: failed fits.
-// Four stages in order: 0 collect vertices, 1 element gradients, 2 fits,
-// 3 decide.
+// unresolved[0]: edges left to the FP32 decision.  Three stages in order:
+// 0 collect vertices, 1 fits, 2 decide.
+constexpr int kGuardStages = 3;
 void launch_guard_stage(int stage, const DevMesh& m, const double* u, const double* out3, const int* items,
                         const int* count, int cap, uint32_t* split, uint32_t* collapse, int* unresolved,
                         GuardScratch g, BatchView bv, cudaStream_t s);

@@ -284,12 +284,22 @@ __device__ __forceinline__ void rdiff(const float4& ah, const float4& al, const 
   dl.w = (al.w - bl.w) + e;
 }
 
+// one vertex record (32 bytes, hi then lo) with a single 256-bit load: a
+// warp's gather then asks L1 for one sector per lane instead of two.  The
+// records start at a cudaMalloc base (256-byte aligned), 32 bytes each.
+__device__ __forceinline__ void ld_record(const float4* p, float4& h, float4& l) {
+  asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+      : "=f"(h.x), "=f"(h.y), "=f"(h.z), "=f"(h.w), "=f"(l.x), "=f"(l.y), "=f"(l.z), "=f"(l.w)
+      : "l"(p));
+}
+
 __device__ __forceinline__ TetData load_tet(const float4* __restrict__ vr, int4 tv) {
   TetData d;
-  const float4 h0 = ld4(vr + 2 * (size_t)tv.x), l0 = ld4(vr + 2 * (size_t)tv.x + 1);
-  const float4 h1 = ld4(vr + 2 * (size_t)tv.y), l1 = ld4(vr + 2 * (size_t)tv.y + 1);
-  const float4 h2 = ld4(vr + 2 * (size_t)tv.z), l2 = ld4(vr + 2 * (size_t)tv.z + 1);
-  const float4 h3 = ld4(vr + 2 * (size_t)tv.w), l3 = ld4(vr + 2 * (size_t)tv.w + 1);
+  float4 h0, l0, h1, l1, h2, l2, h3, l3;
+  ld_record(vr + 2 * (size_t)tv.x, h0, l0);
+  ld_record(vr + 2 * (size_t)tv.y, h1, l1);
+  ld_record(vr + 2 * (size_t)tv.z, h2, l2);
+  ld_record(vr + 2 * (size_t)tv.w, h3, l3);
   rdiff(h1, l1, h0, l0, d.eh[0], d.el[0]);
   rdiff(h2, l2, h0, l0, d.eh[1], d.el[1]);
   rdiff(h3, l3, h0, l0, d.eh[2], d.el[2]);
@@ -299,41 +309,50 @@ __device__ __forceinline__ TetData load_tet(const float4* __restrict__ vr, int4 
 // ---------------------------------------------------------------------------
 // tet: gradient value and packed correction
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kBlock, 5) k_fast_tet(DevMesh m, const float4* __restrict__ vr, float gscale,
+// One wave of resident blocks strides over the elements; each thread loads
+// the next element's vertex ids before working on the current one, so only
+// the record gathers (mostly L2 hits) stay on the dependent chain.  (With
+// the prefetched ids the kernel needs 64 registers: 4 blocks per SM.)
+__global__ void __launch_bounds__(kBlock, 4) k_fast_tet(DevMesh m, const float4* __restrict__ vr, float gscale,
                                                         uint4* __restrict__ td) {
+  const int4* __restrict__ ev4 = reinterpret_cast<const int4*>(m.ev);
+  const int stride = gridDim.x * blockDim.x;
   int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= m.T) return;
-  int4 tv = __ldg(reinterpret_cast<const int4*>(m.ev) + t);
-  TetData d = load_tet(vr, tv);
-  // first estimate with an approximate inverse of the rounded edge matrix
-  // (hi + lo: the high words alone, exact differences of [1, 2] values, are
-  // off by up to 2^-23 absolute, which squared through the correction would
-  // exceed the accuracy the error bound assumes); the correction
-  // J^{-1}(du - J g) with the compensated residual makes the result accurate
-  // to second order in both approximations
-  Cof cf;
-  {
-    float4 er[3];
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-      er[i] = make_float4(d.eh[i].x + d.el[i].x, d.eh[i].y + d.el[i].y, d.eh[i].z + d.el[i].z, 0.f);
-    cf = cofactors(er[0], er[1], er[2]);
+  int4 next = t < m.T ? __ldg(ev4 + t) : make_int4(0, 0, 0, 0);
+  for (; t < m.T; t += stride) {
+    const int4 tv = next;
+    if (t + stride < m.T) next = __ldg(ev4 + t + stride);
+    TetData d = load_tet(vr, tv);
+    // first estimate with an approximate inverse of the rounded edge matrix
+    // (hi + lo: the high words alone, exact differences of [1, 2] values, are
+    // off by up to 2^-23 absolute, which squared through the correction would
+    // exceed the accuracy the error bound assumes); the correction
+    // J^{-1}(du - J g) with the compensated residual makes the result accurate
+    // to second order in both approximations
+    Cof cf;
+    {
+      float4 er[3];
+  #pragma unroll
+      for (int i = 0; i < 3; ++i)
+        er[i] = make_float4(d.eh[i].x + d.el[i].x, d.eh[i].y + d.el[i].y, d.eh[i].z + d.el[i].z, 0.f);
+      cf = cofactors(er[0], er[1], er[2]);
+    }
+    float g[3], c[3], s[3], r[3];
+    apply_inv(cf, d.eh[0].w, d.eh[1].w, d.eh[2].w, g);
+    apply_inv(cf, comp_residual(d.eh[0], d.el[0], g[0], g[1], g[2]), comp_residual(d.eh[1], d.el[1], g[0], g[1], g[2]),
+              comp_residual(d.eh[2], d.el[2], g[0], g[1], g[2]), c);
+    // s + r = g + c exactly (|c| << |g|: Fast2Sum)
+  #pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      s[j] = g[j] + c[j];
+      r[j] = c[j] - (s[j] - g[j]);
+    }
+    // back to the mesh's coordinates: the correction word is relative to the
+    // largest |s_j|, so scaling s by a power of two scales r with it
+    const uint32_t corr = pack_corr(s[0], s[1], s[2], r[0], r[1], r[2]);
+    td[t] = make_uint4(__float_as_uint(s[0] * gscale), __float_as_uint(s[1] * gscale),
+                       __float_as_uint(s[2] * gscale), corr);
   }
-  float g[3], c[3], s[3], r[3];
-  apply_inv(cf, d.eh[0].w, d.eh[1].w, d.eh[2].w, g);
-  apply_inv(cf, comp_residual(d.eh[0], d.el[0], g[0], g[1], g[2]), comp_residual(d.eh[1], d.el[1], g[0], g[1], g[2]),
-            comp_residual(d.eh[2], d.el[2], g[0], g[1], g[2]), c);
-  // s + r = g + c exactly (|c| << |g|: Fast2Sum)
-#pragma unroll
-  for (int j = 0; j < 3; ++j) {
-    s[j] = g[j] + c[j];
-    r[j] = c[j] - (s[j] - g[j]);
-  }
-  // back to the mesh's coordinates: the correction word is relative to the
-  // largest |s_j|, so scaling s by a power of two scales r with it
-  const uint32_t corr = pack_corr(s[0], s[1], s[2], r[0], r[1], r[2]);
-  td[t] = make_uint4(__float_as_uint(s[0] * gscale), __float_as_uint(s[1] * gscale),
-                     __float_as_uint(s[2] * gscale), corr);
 }
 
 // ---------------------------------------------------------------------------
@@ -579,11 +598,26 @@ __global__ void __launch_bounds__(kBlock) k_fast_error(DevMesh m, const uint4* _
     t_end = r.y;
     t_step = blockDim.x;
   }
+  // the next element's ids, gradient and geometry are loaded one iteration
+  // ahead: only the recovered-value gathers stay on the dependent chain
+  int4 ntv = make_int4(0, 0, 0, 0);
+  uint4 nta = make_uint4(0, 0, 0, 0);
+  float2 ngm = make_float2(0.f, 0.f);
+  if (t_beg < t_end) {
+    ntv = __ldg(reinterpret_cast<const int4*>(m.ev) + t_beg);
+    nta = __ldg(td + t_beg);
+    ngm = __ldg(geo + t_beg);
+  }
   for (int t = t_beg; t < t_end; t += t_step) {
     {
-      const int4 tv = __ldg(reinterpret_cast<const int4*>(m.ev) + t);
-      const uint4 ta = __ldg(td + t);
-      const float2 gm = __ldg(geo + t);
+      const int4 tv = ntv;
+      const uint4 ta = nta;
+      const float2 gm = ngm;
+      if (t + t_step < t_end) {
+        ntv = __ldg(reinterpret_cast<const int4*>(m.ev) + t + t_step);
+        nta = __ldg(td + t + t_step);
+        ngm = __ldg(geo + t + t_step);
+      }
       const uint4 R0 = __ldg(rec + tv.x), R1 = __ldg(rec + tv.y), R2 = __ldg(rec + tv.z), R3 = __ldg(rec + tv.w);
       Grad ga = unpack_grad(ta);
       const Grad E0 = unpack_grad(R0), E1 = unpack_grad(R1), E2 = unpack_grad(R2), E3 = unpack_grad(R3);
@@ -796,6 +830,20 @@ int error_grid() {
   return grid;
 }
 
+// the tet kernel runs one full wave as well
+int tet_grid(int T) {
+  static int grid = 0;
+  if (!grid) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fast_tet, kBlock, 0);
+    grid = (sms > 0 ? sms : 152) * (per_sm > 0 ? per_sm : 5);
+  }
+  const int nb = nblk(T);
+  return nb < grid ? nb : grid;
+}
+
 }  // namespace
 
 int fast_error_blocks(int T) {
@@ -817,7 +865,7 @@ void fast_prep(const DevMesh& m, const double* u, const float4* crec, float4* vr
 }
 
 void fast_tet(const DevMesh& m, const float4* vrec, float gscale, uint4* td, cudaStream_t s) {
-  if (m.T) k_fast_tet<<<nblk(m.T), kBlock, 0, s>>>(m, vrec, gscale, td);
+  if (m.T) k_fast_tet<<<tet_grid(m.T), kBlock, 0, s>>>(m, vrec, gscale, td);
 }
 
 void fast_weights(const DevMesh& m, float* w, double* w64, ExpandList xl, int* n_refit, unsigned char* listed,

@@ -238,17 +238,8 @@ __device__ __forceinline__ void recover_vertex_warp(const DevMesh& m, const doub
   }
 }
 
-template <int NT, int NC, int RPL>
-__global__ void __launch_bounds__(kBlock) k_recover(DevMesh m, const double* __restrict__ ip,
-                                                    double* __restrict__ rec, ExpandList xl) {
-  const int lane = threadIdx.x & 31;
-  const int v = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
-  if (v >= m.V) return;
-  recover_vertex_warp<NT, NC, RPL>(m, ip, rec, xl, v, lane);
-}
-
-// the warp path over a vertex list (the patches too large for the thread
-// path); a fixed grid of warps strides over the device-side count
+// the warp path over a vertex list (the triangle patches too large for the
+// thread path); a fixed grid of warps strides over the device-side count
 template <int NT, int NC, int RPL>
 __global__ void __launch_bounds__(kBlock) k_recover_list(DevMesh m, const double* __restrict__ ip,
                                                          double* __restrict__ rec, ExpandList xl, ExpandList list) {
@@ -867,6 +858,40 @@ __global__ void __launch_bounds__(kBlock) k_apply_bits(int E, const uint32_t* __
   if ((threadIdx.x & 31) == 0 && b) atomicAdd(count, (unsigned long long)__popc(b));
 }
 
+// both marking passes over one read and one write of the flag words: per
+// edge the collapse rule, then the split rule (they test and set disjoint
+// bits, so the result equals the two passes in turn); counts[0] split,
+// counts[1] collapse
+__global__ void __launch_bounds__(kBlock) k_apply_marks(int E, const uint32_t* __restrict__ split_bits,
+                                                        const uint32_t* __restrict__ collapse_bits,
+                                                        int* __restrict__ flags, unsigned long long* counts,
+                                                        DevStatus* st) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  int ms = 0, mc = 0;
+  if (e < E) {
+    const int f0 = flags[e];
+    int f = f0;
+    if (f & SPRG_COLLAPSE) {
+      set_status(st, SPRG_EFLAGS, e);
+    } else if (!((SPRG_DONT_COLLAPSE | SPRG_NEED_NOT_COLLAPSE) & f)) {
+      if ((collapse_bits[e >> 5] >> (e & 31)) & 1u) { f |= SPRG_COLLAPSE; mc = 1; }
+      else f |= SPRG_NEED_NOT_COLLAPSE;
+    }
+    if (f & SPRG_SPLIT) {
+      set_status(st, SPRG_EFLAGS, e);
+    } else if (!((SPRG_DONT_SPLIT | SPRG_NEED_NOT_SPLIT) & f)) {
+      if ((split_bits[e >> 5] >> (e & 31)) & 1u) { f |= SPRG_SPLIT; ms = 1; }
+      else f |= SPRG_NEED_NOT_SPLIT;
+    }
+    if (f != f0) flags[e] = f;
+  }
+  const unsigned bs = __ballot_sync(0xffffffffu, ms), bc = __ballot_sync(0xffffffffu, mc);
+  if ((threadIdx.x & 31) == 0) {
+    if (bs) atomicAdd(counts, (unsigned long long)__popc(bs));
+    if (bc) atomicAdd(counts + 1, (unsigned long long)__popc(bc));
+  }
+}
+
 // measureTetQuality / measureTriQuality, useMax = true (ma/maQuality.cc:83-167)
 __device__ __forceinline__ double q_measure(const V3* x, int nn, int edim, const M3& Q) {
   M3 J = ref::jacobian(x, nn, edim);
@@ -939,10 +964,11 @@ __global__ void __launch_bounds__(kBlock) k_quality(DevMesh m, const double* __r
 // ---------------------------------------------------------------------
 constexpr int kGuardMaxTets = 96;  // elements around one end vertex
 
-// FP64 gradient of the scalar field and integration point of tet t
-// (cofactor inverse; FP64 accuracy, not the reference's rounding)
-__device__ __forceinline__ void tet_grad_ip_f64(const DevMesh& m, int t, const double* __restrict__ u, double* g,
-                                                double* p) {
+// FP64 gradient of the scalar field on tet t (cofactor inverse; FP64
+// accuracy, not the reference's rounding).  Every guard kernel that needs an
+// element's gradient evaluates it with this function, so all of them see the
+// same bits.
+__device__ __forceinline__ void tet_grad_f64(const DevMesh& m, int t, const double* __restrict__ u, double* g) {
   const int* ev = m.ev + (size_t)t * 4;
   V3 x0 = load_xyz(m.xyz, ev[0]), x1 = load_xyz(m.xyz, ev[1]), x2 = load_xyz(m.xyz, ev[2]),
      x3 = load_xyz(m.xyz, ev[3]);
@@ -951,24 +977,22 @@ __device__ __forceinline__ void tet_grad_ip_f64(const DevMesh& m, int t, const d
   double d1 = u[ev[1]] - u0, d2 = u[ev[2]] - u0, d3 = u[ev[3]] - u0;
   V3 c1 = ref::cross(e2, e3), c2 = ref::cross(e3, e1), c3 = ref::cross(e1, e2);
   double inv = 1.0 / ref::dot(e1, c1);
-  for (int k = 0; k < 3; ++k) {
-    g[k] = (c1.v[k] * d1 + c2.v[k] * d2 + c3.v[k] * d3) * inv;
-    p[k] = 0.25 * (((x0.v[k] + x1.v[k]) + x2.v[k]) + x3.v[k]);
-  }
+  for (int k = 0; k < 3; ++k) g[k] = (c1.v[k] * d1 + c2.v[k] * d2 + c3.v[k] * d3) * inv;
 }
 
-// Guard pipeline, four kernels over all listed edges at once:
+// Guard pipeline, three kernels over all listed edges at once:
 //   collect  thread per (edge, end, element around the end): the distinct
 //            vertices of those elements (a per-vertex stamp de-duplicates
 //            across edges)
-//   tets     thread per (collected vertex, element of its patch): one FP64
-//            record per distinct element (gradient, integration point,
-//            det J, h_max), so each element is evaluated once
-//   fit      thread per collected vertex: FP64 normal equations of its patch
-//            from the records, Cholesky, the recovered value
+//   fit      warp per collected vertex, lanes over its patch: the FP64
+//            element gradients, weighted with the per-mesh FP64 SPR weights
+//            (fixed reduction tree), the recovered value
 //   decide   warp per edge: FP64 element errors and sizes around both ends,
 //            the vertex averages in adjacency order, the metric length, the
 //            edge's split/collapse bits
+// An element shared by several collected patches has its gradient evaluated
+// once per patch: a few thousand extra FP64 gradients per pass cost less
+// than a de-duplication stage and its per-element scratch.
 // a slot for every winning lane of the warp from one atomic on the shared
 // counter (all 32 lanes call it)
 __device__ __forceinline__ int warp_slot(bool win, int* counter) {
@@ -1012,47 +1036,11 @@ __global__ void k_guard_collect(DevMesh m, const int* __restrict__ items, const 
   }
 }
 
-__global__ void k_guard_tets(DevMesh m, const double* __restrict__ u, const int* __restrict__ fit_items,
-                             const int* __restrict__ fit_count, int fit_cap, GuardScratch g) {
-  // warp per collected vertex: lanes over its patch in rounds of 32
-  const int n = min(*fit_count, fit_cap);
-  const long total = (long)n * 32;
-  const int lane = threadIdx.x & 31;
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
-    const int w = fit_items[i >> 5];
-    if (g.listed[w]) continue;
-    const int b = m.p_off[w], cnt = min(m.p_off[w + 1] - b, kGuardMaxTets);
-    for (int r = 0; r < cnt; r += 32) {
-      const int j = r + lane;
-      const int t = j < cnt ? m.p_el[b + j] : 0;
-      const bool win = j < cnt && atomicExch(&g.tstamp[t], g.stamp_id) != g.stamp_id;
-      const int slot = warp_slot(win, g.tcount);
-      if (!win) continue;
-      if (slot >= g.tcap) {
-        g.tslot[t] = -1;
-        continue;
-      }
-      GuardTet rt;
-      double p[3];
-      tet_grad_ip_f64(m, t, u, rt.g, p);
-      g.trec[slot] = rt;
-      g.tslot[t] = slot;
-    }
-  }
-}
-
-// the element's record, or null when it was not evaluated this pass
-__device__ __forceinline__ const GuardTet* guard_rec(const GuardScratch& g, int t) {
-  if (g.tstamp[t] != g.stamp_id) return nullptr;
-  const int slot = g.tslot[t];
-  return slot < 0 ? nullptr : g.trec + slot;
-}
-
 // eps*(w) = sum_t w_wt eps_t with the per-mesh FP64 SPR weights, warp per
 // collected vertex (lanes over the patch, fixed reduction tree); listed
 // patches take their FP64 reference (QR, grown patch) result
-__global__ void k_guard_fit(DevMesh m, const int* __restrict__ fit_items, const int* __restrict__ fit_count,
-                            int fit_cap, GuardScratch g, int* __restrict__ fit_bad) {
+__global__ void k_guard_fit(DevMesh m, const double* __restrict__ u, const int* __restrict__ fit_items,
+                            const int* __restrict__ fit_count, int fit_cap, GuardScratch g) {
   const int n = min(*fit_count, fit_cap);
   const int lane = threadIdx.x & 31;
   const int nwarps = gridDim.x * (blockDim.x >> 5);
@@ -1064,33 +1052,23 @@ __global__ void k_guard_fit(DevMesh m, const int* __restrict__ fit_items, const 
     }
     const int beg = m.p_off[w], cnt = m.p_off[w + 1] - beg;
     double r0 = 0, r1 = 0, r2 = 0;
-    bool ok = cnt <= kGuardMaxTets;
-    for (int k = lane; ok && k < cnt; k += 32) {
-      const GuardTet* rt = guard_rec(g, m.p_el[beg + k]);
-      if (!rt) {
-        ok = false;
-        break;
-      }
+    for (int k = lane; k < cnt; k += 32) {
+      double gt[3];
+      tet_grad_f64(m, m.p_el[beg + k], u, gt);
       const double wk = g.w64[beg + k];
-      r0 += wk * rt->g[0];
-      r1 += wk * rt->g[1];
-      r2 += wk * rt->g[2];
+      r0 += wk * gt[0];
+      r1 += wk * gt[1];
+      r2 += wk * gt[2];
     }
-    ok = __all_sync(0xffffffffu, ok);
     for (int o = 16; o > 0; o >>= 1) {
       r0 += __shfl_xor_sync(0xffffffffu, r0, o);
       r1 += __shfl_xor_sync(0xffffffffu, r1, o);
       r2 += __shfl_xor_sync(0xffffffffu, r2, o);
     }
     if (lane == 0) {
-      if (!ok) {
-        g.rec64[3 * (size_t)w] = NAN;  // the deciding edges stay with the FP32 result
-        atomicAdd(fit_bad, 1);
-      } else {
-        g.rec64[3 * (size_t)w] = r0;
-        g.rec64[3 * (size_t)w + 1] = r1;
-        g.rec64[3 * (size_t)w + 2] = r2;
-      }
+      g.rec64[3 * (size_t)w] = r0;
+      g.rec64[3 * (size_t)w + 1] = r1;
+      g.rec64[3 * (size_t)w + 2] = r2;
     }
   }
 }
@@ -1114,13 +1092,8 @@ __global__ void __launch_bounds__(128) k_guard_decide(DevMesh m, const double* _
         for (int i = lane; i < cnt[s]; i += 32) {
           const int t = m.a_el[m.a_off[ab[s]] + i];
           const int* ev = m.ev + 4 * (size_t)t;
-          double gt[3], p[3];
-          const GuardTet* rt = guard_rec(g, t);
-          if (rt) {
-            for (int c = 0; c < 3; ++c) gt[c] = rt->g[c];
-          } else {
-            tet_grad_ip_f64(m, t, u, gt, p);  // an element of listed patches only
-          }
+          double gt[3];
+          tet_grad_f64(m, t, u, gt);
           double v2[3] = {0, 0, 0};
           for (int k = 0; k < 4; ++k)
             for (int c = 0; c < 3; ++c) v2[c] += g.rec64[3 * (size_t)ev[k] + c] * 0.25;
@@ -1137,7 +1110,7 @@ __global__ void __launch_bounds__(128) k_guard_decide(DevMesh m, const double* _
         for (int i = 0; i < cnt[s]; ++i) sz[s] += esz[warp][s][i];
         sz[s] /= (double)cnt[s];
       }
-      if (bad || !(sz[0] == sz[0]) || !(sz[1] == sz[1])) {  // a fit failed (NaN) or too many elements
+      if (bad || !(sz[0] == sz[0]) || !(sz[1] == sz[1])) {  // too many elements, or a NaN size
         atomicAdd(unresolved, 1);
       } else {
         double hv[6] = {sz[0], sz[0], sz[0], sz[1], sz[1], sz[1]}, Rv[18];
@@ -2110,25 +2083,17 @@ void launch_grad_ip_f64(const DevMesh& m, const double* f, int ncin, double* ip,
 void launch_recover_f64(const DevMesh& m, const double* ip, int nc, double* rec, ExpandList xl, ExpandList big,
                         DevStatus* st, cudaStream_t s) {
   (void)st;
-  if (!m.V) return;
-  if (m.dim == 3) {
-    // one row per lane: patches of up to 32 elements (every interior patch of
-    // a structured tet mesh); larger ones take the slab path
-    int grid = nblk((long)m.V * 32);
-    if (nc == 3) k_recover<4, 3, 1><<<grid, kBlock, 0, s>>>(m, ip, rec, xl);
-    else k_recover<4, 9, 1><<<grid, kBlock, 0, s>>>(m, ip, rec, xl);
+  if (!m.V || m.dim != 2) return;  // tets recover through the per-mesh QR weights
+  // triangles: a thread per vertex up to kTriThreadRows patch elements, then
+  // the warp path over the vertices it listed
+  const int grid = (m.V + 127) / 128;
+  const int lgrid = 152 * 8;
+  if (nc == 3) {
+    k_recover_tri<3, kTriThreadRows><<<grid, 128, 0, s>>>(m, ip, rec, xl, big);
+    k_recover_list<3, 3, 1><<<lgrid, kBlock, 0, s>>>(m, ip, rec, xl, big);
   } else {
-    // triangles: a thread per vertex up to kTriThreadRows patch elements,
-    // then the warp path over the vertices it listed
-    const int grid = (m.V + 127) / 128;
-    const int lgrid = 152 * 8;
-    if (nc == 3) {
-      k_recover_tri<3, kTriThreadRows><<<grid, 128, 0, s>>>(m, ip, rec, xl, big);
-      k_recover_list<3, 3, 1><<<lgrid, kBlock, 0, s>>>(m, ip, rec, xl, big);
-    } else {
-      k_recover_tri<9, kTriThreadRows><<<grid, 128, 0, s>>>(m, ip, rec, xl, big);
-      k_recover_list<3, 9, 1><<<lgrid, kBlock, 0, s>>>(m, ip, rec, xl, big);
-    }
+    k_recover_tri<9, kTriThreadRows><<<grid, 128, 0, s>>>(m, ip, rec, xl, big);
+    k_recover_list<3, 9, 1><<<lgrid, kBlock, 0, s>>>(m, ip, rec, xl, big);
   }
 }
 
@@ -2199,6 +2164,11 @@ void launch_apply_bits(int E, const uint32_t* bits, int which, int* flags, unsig
   if (E) k_apply_bits<<<nblk(E), kBlock, 0, s>>>(E, bits, which, flags, count, st);
 }
 
+void launch_apply_marks(int E, const uint32_t* split_bits, const uint32_t* collapse_bits, int* flags,
+                        unsigned long long* counts, DevStatus* st, cudaStream_t s) {
+  if (E) k_apply_marks<<<nblk(E), kBlock, 0, s>>>(E, split_bits, collapse_bits, flags, counts, st);
+}
+
 void launch_quality_f64(const DevMesh& m, const double* size, const double* sizes, const double* frames, double* q,
                         cudaStream_t s, const double* logm, DevStatus* st) {
   if (!m.T) return;
@@ -2212,15 +2182,11 @@ void launch_guard_stage(int stage, const DevMesh& m, const double* u, const doub
   switch (stage) {
     case 0:
       cudaMemsetAsync(g.fit_count, 0, sizeof(int), s);
-      cudaMemsetAsync(g.tcount, 0, sizeof(int), s);
       k_guard_collect<<<152 * 4, 256, 0, s>>>(m, items, count, cap, g.stamp_id, g.stamp, g.fit_items, g.fit_count,
                                           g.fit_cap, unresolved);
       break;
     case 1:
-      k_guard_tets<<<152 * 8, 256, 0, s>>>(m, u, g.fit_items, g.fit_count, g.fit_cap, g);
-      break;
-    case 2:
-      k_guard_fit<<<152 * 8, 256, 0, s>>>(m, g.fit_items, g.fit_count, g.fit_cap, g, unresolved + 1);
+      k_guard_fit<<<152 * 8, 256, 0, s>>>(m, u, g.fit_items, g.fit_count, g.fit_cap, g);
       break;
     default:
       k_guard_decide<<<152 * 2, 128, 0, s>>>(m, u, out3, g, items, count, cap, split, collapse, unresolved, bv);
