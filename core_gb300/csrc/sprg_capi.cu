@@ -1608,7 +1608,9 @@ int sprg_estimate_and_mark(sprg_ctx* c, const double* u, double adapt_ratio, dou
     CK(cudaEventCreateWithFlags(&c->size_ready, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&c->size_join, cudaEventDisableTiming));
   }
+  PB("upload_field");
   CK(cudaMemcpyAsync(c->f.p, u, sizeof(double) * (size_t)m.V, cudaMemcpyHostToDevice, c->stream));
+  PE();
   // the flag words are needed only by the write-back at the end: their
   // upload runs on the copy stream beside the pass, after the field's upload
   // (which then has the link to itself) and this stream's earlier work
@@ -1642,12 +1644,18 @@ int sprg_estimate_and_mark(sprg_ctx* c, const double* u, double adapt_ratio, dou
     c->size_valid = true;
   }
   if (flags) CK(cudaStreamWaitEvent(c->stream, c->copy_join, 0));
+  PB("apply_marks");
   CK(cudaMemsetAsync(c->mcount.p, 0, 2 * sizeof(unsigned long long), c->stream));
   launch_apply_marks(m.E, sb, sb + nw, P<int>(c->flags), P<unsigned long long>(c->mcount), P<DevStatus>(c->status),
                      c->stream);
+  PE();
   c->launches += 1;
   if ((rc = check_launch(c, "apply marks"))) return rc;
-  if (flags) CK(cudaMemcpyAsync(flags, c->flags.p, sizeof(int) * (size_t)m.E, cudaMemcpyDeviceToHost, c->stream));
+  if (flags) {
+    PB("download_flags");
+    CK(cudaMemcpyAsync(flags, c->flags.p, sizeof(int) * (size_t)m.E, cudaMemcpyDeviceToHost, c->stream));
+    PE();
+  }
   if (!early_size) {
     if (c->precision == SPRG_FP32) {
       ENSURE(c->size, sizeof(double) * (size_t)m.V);
@@ -1665,8 +1673,10 @@ int sprg_estimate_and_mark(sprg_ctx* c, const double* u, double adapt_ratio, dou
   } else {
     CK(cudaStreamWaitEvent(c->stream, c->size_join, 0));
   }
+  PB("readback");
   CK(cudaMemcpyAsync(c->stage->counts, c->mcount.p, sizeof c->stage->counts, cudaMemcpyDeviceToHost, c->stream));
   if ((rc = enqueue_info(c))) return rc;
+  PE();
   if ((rc = sync_and_status(c))) return rc;
   if (n_split) *n_split = (long)c->stage->counts[0];
   if (n_collapse) *n_collapse = (long)c->stage->counts[1];

@@ -793,29 +793,53 @@ __global__ void __launch_bounds__(kBlock) k_measure_aniso(DevMesh m, const doubl
   L[e] = metric_length(load_xyz(m.xyz, vv[0]), load_xyz(m.xyz, vv[1]), hv, Rv);
 }
 
+// Counting sweeps over entities stride over one wave of blocks and add their
+// count with one atomic per block: a per-warp atomic on the one counter
+// serialises (about a million same-address atomics per 28.9M-edge sweep).
+constexpr int kCountGrid = 152 * 32;  // a wave deep enough for 4-byte accesses
+__device__ __forceinline__ void block_count2(unsigned long long* dst0, unsigned a, unsigned long long* dst1,
+                                             unsigned b) {
+  __shared__ unsigned tot[2][kBlock / 32];
+  a = __reduce_add_sync(0xffffffffu, a);
+  b = __reduce_add_sync(0xffffffffu, b);
+  if ((threadIdx.x & 31) == 0) {
+    tot[0][threadIdx.x >> 5] = a;
+    tot[1][threadIdx.x >> 5] = b;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long ta = 0, tb = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      ta += tot[0][w];
+      tb += tot[1][w];
+    }
+    if (ta) atomicAdd(dst0, ta);
+    if (dst1 && tb) atomicAdd(dst1, tb);
+  }
+}
+
+
 // ma::markEntities (ma/maAdapt.cc:293-324)
 __global__ void __launch_bounds__(kBlock) k_mark(int E, const double* __restrict__ L, int which,
                                                  int* __restrict__ flags, unsigned long long* count,
                                                  DevStatus* st) {
-  int e = blockIdx.x * blockDim.x + threadIdx.x;
   int trueFlag = which == 0 ? SPRG_SPLIT : SPRG_COLLAPSE;
   int setFalse = which == 0 ? SPRG_NEED_NOT_SPLIT : SPRG_NEED_NOT_COLLAPSE;
   int allFalse = which == 0 ? (SPRG_DONT_SPLIT | SPRG_NEED_NOT_SPLIT) : (SPRG_DONT_COLLAPSE | SPRG_NEED_NOT_COLLAPSE);
-  int marked = 0;
-  if (e < E) {
+  unsigned marked = 0;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < E; e += gridDim.x * blockDim.x) {
     int f = flags[e];
     if (f & trueFlag) {
       set_status(st, SPRG_EFLAGS, e);
     } else if (!(allFalse & f)) {
       double l = L[e];
       bool pred = which == 0 ? (l > 1.5) : (l < .5);
-      if (pred) { f |= trueFlag; marked = 1; }
+      if (pred) { f |= trueFlag; ++marked; }
       else f |= setFalse;
       flags[e] = f;
     }
   }
-  unsigned b = __ballot_sync(0xffffffffu, marked);
-  if ((threadIdx.x & 31) == 0 && b) atomicAdd(count, (unsigned long long)__popc(b));
+  block_count2(count, marked, nullptr, 0);
 }
 
 // ShouldSplit / ShouldCollapse predicates as the device edge-mark bitmap
@@ -839,57 +863,71 @@ __global__ void __launch_bounds__(kBlock) k_mark_bits(int E, const double* __res
 __global__ void __launch_bounds__(kBlock) k_apply_bits(int E, const uint32_t* __restrict__ bits, int which,
                                                        int* __restrict__ flags, unsigned long long* count,
                                                        DevStatus* st) {
-  int e = blockIdx.x * blockDim.x + threadIdx.x;
   int trueFlag = which == 0 ? SPRG_SPLIT : SPRG_COLLAPSE;
   int setFalse = which == 0 ? SPRG_NEED_NOT_SPLIT : SPRG_NEED_NOT_COLLAPSE;
   int allFalse = which == 0 ? (SPRG_DONT_SPLIT | SPRG_NEED_NOT_SPLIT) : (SPRG_DONT_COLLAPSE | SPRG_NEED_NOT_COLLAPSE);
-  int marked = 0;
-  if (e < E) {
+  unsigned marked = 0;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < E; e += gridDim.x * blockDim.x) {
     int f = flags[e];
     if (f & trueFlag) {
       set_status(st, SPRG_EFLAGS, e);
     } else if (!(allFalse & f)) {
-      if ((bits[e >> 5] >> (e & 31)) & 1u) { f |= trueFlag; marked = 1; }
+      if ((bits[e >> 5] >> (e & 31)) & 1u) { f |= trueFlag; ++marked; }
       else f |= setFalse;
       flags[e] = f;
     }
   }
-  unsigned b = __ballot_sync(0xffffffffu, marked);
-  if ((threadIdx.x & 31) == 0 && b) atomicAdd(count, (unsigned long long)__popc(b));
+  block_count2(count, marked, nullptr, 0);
 }
 
 // both marking passes over one read and one write of the flag words: per
 // edge the collapse rule, then the split rule (they test and set disjoint
 // bits, so the result equals the two passes in turn); counts[0] split,
-// counts[1] collapse
+// counts[1] collapse.  Four flag words per thread and step (one 16-byte
+// access; their four bits sit in one bitmap word).
+__device__ __forceinline__ int apply_marks_edge(int f, uint32_t split_bit, uint32_t collapse_bit, int e,
+                                                unsigned& ms, unsigned& mc, DevStatus* st) {
+  if (f & SPRG_COLLAPSE) {
+    set_status(st, SPRG_EFLAGS, e);
+  } else if (!((SPRG_DONT_COLLAPSE | SPRG_NEED_NOT_COLLAPSE) & f)) {
+    if (collapse_bit) { f |= SPRG_COLLAPSE; ++mc; }
+    else f |= SPRG_NEED_NOT_COLLAPSE;
+  }
+  if (f & SPRG_SPLIT) {
+    set_status(st, SPRG_EFLAGS, e);
+  } else if (!((SPRG_DONT_SPLIT | SPRG_NEED_NOT_SPLIT) & f)) {
+    if (split_bit) { f |= SPRG_SPLIT; ++ms; }
+    else f |= SPRG_NEED_NOT_SPLIT;
+  }
+  return f;
+}
+
 __global__ void __launch_bounds__(kBlock) k_apply_marks(int E, const uint32_t* __restrict__ split_bits,
                                                         const uint32_t* __restrict__ collapse_bits,
                                                         int* __restrict__ flags, unsigned long long* counts,
                                                         DevStatus* st) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  int ms = 0, mc = 0;
-  if (e < E) {
-    const int f0 = flags[e];
-    int f = f0;
-    if (f & SPRG_COLLAPSE) {
-      set_status(st, SPRG_EFLAGS, e);
-    } else if (!((SPRG_DONT_COLLAPSE | SPRG_NEED_NOT_COLLAPSE) & f)) {
-      if ((collapse_bits[e >> 5] >> (e & 31)) & 1u) { f |= SPRG_COLLAPSE; mc = 1; }
-      else f |= SPRG_NEED_NOT_COLLAPSE;
-    }
-    if (f & SPRG_SPLIT) {
-      set_status(st, SPRG_EFLAGS, e);
-    } else if (!((SPRG_DONT_SPLIT | SPRG_NEED_NOT_SPLIT) & f)) {
-      if ((split_bits[e >> 5] >> (e & 31)) & 1u) { f |= SPRG_SPLIT; ms = 1; }
-      else f |= SPRG_NEED_NOT_SPLIT;
-    }
-    if (f != f0) flags[e] = f;
+  unsigned ms = 0, mc = 0;
+  const int n4 = E >> 2, step = gridDim.x * blockDim.x;
+  int4* __restrict__ f4 = reinterpret_cast<int4*>(flags);
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < n4; g += step) {
+    const int4 v = f4[g];
+    const int e0 = g << 2;
+    const uint32_t sw = __ldg(split_bits + (e0 >> 5)) >> (e0 & 31);
+    const uint32_t cw = __ldg(collapse_bits + (e0 >> 5)) >> (e0 & 31);
+    int4 w;
+    w.x = apply_marks_edge(v.x, sw & 1u, cw & 1u, e0, ms, mc, st);
+    w.y = apply_marks_edge(v.y, (sw >> 1) & 1u, (cw >> 1) & 1u, e0 + 1, ms, mc, st);
+    w.z = apply_marks_edge(v.z, (sw >> 2) & 1u, (cw >> 2) & 1u, e0 + 2, ms, mc, st);
+    w.w = apply_marks_edge(v.w, (sw >> 3) & 1u, (cw >> 3) & 1u, e0 + 3, ms, mc, st);
+    if (w.x != v.x || w.y != v.y || w.z != v.z || w.w != v.w) f4[g] = w;
   }
-  const unsigned bs = __ballot_sync(0xffffffffu, ms), bc = __ballot_sync(0xffffffffu, mc);
-  if ((threadIdx.x & 31) == 0) {
-    if (bs) atomicAdd(counts, (unsigned long long)__popc(bs));
-    if (bc) atomicAdd(counts + 1, (unsigned long long)__popc(bc));
+  for (int e = (n4 << 2) + blockIdx.x * blockDim.x + threadIdx.x; e < E; e += step) {
+    const int f = flags[e];
+    const int w = apply_marks_edge(f, (split_bits[e >> 5] >> (e & 31)) & 1u, (collapse_bits[e >> 5] >> (e & 31)) & 1u,
+                                   e, ms, mc, st);
+    if (w != f) flags[e] = w;
   }
+  block_count2(counts, ms, counts + 1, mc);
 }
 
 // measureTetQuality / measureTriQuality, useMax = true (ma/maQuality.cc:83-167)
@@ -1285,6 +1323,7 @@ __global__ void k_xyz_f32(DevMesh m, float* xyz32) {
 }
 
 inline int nblk(long n, int b = kBlock) { return (int)((n + b - 1) / b); }
+inline int count_grid(long n) { return (int)std::min<long>((n + kBlock - 1) / kBlock, kCountGrid); }
 
 // ---------------------------------------------------------------------
 // MA sweeps around the marks (ma/maSize.cc:652-690, ma/maShape.cc:132-169,
@@ -1444,24 +1483,22 @@ __global__ void __launch_bounds__(kBlock) k_first_equal(long long n, const doubl
 __global__ void __launch_bounds__(kBlock) k_mark_quality(int T, const double* __restrict__ q, double good,
                                                          int* __restrict__ flags, unsigned long long* count,
                                                          DevStatus* st) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  int marked = 0;
-  if (e < T) {
+  unsigned marked = 0;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < T; e += gridDim.x * blockDim.x) {
     int f = flags[e];
     if (f & SPRG_BAD_QUALITY) {
       set_status(st, SPRG_EFLAGS, e);
     } else if (!(f & SPRG_OK_QUALITY)) {
       if (q[e] < good) {
         f |= SPRG_BAD_QUALITY;
-        marked = 1;
+        ++marked;
       } else {
         f |= SPRG_OK_QUALITY;
       }
       flags[e] = f;
     }
   }
-  const unsigned b = __ballot_sync(0xffffffffu, marked);
-  if ((threadIdx.x & 31) == 0 && b) atomicAdd(count, (unsigned long long)__popc(b));
+  block_count2(count, marked, nullptr, 0);
 }
 
 
@@ -2152,7 +2189,7 @@ void launch_measure_aniso_f64(const DevMesh& m, const double* sizes, const doubl
 
 void launch_mark(int E, const double* L, int which, int* flags, unsigned long long* count, DevStatus* st,
                  cudaStream_t s) {
-  if (E) k_mark<<<nblk(E), kBlock, 0, s>>>(E, L, which, flags, count, st);
+  if (E) k_mark<<<count_grid(E), kBlock, 0, s>>>(E, L, which, flags, count, st);
 }
 
 void launch_mark_bits(int E, const double* L, uint32_t* split, uint32_t* collapse, cudaStream_t s) {
@@ -2161,12 +2198,12 @@ void launch_mark_bits(int E, const double* L, uint32_t* split, uint32_t* collaps
 
 void launch_apply_bits(int E, const uint32_t* bits, int which, int* flags, unsigned long long* count, DevStatus* st,
                        cudaStream_t s) {
-  if (E) k_apply_bits<<<nblk(E), kBlock, 0, s>>>(E, bits, which, flags, count, st);
+  if (E) k_apply_bits<<<count_grid(E), kBlock, 0, s>>>(E, bits, which, flags, count, st);
 }
 
 void launch_apply_marks(int E, const uint32_t* split_bits, const uint32_t* collapse_bits, int* flags,
                         unsigned long long* counts, DevStatus* st, cudaStream_t s) {
-  if (E) k_apply_marks<<<nblk(E), kBlock, 0, s>>>(E, split_bits, collapse_bits, flags, counts, st);
+  if (E) k_apply_marks<<<count_grid((E + 3) / 4), kBlock, 0, s>>>(E, split_bits, collapse_bits, flags, counts, st);
 }
 
 void launch_quality_f64(const DevMesh& m, const double* size, const double* sizes, const double* frames, double* q,
@@ -2257,7 +2294,7 @@ void launch_first_min_below(long long n, const double* x, double start, unsigned
 
 void launch_mark_quality(int T, const double* q, double good, int* flags, unsigned long long* count, DevStatus* st,
                          cudaStream_t s) {
-  if (T) k_mark_quality<<<nblk(T), kBlock, 0, s>>>(T, q, good, flags, count, st);
+  if (T) k_mark_quality<<<count_grid(T), kBlock, 0, s>>>(T, q, good, flags, count, st);
 }
 void launch_tri_weights(const DevMesh& m, double* w, unsigned char* listed, ExpandList lst, cudaStream_t s) {
   if (m.V) k_tri_weights<kTriThreadRows><<<(m.V + 127) / 128, 128, 0, s>>>(m, w, listed, lst);
