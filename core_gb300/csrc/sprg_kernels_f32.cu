@@ -746,7 +746,7 @@ __global__ void __launch_bounds__(kBlock) k_fast_average(DevMesh m, const float2
 // ---------------------------------------------------------------------------
 // measure: metric length with 2-point Gauss, h linearly interpolated
 // ---------------------------------------------------------------------------
-// two edges per thread (e and e + 32 within the warp's 64-edge chunk), all
+// four edges per thread (e, e + 32, e + 64, e + 96 within the warp's 128-edge chunk), all
 // loads issued before use; the edge's half length is per-mesh data
 __global__ void __launch_bounds__(kBlock) k_fast_measure(DevMesh m, const float* __restrict__ half_len,
                                                          const float2* __restrict__ sz2, uint32_t* __restrict__ split,
@@ -755,26 +755,26 @@ __global__ void __launch_bounds__(kBlock) k_fast_measure(DevMesh m, const float*
                                                          float guard_rel) {
   const int lane = threadIdx.x & 31;
   const long warp = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5;
-  const int e0 = (int)(warp * 64) + lane;
-  const int eids[2] = {e0, e0 + 32};
-  int2 ab[2];
-  float hl[2];
-  float2 A[2], B[2];
+  const int e0 = (int)(warp * 128) + lane;
+  const int eids[4] = {e0, e0 + 32, e0 + 64, e0 + 96};
+  int2 ab[4];
+  float hl[4];
+  float2 A[4], B[4];
 #pragma unroll
-  for (int i = 0; i < 2; ++i) {
+  for (int i = 0; i < 4; ++i) {
     bool in = eids[i] < m.E;
     ab[i] = in ? __ldg(reinterpret_cast<const int2*>(m.edv) + eids[i]) : make_int2(0, 0);
     hl[i] = in ? __ldg(half_len + eids[i]) : 0.f;
   }
 #pragma unroll
-  for (int i = 0; i < 2; ++i) {
+  for (int i = 0; i < 4; ++i) {
     A[i] = __ldg(sz2 + ab[i].x);
     B[i] = __ldg(sz2 + ab[i].y);
   }
   const float gp = 0.577350269189626f;
   const float n0 = 0.5f * (1.f - gp), n1 = 0.5f * (1.f + gp);
 #pragma unroll
-  for (int i = 0; i < 2; ++i) {
+  for (int i = 0; i < 4; ++i) {
     bool s = false, c = false;
     const int e = eids[i];
     if (e < m.E) {
@@ -900,7 +900,7 @@ void fast_average(const DevMesh& m, const float2* q, const double* out3, float2*
 void fast_measure(const DevMesh& m, const float* half_len, const float2* sz2, uint32_t* split, uint32_t* collapse,
                   int* guard_items, int* guard_count, int guard_cap, float guard_rel, cudaStream_t s) {
   if (m.E)
-    k_fast_measure<<<nblk((m.E + 1) / 2), kBlock, 0, s>>>(m, half_len, sz2, split, collapse, guard_items, guard_count,
+    k_fast_measure<<<nblk((m.E + 3) / 4), kBlock, 0, s>>>(m, half_len, sz2, split, collapse, guard_items, guard_count,
                                                           guard_cap, guard_rel);
 }
 
