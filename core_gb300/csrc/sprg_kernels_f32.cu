@@ -125,37 +125,29 @@ __device__ __forceinline__ float inv_fifth_root(float x) {
 }
 
 // A tet gradient is kept as 16 bytes: the FP32 value s (3 floats) and its
-// correction r = exact - s with |r_j| <= ulp(s_j)/2, packed into one word as
-// a shared-exponent triple.  With E the exponent of max |r_j| and E_s that of
-// max |s_j| (E <= E_s - 24):
-//   bits 27..31  k = E_s - E - 24 (corrections below 2^-56 |s| are dropped)
-//   bits 18..26, 9..17, 0..8  m_j + 256, m_j = rint(r_j 2^(7-E)) in [-255, 255]
-// so r_j = m_j 2^(E_s - k - 31), exact to 2^-32 max|s_j| (half a unit); no
-// correction is k = 31 with m_j = 0 (kNoCorr).  Rounding and the int <-> float
+// correction r = exact - s with |r_j| <= ulp(s_j)/2, packed into one word on
+// the grid of the largest component: with E_s the exponent of max |s_j|,
+//   r_j ~ m_j 2^(E_s - 31),  m_j = rint(r_j 2^(31 - E_s)) in [-128, 128]
+// (|r_j| <= 2^(E_s - 24)), stored as m_j + 256 in bits 18..26, 9..17, 0..8.
+// The stored correction is exact to 2^(E_s - 32) <= 2^-32 max |s_j|.  The
+// grid follows from s alone, so scaling s by a power of two scales the
+// decoded r with it.  Values with max |s_j| below 2^-95, infinite or NaN
+// carry no correction (kNoCorr, m_j = 0).  Rounding and the int <-> float
 // steps use the 1.5 * 2^23 constant (integer and FMA pipes) instead of
 // conversion instructions, which run at a quarter rate.
-constexpr uint32_t kNoCorr = (31u << 27) | (256u << 18) | (256u << 9) | 256u;
+constexpr uint32_t kNoCorr = (256u << 18) | (256u << 9) | 256u;
 __device__ __forceinline__ int fexp(float a) { return ((__float_as_int(a) >> 23) & 0xff) - 127; }
 
 __device__ __forceinline__ uint32_t pack_corr(float s0, float s1, float s2, float r0, float r1, float r2) {
-  float M = fmaxf(fabsf(r0), fmaxf(fabsf(r1), fabsf(r2)));
-  if (!(M > 0.f) || !(M < 3.0e38f)) return kNoCorr;
-  int Es = fexp(fmaxf(fabsf(s0), fmaxf(fabsf(s1), fabsf(s2))));
-  int E = fexp(M);
-  int k = Es - E - 24;
-  if (k > 31) return kNoCorr;
-  if (k < 0) {  // only for subnormal s: keep what fits
-    k = 0;
-    E = Es - 24;
-  }
-  // 2^(7-E) as a float: exact for E > -120 (the exponent field 134 - E <= 254)
-  float sc = E > -120 ? __int_as_float((134 - E) << 23) : ldexpf(1.f, 7 - E);
-  auto q9 = [&](float r) {  // rint(r 2^(7-E)) + 256, clamped to [1, 511]
-    const float x = E > -120 ? r * sc : ldexpf(r, 7 - E);
-    const int mj = __float_as_int(x + 12582912.f) - 0x4B400000;
+  const float smax = fmaxf(fabsf(s0), fmaxf(fabsf(s1), fabsf(s2)));
+  if (!(smax >= 0x1p-95f) || !(smax < 3.0e38f)) return kNoCorr;
+  // 2^(31 - E_s) as a float: exponent field 158 - E_s in [31, 253]
+  const float sc = __int_as_float((158 - fexp(smax)) << 23);
+  auto q9 = [&](float r) {  // rint(r 2^(31 - E_s)) + 256, clamped to [1, 511]
+    const int mj = __float_as_int(fmaf(r, sc, 12582912.f)) - 0x4B400000;
     return (uint32_t)(max(-255, min(255, mj)) + 256);
   };
-  return ((uint32_t)k << 27) | (q9(r0) << 18) | (q9(r1) << 9) | q9(r2);
+  return (q9(r0) << 18) | (q9(r1) << 9) | q9(r2);
 }
 
 struct Grad {
@@ -169,7 +161,8 @@ __device__ __forceinline__ Grad unpack_grad(uint4 a) {
   g.s[1] = __uint_as_float(a.y);
   g.s[2] = __uint_as_float(a.z);
   g.gmax = fmaxf(fabsf(g.s[0]), fmaxf(fabsf(g.s[1]), fabsf(g.s[2])));
-  int ex = fexp(g.gmax) - (int)(a.w >> 27) - 31;
+  // 2^(E_s - 31); below 2^-126 (max |s_j| < 2^-95) the correction is zero
+  const int ex = fexp(g.gmax) - 31;
   const float sc = ex > -127 ? __int_as_float((ex + 127) << 23) : 0.f;
   // m_j as a float: 1.5 * 2^23 + (m_j + 256) read as a float, minus the offset
   const float off = 12582912.f + 256.f;
