@@ -58,6 +58,7 @@ struct sprg_ctx {
   // FP32 path buffers
   DevBuf crec, vrec, rec32, q32, sz2, fcnt, guard, tetd, wts, w64, listed, geo, geo64, elen, fitems;
   DevBuf gstamp, gfit, grec;  // guard pipeline scratch
+  DevBuf tnext;               // work counter of the tet kernel
   // learned form
   DevBuf hess;  // nodal Hessian upload (sprg_hessian_metric)
   // batch of independent meshes (sprg_set_batch)
@@ -755,7 +756,7 @@ int sprg_destroy(sprg_ctx* c) {
                     &c->size,  &c->L,       &c->flags, &c->q,    &c->sizes3,  &c->frames9, &c->partials,
                     &c->out3,  &c->status,  &c->count, &c->mcount, &c->xitems, &c->xcount, &c->slab, &c->bits, &c->titems, &c->tcountb, &c->Lx, &c->pairs, &c->red, &c->eflags, &c->logm, &c->qw, &c->qwlisted, &c->qwitems, &c->qwcount, &c->tw, &c->twlisted, &c->twitems, &c->twcount, &c->met32, &c->qrec32, &c->kidx, &c->kval, &c->klen, &c->rec9, &c->cache2d.v, &c->cache2d.n, &c->cache2d.el, &c->agitems, &c->agcount,
                     &c->crec,  &c->vrec,    &c->rec32, &c->q32, &c->sz2,  &c->fcnt,   &c->guard, &c->tetd,
-                    &c->wts,   &c->w64,     &c->listed, &c->geo, &c->geo64, &c->elen, &c->fitems, &c->gstamp, &c->gfit, &c->grec,
+                    &c->wts,   &c->w64,     &c->listed, &c->geo, &c->geo64, &c->elen, &c->fitems, &c->gstamp, &c->gfit, &c->grec, &c->tnext,
                     &c->hess, &c->pcls, &c->bverts, &c->btiles, &c->bnext, &c->bvoff, &c->bseg, &c->bsegoff, &c->bratios, &c->vvoff, &c->vv, &c->vtile, &c->vr16, &c->rec16,
                     &c->ql,    &c->sizel,   &c->fbitems, &c->fbcount, &c->mlp_packed, &c->mlp_err, &c->mlp_tmp,
                     &c->cache64.v, &c->cache64.n, &c->cache64.el, &c->cache32.v, &c->cache32.n, &c->cache32.el};
@@ -1406,6 +1407,7 @@ static int pass_fast(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_
   ENSURE(c->vrec, 32 * (size_t)m.V);
   ENSURE(c->rec32, 16 * (size_t)m.V);
   ENSURE(c->tetd, 16 * (size_t)m.T);
+  ENSURE(c->tnext, sizeof(int));
   ENSURE(c->q32, 8 * (size_t)m.T);
   ENSURE(c->sz2, 8 * (size_t)m.V);
   ENSURE(c->rec, 24 * (size_t)m.V);
@@ -1433,7 +1435,7 @@ static int pass_fast(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_
   fast_prep(m, P<double>(c->f), P<float4>(c->crec), vrec, c->stream);
   PE();
   PB("tet_f32");
-  fast_tet(m, vrec, (float)c->frame[3], P<uint4>(c->tetd), c->stream);
+  fast_tet(m, vrec, (float)c->frame[3], P<uint4>(c->tetd), P<int>(c->tnext), c->stream);
   PE();
   if (!c->bins_ready) {
     if ((rc = build_bins(c))) return rc;

@@ -302,49 +302,60 @@ __device__ __forceinline__ TetData load_tet(const float4* __restrict__ vr, int4 
 // ---------------------------------------------------------------------------
 // tet: gradient value and packed correction
 // ---------------------------------------------------------------------------
-// One wave of resident blocks strides over the elements; each thread loads
-// the next element's vertex ids before working on the current one, so only
-// the record gathers (mostly L2 hits) stay on the dependent chain.  (With
-// the prefetched ids the kernel needs 64 registers: 4 blocks per SM.)
+// Blocks take chunks of kTetChunk x blockDim elements from a counter (so a
+// kernel running beside this one, such as the listed patches' FP64 fits on
+// the side stream, only delays the chunks of the blocks it displaces); in a
+// chunk each thread loads the next element's vertex ids before working on
+// the current one, so only the record gathers (mostly L2 hits) stay on the
+// dependent chain.
+constexpr int kTetChunk = 8;
 __global__ void __launch_bounds__(kBlock, 4) k_fast_tet(DevMesh m, const float4* __restrict__ vr, float gscale,
-                                                        uint4* __restrict__ td) {
+                                                        uint4* __restrict__ td, int* __restrict__ next_chunk) {
   const int4* __restrict__ ev4 = reinterpret_cast<const int4*>(m.ev);
-  const int stride = gridDim.x * blockDim.x;
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  int4 next = t < m.T ? __ldg(ev4 + t) : make_int4(0, 0, 0, 0);
-  for (; t < m.T; t += stride) {
-    const int4 tv = next;
-    if (t + stride < m.T) next = __ldg(ev4 + t + stride);
-    TetData d = load_tet(vr, tv);
-    // first estimate with an approximate inverse of the rounded edge matrix
-    // (hi + lo: the high words alone, exact differences of [1, 2] values, are
-    // off by up to 2^-23 absolute, which squared through the correction would
-    // exceed the accuracy the error bound assumes); the correction
-    // J^{-1}(du - J g) with the compensated residual makes the result accurate
-    // to second order in both approximations
-    Cof cf;
-    {
-      float4 er[3];
-  #pragma unroll
-      for (int i = 0; i < 3; ++i)
-        er[i] = make_float4(d.eh[i].x + d.el[i].x, d.eh[i].y + d.el[i].y, d.eh[i].z + d.el[i].z, 0.f);
-      cf = cofactors(er[0], er[1], er[2]);
+  __shared__ int chunk;
+  for (;;) {
+    if (threadIdx.x == 0) chunk = atomicAdd(next_chunk, 1);
+    __syncthreads();
+    const long t0 = (long)chunk * (kTetChunk * kBlock);
+    __syncthreads();
+    if (t0 >= m.T) break;
+    const int t_end = (int)min((long)m.T, t0 + kTetChunk * kBlock);
+    int t = (int)t0 + threadIdx.x;
+    int4 next = t < t_end ? __ldg(ev4 + t) : make_int4(0, 0, 0, 0);
+    for (; t < t_end; t += kBlock) {
+      const int4 tv = next;
+      if (t + kBlock < t_end) next = __ldg(ev4 + t + kBlock);
+      TetData d = load_tet(vr, tv);
+      // first estimate with an approximate inverse of the rounded edge matrix
+      // (hi + lo: the high words alone, exact differences of [1, 2] values, are
+      // off by up to 2^-23 absolute, which squared through the correction would
+      // exceed the accuracy the error bound assumes); the correction
+      // J^{-1}(du - J g) with the compensated residual makes the result accurate
+      // to second order in both approximations
+      Cof cf;
+      {
+        float4 er[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+          er[i] = make_float4(d.eh[i].x + d.el[i].x, d.eh[i].y + d.el[i].y, d.eh[i].z + d.el[i].z, 0.f);
+        cf = cofactors(er[0], er[1], er[2]);
+      }
+      float g[3], c[3], s[3], r[3];
+      apply_inv(cf, d.eh[0].w, d.eh[1].w, d.eh[2].w, g);
+      apply_inv(cf, comp_residual(d.eh[0], d.el[0], g[0], g[1], g[2]), comp_residual(d.eh[1], d.el[1], g[0], g[1], g[2]),
+                comp_residual(d.eh[2], d.el[2], g[0], g[1], g[2]), c);
+      // s + r = g + c exactly (|c| << |g|: Fast2Sum)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        s[j] = g[j] + c[j];
+        r[j] = c[j] - (s[j] - g[j]);
+      }
+      // back to the mesh's coordinates: the correction word is relative to the
+      // largest |s_j|, so scaling s by a power of two scales r with it
+      const uint32_t corr = pack_corr(s[0], s[1], s[2], r[0], r[1], r[2]);
+      td[t] = make_uint4(__float_as_uint(s[0] * gscale), __float_as_uint(s[1] * gscale),
+                         __float_as_uint(s[2] * gscale), corr);
     }
-    float g[3], c[3], s[3], r[3];
-    apply_inv(cf, d.eh[0].w, d.eh[1].w, d.eh[2].w, g);
-    apply_inv(cf, comp_residual(d.eh[0], d.el[0], g[0], g[1], g[2]), comp_residual(d.eh[1], d.el[1], g[0], g[1], g[2]),
-              comp_residual(d.eh[2], d.el[2], g[0], g[1], g[2]), c);
-    // s + r = g + c exactly (|c| << |g|: Fast2Sum)
-  #pragma unroll
-    for (int j = 0; j < 3; ++j) {
-      s[j] = g[j] + c[j];
-      r[j] = c[j] - (s[j] - g[j]);
-    }
-    // back to the mesh's coordinates: the correction word is relative to the
-    // largest |s_j|, so scaling s by a power of two scales r with it
-    const uint32_t corr = pack_corr(s[0], s[1], s[2], r[0], r[1], r[2]);
-    td[t] = make_uint4(__float_as_uint(s[0] * gscale), __float_as_uint(s[1] * gscale),
-                       __float_as_uint(s[2] * gscale), corr);
   }
 }
 
@@ -823,7 +834,7 @@ int error_grid() {
   return grid;
 }
 
-// the tet kernel runs one full wave as well
+// the tet kernel runs one full wave of resident blocks as well
 int tet_grid(int T) {
   static int grid = 0;
   if (!grid) {
@@ -833,7 +844,7 @@ int tet_grid(int T) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fast_tet, kBlock, 0);
     grid = (sms > 0 ? sms : 152) * (per_sm > 0 ? per_sm : 5);
   }
-  const int nb = nblk(T);
+  const int nb = (int)((T + (long)kTetChunk * kBlock - 1) / ((long)kTetChunk * kBlock));
   return nb < grid ? nb : grid;
 }
 
@@ -857,8 +868,10 @@ void fast_prep(const DevMesh& m, const double* u, const float4* crec, float4* vr
   if (m.V) k_prep<<<nblk(m.V), kBlock, 0, s>>>(m.V, u, crec, vrec);
 }
 
-void fast_tet(const DevMesh& m, const float4* vrec, float gscale, uint4* td, cudaStream_t s) {
-  if (m.T) k_fast_tet<<<tet_grid(m.T), kBlock, 0, s>>>(m, vrec, gscale, td);
+void fast_tet(const DevMesh& m, const float4* vrec, float gscale, uint4* td, int* next_chunk, cudaStream_t s) {
+  if (!m.T) return;
+  cudaMemsetAsync(next_chunk, 0, sizeof(int), s);
+  k_fast_tet<<<tet_grid(m.T), kBlock, 0, s>>>(m, vrec, gscale, td, next_chunk);
 }
 
 void fast_weights(const DevMesh& m, float* w, double* w64, ExpandList xl, int* n_refit, unsigned char* listed,
