@@ -520,6 +520,19 @@ def gpu_batched(args):
         torch.cuda.synchronize(dev)
         ms = e0.elapsed_time(e1) / args.steps
         clk = clocks.stop()
+        # per-kernel times from as many direct, event-bracketed passes
+        c.profile(True)
+        c.profile_report(reset=True)
+        p0 = torch.cuda.Event(enable_timing=True)
+        p1 = torch.cuda.Event(enable_timing=True)
+        p0.record(st)
+        for _ in range(args.steps):
+            c.estimate_and_mark_resident(d_u.data_ptr(), 1.0, ps, pc)
+        p1.record(st)
+        torch.cuda.synchronize(dev)
+        ms_direct = p0.elapsed_time(p1) / args.steps
+        prof = c.profile_report(reset=True)
+        c.profile(False)
         tune = c.tuning_report()
         c.set_stream(0)
         _, _, _, _, info = c.estimate_and_mark(u, 1.0)
@@ -529,7 +542,10 @@ def gpu_batched(args):
            "config": {"workload": f"4096 unit tet boxes, n per side log-uniform in [4, 40] (seed 3), 1-8 Gaussian "
                                   f"bumps each; {V} vertices, {T} tets, {E} edges; adapt ratio 0.1 per mesh",
                       "form": "plain FP32, batched, CUDA graph", "l2": "inputs larger than L2"},
-           "tuning": tune, "guard_edges": int(info["n_guard_edges"]), "clocks": clk,
+           "tuning": tune, "guard_edges": int(info["n_guard_edges"]),
+           "listed_patches": int(info["n_expanded"] + info["n_fp64_refits"]), "clocks": clk,
+           "timed_by": "CUDA graph replay", "ms_per_step_profiled_direct": ms_direct,
+           "phases": {k: {"launches": n, "total_ms": t, "avg_ms": t / max(n, 1)} for k, (n, t) in prof.items()},
            "setup_s": {"mesh_build": round(t_mesh, 2)}}
     print(json.dumps(out), flush=True)
 

@@ -29,6 +29,9 @@ struct PatchCache {
   bool valid = false;
   int count = 0;
   DevBuf v, n, el;
+  // tets: per-mesh weights of the cached patches' fits (w_ready once built)
+  bool w_ready = false;
+  DevBuf woff, w, wn;
 };
 
 struct sprg_ctx {
@@ -235,14 +238,53 @@ void prof_end(sprg_ctx* c) {
 
 // Listed patches: grow them on the first pass (recording the final element
 // sets), afterwards one QR fit per cached set.
+// Tets: once a patch cache exists, the QR of each cached patch runs once
+// (per mesh) into weights, and later passes take weighted sums.  Runs on
+// the context stream (it reads the patch sizes back).
+int ensure_cache_weights(sprg_ctx* c, PatchCache& pc) {
+  if (!pc.valid || pc.w_ready || c->m.dim != 3 || pc.count <= 0) return SPRG_OK;
+  std::vector<int> n((size_t)pc.count);
+  CK(cudaMemcpyAsync(n.data(), pc.n.p, sizeof(int) * n.size(), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  std::vector<long long> off(n.size());
+  long long total = 0;
+  for (size_t i = 0; i < n.size(); ++i) {
+    off[i] = total;
+    total += n[i] > 0 ? n[i] : 0;
+  }
+  ENSURE(pc.woff, sizeof(long long) * off.size());
+  ENSURE(pc.w, sizeof(double) * (size_t)(total > 0 ? total : 1));
+  ENSURE(pc.wn, sizeof(int) * n.size());
+  ENSURE(c->slab, sizeof(double) * (size_t)expand_grid() * expand_max_elems() * 8);
+  CK(cudaMemcpyAsync(pc.woff.p, off.data(), sizeof(long long) * off.size(), cudaMemcpyHostToDevice, c->stream));
+  PB("cached_weights_f64");
+  launch_cached_weights_f64(c->m, pc.count, P<int>(pc.v), P<int>(pc.n), P<int>(pc.el), P<long long>(pc.woff),
+                            P<double>(pc.w), P<int>(pc.wn), P<double>(c->slab), c->stream);
+  PE();
+  c->launches += 1;
+  int rc = check_launch(c, "cached patch weights");
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(c->stream));  // the host offsets stay alive until the copy is done
+  pc.w_ready = true;
+  return SPRG_OK;
+}
+
 int listed_fits(sprg_ctx* c, PatchCache& pc, const double* ip, const double* u, int nc, double* rec64, ExpandList xl,
                 cudaStream_t on = nullptr) {
   DevMesh& m = c->m;
   if (pc.valid) {
+    if (!on) {
+      int rc = ensure_cache_weights(c, pc);
+      if (rc) return rc;
+    }
     cudaStream_t s = on ? on : c->stream;
     if (!on) PB("cached_fit_f64");
-    launch_cached_fit_f64(m, ip, u, nc, rec64, pc.count, P<int>(pc.v), P<int>(pc.n), P<int>(pc.el), P<double>(c->slab),
-                          P<DevStatus>(c->status), s);
+    if (pc.w_ready)
+      launch_cached_wsum_f64(m, ip, u, nc, rec64, pc.count, P<int>(pc.v), P<int>(pc.el), P<long long>(pc.woff),
+                             P<double>(pc.w), P<int>(pc.wn), P<DevStatus>(c->status), s);
+    else
+      launch_cached_fit_f64(m, ip, u, nc, rec64, pc.count, P<int>(pc.v), P<int>(pc.n), P<int>(pc.el),
+                            P<double>(c->slab), P<DevStatus>(c->status), s);
     if (!on) PE();
     c->launches += 1;
     return check_launch(c, "cached fit");
@@ -264,7 +306,15 @@ int listed_fits(sprg_ctx* c, PatchCache& pc, const double* ip, const double* u, 
   if (rc) return rc;
   pc.count = xc;
   pc.valid = true;
-  return SPRG_OK;
+  if (m.dim != 3) return SPRG_OK;
+  // tets: this pass already takes the weighted sums, so every pass gives the
+  // same bits for the listed patches
+  if ((rc = ensure_cache_weights(c, pc))) return rc;
+  if (!pc.w_ready) return SPRG_OK;
+  launch_cached_wsum_f64(m, ip, u, nc, rec64, pc.count, P<int>(pc.v), P<int>(pc.el), P<long long>(pc.woff),
+                         P<double>(pc.w), P<int>(pc.wn), P<DevStatus>(c->status), c->stream);
+  c->launches += 1;
+  return check_launch(c, "cached fit");
 }
 
 int step_grad(sprg_ctx* c, int ncin) {
@@ -590,6 +640,7 @@ static void invalidate_mesh_state(sprg_ctx* c) {
   c->qw_ready = false;
   c->vv_ready = false;
   c->cache64.valid = c->cache32.valid = c->cache2d.valid = false;
+  c->cache64.w_ready = c->cache32.w_ready = c->cache2d.w_ready = false;
   c->batch_n = 0;
   c->batch_nseg = 0;
   // stamps are zeroed when (re)allocated at the next guard pass
@@ -759,7 +810,9 @@ int sprg_destroy(sprg_ctx* c) {
                     &c->wts,   &c->w64,     &c->listed, &c->geo, &c->geo64, &c->elen, &c->fitems, &c->gstamp, &c->gfit, &c->grec, &c->tnext,
                     &c->hess, &c->pcls, &c->bverts, &c->btiles, &c->bnext, &c->bvoff, &c->bseg, &c->bsegoff, &c->bratios, &c->vvoff, &c->vv, &c->vtile, &c->vr16, &c->rec16,
                     &c->ql,    &c->sizel,   &c->fbitems, &c->fbcount, &c->mlp_packed, &c->mlp_err, &c->mlp_tmp,
-                    &c->cache64.v, &c->cache64.n, &c->cache64.el, &c->cache32.v, &c->cache32.n, &c->cache32.el};
+                    &c->cache64.v, &c->cache64.n, &c->cache64.el, &c->cache32.v, &c->cache32.n, &c->cache32.el,
+                    &c->cache64.woff, &c->cache64.w, &c->cache64.wn, &c->cache32.woff, &c->cache32.w,
+                    &c->cache32.wn};
   for (DevBuf* b : bufs) release(*b);
   for (auto& e : c->ev_pool) cudaEventDestroy(e);
   if (c->copy) {
@@ -1232,6 +1285,8 @@ static int fast_setup(sprg_ctx* c, ExpandList xl) {
 static int listed_fork(sprg_ctx* c, ExpandList xl, bool* forked) {
   *forked = false;
   if (!c->cache32.valid) return SPRG_OK;
+  int wrc = ensure_cache_weights(c, c->cache32);
+  if (wrc) return wrc;
   if (!c->side) {
     CK(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
     CK(cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming));

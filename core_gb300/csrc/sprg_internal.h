@@ -91,6 +91,15 @@ void launch_expand_f64(const DevMesh& m, const double* ip, const double* u, int 
 void launch_cached_fit_f64(const DevMesh& m, const double* ip, const double* u, int nc, double* rec, int n_cached,
                            const int* cache_v, const int* cache_n, const int* cache_el, double* slab, DevStatus* st,
                            cudaStream_t s);
+// Tets: per-mesh weights of the cached patches (w = Q1 R^-T t from the fit's
+// QR; woff: each patch's offset into w, wn: its size or -1 where the rank
+// test fails) and the per-pass weighted sums that replace the fits
+void launch_cached_weights_f64(const DevMesh& m, int n_cached, const int* cache_v, const int* cache_n,
+                               const int* cache_el, const long long* woff, double* w, int* wn, double* slab,
+                               cudaStream_t s);
+void launch_cached_wsum_f64(const DevMesh& m, const double* ip, const double* u, int nc, double* rec, int n_cached,
+                            const int* cache_v, const int* cache_el, const long long* woff, const double* w,
+                            const int* wn, DevStatus* st, cudaStream_t s);
 int expand_max_elems();
 int expand_grid();
 // Per-element error terms + deterministic block partials (2 per block).

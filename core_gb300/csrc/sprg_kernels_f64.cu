@@ -585,6 +585,137 @@ __global__ void __launch_bounds__(32) k_cached_fit(DevMesh m, const double* __re
   }
 }
 
+// Tets: the cached patches' fits are linear in the samples as well.  Per mesh,
+// the fit's Householder QR (slab_fit's reflectors and 1e-10 rank test) of the
+// rows [1, x_ip, y_ip, z_ip] gives w = Q1 R^-T t (t = [1, x_v, y_v, z_v]),
+// and every pass recovers rec(v) = sum_i w_i b_i.  Warp per cached patch;
+// rows (4 geometry columns, then the 4 reflectors) in shared memory up to
+// kExpandSmemRows elements, else in the block's slab.  wn[it] = the patch
+// size, or -1 where the rank test fails (the fit's SPRG_EPATCH).
+__global__ void __launch_bounds__(32) k_cached_weights(DevMesh m, int n_cached, const int* __restrict__ cache_v,
+                                                       const int* __restrict__ cache_n,
+                                                       const int* __restrict__ cache_el,
+                                                       const long long* __restrict__ woff, double* __restrict__ w,
+                                                       int* __restrict__ wn, double* slab) {
+  constexpr int NT = 4, LD = 2 * NT;
+  __shared__ double srows[kExpandSmemRows * 8];
+  const int lane = threadIdx.x & 31;
+  double* grows = slab + (size_t)blockIdx.x * kExpandMaxElems * LD;
+  for (int it = blockIdx.x; it < n_cached; it += gridDim.x) {
+    const int v = cache_v[it], n = cache_n[it];
+    if (n < NT) {  // a failed growth (-1) or too few elements
+      if (lane == 0) wn[it] = -1;
+      continue;
+    }
+    const int* S = cache_el + (size_t)it * kExpandMaxElems;
+    double* rows = n <= kExpandSmemRows ? srows : grows;
+    for (int i = lane; i < n; i += 32) {
+      const V3 p = elem_ip_point(m, S[i]);
+      double* rw = rows + (size_t)i * LD;
+      rw[0] = 1.0; rw[1] = p.v[0]; rw[2] = p.v[1]; rw[3] = p.v[2];
+    }
+    __syncwarp();
+    bool ok = true;
+    for (int k = 0; k < NT && ok; ++k) {
+      double sq = 0;
+      for (int i = k + lane; i < n; i += 32) sq += rows[(size_t)i * LD + k] * rows[(size_t)i * LD + k];
+      const double cn = sqrt(warp_sum(sq));
+      if (cn < 1e-10) {  // uniform across the warp
+        ok = false;
+        break;
+      }
+      const double akk = rows[(size_t)k * LD + k];
+      double s2 = 0;
+      for (int i = lane; i < n; i += 32) {
+        double vi = i < k ? 0.0 : rows[(size_t)i * LD + k];
+        if (i == k) vi += ((akk < 0) ? -1 : 1) * cn;
+        rows[(size_t)i * LD + NT + k] = vi;
+        s2 += vi * vi;
+      }
+      const double rn = sqrt(warp_sum(s2));
+      for (int i = lane; i < n; i += 32) rows[(size_t)i * LD + NT + k] /= rn;
+      __syncwarp();
+      for (int j = k; j < NT; ++j) {
+        double d = 0;
+        for (int i = k + lane; i < n; i += 32) d += rows[(size_t)i * LD + j] * rows[(size_t)i * LD + NT + k];
+        d = warp_sum(d);
+        for (int i = k + lane; i < n; i += 32) rows[(size_t)i * LD + j] -= 2 * d * rows[(size_t)i * LD + NT + k];
+        __syncwarp();
+      }
+    }
+    if (!ok) {
+      if (lane == 0) wn[it] = -1;
+      __syncwarp();
+      continue;
+    }
+    // y = R^-T t (forward substitution), then z = H_0 ... H_{NT-1} [y; 0]
+    const V3 xv = load_xyz(m.xyz, v);
+    const double t[4] = {1.0, xv.v[0], xv.v[1], xv.v[2]};
+    double y[4];
+    for (int i = 0; i < NT; ++i) {
+      double a = t[i];
+      for (int j = 0; j < i; ++j) a -= rows[(size_t)j * LD + i] * y[j];
+      y[i] = a / rows[(size_t)i * LD + i];
+    }
+    double* out = w + woff[it];
+    for (int i = lane; i < n; i += 32) out[i] = i < NT ? y[i] : 0.0;
+    __syncwarp();
+    for (int k = NT - 1; k >= 0; --k) {
+      double d = 0;
+      for (int i = k + lane; i < n; i += 32) d += rows[(size_t)i * LD + NT + k] * out[i];
+      d = warp_sum(d);
+      for (int i = k + lane; i < n; i += 32) out[i] -= 2 * d * rows[(size_t)i * LD + NT + k];
+      __syncwarp();
+    }
+    if (lane == 0) wn[it] = n;
+    __syncwarp();
+  }
+}
+
+// rec(v) = sum_i w_i b_i over a cached patch, warp per patch (lanes over the
+// elements, fixed reduction tree); b_i = the element's IP value, or the
+// gradient of the scalar field (nc = 3) / of the vector field (nc = 9)
+__global__ void __launch_bounds__(kBlock) k_cached_wsum(DevMesh m, const double* __restrict__ ip,
+                                                        const double* __restrict__ u, int nc,
+                                                        double* __restrict__ rec, int n_cached,
+                                                        const int* __restrict__ cache_v,
+                                                        const int* __restrict__ cache_el,
+                                                        const long long* __restrict__ woff,
+                                                        const double* __restrict__ w, const int* __restrict__ wn,
+                                                        DevStatus* st) {
+  const int lane = threadIdx.x & 31;
+  const int nwarps = gridDim.x * (blockDim.x >> 5);
+  for (int it = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); it < n_cached; it += nwarps) {
+    const int v = cache_v[it], n = wn[it];
+    if (n < 0) {
+      if (lane == 0) set_status(st, SPRG_EPATCH, v);
+      continue;
+    }
+    const int* S = cache_el + (size_t)it * kExpandMaxElems;
+    const double* wi = w + woff[it];
+    double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int i = lane; i < n; i += 32) {
+      const int el = S[i];
+      const double wk = wi[i];
+      if (ip) {
+        for (int c = 0; c < nc; ++c) acc[c] += wk * ip[(size_t)el * nc + c];
+      } else if (nc == 3) {
+        const V3 g = elem_grad_scalar(m, el, u);
+        for (int c = 0; c < 3; ++c) acc[c] += wk * g.v[c];
+      } else {
+        for (int r = 0; r < 3; ++r) {
+          const V3 g = elem_grad_component(m, el, u, 3, r);
+          for (int c = 0; c < 3; ++c) acc[3 * r + c] += wk * g.v[c];
+        }
+      }
+    }
+    for (int c = 0; c < nc; ++c) {
+      const double a = warp_sum(acc[c]);
+      if (lane == 0) rec[(size_t)v * nc + c] = a;
+    }
+  }
+}
+
 // ---------------------------------------------------------------------
 // Element error terms (SelfProduct / ElementError, spr/sprEstimateError.cc:98-170)
 // ---------------------------------------------------------------------
@@ -2150,6 +2281,22 @@ void launch_cached_fit_f64(const DevMesh& m, const double* ip, const double* u, 
   if (n_cached > 0)
     k_cached_fit<<<n_cached < kExpandGrid ? n_cached : kExpandGrid, 32, 0, s>>>(m, ip, u, nc, rec, n_cached, cache_v,
                                                                                 cache_n, cache_el, slab, st);
+}
+
+void launch_cached_weights_f64(const DevMesh& m, int n_cached, const int* cache_v, const int* cache_n,
+                               const int* cache_el, const long long* woff, double* w, int* wn, double* slab,
+                               cudaStream_t s) {
+  if (n_cached > 0)
+    k_cached_weights<<<n_cached < kExpandGrid ? n_cached : kExpandGrid, 32, 0, s>>>(m, n_cached, cache_v, cache_n,
+                                                                                   cache_el, woff, w, wn, slab);
+}
+
+void launch_cached_wsum_f64(const DevMesh& m, const double* ip, const double* u, int nc, double* rec, int n_cached,
+                            const int* cache_v, const int* cache_el, const long long* woff, const double* w,
+                            const int* wn, DevStatus* st, cudaStream_t s) {
+  if (n_cached > 0)
+    k_cached_wsum<<<std::min(nblk((long)n_cached * 32), 152 * 8), kBlock, 0, s>>>(m, ip, u, nc, rec, n_cached, cache_v,
+                                                                                cache_el, woff, w, wn, st);
 }
 
 int error_blocks(int T) { return nblk(T); }
