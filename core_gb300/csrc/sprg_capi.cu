@@ -56,7 +56,7 @@ struct sprg_ctx {
   bool qw_ready = false;
   // mixed-precision anisotropic pass: triangle patch weights and their
   // listed vertices (per mesh), FP32 metric records, guarded edges
-  DevBuf tw, twlisted, twitems, twcount, met32, qrec32, agitems, agcount, kidx, kval, klen, rec9;
+  DevBuf tw, twlisted, twitems, twcount, met32, qrec32, agitems, agcount, kidx, kval, klen, rec9, cj64, qties;
   bool tw_ready = false;
   // FP32 path buffers
   DevBuf crec, vrec, rec32, q32, sz2, fcnt, guard, tetd, wts, w64, listed, geo, geo64, elen, fitems;
@@ -805,7 +805,7 @@ int sprg_destroy(sprg_ctx* c) {
   DevBuf* bufs[] = {&c->xyz,   &c->xyz32,   &c->ev,   &c->edv,   &c->poff,    &c->pel,    &c->aoff,
                     &c->ael,   &c->tmp,     &c->f,    &c->ip,    &c->rec,     &c->err,    &c->esize,
                     &c->size,  &c->L,       &c->flags, &c->q,    &c->sizes3,  &c->frames9, &c->partials,
-                    &c->out3,  &c->status,  &c->count, &c->mcount, &c->xitems, &c->xcount, &c->slab, &c->bits, &c->titems, &c->tcountb, &c->Lx, &c->pairs, &c->red, &c->eflags, &c->logm, &c->qw, &c->qwlisted, &c->qwitems, &c->qwcount, &c->tw, &c->twlisted, &c->twitems, &c->twcount, &c->met32, &c->qrec32, &c->kidx, &c->kval, &c->klen, &c->rec9, &c->cache2d.v, &c->cache2d.n, &c->cache2d.el, &c->agitems, &c->agcount,
+                    &c->out3,  &c->status,  &c->count, &c->mcount, &c->xitems, &c->xcount, &c->slab, &c->bits, &c->titems, &c->tcountb, &c->Lx, &c->pairs, &c->red, &c->eflags, &c->logm, &c->qw, &c->qwlisted, &c->qwitems, &c->qwcount, &c->tw, &c->twlisted, &c->twitems, &c->twcount, &c->met32, &c->qrec32, &c->cj64, &c->qties, &c->kidx, &c->kval, &c->klen, &c->rec9, &c->cache2d.v, &c->cache2d.n, &c->cache2d.el, &c->agitems, &c->agcount,
                     &c->crec,  &c->vrec,    &c->rec32, &c->q32, &c->sz2,  &c->fcnt,   &c->guard, &c->tetd,
                     &c->wts,   &c->w64,     &c->listed, &c->geo, &c->geo64, &c->elen, &c->fitems, &c->gstamp, &c->gfit, &c->grec, &c->tnext,
                     &c->hess, &c->pcls, &c->bverts, &c->btiles, &c->bnext, &c->bvoff, &c->bseg, &c->bsegoff, &c->bratios, &c->vvoff, &c->vv, &c->vtile, &c->vr16, &c->rec16,
@@ -1748,7 +1748,7 @@ int sprg_debug_read(sprg_ctx* c, const char* name, void* host, size_t bytes) {
       {"ip", &c->ip},       {"rec", &c->rec},     {"err", &c->err},       {"esize", &c->esize},
       {"size", &c->size},   {"L", &c->L},         {"vrec", &c->vrec},     {"rec32", &c->rec32},
       {"q32", &c->q32},     {"sz2", &c->sz2},     {"tetd", &c->tetd},     {"out3", &c->out3},
-      {"fcnt", &c->fcnt},   {"guard", &c->guard}, {"xitems", &c->xitems}, {"xcount", &c->xcount}, {"agcount", &c->agcount}, {"sizes3", &c->sizes3}, {"frames9", &c->frames9}, {"twcount", &c->twcount},
+      {"fcnt", &c->fcnt},   {"guard", &c->guard}, {"xitems", &c->xitems}, {"xcount", &c->xcount}, {"agcount", &c->agcount}, {"sizes3", &c->sizes3}, {"frames9", &c->frames9}, {"twcount", &c->twcount}, {"met32", &c->met32}, {"rec9", &c->rec9},
       {"wts", &c->wts},     {"geo", &c->geo},     {"elen", &c->elen},     {"rec16", &c->rec16},
       {"sizel", &c->sizel}, {"ql", &c->ql},       {"vr16", &c->vr16},     {"fbitems", &c->fbitems},
       {"fbcount", &c->fbcount}, {"listed", &c->listed}};
@@ -2001,32 +2001,48 @@ static int aniso_pass_mixed(sprg_ctx* c, double eps, double h_min, double h_max,
     if ((rc = step_grad(c, 3)) || (rc = step_recover(c))) return rc;
     H = P<double>(c->rec);
   }
-  PB("hessian_metric");
-  launch_hessian_metric(m, H, eps, h_min, h_max, P<double>(c->sizes3), P<double>(c->frames9), c->stream);
-  PE();
   ENSURE(c->met32, sizeof(float) * 12 * (size_t)(m.V > 0 ? m.V : 1));
   ENSURE(c->qrec32, (size_t)quality_rec_bytes() * (size_t)(m.V > 0 ? m.V : 1));
   ENSURE(c->agitems, sizeof(int) * (size_t)(m.E > 0 ? m.E : 1));
   ENSURE(c->agcount, sizeof(int));
   CK(cudaMemsetAsync(c->agcount.p, 0, sizeof(int), c->stream));
-  PB("metric_f32");
-  launch_metric_f32(m.V, m.dim, P<double>(c->sizes3), P<double>(c->frames9), P<float>(c->met32), c->qrec32.p,
-                    c->stream);
-  PE();
+  // triangles: the FP32 records straight from the Hessian, and the FP64
+  // metric rebuilt only where the guard and the quality's tie-breaks need
+  // it; tets: the FP64 metric, then its FP32 records
+  const double* sizes64 = nullptr;
+  const double* frames64 = nullptr;
+  if (m.dim == 2) {
+    PB("metric_f32");
+    launch_metric_mixed2d(m.V, H, eps, h_min, h_max, P<float>(c->met32), c->qrec32.p, c->stream);
+    PE();
+  } else {
+    PB("hessian_metric");
+    launch_hessian_metric(m, H, eps, h_min, h_max, P<double>(c->sizes3), P<double>(c->frames9), c->stream);
+    PE();
+    PB("metric_f32");
+    launch_metric_f32(m.V, m.dim, P<double>(c->sizes3), P<double>(c->frames9), P<float>(c->met32), c->qrec32.p,
+                      c->stream);
+    PE();
+    sizes64 = P<double>(c->sizes3);
+    frames64 = P<double>(c->frames9);
+  }
   PB("measure_aniso_f32");
   launch_measure_aniso_f32(m, P<float>(c->met32), d_split_bits, d_collapse_bits, P<int>(c->agitems),
                            P<int>(c->agcount), m.E, c->stream);
   PE();
   PB("guard_measure_f64");
-  launch_measure_guard_f64(m, P<double>(c->sizes3), P<double>(c->frames9), P<int>(c->agitems), P<int>(c->agcount),
-                           m.E, d_split_bits, d_collapse_bits, c->stream);
+  launch_measure_guard_f64(m, sizes64, frames64, H, eps, h_min, h_max, P<int>(c->agitems), P<int>(c->agcount), m.E,
+                           d_split_bits, d_collapse_bits, c->stream);
   PE();
   c->launches += 4;
   if (d_quality) {
     PB("quality_f32");
-    launch_quality_aniso_f32(m, c->qrec32.p, P<double>(c->sizes3), P<double>(c->frames9), d_quality, c->stream);
+    ENSURE(c->cj64, sizeof(double) * (size_t)(m.V > 0 ? m.V : 1));
+    ENSURE(c->qties, sizeof(int) * ((size_t)m.T + 1));
+    launch_quality_aniso_f32(m, c->qrec32.p, sizes64, frames64, H, eps, h_min, h_max, P<double>(c->cj64),
+                             P<int>(c->qties) + 1, P<int>(c->qties), d_quality, c->stream);
     PE();
-    c->launches += 1;
+    c->launches += 2;
   }
   c->L_valid = false;  // no FP64 length array in this form
   c->size_valid = false;

@@ -161,10 +161,22 @@ void launch_metric_f32(int V, int dim, const double* sizes, const double* frames
 int quality_rec_bytes();
 void launch_measure_aniso_f32(const DevMesh& m, const float* met, uint32_t* split, uint32_t* collapse, int* guard,
                               int* gcount, int gcap, cudaStream_t s);
-void launch_measure_guard_f64(const DevMesh& m, const double* sizes, const double* frames, const int* guard,
-                              const int* gcount, int gcap, uint32_t* split, uint32_t* collapse, cudaStream_t s);
-void launch_quality_aniso_f32(const DevMesh& m, const void* qrec, const double* sizes, const double* frames, double* q,
-                              cudaStream_t s);
+// sizes / frames: the FP64 metric, or null to rebuild the guarded edges'
+// ends from the Hessian H (hessian_metric_vertex, the FP64 pass's bits)
+void launch_measure_guard_f64(const DevMesh& m, const double* sizes, const double* frames, const double* H,
+                              double eps, double hmin, double hmax, const int* guard, const int* gcount, int gcap,
+                              uint32_t* split, uint32_t* collapse, cudaStream_t s);
+// sizes / frames as for the guard (the FP64 determinants of tie-breaks)
+// two launches: FP32 qualities (listing the elements whose vertex pick the
+// FP32 determinants leave open), then the FP64 tie-breaks; cj64: V doubles,
+// tie_items: T ints, tie_count: one int (scratch, cleared here)
+void launch_quality_aniso_f32(const DevMesh& m, const void* qrec, const double* sizes, const double* frames,
+                              const double* H, double eps, double hmin, double hmax, double* cj64, int* tie_items,
+                              int* tie_count, double* q, cudaStream_t s);
+// triangles: FP32 metric records (12 floats) and quality records straight
+// from the Hessian (FP64 decisions, FP32 magnitudes)
+void launch_metric_mixed2d(int V, const double* H, double eps, double hmin, double hmax, float* out, void* qrec,
+                           cudaStream_t s);
 // Triangle recovery-of-gradient operator (per mesh, FP64): K_va over the
 // patch vertices, tri_operator_slots() slots per vertex (kidx ints, kval 3
 // doubles each, klen counts; patches that are not fans are added to the

@@ -1341,12 +1341,10 @@ __device__ __forceinline__ double metric_size(double lam, double eps, double hmi
   return fmin(fmax(sqrt(eps / a), hmin), hmax);
 }
 
-__global__ void k_hessian_metric(int V, int dim, const double* __restrict__ H, double eps, double hmin, double hmax,
-                                 double* __restrict__ sizes, double* __restrict__ frames) {
-  const int v = blockIdx.x * blockDim.x + threadIdx.x;
-  if (v >= V) return;
-  const double* h = H + 9 * (size_t)v;
-  double R[3][3], hs[3];
+// one vertex's metric from its Hessian row h (9 doubles): sizes hs, frame R
+// (directions as columns)
+__device__ void hessian_metric_vertex(int dim, const double* __restrict__ h, double eps, double hmin, double hmax,
+                                      double hs[3], double R[3][3]) {
   if (dim == 2) {
     const double a = h[0], b = 0.5 * (h[1] + h[3]), c = h[4];
     const double mid = 0.5 * (a + c), hd = 0.5 * (a - c);
@@ -1412,9 +1410,40 @@ __global__ void k_hessian_metric(int V, int dim, const double* __restrict__ H, d
     R[2][2] = R[0][0] * R[1][1] - R[1][0] * R[0][1];
     hs[2] = metric_size(lam[o[2]], eps, hmin, hmax);
   }
+}
+
+__global__ void k_hessian_metric(int V, int dim, const double* __restrict__ H, double eps, double hmin, double hmax,
+                                 double* __restrict__ sizes, double* __restrict__ frames) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= V) return;
+  double R[3][3], hs[3];
+  hessian_metric_vertex(dim, H + 9 * (size_t)v, eps, hmin, hmax, hs, R);
   for (int k = 0; k < 3; ++k) sizes[3 * (size_t)v + k] = hs[k];
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) frames[9 * (size_t)v + 3 * i + j] = R[i][j];
+}
+
+// The FP64 metric of a vertex for the guard and the quality's tie-breaks:
+// read from the materialised arrays, or (mixed pass on triangles, where they
+// are not stored) rebuilt from the Hessian by hessian_metric_vertex, the
+// same function as the FP64 pass's, so the values are that pass's bits.
+struct MetricSrc {
+  const double* sizes;   // V x 3, or null: rebuild from H
+  const double* frames;  // V x 9
+  const double* H;       // V x 9
+  int dim;
+  double eps, hmin, hmax;
+};
+__device__ __forceinline__ void metric_at(const MetricSrc& src, int v, double* hs, double* R) {
+  if (src.sizes) {
+    for (int k = 0; k < 3; ++k) hs[k] = src.sizes[3 * (size_t)v + k];
+    for (int k = 0; k < 9; ++k) R[k] = src.frames[9 * (size_t)v + k];
+    return;
+  }
+  double Rm[3][3];
+  hessian_metric_vertex(src.dim, src.H + 9 * (size_t)v, src.eps, src.hmin, src.hmax, hs, Rm);
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) R[3 * i + j] = Rm[i][j];
 }
 
 // ---------------------------------------------------------------------
@@ -1786,6 +1815,81 @@ __global__ void __launch_bounds__(kBlock) k_metric_f32(int V, int dim, const dou
   qrec[v] = r;
 }
 
+// Mixed pass on triangles: the FP32 metric records and quality records
+// straight from the FP64 Hessian.  Every decision of hessian_metric_vertex
+// (the b == 0 and a >= c branches, the |lambda| order, the sign convention)
+// is taken on the same FP64 values, with the one FP64 square root it needs
+// (the eigenvalue gap); the magnitudes that follow (the direction's
+// normalisation, sqrt(eps / |lambda|)) are FP32 operations on those values,
+// a few ulps from the FP64 results, inside the FP32 measure's bound.  The
+// sign test runs on the unnormalised FP64 direction (the normalisation by a
+// positive length keeps signs and zeros).
+__global__ void __launch_bounds__(kBlock) k_metric_mixed2d(int V, const double* __restrict__ H, double eps,
+                                                           double hmin, double hmax, float* __restrict__ out,
+                                                           QualityRec* __restrict__ qrec) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= V) return;
+  const double* h = H + 9 * (size_t)v;
+  const double a = h[0], b = 0.5 * (h[1] + h[3]), c = h[4];
+  const double mid = 0.5 * (a + c), hd = 0.5 * (a - c);
+  const double d = sqrt(hd * hd + b * b);
+  double l1 = mid + d, l2 = mid - d;
+  double x, y;
+  if (b == 0.0) {
+    x = a >= c ? 1.0 : 0.0;
+    y = a >= c ? 0.0 : 1.0;
+  } else if (a >= c) {
+    x = l1 - c;
+    y = b;
+  } else {
+    x = b;
+    y = l1 - a;
+  }
+  if (fabs(l2) > fabs(l1)) {
+    const double tl = l1;
+    l1 = l2;
+    l2 = tl;
+    const double tx = x;
+    x = -y;
+    y = tx;
+  }
+  if (x < 0 || (x == 0 && y < 0)) {
+    x = -x;
+    y = -y;
+  }
+  // scale by a power of two into FP32 range (exact), then normalise in FP32
+  // 2^-e with e the exponent of max(|x|, |y|) (> 0: one of them is b != 0
+  // or l1 - c > 0), built from the exponent bits; a subnormal maximum takes
+  // 2^1022, the top binade 2^-1022
+  const double ax = fmax(fabs(x), fabs(y));
+  const long long eb = (__double_as_longlong(ax) >> 52) & 0x7ff;
+  const long long sb = eb == 0 ? 2045 : (eb < 2046 ? 2046 - eb : 1);
+  const double sc = __longlong_as_double(sb << 52);
+  float xf = (float)(x * sc), yf = (float)(y * sc);
+  const float nf = sqrtf(xf * xf + yf * yf);
+  xf /= nf;
+  yf /= nf;
+  const float epsf = (float)eps, hminf = (float)hmin, hmaxf = (float)hmax;
+  auto size_f32 = [&](double l) {
+    if (!(fabs(l) > 0)) return hmaxf;
+    return fminf(fmaxf(sqrtf(epsf / fabsf((float)l)), hminf), hmaxf);
+  };
+  float* o = out + 12 * (size_t)v;
+  o[0] = size_f32(l1);
+  o[1] = size_f32(l2);
+  o[2] = hmaxf;
+  o[3] = xf; o[4] = -yf; o[5] = 0.f;
+  o[6] = yf; o[7] = xf;  o[8] = 0.f;
+  o[9] = 0.f; o[10] = 0.f; o[11] = 1.f;
+  float Q[3][3];
+  transform_f32(o, o + 3, Q);
+  QualityRec r;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) r.q[3 * i + j] = Q[i][j];
+  r.cj = det_f32(Q, 2);
+  qrec[v] = r;
+}
+
 // AnisoSizeField measure in FP32 with a relative error bound.  Per Gauss
 // point: R(xi) interpolated and orthogonalised, dV = |(J.r_j / h_j)_j|.  Each
 // term J.r_j / h_j carries an absolute error of a few units of |J| / h_j
@@ -1874,8 +1978,7 @@ __global__ void __launch_bounds__(kBlock) k_measure_aniso_f32(DevMesh m, const f
 }
 
 // the guarded edges re-measured by the FP64 kernel's arithmetic
-__global__ void __launch_bounds__(kBlock) k_measure_guard_f64(DevMesh m, const double* __restrict__ sizes,
-                                                              const double* __restrict__ frames,
+__global__ void __launch_bounds__(kBlock) k_measure_guard_f64(DevMesh m, MetricSrc src,
                                                               const int* __restrict__ guard,
                                                               const int* __restrict__ gcount, int gcap,
                                                               uint32_t* __restrict__ split,
@@ -1886,10 +1989,7 @@ __global__ void __launch_bounds__(kBlock) k_measure_guard_f64(DevMesh m, const d
     const int e = guard[i];
     const int vv[2] = {m.edv[2 * (size_t)e], m.edv[2 * (size_t)e + 1]};
     double hv[6], Rv[18];
-    for (int a = 0; a < 2; ++a) {
-      for (int k = 0; k < 3; ++k) hv[3 * a + k] = sizes[3 * (size_t)vv[a] + k];
-      for (int k = 0; k < 9; ++k) Rv[9 * a + k] = frames[9 * (size_t)vv[a] + k];
-    }
+    for (int a = 0; a < 2; ++a) metric_at(src, vv[a], hv + 3 * a, Rv + 9 * a);
     const double L = metric_length(load_xyz(m.xyz, vv[0]), load_xyz(m.xyz, vv[1]), hv, Rv);
     const uint32_t bit = 1u << (e & 31);
     if (L > 1.5) atomicOr(split + (e >> 5), bit);
@@ -1936,9 +2036,34 @@ __device__ __forceinline__ float quality_with_f32(const DevMesh& m, const double
 // is the reference's value to the FP32 accuracy
 constexpr float kDetTie = 1e-5f, kQualTie = 4e-6f;
 
+// element e's vertex coordinates and FP32 determinant pick: best (the first
+// largest, as the reference picks) and the candidates the FP32 determinants
+// cannot rule out
+__device__ __forceinline__ int quality_pick_f32(const DevMesh& m, const QualityRec* __restrict__ qrec, const int* ev,
+                                                unsigned* cand) {
+  float cj[4];
+  int best = 0;
+  for (int i = 0; i < m.nn; ++i) {
+    cj[i] = qrec[ev[i]].cj;
+    if (cj[i] > cj[best]) best = i;
+  }
+  unsigned c = 0;
+  for (int i = 0; i < m.nn; ++i)
+    if (cj[i] * (1.f + kDetTie) >= cj[best]) c |= 1u << i;
+  *cand = c;
+  return best;
+}
+
+__device__ __forceinline__ void load_qrec(const QualityRec& r, float (*T)[3]) {
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b) T[a][b] = r.q[3 * a + b];
+}
+
+// FP32 qualities.  Elements whose candidate vertices give qualities that
+// differ by more than kQualTie are listed for k_quality_ties (FP64
+// determinants decide there); their entry here is the FP32 pick's quality.
 __global__ void __launch_bounds__(kBlock) k_quality_aniso_f32(DevMesh m, const QualityRec* __restrict__ qrec,
-                                                              const double* __restrict__ sizes,
-                                                              const double* __restrict__ frames,
+                                                              int* __restrict__ tie_items, int* __restrict__ tie_count,
                                                               double* __restrict__ q) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= m.T) return;
@@ -1948,53 +2073,72 @@ __global__ void __launch_bounds__(kBlock) k_quality_aniso_f32(DevMesh m, const Q
     for (int k = 0; k < 3; ++k) x[a][k] = m.xyz[3 * (size_t)ev[a] + k];
   // getMetricWithMaxJacobean (ma/maQuality.cc:83-108): the first vertex with
   // the largest determinant
-  float cj[4];
-  int best = 0;
-  for (int i = 0; i < m.nn; ++i) {
-    cj[i] = qrec[ev[i]].cj;
-    if (cj[i] > cj[best]) best = i;
-  }
-  unsigned cand = 0;  // vertices the FP32 determinants cannot rule out
-  for (int i = 0; i < m.nn; ++i)
-    if (cj[i] * (1.f + kDetTie) >= cj[best]) cand |= 1u << i;
+  unsigned cand;
+  const int best = quality_pick_f32(m, qrec, ev, &cand);
   float Q[3][3];
-  auto load_q = [&](int i, float (*T)[3]) {
-    const QualityRec& r = qrec[ev[i]];
-    for (int a = 0; a < 3; ++a)
-      for (int b = 0; b < 3; ++b) T[a][b] = r.q[3 * a + b];
-  };
-  load_q(best, Q);
-  float res = quality_with_f32(m, x, Q);
+  load_qrec(qrec[ev[best]], Q);
+  const float res = quality_with_f32(m, x, Q);
+  bool tie = false;
   if (cand != (1u << best)) {
-    bool agree = true;
     for (int i = 0; i < m.nn; ++i) {
       if (!(cand >> i & 1) || i == best) continue;
       float T[3][3];
-      load_q(i, T);
+      load_qrec(qrec[ev[i]], T);
       const float qi = quality_with_f32(m, x, T);
-      if (!(fabsf(qi - res) <= kQualTie * fabsf(res))) agree = false;
-    }
-    if (!agree) {  // the FP64 determinants decide, in the reference's order
-      double maxJ = -1.0;
-      int pick = best;
-      for (int i = 0; i < m.nn; ++i) {
-        double hv[3], Rv[9];
-        for (int k = 0; k < 3; ++k) hv[k] = sizes[3 * (size_t)ev[i] + k];
-        for (int k = 0; k < 9; ++k) Rv[k] = frames[9 * (size_t)ev[i] + k];
-        const double N[1] = {1.0};
-        const double cJ = ref::jacobian_det(ref::get_transform(hv, Rv, N, 1), m.dim);
-        if (cJ > maxJ) {
-          maxJ = cJ;
-          pick = i;
-        }
-      }
-      if (pick != best) {
-        load_q(pick, Q);
-        res = quality_with_f32(m, x, Q);
-      }
+      if (!(fabsf(qi - res) <= kQualTie * fabsf(res))) tie = true;
     }
   }
   q[e] = res;
+  // list the ties, one counter atomic per warp
+  const unsigned act = __activemask();
+  const unsigned bal = __ballot_sync(act, tie);
+  if (bal) {
+    const int lane = threadIdx.x & 31, leader = __ffs(bal) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(tie_count, __popc(bal));
+    base = __shfl_sync(act, base, leader);
+    if (tie) tie_items[base + __popc(bal & ((1u << lane) - 1))] = e;
+  }
+}
+
+// The listed ties: the FP64 determinants of the FP64 quality kernel's
+// arithmetic pick the vertex, in the reference's order.  cj64: per-vertex
+// FP64 determinants of this pass, NaN until first needed (concurrent
+// writers store the same bits).
+__global__ void __launch_bounds__(kBlock) k_quality_ties(DevMesh m, const QualityRec* __restrict__ qrec, MetricSrc src,
+                                                         double* __restrict__ cj64, const int* __restrict__ tie_items,
+                                                         const int* __restrict__ tie_count, double* __restrict__ q) {
+  const int n = *tie_count;
+  for (int i0 = blockIdx.x * blockDim.x + threadIdx.x; i0 < n; i0 += gridDim.x * blockDim.x) {
+    const int e = tie_items[i0];
+    const int* ev = m.ev + (size_t)e * m.nn;
+    unsigned cand;
+    const int best = quality_pick_f32(m, qrec, ev, &cand);
+    double maxJ = -1.0;
+    int pick = best;
+    for (int i = 0; i < m.nn; ++i) {
+      double cJ = cj64[ev[i]];
+      if (cJ != cJ) {
+        double hv[3], Rv[9];
+        metric_at(src, ev[i], hv, Rv);
+        const double N[1] = {1.0};
+        cJ = ref::jacobian_det(ref::get_transform(hv, Rv, N, 1), m.dim);
+        cj64[ev[i]] = cJ;
+      }
+      if (cJ > maxJ) {
+        maxJ = cJ;
+        pick = i;
+      }
+    }
+    if (pick != best) {
+      double x[4][3];
+      for (int a = 0; a < m.nn; ++a)
+        for (int k = 0; k < 3; ++k) x[a][k] = m.xyz[3 * (size_t)ev[a] + k];
+      float Q[3][3];
+      load_qrec(qrec[ev[pick]], Q);
+      q[e] = quality_with_f32(m, x, Q);
+    }
+  }
 }
 
 
@@ -2457,17 +2601,30 @@ void launch_measure_aniso_f32(const DevMesh& m, const float* met, uint32_t* spli
   if (m.E) k_measure_aniso_f32<<<nblk(m.E), kBlock, 0, s>>>(m, met, split, collapse, guard, gcount, gcap);
 }
 
-void launch_measure_guard_f64(const DevMesh& m, const double* sizes, const double* frames, const int* guard,
-                              const int* gcount, int gcap, uint32_t* split, uint32_t* collapse, cudaStream_t s) {
-  k_measure_guard_f64<<<152 * 4, kBlock, 0, s>>>(m, sizes, frames, guard, gcount, gcap, split, collapse);
+void launch_measure_guard_f64(const DevMesh& m, const double* sizes, const double* frames, const double* H,
+                              double eps, double hmin, double hmax, const int* guard, const int* gcount, int gcap,
+                              uint32_t* split, uint32_t* collapse, cudaStream_t s) {
+  const MetricSrc src{sizes, frames, H, m.dim, eps, hmin, hmax};
+  k_measure_guard_f64<<<152 * 4, kBlock, 0, s>>>(m, src, guard, gcount, gcap, split, collapse);
+}
+
+void launch_metric_mixed2d(int V, const double* H, double eps, double hmin, double hmax, float* out, void* qrec,
+                           cudaStream_t s) {
+  if (V) k_metric_mixed2d<<<nblk(V), kBlock, 0, s>>>(V, H, eps, hmin, hmax, out, static_cast<QualityRec*>(qrec));
 }
 
 int quality_rec_bytes() { return (int)sizeof(QualityRec); }
 
-void launch_quality_aniso_f32(const DevMesh& m, const void* qrec, const double* sizes, const double* frames, double* q,
-                              cudaStream_t s) {
-  if (m.T)
-    k_quality_aniso_f32<<<nblk(m.T), kBlock, 0, s>>>(m, static_cast<const QualityRec*>(qrec), sizes, frames, q);
+void launch_quality_aniso_f32(const DevMesh& m, const void* qrec, const double* sizes, const double* frames,
+                              const double* H, double eps, double hmin, double hmax, double* cj64, int* tie_items,
+                              int* tie_count, double* q, cudaStream_t s) {
+  const MetricSrc src{sizes, frames, H, m.dim, eps, hmin, hmax};
+  if (!m.T) return;
+  const QualityRec* r = static_cast<const QualityRec*>(qrec);
+  cudaMemsetAsync(cj64, 0xff, sizeof(double) * (size_t)m.V, s);  // all NaN
+  cudaMemsetAsync(tie_count, 0, sizeof(int), s);
+  k_quality_aniso_f32<<<nblk(m.T), kBlock, 0, s>>>(m, r, tie_items, tie_count, q);
+  k_quality_ties<<<152 * 8, kBlock, 0, s>>>(m, r, src, cj64, tie_items, tie_count, q);
 }
 
 int tri_operator_slots() { return kOpSlots; }
