@@ -105,6 +105,7 @@ struct sprg_ctx {
   HostStage* stage = nullptr;
   int pass_id = 0;
   bool vrec_ready = false;  // coordinate records and SPR weights (per mesh)
+  bool crec_ready = false;  // coordinate records alone (the mixed anisotropic pass)
   double frame[4] = {0, 0, 0, 1};  // coordinate records: x' = (x - c) s + 1 in [1, 2]
   int n_listed = 0, n_refit = 0;
   PatchCache cache64, cache32, cache2d;
@@ -634,6 +635,7 @@ int sprg_create(const sprg_mesh_view* mv, int device, sprg_ctx** out) {
 static void invalidate_mesh_state(sprg_ctx* c) {
   c->ip_valid = c->size_valid = c->L_valid = c->q_valid = false;
   c->vrec_ready = false;
+  c->crec_ready = false;
   c->bins_ready = false;
   c->tuned = false;
   c->tw_ready = false;
@@ -1266,6 +1268,7 @@ static int fast_setup(sprg_ctx* c, ExpandList xl) {
   ENSURE(c->elen, 4 * (size_t)m.E);
   CK(cudaMemsetAsync(c->fcnt.p, 0, 8 * sizeof(int), c->stream));
   fast_prep_coords(m, c->frame, P<float4>(c->crec), c->stream);
+  c->crec_ready = true;
   fast_geometry(m, P<float2>(c->geo), P<double2>(c->geo64), P<float>(c->elen), c->stream);
   fast_weights(m, P<float>(c->wts), P<double>(c->w64), xl, P<int>(c->fcnt), P<unsigned char>(c->listed), c->stream);
   int h[2] = {0, 0};
@@ -2003,6 +2006,12 @@ static int aniso_pass_mixed(sprg_ctx* c, double eps, double h_min, double h_max,
   }
   ENSURE(c->met32, sizeof(float) * 12 * (size_t)(m.V > 0 ? m.V : 1));
   ENSURE(c->qrec32, (size_t)quality_rec_bytes() * (size_t)(m.V > 0 ? m.V : 1));
+  if (!c->crec_ready) {  // the coordinate records of the edge and element Jacobians (per mesh)
+    ENSURE(c->crec, 32 * (size_t)(m.V > 0 ? m.V : 1));
+    fast_prep_coords(m, c->frame, P<float4>(c->crec), c->stream);
+    c->launches += 1;
+    c->crec_ready = true;
+  }
   ENSURE(c->agitems, sizeof(int) * (size_t)(m.E > 0 ? m.E : 1));
   ENSURE(c->agcount, sizeof(int));
   CK(cudaMemsetAsync(c->agcount.p, 0, sizeof(int), c->stream));
@@ -2027,8 +2036,8 @@ static int aniso_pass_mixed(sprg_ctx* c, double eps, double h_min, double h_max,
     frames64 = P<double>(c->frames9);
   }
   PB("measure_aniso_f32");
-  launch_measure_aniso_f32(m, P<float>(c->met32), d_split_bits, d_collapse_bits, P<int>(c->agitems),
-                           P<int>(c->agcount), m.E, c->stream);
+  launch_measure_aniso_f32(m, P<float>(c->met32), P<float4>(c->crec), c->frame[3], d_split_bits, d_collapse_bits,
+                           P<int>(c->agitems), P<int>(c->agcount), m.E, c->stream);
   PE();
   PB("guard_measure_f64");
   launch_measure_guard_f64(m, sizes64, frames64, H, eps, h_min, h_max, P<int>(c->agitems), P<int>(c->agcount), m.E,
@@ -2039,8 +2048,8 @@ static int aniso_pass_mixed(sprg_ctx* c, double eps, double h_min, double h_max,
     PB("quality_f32");
     ENSURE(c->cj64, sizeof(double) * (size_t)(m.V > 0 ? m.V : 1));
     ENSURE(c->qties, sizeof(int) * ((size_t)m.T + 1));
-    launch_quality_aniso_f32(m, c->qrec32.p, sizes64, frames64, H, eps, h_min, h_max, P<double>(c->cj64),
-                             P<int>(c->qties) + 1, P<int>(c->qties), d_quality, c->stream);
+    launch_quality_aniso_f32(m, c->qrec32.p, P<float4>(c->crec), c->frame[3], sizes64, frames64, H, eps, h_min,
+                             h_max, P<double>(c->cj64), P<int>(c->qties) + 1, P<int>(c->qties), d_quality, c->stream);
     PE();
     c->launches += 2;
   }

@@ -159,8 +159,10 @@ void launch_tri_weights(const DevMesh& m, double* w, unsigned char* listed, Expa
 void launch_metric_f32(int V, int dim, const double* sizes, const double* frames, float* out, void* qrec,
                        cudaStream_t s);
 int quality_rec_bytes();
-void launch_measure_aniso_f32(const DevMesh& m, const float* met, uint32_t* split, uint32_t* collapse, int* guard,
-                              int* gcount, int gcap, cudaStream_t s);
+// crec: the FP32 path's coordinate records in the frame x' = (x - c) s + 1
+// (frame_scale = s)
+void launch_measure_aniso_f32(const DevMesh& m, const float* met, const float4* crec, double frame_scale,
+                              uint32_t* split, uint32_t* collapse, int* guard, int* gcount, int gcap, cudaStream_t s);
 // sizes / frames: the FP64 metric, or null to rebuild the guarded edges'
 // ends from the Hessian H (hessian_metric_vertex, the FP64 pass's bits)
 void launch_measure_guard_f64(const DevMesh& m, const double* sizes, const double* frames, const double* H,
@@ -170,9 +172,9 @@ void launch_measure_guard_f64(const DevMesh& m, const double* sizes, const doubl
 // two launches: FP32 qualities (listing the elements whose vertex pick the
 // FP32 determinants leave open), then the FP64 tie-breaks; cj64: V doubles,
 // tie_items: T ints, tie_count: one int (scratch, cleared here)
-void launch_quality_aniso_f32(const DevMesh& m, const void* qrec, const double* sizes, const double* frames,
-                              const double* H, double eps, double hmin, double hmax, double* cj64, int* tie_items,
-                              int* tie_count, double* q, cudaStream_t s);
+void launch_quality_aniso_f32(const DevMesh& m, const void* qrec, const float4* crec, double frame_scale,
+                              const double* sizes, const double* frames, const double* H, double eps, double hmin,
+                              double hmax, double* cj64, int* tie_items, int* tie_count, double* q, cudaStream_t s);
 // triangles: FP32 metric records (12 floats) and quality records straight
 // from the Hessian (FP64 decisions, FP32 magnitudes)
 void launch_metric_mixed2d(int V, const double* H, double eps, double hmin, double hmax, float* out, void* qrec,

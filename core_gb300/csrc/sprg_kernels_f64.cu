@@ -1928,7 +1928,13 @@ __device__ __forceinline__ float aniso_dv_f32(float Jx, float Jy, float Jz, cons
   return dv;
 }
 
+// crec: the FP32 path's coordinate records (per vertex {x,y,z}_hi then
+// {x,y,z}_lo, coordinates mapped into [1, 2] by x' = (x - c) s + 1), so the
+// edge Jacobian J = (x_b - x_a) / 2 = ((hi_b - hi_a) + (lo_b - lo_a)) 0.5 / s
+// comes out of exact high-word differences with one rounding, without FP64
+// arithmetic; jscale = 0.5 / s (a power of two)
 __global__ void __launch_bounds__(kBlock) k_measure_aniso_f32(DevMesh m, const float* __restrict__ met,
+                                                              const float4* __restrict__ crec, float jscale,
                                                               uint32_t* __restrict__ split,
                                                               uint32_t* __restrict__ collapse,
                                                               int* __restrict__ guard, int* __restrict__ gcount,
@@ -1937,10 +1943,12 @@ __global__ void __launch_bounds__(kBlock) k_measure_aniso_f32(DevMesh m, const f
   bool sp = false, co = false, g = false;
   if (e < m.E) {
     const int a = m.edv[2 * (size_t)e], b = m.edv[2 * (size_t)e + 1];
-    // J = x_b / 2 - x_a / 2 in FP64 (the reference's edge Jacobian), then rounded
-    const float Jx = (float)(0.5 * m.xyz[3 * (size_t)b] - 0.5 * m.xyz[3 * (size_t)a]);
-    const float Jy = (float)(0.5 * m.xyz[3 * (size_t)b + 1] - 0.5 * m.xyz[3 * (size_t)a + 1]);
-    const float Jz = (float)(0.5 * m.xyz[3 * (size_t)b + 2] - 0.5 * m.xyz[3 * (size_t)a + 2]);
+    // J = x_b / 2 - x_a / 2 (the reference's edge Jacobian) to half an ulp
+    const float4 ha = __ldg(crec + 2 * (size_t)a), la = __ldg(crec + 2 * (size_t)a + 1);
+    const float4 hb = __ldg(crec + 2 * (size_t)b), lb = __ldg(crec + 2 * (size_t)b + 1);
+    const float Jx = ((hb.x - ha.x) + (lb.x - la.x)) * jscale;
+    const float Jy = ((hb.y - ha.y) + (lb.y - la.y)) * jscale;
+    const float Jz = ((hb.z - ha.z) + (lb.z - la.z)) * jscale;
     float ma[12], mb[12];
 #pragma unroll
     for (int k = 0; k < 12; ++k) {
@@ -2001,33 +2009,47 @@ __global__ void __launch_bounds__(kBlock) k_measure_guard_f64(DevMesh m, MetricS
 
 // mean-ratio quality under the anisotropic metric in FP32 (the vertex
 // transform with the largest determinant, ma/maQuality.cc:83-167)
-// FP32 mean-ratio quality of element e under transform Q
-__device__ __forceinline__ float quality_with_f32(const DevMesh& m, const double (*x)[3], const float Q[3][3]) {
-  auto mvec = [&](int r, int p, float* t) {
-    float d[3];
-    for (int k = 0; k < 3; ++k) d[k] = (float)(x[r][k] - x[p][k]);
-    for (int c = 0; c < 3; ++c) t[c] = d[0] * Q[0][c] + d[1] * Q[1][c] + d[2] * Q[2][c];
-  };
-  float s = 0.f;
-  for (int i = 0; i < m.ne_el; ++i) {
-    float t[3];
-    mvec(m.dim == 3 ? c_tet_edges[i][1] : c_tri_edges[i][1], m.dim == 3 ? c_tet_edges[i][0] : c_tri_edges[i][0], t);
-    s += t[0] * t[0] + t[1] * t[1] + t[2] * t[2];
-  }
-  float a0[3], a1[3];
-  mvec(1, 0, a0);
-  mvec(2, 0, a1);
-  const float cx = a0[1] * a1[2] - a0[2] * a1[1], cy = a0[2] * a1[0] - a0[0] * a1[2],
-              cz = a0[0] * a1[1] - a0[1] * a1[0];
+// FP32 mean-ratio quality of an element under transform Q, from its edge
+// vectors E[k] = x_{k+1} - x_0 (FP64 differences rounded to FP32 once per
+// element): t_k = Q^T E_k, the element's edges map to t_1, t_2 - t_1, -t_2
+// (and t_3, t_3 - t_1, t_3 - t_2 on tets), the volume to det(t_1, t_2, t_3)
+__device__ __forceinline__ float quality_with_f32(const DevMesh& m, const float (*E)[3], const float Q[3][3]) {
+  float t[3][3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) t[k][c] = E[k][0] * Q[0][c] + E[k][1] * Q[1][c] + E[k][2] * Q[2][c];
+  auto n2 = [](float x, float y, float z) { return x * x + y * y + z * z; };
+  float s = n2(t[0][0], t[0][1], t[0][2]) + n2(t[1][0] - t[0][0], t[1][1] - t[0][1], t[1][2] - t[0][2]) +
+            n2(t[1][0], t[1][1], t[1][2]);
+  const float cx = t[0][1] * t[1][2] - t[0][2] * t[1][1], cy = t[0][2] * t[1][0] - t[0][0] * t[1][2],
+              cz = t[0][0] * t[1][1] - t[0][1] * t[1][0];
   if (m.dim == 3) {
-    float a2[3];
-    mvec(3, 0, a2);
-    const float Vm = (cx * a2[0] + cy * a2[1] + cz * a2[2]) / 6.f;  // det(J Q) / 6
+    s += n2(t[2][0], t[2][1], t[2][2]) + n2(t[2][0] - t[0][0], t[2][1] - t[0][1], t[2][2] - t[0][2]) +
+         n2(t[2][0] - t[1][0], t[2][1] - t[1][1], t[2][2] - t[1][2]);
+    const float Vm = (cx * t[2][0] + cy * t[2][1] + cz * t[2][2]) / 6.f;  // det(J Q) / 6
     const float res = 15552.f * (Vm * Vm) / (s * s * s);
     return Vm < 0 ? -res : res;
   }
   const float A = 0.5f * sqrtf(cx * cx + cy * cy + cz * cz);
   return 48.f * (A * A) / (s * s);
+}
+
+// the element's edge vectors from vertex 0 out of the coordinate records
+// (exact high-word differences plus the low words' difference, one
+// rounding; escale = 1 / s)
+__device__ __forceinline__ void elem_edges_f32(const DevMesh& m, const float4* __restrict__ crec, float escale,
+                                               const int* ev, float (*E)[3]) {
+  const float4 h0 = __ldg(crec + 2 * (size_t)ev[0]), l0 = __ldg(crec + 2 * (size_t)ev[0] + 1);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const bool in = k < m.nn - 1;  // triangles: E[2] = 0
+    const float4 hk = in ? __ldg(crec + 2 * (size_t)ev[k + 1]) : h0;
+    const float4 lk = in ? __ldg(crec + 2 * (size_t)ev[k + 1] + 1) : l0;
+    E[k][0] = ((hk.x - h0.x) + (lk.x - l0.x)) * escale;
+    E[k][1] = ((hk.y - h0.y) + (lk.y - l0.y)) * escale;
+    E[k][2] = ((hk.z - h0.z) + (lk.z - l0.z)) * escale;
+  }
 }
 
 // relative separation of FP32 determinants taken as certain (their error
@@ -2043,13 +2065,19 @@ __device__ __forceinline__ int quality_pick_f32(const DevMesh& m, const QualityR
                                                 unsigned* cand) {
   float cj[4];
   int best = 0;
-  for (int i = 0; i < m.nn; ++i) {
-    cj[i] = qrec[ev[i]].cj;
-    if (cj[i] > cj[best]) best = i;
+  float cb = 0.f;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    cj[i] = i < m.nn ? qrec[ev[i]].cj : 0.f;
+    if (i < m.nn && (i == 0 || cj[i] > cb)) {
+      best = i;
+      cb = cj[i];
+    }
   }
   unsigned c = 0;
-  for (int i = 0; i < m.nn; ++i)
-    if (cj[i] * (1.f + kDetTie) >= cj[best]) c |= 1u << i;
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+    if (i < m.nn && cj[i] * (1.f + kDetTie) >= cb) c |= 1u << i;
   *cand = c;
   return best;
 }
@@ -2063,28 +2091,28 @@ __device__ __forceinline__ void load_qrec(const QualityRec& r, float (*T)[3]) {
 // differ by more than kQualTie are listed for k_quality_ties (FP64
 // determinants decide there); their entry here is the FP32 pick's quality.
 __global__ void __launch_bounds__(kBlock) k_quality_aniso_f32(DevMesh m, const QualityRec* __restrict__ qrec,
+                                                              const float4* __restrict__ crec, float escale,
                                                               int* __restrict__ tie_items, int* __restrict__ tie_count,
                                                               double* __restrict__ q) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= m.T) return;
   const int* ev = m.ev + (size_t)e * m.nn;
-  double x[4][3];
-  for (int a = 0; a < m.nn; ++a)
-    for (int k = 0; k < 3; ++k) x[a][k] = m.xyz[3 * (size_t)ev[a] + k];
+  float E[3][3];
+  elem_edges_f32(m, crec, escale, ev, E);
   // getMetricWithMaxJacobean (ma/maQuality.cc:83-108): the first vertex with
   // the largest determinant
   unsigned cand;
   const int best = quality_pick_f32(m, qrec, ev, &cand);
   float Q[3][3];
   load_qrec(qrec[ev[best]], Q);
-  const float res = quality_with_f32(m, x, Q);
+  const float res = quality_with_f32(m, E, Q);
   bool tie = false;
   if (cand != (1u << best)) {
     for (int i = 0; i < m.nn; ++i) {
       if (!(cand >> i & 1) || i == best) continue;
       float T[3][3];
       load_qrec(qrec[ev[i]], T);
-      const float qi = quality_with_f32(m, x, T);
+      const float qi = quality_with_f32(m, E, T);
       if (!(fabsf(qi - res) <= kQualTie * fabsf(res))) tie = true;
     }
   }
@@ -2106,6 +2134,7 @@ __global__ void __launch_bounds__(kBlock) k_quality_aniso_f32(DevMesh m, const Q
 // FP64 determinants of this pass, NaN until first needed (concurrent
 // writers store the same bits).
 __global__ void __launch_bounds__(kBlock) k_quality_ties(DevMesh m, const QualityRec* __restrict__ qrec, MetricSrc src,
+                                                         const float4* __restrict__ crec, float escale,
                                                          double* __restrict__ cj64, const int* __restrict__ tie_items,
                                                          const int* __restrict__ tie_count, double* __restrict__ q) {
   const int n = *tie_count;
@@ -2131,12 +2160,11 @@ __global__ void __launch_bounds__(kBlock) k_quality_ties(DevMesh m, const Qualit
       }
     }
     if (pick != best) {
-      double x[4][3];
-      for (int a = 0; a < m.nn; ++a)
-        for (int k = 0; k < 3; ++k) x[a][k] = m.xyz[3 * (size_t)ev[a] + k];
+      float E[3][3];
+      elem_edges_f32(m, crec, escale, ev, E);
       float Q[3][3];
       load_qrec(qrec[ev[pick]], Q);
-      q[e] = quality_with_f32(m, x, Q);
+      q[e] = quality_with_f32(m, E, Q);
     }
   }
 }
@@ -2596,9 +2624,11 @@ void launch_metric_f32(int V, int dim, const double* sizes, const double* frames
   if (V) k_metric_f32<<<nblk(V), kBlock, 0, s>>>(V, dim, sizes, frames, out, static_cast<QualityRec*>(qrec));
 }
 
-void launch_measure_aniso_f32(const DevMesh& m, const float* met, uint32_t* split, uint32_t* collapse, int* guard,
-                              int* gcount, int gcap, cudaStream_t s) {
-  if (m.E) k_measure_aniso_f32<<<nblk(m.E), kBlock, 0, s>>>(m, met, split, collapse, guard, gcount, gcap);
+void launch_measure_aniso_f32(const DevMesh& m, const float* met, const float4* crec, double frame_scale,
+                              uint32_t* split, uint32_t* collapse, int* guard, int* gcount, int gcap, cudaStream_t s) {
+  const float jscale = (float)(0.5 / frame_scale);
+  if (m.E)
+    k_measure_aniso_f32<<<nblk(m.E), kBlock, 0, s>>>(m, met, crec, jscale, split, collapse, guard, gcount, gcap);
 }
 
 void launch_measure_guard_f64(const DevMesh& m, const double* sizes, const double* frames, const double* H,
@@ -2615,16 +2645,17 @@ void launch_metric_mixed2d(int V, const double* H, double eps, double hmin, doub
 
 int quality_rec_bytes() { return (int)sizeof(QualityRec); }
 
-void launch_quality_aniso_f32(const DevMesh& m, const void* qrec, const double* sizes, const double* frames,
-                              const double* H, double eps, double hmin, double hmax, double* cj64, int* tie_items,
-                              int* tie_count, double* q, cudaStream_t s) {
+void launch_quality_aniso_f32(const DevMesh& m, const void* qrec, const float4* crec, double frame_scale,
+                              const double* sizes, const double* frames, const double* H, double eps, double hmin,
+                              double hmax, double* cj64, int* tie_items, int* tie_count, double* q, cudaStream_t s) {
   const MetricSrc src{sizes, frames, H, m.dim, eps, hmin, hmax};
   if (!m.T) return;
   const QualityRec* r = static_cast<const QualityRec*>(qrec);
+  const float escale = (float)(1.0 / frame_scale);
   cudaMemsetAsync(cj64, 0xff, sizeof(double) * (size_t)m.V, s);  // all NaN
   cudaMemsetAsync(tie_count, 0, sizeof(int), s);
-  k_quality_aniso_f32<<<nblk(m.T), kBlock, 0, s>>>(m, r, tie_items, tie_count, q);
-  k_quality_ties<<<152 * 8, kBlock, 0, s>>>(m, r, src, cj64, tie_items, tie_count, q);
+  k_quality_aniso_f32<<<nblk(m.T), kBlock, 0, s>>>(m, r, crec, escale, tie_items, tie_count, q);
+  k_quality_ties<<<152 * 8, kBlock, 0, s>>>(m, r, src, crec, escale, cj64, tie_items, tie_count, q);
 }
 
 int tri_operator_slots() { return kOpSlots; }
