@@ -58,6 +58,7 @@ struct sprg_ctx {
   // listed vertices (per mesh), FP32 metric records, guarded edges
   DevBuf tw, twlisted, twitems, twcount, met32, qrec32, agitems, agcount, kidx, kval, klen, rec9, cj64, qties;
   bool tw_ready = false;
+  int op_kc = 3;  // operator components per slot (2 on a mesh in the z = 0 plane)
   // FP32 path buffers
   DevBuf crec, vrec, rec32, q32, sz2, fcnt, guard, tetd, wts, w64, listed, geo, geo64, elen, fitems;
   DevBuf gstamp, gfit, grec;  // guard pipeline scratch
@@ -107,6 +108,7 @@ struct sprg_ctx {
   bool vrec_ready = false;  // coordinate records and SPR weights (per mesh)
   bool crec_ready = false;  // coordinate records alone (the mixed anisotropic pass)
   double frame[4] = {0, 0, 0, 1};  // coordinate records: x' = (x - c) s + 1 in [1, 2]
+  bool planar = false;             // every vertex has z = 0
   int n_listed = 0, n_refit = 0;
   PatchCache cache64, cache32, cache2d;
   static constexpr int kGuardCap = 1 << 20;
@@ -507,6 +509,7 @@ static void set_frame(sprg_ctx* c, const double* lo, const double* hi) {
   c->frame[1] = lo[1];
   c->frame[2] = lo[2];
   c->frame[3] = s;
+  c->planar = lo[2] == 0.0 && hi[2] == 0.0;
 }
 
 // index arrays must stay inside the entity counts: a bad id would reach
@@ -1956,14 +1959,15 @@ static int hessian_operator_2d(sprg_ctx* c) {
     ENSURE(c->tw, sizeof(double) * (size_t)m.T * m.nn);
     ENSURE(c->twlisted, (size_t)(m.V > 0 ? m.V : 1));
     ENSURE(c->kidx, sizeof(int) * (size_t)m.V * ks);
-    ENSURE(c->kval, sizeof(double) * 3 * (size_t)m.V * ks);
+    c->op_kc = c->planar ? 2 : 3;
+    ENSURE(c->kval, sizeof(double) * c->op_kc * (size_t)m.V * ks);
     ENSURE(c->klen, sizeof(int) * (size_t)(m.V > 0 ? m.V : 1));
     CK(cudaMemsetAsync(c->twcount.p, 0, sizeof(int), c->stream));
     PB("tri_weights_f64");
     launch_tri_weights(m, P<double>(c->tw), P<unsigned char>(c->twlisted), lst, c->stream);
     PE();
     PB("tri_operator_f64");
-    launch_tri_operator(m, P<double>(c->tw), P<unsigned char>(c->twlisted), lst, P<int>(c->kidx),
+    launch_tri_operator(m, c->op_kc, P<double>(c->tw), P<unsigned char>(c->twlisted), lst, P<int>(c->kidx),
                         P<double>(c->kval), P<int>(c->klen), c->stream);
     PE();
     c->launches += 2;
@@ -1974,14 +1978,14 @@ static int hessian_operator_2d(sprg_ctx* c) {
   ENSURE(c->rec9, sizeof(double) * 9 * (size_t)m.V);
   ENSURE(c->slab, sizeof(double) * (size_t)expand_grid() * expand_max_elems() * (4 + 9 + 1));
   PB("recover_grad_op_f64");
-  launch_apply_operator(m.V, 1, P<unsigned char>(c->twlisted), P<int>(c->kidx), P<double>(c->kval), P<int>(c->klen),
-                        P<double>(c->f), P<double>(c->rec), c->stream);
+  launch_apply_operator(m.V, 1, c->op_kc, P<unsigned char>(c->twlisted), P<int>(c->kidx), P<double>(c->kval),
+                        P<int>(c->klen), P<double>(c->f), P<double>(c->rec), c->stream);
   PE();
   c->launches += 1;
   if ((rc = listed_fits(c, c->cache2d, nullptr, P<double>(c->f), 3, P<double>(c->rec), lst))) return rc;
   PB("recover_grad_op_f64");
-  launch_apply_operator(m.V, 3, P<unsigned char>(c->twlisted), P<int>(c->kidx), P<double>(c->kval), P<int>(c->klen),
-                        P<double>(c->rec), P<double>(c->rec9), c->stream);
+  launch_apply_operator(m.V, 3, c->op_kc, P<unsigned char>(c->twlisted), P<int>(c->kidx), P<double>(c->kval),
+                        P<int>(c->klen), P<double>(c->rec), P<double>(c->rec9), c->stream);
   PE();
   c->launches += 1;
   return listed_fits(c, c->cache2d, nullptr, P<double>(c->rec), 9, P<double>(c->rec9), lst);

@@ -185,9 +185,10 @@ void launch_metric_mixed2d(int V, const double* H, double eps, double hmin, doub
 // listed set); applied to a scalar (ncin 1 -> V x 3) or a
 // VECTOR field (ncin 3 -> V x 9) at the covered (not listed) vertices
 int tri_operator_slots();
-void launch_tri_operator(const DevMesh& m, const double* w, unsigned char* listed, ExpandList lst, int* kidx,
+// kc: components per operator slot, 3, or 2 for a mesh in the z = 0 plane
+void launch_tri_operator(const DevMesh& m, int kc, const double* w, unsigned char* listed, ExpandList lst, int* kidx,
                          double* kval, int* klen, cudaStream_t s);
-void launch_apply_operator(int V, int ncin, const unsigned char* listed, const int* kidx, const double* kval,
+void launch_apply_operator(int V, int ncin, int kc, const unsigned char* listed, const int* kidx, const double* kval,
                            const int* klen, const double* f, double* out, cudaStream_t s);
 // incremental mesh update: dst[ids[r] * width + j] = vals[r * width + j];
 // the coordinates' bounding box as order keys (3 minima, 3 maxima)

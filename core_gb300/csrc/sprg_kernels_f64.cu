@@ -2181,6 +2181,9 @@ __global__ void __launch_bounds__(kBlock) k_quality_ties(DevMesh m, const Qualit
 // kTriThreadRows + 2 vertices); a patch touching more is listed for the
 // FP64 slab fit instead.
 constexpr int kOpSlots = kTriThreadRows + 2;
+// KC: components stored per slot, 3, or 2 on a mesh in the z = 0 plane
+// (there the z component of every element gradient is exactly zero)
+template <int KC>
 __global__ void __launch_bounds__(kBlock) k_tri_operator(DevMesh m, const double* __restrict__ w,
                                                          unsigned char* __restrict__ listed, ExpandList lst,
                                                          int* __restrict__ kidx, double* __restrict__ kval,
@@ -2226,18 +2229,22 @@ __global__ void __launch_bounds__(kBlock) k_tri_operator(DevMesh m, const double
   klen[v] = n;
   for (int s = 0; s < n; ++s) {
     kidx[(size_t)v * kOpSlots + s] = ids[s];
-    for (int c = 0; c < 3; ++c) kval[((size_t)v * kOpSlots + s) * 3 + c] = acc[s][c];
+    for (int c = 0; c < KC; ++c) kval[((size_t)v * kOpSlots + s) * KC + c] = acc[s][c];
   }
 }
 
 // out (V x 3 NCIN) = K f (f: V x NCIN) at the covered vertices; row r of a
-// MATRIX value is the recovered gradient of component r
-template <int NCIN>
+// MATRIX value is the recovered gradient of component r.  KC = 2 (mesh in
+// the z = 0 plane): K's z components, and the z components of a gradient
+// input, are zero, so only the x / y products are formed and the z entries
+// of the output are zero.
+template <int NCIN, int KC>
 __global__ void __launch_bounds__(kBlock) k_apply_operator(int V, const unsigned char* __restrict__ listed,
                                                            const int* __restrict__ kidx,
                                                            const double* __restrict__ kval,
                                                            const int* __restrict__ klen, const double* __restrict__ f,
                                                            double* __restrict__ out) {
+  constexpr int NR = (KC == 2 && NCIN == 3) ? 2 : NCIN;  // input components that can be nonzero
   const int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= V || listed[v]) return;
   const int n = klen[v];
@@ -2247,13 +2254,14 @@ __global__ void __launch_bounds__(kBlock) k_apply_operator(int V, const unsigned
   for (int s = 0; s < n; ++s) {
     const size_t slot = (size_t)v * kOpSlots + s;
     const int a = kidx[slot];
-    const double k0 = kval[3 * slot], k1 = kval[3 * slot + 1], k2 = kval[3 * slot + 2];
+    double k[KC];
 #pragma unroll
-    for (int r = 0; r < NCIN; ++r) {
+    for (int c = 0; c < KC; ++c) k[c] = kval[KC * slot + c];
+#pragma unroll
+    for (int r = 0; r < NR; ++r) {
       const double fa = f[(size_t)a * NCIN + r];
-      acc[r][0] = fma(k0, fa, acc[r][0]);
-      acc[r][1] = fma(k1, fa, acc[r][1]);
-      acc[r][2] = fma(k2, fa, acc[r][2]);
+#pragma unroll
+      for (int c = 0; c < KC; ++c) acc[r][c] = fma(k[c], fa, acc[r][c]);
     }
   }
 #pragma unroll
@@ -2660,16 +2668,24 @@ void launch_quality_aniso_f32(const DevMesh& m, const void* qrec, const float4* 
 
 int tri_operator_slots() { return kOpSlots; }
 
-void launch_tri_operator(const DevMesh& m, const double* w, unsigned char* listed, ExpandList lst, int* kidx,
+void launch_tri_operator(const DevMesh& m, int kc, const double* w, unsigned char* listed, ExpandList lst, int* kidx,
                          double* kval, int* klen, cudaStream_t s) {
-  if (m.V) k_tri_operator<<<nblk(m.V), kBlock, 0, s>>>(m, w, listed, lst, kidx, kval, klen);
+  if (!m.V) return;
+  if (kc == 2) k_tri_operator<2><<<nblk(m.V), kBlock, 0, s>>>(m, w, listed, lst, kidx, kval, klen);
+  else k_tri_operator<3><<<nblk(m.V), kBlock, 0, s>>>(m, w, listed, lst, kidx, kval, klen);
 }
 
-void launch_apply_operator(int V, int ncin, const unsigned char* listed, const int* kidx, const double* kval,
+void launch_apply_operator(int V, int ncin, int kc, const unsigned char* listed, const int* kidx, const double* kval,
                            const int* klen, const double* f, double* out, cudaStream_t s) {
   if (!V) return;
-  if (ncin == 1) k_apply_operator<1><<<nblk(V), kBlock, 0, s>>>(V, listed, kidx, kval, klen, f, out);
-  else k_apply_operator<3><<<nblk(V), kBlock, 0, s>>>(V, listed, kidx, kval, klen, f, out);
+  const int g = nblk(V);
+  if (kc == 2) {
+    if (ncin == 1) k_apply_operator<1, 2><<<g, kBlock, 0, s>>>(V, listed, kidx, kval, klen, f, out);
+    else k_apply_operator<3, 2><<<g, kBlock, 0, s>>>(V, listed, kidx, kval, klen, f, out);
+  } else {
+    if (ncin == 1) k_apply_operator<1, 3><<<g, kBlock, 0, s>>>(V, listed, kidx, kval, klen, f, out);
+    else k_apply_operator<3, 3><<<g, kBlock, 0, s>>>(V, listed, kidx, kval, klen, f, out);
+  }
 }
 
 void launch_scatter_rows_f64(long long n, int width, const int* ids, const double* vals, double* dst, cudaStream_t s) {
