@@ -1907,23 +1907,27 @@ __device__ __forceinline__ float aniso_dv_f32(float Jx, float Jy, float Jz, cons
   for (int k = 0; k < 3; ++k) h[k] = n0 * ma[k] + n1 * mb[k];
 #pragma unroll
   for (int k = 0; k < 9; ++k) R[k] = n0 * ma[3 + k] + n1 * mb[3 + k];
-  // columns of R
+  // columns of R, normalised by hardware reciprocal square roots, and the
+  // sizes' hardware reciprocals (each within 2 ulps: a few ulps per term on
+  // top of the roundings kAnisoUlps already covers, against the dozen or so
+  // the terms carry)
   float c0x = R[0], c0y = R[3], c0z = R[6];
   float c1x = R[1], c1y = R[4], c1z = R[7];
-  const float l0 = sqrtf(c0x * c0x + c0y * c0y + c0z * c0z);
-  const float r0x = c0x / l0, r0y = c0y / l0, r0z = c0z / l0;
+  const float il0 = rsqrtf(c0x * c0x + c0y * c0y + c0z * c0z);
+  const float r0x = c0x * il0, r0y = c0y * il0, r0z = c0z * il0;
   const float d01 = r0x * c1x + r0y * c1y + r0z * c1z;
   c1x -= r0x * d01; c1y -= r0y * d01; c1z -= r0z * d01;
-  const float l1 = sqrtf(c1x * c1x + c1y * c1y + c1z * c1z);
-  const float r1x = c1x / l1, r1y = c1y / l1, r1z = c1z / l1;
+  const float il1 = rsqrtf(c1x * c1x + c1y * c1y + c1z * c1z);
+  const float r1x = c1x * il1, r1y = c1y * il1, r1z = c1z * il1;
   const float r2x = r0y * r1z - r0z * r1y, r2y = r0z * r1x - r0x * r1z, r2z = r0x * r1y - r0y * r1x;
-  const float t0 = (Jx * r0x + Jy * r0y + Jz * r0z) / h[0];
-  const float t1 = (Jx * r1x + Jy * r1y + Jz * r1z) / h[1];
-  const float t2 = (Jx * r2x + Jy * r2y + Jz * r2z) / h[2];
+  const float ih0 = __fdividef(1.f, h[0]), ih1 = __fdividef(1.f, h[1]), ih2 = __fdividef(1.f, h[2]);
+  const float t0 = (Jx * r0x + Jy * r0y + Jz * r0z) * ih0;
+  const float t1 = (Jx * r1x + Jy * r1y + Jz * r1z) * ih1;
+  const float t2 = (Jx * r2x + Jy * r2y + Jz * r2z) * ih2;
   const float dv = sqrtf(t0 * t0 + t1 * t1 + t2 * t2);
   const float jn = sqrtf(Jx * Jx + Jy * Jy + Jz * Jz);
-  const float sum = jn / fabsf(h[0]) + jn / fabsf(h[1]) + jn / fabsf(h[2]);
-  const float cond = (1.f + 1.f / l0) * (1.f + 1.f / l1);
+  const float sum = jn * (fabsf(ih0) + fabsf(ih1) + fabsf(ih2));
+  const float cond = (1.f + il0) * (1.f + il1);
   *bound = fmaxf(*bound, kAnisoUlps * 5.9604645e-8f * cond * sum / dv);
   return dv;
 }
