@@ -1771,10 +1771,32 @@ __global__ void __launch_bounds__(128) k_tri_weights(DevMesh m, double* __restri
 // does; where the FP32 determinants cannot separate the candidates and the
 // candidates give different qualities, it decides with the FP64
 // determinants of the FP64 quality kernel's arithmetic.
-struct QualityRec {
+// 48 bytes (three 16-byte words) so the records move with vector accesses
+struct __align__(16) QualityRec {
   float q[9];
   float cj;
+  float pad[2];
 };
+__device__ __forceinline__ void store_qrec(QualityRec* dst, const float Q[3][3], float cj) {
+  float4* d = reinterpret_cast<float4*>(dst);
+  d[0] = make_float4(Q[0][0], Q[0][1], Q[0][2], Q[1][0]);
+  d[1] = make_float4(Q[1][1], Q[1][2], Q[2][0], Q[2][1]);
+  d[2] = make_float4(Q[2][2], cj, 0.f, 0.f);
+}
+// a metric record (12 floats: h, frame) as three 16-byte stores / loads
+__device__ __forceinline__ void store_met(float* dst, const float* o) {
+  float4* d = reinterpret_cast<float4*>(dst);
+  d[0] = make_float4(o[0], o[1], o[2], o[3]);
+  d[1] = make_float4(o[4], o[5], o[6], o[7]);
+  d[2] = make_float4(o[8], o[9], o[10], o[11]);
+}
+__device__ __forceinline__ void load_met(const float* src, float* o) {
+  const float4* p = reinterpret_cast<const float4*>(src);
+  const float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
+  o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
+  o[4] = b.x; o[5] = b.y; o[6] = b.z; o[7] = b.w;
+  o[8] = c.x; o[9] = c.y; o[10] = c.z; o[11] = c.w;
+}
 __device__ __forceinline__ void transform_f32(const float* h, const float* R, float Q[3][3]) {
   // orthogonalised frame columns, then Q = R diag(1 / h)
   float c0x = R[0], c0y = R[3], c0z = R[6], c1x = R[1], c1y = R[4], c1z = R[7];
@@ -1803,27 +1825,52 @@ __global__ void __launch_bounds__(kBlock) k_metric_f32(int V, int dim, const dou
                                                        QualityRec* __restrict__ qrec) {
   const int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= V) return;
-  float* o = out + 12 * (size_t)v;
+  float o[12];
   for (int k = 0; k < 3; ++k) o[k] = (float)sizes[3 * (size_t)v + k];
   for (int k = 0; k < 9; ++k) o[3 + k] = (float)frames[9 * (size_t)v + k];
+  store_met(out + 12 * (size_t)v, o);
   float Q[3][3];
   transform_f32(o, o + 3, Q);
-  QualityRec r;
-  for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j) r.q[3 * i + j] = Q[i][j];
-  r.cj = det_f32(Q, dim);
-  qrec[v] = r;
+  store_qrec(qrec + v, Q, det_f32(Q, dim));
+}
+
+// Integer forms of the FP64 tests and conversions the mixed metric needs
+// (on this GPU the FP64 pipe is the scarce one: the comparisons, min / max
+// and conversions would each take an FP64 issue slot).  Non-NaN operands.
+__device__ __forceinline__ unsigned long long dbits(double x) {
+  return (unsigned long long)__double_as_longlong(x);
+}
+__device__ __forceinline__ bool d_is_zero(double x) { return (dbits(x) << 1) == 0; }
+__device__ __forceinline__ bool d_is_neg(double x) { return (dbits(x) >> 63) && !d_is_zero(x); }  // x < 0
+__device__ __forceinline__ bool d_abs_gt(double x, double y) { return (dbits(x) << 1) > (dbits(y) << 1); }
+// x >= y: doubles ordered as signed integers after flipping the magnitude
+// bits of negatives (-0 taken as +0)
+__device__ __forceinline__ long long d_key(double x) {
+  const long long b = __double_as_longlong(x);
+  return d_is_zero(x) ? 0 : (b ^ ((b >> 63) & 0x7fffffffffffffffLL));
+}
+// x 2^-e rounded toward zero to FP32; below FP32's normal range 0, above it
+// infinity
+__device__ __forceinline__ float d_to_f32_scaled(double x, int e) {
+  const unsigned long long b = dbits(x);
+  const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+  const int ef = (int)((b >> 52) & 0x7ff) - 1023 - e + 127;
+  if (ef <= 0 || d_is_zero(x)) return __uint_as_float(sign);
+  if (ef >= 255) return __uint_as_float(sign | 0x7f800000u);
+  return __uint_as_float(sign | ((unsigned)ef << 23) | (unsigned)((b >> 29) & 0x7fffffu));
 }
 
 // Mixed pass on triangles: the FP32 metric records and quality records
 // straight from the FP64 Hessian.  Every decision of hessian_metric_vertex
 // (the b == 0 and a >= c branches, the |lambda| order, the sign convention)
-// is taken on the same FP64 values, with the one FP64 square root it needs
-// (the eigenvalue gap); the magnitudes that follow (the direction's
-// normalisation, sqrt(eps / |lambda|)) are FP32 operations on those values,
-// a few ulps from the FP64 results, inside the FP32 measure's bound.  The
-// sign test runs on the unnormalised FP64 direction (the normalisation by a
-// positive length keeps signs and zeros).
+// is taken on the same FP64 values as there, with the FP64 arithmetic those
+// values need (one square root); the tests themselves and the conversions
+// run as integer operations on the bit patterns.  The magnitudes that
+// follow (the direction's normalisation, sqrt(eps / |lambda|)) are FP32
+// operations on those values rounded toward zero, a few ulps from the FP64
+// results, inside the FP32 measure's bound.  The sign test runs on the
+// unnormalised FP64 direction (the normalisation by a positive length keeps
+// signs and zeros).
 __global__ void __launch_bounds__(kBlock) k_metric_mixed2d(int V, const double* __restrict__ H, double eps,
                                                            double hmin, double hmax, float* __restrict__ out,
                                                            QualityRec* __restrict__ qrec) {
@@ -1835,17 +1882,18 @@ __global__ void __launch_bounds__(kBlock) k_metric_mixed2d(int V, const double* 
   const double d = sqrt(hd * hd + b * b);
   double l1 = mid + d, l2 = mid - d;
   double x, y;
-  if (b == 0.0) {
-    x = a >= c ? 1.0 : 0.0;
-    y = a >= c ? 0.0 : 1.0;
-  } else if (a >= c) {
+  const bool ageqc = d_key(a) >= d_key(c);
+  if (d_is_zero(b)) {
+    x = ageqc ? 1.0 : 0.0;
+    y = ageqc ? 0.0 : 1.0;
+  } else if (ageqc) {
     x = l1 - c;
     y = b;
   } else {
     x = b;
     y = l1 - a;
   }
-  if (fabs(l2) > fabs(l1)) {
+  if (d_abs_gt(l2, l1)) {
     const double tl = l1;
     l1 = l2;
     l2 = tl;
@@ -1853,41 +1901,29 @@ __global__ void __launch_bounds__(kBlock) k_metric_mixed2d(int V, const double* 
     x = -y;
     y = tx;
   }
-  if (x < 0 || (x == 0 && y < 0)) {
-    x = -x;
-    y = -y;
+  const bool flip = d_is_neg(x) || (d_is_zero(x) && d_is_neg(y));
+  // FP32 direction scaled by 2^-e, e the exponent of max(|x|, |y|) (> 0: one
+  // of them is b != 0 or l1 - c > 0), then normalised in FP32
+  const unsigned long long mx = (dbits(x) << 1) > (dbits(y) << 1) ? dbits(x) : dbits(y);
+  const int ex = (int)((mx >> 52) & 0x7ff) - 1023;
+  float xf = d_to_f32_scaled(x, ex), yf = d_to_f32_scaled(y, ex);
+  if (flip) {
+    xf = -xf;
+    yf = -yf;
   }
-  // scale by a power of two into FP32 range (exact), then normalise in FP32
-  // 2^-e with e the exponent of max(|x|, |y|) (> 0: one of them is b != 0
-  // or l1 - c > 0), built from the exponent bits; a subnormal maximum takes
-  // 2^1022, the top binade 2^-1022
-  const double ax = fmax(fabs(x), fabs(y));
-  const long long eb = (__double_as_longlong(ax) >> 52) & 0x7ff;
-  const long long sb = eb == 0 ? 2045 : (eb < 2046 ? 2046 - eb : 1);
-  const double sc = __longlong_as_double(sb << 52);
-  float xf = (float)(x * sc), yf = (float)(y * sc);
   const float nf = sqrtf(xf * xf + yf * yf);
   xf /= nf;
   yf /= nf;
   const float epsf = (float)eps, hminf = (float)hmin, hmaxf = (float)hmax;
   auto size_f32 = [&](double l) {
-    if (!(fabs(l) > 0)) return hmaxf;
-    return fminf(fmaxf(sqrtf(epsf / fabsf((float)l)), hminf), hmaxf);
+    if (d_is_zero(l) || (((dbits(l) >> 52) & 0x7ff) == 0x7ff && (dbits(l) << 12) != 0)) return hmaxf;  // 0, NaN
+    return fminf(fmaxf(sqrtf(epsf / fabsf(d_to_f32_scaled(l, 0))), hminf), hmaxf);
   };
-  float* o = out + 12 * (size_t)v;
-  o[0] = size_f32(l1);
-  o[1] = size_f32(l2);
-  o[2] = hmaxf;
-  o[3] = xf; o[4] = -yf; o[5] = 0.f;
-  o[6] = yf; o[7] = xf;  o[8] = 0.f;
-  o[9] = 0.f; o[10] = 0.f; o[11] = 1.f;
+  const float o[12] = {size_f32(l1), size_f32(l2), hmaxf, xf, -yf, 0.f, yf, xf, 0.f, 0.f, 0.f, 1.f};
+  store_met(out + 12 * (size_t)v, o);
   float Q[3][3];
   transform_f32(o, o + 3, Q);
-  QualityRec r;
-  for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j) r.q[3 * i + j] = Q[i][j];
-  r.cj = det_f32(Q, 2);
-  qrec[v] = r;
+  store_qrec(qrec + v, Q, det_f32(Q, 2));
 }
 
 // AnisoSizeField measure in FP32 with a relative error bound.  Per Gauss
@@ -1954,11 +1990,8 @@ __global__ void __launch_bounds__(kBlock) k_measure_aniso_f32(DevMesh m, const f
     const float Jy = ((hb.y - ha.y) + (lb.y - la.y)) * jscale;
     const float Jz = ((hb.z - ha.z) + (lb.z - la.z)) * jscale;
     float ma[12], mb[12];
-#pragma unroll
-    for (int k = 0; k < 12; ++k) {
-      ma[k] = met[12 * (size_t)a + k];
-      mb[k] = met[12 * (size_t)b + k];
-    }
+    load_met(met + 12 * (size_t)a, ma);
+    load_met(met + 12 * (size_t)b, mb);
     float bound = 0.f;
     const float g0 = 0.577350269189626f;
     const float L = aniso_dv_f32(Jx, Jy, Jz, ma, mb, (1.f - g0) * 0.5f, (1.f + g0) * 0.5f, &bound) +
@@ -2087,8 +2120,11 @@ __device__ __forceinline__ int quality_pick_f32(const DevMesh& m, const QualityR
 }
 
 __device__ __forceinline__ void load_qrec(const QualityRec& r, float (*T)[3]) {
-  for (int a = 0; a < 3; ++a)
-    for (int b = 0; b < 3; ++b) T[a][b] = r.q[3 * a + b];
+  const float4* p = reinterpret_cast<const float4*>(&r);
+  const float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
+  T[0][0] = a.x; T[0][1] = a.y; T[0][2] = a.z; T[1][0] = a.w;
+  T[1][1] = b.x; T[1][2] = b.y; T[2][0] = b.z; T[2][1] = b.w;
+  T[2][2] = c.x;
 }
 
 // FP32 qualities.  Elements whose candidate vertices give qualities that
