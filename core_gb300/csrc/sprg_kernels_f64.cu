@@ -2295,8 +2295,14 @@ __global__ void __launch_bounds__(kBlock) k_apply_operator(int V, const unsigned
     const size_t slot = (size_t)v * kOpSlots + s;
     const int a = kidx[slot];
     double k[KC];
+    if (KC == 2) {  // one 16-byte load per slot
+      const double2 kk = __ldg(reinterpret_cast<const double2*>(kval) + slot);
+      k[0] = kk.x;
+      k[KC - 1] = kk.y;
+    } else {
 #pragma unroll
-    for (int c = 0; c < KC; ++c) k[c] = kval[KC * slot + c];
+      for (int c = 0; c < KC; ++c) k[c] = kval[KC * slot + c];
+    }
 #pragma unroll
     for (int r = 0; r < NR; ++r) {
       const double fa = f[(size_t)a * NCIN + r];
