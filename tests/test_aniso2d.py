@@ -200,3 +200,53 @@ def test_isotropic_fp32_pass_rejects_triangles(gpu_lib):
         with pytest.raises(K.SprgError) as ei:
             c.estimate_and_mark(workload.bump_field(m.coords, seed=1), 0.1)
         assert ei.value.code == K.SPRG_EINVAL
+
+
+# Fields whose Hessians hit the metric's special cases: b = 0 with a != c
+# (axis-aligned), a = c with b = 0 (isotropic: the frame comes from the
+# a >= c branch), a = c = 0 with b != 0 (pure shear), negative eigenvalues
+# (the |lambda| swap and the sign convention), and a linear field (zero
+# Hessian: both sizes h_max).  The mixed pass takes those decisions with
+# integer tests on the FP64 bits; marks and qualities must still be the
+# FP64 pass's.
+SPECIAL_FIELDS = {
+    "axis": lambda x, y: 3.0 * x * x - 0.5 * y * y,
+    "isotropic": lambda x, y: x * x + y * y,
+    "shear": lambda x, y: 4.0 * x * y,
+    "negative": lambda x, y: -(x * x + 3.0 * y * y) + 0.2 * x * y,
+    "linear": lambda x, y: 2.0 * x - y,
+}
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", sorted(SPECIAL_FIELDS))
+def test_mixed_metric_special_hessians(gpu_lib, name):
+    from core_gb300 import workload
+    m = workload.box(40, nz=0, jitter=0.15, seed=11)
+    x, y = m.coords[:, 0], m.coords[:, 1]
+    u = SPECIAL_FIELDS[name](x, y)
+    eps, hmin, hmax = 2e-3, 1.0 / 160, 0.2
+    s64, c64, q64, M64, _, _ = run_aniso(m, u, eps, hmin, hmax, "fp64")
+    s32, c32, q32, M32, _, guard = run_aniso(m, u, eps, hmin, hmax, "fp32")
+    assert np.array_equal(s32, s64) and np.array_equal(c32, c64)
+    assert np.abs(q32 - q64).max() <= 1e-4 * np.abs(q64).max()
+    scale = np.abs(M64).reshape(len(M64), -1).max(axis=1)
+    assert (np.abs(M32 - M64).reshape(len(M64), -1).max(axis=1) / scale).max() <= 1e-5
+
+
+@pytest.mark.gpu
+def test_mixed_aniso_pass_off_plane(gpu_lib):
+    """A triangle mesh in the plane z = 0.25 (not z = 0) keeps three
+    operator components per slot; its marks equal the FP64 pass's and the
+    same mesh in z = 0 (two components)."""
+    from core_gb300.mesh import Mesh
+    m, u, (eps, hmin, hmax) = case(64)
+    x = m.coords.copy()
+    x[:, 2] = 0.25
+    lifted = Mesh(m.dim, x, m.elem_verts, m.edge_verts)
+    s0, c0, q0, _, _, _ = run_aniso(m, u, eps, hmin, hmax, "fp32")
+    s1, c1, q1, _, _, _ = run_aniso(lifted, u, eps, hmin, hmax, "fp32")
+    s64, c64, _, _, _, _ = run_aniso(lifted, u, eps, hmin, hmax, "fp64")
+    assert np.array_equal(s1, s64) and np.array_equal(c1, c64)
+    assert np.array_equal(s1, s0) and np.array_equal(c1, c0)
+    assert np.abs(q1 - q0).max() <= 1e-5 * np.abs(q0).max()
