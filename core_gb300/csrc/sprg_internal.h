@@ -206,7 +206,7 @@ void launch_recover_w64(const DevMesh& m, const double* ip, int nc, const double
 // FP64 guard band of the FP32 path: re-decide the listed edges' bits.
 struct GuardScratch {
   int* stamp;      // V ints, persistent (de-duplication stamps)
-  int stamp_id;    // distinct per pass
+  int* stamp_id;   // device counter: this pass's stamp id (starts at 1; the decide stage bumps it)
   int* fit_items;  // fit_cap ints
   int* fit_count;
   int fit_cap;

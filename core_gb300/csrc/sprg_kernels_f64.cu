@@ -1177,10 +1177,12 @@ __device__ __forceinline__ int warp_slot(bool win, int* counter) {
 }
 
 __global__ void k_guard_collect(DevMesh m, const int* __restrict__ items, const int* __restrict__ count, int cap,
-                                int stamp_id, int* __restrict__ stamp, int* __restrict__ fit_items,
+                                const int* __restrict__ stamp_id_ptr, int* __restrict__ stamp,
+                                int* __restrict__ fit_items,
                                 int* __restrict__ fit_count, int fit_cap, int* __restrict__ unresolved) {
   // warp per (edge, end): lanes over the end's elements in rounds of 32
   const int n = min(*count, cap);
+  const int stamp_id = *stamp_id_ptr;
   const long total = (long)n * 2 * 32;
   const int lane = threadIdx.x & 31;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
@@ -1247,6 +1249,13 @@ __global__ void __launch_bounds__(128) k_guard_decide(DevMesh m, const double* _
                                                       const int* __restrict__ items, const int* __restrict__ count,
                                                       int cap, uint32_t* split, uint32_t* collapse,
                                                       int* __restrict__ unresolved, BatchView bv) {
+  // the stamp id of the next guard pass (the collect stage of this one is
+  // done): a device counter, so a pass replayed from a CUDA graph still
+  // de-duplicates with a fresh id; 0, the stamps' initial value, is skipped
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    const int next = *g.stamp_id + 1;
+    *g.stamp_id = next > 0 ? next : 1;
+  }
   __shared__ double esz[4][2][kGuardMaxTets];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int n = min(*count, cap);

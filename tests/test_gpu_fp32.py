@@ -123,3 +123,57 @@ def test_fp32_marks_bit_exact_at_128cube(gpu_lib):
     assert info["n_guard_unresolved"] == 0
     fin = np.isfinite(s32) & np.isfinite(s64)
     assert np.median(np.abs(s32[fin] - s64[fin]) / s64[fin]) <= 1e-6
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp32", "fp64", "learned"])
+def test_host_entry_graph_replays_follow_the_field(gpu_lib, precision):
+    """The host entry point replays its pass from a CUDA graph from the
+    third call on; with the field changing between calls every result
+    equals a fresh context's (nothing per pass is frozen into the graph)."""
+    import core_gb300 as cg
+    from core_gb300 import workload
+    m = workload.box(24, jitter=0.2, seed=41)
+    us = [workload.bump_field(m.coords, seed=s) for s in (41, 42, 43)]
+    ratio = 0.008 * 24 / 160
+    with cg.Context(m, precision=precision) as ctx:
+        got = [ctx.estimate_and_mark(us[i % 3], ratio)[:4] for i in range(7)]
+    want = []
+    for i in range(3):
+        with cg.Context(m, precision=precision) as fresh:
+            want.append(fresh.estimate_and_mark(us[i], ratio)[:4])
+    for i, g in enumerate(got):
+        w = want[i % 3]
+        assert np.array_equal(g[0], w[0], equal_nan=True)
+        assert np.array_equal(g[1], w[1]) and g[2:] == w[2:]
+
+
+@pytest.mark.gpu
+def test_user_graph_replays_follow_the_field(gpu_lib):
+    """sprg_graph_capture / sprg_graph_replay with new field values written
+    into the captured input between replays: bits equal direct passes."""
+    import torch
+    import core_gb300 as cg
+    from core_gb300 import workload
+    m = workload.box(24, jitter=0.2, seed=44)
+    us = [workload.bump_field(m.coords, seed=s) for s in (44, 45)]
+    ratio = 0.008 * 24 / 160
+    E = m.n_edges
+    nw = (E + 31) // 32
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    d_u = torch.from_numpy(us[0]).cuda()
+    bits = torch.zeros(2 * nw, dtype=torch.int32, device="cuda")
+    ref = torch.zeros(2 * nw, dtype=torch.int32, device="cuda")
+    with cg.Context(m, precision="fp32") as ctx, cg.Context(m, precision="fp32") as direct:
+        ctx.set_stream(stream.cuda_stream)
+        direct.set_stream(stream.cuda_stream)
+        ctx.graph_capture(d_u.data_ptr(), ratio, bits.data_ptr(), bits.data_ptr() + 4 * nw)
+        for i in range(4):
+            d_u.copy_(torch.from_numpy(us[i % 2]))
+            bits.zero_()
+            ctx.graph_replay()
+            direct.estimate_and_mark_resident(d_u.data_ptr(), ratio, ref.data_ptr(), ref.data_ptr() + 4 * nw)
+            torch.cuda.synchronize()
+            assert torch.equal(bits, ref)
+    assert ref.any()
