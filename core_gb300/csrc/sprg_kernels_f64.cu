@@ -1137,16 +1137,22 @@ constexpr int kGuardMaxTets = 96;  // elements around one end vertex
 // accuracy, not the reference's rounding).  Every guard kernel that needs an
 // element's gradient evaluates it with this function, so all of them see the
 // same bits.
+// (explicit fused multiply-adds: the guard wants FP64 accuracy, not the
+// reference's rounding, and the FP64 pipe bounds these kernels)
 __device__ __forceinline__ void tet_grad_f64(const DevMesh& m, int t, const double* __restrict__ u, double* g) {
-  const int* ev = m.ev + (size_t)t * 4;
-  V3 x0 = load_xyz(m.xyz, ev[0]), x1 = load_xyz(m.xyz, ev[1]), x2 = load_xyz(m.xyz, ev[2]),
-     x3 = load_xyz(m.xyz, ev[3]);
-  double u0 = u[ev[0]];
-  V3 e1 = ref::sub(x1, x0), e2 = ref::sub(x2, x0), e3 = ref::sub(x3, x0);
-  double d1 = u[ev[1]] - u0, d2 = u[ev[2]] - u0, d3 = u[ev[3]] - u0;
-  V3 c1 = ref::cross(e2, e3), c2 = ref::cross(e3, e1), c3 = ref::cross(e1, e2);
-  double inv = 1.0 / ref::dot(e1, c1);
-  for (int k = 0; k < 3; ++k) g[k] = (c1.v[k] * d1 + c2.v[k] * d2 + c3.v[k] * d3) * inv;
+  const int4 tv = __ldg(reinterpret_cast<const int4*>(m.ev) + t);
+  const V3 x0 = load_xyz(m.xyz, tv.x), x1 = load_xyz(m.xyz, tv.y), x2 = load_xyz(m.xyz, tv.z),
+           x3 = load_xyz(m.xyz, tv.w);
+  const double u0 = u[tv.x];
+  const V3 e1 = ref::sub(x1, x0), e2 = ref::sub(x2, x0), e3 = ref::sub(x3, x0);
+  const double d1 = u[tv.y] - u0, d2 = u[tv.z] - u0, d3 = u[tv.w] - u0;
+  auto crs = [](const V3& a, const V3& b) {
+    return V3{{fma(a.v[1], b.v[2], -a.v[2] * b.v[1]), fma(a.v[2], b.v[0], -a.v[0] * b.v[2]),
+               fma(a.v[0], b.v[1], -a.v[1] * b.v[0])}};
+  };
+  const V3 c1 = crs(e2, e3), c2 = crs(e3, e1), c3 = crs(e1, e2);
+  const double inv = 1.0 / fma(e1.v[0], c1.v[0], fma(e1.v[1], c1.v[1], e1.v[2] * c1.v[2]));
+  for (int k = 0; k < 3; ++k) g[k] = fma(c1.v[k], d1, fma(c2.v[k], d2, c3.v[k] * d3)) * inv;
 }
 
 // Guard pipeline, three kernels over all listed edges at once:
@@ -1244,6 +1250,8 @@ __global__ void k_guard_fit(DevMesh m, const double* __restrict__ u, const int* 
   }
 }
 
+// 64 threads per edge (two edges per block): thread j takes element j of
+// the two ends' lists, so each computes one element size
 __global__ void __launch_bounds__(128) k_guard_decide(DevMesh m, const double* __restrict__ u,
                                                       const double* __restrict__ out3, GuardScratch g,
                                                       const int* __restrict__ items, const int* __restrict__ count,
@@ -1256,19 +1264,30 @@ __global__ void __launch_bounds__(128) k_guard_decide(DevMesh m, const double* _
     const int next = *g.stamp_id + 1;
     *g.stamp_id = next > 0 ? next : 1;
   }
-  __shared__ double esz[4][2][kGuardMaxTets];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  __shared__ double esz[2][2 * kGuardMaxTets];
+  const int half = threadIdx.x >> 6, j0 = threadIdx.x & 63;
   const int n = min(*count, cap);
-  for (int it = blockIdx.x * 4 + warp; it < n; it += gridDim.x * 4) {
-    const int e = items[it];
-    const int ab[2] = {m.edv[2 * (size_t)e], m.edv[2 * (size_t)e + 1]};
-    const double sf = batch_sf(bv, out3, ab[0]);
-    int cnt[2] = {m.a_off[ab[0] + 1] - m.a_off[ab[0]], m.a_off[ab[1] + 1] - m.a_off[ab[1]]};
-    bool bad = cnt[0] > kGuardMaxTets || cnt[1] > kGuardMaxTets;
-    if (!bad) {
-      for (int s = 0; s < 2; ++s)
-        for (int i = lane; i < cnt[s]; i += 32) {
-          const int t = m.a_el[m.a_off[ab[s]] + i];
+  // every thread of the block runs the same number of rounds (the barriers)
+  for (int base = blockIdx.x * 2; base < n; base += gridDim.x * 2) {
+    const int it = base + half;
+    const bool live = it < n;
+    int e = 0, ab[2] = {0, 0}, cnt[2] = {0, 0}, off[2] = {0, 0};
+    bool bad = false;
+    double sf = 0;
+    if (live) {
+      e = items[it];
+      ab[0] = m.edv[2 * (size_t)e];
+      ab[1] = m.edv[2 * (size_t)e + 1];
+      sf = batch_sf(bv, out3, ab[0]);
+      for (int s = 0; s < 2; ++s) {
+        off[s] = m.a_off[ab[s]];
+        cnt[s] = m.a_off[ab[s] + 1] - off[s];
+      }
+      bad = cnt[0] > kGuardMaxTets || cnt[1] > kGuardMaxTets;
+      if (!bad)
+        for (int j = j0; j < cnt[0] + cnt[1]; j += 64) {
+          const int s = j < cnt[0] ? 0 : 1;
+          const int t = m.a_el[off[s] + j - (s ? cnt[0] : 0)];
           const int* ev = m.ev + 4 * (size_t)t;
           double gt[3];
           tet_grad_f64(m, t, u, gt);
@@ -1278,14 +1297,14 @@ __global__ void __launch_bounds__(128) k_guard_decide(DevMesh m, const double* _
           const double2 dh = g.geo64[t];  // det J, h_max
           double dd = 0;
           for (int c = 0; c < 3; ++c) dd += (gt[c] - v2[c]) * (gt[c] - v2[c]);
-          esz[warp][s][i] = dh.y * pow(dd * (1.0 / 6.0) * dh.x, -0.2) * sf;
+          esz[half][j] = dh.y * pow(dd * (1.0 / 6.0) * dh.x, -0.2) * sf;
         }
     }
-    __syncwarp();
-    if (lane == 0) {
+    __syncthreads();
+    if (live && j0 == 0) {
       double sz[2] = {0, 0};
       for (int s = 0; s < 2 && !bad; ++s) {
-        for (int i = 0; i < cnt[s]; ++i) sz[s] += esz[warp][s][i];
+        for (int i = 0; i < cnt[s]; ++i) sz[s] += esz[half][(s ? cnt[0] : 0) + i];
         sz[s] /= (double)cnt[s];
       }
       if (bad || !(sz[0] == sz[0]) || !(sz[1] == sz[1])) {  // too many elements, or a NaN size
@@ -1300,7 +1319,7 @@ __global__ void __launch_bounds__(128) k_guard_decide(DevMesh m, const double* _
         if (L < .5) atomicOr(&collapse[e >> 5], bit); else atomicAnd(&collapse[e >> 5], ~bit);
       }
     }
-    __syncwarp();
+    __syncthreads();
   }
 }
 
@@ -2608,7 +2627,7 @@ void launch_guard_stage(int stage, const DevMesh& m, const double* u, const doub
       k_guard_fit<<<152 * 8, 256, 0, s>>>(m, u, g.fit_items, g.fit_count, g.fit_cap, g);
       break;
     default:
-      k_guard_decide<<<152 * 2, 128, 0, s>>>(m, u, out3, g, items, count, cap, split, collapse, unresolved, bv);
+      k_guard_decide<<<152 * 4, 128, 0, s>>>(m, u, out3, g, items, count, cap, split, collapse, unresolved, bv);
   }
 }
 
