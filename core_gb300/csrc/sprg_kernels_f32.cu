@@ -28,11 +28,12 @@
 //   prep      four vertices per thread: the field pairs
 //   tet       thread per tet: its gradient as 16 bytes, the FP32 value s
 //             and the packed correction r (exact = s + r, see pack_corr)
-//   recover   4 lanes per vertex: eps*(v) = g_ref + sum w_vt (eps_t - g_ref)
+//   recover   1, 2 or 4 lanes per vertex (tuned per patch-size bin):
+//             eps*(v) = g_ref + sum w_vt (eps_t - g_ref)
 //   error     thread per tet: element error, SelfProduct and Error terms
 //             (compensated), q_t = h_max * err^(-1/5) and a relative error
 //             bound of q_t
-//   average   4 lanes per vertex: size = size_factor * mean(q_t)
+//   average   2 lanes per vertex: size = size_factor * mean(q_t)
 //             (compensated) and the size's error bound, packed as a pair
 //   measure   thread per edge: metric length, split/collapse bitmaps, and the
 //             list of edges whose distance to 0.5 / 1.5 is within the error
@@ -43,7 +44,9 @@ namespace sprg {
 namespace {
 
 constexpr int kBlock = 256;
-constexpr int kGroup = 4;  // lanes per vertex in the average kernel
+// lanes per vertex in the average kernel (2: 166 -> 129 us at 160^3 against
+// 4; 1 or 8, or more entries unrolled per lane, were slower)
+constexpr int kGroup = 2;
 // relative accuracy assumed for each quantity entering an element-error
 // deviation (about 4 FP32 ulps), scaled into the error bound of q_t; on the
 // 160^3 workload the largest observed error is 0.43 of the resulting bound
@@ -715,7 +718,7 @@ __global__ void __launch_bounds__(kBlock) k_fast_average(DevMesh m, const float2
 #pragma unroll
   for (int j = 0; j < 8; ++j)
     if (b + gl + j * kGroup < e) take(x[j]);
-  for (int k = b + gl + 8 * kGroup; k < e; k += kGroup) take(__ldg(q + __ldg(m.a_el + k)));  // > 32 elements
+  for (int k = b + gl + 8 * kGroup; k < e; k += kGroup) take(__ldg(q + __ldg(m.a_el + k)));  // > 16 elements
 #pragma unroll
   for (int o = 1; o < kGroup; o <<= 1) {
     float oh = __shfl_xor_sync(0xffffffffu, s.h, o), ol = __shfl_xor_sync(0xffffffffu, s.l, o);
