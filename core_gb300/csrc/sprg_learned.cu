@@ -774,8 +774,9 @@ __global__ void __launch_bounds__(kBlock) k_lerror(DevMesh m, const float4* __re
 
 __global__ void __launch_bounds__(kBlock) k_laverage(DevMesh m, const float* __restrict__ q,
                                                      const double* __restrict__ out3, float* __restrict__ size) {
+  // two lanes per vertex (as the FP32 path's average: 4 lanes were slower)
   const int gid = blockIdx.x * blockDim.x + threadIdx.x;
-  const int v = gid >> 2, gl = gid & 3;
+  const int v = gid >> 1, gl = gid & 1;
   int b = 0, e = 0;
   if (v < m.V) {
     b = m.a_off[v];
@@ -784,15 +785,14 @@ __global__ void __launch_bounds__(kBlock) k_laverage(DevMesh m, const float* __r
   float x[8];
 #pragma unroll
   for (int j = 0; j < 8; ++j) {
-    const int k = b + gl + 4 * j;
+    const int k = b + gl + 2 * j;
     x[j] = k < e ? __ldg(q + __ldg(m.a_el + k)) : 0.f;
   }
   float s = 0.f;
 #pragma unroll
   for (int j = 0; j < 8; ++j) s += x[j];
-  for (int k = b + gl + 32; k < e; k += 4) s += __ldg(q + __ldg(m.a_el + k));
+  for (int k = b + gl + 16; k < e; k += 2) s += __ldg(q + __ldg(m.a_el + k));
   s += __shfl_xor_sync(0xffffffffu, s, 1);
-  s += __shfl_xor_sync(0xffffffffu, s, 2);
   if (v < m.V && gl == 0) size[v] = (float)out3[2] * (s / (float)(e - b));
 }
 
@@ -801,25 +801,27 @@ __global__ void __launch_bounds__(kBlock) k_lmeasure(DevMesh m, const float* __r
                                                      uint32_t* __restrict__ collapse) {
   const int lane = threadIdx.x & 31;
   const long warp = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5;
-  const int e0 = (int)(warp * 64) + lane;
-  const int eids[2] = {e0, e0 + 32};
-  int2 ab[2];
-  float hl[2], A[2], B[2];
+  // four edges per thread (e, e + 32, e + 64, e + 96 within the warp's
+  // 128-edge chunk), all loads issued before use
+  const int e0 = (int)(warp * 128) + lane;
+  const int eids[4] = {e0, e0 + 32, e0 + 64, e0 + 96};
+  int2 ab[4];
+  float hl[4], A[4], B[4];
 #pragma unroll
-  for (int i = 0; i < 2; ++i) {
+  for (int i = 0; i < 4; ++i) {
     const bool in = eids[i] < m.E;
     ab[i] = in ? __ldg(reinterpret_cast<const int2*>(m.edv) + eids[i]) : make_int2(0, 0);
     hl[i] = in ? __ldg(half_len + eids[i]) : 0.f;
   }
 #pragma unroll
-  for (int i = 0; i < 2; ++i) {
+  for (int i = 0; i < 4; ++i) {
     A[i] = __ldg(size + ab[i].x);
     B[i] = __ldg(size + ab[i].y);
   }
   const float gp = 0.577350269189626f;
   const float n0 = 0.5f * (1.f - gp), n1 = 0.5f * (1.f + gp);
 #pragma unroll
-  for (int i = 0; i < 2; ++i) {
+  for (int i = 0; i < 4; ++i) {
     const int e = eids[i];
     bool s = false, c = false;
     if (e < m.E) {
@@ -1181,12 +1183,12 @@ void learned_error(const DevMesh& m, const float4* rec, const float2* geo, float
 }
 
 void learned_average(const DevMesh& m, const float* q, const double* out3, float* size, cudaStream_t s) {
-  if (m.V) k_laverage<<<nblk(4L * m.V), kBlock, 0, s>>>(m, q, out3, size);
+  if (m.V) k_laverage<<<nblk(2L * m.V), kBlock, 0, s>>>(m, q, out3, size);
 }
 
 void learned_measure(const DevMesh& m, const float* half_len, const float* size, uint32_t* split, uint32_t* collapse,
                      cudaStream_t s) {
-  if (m.E) k_lmeasure<<<nblk((m.E + 1) / 2), kBlock, 0, s>>>(m, half_len, size, split, collapse);
+  if (m.E) k_lmeasure<<<nblk((m.E + 3) / 4), kBlock, 0, s>>>(m, half_len, size, split, collapse);
 }
 
 void learned_size_to_f64(int V, const float* s32, double* s64, cudaStream_t s) {
