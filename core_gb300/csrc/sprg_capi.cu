@@ -63,6 +63,7 @@ struct sprg_ctx {
   DevBuf crec, vrec, rec32, q32, sz2, fcnt, guard, tetd, wts, w64, listed, geo, geo64, elen, fitems;
   DevBuf gstamp, gfit, grec;  // guard pipeline scratch
   DevBuf tnext;               // work counter of the tet kernel
+  DevBuf edone;               // blocks of the error kernel done (zero between passes)
   // learned form
   DevBuf hess;  // nodal Hessian upload (sprg_hessian_metric)
   // batch of independent meshes (sprg_set_batch)
@@ -829,7 +830,7 @@ int sprg_destroy(sprg_ctx* c) {
                     &c->size,  &c->L,       &c->flags, &c->q,    &c->sizes3,  &c->frames9, &c->partials,
                     &c->out3,  &c->status,  &c->count, &c->mcount, &c->xitems, &c->xcount, &c->slab, &c->bits, &c->titems, &c->tcountb, &c->Lx, &c->pairs, &c->red, &c->eflags, &c->logm, &c->qw, &c->qwlisted, &c->qwitems, &c->qwcount, &c->tw, &c->twlisted, &c->twitems, &c->twcount, &c->met32, &c->qrec32, &c->cj64, &c->qties, &c->kidx, &c->kval, &c->klen, &c->rec9, &c->cache2d.v, &c->cache2d.n, &c->cache2d.el, &c->agitems, &c->agcount,
                     &c->crec,  &c->vrec,    &c->rec32, &c->q32, &c->sz2,  &c->fcnt,   &c->guard, &c->tetd,
-                    &c->wts,   &c->w64,     &c->listed, &c->geo, &c->geo64, &c->elen, &c->fitems, &c->gstamp, &c->gfit, &c->grec, &c->tnext,
+                    &c->wts,   &c->w64,     &c->listed, &c->geo, &c->geo64, &c->elen, &c->fitems, &c->gstamp, &c->gfit, &c->grec, &c->tnext, &c->edone,
                     &c->hess, &c->pcls, &c->bverts, &c->btiles, &c->bnext, &c->bvoff, &c->bseg, &c->bsegoff, &c->bratios, &c->vvoff, &c->vv, &c->vtile, &c->vr16, &c->rec16,
                     &c->ql,    &c->sizel,   &c->fbitems, &c->fbcount, &c->mlp_packed, &c->mlp_err, &c->mlp_tmp,
                     &c->cache64.v, &c->cache64.n, &c->cache64.el, &c->cache32.v, &c->cache32.n, &c->cache32.el,
@@ -1489,6 +1490,10 @@ static int pass_fast(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_
   ENSURE(c->rec32, 16 * (size_t)m.V);
   ENSURE(c->tetd, 16 * (size_t)m.T);
   ENSURE(c->tnext, sizeof(int));
+  if (!c->edone.p) {
+    ENSURE(c->edone, sizeof(unsigned));
+    CK(cudaMemsetAsync(c->edone.p, 0, sizeof(unsigned), c->stream));
+  }
   ENSURE(c->q32, 8 * (size_t)m.T);
   ENSURE(c->sz2, 8 * (size_t)m.V);
   ENSURE(c->rec, 24 * (size_t)m.V);
@@ -1530,16 +1535,17 @@ static int pass_fast(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_
   PB("merge_f64");
   fast_merge_ref(xl, P<double>(c->rec), rec32, c->stream);
   PE();
+  // one mesh: the error kernel's last block also computes the size factor
   PB("error_f32");
   fast_error(m, P<uint4>(c->tetd), P<float2>(c->geo), rec32, P<float2>(c->q32), P<double>(c->partials), nb,
-             bv.n ? P<int2>(c->bseg) : nullptr, c->stream);
+             bv.n ? P<int2>(c->bseg) : nullptr, bv.n ? nullptr : P<unsigned>(c->edone), adapt_ratio,
+             P<double>(c->out3), c->stream);
   PE();
-  PB("size_factor");
-  if (bv.n)
+  if (bv.n) {
+    PB("size_factor");
     launch_size_factor_batch(P<double>(c->partials), bv, m.dim, P<double>(c->out3), c->stream);
-  else
-    launch_size_factor(P<double>(c->partials), nb, 0, adapt_ratio, 0, m.dim, P<double>(c->out3), c->stream);
-  PE();
+    PE();
+  }
   PB("average_f32");
   fast_average(m, P<float2>(c->q32), P<double>(c->out3), P<float2>(c->sz2), bv, c->stream);
   PE();
@@ -1576,7 +1582,7 @@ static int pass_fast(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_
                        sprg_ctx::kGuardCap, d_split, d_collapse, P<int>(c->fcnt) + 4, gs, bv, c->stream);
     PE();
   }
-  c->launches += 8 + kGuardStages;  // FP32-path kernels and guard kernels (listed_fits counts its own)
+  c->launches += (bv.n ? 8 : 7) + kGuardStages;  // FP32-path and guard kernels (listed_fits counts its own)
   c->size_valid = false;  // the FP64 size buffer is filled on demand
   c->L_valid = false;
   return check_launch(c, "fast pass");

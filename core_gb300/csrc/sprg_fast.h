@@ -32,8 +32,10 @@ void fast_recover_tiles(const DevMesh& m, const float* w, const uint4* td, uint4
                         const int4* tiles, int n_tiles, int* next, int grid, cudaStream_t s);
 // q: (h_max err^(-1/5), its relative error bound) per tet
 // seg (batch): one element range per block, nb = number of segments
+// done (one unsigned, zero between passes) and out3: the last block also
+// computes the size factor (one mesh; pass null for a batch)
 void fast_error(const DevMesh& m, const uint4* td, const float2* geo, const uint4* rec, float2* q, double* partials,
-                int nb, const int2* seg, cudaStream_t s);
+                int nb, const int2* seg, unsigned* done, double adapt_ratio, double* out3, cudaStream_t s);
 // sz2: (size, its relative error bound) per vertex
 void fast_average(const DevMesh& m, const float2* q, const double* out3, float2* sz2, BatchView bv, cudaStream_t s);
 void fast_measure(const DevMesh& m, const float* half_len, const float2* sz2, uint32_t* split, uint32_t* collapse,

@@ -39,6 +39,7 @@
 //             list of edges whose distance to 0.5 / 1.5 is within the error
 //             bound (re-decided in FP64 by the guard kernels)
 #include "sprg_fast.h"
+#include "sprg_reduce.cuh"
 
 namespace sprg {
 namespace {
@@ -592,10 +593,15 @@ __device__ __forceinline__ double warp_pair_total(PairSum p) {
 
 // grid-stride over all elements, or (batch) block b over the element range
 // seg[b] of one mesh, so each block's partials belong to one mesh
+// done != null (one mesh): the last block to finish reduces the partials
+// and writes the size factor to out3 (the work of the FP64 size-factor
+// kernel, the same function), then clears the counter for the next pass
 __global__ void __launch_bounds__(kBlock) k_fast_error(DevMesh m, const uint4* __restrict__ td,
                                                        const float2* __restrict__ geo,
                                                        const uint4* __restrict__ rec, float2* __restrict__ q,
-                                                       double* __restrict__ partials, const int2* __restrict__ seg) {
+                                                       double* __restrict__ partials, const int2* __restrict__ seg,
+                                                       unsigned* __restrict__ done, double adapt_ratio, int dim,
+                                                       double* __restrict__ out3) {
   __shared__ double sh[2][kBlock / 32];
   PairSum self{0.f, 0.f}, gsum{0.f, 0.f};
   int t_beg = blockIdx.x * blockDim.x + threadIdx.x, t_end = m.T, t_step = gridDim.x * blockDim.x;
@@ -676,6 +682,18 @@ __global__ void __launch_bounds__(kBlock) k_fast_error(DevMesh m, const uint4* _
     partials[2 * blockIdx.x] = a;
     partials[2 * blockIdx.x + 1] = b;
   }
+  if (!done) return;
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+    __threadfence();  // this block's partials before its arrival
+    last = atomicAdd(done, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();  // every block's partials are visible to the last one
+  __shared__ double shr[kBlock / 32];
+  rd_size_factor(partials, gridDim.x, 0, adapt_ratio, 0.0, dim, out3, shr);
+  if (threadIdx.x == 0) *done = 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -898,8 +916,8 @@ void fast_merge_ref(ExpandList xl, const double* rec64, uint4* rec, cudaStream_t
 }
 
 void fast_error(const DevMesh& m, const uint4* td, const float2* geo, const uint4* rec, float2* q, double* partials,
-                int nb, const int2* seg, cudaStream_t s) {
-  if (nb) k_fast_error<<<nb, kBlock, 0, s>>>(m, td, geo, rec, q, partials, seg);
+                int nb, const int2* seg, unsigned* done, double adapt_ratio, double* out3, cudaStream_t s) {
+  if (nb) k_fast_error<<<nb, kBlock, 0, s>>>(m, td, geo, rec, q, partials, seg, done, adapt_ratio, m.dim, out3);
 }
 
 void fast_average(const DevMesh& m, const float2* q, const double* out3, float2* sz2, BatchView bv, cudaStream_t s) {

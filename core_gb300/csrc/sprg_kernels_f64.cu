@@ -13,6 +13,7 @@
 
 #include "sprg_internal.h"
 #include "sprg_refmath.cuh"
+#include "sprg_reduce.cuh"
 
 namespace sprg {
 
@@ -771,32 +772,12 @@ __global__ void __launch_bounds__(kBlock) k_error(DevMesh m, const double* __res
 }
 
 // one block: fixed-order reduction of the partials, then the size factor
+// (the FP32 error kernel's last block runs the same function)
 __global__ void __launch_bounds__(kBlock) k_size_factor(const double* __restrict__ partials, int nb, int mode,
                                                         double adapt_ratio, double target, int dim,
                                                         double* out3) {
   __shared__ double sh[kBlock / 32];
-  double a = 0, g = 0;
-  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
-    a += partials[2 * i];
-    g += partials[2 * i + 1];
-  }
-  double snorm = block_sum(a, sh);
-  double gsum = block_sum(g, sh);
-  if (threadIdx.x == 0) {
-    double p = 1, d = dim, sf;
-    if (mode == 0) {
-      double esn = sqrt(snorm);
-      double aa = adapt_ratio * adapt_ratio * esn * esn;
-      double b = aa / gsum;
-      sf = pow(b, 1.0 / (2.0 * p));
-    } else {
-      sf = pow((gsum / target), (1.0 / dim));
-    }
-    (void)d;
-    out3[0] = snorm;
-    out3[1] = gsum;
-    out3[2] = sf;
-  }
+  rd_size_factor(partials, nb, mode, adapt_ratio, target, dim, out3, sh);
 }
 
 // one block per mesh of a batch: its segments' partials in a fixed order
