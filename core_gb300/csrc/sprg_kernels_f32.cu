@@ -39,6 +39,7 @@
 //             list of edges whose distance to 0.5 / 1.5 is within the error
 //             bound (re-decided in FP64 by the guard kernels)
 #include "sprg_fast.h"
+#include "sprg_ld.cuh"
 #include "sprg_reduce.cuh"
 
 namespace sprg {
@@ -279,15 +280,6 @@ __device__ __forceinline__ void rdiff(const float4& ah, const float4& al, const 
   float e;
   two_sum(ah.w, -bh.w, dh.w, e);
   dl.w = (al.w - bl.w) + e;
-}
-
-// one vertex record (32 bytes, hi then lo) with a single 256-bit load: a
-// warp's gather then asks L1 for one sector per lane instead of two.  The
-// records start at a cudaMalloc base (256-byte aligned), 32 bytes each.
-__device__ __forceinline__ void ld_record(const float4* p, float4& h, float4& l) {
-  asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
-      : "=f"(h.x), "=f"(h.y), "=f"(h.z), "=f"(h.w), "=f"(l.x), "=f"(l.y), "=f"(l.z), "=f"(l.w)
-      : "l"(p));
 }
 
 __device__ __forceinline__ TetData load_tet(const float4* __restrict__ vr, int4 tv) {

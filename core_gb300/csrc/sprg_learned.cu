@@ -24,6 +24,7 @@
 #include <cuda_bf16.h>
 #include <cub/cub.cuh>
 
+#include "sprg_ld.cuh"
 #include "sprg_learned.h"
 
 namespace sprg {
@@ -703,14 +704,6 @@ __global__ void k_lfallback(DevMesh m, LearnMesh lm, const float4* __restrict__ 
 // ---------------------------------------------------------------------------
 // two elements per iteration, all loads issued before use; w dV and h_max
 // are the per-mesh element geometry
-// one 32-byte vertex record with a single 256-bit load (one L1 sector per
-// lane instead of two); the records start at a cudaMalloc base, 32 bytes each
-__device__ __forceinline__ void ld_record32(const float4* p, float4& a, float4& b) {
-  asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
-      : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
-      : "l"(p));
-}
-
 __global__ void __launch_bounds__(kBlock) k_lerror(DevMesh m, const float4* __restrict__ rec,
                                                    const float2* __restrict__ geo, float* __restrict__ q,
                                                    double* __restrict__ partials) {
@@ -733,7 +726,7 @@ __global__ void __launch_bounds__(kBlock) k_lerror(DevMesh m, const float4* __re
     for (int i = 0; i < 2; ++i) {
       const int vs[4] = {tv[i].x, tv[i].y, tv[i].z, tv[i].w};
 #pragma unroll
-      for (int k = 0; k < 4; ++k) ld_record32(rec + 2 * (size_t)vs[k], P[i][k], E[i][k]);
+      for (int k = 0; k < 4; ++k) ld_record(rec + 2 * (size_t)vs[k], P[i][k], E[i][k]);
     }
 #pragma unroll
     for (int i = 0; i < 2; ++i) {
