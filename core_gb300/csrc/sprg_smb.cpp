@@ -73,6 +73,15 @@ struct Reader {
     }
     return true;
   }
+  // bytes from the current position to the end of the file, or -1
+  int64_t remaining() {
+    if (!ok) return -1;
+    const long here = std::ftell(f);
+    if (here < 0 || std::fseek(f, 0, SEEK_END) != 0) return -1;
+    const long end = std::ftell(f);
+    if (end < 0 || std::fseek(f, here, SEEK_SET) != 0) return -1;
+    return (int64_t)end - here;
+  }
 };
 
 struct SmbMesh {
@@ -98,6 +107,12 @@ int read_smb(const char* path, SmbMesh& s, bool with_arrays) {
   if ((s.dim == 3 && (!s.n[kTet] || !s.n[kTri])) || (s.dim == 2 && (s.n[kTet] || !s.n[kTri])) || !s.n[kEdge] ||
       !s.n[kVert])
     return SPRG_EINVAL;
+  // the connectivity and coordinates the counts announce must be in the
+  // file, so that a short or damaged file sizes no allocation
+  const uint64_t need =
+      4ull * (2ull * s.n[kEdge] + 3ull * s.n[kTri] + 4ull * s.n[kTet]) + 24ull * s.n[kVert];
+  const int64_t have = r.remaining();
+  if (have < 0 || (uint64_t)have < need) return SPRG_EINVAL;
   if (!with_arrays) return SPRG_OK;
   try {
     s.edge_verts.resize(2 * (size_t)s.n[kEdge]);

@@ -183,3 +183,95 @@ def test_writer_refuses_inconsistent_meshes(host_lib, tmp_path):
     dup = Mesh(3, m.coords, m.elem_verts, np.vstack([m.edge_verts, m.edge_verts[:1]]))
     with pytest.raises(K.SprgError):
         write_smb(dup, tmp_path / "dup0.smb")
+
+
+def _required_bytes(o):
+    """Header, counts, connectivity and coordinates of a tet file: the part
+    the reader needs."""
+    E, F, T = len(o.down(1)), len(o.down(2)), len(o.down(3))
+    return 16 + 32 + 4 * (2 * E + 3 * F + 4 * T) + 24 * o.V
+
+
+def test_counts_never_exceed_the_file(host_lib, oracle_lib, tmp_path):
+    """A file whose counts announce more entities than it holds is refused
+    by sprg_smb_counts, before a caller sizes arrays by them."""
+    import ctypes
+    from core_gb300 import _lib as K
+    o = oracle_lib.OracleMesh.box(2, 2, 2)
+    good = tmp_path / "good0.smb"
+    write_smb(good, 3, o.coords, o.down(1), o.down(2), o.down(3))
+    raw = bytearray(good.read_bytes())
+    for slot, value in ((0, 50_000_000), (1, 90_000_000), (2, 7_000_000), (7, 99_999_999), (0, o.V + 1)):
+        bad = bytearray(raw)
+        bad[16 + 4 * slot: 20 + 4 * slot] = struct.pack(">I", value)
+        p = tmp_path / f"count{slot}_{value}0.smb"
+        p.write_bytes(bytes(bad))
+        dim, V, T, E = ctypes.c_int(), ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        rc = host_lib.sprg_smb_counts(str(p).encode(), ctypes.byref(dim), ctypes.byref(V), ctypes.byref(T),
+                                      ctypes.byref(E))
+        if value > 1000:
+            assert rc == K.SPRG_EINVAL, (slot, value)
+        else:
+            # one more vertex than written: the file is still long enough
+            # (its tail holds more than 24 bytes), the read must then refuse
+            # or return a mesh whose ids stay in range
+            assert rc in (K.SPRG_OK, K.SPRG_EINVAL)
+
+
+def test_truncated_files(host_lib, oracle_lib, tmp_path):
+    """Cut anywhere inside the part the reader needs, a file is refused; cut
+    after it (parametric coordinates, remotes, classification, tags), it
+    reads as the whole file does."""
+    from core_gb300 import _lib as K
+    from core_gb300.mesh import read_smb
+    o = oracle_lib.OracleMesh.box(2, 1, 1)
+    good = tmp_path / "good0.smb"
+    write_smb(good, 3, o.coords, o.down(1), o.down(2), o.down(3))
+    raw = good.read_bytes()
+    need = _required_bytes(o)
+    want = read_smb(good)
+    rng = np.random.default_rng(5)
+    cuts = sorted(set([0, 3, 16, 47, 48, need - 1, need, need + 1, len(raw) - 1]
+                      + list(rng.integers(0, len(raw), 40))))
+    for cut in cuts:
+        p = tmp_path / f"cut{cut}0.smb"
+        p.write_bytes(raw[:cut])
+        if cut < need:
+            with pytest.raises(K.SprgError) as ei:
+                read_smb(p)
+            assert ei.value.code == K.SPRG_EINVAL, cut
+        else:
+            got = read_smb(p)
+            assert np.array_equal(got.elem_verts, want.elem_verts)
+            assert np.array_equal(got.coords, want.coords)
+
+
+def test_damaged_files_are_read_or_refused(host_lib, oracle_lib, tmp_path):
+    """Bytes overwritten at random inside the part the reader needs: every
+    read either returns an error code or a mesh whose ids stay in range."""
+    from core_gb300 import _lib as K
+    from core_gb300.mesh import read_smb
+    o = oracle_lib.OracleMesh.box(2, 2, 1)
+    good = tmp_path / "good0.smb"
+    write_smb(good, 3, o.coords, o.down(1), o.down(2), o.down(3))
+    raw = good.read_bytes()
+    need = _required_bytes(o)
+    rng = np.random.default_rng(9)
+    refused = accepted = 0
+    for trial in range(300):
+        bad = bytearray(raw)
+        for _ in range(int(rng.integers(1, 6))):
+            pos = int(rng.integers(0, need))
+            bad[pos] = int(rng.integers(0, 256))
+        p = tmp_path / "damaged0.smb"
+        p.write_bytes(bytes(bad))
+        try:
+            m = read_smb(p)
+        except K.SprgError as e:
+            assert e.code in (K.SPRG_EINVAL, K.SPRG_ENOMEM)
+            refused += 1
+            continue
+        accepted += 1
+        assert m.elem_verts.min() >= 0 and m.elem_verts.max() < m.n_verts
+        assert m.edge_verts.min() >= 0 and m.edge_verts.max() < m.n_verts
+    assert refused > 0 and accepted > 0
