@@ -229,3 +229,28 @@ def test_apply_marks_arguments(lib):
     assert lib.sprg_apply_marks(4, None, None, None, ctypes.byref(n), ctypes.byref(n)) == _lib.SPRG_EINVAL
     assert lib.sprg_apply_marks(4, None, None, flags.ctypes.data, None, None) == _lib.SPRG_OK
     assert not flags.any()
+
+
+def test_box_arguments(lib):
+    V, T, E = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+    for nx, ny, nz in ((0, 1, 1), (1, 0, 1), (1, 1, -1), (-3, 2, 2)):
+        assert lib.sprg_box_counts(nx, ny, nz, ctypes.byref(V), ctypes.byref(T), ctypes.byref(E)) \
+            == _lib.SPRG_EINVAL
+    assert lib.sprg_box_counts(1, 1, 1, None, ctypes.byref(T), ctypes.byref(E)) == _lib.SPRG_EINVAL
+    # counts past 32-bit ids are reported but the box is not built
+    assert lib.sprg_box_counts(1024, 1024, 1024, ctypes.byref(V), ctypes.byref(T), ctypes.byref(E)) == _lib.SPRG_OK
+    assert T.value == 6 * 1024 ** 3
+    one = np.zeros(8, np.float64)
+    assert lib.sprg_box_fill(1024, 1024, 1024, 1.0, 1.0, 1.0, one.ctypes.data, one.ctypes.data,
+                             one.ctypes.data) == _lib.SPRG_EINVAL
+    assert lib.sprg_box_fill(1, 1, 1, 1.0, 1.0, 1.0, None, None, None) == _lib.SPRG_EINVAL
+
+
+def test_max_iterations_rule_host(lib):
+    """updateMaxIterBasedOnSize (ma/maInput.cc:174-190): ceil(log2 L) + 1,
+    and 10 once ceil(log2 L) reaches 10."""
+    import math
+    for L in (1.0000001, 1.5, 2.0, 2.5, 7.9, 64.0, 300.0, 511.0, 512.0, 513.0, 1e6):
+        c = math.ceil(math.log2(L))
+        want = 10 if c >= 10 else c + 1
+        assert lib.sprg_max_iterations_for_length(L) == want, L
