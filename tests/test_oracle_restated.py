@@ -1,0 +1,147 @@
+"""A second, independent restatement of the gradient at integration points
+and of the SPR patch fit, in numpy, against the oracle's C restatement.
+
+Followed here from the reference directly:
+* spr/sprGetGradIPField.cc:15-65 - order-1 elements carry one integration
+  point, the element's constant gradient of the linear interpolant;
+* spr/sprRecoverField.cc:155-192 - a vertex's patch starts as its adjacent
+  elements; while it has fewer points than polynomial terms or its
+  least-squares matrix is rank-deficient, it takes (from the elements it had
+  when growth began) the elements that share a face, then an edge, then a
+  vertex with them, testing after each stage, and repeats from the larger
+  set (spr/sprRecoverField.cc:365-386);
+* spr/sprRecoverField.cc:193-353 - sample points at the element centroids,
+  polynomial terms [1, x, y(, z)], the least-squares fit evaluated at the
+  vertex.
+numpy's lstsq solves the same full-rank systems through another
+factorisation, so values agree to rounding (1e-10 relative), and the
+growth decisions are checked to sit far from the rank threshold."""
+import itertools
+
+import numpy as np
+import pytest
+
+
+def jittered(o, n, nz, seed):
+    rng = np.random.default_rng(seed)
+    x = o.coords.copy()
+    h = np.array([1.0 / n, 1.0 / n, 1.0 / nz if nz else 0.0])
+    inner = np.all((x > 1e-12) & (x < 1 - 1e-12), axis=1) if nz else \
+        np.all((x[:, :2] > 1e-12) & (x[:, :2] < 1 - 1e-12), axis=1)
+    x[inner] += rng.uniform(-0.2, 0.2, (inner.sum(), 3)) * h
+    o.set_coords(x)
+    return x
+
+
+def field(x):
+    return np.sin(2.1 * x[:, 0]) * np.cos(1.3 * x[:, 1]) + 0.7 * x[:, 2] ** 2 + 0.3 * x[:, 0] * x[:, 1]
+
+
+def grad_ip_numpy(x, ev, f):
+    d = ev.shape[1] - 1
+    g = np.empty((ev.shape[0], 3))
+    for t, vs in enumerate(ev):
+        J = (x[vs[1:]] - x[vs[0]])[:, :d]
+        g[t, :d] = np.linalg.solve(J, f[vs[1:]] - f[vs[0]])
+        g[t, d:] = 0.0
+    return g
+
+
+class Adjacency:
+    """Downward entities of every element as vertex tuples and the elements
+    around each entity (the MDS upward adjacency, as sets)."""
+
+    def __init__(self, ev):
+        self.ev = ev
+        d = ev.shape[1] - 1
+        self.down = {k: [] for k in range(d)}
+        self.up = {k: {} for k in range(d)}
+        for t, vs in enumerate(ev):
+            for k in range(d):
+                ents = [tuple(sorted(c)) for c in itertools.combinations(vs, k + 1)]
+                self.down[k].append(ents)
+                for e in ents:
+                    self.up[k].setdefault(e, set()).add(t)
+
+    def sharing(self, elems, k):
+        out = set()
+        for t in elems:
+            for e in self.down[k][t]:
+                out |= self.up[k][e]
+        return out
+
+
+def fit_matrix(x, elems, ev, d):
+    c = x[ev[sorted(elems)]].mean(axis=1)[:, :d]
+    return np.hstack([np.ones((len(elems), 1)), c])
+
+
+def recover_numpy(x, ev, ip):
+    d = ev.shape[1] - 1
+    nterms = d + 1
+    adj = Adjacency(ev)
+    out = np.empty((x.shape[0], ip.shape[1]))
+    grown = 0
+    margins = []
+
+    def enough(elems):
+        if len(elems) < nterms:
+            return False
+        s = np.linalg.svd(fit_matrix(x, elems, ev, d), compute_uv=False)
+        margins.append(s[-1])
+        return s[-1] > 1e-8
+
+    for v in range(x.shape[0]):
+        patch = set(adj.up[0][(v,)])
+        if not enough(patch):
+            grown += 1
+            while True:
+                old = set(patch)
+                done = False
+                for k in range(d - 1, -1, -1):
+                    patch |= adj.sharing(old, k)
+                    if enough(patch):
+                        done = True
+                        break
+                if done:
+                    break
+                assert len(patch) > len(old), "no growth possible"
+        els = sorted(patch)
+        A = fit_matrix(x, patch, ev, d)
+        coef, *_ = np.linalg.lstsq(A, ip[els], rcond=None)
+        out[v] = np.concatenate([[1.0], x[v, :d]]) @ coef
+    return out, grown, np.array(margins)
+
+
+@pytest.mark.parametrize("n,nz,seed", [(4, 3, 1), (5, 0, 2), (3, 3, 7)])
+def test_spr_restated_twice(oracle_lib, n, nz, seed):
+    o = oracle_lib.OracleMesh.box(n, n - 1 if nz else n, nz)
+    x = jittered(o, n, nz, seed)
+    ev = o.elem_verts
+    f = field(x)
+    ip = o.grad_ip(f)
+    ip_np = grad_ip_numpy(x, ev, f)
+    scale = np.abs(ip_np).max()
+    assert np.abs(ip - ip_np).max() <= 1e-12 * scale
+    rc, rec, nexp, fail = o.recover(ip)
+    assert rc == 0 and fail == -1
+    rec_np, grown, margins = recover_numpy(x, ev, ip_np)
+    # every growth decision far from the 1e-10 rank threshold of mth::decomposeQR
+    assert not np.any((margins > 1e-13) & (margins < 1e-6))
+    assert nexp == grown
+    assert np.abs(rec - rec_np).max() <= 1e-10 * np.abs(rec_np).max()
+
+
+def test_linear_field_is_recovered_exactly_by_both(oracle_lib):
+    """SPR's patch test: the gradient of a linear field is constant, so
+    both restatements return it at every vertex, grown patches included."""
+    o = oracle_lib.OracleMesh.box(3, 3, 2)
+    x = jittered(o, 3, 2, 4)
+    g = np.array([0.4, -1.1, 2.5])
+    f = x @ g - 0.2
+    ip = o.grad_ip(f)
+    rc, rec, nexp, fail = o.recover(ip)
+    rec_np, grown, _ = recover_numpy(x, o.elem_verts, grad_ip_numpy(x, o.elem_verts, f))
+    assert rc == 0 and nexp == grown > 0
+    assert np.abs(rec - g).max() < 1e-10
+    assert np.abs(rec_np - g).max() < 1e-10
