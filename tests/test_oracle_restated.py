@@ -145,3 +145,90 @@ def test_linear_field_is_recovered_exactly_by_both(oracle_lib):
     assert rc == 0 and nexp == grown > 0
     assert np.abs(rec - g).max() < 1e-10
     assert np.abs(rec_np - g).max() < 1e-10
+
+
+def size_field_numpy(x, ev, ip, rec, adapt_ratio):
+    """getSPRSizeField (spr/sprEstimateError.cc:98-321) for order-1 fields:
+    integration order 1 (one point at the centroid, w dV = the element's
+    measure), recovered order p = 1.  Returns (vertex sizes, element sizes,
+    ||eps*||^2, sum of err^(2d/(2p+d)), size factor)."""
+    d = ev.shape[1] - 1
+    p = 1.0
+    X = x[ev][:, :, :d]
+    J = X[:, 1:] - X[:, :1]
+    vol = np.abs(np.linalg.det(J)) / (6.0 if d == 3 else 2.0)
+    star_c = rec[ev].mean(axis=1)                       # eps* at the centroid
+    self_product = np.sum(np.sum(star_c * star_c, axis=1) * vol)
+    e2 = np.sum((ip - star_c) ** 2, axis=1) * vol       # element error integral
+    G = np.sum(np.sqrt(e2) ** (2 * d / (2 * p + d)))
+    a = adapt_ratio * adapt_ratio * np.sqrt(self_product) ** 2
+    factor = (a / G) ** (1.0 / (2.0 * p))
+    pairs = list(itertools.combinations(range(d + 1), 2))
+    h = np.max([np.linalg.norm(x[ev[:, i]] - x[ev[:, j]], axis=1) for i, j in pairs], axis=0)
+    esize = h * np.sqrt(e2) ** (-(2 / (2 * p + d))) * factor
+    V = x.shape[0]
+    s = np.zeros(V)
+    c = np.zeros(V)
+    for k in range(d + 1):
+        np.add.at(s, ev[:, k], esize)
+        np.add.at(c, ev[:, k], 1)
+    return s / c, esize, self_product, G, factor
+
+
+@pytest.mark.parametrize("n,nz,seed,ratio", [(4, 3, 1, 0.1), (6, 0, 2, 0.05), (3, 3, 7, 0.008)])
+def test_size_field_restated_twice(oracle_lib, n, nz, seed, ratio):
+    o = oracle_lib.OracleMesh.box(n, n - 1 if nz else n, nz)
+    x = jittered(o, n, nz, seed)
+    ev = o.elem_verts
+    f = field(x)
+    ip = o.grad_ip(f)
+    rc, size, rec, esize, err, info = o.size_field(ip, ratio)
+    assert rc == 0
+    size_np, esize_np, sp, G, factor = size_field_numpy(x, ev, ip, rec, ratio)
+    assert abs(info["eps_star_norm2"] - sp) <= 1e-12 * sp
+    assert abs(info["error_sum"] - G) <= 1e-12 * G
+    assert abs(info["size_factor"] - factor) <= 1e-12 * factor
+    assert np.abs(esize - esize_np).max() <= 1e-11 * np.abs(esize_np).max()
+    assert np.abs(size - size_np).max() <= 1e-11 * np.abs(size_np).max()
+
+
+def target_size_field_numpy(x, ev, ip, rec, target, alpha, beta):
+    """getTargetSPRSizeField (spr/sprEstimateTargetError.cc:129-258): size
+    factor (G / N)^(1/d), the new element size clamped to [alpha h, beta h],
+    then the vertex average."""
+    d = ev.shape[1] - 1
+    p = 1.0
+    X = x[ev][:, :, :d]
+    vol = np.abs(np.linalg.det(X[:, 1:] - X[:, :1])) / (6.0 if d == 3 else 2.0)
+    e2 = np.sum((ip - rec[ev].mean(axis=1)) ** 2, axis=1) * vol
+    G = np.sum(np.sqrt(e2) ** (2 * d / (2 * p + d)))
+    factor = (G / target) ** (1.0 / d)
+    pairs = list(itertools.combinations(range(d + 1), 2))
+    h = np.max([np.linalg.norm(x[ev[:, i]] - x[ev[:, j]], axis=1) for i, j in pairs], axis=0)
+    hn = factor * np.sqrt(e2) ** (-2.0 / (2.0 * p + d)) * h
+    hn = np.where(hn < alpha * h, alpha * h, hn)
+    hn = np.where(hn > beta * h, beta * h, hn)
+    s = np.zeros(x.shape[0])
+    c = np.zeros(x.shape[0])
+    for k in range(d + 1):
+        np.add.at(s, ev[:, k], hn)
+        np.add.at(c, ev[:, k], 1)
+    return s / c, hn, G, factor
+
+
+@pytest.mark.parametrize("n,nz,seed,target,alpha,beta", [(4, 3, 1, 5000, 0.25, 2.0), (6, 0, 2, 300, 0.5, 1.5),
+                                                          (3, 3, 7, 40, 0.25, 2.0)])
+def test_target_size_field_restated_twice(oracle_lib, n, nz, seed, target, alpha, beta):
+    o = oracle_lib.OracleMesh.box(n, n - 1 if nz else n, nz)
+    x = jittered(o, n, nz, seed)
+    ev = o.elem_verts
+    ip = o.grad_ip(field(x))
+    rc, size, rec, esize, err, info = o.size_field(ip, 0.0, target=target, alpha=alpha, beta=beta)
+    assert rc == 0
+    size_np, esize_np, G, factor = target_size_field_numpy(x, ev, ip, rec, target, alpha, beta)
+    assert abs(info["error_sum"] - G) <= 1e-12 * G
+    assert abs(info["size_factor"] - factor) <= 1e-12 * factor
+    # the cases clamp 7 elements at alpha h (first), 32 at alpha h and 3 at
+    # beta h (second), 11 at beta h (third)
+    assert np.abs(esize - esize_np).max() <= 1e-11 * np.abs(esize_np).max()
+    assert np.abs(size - size_np).max() <= 1e-11 * np.abs(size_np).max()
