@@ -232,3 +232,34 @@ def test_target_size_field_restated_twice(oracle_lib, n, nz, seed, target, alpha
     # beta h (second), 11 at beta h (third)
     assert np.abs(esize - esize_np).max() <= 1e-11 * np.abs(esize_np).max()
     assert np.abs(size - size_np).max() <= 1e-11 * np.abs(size_np).max()
+
+
+def iso_lengths_numpy(x, ed, size):
+    """MetricSizeField::measure of an edge under an isotropic size field
+    (ma/maSize.cc:208-216, 140-196): apf's edge rule of accuracy 3 (two
+    points at +-0.577350269189626, weight 1, apf/apfIntegrate.cc:41-52) of
+    |dx/dxi| / h(xi), h interpolated linearly along the edge."""
+    a, b = ed[:, 0], ed[:, 1]
+    half = np.linalg.norm(x[b] - x[a], axis=1) / 2.0
+    out = np.zeros(ed.shape[0])
+    for xi in (0.577350269189626, -0.577350269189626):
+        h = size[a] * (1 - xi) / 2 + size[b] * (1 + xi) / 2
+        out += 1.0 * half / h
+    return out
+
+
+@pytest.mark.parametrize("n,nz,seed", [(4, 3, 1), (6, 0, 2)])
+def test_iso_edge_lengths_and_marks_restated_twice(oracle_lib, n, nz, seed):
+    o = oracle_lib.OracleMesh.box(n, n - 1 if nz else n, nz)
+    x = jittered(o, n, nz, seed)
+    rng = np.random.default_rng(seed)
+    size = rng.uniform(0.05, 0.6, o.V)
+    L = o.measure(size=size)
+    L_np = iso_lengths_numpy(x, o.edge_verts, size)
+    assert np.abs(L - L_np).max() <= 1e-13 * L_np.max()
+    # markEdgesToSplit / markEdgesToCollapse: > 1.5 and < 0.5 (ma/maSize.h:26-27)
+    flags = np.zeros(o.E, np.int32)
+    rc, ns = oracle_lib.mark_edges(L, 0, flags)
+    assert rc == 0 and ns == int(np.sum(L_np > 1.5))
+    rc, nc = oracle_lib.mark_edges(L, 1, flags)
+    assert rc == 0 and nc == int(np.sum(L_np < 0.5))
