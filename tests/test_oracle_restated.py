@@ -263,3 +263,34 @@ def test_iso_edge_lengths_and_marks_restated_twice(oracle_lib, n, nz, seed):
     assert rc == 0 and ns == int(np.sum(L_np > 1.5))
     rc, nc = oracle_lib.mark_edges(L, 1, flags)
     assert rc == 0 and nc == int(np.sum(L_np < 0.5))
+
+
+def iso_quality_numpy(x, ev, size):
+    """measureTetQuality / measureTriQuality with useMax = true under an
+    isotropic size field (ma/maQuality.cc:83-167): the metric of the element
+    vertex with the largest det Q (the smallest h), edge lengths and measure
+    in it; 15552 V^2 / (sum l^2)^3 with V's sign for tets, 48 A^2 / (sum
+    l^2)^2 for triangles."""
+    d = ev.shape[1] - 1
+    h = size[ev].min(axis=1)
+    X = x[ev]
+    pairs = list(itertools.combinations(range(d + 1), 2))
+    s = sum(np.sum((X[:, j] - X[:, i]) ** 2, axis=1) for i, j in pairs) / h ** 2
+    if d == 3:
+        V = np.linalg.det(X[:, 1:] - X[:, :1]) / 6.0 / h ** 3
+        return np.sign(V) * 15552.0 * V * V / (s * s * s)
+    e1, e2 = X[:, 1] - X[:, 0], X[:, 2] - X[:, 0]
+    A = 0.5 * np.linalg.norm(np.cross(e1, e2), axis=1) / h ** 2
+    return 48.0 * A * A / (s * s)
+
+
+@pytest.mark.parametrize("n,nz,seed", [(4, 3, 1), (6, 0, 2), (3, 2, 5)])
+def test_iso_quality_restated_twice(oracle_lib, n, nz, seed):
+    o = oracle_lib.OracleMesh.box(n, n - 1 if nz else n, nz)
+    x = jittered(o, n, nz, seed)
+    rng = np.random.default_rng(seed + 10)
+    size = rng.uniform(0.05, 0.6, o.V)
+    q = o.quality(size=size)
+    q_np = iso_quality_numpy(x, o.elem_verts, size)
+    assert np.all(q > 0) and np.all(q <= 1 + 1e-12)
+    assert np.abs(q - q_np).max() <= 1e-12
