@@ -294,3 +294,53 @@ def test_iso_quality_restated_twice(oracle_lib, n, nz, seed):
     q_np = iso_quality_numpy(x, o.elem_verts, size)
     assert np.all(q > 0) and np.all(q <= 1 + 1e-12)
     assert np.abs(q - q_np).max() <= 1e-12
+
+
+def aniso_lengths_numpy(x, ed, sizes, frames):
+    """AnisoSizeField::measure of an edge (ma/maSize.cc:94-121, 364-412):
+    at each point of the two-point rule the sizes and the frame R are
+    interpolated linearly, R is re-orthogonalised (first column normalised,
+    second made orthogonal to it and normalised, third their cross
+    product), Q = R diag(1/h), and the edge's tangent row dx/dxi times Q
+    gives the length element."""
+    a, b = ed[:, 0], ed[:, 1]
+    g = (x[b] - x[a]) / 2.0
+    Ra, Rb = frames[a].reshape(-1, 3, 3), frames[b].reshape(-1, 3, 3)
+    out = np.zeros(ed.shape[0])
+    for xi in (0.577350269189626, -0.577350269189626):
+        wa, wb = (1 - xi) / 2, (1 + xi) / 2
+        h = sizes[a] * wa + sizes[b] * wb
+        RT = np.transpose(Ra * wa + Rb * wb, (0, 2, 1))
+        r0 = RT[:, 0] / np.linalg.norm(RT[:, 0], axis=1)[:, None]
+        r1 = RT[:, 1] - r0 * np.sum(r0 * RT[:, 1], axis=1)[:, None]
+        r1 = r1 / np.linalg.norm(r1, axis=1)[:, None]
+        r2 = np.cross(r0, r1)
+        R = np.stack([r0, r1, r2], axis=2)              # columns: the directions
+        gq = np.einsum("ei,eik->ek", g, R) / h
+        out += np.linalg.norm(gq, axis=1)
+    return out
+
+
+def random_frames(rng, V, spread):
+    """Rotations near a common one, so neighbouring frames interpolate to a
+    usable frame."""
+    base = np.linalg.qr(rng.normal(size=(3, 3)))[0]
+    F = np.empty((V, 3, 3))
+    for v in range(V):
+        w = rng.normal(size=3) * spread
+        K = np.array([[0, -w[2], w[1]], [w[2], 0, -w[0]], [-w[1], w[0], 0]])
+        F[v] = base @ (np.eye(3) + K + K @ K / 2)     # close to a rotation
+        F[v] = np.linalg.qr(F[v])[0]
+    return F.reshape(V, 9)
+
+
+@pytest.mark.parametrize("n,nz,seed", [(4, 3, 1), (5, 0, 2)])
+def test_aniso_edge_lengths_restated_twice(oracle_lib, n, nz, seed):
+    o = oracle_lib.OracleMesh.box(n, n - 1 if nz else n, nz)
+    x = jittered(o, n, nz, seed)
+    rng = np.random.default_rng(seed + 20)
+    sizes = rng.uniform(0.05, 0.6, (o.V, 3))
+    frames = random_frames(rng, o.V, 0.3)
+    L = o.measure(sizes=sizes, frames=frames)
+    L_np = aniso_lengths_numpy(x, o.edge_verts, sizes, frames)
+    assert np.abs(L - L_np).max() <= 1e-12 * L_np.max()
