@@ -11,7 +11,9 @@ same pass through the public host API (sprg_estimate_and_mark) with pinned
 host buffers, copies included.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp64|fp32]
-  python bench.py --impl reference ...   # the CPU oracle port on the host cores
+  python bench.py --impl reference ...   # the reference's CPU path (compiled from
+                                         # source where its tree is present; else
+                                         # the oracle port) on the host cores
 
 Multi-GPU: one process per GPU (torchrun), each an independent replica of
 the workload (the pass needs no exchange); value = total vertices / max time.
@@ -172,18 +174,37 @@ def summarize_clocks(lines):
 # ---------------------------------------------------------------------------
 # CPU arms
 # ---------------------------------------------------------------------------
-def cpu_port_run(budget_s, threads, n_sample=None, ratio=0.008):
-    """Times the oracle port of the reference path on the host cores on a
-    bounded sample of the same workload family.  Returns (vertices/s, desc)."""
+def cpu_sample(n, seed=4):
+    """The CPU baselines' sample: the n^3 box of the benchmark's family, built
+    by the oracle's own MDS box builder (no product code is loaded), interior
+    jitter +-0.2h and the 4-bump + ramp field with the benchmark's seed,
+    restated with numpy (the same numbers core_gb300.workload gives)."""
     import oracle
-    from core_gb300 import workload
-    used = oracle.set_threads(threads)
-    n = n_sample or 48
-    ratio = ratio * n / 160.0  # same lengths-to-size regime as the 160^3 workload
-    m = workload.box(n, jitter=0.2, seed=4)
-    u = workload.bump_field(m.coords, seed=4)
     o = oracle.OracleMesh.box(n, n, n)
-    o.set_coords(m.coords)
+    x = o.coords.copy()
+    rng = np.random.Generator(np.random.PCG64(seed))
+    d = rng.uniform(-0.2 / n, 0.2 / n, size=x.shape)
+    d[np.any((x == 0.0) | (x == 1.0), axis=1)] = 0.0
+    x = x + d
+    rng = np.random.Generator(np.random.PCG64(seed))
+    c = rng.uniform(0.0, 1.0, size=(4, 3))
+    w = rng.uniform(0.05, 0.2, size=4)
+    u = x @ np.array([0.3, -0.2, 0.1])
+    for k in range(4):
+        u = u + np.exp(-((x - c[k]) ** 2).sum(axis=1) / (2 * w[k] ** 2))
+    o.set_coords(x)
+    return o, x, u
+
+
+def cpu_port_run(budget_s, threads, n=48, ratio=0.008):
+    """Times the oracle port of the reference path (C, the reference's
+    operation order, pinned bitwise to it) on `threads` host threads on a
+    bounded sample of the benchmark's workload family.  Returns (vertices/s,
+    desc)."""
+    import oracle
+    used = oracle.set_threads(threads)
+    ratio = ratio * n / 160.0
+    o, _, u = cpu_sample(n)
     o.estimate_and_mark(u, ratio)  # warm
     t0 = time.perf_counter()
     passes = 0
@@ -195,34 +216,78 @@ def cpu_port_run(budget_s, threads, n_sample=None, ratio=0.008):
         if el >= budget_s or passes >= 1000:
             break
     V = (n + 1) ** 3
-    return V * passes / el, {"cores": used, "sample": f"{passes} passes of the {n}^3 jittered box "
-                                                         f"({V} vertices, {6 * n ** 3} tets) in {el:.1f} s"}
+    return V * passes / el, {"cores": used, "kind": "port",
+                             "sample": f"{passes} passes of the {n}^3 jittered box ({V} vertices, {6 * n ** 3} tets, "
+                                       f"adapt ratio {ratio:g}) in {el:.1f} s on {used} threads (oracle port, "
+                                       "OpenMP; pinned bitwise to the reference by tests/test_reference_pin.py)"}
+
+
+def cpu_reference_run(budget_s, n=24, ratio=0.008):
+    """Times the reference's own path, compiled from its sources
+    (oracle/_ref/libspr_ref.so): getGradIPField -> getSPRSizeField ->
+    ma::configure -> markEdgesToCollapse -> markEdgesToSplit on an
+    apf::makeMdsBox mesh with the sample's coordinates and field, on one host
+    core (the path is serial).  Returns (vertices/s, desc) or None where the
+    library is absent (hosts without the reference tree)."""
+    from oracle import reference
+    if not reference.available():
+        return None
+    ratio = ratio * n / 160.0
+    _, x, u = cpu_sample(n)
+    r = reference.RefMesh.box(n, n, n)
+    r.set_coords(x)
+    passes, el, ph = 0, 0.0, np.zeros(4)
+    while el < budget_s and passes < 100:
+        *_, sec = r.estimate_and_mark(u, ratio)
+        ph += sec
+        el += float(sec.sum())
+        passes += 1
+    V = (n + 1) ** 3
+    return V * passes / el, {"cores": 1, "kind": "reference",
+                             "sample": f"{passes} passes of the {n}^3 jittered box ({V} vertices, {6 * n ** 3} tets, "
+                                       f"adapt ratio {ratio:g}) in {el:.1f} s on 1 core (the reference, serial; "
+                                       f"phases gradient {ph[0] / passes:.3f} s, size field {ph[1] / passes:.3f} s, "
+                                       f"configure {ph[2] / passes:.3f} s, marks {ph[3] / passes:.3f} s per pass; "
+                                       f"{os.cpu_count()} host cores)"}
+
+
+def cpu_baseline_run(budget_s, ratio):
+    """The reference itself where it was built on this host, else the port on
+    every host thread."""
+    got = cpu_reference_run(budget_s, ratio=ratio)
+    if got is None:
+        got = cpu_port_run(budget_s, os.cpu_count() or 1, ratio=ratio)
+    return got
 
 
 def reference_arm(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    threads = os.cpu_count() or 1
     steps = []
     desc = None
     budget = max(1.0, min(20.0, 60.0 / max(1, args.steps + args.warmup)))
     for i in range(args.warmup + args.steps):
-        v, desc = cpu_port_run(budget, threads, ratio=args.adapt_ratio)
+        v, desc = cpu_baseline_run(budget, args.adapt_ratio)
         if i >= args.warmup:
             steps.append(v)
     value = float(np.mean(steps))
+    note = ("the reference's own path, compiled from its sources (oracle/Makefile refall), on one core"
+            if desc["kind"] == "reference" else
+            "the reference's source tree is not on this host, so its path cannot be compiled here; the oracle port "
+            "(C, the reference's operation order and FP64 arithmetic, pinned bitwise to the compiled reference's "
+            "outputs by tests/test_reference_pin.py and tests/golden/ref_path.npz) is timed instead, on every host "
+            "thread, on a bounded sample of the same workload family; no product library is loaded")
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
            "config": dict(workload_desc(args.n, args.precision, args.adapt_ratio),
-                          form="plain " + args.precision.upper()),
-           "cpu_baseline": {"value": value, "unit": UNIT, "cores": desc["cores"], "kind": "port",
+                          form="plain " + args.precision.upper(),
+                          sample="bounded CPU sample of the workload family (see cpu_baseline.sample)"),
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": desc["cores"], "kind": desc["kind"],
                             "sample": desc["sample"]},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-           "note": "reference path (apf/spr/ma) needs cmake-generated headers and is not compiled here; "
-                   "the oracle/ restatement of it (FP64, the reference's operation order) is timed instead, "
-                   "on the same workload family at a bounded sample size"}
+           "note": note}
     print(json.dumps(out), flush=True)
 
 
@@ -467,8 +532,8 @@ def gpu_arm(args):
     cpu = None
     if not args.no_cpu_baseline:
         try:
-            v, desc = cpu_port_run(args.cpu_seconds, os.cpu_count() or 1, ratio=args.adapt_ratio)
-            cpu = {"value": v, "unit": UNIT, "cores": desc["cores"], "kind": "port", "sample": desc["sample"]}
+            v, desc = cpu_baseline_run(args.cpu_seconds, args.adapt_ratio)
+            cpu = {"value": v, "unit": UNIT, "cores": desc["cores"], "kind": desc["kind"], "sample": desc["sample"]}
         except Exception as e:  # the baseline is reported, never the target
             cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": f"unavailable: {e}"}
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

@@ -77,13 +77,28 @@ def build(verbose=False, force=False):
     return OUT
 
 
+def reference_tree():
+    """The SCOREC/core source tree to build the pinning checker from:
+    $SPRG_REFERENCE_TREE, else the tree's mount point in the development
+    container; None where neither exists (the GPU host)."""
+    for cand in (os.environ.get("SPRG_REFERENCE_TREE"), "/root/reference"):
+        if cand and os.path.isdir(os.path.join(cand, "mth")):
+            return cand
+    return None
+
+
 def build_oracle():
     """Builds the CPU oracle (test infrastructure) and, when the reference
-    tree is present on this machine, the reference's own QR for pinning."""
-    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
-    ref = os.environ.get("SPRG_REFERENCE_TREE", "/root/reference")
-    if os.path.isdir(os.path.join(ref, "mth")):
-        subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", "REF=" + ref], check=True)
+    tree is present on this machine, the checker's copies of the reference:
+    its QR alone (oracle/_ref/libmthqr_ref.so) and its whole
+    estimate-and-mark path (oracle/_ref/libspr_ref.so), compiled from the
+    tree's sources by oracle/Makefile."""
+    oracle_dir = os.path.join(ROOT, "oracle")
+    subprocess.run(["make", "-s", "-C", oracle_dir], check=True)
+    ref = reference_tree()
+    if ref:
+        jobs = "-j%d" % max(1, os.cpu_count() or 1)
+        subprocess.run(["make", "-s", jobs, "-C", oracle_dir, "ref", "refall", "REF=" + ref], check=True)
 
 
 if __name__ == "__main__":
