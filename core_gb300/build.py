@@ -98,7 +98,7 @@ def build_oracle():
     ref = reference_tree()
     if ref:
         jobs = "-j%d" % max(1, os.cpu_count() or 1)
-        subprocess.run(["make", "-s", jobs, "-C", oracle_dir, "ref", "refall", "REF=" + ref], check=True)
+        subprocess.run(["make", "-s", jobs, "-C", oracle_dir, "ref", "refall", "shim", "REF=" + ref], check=True)
 
 
 if __name__ == "__main__":
