@@ -57,7 +57,7 @@ EXPORTS = [
     "sprg_measure_vertex_pairs", "sprg_get_maximum_edge_length", "sprg_get_average_edge_length",
     "sprg_max_iterations_for_length", "sprg_mark_bad_quality", "sprg_get_min_quality",
     "sprg_measure_edges_log_aniso", "sprg_measure_quality_log_aniso", "sprg_update_mesh",
-    "sprg_smb_counts", "sprg_smb_read", "sprg_smb_write",
+    "sprg_smb_counts", "sprg_smb_read", "sprg_smb_write", "sprg_e2e_timing", "sprg_e2e_timing_report",
 ]
 NOALLOC_MAX_ELEMS = 1 << 20
 
@@ -197,6 +197,9 @@ def load():
     lib.sprg_smb_read.argtypes = [ctypes.c_char_p, P, P, P]
     lib.sprg_smb_write.argtypes = [ctypes.c_char_p, ctypes.POINTER(MeshView)]
     lib.sprg_measure_quality_log_aniso.argtypes = [P, P, P, P]
+    lib.sprg_e2e_timing.argtypes = [P, I]
+    lib.sprg_e2e_timing_report.argtypes = [P]
+    lib.sprg_e2e_timing_report.restype = ctypes.c_char_p
     _lib = lib
     return lib
 

@@ -7,6 +7,7 @@ in MDS index order.  Errors raise :class:`SprgError` where the reference
 would abort.
 """
 import ctypes
+import json
 
 import numpy as np
 
@@ -99,6 +100,14 @@ class Context:
         out = np.empty(count, dtype)
         self._check(self._lib.sprg_debug_read(self.h, name.encode(), out.ctypes.data, out.nbytes))
         return out
+
+    def e2e_timing(self, on=True):
+        """Stage timing of estimate_and_mark calls (clears the sums)."""
+        self._check(self._lib.sprg_e2e_timing(self.h, 1 if on else 0))
+
+    def e2e_timing_report(self):
+        """Per-call averages (ms) of the stages of the timed calls."""
+        return json.loads(self._lib.sprg_e2e_timing_report(self.h).decode())
 
     @property
     def last_launch_count(self):

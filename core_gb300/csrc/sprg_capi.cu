@@ -3,6 +3,7 @@
 // reference call.  See include/spr_gb300.h for the contract of every entry.
 #include <cuda_runtime.h>
 
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -33,6 +34,16 @@ struct PatchCache {
   bool w_ready = false;
   DevBuf woff, w, wn;
 };
+
+// events of one timed host call: 0 call start, 1 field uploaded, 2 pass done,
+// 3 flags upload joined, 4 marks applied, 5 flags downloaded, 6 call end (main
+// stream); 7 / 8 flags upload, 9 / 10 size conversion + download (copy stream)
+constexpr int kE2EEvents = 11;
+constexpr int kE2EStages = 8;
+const char* const kE2EStageNames[kE2EStages] = {"upload_field", "pass", "wait_flags_upload", "mark_sweep",
+                                                "download_flags", "tail", "upload_flags_overlapped",
+                                                "size_download_overlapped"};
+const int kE2EStagePairs[kE2EStages][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 4}, {4, 5}, {5, 6}, {7, 8}, {9, 10}};
 
 struct sprg_ctx {
   int device = 0;
@@ -105,6 +116,15 @@ struct sprg_ctx {
   cudaEvent_t copy_fork = nullptr, copy_join = nullptr;
   cudaEvent_t size_ready = nullptr, size_join = nullptr;
   bool size_hook = false;  // the FP32 pass records size_ready after the vertex average
+  // stage timing of the host entry point (sprg_e2e_timing): events at the
+  // stage boundaries of each call, summed per stage, plus the host's enqueue
+  // and wait times
+  bool e2e_timing = false;
+  cudaEvent_t e2e_ev[kE2EEvents] = {};
+  double e2e_sum[kE2EStages] = {};
+  double e2e_host[3] = {};  // enqueue, wait, whole call (ms)
+  int e2e_n = 0;
+  std::string e2e_json;
   DevBuf mcount;           // split / collapse counts of the host entry point
   // pinned staging of the small results read back after a pass (status,
   // integrals, counters): enqueued on the stream, read after one synchronize
@@ -846,6 +866,8 @@ int sprg_destroy(sprg_ctx* c) {
     if (c->size_ready) cudaEventDestroy(c->size_ready);
     if (c->size_join) cudaEventDestroy(c->size_join);
   }
+  for (auto& e : c->e2e_ev)
+    if (e) cudaEventDestroy(e);
   if (c->stage) cudaFreeHost(c->stage);
   if (c->side) {
     cudaStreamSynchronize(c->side);
@@ -1744,9 +1766,15 @@ int sprg_estimate_and_mark(sprg_ctx* c, const double* u, double adapt_ratio, dou
     CK(cudaEventCreateWithFlags(&c->size_ready, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&c->size_join, cudaEventDisableTiming));
   }
+  const auto t_call = std::chrono::steady_clock::now();
+  if (c->e2e_timing && !c->e2e_ev[0])
+    for (auto& e : c->e2e_ev) CK(cudaEventCreate(&e));
+  auto mark = [&](int i, cudaStream_t s) { return c->e2e_timing ? cudaEventRecord(c->e2e_ev[i], s) : cudaSuccess; };
+  CK(mark(0, c->stream));
   PB("upload_field");
   CK(cudaMemcpyAsync(c->f.p, u, sizeof(double) * (size_t)m.V, cudaMemcpyHostToDevice, c->stream));
   PE();
+  CK(mark(1, c->stream));
   // the flag words are needed only by the write-back at the end: their
   // upload runs on the copy stream beside the pass, after the field's upload
   // (which then has the link to itself) and this stream's earlier work
@@ -1754,9 +1782,13 @@ int sprg_estimate_and_mark(sprg_ctx* c, const double* u, double adapt_ratio, dou
   if (flags) {
     CK(cudaEventRecord(c->copy_fork, c->stream));
     CK(cudaStreamWaitEvent(c->copy, c->copy_fork, 0));
+    CK(mark(7, c->copy));
     CK(cudaMemcpyAsync(c->flags.p, flags, sizeof(int) * (size_t)m.E, cudaMemcpyHostToDevice, c->copy));
+    CK(mark(8, c->copy));
     CK(cudaEventRecord(c->copy_join, c->copy));
   } else {
+    CK(mark(7, c->stream));
+    CK(mark(8, c->stream));
     CK(cudaMemsetAsync(c->flags.p, 0, sizeof(int) * (size_t)m.E, c->stream));
   }
   size_t nw = ((size_t)m.E + 31) / 32;
@@ -1779,15 +1811,19 @@ int sprg_estimate_and_mark(sprg_ctx* c, const double* u, double adapt_ratio, dou
   rc = e2e_pass(c, adapt_ratio, sb, sb + nw);
   c->size_hook = false;
   if (rc) return rc;
+  CK(mark(2, c->stream));
   if (early_size) {
     CK(cudaStreamWaitEvent(c->copy, c->size_ready, 0));
+    CK(mark(9, c->copy));
     fast_size_to_f64(m.V, P<float2>(c->sz2), P<double>(c->size), c->copy);
     c->launches += 1;
     CK(cudaMemcpyAsync(size_out, c->size.p, sizeof(double) * (size_t)m.V, cudaMemcpyDeviceToHost, c->copy));
+    CK(mark(10, c->copy));
     CK(cudaEventRecord(c->size_join, c->copy));
     c->size_valid = true;
   }
   if (flags) CK(cudaStreamWaitEvent(c->stream, c->copy_join, 0));
+  CK(mark(3, c->stream));
   PB("apply_marks");
   CK(cudaMemsetAsync(c->mcount.p, 0, 2 * sizeof(unsigned long long), c->stream));
   launch_apply_marks(m.E, sb, sb + nw, P<int>(c->flags), P<unsigned long long>(c->mcount), P<DevStatus>(c->status),
@@ -1795,12 +1831,15 @@ int sprg_estimate_and_mark(sprg_ctx* c, const double* u, double adapt_ratio, dou
   PE();
   c->launches += 1;
   if ((rc = check_launch(c, "apply marks"))) return rc;
+  CK(mark(4, c->stream));
   if (flags) {
     PB("download_flags");
     CK(cudaMemcpyAsync(flags, c->flags.p, sizeof(int) * (size_t)m.E, cudaMemcpyDeviceToHost, c->stream));
     PE();
   }
+  CK(mark(5, c->stream));
   if (!early_size) {
+    CK(mark(9, c->stream));
     if (c->precision == SPRG_FP32) {
       ENSURE(c->size, sizeof(double) * (size_t)m.V);
       fast_size_to_f64(m.V, P<float2>(c->sz2), P<double>(c->size), c->stream);
@@ -1814,6 +1853,7 @@ int sprg_estimate_and_mark(sprg_ctx* c, const double* u, double adapt_ratio, dou
     }
     if (size_out)
       CK(cudaMemcpyAsync(size_out, c->size.p, sizeof(double) * (size_t)m.V, cudaMemcpyDeviceToHost, c->stream));
+    CK(mark(10, c->stream));
   } else {
     CK(cudaStreamWaitEvent(c->stream, c->size_join, 0));
   }
@@ -1821,7 +1861,21 @@ int sprg_estimate_and_mark(sprg_ctx* c, const double* u, double adapt_ratio, dou
   CK(cudaMemcpyAsync(c->stage->counts, c->mcount.p, sizeof c->stage->counts, cudaMemcpyDeviceToHost, c->stream));
   if ((rc = enqueue_info(c))) return rc;
   PE();
+  CK(mark(6, c->stream));
+  const auto t_enq = std::chrono::steady_clock::now();
   if ((rc = sync_and_status(c))) return rc;
+  if (c->e2e_timing) {
+    const auto t_end = std::chrono::steady_clock::now();
+    for (int k = 0; k < kE2EStages; ++k) {
+      float ms = 0.f;
+      CK(cudaEventElapsedTime(&ms, c->e2e_ev[kE2EStagePairs[k][0]], c->e2e_ev[kE2EStagePairs[k][1]]));
+      c->e2e_sum[k] += ms;
+    }
+    c->e2e_host[0] += std::chrono::duration<double, std::milli>(t_enq - t_call).count();
+    c->e2e_host[1] += std::chrono::duration<double, std::milli>(t_end - t_enq).count();
+    c->e2e_host[2] += std::chrono::duration<double, std::milli>(t_end - t_call).count();
+    c->e2e_n += 1;
+  }
   if (n_split) *n_split = (long)c->stage->counts[0];
   if (n_collapse) *n_collapse = (long)c->stage->counts[1];
   return info_from_stage(c, info);
@@ -1897,6 +1951,31 @@ const char* sprg_profile_report(sprg_ctx* c, int reset) {
   c->prof_json = j;
   if (reset) c->prof_acc.clear();
   return c->prof_json.c_str();
+}
+
+int sprg_e2e_timing(sprg_ctx* c, int on) {
+  if (!c) return SPRG_EINVAL;
+  c->e2e_timing = on != 0;
+  for (double& x : c->e2e_sum) x = 0;
+  for (double& x : c->e2e_host) x = 0;
+  c->e2e_n = 0;
+  return SPRG_OK;
+}
+
+const char* sprg_e2e_timing_report(sprg_ctx* c) {
+  if (!c) return "{}";
+  const double n = c->e2e_n > 0 ? c->e2e_n : 1;
+  std::string j = "{\"calls\": " + std::to_string(c->e2e_n);
+  char buf[128];
+  for (int k = 0; k < kE2EStages; ++k) {
+    snprintf(buf, sizeof buf, ", \"%s_ms\": %.6f", kE2EStageNames[k], c->e2e_sum[k] / n);
+    j += buf;
+  }
+  snprintf(buf, sizeof buf, ", \"host_enqueue_ms\": %.6f, \"host_wait_ms\": %.6f, \"call_ms\": %.6f}",
+           c->e2e_host[0] / n, c->e2e_host[1] / n, c->e2e_host[2] / n);
+  j += buf;
+  c->e2e_json = j;
+  return c->e2e_json.c_str();
 }
 
 int sprg_apply_marks(int64_t n_edges, const uint32_t* split_bits, const uint32_t* collapse_bits, int32_t* flags,

@@ -318,6 +318,18 @@ int sprg_debug_read(sprg_ctx* ctx, const char* name, void* host, size_t bytes);
 /* Number of kernel launches issued by the last call (instrumentation). */
 int64_t sprg_last_launch_count(const sprg_ctx* ctx);
 
+/* Stage timing of sprg_estimate_and_mark (instrumentation): when on, each
+   call records CUDA events at its stage boundaries and host clocks around
+   its enqueue and its final wait; on = 1 or 0 also clears the sums.  The
+   report is a JSON object of per-call averages since then: calls,
+   upload_field_ms, pass_ms, wait_flags_upload_ms, mark_sweep_ms,
+   download_flags_ms, tail_ms (size conversion / download when not
+   overlapped, counts), upload_flags_overlapped_ms and
+   size_download_overlapped_ms (copy stream, beside the pass),
+   host_enqueue_ms, host_wait_ms, call_ms. */
+int sprg_e2e_timing(sprg_ctx* ctx, int on);
+const char* sprg_e2e_timing_report(sprg_ctx* ctx);
+
 /* ---- size field without device allocation ------------------------------- */
 
 /* No counterpart in the reference.  The size-field stage of

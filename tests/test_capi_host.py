@@ -104,7 +104,7 @@ CTX_CALLS = [
     "sprg_graph_capture", "sprg_graph_replay", "sprg_set_tiling", "sprg_measure_vertex_pairs",
     "sprg_get_maximum_edge_length", "sprg_get_average_edge_length", "sprg_mark_bad_quality",
     "sprg_get_min_quality", "sprg_measure_edges_log_aniso", "sprg_measure_quality_log_aniso",
-    "sprg_update_mesh",
+    "sprg_update_mesh", "sprg_e2e_timing",
 ]
 
 
@@ -133,6 +133,7 @@ def test_null_context_queries(lib):
     assert lib.sprg_last_launch_count(None) == 0
     assert lib.sprg_profile_report(None, 0) == b"{}"
     assert lib.sprg_tuning_report(None) == b""
+    assert lib.sprg_e2e_timing_report(None) == b"{}"
     assert lib.sprg_mlp_scratch_bytes(0) == 0
     assert lib.sprg_mlp_scratch_bytes(1000) > 0
 
@@ -144,7 +145,7 @@ def test_ctx_calls_cover_the_header():
             "sprg_box_counts", "sprg_box_fill", "sprg_profile_report", "sprg_spr_size_from_recovered_noalloc",
             "sprg_mlp_scratch_bytes", "sprg_mlp_forward", "sprg_mlp_grad", "sprg_mlp_adam",
             "sprg_tuning_report", "sprg_max_iterations_for_length", "sprg_smb_counts", "sprg_smb_read",
-            "sprg_smb_write"}
+            "sprg_smb_write", "sprg_e2e_timing_report"}
     assert set(CTX_CALLS) | free == set(_lib.EXPORTS)
     assert not set(CTX_CALLS) & free
 
