@@ -15,8 +15,16 @@
 // Set-up: the first call on a device (with that device current) resolves the
 // array's device address with cudaGetSymbolAddress; later calls reuse it.
 // The first call on a device should therefore come before any stream capture.
+// CUDA loads a library's device code lazily by default, so that first call
+// is also the moment the module is loaded and the array's memory committed
+// on the device: a caller that reserves the device heap for its own pool
+// should make the first call before reserving it (or load modules eagerly,
+// CUDA_MODULE_LOADING=EAGER).  Later calls commit no memory.
 // Every call shares the array and it keeps the last call's contents; calls
 // that overlap on the GPU (two streams, two host threads) race on it.
+// A CUDA error already pending from the caller's earlier work is left in
+// place and reported as SPRG_ECUDA before anything is launched, so this
+// call never claims another call's failure as its own.
 #include <mutex>
 
 #include "spr_gb300.h"
@@ -65,6 +73,7 @@ extern "C" int sprg_spr_size_from_recovered_noalloc(int dim, int64_t n_verts, in
   if (!d_coords || !d_elem_verts || !d_vert_elem_offsets || !d_vert_elems || !d_ip || !d_rec || !d_size)
     return SPRG_EINVAL;
   if (!(adapt_ratio > 0)) return SPRG_EINVAL;
+  if (cudaPeekAtLastError() != cudaSuccess) return SPRG_ECUDA;  // the caller's pending error, untouched
   double* base = nullptr;
   int rc = scratch_on_current_device(&base);
   if (rc) return rc;

@@ -346,9 +346,15 @@ const char* sprg_e2e_timing_report(sprg_ctx* ctx);
    SPRG_NOALLOC_MAX_ELEMS elements (about 17 MB, held by every GPU that loads
    the library until exit); larger meshes are rejected with SPRG_EINVAL.  The
    first call on a device resolves that array's address (do it before any
-   stream capture).  Calls share the array: calls that overlap on the GPU
-   race.  Enqueued on `stream` (cudaStream_t, NULL = legacy default); when
-   size_factor_out (host) is given, the call waits and stores the size factor. */
+   stream capture); as CUDA loads device code lazily by default, that first
+   call also loads the library's module and commits the array's memory, so a
+   caller that reserves the device heap should make it before reserving (or
+   set CUDA_MODULE_LOADING=EAGER).  Later calls commit nothing.  Calls share
+   the array: calls that overlap on the GPU race.  A CUDA error pending from
+   the caller's earlier work makes the call return SPRG_ECUDA before any
+   launch, leaving that error in place.  Enqueued on `stream` (cudaStream_t,
+   NULL = legacy default); when size_factor_out (host) is given, the call
+   waits and stores the size factor. */
 #define SPRG_NOALLOC_MAX_ELEMS (1 << 20)
 int sprg_spr_size_from_recovered_noalloc(int dim, int64_t n_verts, int64_t n_elems, const double* d_coords,
                                          const int32_t* d_elem_verts, const int32_t* d_vert_elem_offsets,
