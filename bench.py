@@ -43,7 +43,7 @@ def parse():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--precision", default="fp32", choices=["fp64", "fp32", "learned"],
                    help="form of the headline line: plain FP32 (exact marks), FP64, or learned")
-    p.add_argument("--workload", default="jbox", choices=["jbox", "batched", "aniso2d"],
+    p.add_argument("--workload", default="jbox", choices=["jbox", "batched", "aniso2d", "order"],
                    help="jbox: 160^3 jittered box (the headline); batched: 4096 uneven boxes; "
                         "aniso2d: 4096^2 anisotropic square")
     p.add_argument("--no-compare", action="store_true", help="skip the learned / FP64 comparison blocks")
@@ -727,6 +727,48 @@ def gpu_aniso2d(args):
     print(json.dumps(out), flush=True)
 
 
+def gpu_order(args):
+    """Locality renumbering: the plain FP32 pass on the jittered n^3 box in its
+    own (makeMdsBox) numbering, with every entity kind's numbering randomly
+    shuffled, and on the shuffled mesh after core_gb300.mesh.reorder
+    (sprg_locality_order); marks of the shuffled and renumbered passes mapped
+    back and compared with the ordered box's."""
+    import torch
+    import core_gb300 as cg
+    from core_gb300.mesh import reorder
+    n = args.n if args.n != 160 else 96
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    m, u = build_workload(n)
+    rng = np.random.Generator(np.random.PCG64(9))
+    ms, vs, ts, es = reorder(m, rng.permutation(m.n_verts).astype(np.int32),
+                             rng.permutation(m.n_elems).astype(np.int32), rng.permutation(m.n_edges).astype(np.int32))
+    us = np.empty_like(u)
+    us[vs] = u
+    t0 = time.perf_counter()
+    mr, vr, tr, er = reorder(ms)
+    t_order = time.perf_counter() - t0
+    ur = np.empty_like(us)
+    ur[vr] = us
+    ratio = args.adapt_ratio * n / 160.0
+    out, flags = {}, {}
+    for name, mm, uu in (("ordered", m, u), ("shuffled", ms, us), ("renumbered", mr, ur)):
+        out[name] = time_form(mm, uu, "fp32", ratio, args.steps, dev)
+        with cg.Context(mm, precision="fp32") as c:
+            flags[name] = c.estimate_and_mark(uu, ratio)[1]
+    same = bool(np.array_equal(flags["renumbered"][er][es], flags["ordered"]) and
+                np.array_equal(flags["shuffled"][es], flags["ordered"]))
+    V = m.n_verts
+    res = {"metric": METRIC, "value": out["renumbered"]["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": out["renumbered"]["ms_per_step"], "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": f"{n}^3 jittered box ({V} vertices, {m.n_elems} tets), numbering shuffled, then "
+                                  f"locality-renumbered (sprg_locality_order); plain FP32 pass, adapt ratio {ratio:g}",
+                      "l2": "inputs larger than L2"},
+           "forms": out, "marks_identical_after_mapping_back": same, "renumber_host_s": round(t_order, 3)}
+    print(json.dumps(res), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -735,6 +777,8 @@ def main():
         gpu_batched(args)
     elif args.workload == "aniso2d":
         gpu_aniso2d(args)
+    elif args.workload == "order":
+        gpu_order(args)
     else:
         gpu_arm(args)
 

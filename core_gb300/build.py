@@ -28,6 +28,7 @@ UNITS = {
     "sprg_learned.cu": [],
     "sprg_box.cpp": ["-x", "cu"],
     "sprg_smb.cpp": [],
+    "sprg_order.cpp": [],
 }
 
 

@@ -111,3 +111,55 @@ def write_smb(mesh, path):
     lib = _lib.load()
     view = mesh.view()
     _lib.check(lib.sprg_smb_write(str(path).encode(), ctypes.byref(view)))
+
+
+def locality_order(mesh):
+    """New index of every vertex, element and edge under the locality
+    renumbering (sprg_locality_order: apf::reorderMdsMesh's breadth-first
+    order on the flattened arrays)."""
+    lib = _lib.load()
+    vn = np.empty(mesh.n_verts, np.int32)
+    tn = np.empty(mesh.n_elems, np.int32)
+    en = np.empty(mesh.n_edges, np.int32)
+    view = mesh.view()
+    _lib.check(lib.sprg_locality_order(ctypes.byref(view), vn.ctypes.data, tn.ctypes.data, en.ctypes.data))
+    return vn, tn, en
+
+
+def reorder(mesh, vert_new=None, elem_new=None, edge_new=None):
+    """The mesh renumbered (by default in locality order): rows moved to their
+    new indices, ids mapped, every element's and edge's vertex order kept.
+    The vertex-element adjacency keeps each vertex's element order (mapped),
+    so the size average sums as on the original mesh; without one, the
+    original mesh's ascending order is carried over.  Returns (mesh,
+    vert_new, elem_new, edge_new); a field f on the original vertices is
+    f_new[vert_new] = f, and a result r on the renumbered vertices maps back
+    as r[vert_new]."""
+    if vert_new is None:
+        vert_new, elem_new, edge_new = locality_order(mesh)
+    V, T = mesh.n_verts, mesh.n_elems
+    coords = np.empty_like(mesh.coords)
+    coords[vert_new] = mesh.coords
+    ev = np.empty_like(mesh.elem_verts)
+    ev[elem_new] = vert_new[mesh.elem_verts]
+    ed = np.empty_like(mesh.edge_verts)
+    ed[edge_new] = vert_new[mesh.edge_verts]
+    if mesh.v2e_off is not None:
+        off, adj = mesh.v2e_off, mesh.v2e
+    else:
+        verts = mesh.elem_verts.reshape(-1)
+        elems = np.repeat(np.arange(T, dtype=np.int32), mesh.elem_verts.shape[1])
+        o = np.lexsort((elems, verts))
+        adj = elems[o].astype(np.int32)
+        off = np.zeros(V + 1, np.int32)
+        np.cumsum(np.bincount(verts, minlength=V), out=off[1:])
+    cnt = np.diff(off)
+    old_of = np.empty(V, np.int64)
+    old_of[vert_new] = np.arange(V)
+    new_cnt = cnt[old_of]
+    new_off = np.zeros(V + 1, np.int32)
+    np.cumsum(new_cnt, out=new_off[1:])
+    rows = np.repeat(old_of, new_cnt)
+    pos = np.arange(new_off[-1]) - np.repeat(new_off[:-1], new_cnt)
+    new_adj = elem_new[adj[off[rows] + pos]].astype(np.int32)
+    return Mesh(mesh.dim, coords, ev, ed, v2e_off=new_off, v2e=new_adj), vert_new, elem_new, edge_new

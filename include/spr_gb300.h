@@ -231,6 +231,20 @@ int sprg_smb_read(const char* path, double* coords, int32_t* elem_verts, int32_t
    tags or matches.  The optional averaging CSR of the view is not stored. */
 int sprg_smb_write(const char* path, const sprg_mesh_view* mesh);
 
+/* ---- locality renumbering ------------------------------------------------------
+   apf::reorderMdsMesh (mds/apfMDS.cc:957, mds_reorder mds/mds_order.c:409) on
+   the flattened arrays: vertices numbered breadth-first from a seed (the
+   first vertex of the smallest degree: a flattened view has no model to
+   pick the reference's model-vertex seed from), neighbours in descending
+   edge id, unreached vertices starting new searches in index order; elements
+   and edges then numbered in the order the renumbered vertices first reach
+   them (elements through the view's getAdjacent CSR when given, else
+   ascending).  Outputs the new index of every old entity (vert_new: n_verts,
+   elem_new: n_elems, edge_new: n_edges); the caller builds the renumbered
+   view (ids mapped, rows moved; each element's and edge's own vertex order
+   kept) and maps results back.  Host-only; no context needed. */
+int sprg_locality_order(const sprg_mesh_view* mesh, int32_t* vert_new, int32_t* elem_new, int32_t* edge_new);
+
 /* ---- incremental update after host topology changes ------------------------
    The adapt loop modifies the mesh on the host (refine, coarsen, swap, snap)
    and re-marks it every iteration (ma/maRefine.cc:420-448,

@@ -145,7 +145,7 @@ def test_ctx_calls_cover_the_header():
             "sprg_box_counts", "sprg_box_fill", "sprg_profile_report", "sprg_spr_size_from_recovered_noalloc",
             "sprg_mlp_scratch_bytes", "sprg_mlp_forward", "sprg_mlp_grad", "sprg_mlp_adam",
             "sprg_tuning_report", "sprg_max_iterations_for_length", "sprg_smb_counts", "sprg_smb_read",
-            "sprg_smb_write", "sprg_e2e_timing_report"}
+            "sprg_smb_write", "sprg_e2e_timing_report", "sprg_locality_order"}
     assert set(CTX_CALLS) | free == set(_lib.EXPORTS)
     assert not set(CTX_CALLS) & free
 
