@@ -57,7 +57,7 @@ EXPORTS = [
     "sprg_measure_vertex_pairs", "sprg_get_maximum_edge_length", "sprg_get_average_edge_length",
     "sprg_max_iterations_for_length", "sprg_mark_bad_quality", "sprg_get_min_quality",
     "sprg_measure_edges_log_aniso", "sprg_measure_quality_log_aniso", "sprg_update_mesh",
-    "sprg_smb_counts", "sprg_smb_read", "sprg_smb_write", "sprg_e2e_timing", "sprg_e2e_timing_report",
+    "sprg_smb_counts", "sprg_smb_read", "sprg_smb_write", "sprg_e2e_timing", "sprg_e2e_timing_report", "sprg_test_hooks",
     "sprg_locality_order",
 ]
 NOALLOC_MAX_ELEMS = 1 << 20
@@ -199,6 +199,7 @@ def load():
     lib.sprg_smb_write.argtypes = [ctypes.c_char_p, ctypes.POINTER(MeshView)]
     lib.sprg_measure_quality_log_aniso.argtypes = [P, P, P, P]
     lib.sprg_e2e_timing.argtypes = [P, I]
+    lib.sprg_test_hooks.argtypes = [P, I, I]
     lib.sprg_locality_order.argtypes = [ctypes.POINTER(MeshView), P, P, P]
     lib.sprg_e2e_timing_report.argtypes = [P]
     lib.sprg_e2e_timing_report.restype = ctypes.c_char_p

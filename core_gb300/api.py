@@ -101,6 +101,11 @@ class Context:
         self._check(self._lib.sprg_debug_read(self.h, name.encode(), out.ctypes.data, out.nbytes))
         return out
 
+    def test_hooks(self, wait_polls=0, alloc_fail_after=-1):
+        """Failure-path hooks (sprg_test_hooks): a network-kernel wait limit
+        in polls, and a device allocation that fails after n more."""
+        self._check(self._lib.sprg_test_hooks(self.h, int(wait_polls), int(alloc_fail_after)))
+
     def e2e_timing(self, on=True):
         """Stage timing of estimate_and_mark calls (clears the sums)."""
         self._check(self._lib.sprg_e2e_timing(self.h, 1 if on else 0))

@@ -106,6 +106,8 @@ struct sprg_ctx {
   int max_degree = 0;
   int use_mlp = 1;
   float z_max = 8.f;
+  int stall_polls = 0;      // test hook: network-kernel wait on a barrier nothing completes (0: off)
+  int alloc_fail_in = -1;   // test hook: device allocations left before one fails (-1: off)
   // side stream for the FP64 fits of listed patches, forked from and joined
   // back into the pass's stream
   cudaStream_t side = nullptr;
@@ -179,6 +181,8 @@ int cuda_fail(sprg_ctx* c, cudaError_t e, const char* where) {
 int ensure(sprg_ctx* c, DevBuf& b, size_t bytes) {
   if (bytes == 0) bytes = 16;
   if (b.bytes >= bytes) return SPRG_OK;
+  if (c->alloc_fail_in == 0) return fail(c, SPRG_ENOMEM, "device allocation failed (injected)");
+  if (c->alloc_fail_in > 0) --c->alloc_fail_in;
   if (b.p) cudaFree(b.p);
   b.p = nullptr;
   b.bytes = 0;
@@ -1543,7 +1547,7 @@ static int pass_fast(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_
   fast_prep(m, P<double>(c->f), P<float4>(c->crec), vrec, c->stream);
   PE();
   PB("tet_f32");
-  fast_tet(m, vrec, (float)c->frame[3], P<uint4>(c->tetd), P<int>(c->tnext), c->stream);
+  fast_tet(m, vrec, P<double>(c->f), (float)c->frame[3], P<uint4>(c->tetd), P<int>(c->tnext), c->stream);
   PE();
   if (!c->bins_ready) {
     if ((rc = build_bins(c))) return rc;
@@ -1657,9 +1661,9 @@ static int pass_learned(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint
   learned_prep(m, P<double>(c->f), vr, c->stream);
   PE();
   PB("mlp_l");
+  CK(cudaMemsetAsync(c->mlp_err.p, 0, sizeof(int), c->stream));  // a wait that ran out is reported once
   learned_infer(m, lm, vr, P<double>(c->f), c->mlp_packed.p, rec, P<int>(c->fbitems), P<int>(c->fbcount), c->z_max,
-                c->use_mlp, c->max_degree,
-                P<int>(c->mlp_err), c->stream);
+                c->use_mlp, c->max_degree, c->stall_polls, P<int>(c->mlp_err), c->stream);
   PE();
   if ((rc = listed_join(c, xl, fork))) return rc;
   PB("fallback_l");
@@ -2017,6 +2021,14 @@ int sprg_set_mlp_params(sprg_ctx* c, const float* params, int n_params) {
   CK(cudaStreamSynchronize(c->stream));
   if ((rc = check_launch(c, "pack network parameters"))) return rc;
   c->have_mlp = true;
+  drop_e2e_graph(c);
+  return SPRG_OK;
+}
+
+int sprg_test_hooks(sprg_ctx* c, int wait_polls, int alloc_fail_after) {
+  if (!c || wait_polls < 0 || alloc_fail_after < -1) return SPRG_EINVAL;
+  c->stall_polls = wait_polls;
+  c->alloc_fail_in = alloc_fail_after;
   drop_e2e_graph(c);
   return SPRG_OK;
 }

@@ -15,9 +15,11 @@ void fast_geometry(const DevMesh& m, float2* geo, double2* geo64, float* half_le
 // the pass's vertex records: coordinate records with the field pair (u_hi, u_lo)
 void fast_prep(const DevMesh& m, const double* u, const float4* crec, float4* vrec, cudaStream_t s);
 // per tet: gradient value (3 floats) and packed correction (1 word)
-// gscale = the frame's s (gradients in the mesh's coordinates)
+// gscale = the frame's s (gradients in the mesh's coordinates); u: the FP64
+// field, read for the ill-conditioned tets solved in FP64
 // next_chunk: one device int (the kernel's work counter, cleared here)
-void fast_tet(const DevMesh& m, const float4* vrec, float gscale, uint4* td, int* next_chunk, cudaStream_t s);
+void fast_tet(const DevMesh& m, const float4* vrec, const double* u, float gscale, uint4* td, int* next_chunk,
+              cudaStream_t s);
 // once per mesh: SPR weights in patch-CSR order (FP32 for the pass, FP64 for
 // the guard), listed patches
 void fast_weights(const DevMesh& m, float* w, double* w64, ExpandList xl, int* n_refit, unsigned char* listed,

@@ -142,6 +142,8 @@ __device__ __forceinline__ float inv_fifth_root(float x) {
 // conversion instructions, which run at a quarter rate.
 constexpr uint32_t kNoCorr = (256u << 18) | (256u << 9) | 256u;
 __device__ __forceinline__ int fexp(float a) { return ((__float_as_int(a) >> 23) & 0xff) - 127; }
+// 2^k as a float, -126 <= k <= 127
+__device__ __forceinline__ float pow2f(int k) { return __int_as_float((127 + k) << 23); }
 
 __device__ __forceinline__ uint32_t pack_corr(float s0, float s1, float s2, float r0, float r1, float r2) {
   const float smax = fmaxf(fabsf(s0), fmaxf(fabsf(s1), fabsf(s2)));
@@ -305,8 +307,44 @@ __device__ __forceinline__ TetData load_tet(const float4* __restrict__ vr, int4 
 // the current one, so only the record gathers (mostly L2 hits) stay on the
 // dependent chain.
 constexpr int kTetChunk = 8;
-__global__ void __launch_bounds__(kBlock, 4) k_fast_tet(DevMesh m, const float4* __restrict__ vr, float gscale,
-                                                        uint4* __restrict__ td, int* __restrict__ next_chunk) {
+
+// The gradient of an ill-conditioned tet from the mesh's FP64 coordinates and
+// field: J g = du solved with FP64 cofactors (the FP64 path's arithmetic,
+// accurate to about cond(J) 2^-53), as FP32 value + packed remainder in the
+// mesh's units
+__device__ __noinline__ uint4 tet_grad_f64(const double* __restrict__ xyz, const double* __restrict__ u, int4 tv) {
+  const int id[4] = {tv.x, tv.y, tv.z, tv.w};
+  double e[3][3], du[3];
+  const double u0 = u[id[0]];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) e[i][k] = xyz[3 * (size_t)id[i + 1] + k] - xyz[3 * (size_t)id[0] + k];
+    du[i] = u[id[i + 1]] - u0;
+  }
+  double cf[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const double* a = e[(i + 1) % 3];
+    const double* b = e[(i + 2) % 3];
+    cf[i][0] = a[1] * b[2] - a[2] * b[1];
+    cf[i][1] = a[2] * b[0] - a[0] * b[2];
+    cf[i][2] = a[0] * b[1] - a[1] * b[0];
+  }
+  const double det = e[0][0] * cf[0][0] + e[0][1] * cf[0][1] + e[0][2] * cf[0][2];
+  float s[3], r[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    const double g = (cf[0][j] * du[0] + cf[1][j] * du[1] + cf[2][j] * du[2]) / det;
+    s[j] = (float)g;
+    r[j] = (float)(g - (double)s[j]);
+  }
+  return make_uint4(__float_as_uint(s[0]), __float_as_uint(s[1]), __float_as_uint(s[2]),
+                    pack_corr(s[0], s[1], s[2], r[0], r[1], r[2]));
+}
+
+__global__ void __launch_bounds__(kBlock, 4) k_fast_tet(DevMesh m, const float4* __restrict__ vr, const double* __restrict__ u,
+                                                        float gscale, uint4* __restrict__ td, int* __restrict__ next_chunk) {
   const int4* __restrict__ ev4 = reinterpret_cast<const int4*>(m.ev);
   __shared__ int chunk;
   for (;;) {
@@ -337,9 +375,19 @@ __global__ void __launch_bounds__(kBlock, 4) k_fast_tet(DevMesh m, const float4*
         cf = cofactors(er[0], er[1], er[2]);
       }
       float g[3], c[3], s[3], r[3];
-      apply_inv(cf, d.eh[0].w, d.eh[1].w, d.eh[2].w, g);
+      apply_inv(cf, d.eh[0].w + d.el[0].w, d.eh[1].w + d.el[1].w, d.eh[2].w + d.el[2].w, g);
       apply_inv(cf, comp_residual(d.eh[0], d.el[0], g[0], g[1], g[2]), comp_residual(d.eh[1], d.el[1], g[0], g[1], g[2]),
                 comp_residual(d.eh[2], d.el[2], g[0], g[1], g[2]), c);
+      // (the first estimate takes du rounded to FP32, so) |c| is about
+      // cond(J) 2^-23 |g|, and what the correction leaves about
+      // |c|^2 / |g|; past |c| = 2^-17 |g| (cond(J) around 64 and up: a few
+      // elements per million of a jittered box) that and the records' own
+      // 2^-48 rounding, amplified by cond(J), pass the accuracy the error
+      // bound assumes, so the gradient is solved in FP64 instead
+      if (c[0] * c[0] + c[1] * c[1] + c[2] * c[2] > 0x1p-34f * (g[0] * g[0] + g[1] * g[1] + g[2] * g[2])) {
+        td[t] = tet_grad_f64(m.xyz, u, tv);
+        continue;
+      }
       // s + r = g + c exactly (|c| << |g|: Fast2Sum)
 #pragma unroll
       for (int j = 0; j < 3; ++j) {
@@ -635,13 +683,8 @@ __global__ void __launch_bounds__(kBlock) k_fast_error(DevMesh m, const uint4* _
       float dx = ((ga.s[0] - g0) + ga.r[0]) - D0, dy = ((ga.s[1] - g1) + ga.r[1]) - D1,
             dz = ((ga.s[2] - g2) + ga.r[2]) - D2;
       float wdv = gm.x;
-      float err = (dx * dx + dy * dy + dz * dz) * wdv;
       float ex = g0 + D0, ey = g1 + D1, ez = g2 + D2;
       self.add((ex * ex + ey * ey + ez * ez) * wdv);
-      // (sqrt err)^(6/5) = err^(3/5) = err r^2 and h_max (sqrt err)^(-2/5) =
-      // h_max r, with r = err^(-1/5)
-      float rr = inv_fifth_root(err);
-      gsum.add(err > 0.f ? err * (rr * rr) : 0.f);  // (sqrt 0)^(6/5) = 0; q = +inf as in FP64
       // error bound of q: the deviation (dx, dy, dz) is a difference of
       // quantities of size `scale`, each good to a few FP32 ulps, plus the
       // packed corrections; delta is 0.4 x that absolute deviation error
@@ -649,13 +692,39 @@ __global__ void __launch_bounds__(kBlock) k_fast_error(DevMesh m, const uint4* _
                     fmaxf(fmaxf(fabsf(D0), fabsf(D1)), fabsf(D2));
       // (plus a floor for field values below FP32's range, which read as 0)
       const float delta = kBoundUlps * scale + kQuantRel * ga.gmax + 1e-30f;
-      float dn = sqrtf(dx * dx + dy * dy + dz * dz);
-      // a zero deviation (q = +inf) keeps a lower bound of q instead: the FP64
-      // deviation is at most delta / 0.4, so q >= h_max (w dV (delta / 0.4)^2)^(-1/5)
-      // (stored negated)
-      float b = delta / dn;
-      if (!(dn > 0.f)) b = -(gm.y * inv_fifth_root(wdv * (2.5f * delta) * (2.5f * delta)));
-      q[t] = make_float2(gm.y * rr, b);
+      const float amax = fmaxf(fmaxf(fabsf(dx), fabsf(dy)), fabsf(dz));
+      float qv, b;
+      if (!(amax < 0x1p-40f)) {
+        float err = (dx * dx + dy * dy + dz * dz) * wdv;
+        // (sqrt err)^(6/5) = err^(3/5) = err r^2 and h_max (sqrt err)^(-2/5) =
+        // h_max r, with r = err^(-1/5)
+        float rr = inv_fifth_root(err);
+        gsum.add(err > 0.f ? err * (rr * rr) : 0.f);  // (sqrt 0)^(6/5) = 0; q = +inf as in FP64
+        qv = gm.y * rr;
+        b = delta / sqrtf(dx * dx + dy * dy + dz * dz);
+      } else if (amax > 0.f) {
+        // a deviation this small (the field almost linear over the patch,
+        // against the largest gradient) would underflow when squared: it is
+        // scaled by 2^(5j) into [2^-5, 2) first, and err^(-1/5) = rs 2^(2j),
+        // err^(3/5) = es rs^2 2^(-6j) with es, rs the scaled values
+        const int j = (-fexp(amax)) / 5;  // 8 <= j <= 25
+        const float up = pow2f(5 * j), dn3 = pow2f(-3 * j);
+        const float sx = dx * up, sy = dy * up, sz = dz * up;
+        const float es = (sx * sx + sy * sy + sz * sz) * wdv;
+        const float rs = inv_fifth_root(es);
+        gsum.add(es > 0.f ? ((es * (rs * rs)) * dn3) * dn3 : 0.f);
+        qv = (gm.y * rs) * pow2f(2 * j);
+        b = (delta * up) / sqrtf(sx * sx + sy * sy + sz * sz);
+      } else {
+        // a zero deviation (q = +inf) keeps a lower bound of q instead: the FP64
+        // deviation is at most delta / 0.4, so q >= h_max (w dV (delta / 0.4)^2)^(-1/5)
+        // (stored negated; delta scaled like a small deviation)
+        const int j = delta < 0x1p-40f ? (-fexp(delta)) / 5 : 0;
+        const float ds = (2.5f * delta) * pow2f(5 * j);
+        qv = gm.y * __int_as_float(0x7f800000);
+        b = -((gm.y * inv_fifth_root(wdv * ds * ds)) * pow2f(2 * j));
+      }
+      q[t] = make_float2(qv, b);
     }
   }
   double s1 = warp_pair_total(self), s2 = warp_pair_total(gsum);
@@ -881,10 +950,11 @@ void fast_prep(const DevMesh& m, const double* u, const float4* crec, float4* vr
   if (m.V) k_prep<<<nblk(m.V), kBlock, 0, s>>>(m.V, u, crec, vrec);
 }
 
-void fast_tet(const DevMesh& m, const float4* vrec, float gscale, uint4* td, int* next_chunk, cudaStream_t s) {
+void fast_tet(const DevMesh& m, const float4* vrec, const double* u, float gscale, uint4* td, int* next_chunk,
+              cudaStream_t s) {
   if (!m.T) return;
   cudaMemsetAsync(next_chunk, 0, sizeof(int), s);
-  k_fast_tet<<<tet_grid(m.T), kBlock, 0, s>>>(m, vrec, gscale, td, next_chunk);
+  k_fast_tet<<<tet_grid(m.T), kBlock, 0, s>>>(m, vrec, u, gscale, td, next_chunk);
 }
 
 void fast_weights(const DevMesh& m, float* w, double* w64, ExpandList xl, int* n_refit, unsigned char* listed,

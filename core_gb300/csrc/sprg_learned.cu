@@ -317,6 +317,15 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int ma
   }
   return false;
 }
+// the same, giving up early once *abort is set (by the other warp group)
+__device__ __forceinline__ bool mbar_wait_unless(uint64_t* bar, uint32_t parity, int max_iter,
+                                                 const volatile int* abort) {
+  for (int i = 0; i < max_iter; ++i) {
+    if (mbar_wait(bar, parity, 1)) return true;
+    if (*abort) return false;
+  }
+  return false;
+}
 // 32 lanes x 16 consecutive FP32 columns: thread i gets lane (base + i)
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
   uint32_t r[16];
@@ -369,7 +378,8 @@ struct InferSmem {
   static constexpr int kA2 = kA1 + 2 * kA1Bytes;
   static constexpr int kAux = kA2 + 2 * 128 * kMlpHidden;
   static constexpr int kAuxBytes = 128 * 5 * 4 + 16;  // g_c [128][3], scale [128], flag [128], K flag
-  static constexpr int kBar = kAux + 2 * kAuxBytes;   // mma, full[2], empty[2] (8 B each), tmem slot
+  // mma, full[2], empty[2], (unused), stall (8 B each); tmem slot at +40, abort flag at +56
+  static constexpr int kBar = kAux + 2 * kAuxBytes;
   static constexpr int kGelu = kBar + 64;
   static constexpr int kTotal = kGelu + 8 * kGeluN;
   static_assert(kA1 >= kMlpPackedBytes, "operand tiles after the parameters");
@@ -439,12 +449,16 @@ constexpr int kWaitLimit = 1 << 22;
 // consumers (warps 0-7) wait on full[b], issue the three layers (thread 0)
 // and run the epilogues, then arrive on empty[b], which the producers wait on
 // before refilling the buffer.  Every wait is bounded; a wait that runs out
-// sets *err and both groups leave their loops.
+// sets *err and both groups leave their loops (the consumers raise a shared
+// abort flag the producers' waits watch).  stall_polls > 0 (a test of that
+// path) replaces the first layer-1 completion wait by a wait of that many
+// polls on a barrier nothing completes: it runs out with the layer's MMAs in
+// flight, which are drained before the tensor memory is freed.
 template <int KMAX>
 __global__ void __launch_bounds__(kInferThreads, KMAX == 64 ? 2 : 1)
     k_mlp_infer(int V, LearnMesh lm, const float4* __restrict__ vr, const double* __restrict__ u,
                 const uint4* __restrict__ packed, float4* __restrict__ rec16, int* __restrict__ fb_items,
-                int* __restrict__ fb_count, float z_max, int use_mlp, int* __restrict__ err) {
+                int* __restrict__ fb_count, float z_max, int use_mlp, int stall_polls, int* __restrict__ err) {
   using S = InferSmem<KMAX>;
   extern __shared__ __align__(1024) unsigned char sm[];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -452,6 +466,7 @@ __global__ void __launch_bounds__(kInferThreads, KMAX == 64 ? 2 : 1)
   __nv_bfloat16* A2 = reinterpret_cast<__nv_bfloat16*>(sm + S::kA2);
   uint64_t* bars = reinterpret_cast<uint64_t*>(sm + S::kBar);  // [0] mma, [1..2] full, [3..4] empty
   uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + S::kBar + 40);
+  volatile int* abort = reinterpret_cast<volatile int*>(sm + S::kBar + 56);
   float2* gtab = reinterpret_cast<float2*>(sm + S::kGelu);
 
   for (int i = tid; i < kMlpPackedBytes / 16; i += blockDim.x) reinterpret_cast<uint4*>(sm)[i] = packed[i];
@@ -467,6 +482,8 @@ __global__ void __launch_bounds__(kInferThreads, KMAX == 64 ? 2 : 1)
       mbar_init(bars + 1 + b, kInferThreads - kConsumers);
       mbar_init(bars + 3 + b, kConsumers);
     }
+    mbar_init(bars + 6, 1);
+    *abort = 0;
   }
   tc_fence_before();
   __syncthreads();
@@ -482,7 +499,7 @@ __global__ void __launch_bounds__(kInferThreads, KMAX == 64 ? 2 : 1)
       const int tile = blockIdx.x + k * gridDim.x;
       if (tile >= ntiles) break;
       const int b = k & 1;
-      if (k >= 2 && !mbar_wait(bars + 3 + b, ((k - 2) >> 1) & 1, kWaitLimit)) {
+      if (k >= 2 && !mbar_wait_unless(bars + 3 + b, ((k - 2) >> 1) & 1, kWaitLimit, abort)) {
         ok = false;
         break;
       }
@@ -526,6 +543,7 @@ __global__ void __launch_bounds__(kInferThreads, KMAX == 64 ? 2 : 1)
                    sW3 = smem_u32(sm + kSmW3);
     constexpr uint32_t id64 = idesc_bf16(128, 64), id16 = idesc_bf16(128, 16);
     uint32_t mph = 0;
+    bool mma_pending = false;  // thread 0: MMAs committed whose completion was not yet seen
     for (int k = 0;; ++k) {
       const int tile = blockIdx.x + k * gridDim.x;
       if (tile >= ntiles) break;
@@ -545,10 +563,15 @@ __global__ void __launch_bounds__(kInferThreads, KMAX == 64 ? 2 : 1)
           mma_bf16(tbase, sdesc(sA1 + 256 * kk, 128, 16 * KMAX), sdesc(sW1 + 256 * kk, 128, 16 * kMlpIn), id64,
                    kk > 0);
         mma_commit(bars);
+        mma_pending = true;
       }
-      ok = bar_and(1, kConsumers, tid == 0 ? mbar_wait(bars, mph, kWaitLimit) : true);
-      mph ^= 1;
+      ok = bar_and(1, kConsumers,
+                   tid == 0 ? (stall_polls > 0 && k == 0 ? mbar_wait(bars + 6, 0, stall_polls)
+                                                         : mbar_wait(bars, mph, kWaitLimit))
+                            : true);
       if (!ok) break;
+      mma_pending = false;
+      mph ^= 1;
       tc_fence_after();
       hidden_epilogue(tbase, bias, gtab, A2, warp, lane);
       fence_async_smem();
@@ -561,10 +584,12 @@ __global__ void __launch_bounds__(kInferThreads, KMAX == 64 ? 2 : 1)
           mma_bf16(tbase, sdesc(sA2 + 256 * kk, 128, 16 * kMlpHidden), sdesc(sW2 + 256 * kk, 128, 16 * kMlpHidden),
                    id64, kk > 0);
         mma_commit(bars);
+        mma_pending = true;
       }
       ok = bar_and(1, kConsumers, tid == 0 ? mbar_wait(bars, mph, kWaitLimit) : true);
-      mph ^= 1;
       if (!ok) break;
+      mma_pending = false;
+      mph ^= 1;
       tc_fence_after();
       hidden_epilogue(tbase, bias + kMlpHidden, gtab, A2, warp, lane);
       fence_async_smem();
@@ -577,10 +602,12 @@ __global__ void __launch_bounds__(kInferThreads, KMAX == 64 ? 2 : 1)
           mma_bf16(tbase + 64, sdesc(sA2 + 256 * kk, 128, 16 * kMlpHidden),
                    sdesc(sW3 + 256 * kk, 128, 16 * kMlpHidden), id16, kk > 0);
         mma_commit(bars);
+        mma_pending = true;
       }
       ok = bar_and(1, kConsumers, tid == 0 ? mbar_wait(bars, mph, kWaitLimit) : true);
-      mph ^= 1;
       if (!ok) break;
+      mma_pending = false;
+      mph ^= 1;
       tc_fence_after();
       if (warp < 4) {
         float z[16];
@@ -604,7 +631,12 @@ __global__ void __launch_bounds__(kInferThreads, KMAX == 64 ? 2 : 1)
       tc_fence_before();
       mbar_arrive(bars + 3 + b);
     }
-    if (!ok) mbar_wait(bars, mph, kWaitLimit);  // MMAs in flight finish before the memory is freed
+    // MMAs in flight finish before the memory is freed (a full-length bounded
+    // wait, whatever limit the pass's waits had)
+    if (!ok && tid == 0) {
+      *abort = 1;
+      if (mma_pending) mbar_wait(bars, mph, kWaitLimit);
+    }
   }
   if (!ok) atomicExch(err, 1);
   __syncthreads();
@@ -1149,18 +1181,18 @@ void learned_pack(const float* params, void* packed, cudaStream_t s) {
 }
 
 void learned_infer(const DevMesh& m, const LearnMesh& lm, const float4* vr16, const double* u, const void* packed,
-                   float4* rec16, int* fb_items, int* fb_count, float z_max, int use_mlp, int max_degree, int* err,
-                   cudaStream_t s) {
+                   float4* rec16, int* fb_items, int* fb_count, float z_max, int use_mlp, int max_degree,
+                   int stall_polls, int* err, cudaStream_t s) {
   if (!m.V) return;
   const int ntiles = (m.V + 127) / 128;
   if (max_degree <= kMlpSlots / 2) {
     const int grid = std::min(infer_grid<64>(), ntiles);
     k_mlp_infer<64><<<grid, kInferThreads, InferSmem<64>::kTotal, s>>>(
-        m.V, lm, vr16, u, static_cast<const uint4*>(packed), rec16, fb_items, fb_count, z_max, use_mlp, err);
+        m.V, lm, vr16, u, static_cast<const uint4*>(packed), rec16, fb_items, fb_count, z_max, use_mlp, stall_polls, err);
   } else {
     const int grid = std::min(infer_grid<128>(), ntiles);
     k_mlp_infer<128><<<grid, kInferThreads, InferSmem<128>::kTotal, s>>>(
-        m.V, lm, vr16, u, static_cast<const uint4*>(packed), rec16, fb_items, fb_count, z_max, use_mlp, err);
+        m.V, lm, vr16, u, static_cast<const uint4*>(packed), rec16, fb_items, fb_count, z_max, use_mlp, stall_polls, err);
   }
 }
 

@@ -50,9 +50,11 @@ void learned_pack(const float* params, void* packed, cudaStream_t s);
 // network answers, the rest appended to fb_items (fb_count); use_mlp = 0
 // gives the cheap gradient alone.  err: set when a wait timed out.
 // max_degree <= 16 selects the K = 64 kernel (two blocks per SM)
+// stall_polls > 0 (test hook): the first layer-1 completion wait of each
+// block waits that many polls on a barrier nothing completes and runs out
 void learned_infer(const DevMesh& m, const LearnMesh& lm, const float4* vr16, const double* u, const void* packed,
-                   float4* rec16, int* fb_items, int* fb_count, float z_max, int use_mlp, int max_degree, int* err,
-                   cudaStream_t s);
+                   float4* rec16, int* fb_items, int* fb_count, float z_max, int use_mlp, int max_degree,
+                   int stall_polls, int* err, cudaStream_t s);
 // plain SPR for the fallback vertices (FP32 weights, FP32 element gradients;
 // listed patches take rec64, their FP64 reference result)
 void learned_fallback(const DevMesh& m, const LearnMesh& lm, const float4* vr16, const double* u, const float* w,

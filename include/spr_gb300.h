@@ -4,9 +4,9 @@
  * The entry points replace, one for one, the PUMI (SCOREC/core) calls of the
  * estimate-and-mark path.  Each declaration names the reference interface it
  * stands in for (paths relative to the SCOREC/core tree).  A C++ shim on the
- * reference side flattens an apf::Mesh2 into a
- * sprg_mesh_view, calls these functions, and writes the results back into
- * the apf fields and the "ma_flags" tag, so callers keep the unchanged
+ * reference side (core_gb300/shim/sprGB300.{h,cc}) flattens an apf::Mesh2
+ * into a sprg_mesh_view, calls these functions, and writes the results back
+ * into the apf fields and the "ma_flags" tag, so callers keep the unchanged
  * spr::/ma:: signatures.
  *
  * Conventions
@@ -343,6 +343,15 @@ int64_t sprg_last_launch_count(const sprg_ctx* ctx);
    host_enqueue_ms, host_wait_ms, call_ms. */
 int sprg_e2e_timing(sprg_ctx* ctx, int on);
 const char* sprg_e2e_timing_report(sprg_ctx* ctx);
+
+/* Test hooks (failure paths, no reference counterpart): wait_polls > 0 makes
+   the learned form's network kernel wait, in place of its first layer's
+   completion, wait_polls polls on a barrier that nothing completes (0: off);
+   that bounded wait runs out and the pass returns SPRG_ECUDA ("a tensor-core
+   wait ran out of time") after the kernel has drained the matrix multiplies
+   in flight and freed its tensor memory; the context stays usable.  alloc_fail_after >= 0 makes the context's device
+   allocation after that many more succeed fail with SPRG_ENOMEM (-1: off). */
+int sprg_test_hooks(sprg_ctx* ctx, int wait_polls, int alloc_fail_after);
 
 /* ---- size field without device allocation ------------------------------- */
 

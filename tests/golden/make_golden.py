@@ -16,7 +16,7 @@ reads the reference).
   box8_oracle.npz oracle outputs of the 8^3 sine-field pass (regression
                   fixture of the oracle itself, not a reference output).
 
-Usage: python tests/golden/make_golden.py [/path/to/reference]
+Usage: python tests/golden/make_golden.py <SCOREC/core source tree>
 """
 import ctypes
 import json
@@ -152,4 +152,7 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    tree = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SPRG_REFERENCE_TREE")
+    if not tree:
+        sys.exit("usage: make_golden.py <SCOREC/core source tree>  (or set SPRG_REFERENCE_TREE)")
+    main(tree)

@@ -3,8 +3,9 @@
 Seeded meshes and fields restated with numpy only (no product code), so the
 reference, the oracle and the GPU path all see the same numbers:
 jittered boxes, the bump and boundary-layer fields, random anisotropic
-metrics, a box with shuffled numbering, and the case list that
-tests/golden/make_ref_golden.py runs through the reference.
+metrics, a box with shuffled numbering, the case list that
+tests/golden/make_ref_golden.py runs through the reference, and the mask of
+vertices whose FP64 size is well conditioned.
 """
 import numpy as np
 
@@ -107,3 +108,17 @@ def field(name, x, seed):
     if name == "layer":
         return layer(x)
     return bump(x, seed)
+
+
+def conditioned(n_verts, elem_verts, ip, rec, rel=1e-7):
+    """Vertices whose size is well conditioned in FP64: every adjacent
+    element's deviation |eps_t - eps*(IP)| is above `rel` of the largest
+    gradient.  Where a patch is linear to the rounding level, the element
+    error is rounding noise and err^(-1/5) turns a 1e-16 change of the
+    recovered field into an O(1) change of that element's size, in the
+    reference as in any other summation order."""
+    d = ip - rec[elem_verts].mean(axis=1)
+    good_el = np.linalg.norm(d, axis=1) > rel * np.abs(ip).max()
+    bad_v = np.zeros(n_verts, bool)
+    bad_v[elem_verts[~good_el].reshape(-1)] = True
+    return ~bad_v

@@ -1,8 +1,8 @@
 """The batched workload: many uneven boxes in one context (disjoint union),
 per-mesh size factors, FP32 with the FP64 guard band.
 
-Each mesh of the batch gets the marks of its own FP64 pass (identical) and
-its own size factor (within 1e-7 relative of the FP64 one), and the batch
+Each mesh of the batch gets the marks of its own FP64 pass and of the oracle
+(identical) and its own size factor (within 1e-7 relative), and the batch
 pass is bitwise repeatable.
 """
 import numpy as np
@@ -35,6 +35,36 @@ def test_batch_matches_per_mesh_passes(gpu_lib):
         fin = np.isfinite(sk) & np.isfinite(s64)
         rel = np.abs(sk[fin] - s64[fin]) / s64[fin]
         assert np.median(rel) <= 1e-6
+
+
+def test_batch_matches_the_oracle(gpu_lib, oracle_lib):
+    """Meshes of a jittered batch against the oracle directly (the oracle is
+    pinned to the reference): every mesh's marks identical to the oracle's,
+    its size factor within 1e-7, its sizes within the bounds the FP32 path
+    carries."""
+    import core_gb300 as cg
+    from core_gb300 import workload
+    m, u, voff, eoff, doff, ns = workload.batch_boxes(12, seed=11, lo=4, hi=16, jitter=0.2)
+    K = len(ns)
+    ratios = np.linspace(0.02, 0.2, K)
+    with cg.Context(m, precision="fp32") as c:
+        c.set_batch(voff, eoff, ratios)
+        size, flags, *_ = c.estimate_and_mark(u, 1.0)
+        per = c.batch_info()
+        bound = c.debug_read("sz2", np.float32, 2 * m.n_verts)[1::2].astype(np.float64)
+    for k in range(K):
+        n = int(ns[k])
+        o = oracle_lib.OracleMesh.box(n, n, n)
+        o.set_coords(m.coords[voff[k]:voff[k + 1]])
+        assert np.array_equal(o.elem_verts, m.elem_verts[eoff[k]:eoff[k + 1]] - voff[k])
+        rc, so, Lo, fo, nso, nco, io = o.estimate_and_mark(u[voff[k]:voff[k + 1]], ratios[k])
+        assert rc == 0
+        assert np.array_equal(flags[doff[k]:doff[k + 1]], fo), k
+        assert abs(per[k, 2] - io["size_factor"]) <= 1e-7 * io["size_factor"], k
+        sk, bk = size[voff[k]:voff[k + 1]], bound[voff[k]:voff[k + 1]]
+        fin = np.isfinite(sk) & np.isfinite(so)
+        rel = np.abs(sk[fin] - so[fin]) / so[fin]
+        assert np.all(rel <= bk[fin] + 1e-6), k
 
 
 def test_batch_rejects_bad_offsets(gpu_lib):

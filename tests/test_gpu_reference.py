@@ -18,6 +18,7 @@ import os
 import numpy as np
 import pytest
 
+import refcases
 from refcases import REF_CASES
 
 GOLD = os.path.join(os.path.dirname(__file__), "golden", "ref_path.npz")
@@ -42,18 +43,7 @@ def rel(a, b):
 
 
 def conditioned(m, g):
-    """Vertices whose size is well conditioned in FP64: every adjacent
-    element's deviation |eps_t - eps*(IP)| is above 1e-7 of the largest
-    gradient.  Where a patch is linear to the rounding level, the element
-    error is rounding noise and err^(-1/5) turns a 1e-16 change of the
-    recovered field into an O(1) change of that element's size, in the
-    reference as in any other summation order."""
-    ev = g["elem_verts"]
-    d = g["ip"] - g["rec"][ev].mean(axis=1)
-    good_el = np.linalg.norm(d, axis=1) > 1e-7 * np.abs(g["ip"]).max()
-    bad_v = np.zeros(m.n_verts, bool)
-    bad_v[ev[~good_el].reshape(-1)] = True
-    return ~bad_v
+    return refcases.conditioned(m.n_verts, g["elem_verts"], g["ip"], g["rec"])
 
 
 ISO = sorted(k for k, (kind, _) in REF_CASES.items() if kind != "aniso")
