@@ -26,15 +26,14 @@
  * contraction, results are bitwise those of the reference on the same
  * platform libm.
  *
- * Parity pinning: the QR/rank kernel (orc_qr_*) is pinned against the
- * reference's own known-answer test (test/qr.cc) and against mth/mthQR.cc
- * compiled from source (oracle/Makefile -> oracle/_ref).  The rest of the
- * path (apf/mds/spr/ma) needs cmake-generated headers (mds_config.h,
- * SCOREC_config.h) and cannot be compiled from its sources alone, and the
- * reference's tests hold no golden values for it, so those functions are
- * parity-unpinned beyond the QR sub-step: they are checked through analytic
- * identities (linear-field patch test, Kuhn-tet quality, box entity counts,
- * the reference's own printed config-1 outcome of all 4184 edges split).
+ * Parity pinning: the reference's estimate-and-mark path is compiled from
+ * its sources (oracle/Makefile refall -> oracle/_ref/libspr_ref.so) and this
+ * restatement equals it bitwise on box numbering, IP gradients, recovered
+ * and size fields, edge lengths, qualities and ma_flags words
+ * (tests/test_reference_pin.py, and tests/golden/ref_path.npz for hosts
+ * without the reference tree); the QR/rank kernel (orc_qr_*) is also pinned
+ * against the reference's known-answer test (test/qr.cc) and against
+ * mth/mthQR.cc compiled alone (oracle/Makefile ref).
  */
 #include <math.h>
 #include <stdint.h>
