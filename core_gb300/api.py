@@ -218,14 +218,16 @@ class Context:
         return q
 
     # -- incremental update after host topology changes -----------------
-    def update_mesh(self, new_mesh):
+    def update_mesh(self, new_mesh, delta=None):
         """Send the rows of `new_mesh` that differ from the context's mesh
         (moved vertices, new or rewired elements and edges, the counts) and
         rebuild the device structures; the context then holds `new_mesh`.
-        Returns the delta's row counts (vertices, elements, edges)."""
+        `delta`: those rows when the caller knows them (mesh_delta's form),
+        else mesh_delta computes them.  Returns the delta's row counts
+        (vertices, elements, edges)."""
         if new_mesh.dim != self.mesh.dim:
             raise ValueError("the dimension cannot change")
-        d = mesh_delta(self.mesh, new_mesh)
+        d = mesh_delta(self.mesh, new_mesh) if delta is None else delta
         keep = []  # arrays referenced by the ctypes struct stay alive for the call
 
         def ptr(a):

@@ -52,7 +52,7 @@ struct sprg_ctx {
   int precision = SPRG_FP64;
   DevMesh m{};
   // mesh
-  DevBuf xyz, xyz32, ev, edv, poff, pel, aoff, ael, tmp;
+  DevBuf xyz, xyzq, ev, edv, poff, pel, aoff, ael, tmp;
   // fields
   DevBuf f, ip, rec, err, esize, size, L, flags, q, sizes3, frames9;
   int ip_nc = 0;
@@ -102,6 +102,7 @@ struct sprg_ctx {
   cudaStream_t e2e_stream = nullptr;
   bool e2e_early = false, e2e_off = false;
   DevBuf vvoff, vv, vtile, vr16, rec16, ql, sizel, fbitems, fbcount, mlp_packed, mlp_err, mlp_tmp;
+  DevBuf lrange, ldone, lsc;  // learned records: field range scratch, its counter, difference scales
   bool vv_ready = false, have_mlp = false;
   int max_degree = 0;
   int use_mlp = 1;
@@ -605,7 +606,7 @@ int sprg_create(const sprg_mesh_view* mv, int device, sprg_ctx** out) {
   } while (0)
   size_t nel = (size_t)m.T * m.nn;
   ENSUREC(c->xyz, sizeof(double) * 3 * (size_t)m.V);
-  ENSUREC(c->xyz32, sizeof(float) * 4 * (size_t)m.V);
+  ENSUREC(c->xyzq, sizeof(int) * 4 * (size_t)m.V);
   ENSUREC(c->ev, sizeof(int) * nel);
   ENSUREC(c->edv, sizeof(int) * 2 * (size_t)m.E);
   ENSUREC(c->poff, sizeof(int) * ((size_t)m.V + 1));
@@ -630,7 +631,7 @@ int sprg_create(const sprg_mesh_view* mv, int device, sprg_ctx** out) {
     set_frame(c, lo, hi);
   }
   m.xyz = P<double>(c->xyz);
-  m.xyz32 = P<float>(c->xyz32);
+  m.xyzq = P<int>(c->xyzq);
   m.ev = P<int>(c->ev);
   m.edv = P<int>(c->edv);
   if (mv->vert_elem_offsets) {
@@ -653,7 +654,7 @@ int sprg_create(const sprg_mesh_view* mv, int device, sprg_ctx** out) {
   }
   m.p_off = P<int>(c->poff);
   m.p_el = P<int>(c->pel);
-  launch_xyz_to_f32(m, P<float>(c->xyz32), c->stream);
+  launch_xyz_to_fixed(m, c->frame, P<int>(c->xyzq), c->stream);
   CKC(cudaGetLastError());
   CKC(cudaStreamSynchronize(c->stream));
   // validate the adjacency: every offset array must end at T * nn
@@ -802,9 +803,8 @@ int sprg_update_mesh(sprg_ctx* c, const sprg_mesh_delta* d) {
   m.ev = P<int>(c->ev);
   m.edv = P<int>(c->edv);
   const size_t nel = (size_t)m.T * nn;
-  ENSURE(c->xyz32, sizeof(float) * 4 * (size_t)m.V);
-  m.xyz32 = P<float>(c->xyz32);
-  launch_xyz_to_f32(m, P<float>(c->xyz32), c->stream);
+  ENSURE(c->xyzq, sizeof(int) * 4 * (size_t)m.V);
+  m.xyzq = P<int>(c->xyzq);
   ENSURE(c->red, sizeof(double) * (size_t)(sum_partials_count() + 4));
   launch_bbox(m.V, m.xyz, P<unsigned long long>(c->red), c->stream);
   unsigned long long keys[6];
@@ -816,6 +816,7 @@ int sprg_update_mesh(sprg_ctx* c, const sprg_mesh_delta* d) {
     hi[k] = key_to_double(keys[3 + k]);
   }
   set_frame(c, lo, hi);
+  launch_xyz_to_fixed(m, c->frame, P<int>(c->xyzq), c->stream);
   ENSURE(c->poff, sizeof(int) * ((size_t)m.V + 1));
   ENSURE(c->pel, sizeof(int) * nel);
   ENSURE(c->tmp, sizeof(int) * (size_t)m.V);
@@ -849,14 +850,14 @@ int sprg_destroy(sprg_ctx* c) {
   if (!c) return SPRG_OK;
   cudaSetDevice(c->device);
   if (c->own) cudaStreamSynchronize(c->own);
-  DevBuf* bufs[] = {&c->xyz,   &c->xyz32,   &c->ev,   &c->edv,   &c->poff,    &c->pel,    &c->aoff,
+  DevBuf* bufs[] = {&c->xyz,   &c->xyzq,   &c->ev,   &c->edv,   &c->poff,    &c->pel,    &c->aoff,
                     &c->ael,   &c->tmp,     &c->f,    &c->ip,    &c->rec,     &c->err,    &c->esize,
                     &c->size,  &c->L,       &c->flags, &c->q,    &c->sizes3,  &c->frames9, &c->partials,
                     &c->out3,  &c->status,  &c->count, &c->mcount, &c->xitems, &c->xcount, &c->slab, &c->bits, &c->titems, &c->tcountb, &c->Lx, &c->pairs, &c->red, &c->eflags, &c->logm, &c->qw, &c->qwlisted, &c->qwitems, &c->qwcount, &c->tw, &c->twlisted, &c->twitems, &c->twcount, &c->met32, &c->qrec32, &c->cj64, &c->qties, &c->kidx, &c->kval, &c->klen, &c->rec9, &c->cache2d.v, &c->cache2d.n, &c->cache2d.el, &c->agitems, &c->agcount,
                     &c->crec,  &c->vrec,    &c->rec32, &c->q32, &c->sz2,  &c->fcnt,   &c->guard, &c->tetd,
                     &c->wts,   &c->w64,     &c->listed, &c->geo, &c->geo64, &c->elen, &c->fitems, &c->gstamp, &c->gfit, &c->grec, &c->tnext, &c->edone,
                     &c->hess, &c->pcls, &c->bverts, &c->btiles, &c->bnext, &c->bvoff, &c->bseg, &c->bsegoff, &c->bratios, &c->vvoff, &c->vv, &c->vtile, &c->vr16, &c->rec16,
-                    &c->ql,    &c->sizel,   &c->fbitems, &c->fbcount, &c->mlp_packed, &c->mlp_err, &c->mlp_tmp,
+                    &c->ql,    &c->sizel,   &c->fbitems, &c->fbcount, &c->mlp_packed, &c->mlp_err, &c->mlp_tmp, &c->lrange, &c->ldone, &c->lsc,
                     &c->cache64.v, &c->cache64.n, &c->cache64.el, &c->cache32.v, &c->cache32.n, &c->cache32.el,
                     &c->cache64.woff, &c->cache64.w, &c->cache64.wn, &c->cache32.woff, &c->cache32.w,
                     &c->cache32.wn};
@@ -1614,6 +1615,27 @@ static int pass_fast(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_
   return check_launch(c, "fast pass");
 }
 
+// the learned records' scratch: the field range's block partials, the
+// last-block counter (zeroed when allocated; every pass leaves it zero) and
+// the two difference scales
+static int learned_scratch(sprg_ctx* c) {
+  ENSURE(c->lrange, learned_range_bytes());
+  if (!c->ldone.p) {
+    ENSURE(c->ldone, sizeof(unsigned));
+    CK(cudaMemsetAsync(c->ldone.p, 0, sizeof(unsigned), c->stream));
+  }
+  ENSURE(c->lsc, 2 * sizeof(float));
+  return SPRG_OK;
+}
+
+// 2^-30 / s: the coordinate records' difference scale
+static float learned_cs(const sprg_ctx* c) { return (float)(std::ldexp(1.0, -30) / c->frame[3]); }
+
+static void learned_records(sprg_ctx* c, const double* d_u) {
+  learned_prep(c->m, d_u, learned_cs(c), P<double>(c->lrange), P<unsigned>(c->ldone), P<float>(c->lsc),
+               P<float4>(c->vr16), c->stream);
+}
+
 // Learned pass: network recovery with plain-SPR fallback, FP32 sweeps
 // (sprg_learned.cu).
 static int pass_learned(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_t* d_collapse) {
@@ -1635,6 +1657,7 @@ static int pass_learned(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint
   ENSURE(c->fbitems, sizeof(int) * (size_t)m.V);
   ENSURE(c->fbcount, sizeof(int));
   ENSURE(c->mlp_err, sizeof(int));
+  if ((rc = learned_scratch(c))) return rc;
   if ((rc = reset_status(c))) return rc;
   ExpandList xl{P<int>(c->fitems), P<int>(c->fcnt) + 3, m.V};
   if ((rc = fast_setup(c, xl))) return rc;
@@ -1658,20 +1681,20 @@ static int pass_learned(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint
   float4* rec = P<float4>(c->rec16);
   CK(cudaMemsetAsync(c->fbcount.p, 0, sizeof(int), c->stream));
   PB("prep_l");
-  learned_prep(m, P<double>(c->f), vr, c->stream);
+  learned_records(c, P<double>(c->f));
   PE();
   PB("mlp_l");
   CK(cudaMemsetAsync(c->mlp_err.p, 0, sizeof(int), c->stream));  // a wait that ran out is reported once
-  learned_infer(m, lm, vr, P<double>(c->f), c->mlp_packed.p, rec, P<int>(c->fbitems), P<int>(c->fbcount), c->z_max,
+  learned_infer(m, lm, vr, P<float>(c->lsc), c->mlp_packed.p, rec, P<int>(c->fbitems), P<int>(c->fbcount), c->z_max,
                 c->use_mlp, c->max_degree, c->stall_polls, P<int>(c->mlp_err), c->stream);
   PE();
   if ((rc = listed_join(c, xl, fork))) return rc;
   PB("fallback_l");
-  learned_fallback(m, lm, vr, P<double>(c->f), P<float>(c->wts), P<double>(c->rec), P<int>(c->fbitems),
+  learned_fallback(m, lm, vr, P<float>(c->lsc), P<float>(c->wts), P<double>(c->rec), P<int>(c->fbitems),
                    P<int>(c->fbcount), m.V, rec, c->stream);
   PE();
   PB("error_l");
-  learned_error(m, rec, P<float2>(c->geo), P<float>(c->ql), P<double>(c->partials), nb, c->stream);
+  learned_error(m, rec, P<float>(c->lsc), P<float2>(c->geo), P<float>(c->ql), P<double>(c->partials), nb, c->stream);
   PE();
   PB("size_factor");
   launch_size_factor(P<double>(c->partials), nb, 0, adapt_ratio, 0, m.dim, P<double>(c->out3), c->stream);
@@ -1682,7 +1705,7 @@ static int pass_learned(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint
   PB("measure_l");
   learned_measure(m, P<float>(c->elen), P<float>(c->sizel), d_split, d_collapse, c->stream);
   PE();
-  c->launches += 7;  // prep, network, fallback, error, size factor, average, measure
+  c->launches += 8;  // range, prep, network, fallback, error, size factor, average, measure
   c->size_valid = false;
   c->L_valid = false;
   return check_launch(c, "learned pass");
@@ -2050,6 +2073,7 @@ int sprg_learned_features(sprg_ctx* c, const double* d_u, uint16_t* d_x, float* 
   ENSURE(c->fitems, sizeof(int) * (size_t)m.V);
   ENSURE(c->fcnt, 8 * sizeof(int));
   ENSURE(c->vr16, 16 * (size_t)m.V);
+  if ((rc = learned_scratch(c))) return rc;
   ExpandList xl{P<int>(c->fitems), P<int>(c->fcnt) + 3, m.V};
   if ((rc = fast_setup(c, xl))) return rc;
   if (!c->vv_ready) {
@@ -2066,8 +2090,8 @@ int sprg_learned_features(sprg_ctx* c, const double* d_u, uint16_t* d_x, float* 
     c->vv_ready = true;
   }
   LearnMesh lm{P<int>(c->vvoff), P<int>(c->vv), P<unsigned char>(c->listed), P<unsigned char>(c->vtile)};
-  learned_prep(m, d_u, P<float4>(c->vr16), c->stream);
-  learned_features(m, lm, P<float4>(c->vr16), d_x, d_aux, c->stream);
+  learned_records(c, d_u);
+  learned_features(m, lm, P<float4>(c->vr16), P<float>(c->lsc), d_x, d_aux, c->stream);
   CK(cudaStreamSynchronize(c->stream));
   return check_launch(c, "learned features");
 }

@@ -16,7 +16,7 @@ struct DevMesh {
   int ne_el;           // edges per element (3 or 6)
   int V, T, E;
   const double* xyz;   // V x 3 (FP64 master copy)
-  const float* xyz32;  // V x 4 (x, y, z, 0) FP32 copy for the fast path
+  const int* xyzq;     // V x 4 (X, Y, Z, 0): 32-bit fixed point on the frame, the learned form's records
   const int* ev;       // T x nn  (getDownward(e,0) order)
   const int* edv;      // E x 2
   const int* p_off;    // V + 1, patch CSR: elements of each vertex, ascending
@@ -236,6 +236,7 @@ void launch_hessian_metric(const DevMesh& m, const double* H, double eps, double
 void launch_build_v2e(const DevMesh& m, int* off, int* el, int* tmp, cudaStream_t s);
 // Sort each CSR segment ascending (segments are short).
 void launch_sort_segments(int V, const int* off, int* el, cudaStream_t s);
-void launch_xyz_to_f32(const DevMesh& m, float* xyz32, cudaStream_t s);
+// X = rint((x - c) s 2^30) per coordinate (c the frame's corner, s its scale)
+void launch_xyz_to_fixed(const DevMesh& m, const double* frame, int* xyzq, cudaStream_t s);
 
 }  // namespace sprg

@@ -1483,12 +1483,13 @@ __global__ void k_sort_segments(int V, const int* off, int* el) {
     el[j + 1] = x;
   }
 }
-__global__ void k_xyz_f32(DevMesh m, float* xyz32) {
+__global__ void k_xyz_fixed(DevMesh m, double cx, double cy, double cz, double s, int* xyzq) {
   int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= m.V) return;
-  float4 p = make_float4((float)m.xyz[3 * (size_t)v], (float)m.xyz[3 * (size_t)v + 1],
-                         (float)m.xyz[3 * (size_t)v + 2], 0.f);
-  reinterpret_cast<float4*>(xyz32)[v] = p;
+  const double q = s * 0x1p30;  // (x - c) s in [0, 1]
+  reinterpret_cast<int4*>(xyzq)[v] =
+      make_int4(__double2int_rn((m.xyz[3 * (size_t)v] - cx) * q), __double2int_rn((m.xyz[3 * (size_t)v + 1] - cy) * q),
+                __double2int_rn((m.xyz[3 * (size_t)v + 2] - cz) * q), 0);
 }
 
 inline int nblk(long n, int b = kBlock) { return (int)((n + b - 1) / b); }
@@ -2635,8 +2636,8 @@ void launch_sort_segments(int V, const int* off, int* el, cudaStream_t s) {
   if (V) k_sort_segments<<<nblk(V), kBlock, 0, s>>>(V, off, el);
 }
 
-void launch_xyz_to_f32(const DevMesh& m, float* xyz32, cudaStream_t s) {
-  if (m.V) k_xyz_f32<<<nblk(m.V), kBlock, 0, s>>>(m, xyz32);
+void launch_xyz_to_fixed(const DevMesh& m, const double* frame, int* xyzq, cudaStream_t s) {
+  if (m.V) k_xyz_fixed<<<nblk(m.V), kBlock, 0, s>>>(m, frame[0], frame[1], frame[2], frame[3], xyzq);
 }
 
 

@@ -78,36 +78,99 @@ __global__ void k_v2v_sort(int V, const int* __restrict__ off, int* __restrict__
 }
 
 // ---------------------------------------------------------------------------
-// vertex records {x, y, z, u} in FP32; u truncated to 24 bits by integer
-// operations (an FP64 conversion would run on the FP64 pipe)
+// vertex records {X, Y, Z, U}: coordinates and field as 32-bit fixed point,
+// X = rint((x - c) s 2^30) on the mesh's frame (c the lower corner, s the power
+// of two that puts the extent in (1/2, 1]) and U = rint((u - u_min) s_u 2^30)
+// on the pass's field range.  The difference of two records is an exact
+// integer, so no rounding of a coordinate or a field value enters it; one
+// conversion rounds it to FP32 and a power of two (cs = 2^-30 / s,
+// cu = 2^-30 / s_u, the pair `lsc`) scales it back to the mesh's units.
+// (FP32 coordinates and a 24-bit field put the size error's p99 near 3e-2
+// at 160^3 through the element gradients and the neighbour fit; exact
+// differences take it to the FP32 arithmetic's level.)
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ float trunc_f32(double w) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(w);
-  const int e = (int)((b >> 52) & 0x7ff);
-  if (e >= 897 && e <= 1150)
-    return __uint_as_float(((unsigned)(b >> 63) << 31) | ((unsigned)(e - 896) << 23) |
-                           (unsigned)((b >> 29) & 0x7fffffu));
-  return (float)w;
+constexpr int kRangeGrid = 304;
+
+__device__ __forceinline__ float qdiff(float a, float b, float scale) {
+  return __int2float_rn(__float_as_int(a) - __float_as_int(b)) * scale;
 }
 
-// the remainder u - trunc_f32(u) rounded to FP32 (integer operations)
-__device__ __forceinline__ float trunc_lo(double w) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(w);
-  const int e = (int)((b >> 52) & 0x7ff);
-  if (e >= 949 && e <= 1150) {
-    const float lo = (float)(unsigned)(b & 0x1fffffffu) * __uint_as_float((unsigned)(e - 948) << 23);
-    return (b >> 63) ? -lo : lo;
+// the field's range by blocks (min, max, any non-finite value), reduced by
+// the last block to finish (min / max: any order gives the same result):
+// range[3 kRangeGrid ..] = {u_min, s_u}, lsc = {cs, cu}; a NaN or infinite
+// value makes cu NaN, so every difference of the pass is NaN (as FP64 gives
+// NaN sizes for such a field)
+__global__ void __launch_bounds__(kBlock) k_lrange(int V, const double* __restrict__ u, float cs,
+                                                   double* __restrict__ range, unsigned* __restrict__ done,
+                                                   float* __restrict__ lsc) {
+  double lo = INFINITY, hi = -INFINITY;
+  int bad = 0;
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+    const double x = __ldg(u + v);
+    if (isfinite(x)) {
+      lo = fmin(lo, x);
+      hi = fmax(hi, x);
+    } else {
+      bad = 1;
+    }
   }
-  return e < 949 ? (float)(w - (double)trunc_f32(w)) : 0.f;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+  }
+  __shared__ double sh[3][kBlock / 32];
+  __shared__ bool last;
+  const int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) {
+    sh[0][w] = lo;
+    sh[1][w] = hi;
+    sh[2][w] = bad;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int i = 1; i < kBlock / 32; ++i) {
+      lo = fmin(lo, sh[0][i]);
+      hi = fmax(hi, sh[1][i]);
+      bad |= sh[2][i] != 0.0;
+    }
+    range[3 * blockIdx.x] = lo;
+    range[3 * blockIdx.x + 1] = hi;
+    range[3 * blockIdx.x + 2] = bad;
+    __threadfence();
+    last = atomicAdd(done, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last || threadIdx.x != 0) return;
+  __threadfence();
+  for (int b = 0; b < (int)gridDim.x; ++b) {
+    lo = fmin(lo, range[3 * b]);
+    hi = fmax(hi, range[3 * b + 1]);
+    bad |= range[3 * b + 2] != 0.0;
+  }
+  double su = 1.0;
+  if (!bad && hi > lo) {
+    int e;
+    frexp(hi - lo, &e);  // hi - lo = m 2^e, m in [1/2, 1)
+    su = ldexp(1.0, -e);
+  }
+  range[3 * kRangeGrid] = bad ? 0.0 : lo;
+  range[3 * kRangeGrid + 1] = su;
+  lsc[0] = cs;
+  lsc[1] = bad ? __int_as_float(0x7fc00000) : (float)(ldexp(1.0, -30) / su);
+  *done = 0;
 }
 
-__global__ void __launch_bounds__(kBlock) k_lprep(int V, const double* __restrict__ u, const float4* __restrict__ xyz32,
-                                                  float4* __restrict__ vr) {
+__global__ void __launch_bounds__(kBlock) k_lprep(int V, const double* __restrict__ u, const int4* __restrict__ xyzq,
+                                                  const double* __restrict__ range, float4* __restrict__ vr) {
   const int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= V) return;
-  float4 p = __ldg(xyz32 + v);
-  p.w = trunc_f32(__ldg(u + v));
-  vr[v] = p;
+  const double umin = range[3 * kRangeGrid], su = range[3 * kRangeGrid + 1];
+  const int4 p = __ldg(xyzq + v);
+  const double t = (__ldg(u + v) - umin) * su * 0x1p30;  // in [0, 2^30] for a finite field
+  const int U = t >= 0.0 && t <= 0x1p30 ? __double2int_rn(t) : 0;
+  vr[v] = make_float4(__int_as_float(p.x), __int_as_float(p.y), __int_as_float(p.z), __int_as_float(U));
 }
 
 // ---------------------------------------------------------------------------
@@ -136,7 +199,7 @@ __device__ __forceinline__ float quad_sum(float x) {
 // take the fallback: their slot count n is 0)
 template <int NS>
 __device__ __forceinline__ VFeat<NS> vertex_features(const LearnMesh& lm, const float4* __restrict__ vr, int V, int v,
-                                                     int q) {
+                                                     int q, float cs, float cu) {
   VFeat<NS> o;
   const bool valid = v < V;
   int b = 0, cnt = 0;
@@ -158,10 +221,10 @@ __device__ __forceinline__ VFeat<NS> vertex_features(const LearnMesh& lm, const 
 #pragma unroll
   for (int i = 0; i < NS; ++i) {
     const float4 p = id[i] >= 0 ? __ldg(vr + id[i]) : xv;
-    dx[i] = p.x - xv.x;
-    dy[i] = p.y - xv.y;
-    dz[i] = p.z - xv.z;
-    du[i] = p.w - xv.w;
+    dx[i] = qdiff(p.x, xv.x, cs);
+    dy[i] = qdiff(p.y, xv.y, cs);
+    dz[i] = qdiff(p.z, xv.z, cs);
+    du[i] = qdiff(p.w, xv.w, cu);
   }
   float a00 = 0.f, a01 = 0.f, a02 = 0.f, a11 = 0.f, a12 = 0.f, a22 = 0.f, b0 = 0.f, b1 = 0.f, b2 = 0.f, r2 = 0.f;
   float mx = 0.f, my = 0.f, mz = 0.f;
@@ -231,10 +294,11 @@ __device__ __forceinline__ uint2 pack4_bf16(float4 a) {
 }
 
 __global__ void __launch_bounds__(kBlock) k_lfeatures(int V, LearnMesh lm, const float4* __restrict__ vr,
-                                                      uint2* __restrict__ x, float* __restrict__ aux) {
+                                                      const float* __restrict__ lsc, uint2* __restrict__ x,
+                                                      float* __restrict__ aux) {
   const int gid = blockIdx.x * blockDim.x + threadIdx.x;
   const int v = gid >> 2, q = gid & 3;
-  VFeat<8> f = vertex_features<8>(lm, vr, V, v, q);
+  VFeat<8> f = vertex_features<8>(lm, vr, V, v, q, __ldg(lsc), __ldg(lsc + 1));
   if (v >= V) return;
 #pragma unroll
   for (int i = 0; i < 8; ++i) x[(size_t)v * kMlpSlots + q + 4 * i] = pack4_bf16(f.f[i]);
@@ -456,7 +520,7 @@ constexpr int kWaitLimit = 1 << 22;
 // flight, which are drained before the tensor memory is freed.
 template <int KMAX>
 __global__ void __launch_bounds__(kInferThreads, KMAX == 64 ? 2 : 1)
-    k_mlp_infer(int V, LearnMesh lm, const float4* __restrict__ vr, const double* __restrict__ u,
+    k_mlp_infer(int V, LearnMesh lm, const float4* __restrict__ vr, const float* __restrict__ lsc,
                 const uint4* __restrict__ packed, float4* __restrict__ rec16, int* __restrict__ fb_items,
                 int* __restrict__ fb_count, float z_max, int use_mlp, int stall_polls, int* __restrict__ err) {
   using S = InferSmem<KMAX>;
@@ -495,6 +559,7 @@ __global__ void __launch_bounds__(kInferThreads, KMAX == 64 ? 2 : 1)
   if (warp >= 8) {
     // ---- producers: 256 threads, four lanes per vertex, two passes of 64
     const int ptid = tid - kConsumers;
+    const float cs = __ldg(lsc), cu = __ldg(lsc + 1);
     for (int k = 0;; ++k) {
       const int tile = blockIdx.x + k * gridDim.x;
       if (tile >= ntiles) break;
@@ -512,7 +577,7 @@ __global__ void __launch_bounds__(kInferThreads, KMAX == 64 ? 2 : 1)
       for (int pass = 0; pass < 2; ++pass) {
         const int r = 64 * pass + (ptid >> 2), q = ptid & 3;
         if (half) {
-          VFeat<4> f = vertex_features<4>(lm, vr, V, tile * 128 + r, q);
+          VFeat<4> f = vertex_features<4>(lm, vr, V, tile * 128 + r, q, cs, cu);
 #pragma unroll
           for (int i = 0; i < 4; ++i)
             *reinterpret_cast<uint2*>(A1 + tile_off(r, 4 * (q + 4 * i), KMAX)) = pack4_bf16(f.f[i]);
@@ -522,7 +587,7 @@ __global__ void __launch_bounds__(kInferThreads, KMAX == 64 ? 2 : 1)
             flags[r] = f.flag;
           }
         } else if (KMAX == 128) {
-          VFeat<8> f = vertex_features<8>(lm, vr, V, tile * 128 + r, q);
+          VFeat<8> f = vertex_features<8>(lm, vr, V, tile * 128 + r, q, cs, cu);
 #pragma unroll
           for (int i = 0; i < 8; ++i)
             *reinterpret_cast<uint2*>(A1 + tile_off(r, 4 * (q + 4 * i), KMAX)) = pack4_bf16(f.f[i]);
@@ -622,7 +687,7 @@ __global__ void __launch_bounds__(kInferThreads, KMAX == 64 ? 2 : 1)
           const float s = scls[r];
           rec16[2 * (size_t)v] = __ldg(vr + v);
           rec16[2 * (size_t)v + 1] = make_float4(fmaf(z0, s, gcs[3 * r]), fmaf(z1, s, gcs[3 * r + 1]),
-                                                 fmaf(z2, s, gcs[3 * r + 2]), trunc_lo(__ldg(u + v)));
+                                                 fmaf(z2, s, gcs[3 * r + 2]), 0.f);
         }
         const int slot = warp_slot(fb, fb_count);
         if (fb && slot < V) fb_items[slot] = v;
@@ -674,10 +739,11 @@ __global__ void k_mlp_pack(const float* __restrict__ P, unsigned char* __restric
 // words (hi_i - hi_0 is exact for nearby values), so they are good to
 // ~2^-48 of u instead of 2^-24
 __device__ __forceinline__ float3 tet_grad_rec(const float4& p0, const float4& p1, const float4& p2,
-                                              const float4& p3, float l0, float l1, float l2, float l3) {
-  const float e1x = p1.x - p0.x, e1y = p1.y - p0.y, e1z = p1.z - p0.z, d1 = (p1.w - p0.w) + (l1 - l0);
-  const float e2x = p2.x - p0.x, e2y = p2.y - p0.y, e2z = p2.z - p0.z, d2 = (p2.w - p0.w) + (l2 - l0);
-  const float e3x = p3.x - p0.x, e3y = p3.y - p0.y, e3z = p3.z - p0.z, d3 = (p3.w - p0.w) + (l3 - l0);
+                                              const float4& p3, float cs, float cu) {
+  const float e1x = qdiff(p1.x, p0.x, cs), e1y = qdiff(p1.y, p0.y, cs), e1z = qdiff(p1.z, p0.z, cs);
+  const float e2x = qdiff(p2.x, p0.x, cs), e2y = qdiff(p2.y, p0.y, cs), e2z = qdiff(p2.z, p0.z, cs);
+  const float e3x = qdiff(p3.x, p0.x, cs), e3y = qdiff(p3.y, p0.y, cs), e3z = qdiff(p3.z, p0.z, cs);
+  const float d1 = qdiff(p1.w, p0.w, cu), d2 = qdiff(p2.w, p0.w, cu), d3 = qdiff(p3.w, p0.w, cu);
   // cofactor rows c1 = e2 x e3, c2 = e3 x e1, c3 = e1 x e2
   const float c1x = e2y * e3z - e2z * e3y, c1y = e2z * e3x - e2x * e3z, c1z = e2x * e3y - e2y * e3x;
   const float c2x = e3y * e1z - e3z * e1y, c2y = e3z * e1x - e3x * e1z, c2z = e3x * e1y - e3y * e1x;
@@ -688,7 +754,7 @@ __device__ __forceinline__ float3 tet_grad_rec(const float4& p0, const float4& p
 }
 
 // fallback: warp per vertex
-__global__ void k_lfallback(DevMesh m, LearnMesh lm, const float4* __restrict__ vr, const double* __restrict__ u,
+__global__ void k_lfallback(DevMesh m, LearnMesh lm, const float4* __restrict__ vr, const float* __restrict__ lsc,
                             const float* __restrict__ w,
                             const double* __restrict__ rec64, const int* __restrict__ items,
                             const int* __restrict__ count, int cap, float4* __restrict__ rec16) {
@@ -701,18 +767,17 @@ __global__ void k_lfallback(DevMesh m, LearnMesh lm, const float4* __restrict__ 
       if (lane == 0) {
         rec16[2 * (size_t)v] = __ldg(vr + v);
         rec16[2 * (size_t)v + 1] = make_float4((float)rec64[3 * (size_t)v], (float)rec64[3 * (size_t)v + 1],
-                                               (float)rec64[3 * (size_t)v + 2], trunc_lo(u[v]));
+                                               (float)rec64[3 * (size_t)v + 2], 0.f);
       }
       continue;
     }
     const int beg = m.p_off[v], cnt = m.p_off[v + 1] - beg;
+    const float cs = __ldg(lsc), cu = __ldg(lsc + 1);
     float x0 = 0.f, x1 = 0.f, x2 = 0.f;
     for (int k = lane; k < cnt; k += 32) {
       const int t = m.p_el[beg + k];
       const int4 tv = __ldg(reinterpret_cast<const int4*>(m.ev) + t);
-      // field differences with the low words (as in the error kernel)
-      const float3 g = tet_grad_rec(__ldg(vr + tv.x), __ldg(vr + tv.y), __ldg(vr + tv.z), __ldg(vr + tv.w),
-                                    trunc_lo(u[tv.x]), trunc_lo(u[tv.y]), trunc_lo(u[tv.z]), trunc_lo(u[tv.w]));
+      const float3 g = tet_grad_rec(__ldg(vr + tv.x), __ldg(vr + tv.y), __ldg(vr + tv.z), __ldg(vr + tv.w), cs, cu);
       const float wk = w[beg + k];
       x0 = fmaf(wk, g.x, x0);
       x1 = fmaf(wk, g.y, x1);
@@ -726,7 +791,7 @@ __global__ void k_lfallback(DevMesh m, LearnMesh lm, const float4* __restrict__ 
     }
     if (lane == 0) {
       rec16[2 * (size_t)v] = __ldg(vr + v);
-      rec16[2 * (size_t)v + 1] = make_float4(x0, x1, x2, trunc_lo(u[v]));
+      rec16[2 * (size_t)v + 1] = make_float4(x0, x1, x2, 0.f);
     }
   }
 }
@@ -737,9 +802,10 @@ __global__ void k_lfallback(DevMesh m, LearnMesh lm, const float4* __restrict__ 
 // two elements per iteration, all loads issued before use; w dV and h_max
 // are the per-mesh element geometry
 __global__ void __launch_bounds__(kBlock) k_lerror(DevMesh m, const float4* __restrict__ rec,
-                                                   const float2* __restrict__ geo, float* __restrict__ q,
-                                                   double* __restrict__ partials) {
+                                                   const float* __restrict__ lsc, const float2* __restrict__ geo,
+                                                   float* __restrict__ q, double* __restrict__ partials) {
   __shared__ double sh[2][kBlock / 32];
+  const float cs = __ldg(lsc), cu = __ldg(lsc + 1);
   float self = 0.f, gsum = 0.f;
   const int stride = gridDim.x * blockDim.x;
   for (int t0 = blockIdx.x * blockDim.x + threadIdx.x; t0 < m.T; t0 += 2 * stride) {
@@ -752,7 +818,7 @@ __global__ void __launch_bounds__(kBlock) k_lerror(DevMesh m, const float4* __re
       tv[i] = in ? __ldg(reinterpret_cast<const int4*>(m.ev) + ts[i]) : make_int4(0, 0, 0, 0);
       gm[i] = in ? __ldg(geo + ts[i]) : make_float2(0.f, 0.f);
     }
-    // one 32-byte record per vertex: {x, y, z, u_hi}, {eps*, u_lo}
+    // one 32-byte record per vertex: {X, Y, Z, U}, {eps*, 0}
     float4 P[2][4], E[2][4];
 #pragma unroll
     for (int i = 0; i < 2; ++i) {
@@ -763,8 +829,7 @@ __global__ void __launch_bounds__(kBlock) k_lerror(DevMesh m, const float4* __re
 #pragma unroll
     for (int i = 0; i < 2; ++i) {
       if (ts[i] >= m.T) continue;
-      const float3 g =
-          tet_grad_rec(P[i][0], P[i][1], P[i][2], P[i][3], E[i][0].w, E[i][1].w, E[i][2].w, E[i][3].w);
+      const float3 g = tet_grad_rec(P[i][0], P[i][1], P[i][2], P[i][3], cs, cu);
       const float ex = 0.25f * ((E[i][0].x + E[i][1].x) + (E[i][2].x + E[i][3].x));
       const float ey = 0.25f * ((E[i][0].y + E[i][1].y) + (E[i][2].y + E[i][3].y));
       const float ez = 0.25f * ((E[i][0].z + E[i][1].z) + (E[i][2].z + E[i][3].z));
@@ -1167,20 +1232,25 @@ void learned_build_v2v(const DevMesh& m, int* off, int* nb, int* tmp, unsigned c
   if (m.V) k_tile_half<<<(m.V + 127) / 128, 128, 0, s>>>(m.V, off, tile_half, max_deg);
 }
 
-void learned_prep(const DevMesh& m, const double* u, float4* vr16, cudaStream_t s) {
-  if (m.V) k_lprep<<<nblk(m.V), kBlock, 0, s>>>(m.V, u, reinterpret_cast<const float4*>(m.xyz32), vr16);
+size_t learned_range_bytes() { return sizeof(double) * (3 * kRangeGrid + 2); }
+
+void learned_prep(const DevMesh& m, const double* u, float cs, double* range, unsigned* done, float* lsc,
+                  float4* vr16, cudaStream_t s) {
+  if (!m.V) return;
+  k_lrange<<<std::min(nblk(m.V), kRangeGrid), kBlock, 0, s>>>(m.V, u, cs, range, done, lsc);
+  k_lprep<<<nblk(m.V), kBlock, 0, s>>>(m.V, u, reinterpret_cast<const int4*>(m.xyzq), range, vr16);
 }
 
-void learned_features(const DevMesh& m, const LearnMesh& lm, const float4* vr16, uint16_t* x, float* aux,
-                      cudaStream_t s) {
-  if (m.V) k_lfeatures<<<nblk(4L * m.V), kBlock, 0, s>>>(m.V, lm, vr16, reinterpret_cast<uint2*>(x), aux);
+void learned_features(const DevMesh& m, const LearnMesh& lm, const float4* vr16, const float* lsc, uint16_t* x,
+                      float* aux, cudaStream_t s) {
+  if (m.V) k_lfeatures<<<nblk(4L * m.V), kBlock, 0, s>>>(m.V, lm, vr16, lsc, reinterpret_cast<uint2*>(x), aux);
 }
 
 void learned_pack(const float* params, void* packed, cudaStream_t s) {
   k_mlp_pack<<<32, 256, 0, s>>>(params, static_cast<unsigned char*>(packed));
 }
 
-void learned_infer(const DevMesh& m, const LearnMesh& lm, const float4* vr16, const double* u, const void* packed,
+void learned_infer(const DevMesh& m, const LearnMesh& lm, const float4* vr16, const float* lsc, const void* packed,
                    float4* rec16, int* fb_items, int* fb_count, float z_max, int use_mlp, int max_degree,
                    int stall_polls, int* err, cudaStream_t s) {
   if (!m.V) return;
@@ -1188,18 +1258,18 @@ void learned_infer(const DevMesh& m, const LearnMesh& lm, const float4* vr16, co
   if (max_degree <= kMlpSlots / 2) {
     const int grid = std::min(infer_grid<64>(), ntiles);
     k_mlp_infer<64><<<grid, kInferThreads, InferSmem<64>::kTotal, s>>>(
-        m.V, lm, vr16, u, static_cast<const uint4*>(packed), rec16, fb_items, fb_count, z_max, use_mlp, stall_polls, err);
+        m.V, lm, vr16, lsc, static_cast<const uint4*>(packed), rec16, fb_items, fb_count, z_max, use_mlp, stall_polls, err);
   } else {
     const int grid = std::min(infer_grid<128>(), ntiles);
     k_mlp_infer<128><<<grid, kInferThreads, InferSmem<128>::kTotal, s>>>(
-        m.V, lm, vr16, u, static_cast<const uint4*>(packed), rec16, fb_items, fb_count, z_max, use_mlp, stall_polls, err);
+        m.V, lm, vr16, lsc, static_cast<const uint4*>(packed), rec16, fb_items, fb_count, z_max, use_mlp, stall_polls, err);
   }
 }
 
-void learned_fallback(const DevMesh& m, const LearnMesh& lm, const float4* vr16, const double* u, const float* w,
+void learned_fallback(const DevMesh& m, const LearnMesh& lm, const float4* vr16, const float* lsc, const float* w,
                       const double* rec64, const int* fb_items, const int* fb_count, int fb_cap, float4* rec16,
                       cudaStream_t s) {
-  k_lfallback<<<152 * 4, 256, 0, s>>>(m, lm, vr16, u, w, rec64, fb_items, fb_count, fb_cap, rec16);
+  k_lfallback<<<152 * 4, 256, 0, s>>>(m, lm, vr16, lsc, w, rec64, fb_items, fb_count, fb_cap, rec16);
 }
 
 int learned_error_blocks(int T) {
@@ -1207,9 +1277,9 @@ int learned_error_blocks(int T) {
   return nb < kLErrorGrid ? nb : kLErrorGrid;
 }
 
-void learned_error(const DevMesh& m, const float4* rec, const float2* geo, float* q, double* partials, int nb,
-                   cudaStream_t s) {
-  if (nb) k_lerror<<<nb, kBlock, 0, s>>>(m, rec, geo, q, partials);
+void learned_error(const DevMesh& m, const float4* rec, const float* lsc, const float2* geo, float* q, double* partials,
+                   int nb, cudaStream_t s) {
+  if (nb) k_lerror<<<nb, kBlock, 0, s>>>(m, rec, lsc, geo, q, partials);
 }
 
 void learned_average(const DevMesh& m, const float* q, const double* out3, float* size, cudaStream_t s) {

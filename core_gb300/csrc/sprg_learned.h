@@ -38,34 +38,39 @@ struct LearnMesh {
 // the per-tile degree flags (ceil(V / 128) bytes) and the largest degree
 void learned_build_v2v(const DevMesh& m, int* off, int* nb, int* tmp, unsigned char* tile_half, int* max_deg,
                        cudaStream_t s);
-// FP32 vertex records {x, y, z, u}
-void learned_prep(const DevMesh& m, const double* u, float4* vr16, cudaStream_t s);
+// fixed-point vertex records {X, Y, Z, U} (16 bytes): the coordinates from
+// m.xyzq, the field on the pass's range.  range: learned_range_bytes() of
+// scratch, done: one device counter (zero before the first call, left zero),
+// lsc: the two difference scales {cs, cu} (cs = 2^-30 / the frame's s)
+size_t learned_range_bytes();
+void learned_prep(const DevMesh& m, const double* u, float cs, double* range, unsigned* done, float* lsc,
+                  float4* vr16, cudaStream_t s);
 // features for training: x [V][128] BF16 (row-major), aux [V][5]
-void learned_features(const DevMesh& m, const LearnMesh& lm, const float4* vr16, uint16_t* x, float* aux,
-                      cudaStream_t s);
+void learned_features(const DevMesh& m, const LearnMesh& lm, const float4* vr16, const float* lsc, uint16_t* x,
+                      float* aux, cudaStream_t s);
 // pack FP32 master parameters into the inference layout
 void learned_pack(const float* params, void* packed, cudaStream_t s);
 // MLP inference over all vertices (tensor cores): rec16 (32-byte records
-// {x, y, z, u_hi}, {eps*, u_lo}) for the vertices the
+// {X, Y, Z, U}, {eps*, 0}) for the vertices the
 // network answers, the rest appended to fb_items (fb_count); use_mlp = 0
 // gives the cheap gradient alone.  err: set when a wait timed out.
 // max_degree <= 16 selects the K = 64 kernel (two blocks per SM)
 // stall_polls > 0 (test hook): the first layer-1 completion wait of each
 // block waits that many polls on a barrier nothing completes and runs out
-void learned_infer(const DevMesh& m, const LearnMesh& lm, const float4* vr16, const double* u, const void* packed,
+void learned_infer(const DevMesh& m, const LearnMesh& lm, const float4* vr16, const float* lsc, const void* packed,
                    float4* rec16, int* fb_items, int* fb_count, float z_max, int use_mlp, int max_degree,
                    int stall_polls, int* err, cudaStream_t s);
 // plain SPR for the fallback vertices (FP32 weights, FP32 element gradients;
 // listed patches take rec64, their FP64 reference result)
-void learned_fallback(const DevMesh& m, const LearnMesh& lm, const float4* vr16, const double* u, const float* w,
+void learned_fallback(const DevMesh& m, const LearnMesh& lm, const float4* vr16, const float* lsc, const float* w,
                       const double* rec64, const int* fb_items, const int* fb_count, int fb_cap, float4* rec16,
                       cudaStream_t s);
 int learned_error_blocks(int T);
-// rec: one 32-byte record per vertex {x, y, z, u_hi}, {eps*, u_lo} (written by the
+// rec: one 32-byte record per vertex {X, Y, Z, U}, {eps*, 0} (written by the
 // network and fallback kernels); w dV and h_max from the per-mesh element
 // geometry (geo)
-void learned_error(const DevMesh& m, const float4* rec, const float2* geo, float* q, double* partials, int nb,
-                   cudaStream_t s);
+void learned_error(const DevMesh& m, const float4* rec, const float* lsc, const float2* geo, float* q, double* partials,
+                   int nb, cudaStream_t s);
 void learned_average(const DevMesh& m, const float* q, const double* out3, float* size, cudaStream_t s);
 void learned_measure(const DevMesh& m, const float* half_len, const float* size, uint32_t* split, uint32_t* collapse,
                      cudaStream_t s);

@@ -4,7 +4,10 @@ training kernels' forward pass, and the pass itself against the FP64 path.
 
 Stated tolerances of the learned form (SPRG_LEARNED), on the 64^3 jittered
 box with the Gaussian-bump field, against the FP64 path (which equals the
-oracle to 1e-10): size field relative error median <= 2e-3 and p99 <= 3e-2,
+oracle to 1e-10): size field relative error median <= 2e-3 and p99 <= 2e-2
+(measured 1.4e-3 and 1.6e-2; the form's target of 1e-2 for the p99 is not
+met: with exact sweeps the network's recovered values alone leave 1.65e-2
+at 160^3, its prediction of the correction being good to about 7 % RMS),
 mark agreement >= 99.5 %, and the network cuts the median error of the
 method without it (the cheap least-squares gradient) by 10x or more.  The network's gradient kernels agree with the FP64 CPU network
 (same BF16 rounding points) to 1e-3 relative.
@@ -170,7 +173,7 @@ def test_learned_pass_accuracy_and_ablation(gpu_lib):
         pytest.skip("no trained parameters shipped")
     rel, agree, info = learned_vs_fp64(64)
     assert np.median(rel) <= 2e-3
-    assert np.percentile(rel, 99) <= 3e-2
+    assert np.percentile(rel, 99) <= 2e-2
     assert agree >= 0.995
     assert info["n_learned_fallback"] < 0.05 * 65 ** 3
     # the method without the network (the cheap gradient alone) is far worse
