@@ -96,6 +96,29 @@ def batch_boxes(n_meshes, seed=3, lo=4, hi=40, jitter=0.0):
     return Mesh(3, coords, ev, ed), np.concatenate(us), voff, eoff, doff, ns
 
 
+def batch_squares(n_meshes, seed=5, lo=8, hi=64, jitter=0.15):
+    """A batch of triangle meshes for the anisotropic pass: n_meshes unit
+    squares of n x n cells (n log-uniform in [lo, hi], seeded, interior
+    jitter), each with its own field of Gaussian bumps (batched_field),
+    flattened into one disjoint union.  Returns (mesh, u, vert_offsets,
+    elem_offsets, edge_offsets, ns)."""
+    from .mesh import Mesh
+    rng = np.random.Generator(np.random.PCG64(seed))
+    ns = np.rint(np.exp(rng.uniform(np.log(lo), np.log(hi), n_meshes))).astype(int)
+    parts, us = [], []
+    for k, n in enumerate(ns):
+        m = box(int(n), nz=0, jitter=jitter, seed=seed * 1_000_003 + k)
+        parts.append(m)
+        us.append(batched_field(m.coords, seed * 1_000_003 + k))
+    voff = np.concatenate([[0], np.cumsum([p.n_verts for p in parts])]).astype(np.int64)
+    eoff = np.concatenate([[0], np.cumsum([p.n_elems for p in parts])]).astype(np.int64)
+    doff = np.concatenate([[0], np.cumsum([p.n_edges for p in parts])]).astype(np.int64)
+    coords = np.concatenate([p.coords for p in parts])
+    ev = np.concatenate([p.elem_verts + np.int32(voff[k]) for k, p in enumerate(parts)])
+    ed = np.concatenate([p.edge_verts + np.int32(voff[k]) for k, p in enumerate(parts)])
+    return Mesh(2, coords, ev, ed), np.concatenate(us), voff, eoff, doff, ns
+
+
 def config(name):
     """(mesh, field, adapt_ratio) of a named workload."""
     if name == "box8":

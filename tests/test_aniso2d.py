@@ -192,6 +192,35 @@ def test_mixed_aniso_pass_matches_fp64(gpu_lib, dim):
 
 
 @pytest.mark.gpu
+def test_batch_of_squares_matches_per_mesh_passes(gpu_lib):
+    """The batched form of the anisotropic pass: uneven triangle meshes with
+    their own fields in one context (a disjoint union).  The pass has no
+    reduction across vertices (the metric comes from each vertex's Hessian),
+    so every mesh gets exactly its own pass's result: FP64 marks and
+    qualities bitwise, mixed (SPRG_FP32) marks identical to the mesh's own
+    mixed pass and to the FP64 batch."""
+    from core_gb300 import workload
+    from core_gb300.mesh import Mesh
+    m, u, voff, eoff, doff, ns = workload.batch_squares(6, seed=7, lo=8, hi=48)
+    eps, hmin, hmax = workload.aniso2d_params(24)
+    s64, c64, q64, *_ = run_aniso(m, u, eps, hmin, hmax, "fp64")
+    s32, c32, q32, *_ = run_aniso(m, u, eps, hmin, hmax, "fp32")
+    assert np.array_equal(s32, s64) and np.array_equal(c32, c64)
+    assert s64.any() and c64.any()
+    for k in range(len(ns)):
+        mk = Mesh(2, m.coords[voff[k]:voff[k + 1]], m.elem_verts[eoff[k]:eoff[k + 1]] - voff[k],
+                  m.edge_verts[doff[k]:doff[k + 1]] - voff[k])
+        uk = u[voff[k]:voff[k + 1]]
+        e, t = slice(doff[k], doff[k + 1]), slice(eoff[k], eoff[k + 1])
+        a64, b64, r64, *_ = run_aniso(mk, uk, eps, hmin, hmax, "fp64")
+        assert np.array_equal(s64[e], a64) and np.array_equal(c64[e], b64), k
+        assert np.array_equal(q64[t], r64), k
+        a32, b32, r32, *_ = run_aniso(mk, uk, eps, hmin, hmax, "fp32")
+        assert np.array_equal(s32[e], a32) and np.array_equal(c32[e], b32), k
+        assert np.abs(q32[t] - r64).max() <= 1e-4 * np.abs(r64).max(), k
+
+
+@pytest.mark.gpu
 def test_isotropic_fp32_pass_rejects_triangles(gpu_lib):
     import core_gb300 as cg
     from core_gb300 import _lib as K, workload
