@@ -82,7 +82,7 @@ struct sprg_ctx {
   DevBuf bvoff, bseg, bsegoff, bratios;
   static constexpr int kSegTets = 2048;  // elements per error segment (8 per thread)
   // binned recover: patch-size bins, tiles, tuned configuration
-  DevBuf pcls, bverts, btiles, bnext;
+  DevBuf pcls, bverts, btiles, bnext, bcnt;
   bool bins_ready = false, tuned = false, autotune = true;
   int bin_count[4] = {0, 0, 0, 0};
   int bin_lanes[4] = {4, 4, 4, 4};
@@ -683,7 +683,8 @@ static void invalidate_mesh_state(sprg_ctx* c) {
   c->vrec_ready = false;
   c->crec_ready = false;
   c->bins_ready = false;
-  c->tuned = false;
+  // the tuned launch shape stays: every choice gives bitwise the same result,
+  // and an adapt iteration changes the patch-size mix little
   c->tw_ready = false;
   c->qw_ready = false;
   c->vv_ready = false;
@@ -850,7 +851,7 @@ int sprg_destroy(sprg_ctx* c) {
   if (!c) return SPRG_OK;
   cudaSetDevice(c->device);
   if (c->own) cudaStreamSynchronize(c->own);
-  DevBuf* bufs[] = {&c->xyz,   &c->xyzq,   &c->ev,   &c->edv,   &c->poff,    &c->pel,    &c->aoff,
+  DevBuf* bufs[] = {&c->bcnt, &c->xyz,   &c->xyzq,   &c->ev,   &c->edv,   &c->poff,    &c->pel,    &c->aoff,
                     &c->ael,   &c->tmp,     &c->f,    &c->ip,    &c->rec,     &c->err,    &c->esize,
                     &c->size,  &c->L,       &c->flags, &c->q,    &c->sizes3,  &c->frames9, &c->partials,
                     &c->out3,  &c->status,  &c->count, &c->mcount, &c->xitems, &c->xcount, &c->slab, &c->bits, &c->titems, &c->tcountb, &c->Lx, &c->pairs, &c->red, &c->eflags, &c->logm, &c->qw, &c->qwlisted, &c->qwitems, &c->qwcount, &c->tw, &c->twlisted, &c->twitems, &c->twcount, &c->met32, &c->qrec32, &c->cj64, &c->qties, &c->kidx, &c->kval, &c->klen, &c->rec9, &c->cache2d.v, &c->cache2d.n, &c->cache2d.el, &c->agitems, &c->agcount,
@@ -1318,10 +1319,16 @@ static int fast_setup(sprg_ctx* c, ExpandList xl) {
   ENSURE(c->geo64, 16 * (size_t)m.T);
   ENSURE(c->elen, 4 * (size_t)m.E);
   CK(cudaMemsetAsync(c->fcnt.p, 0, 8 * sizeof(int), c->stream));
+  PB("setup_coords");
   fast_prep_coords(m, c->frame, P<float4>(c->crec), c->stream);
+  PE();
   c->crec_ready = true;
+  PB("setup_geometry");
   fast_geometry(m, P<float2>(c->geo), P<double2>(c->geo64), P<float>(c->elen), c->stream);
+  PE();
+  PB("setup_weights");
   fast_weights(m, P<float>(c->wts), P<double>(c->w64), xl, P<int>(c->fcnt), P<unsigned char>(c->listed), c->stream);
+  PE();
   int h[2] = {0, 0};
   CK(cudaMemcpyAsync(&h[0], P<int>(c->fcnt) + 3, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaMemcpyAsync(&h[1], c->fcnt.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
@@ -1368,22 +1375,34 @@ static int listed_join(sprg_ctx* c, ExpandList xl, bool forked) {
 static int build_bins(sprg_ctx* c) {
   if (c->bins_ready) return SPRG_OK;
   DevMesh& m = c->m;
+  int rc;
   ENSURE(c->pcls, (size_t)m.V);
   ENSURE(c->bverts, sizeof(int) * (size_t)m.V);
   ENSURE(c->bnext, sizeof(int));
   fast_patch_class(m, P<unsigned char>(c->listed), P<unsigned char>(c->pcls), c->stream);
-  std::vector<unsigned char> cls(m.V);
-  CK(cudaMemcpyAsync(cls.data(), c->pcls.p, (size_t)m.V, cudaMemcpyDeviceToHost, c->stream));
+  // per-block class counts -> per-class exclusive offsets of every block
+  // (host scan of 4 ints per 1024 vertices) -> device scatter
+  const int nb = fast_bin_blocks(m.V);
+  ENSURE(c->bcnt, sizeof(int) * 8 * (size_t)nb);
+  fast_bin_count(m.V, P<unsigned char>(c->pcls), P<int>(c->bcnt), c->stream);
+  std::vector<int> cnt(4 * (size_t)nb), offs(4 * (size_t)nb);
+  CK(cudaMemcpyAsync(cnt.data(), c->bcnt.p, sizeof(int) * cnt.size(), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
-  std::vector<int> order;
-  order.reserve(m.V);
+  long long base = 0;
   for (int b = 0; b < 4; ++b) {
-    const size_t before = order.size();
-    for (int v = 0; v < m.V; ++v)
-      if (cls[v] == b) order.push_back(v);
-    c->bin_count[b] = (int)(order.size() - before);
+    long long run = base;
+    for (int k = 0; k < nb; ++k) {
+      offs[4 * (size_t)k + b] = (int)run;
+      run += cnt[4 * (size_t)k + b];
+    }
+    c->bin_count[b] = (int)(run - base);
+    base = run;
   }
-  CK(cudaMemcpy(c->bverts.p, order.data(), sizeof(int) * order.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpyAsync(P<int>(c->bcnt) + 4 * (size_t)nb, offs.data(), sizeof(int) * offs.size(),
+                     cudaMemcpyHostToDevice, c->stream));
+  fast_bin_scatter(m.V, P<unsigned char>(c->pcls), P<int>(c->bcnt) + 4 * (size_t)nb, P<int>(c->bverts), c->stream);
+  CK(cudaStreamSynchronize(c->stream));  // offs lives on this frame
+  if ((rc = check_launch(c, "patch-size bins"))) return rc;
   int dev = 0;
   CK(cudaGetDevice(&dev));
   CK(cudaDeviceGetAttribute(&c->n_sms, cudaDevAttrMultiProcessorCount, dev));
@@ -1551,8 +1570,10 @@ static int pass_fast(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_
   fast_tet(m, vrec, P<double>(c->f), (float)c->frame[3], P<uint4>(c->tetd), P<int>(c->tnext), c->stream);
   PE();
   if (!c->bins_ready) {
+    PB("setup_bins");
     if ((rc = build_bins(c))) return rc;
     if ((rc = build_tiles(c))) return rc;
+    PE();
   }
   if (c->autotune && !c->tuned && (rc = autotune(c, rec32))) return rc;
   PB("recover_f32");
@@ -1919,7 +1940,7 @@ int sprg_debug_read(sprg_ctx* c, const char* name, void* host, size_t bytes) {
       {"fcnt", &c->fcnt},   {"guard", &c->guard}, {"xitems", &c->xitems}, {"xcount", &c->xcount}, {"agcount", &c->agcount}, {"sizes3", &c->sizes3}, {"frames9", &c->frames9}, {"twcount", &c->twcount}, {"met32", &c->met32}, {"rec9", &c->rec9},
       {"wts", &c->wts},     {"geo", &c->geo},     {"elen", &c->elen},     {"rec16", &c->rec16},
       {"sizel", &c->sizel}, {"ql", &c->ql},       {"vr16", &c->vr16},     {"fbitems", &c->fbitems},
-      {"fbcount", &c->fbcount}, {"listed", &c->listed}};
+      {"fbcount", &c->fbcount}, {"listed", &c->listed}, {"bverts", &c->bverts}, {"pcls", &c->pcls}};
   for (auto& e : table) {
     if (strcmp(e.n, name) != 0) continue;
     if (!e.b->p) return fail(c, SPRG_ESTATE, std::string("buffer not allocated: ") + name);
@@ -2359,6 +2380,7 @@ int sprg_batch_info(sprg_ctx* c, double* out) {
 int sprg_set_autotune(sprg_ctx* c, int on) {
   if (!c) return SPRG_EINVAL;
   c->autotune = on != 0;
+  c->tuned = false;  // on: tune again at the next pass
   drop_e2e_graph(c);
   return SPRG_OK;
 }

@@ -28,6 +28,12 @@ void fast_weights(const DevMesh& m, float* w, double* w64, ExpandList xl, int* n
 void fast_merge_ref(ExpandList xl, const double* rec64, uint4* rec32, cudaStream_t s);
 // patch-size class per vertex: 0 (<= 8 elements), 1 (<= 16), 2 (<= 32), 3, 4 = listed
 void fast_patch_class(const DevMesh& m, const unsigned char* listed, unsigned char* cls, cudaStream_t s);
+// the bins' vertex order on the device: per-block class counts (4 ints per
+// block of fast_bin_blocks(V)), then, with the blocks' exclusive offsets per
+// class (4 ints per block), the scatter: each bin in ascending vertex order
+int fast_bin_blocks(int V);
+void fast_bin_count(int V, const unsigned char* cls, int* counts, cudaStream_t s);
+void fast_bin_scatter(int V, const unsigned char* cls, const int* offs, int* order, cudaStream_t s);
 // binned recover: tiles (first, count, lanes in {1, 2, 4}, bin) over verts, taken
 // from a counter by a persistent grid; every tiling gives the same bits
 void fast_recover_tiles(const DevMesh& m, const float* w, const uint4* td, uint4* rec, const int* verts,

@@ -591,6 +591,49 @@ __global__ void k_patch_class(DevMesh m, const unsigned char* __restrict__ liste
   cls[v] = listed[v] ? 4 : (unsigned char)patch_class(m.p_off[v + 1] - m.p_off[v]);
 }
 
+constexpr int kBinBlock = 1024;
+
+// Stable partition of the vertices by patch class (bins 0..3; class 4, the
+// listed patches, stays out): per-block class counts, then a scatter over
+// the same blocks, each class in ascending vertex order.  Counts are sums of
+// ballots, the ranks prefix sums over warps: the order is fixed.
+__global__ void __launch_bounds__(kBinBlock) k_bin_count(int V, const unsigned char* __restrict__ cls,
+                                                         int* __restrict__ counts) {
+  __shared__ int sc[4];
+  if (threadIdx.x < 4) sc[threadIdx.x] = 0;
+  __syncthreads();
+  const int v = blockIdx.x * kBinBlock + threadIdx.x;
+  const int b = v < V ? cls[v] : 4;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const unsigned mask = __ballot_sync(0xffffffffu, b == k);
+    if ((threadIdx.x & 31) == 0 && mask) atomicAdd(&sc[k], __popc(mask));
+  }
+  __syncthreads();
+  if (threadIdx.x < 4) counts[4 * blockIdx.x + threadIdx.x] = sc[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(kBinBlock) k_bin_scatter(int V, const unsigned char* __restrict__ cls,
+                                                           const int* __restrict__ offs, int* __restrict__ order) {
+  __shared__ int wc[kBinBlock / 32][4];
+  const int v = blockIdx.x * kBinBlock + threadIdx.x;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int b = v < V ? cls[v] : 4;
+  unsigned mine = 0;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const unsigned mask = __ballot_sync(0xffffffffu, b == k);
+    if (lane == 0) wc[w][k] = __popc(mask);
+    if (b == k) mine = mask;
+  }
+  __syncthreads();
+  if (b < 4) {
+    int before = 0;
+    for (int j = 0; j < w; ++j) before += wc[j][b];
+    order[offs[4 * blockIdx.x + b] + before + __popc(mine & ((1u << lane) - 1))] = v;
+  }
+}
+
 // listed vertices take the FP64 reference result, as value + packed remainder
 __global__ void k_merge_ref(const int* __restrict__ items, const int* __restrict__ count, int cap,
                             const double* __restrict__ rec64, uint4* __restrict__ rec) {
@@ -965,6 +1008,16 @@ void fast_weights(const DevMesh& m, float* w, double* w64, ExpandList xl, int* n
 
 void fast_patch_class(const DevMesh& m, const unsigned char* listed, unsigned char* cls, cudaStream_t s) {
   if (m.V) k_patch_class<<<nblk(m.V), kBlock, 0, s>>>(m, listed, cls);
+}
+
+int fast_bin_blocks(int V) { return (V + kBinBlock - 1) / kBinBlock; }
+
+void fast_bin_count(int V, const unsigned char* cls, int* counts, cudaStream_t s) {
+  if (V) k_bin_count<<<fast_bin_blocks(V), kBinBlock, 0, s>>>(V, cls, counts);
+}
+
+void fast_bin_scatter(int V, const unsigned char* cls, const int* offs, int* order, cudaStream_t s) {
+  if (V) k_bin_scatter<<<fast_bin_blocks(V), kBinBlock, 0, s>>>(V, cls, offs, order);
 }
 
 void fast_recover_tiles(const DevMesh& m, const float* w, const uint4* td, uint4* rec, const int* verts,

@@ -417,8 +417,9 @@ int sprg_batch_info(sprg_ctx* ctx, double* out);
    The FP32 recovery runs over patch-size bins (<= 8, <= 16, <= 32, more
    elements) in one persistent launch; on the first pass of a mesh an
    autotuner times lanes per bin, tile size and blocks per SM on the real
-   data (every choice gives bitwise the same result).  on = 0 keeps the
-   default configuration. */
+   data (every choice gives bitwise the same result).  The choice is kept
+   across sprg_update_mesh; calling this with on = 1 tunes again at the next
+   pass.  on = 0 keeps the current configuration. */
 int sprg_set_autotune(sprg_ctx* ctx, int on);
 /* fix the binned recovery's configuration (lanes per bin in {1, 2, 4}, tile
    size in vertices, blocks per SM); turns the autotuner off */

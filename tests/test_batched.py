@@ -135,3 +135,30 @@ def test_graph_replay_matches_direct_passes(gpu_lib):
             c.graph_replay()
             torch.cuda.synchronize()
             assert np.array_equal(bits.cpu().numpy(), want)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("which", ["box", "batch"])
+def test_bins_are_the_stable_class_order(gpu_lib, which):
+    """The recovery's patch-size bins, built on the device (per-block class
+    counts, host scan, ballot scatter): every bin (<= 8, <= 16, <= 32, more
+    patch elements; listed patches left out) lists its vertices in ascending
+    order, as a plain loop over the vertices would."""
+    import core_gb300 as cg
+    from core_gb300 import workload
+    if which == "box":
+        m = workload.box(37, jitter=0.2, seed=3)
+        u = workload.bump_field(m.coords, seed=3)
+    else:
+        m, u, *_ = workload.batch_boxes(40, seed=5, lo=3, hi=14, jitter=0.2)
+    with cg.Context(m, precision="fp32") as c:
+        c.estimate_and_mark(u, 0.05)
+        listed = c.debug_read("listed", np.uint8, m.n_verts)
+        order = c.debug_read("bverts", np.int32, m.n_verts)
+        bins = c.tuning_report()["bins"]
+    cnt = np.bincount(m.elem_verts.reshape(-1), minlength=m.n_verts)
+    cls = np.where(cnt <= 8, 0, np.where(cnt <= 16, 1, np.where(cnt <= 32, 2, 3)))
+    cls[listed != 0] = 4
+    want = np.concatenate([np.nonzero(cls == b)[0] for b in range(4)]).astype(np.int32)
+    assert list(bins) == [int(np.sum(cls == b)) for b in range(4)]
+    assert np.array_equal(order[:len(want)], want)
