@@ -73,3 +73,22 @@ def test_oracle_reproduces_reference_outputs(oracle_lib, gold, name):
     assert rc == 0 and rc2 == 0
     assert np.array_equal(flags, g["flags"])
     assert (ns, nc) == (int(g["n_split"]), int(g["n_collapse"]))
+
+
+def test_oracle_full_size_flags_digest(oracle_lib):
+    """The oracle on the 128^3 jittered box (config 2, 12.6M tets) writes the
+    reference's ma_flags words (SHA-256 digest and counts from
+    tests/golden/ref_full_hashes.json, made by make_ref_hashes.py)."""
+    import hashlib
+    import json
+    from refcases import bump, jitter_coords
+    with open(os.path.join(os.path.dirname(__file__), "golden", "ref_full_hashes.json")) as f:
+        g = json.load(f)["box128"]
+    n = g["n"]
+    oracle_lib.set_threads(os.cpu_count() or 1)
+    o = oracle_lib.OracleMesh.box(n, n, n)
+    x = jitter_coords(o.coords.copy(), n, n, 0.2, g["seed"])
+    o.set_coords(x)
+    rc, size, L, flags, ns, nc, info = o.estimate_and_mark(bump(x, g["seed"]), g["ratio"])
+    assert rc == 0 and (ns, nc) == (g["n_split"], g["n_collapse"])
+    assert hashlib.sha256(flags.astype("<i4").tobytes()).hexdigest() == g["flags_sha256"]
