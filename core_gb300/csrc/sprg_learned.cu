@@ -89,52 +89,73 @@ __global__ void k_v2v_sort(int V, const int* __restrict__ off, int* __restrict__
 // at 160^3 through the element gradients and the neighbour fit; exact
 // differences take it to the FP32 arithmetic's level.)
 // ---------------------------------------------------------------------------
-constexpr int kRangeGrid = 304;
+constexpr int kRangeGrid = 1216;
 
 __device__ __forceinline__ float qdiff(float a, float b, float scale) {
   return __int2float_rn(__float_as_int(a) - __float_as_int(b)) * scale;
 }
 
-// the field's range by blocks (min, max, any non-finite value), reduced by
-// the last block to finish (min / max: any order gives the same result):
-// range[3 kRangeGrid ..] = {u_min, s_u}, lsc = {cs, cu}; a NaN or infinite
-// value makes cu NaN, so every difference of the pass is NaN (as FP64 gives
-// NaN sizes for such a field)
-__global__ void __launch_bounds__(kBlock) k_lrange(int V, const double* __restrict__ u, float cs,
-                                                   double* __restrict__ range, unsigned* __restrict__ done,
-                                                   float* __restrict__ lsc) {
-  double lo = INFINITY, hi = -INFINITY;
-  int bad = 0;
-  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
-    const double x = __ldg(u + v);
-    if (isfinite(x)) {
-      lo = fmin(lo, x);
-      hi = fmax(hi, x);
-    } else {
-      bad = 1;
-    }
-  }
+// (min, max, any non-finite) of a block's values, in every thread of warp 0
+// after the call (order-independent reductions)
+__device__ __forceinline__ void range_block(double& lo, double& hi, int& bad) {
+  __shared__ double sh[3][kBlock / 32];
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));
     hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, o));
     bad |= __shfl_xor_sync(0xffffffffu, bad, o);
   }
-  __shared__ double sh[3][kBlock / 32];
-  __shared__ bool last;
-  const int w = threadIdx.x >> 5;
-  if ((threadIdx.x & 31) == 0) {
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) {
     sh[0][w] = lo;
     sh[1][w] = hi;
     sh[2][w] = bad;
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    for (int i = 1; i < kBlock / 32; ++i) {
-      lo = fmin(lo, sh[0][i]);
-      hi = fmax(hi, sh[1][i]);
-      bad |= sh[2][i] != 0.0;
+  if (w == 0) {
+    lo = lane < kBlock / 32 ? sh[0][lane] : INFINITY;
+    hi = lane < kBlock / 32 ? sh[1][lane] : -INFINITY;
+    bad = lane < kBlock / 32 ? (sh[2][lane] != 0.0) : 0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+      hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+      bad |= __shfl_xor_sync(0xffffffffu, bad, o);
     }
+  }
+  __syncthreads();  // sh is reused by the caller's next call
+}
+
+// the field's range by blocks (min, max, any non-finite value), four
+// independent loads in flight per thread, reduced by the last block to
+// finish: range[3 kRangeGrid ..] = {u_min, K} with s_u 2^30 = 2^K, lsc =
+// {cs, cu}; a NaN
+// or infinite value makes cu NaN, so every difference of the pass is NaN
+// (as FP64 gives NaN sizes for such a field)
+__global__ void __launch_bounds__(kBlock) k_lrange(int V, const double* __restrict__ u, float cs,
+                                                   double* __restrict__ range, unsigned* __restrict__ done,
+                                                   float* __restrict__ lsc) {
+  double lo = INFINITY, hi = -INFINITY;
+  int bad = 0;
+  const int stride = gridDim.x * blockDim.x;
+  for (int v0 = blockIdx.x * blockDim.x + threadIdx.x; v0 < V; v0 += 4 * stride) {
+    double x[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) x[i] = v0 + i * stride < V ? __ldg(u + v0 + i * stride) : 0.0;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      if (v0 + i * stride >= V) continue;
+      if (isfinite(x[i])) {
+        lo = fmin(lo, x[i]);
+        hi = fmax(hi, x[i]);
+      } else {
+        bad = 1;
+      }
+    }
+  }
+  range_block(lo, hi, bad);
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
     range[3 * blockIdx.x] = lo;
     range[3 * blockIdx.x + 1] = hi;
     range[3 * blockIdx.x + 2] = bad;
@@ -142,23 +163,24 @@ __global__ void __launch_bounds__(kBlock) k_lrange(int V, const double* __restri
     last = atomicAdd(done, 1u) == gridDim.x - 1;
   }
   __syncthreads();
-  if (!last || threadIdx.x != 0) return;
+  if (!last) return;
   __threadfence();
-  for (int b = 0; b < (int)gridDim.x; ++b) {
+  lo = INFINITY;
+  hi = -INFINITY;
+  bad = 0;
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
     lo = fmin(lo, range[3 * b]);
     hi = fmax(hi, range[3 * b + 1]);
     bad |= range[3 * b + 2] != 0.0;
   }
-  double su = 1.0;
-  if (!bad && hi > lo) {
-    int e;
-    frexp(hi - lo, &e);  // hi - lo = m 2^e, m in [1/2, 1)
-    su = ldexp(1.0, -e);
-  }
+  range_block(lo, hi, bad);
+  if (threadIdx.x != 0) return;
+  int e = 0;  // s_u = 2^-e: 1 for a constant field
+  if (!bad && hi > lo) frexp(hi - lo, &e);  // hi - lo = m 2^e, m in [1/2, 1)
   range[3 * kRangeGrid] = bad ? 0.0 : lo;
-  range[3 * kRangeGrid + 1] = su;
+  range[3 * kRangeGrid + 1] = 30 - e;
   lsc[0] = cs;
-  lsc[1] = bad ? __int_as_float(0x7fc00000) : (float)(ldexp(1.0, -30) / su);
+  lsc[1] = bad ? __int_as_float(0x7fc00000) : (float)ldexp(1.0, e - 30);
   *done = 0;
 }
 
@@ -166,10 +188,20 @@ __global__ void __launch_bounds__(kBlock) k_lprep(int V, const double* __restric
                                                   const double* __restrict__ range, float4* __restrict__ vr) {
   const int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= V) return;
-  const double umin = range[3 * kRangeGrid], su = range[3 * kRangeGrid + 1];
+  const double umin = range[3 * kRangeGrid];
+  const int K = (int)range[3 * kRangeGrid + 1];  // s_u 2^30 = 2^K
   const int4 p = __ldg(xyzq + v);
-  const double t = (__ldg(u + v) - umin) * su * 0x1p30;  // in [0, 2^30] for a finite field
-  const int U = t >= 0.0 && t <= 0x1p30 ? __double2int_rn(t) : 0;
+  // U = (u - u_min) 2^K rounded, from the difference's bits (no FP64
+  // multiply or conversion): d = m 2^(e - 1075), U = m >> (1075 - e - K);
+  // zero, subnormal and non-finite differences give 0 (non-finite fields
+  // are NaN through cu)
+  const long long b = __double_as_longlong(__ldg(u + v) - umin);
+  const int sh = 1075 - (int)((b >> 52) & 0x7ff) - K;
+  int U = 0;
+  if (b > 0 && sh >= 23 && sh < 64) {
+    const unsigned long long mm = (unsigned long long)(b & 0xfffffffffffffLL) | (1ull << 52);
+    U = (int)((mm + (1ull << (sh - 1))) >> sh);
+  }
   vr[v] = make_float4(__int_as_float(p.x), __int_as_float(p.y), __int_as_float(p.z), __int_as_float(U));
 }
 
