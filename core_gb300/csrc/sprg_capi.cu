@@ -82,7 +82,7 @@ struct sprg_ctx {
   DevBuf bvoff, bseg, bsegoff, bratios;
   static constexpr int kSegTets = 2048;  // elements per error segment (8 per thread)
   // binned recover: patch-size bins, tiles, tuned configuration
-  DevBuf pcls, bverts, btiles, bnext, bcnt;
+  DevBuf pcls, bverts, btiles, bnext, bcnt, cent;
   bool bins_ready = false, tuned = false, autotune = true;
   int bin_count[4] = {0, 0, 0, 0};
   int bin_lanes[4] = {4, 4, 4, 4};
@@ -851,7 +851,7 @@ int sprg_destroy(sprg_ctx* c) {
   if (!c) return SPRG_OK;
   cudaSetDevice(c->device);
   if (c->own) cudaStreamSynchronize(c->own);
-  DevBuf* bufs[] = {&c->bcnt, &c->xyz,   &c->xyzq,   &c->ev,   &c->edv,   &c->poff,    &c->pel,    &c->aoff,
+  DevBuf* bufs[] = {&c->bcnt, &c->cent, &c->xyz,   &c->xyzq,   &c->ev,   &c->edv,   &c->poff,    &c->pel,    &c->aoff,
                     &c->ael,   &c->tmp,     &c->f,    &c->ip,    &c->rec,     &c->err,    &c->esize,
                     &c->size,  &c->L,       &c->flags, &c->q,    &c->sizes3,  &c->frames9, &c->partials,
                     &c->out3,  &c->status,  &c->count, &c->mcount, &c->xitems, &c->xcount, &c->slab, &c->bits, &c->titems, &c->tcountb, &c->Lx, &c->pairs, &c->red, &c->eflags, &c->logm, &c->qw, &c->qwlisted, &c->qwitems, &c->qwcount, &c->tw, &c->twlisted, &c->twitems, &c->twcount, &c->met32, &c->qrec32, &c->cj64, &c->qties, &c->kidx, &c->kval, &c->klen, &c->rec9, &c->cache2d.v, &c->cache2d.n, &c->cache2d.el, &c->agitems, &c->agcount,
@@ -1317,6 +1317,7 @@ static int fast_setup(sprg_ctx* c, ExpandList xl) {
   ENSURE(c->listed, (size_t)m.V);
   ENSURE(c->geo, 8 * (size_t)m.T);
   ENSURE(c->geo64, 16 * (size_t)m.T);
+  ENSURE(c->cent, 24 * (size_t)m.T);
   ENSURE(c->elen, 4 * (size_t)m.E);
   CK(cudaMemsetAsync(c->fcnt.p, 0, 8 * sizeof(int), c->stream));
   PB("setup_coords");
@@ -1324,10 +1325,11 @@ static int fast_setup(sprg_ctx* c, ExpandList xl) {
   PE();
   c->crec_ready = true;
   PB("setup_geometry");
-  fast_geometry(m, P<float2>(c->geo), P<double2>(c->geo64), P<float>(c->elen), c->stream);
+  fast_geometry(m, P<float2>(c->geo), P<double2>(c->geo64), P<double>(c->cent), P<float>(c->elen), c->stream);
   PE();
   PB("setup_weights");
-  fast_weights(m, P<float>(c->wts), P<double>(c->w64), xl, P<int>(c->fcnt), P<unsigned char>(c->listed), c->stream);
+  fast_weights(m, P<double>(c->cent), P<float>(c->wts), P<double>(c->w64), xl, P<int>(c->fcnt),
+               P<unsigned char>(c->listed), c->stream);
   PE();
   int h[2] = {0, 0};
   CK(cudaMemcpyAsync(&h[0], P<int>(c->fcnt) + 3, sizeof(int), cudaMemcpyDeviceToHost, c->stream));

@@ -11,7 +11,9 @@ int fast_error_blocks(int T);
 void fast_prep_coords(const DevMesh& m, const double* frame, float4* vrec, cudaStream_t s);
 // once per mesh: per tet {w dV, h_max} (FP32) and {det J, h_max} (FP64), per
 // edge half its length
-void fast_geometry(const DevMesh& m, float2* geo, double2* geo64, float* half_len, cudaStream_t s);
+// cent: 3 doubles per element, the integration point (once per mesh, read by
+// fast_weights)
+void fast_geometry(const DevMesh& m, float2* geo, double2* geo64, double* cent, float* half_len, cudaStream_t s);
 // the pass's vertex records: coordinate records with the field pair (u_hi, u_lo)
 void fast_prep(const DevMesh& m, const double* u, const float4* crec, float4* vrec, cudaStream_t s);
 // per tet: gradient value (3 floats) and packed correction (1 word)
@@ -22,8 +24,8 @@ void fast_tet(const DevMesh& m, const float4* vrec, const double* u, float gscal
               cudaStream_t s);
 // once per mesh: SPR weights in patch-CSR order (FP32 for the pass, FP64 for
 // the guard), listed patches
-void fast_weights(const DevMesh& m, float* w, double* w64, ExpandList xl, int* n_refit, unsigned char* listed,
-                  cudaStream_t s);
+void fast_weights(const DevMesh& m, const double* cent, float* w, double* w64, ExpandList xl, int* n_refit,
+                  unsigned char* listed, cudaStream_t s);
 // recovered value per vertex as value + packed remainder (16 bytes)
 void fast_merge_ref(ExpandList xl, const double* rec64, uint4* rec32, cudaStream_t s);
 // patch-size class per vertex: 0 (<= 8 elements), 1 (<= 16), 2 (<= 32), 3, 4 = listed

@@ -229,7 +229,8 @@ __global__ void __launch_bounds__(kBlock) k_prep(int V, const double* __restrict
 
 // per tet {w dV, h_max} (FP32 for the pass, {det J, h_max} in FP64 for the
 // guard) and per edge half its length, FP64 then rounded (once per mesh)
-__global__ void __launch_bounds__(kBlock) k_fast_geo(DevMesh m, float2* __restrict__ geo, double2* __restrict__ geo64) {
+__global__ void __launch_bounds__(kBlock) k_fast_geo(DevMesh m, float2* __restrict__ geo, double2* __restrict__ geo64,
+                                                     double* __restrict__ cent) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= m.T) return;
   const int* ev = m.ev + 4 * (size_t)t;
@@ -256,6 +257,9 @@ __global__ void __launch_bounds__(kBlock) k_fast_geo(DevMesh m, float2* __restri
   const double h = sqrt(h2);
   geo[t] = make_float2((float)(det * (1.0 / 6.0)), (float)h);
   geo64[t] = make_double2(det, h);
+  // the integration point, summed in vertex order as the weights use it
+#pragma unroll
+  for (int k = 0; k < 3; ++k) cent[3 * (size_t)t + k] = 0.25 * (((x[0][k] + x[1][k]) + x[2][k]) + x[3][k]);
 }
 
 __global__ void __launch_bounds__(kBlock) k_fast_elen(DevMesh m, float* __restrict__ half_len) {
@@ -414,8 +418,8 @@ __global__ void __launch_bounds__(kBlock, 4) k_fast_tet(DevMesh m, const float4*
 // fewer than four elements or a condition estimate above 1e6 are listed for
 // the FP64 reference path (growth + Householder QR) instead.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kBlock) k_fast_weights(DevMesh m, float* __restrict__ w, double* __restrict__ w64,
-                                                         ExpandList xl,
+__global__ void __launch_bounds__(kBlock) k_fast_weights(DevMesh m, const double* __restrict__ cent,
+                                                         float* __restrict__ w, double* __restrict__ w64, ExpandList xl,
                                                          int* __restrict__ n_refit, unsigned char* __restrict__ listed) {
   int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= m.V) return;
@@ -425,14 +429,8 @@ __global__ void __launch_bounds__(kBlock) k_fast_weights(DevMesh m, float* __res
   double inv_h = 0;
   bool ok = cnt >= 4;
   for (int k = 0; ok && k < cnt; ++k) {
-    const int* ev = m.ev + 4 * (size_t)m.p_el[beg + k];
-    double px = 0, py = 0, pz = 0;
-    for (int i = 0; i < 4; ++i) {
-      px += m.xyz[3 * (size_t)ev[i]];
-      py += m.xyz[3 * (size_t)ev[i] + 1];
-      pz += m.xyz[3 * (size_t)ev[i] + 2];
-    }
-    double sx = 0.25 * px - xv, sy = 0.25 * py - yv, sz = 0.25 * pz - zv;
+    const double* ce = cent + 3 * (size_t)m.p_el[beg + k];
+    double sx = ce[0] - xv, sy = ce[1] - yv, sz = ce[2] - zv;
     if (k == 0) inv_h = 1.0 / sqrt(sx * sx + sy * sy + sz * sz);
     sx *= inv_h; sy *= inv_h; sz *= inv_h;
     a[0] += 1; a[1] += sx; a[2] += sy; a[3] += sz;
@@ -470,14 +468,8 @@ __global__ void __launch_bounds__(kBlock) k_fast_weights(DevMesh m, float* __res
   double q1 = (y1 - l21 * q2 - l31 * q3) / l11;
   double q0 = (y0 - l10 * q1 - l20 * q2 - l30 * q3) / l00;
   for (int k = 0; k < cnt; ++k) {
-    const int* ev = m.ev + 4 * (size_t)m.p_el[beg + k];
-    double px = 0, py = 0, pz = 0;
-    for (int i = 0; i < 4; ++i) {
-      px += m.xyz[3 * (size_t)ev[i]];
-      py += m.xyz[3 * (size_t)ev[i] + 1];
-      pz += m.xyz[3 * (size_t)ev[i] + 2];
-    }
-    double sx = (0.25 * px - xv) * inv_h, sy = (0.25 * py - yv) * inv_h, sz = (0.25 * pz - zv) * inv_h;
+    const double* ce = cent + 3 * (size_t)m.p_el[beg + k];
+    double sx = (ce[0] - xv) * inv_h, sy = (ce[1] - yv) * inv_h, sz = (ce[2] - zv) * inv_h;
     const double wk = q0 + q1 * sx + q2 * sy + q3 * sz;
     w[beg + k] = (float)wk;
     w64[beg + k] = wk;
@@ -984,8 +976,8 @@ void fast_prep_coords(const DevMesh& m, const double* frame, float4* vrec, cudaS
   if (m.V) k_prep_coords<<<nblk(m.V), kBlock, 0, s>>>(m.V, m.xyz, frame[0], frame[1], frame[2], frame[3], vrec);
 }
 
-void fast_geometry(const DevMesh& m, float2* geo, double2* geo64, float* half_len, cudaStream_t s) {
-  if (m.T) k_fast_geo<<<nblk(m.T), kBlock, 0, s>>>(m, geo, geo64);
+void fast_geometry(const DevMesh& m, float2* geo, double2* geo64, double* cent, float* half_len, cudaStream_t s) {
+  if (m.T) k_fast_geo<<<nblk(m.T), kBlock, 0, s>>>(m, geo, geo64, cent);
   if (m.E) k_fast_elen<<<nblk(m.E), kBlock, 0, s>>>(m, half_len);
 }
 
@@ -1000,9 +992,9 @@ void fast_tet(const DevMesh& m, const float4* vrec, const double* u, float gscal
   k_fast_tet<<<tet_grid(m.T), kBlock, 0, s>>>(m, vrec, u, gscale, td, next_chunk);
 }
 
-void fast_weights(const DevMesh& m, float* w, double* w64, ExpandList xl, int* n_refit, unsigned char* listed,
-                  cudaStream_t s) {
-  if (m.V) k_fast_weights<<<nblk(m.V), kBlock, 0, s>>>(m, w, w64, xl, n_refit, listed);
+void fast_weights(const DevMesh& m, const double* cent, float* w, double* w64, ExpandList xl, int* n_refit,
+                  unsigned char* listed, cudaStream_t s) {
+  if (m.V) k_fast_weights<<<nblk(m.V), kBlock, 0, s>>>(m, cent, w, w64, xl, n_refit, listed);
 }
 
 
