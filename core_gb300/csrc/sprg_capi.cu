@@ -1431,13 +1431,13 @@ static int build_tiles(sprg_ctx* c, int only = -1) {
   return SPRG_OK;
 }
 
-static void run_tiles(sprg_ctx* c, uint4* rec32) {
+static void run_tiles(sprg_ctx* c, float4* rec32) {
   fast_recover_tiles(c->m, P<float>(c->wts), P<uint4>(c->tetd), rec32, P<int>(c->bverts), P<int4>(c->btiles),
                      c->n_tiles, P<int>(c->bnext), c->n_sms * c->grid_per_sm, c->stream);
 }
 
 // CUDA-event time of the binned recover under the current configuration
-static float time_tiles(sprg_ctx* c, uint4* rec32, int only) {
+static float time_tiles(sprg_ctx* c, float4* rec32, int only) {
   if (build_tiles(c, only)) return 1e30f;
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
@@ -1462,7 +1462,7 @@ static float time_tiles(sprg_ctx* c, uint4* rec32, int only) {
 // blocks per SM {4, 8, 16}; every configuration gives bitwise the same
 // result, so the choice only changes time.  The choice and the timings are
 // kept for sprg_tuning_report.
-static int autotune(sprg_ctx* c, uint4* rec32) {
+static int autotune(sprg_ctx* c, float4* rec32) {
   std::string log = "[";
   auto note = [&](const char* what, int val, float ms) {
     if (log.size() > 1) log += ",";
@@ -1535,7 +1535,7 @@ static int pass_fast(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_
   const int nb = bv.n ? c->batch_nseg : fast_error_blocks(m.T);
   const size_t nel = (size_t)m.T * m.nn;
   ENSURE(c->vrec, 32 * (size_t)m.V);
-  ENSURE(c->rec32, 16 * (size_t)m.V);
+  ENSURE(c->rec32, 32 * (size_t)m.V);
   ENSURE(c->tetd, 16 * (size_t)m.T);
   ENSURE(c->tnext, sizeof(int));
   if (!c->edone.p) {
@@ -1557,7 +1557,7 @@ static int pass_fast(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_
   // [4] unresolved guard edges (0, 3 per mesh; 1, 4 per pass)
   ExpandList xl{P<int>(c->fitems), P<int>(c->fcnt) + 3, m.V};
   float4* vrec = P<float4>(c->vrec);
-  uint4* rec32 = P<uint4>(c->rec32);
+  float4* rec32 = P<float4>(c->rec32);
   if ((rc = fast_setup(c, xl))) return rc;
   // the FP64 fits of the listed patches depend on the field only: once their
   // patches are cached they run on the side stream, beside the FP32 phases

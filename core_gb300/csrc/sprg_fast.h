@@ -26,8 +26,9 @@ void fast_tet(const DevMesh& m, const float4* vrec, const double* u, float gscal
 // the guard), listed patches
 void fast_weights(const DevMesh& m, const double* cent, float* w, double* w64, ExpandList xl, int* n_refit,
                   unsigned char* listed, cudaStream_t s);
-// recovered value per vertex as value + packed remainder (16 bytes)
-void fast_merge_ref(ExpandList xl, const double* rec64, uint4* rec32, cudaStream_t s);
+// recovered value per vertex as a 32-byte record {s0, s1, s2, r0}, {r1, r2,
+// 0, 0}: the FP32 value and its FP32 remainder (listed vertices: from rec64)
+void fast_merge_ref(ExpandList xl, const double* rec64, float4* rec32, cudaStream_t s);
 // patch-size class per vertex: 0 (<= 8 elements), 1 (<= 16), 2 (<= 32), 3, 4 = listed
 void fast_patch_class(const DevMesh& m, const unsigned char* listed, unsigned char* cls, cudaStream_t s);
 // the bins' vertex order on the device: per-block class counts (4 ints per
@@ -38,13 +39,13 @@ void fast_bin_count(int V, const unsigned char* cls, int* counts, cudaStream_t s
 void fast_bin_scatter(int V, const unsigned char* cls, const int* offs, int* order, cudaStream_t s);
 // binned recover: tiles (first, count, lanes in {1, 2, 4}, bin) over verts, taken
 // from a counter by a persistent grid; every tiling gives the same bits
-void fast_recover_tiles(const DevMesh& m, const float* w, const uint4* td, uint4* rec, const int* verts,
+void fast_recover_tiles(const DevMesh& m, const float* w, const uint4* td, float4* rec, const int* verts,
                         const int4* tiles, int n_tiles, int* next, int grid, cudaStream_t s);
 // q: (h_max err^(-1/5), its relative error bound) per tet
 // seg (batch): one element range per block, nb = number of segments
 // done (one unsigned, zero between passes) and out3: the last block also
 // computes the size factor (one mesh; pass null for a batch)
-void fast_error(const DevMesh& m, const uint4* td, const float2* geo, const uint4* rec, float2* q, double* partials,
+void fast_error(const DevMesh& m, const uint4* td, const float2* geo, const float4* rec, float2* q, double* partials,
                 int nb, const int2* seg, unsigned* done, double adapt_ratio, double* out3, cudaStream_t s);
 // sz2: (size, its relative error bound) per vertex
 void fast_average(const DevMesh& m, const float2* q, const double* out3, float2* sz2, BatchView bv, cudaStream_t s);

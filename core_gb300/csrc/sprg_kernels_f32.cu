@@ -179,6 +179,16 @@ __device__ __forceinline__ Grad unpack_grad(uint4 a) {
   return g;
 }
 
+// a recovered value's 32-byte record {s0, s1, s2, r0}, {r1, r2, -, -}: the
+// value and its exact FP32 remainder (gmax unused for these)
+__device__ __forceinline__ Grad rec_grad(const float4& h, const float4& l) {
+  Grad g;
+  g.s[0] = h.x; g.s[1] = h.y; g.s[2] = h.z;
+  g.r[0] = h.w; g.r[1] = l.x; g.r[2] = l.y;
+  g.gmax = 0.f;
+  return g;
+}
+
 // ---------------------------------------------------------------------------
 // coordinate records (once per mesh) and the field pair (once per pass).
 // The coordinates are mapped into [1, 2] (x' = (x - c) s + 1, s a power of
@@ -478,7 +488,8 @@ __global__ void __launch_bounds__(kBlock) k_fast_weights(DevMesh m, const double
 
 // ---------------------------------------------------------------------------
 // recover: eps*(v) = g_ref + sum_t w_vt ((s_t - g_ref) + r_t), stored as the
-// value + packed remainder pair.  Vertices are binned by patch size; one
+// value + FP32 remainder in a 32-byte record (the error kernel reads it with
+// one 256-bit load and no decoding).  Vertices are binned by patch size; one
 // persistent grid takes tiles (first, count, lanes, bin) from a counter and
 // gives a tile's vertices `lanes` lanes each.  Lane l sums the elements
 // k = l, l + L, ... of the patch into the class sums x_{k mod 4} (each in
@@ -488,7 +499,7 @@ __global__ void __launch_bounds__(kBlock) k_fast_weights(DevMesh m, const double
 // ---------------------------------------------------------------------------
 template <int L>
 __device__ __forceinline__ void recover_tile(const DevMesh& m, const float* __restrict__ w,
-                                             const uint4* __restrict__ td, uint4* __restrict__ rec,
+                                             const uint4* __restrict__ td, float4* __restrict__ rec,
                                              const int* __restrict__ verts, int first, int count) {
   constexpr int NX = 4 / L;
   const int gl = threadIdx.x % L, slot = threadIdx.x / L;
@@ -549,14 +560,14 @@ __device__ __forceinline__ void recover_tile(const DevMesh& m, const float* __re
       two_sum(gr0, tot[0], s0, r0);
       two_sum(gr1, tot[1], s1, r1);
       two_sum(gr2, tot[2], s2, r2);
-      rec[v] = make_uint4(__float_as_uint(s0), __float_as_uint(s1), __float_as_uint(s2),
-                          pack_corr(s0, s1, s2, r0, r1, r2));
+      rec[2 * (size_t)v] = make_float4(s0, s1, s2, r0);
+      rec[2 * (size_t)v + 1] = make_float4(r1, r2, 0.f, 0.f);
     }
   }
 }
 
 __global__ void __launch_bounds__(kBlock) k_fast_recover_tiles(DevMesh m, const float* __restrict__ w,
-                                                               const uint4* __restrict__ td, uint4* __restrict__ rec,
+                                                               const uint4* __restrict__ td, float4* __restrict__ rec,
                                                                const int* __restrict__ verts,
                                                                const int4* __restrict__ tiles, int n_tiles,
                                                                int* __restrict__ next) {
@@ -626,16 +637,16 @@ __global__ void __launch_bounds__(kBinBlock) k_bin_scatter(int V, const unsigned
   }
 }
 
-// listed vertices take the FP64 reference result, as value + packed remainder
+// listed vertices take the FP64 reference result, as value + remainder
 __global__ void k_merge_ref(const int* __restrict__ items, const int* __restrict__ count, int cap,
-                            const double* __restrict__ rec64, uint4* __restrict__ rec) {
+                            const double* __restrict__ rec64, float4* __restrict__ rec) {
   int n = min(*count, cap);
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     int v = items[i];
     double a = rec64[3 * (size_t)v], b = rec64[3 * (size_t)v + 1], c = rec64[3 * (size_t)v + 2];
     float ah = (float)a, bh = (float)b, ch = (float)c;
-    rec[v] = make_uint4(__float_as_uint(ah), __float_as_uint(bh), __float_as_uint(ch),
-                        pack_corr(ah, bh, ch, (float)(a - ah), (float)(b - bh), (float)(c - ch)));
+    rec[2 * (size_t)v] = make_float4(ah, bh, ch, (float)(a - ah));
+    rec[2 * (size_t)v + 1] = make_float4((float)(b - bh), (float)(c - ch), 0.f, 0.f);
   }
 }
 
@@ -673,7 +684,7 @@ __device__ __forceinline__ double warp_pair_total(PairSum p) {
 // kernel, the same function), then clears the counter for the next pass
 __global__ void __launch_bounds__(kBlock) k_fast_error(DevMesh m, const uint4* __restrict__ td,
                                                        const float2* __restrict__ geo,
-                                                       const uint4* __restrict__ rec, float2* __restrict__ q,
+                                                       const float4* __restrict__ rec, float2* __restrict__ q,
                                                        double* __restrict__ partials, const int2* __restrict__ seg,
                                                        unsigned* __restrict__ done, double adapt_ratio, int dim,
                                                        double* __restrict__ out3) {
@@ -706,9 +717,13 @@ __global__ void __launch_bounds__(kBlock) k_fast_error(DevMesh m, const uint4* _
         nta = __ldg(td + t + t_step);
         ngm = __ldg(geo + t + t_step);
       }
-      const uint4 R0 = __ldg(rec + tv.x), R1 = __ldg(rec + tv.y), R2 = __ldg(rec + tv.z), R3 = __ldg(rec + tv.w);
+      float4 H0, L0, H1, L1, H2, L2, H3, L3;
+      ld_record(rec + 2 * (size_t)tv.x, H0, L0);
+      ld_record(rec + 2 * (size_t)tv.y, H1, L1);
+      ld_record(rec + 2 * (size_t)tv.z, H2, L2);
+      ld_record(rec + 2 * (size_t)tv.w, H3, L3);
       Grad ga = unpack_grad(ta);
-      const Grad E0 = unpack_grad(R0), E1 = unpack_grad(R1), E2 = unpack_grad(R2), E3 = unpack_grad(R3);
+      const Grad E0 = rec_grad(H0, L0), E1 = rec_grad(H1, L1), E2 = rec_grad(H2, L2), E3 = rec_grad(H3, L3);
       // eps*(IP) = g + D with g = s of vertex 0, D = sum ((s_i - g) + r_i) / 4
       const float g0 = E0.s[0], g1 = E0.s[1], g2 = E0.s[2];
       float D0 = 0.25f * ((E0.r[0] + ((E1.s[0] - g0) + E1.r[0])) + (((E2.s[0] - g0) + E2.r[0]) + ((E3.s[0] - g0) + E3.r[0])));
@@ -1012,17 +1027,17 @@ void fast_bin_scatter(int V, const unsigned char* cls, const int* offs, int* ord
   if (V) k_bin_scatter<<<fast_bin_blocks(V), kBinBlock, 0, s>>>(V, cls, offs, order);
 }
 
-void fast_recover_tiles(const DevMesh& m, const float* w, const uint4* td, uint4* rec, const int* verts,
+void fast_recover_tiles(const DevMesh& m, const float* w, const uint4* td, float4* rec, const int* verts,
                         const int4* tiles, int n_tiles, int* next, int grid, cudaStream_t s) {
   cudaMemsetAsync(next, 0, sizeof(int), s);
   if (n_tiles) k_fast_recover_tiles<<<grid, kBlock, 0, s>>>(m, w, td, rec, verts, tiles, n_tiles, next);
 }
 
-void fast_merge_ref(ExpandList xl, const double* rec64, uint4* rec, cudaStream_t s) {
+void fast_merge_ref(ExpandList xl, const double* rec64, float4* rec, cudaStream_t s) {
   k_merge_ref<<<152, 256, 0, s>>>(xl.items, xl.count, xl.cap, rec64, rec);
 }
 
-void fast_error(const DevMesh& m, const uint4* td, const float2* geo, const uint4* rec, float2* q, double* partials,
+void fast_error(const DevMesh& m, const uint4* td, const float2* geo, const float4* rec, float2* q, double* partials,
                 int nb, const int2* seg, unsigned* done, double adapt_ratio, double* out3, cudaStream_t s) {
   if (nb) k_fast_error<<<nb, kBlock, 0, s>>>(m, td, geo, rec, q, partials, seg, done, adapt_ratio, m.dim, out3);
 }
