@@ -603,6 +603,9 @@ def gpu_arm(args):
                              "unit": "GB/s",
                              "frac": pass_bytes(V, T, E) / (ms_max / args.steps / 1e3) / 1e9 / hbm},
            "setup_s": dict({"mesh_build": round(t_mesh, 3), "flatten_upload": round(t_flatten, 3)}, **first)}
+    if args.precision == "fp32":
+        tr = ctx.tuning_report()
+        out["tuning"] = {k: tr[k] for k in ("bins", "lanes", "tile_verts", "blocks_per_sm") if k in tr}
     print(json.dumps(out), flush=True)
     ctx.close()
     if world > 1:
