@@ -698,7 +698,9 @@ def gpu_aniso2d(args):
     V, T, E = m.n_verts, m.n_elems, m.n_edges
     nw = (E + 31) // 32
 
-    def run_form(precision):
+    def run_form(precision, m=m, u=u, eps=eps, hmin=hmin, hmax=hmax):
+        T, E = m.n_elems, m.n_edges
+        nw = (E + 31) // 32
         with cg.Context(m, precision=precision) as c:
             st = torch.cuda.Stream(dev)
             torch.cuda.set_stream(st)
@@ -748,6 +750,25 @@ def gpu_aniso2d(args):
         forms["fp32"].update({"marks_identical": bool(np.array_equal(b32, b64)),
                               "quality_rel_err_max": float(rel.max()),
                               "quality_rel_err_median": float(np.median(rel))})
+    if not args.no_compare:
+        # the batched form: uneven squares with their own fields in one
+        # context (a disjoint union; the anisotropic pass has no reduction
+        # across vertices), both forms, marks compared
+        mb, ub, voff, eoff, doff, ns = workload.batch_squares(256, seed=5, lo=32, hi=512)
+        pb = workload.aniso2d_params(256)
+        bat = {"meshes": int(len(ns)), "vertices": int(mb.n_verts), "triangles": int(mb.n_elems),
+               "n_range": [int(ns.min()), int(ns.max())], "fields": "1-8 Gaussian bumps per mesh",
+               "eps_hmin_hmax": list(pb)}
+        bres = {}
+        for prec in ("fp64", "fp32"):
+            ms, steps, prof, guard, launches, res = run_form(prec, mb, ub, *pb)
+            bres[prec] = res
+            bat[prec] = {"ms_per_step": ms, "value": mb.n_verts / (ms / 1e3), "unit": UNIT,
+                         "gpu_launches_per_step": launches}
+            if prec == "fp32":
+                bat[prec]["guard_edges"] = guard
+        bat["marks_identical"] = bool(np.array_equal(bres["fp32"][0], bres["fp64"][0]))
+        forms["batched"] = bat
     f = forms[main_form]
     out = {"metric": METRIC, "value": f["value"], "unit": UNIT, "n_gpus": 1, "steps": f["steps"],
            "warmup": args.warmup, "ms_per_step": f["ms_per_step"], "higher_is_better": True, "scaling": "weak",

@@ -1352,10 +1352,39 @@ __device__ __forceinline__ double metric_size(double lam, double eps, double hmi
 
 // one vertex's metric from its Hessian row h (9 doubles): sizes hs, frame R
 // (directions as columns)
+// Power-of-two prescaling of a Hessian before its eigen-decomposition, from
+// the largest biased exponent E of its entries (integer operations): none
+// while the largest entry lies in [2^-400, 2^401) or an entry is not finite,
+// else by 2^-e with e = E - 1022 (the largest entry then in [1/2, 1); e =
+// -1022 when every entry is zero or subnormal).  Eigenvectors are scale-free
+// and eigenvalues scale exactly (they are scaled back by 2^e), so this only
+// changes Hessians whose products underflow or overflow: a field flat to
+// 1e-160, where hd^2 + b^2 underflowed and the direction came out 0 / 0, now
+// gets the direction the exact arithmetic would.
+__device__ __forceinline__ int dbexp(double x) { return (int)((__double_as_longlong(x) >> 52) & 0x7ff); }
+__device__ __forceinline__ int hessian_scale_exp(int E) {
+  if (E == 2047 || (E >= 623 && E <= 1423)) return 0;
+  return E == 0 ? -1022 : E - 1022;
+}
+// x 2^k, exact unless the result under- or overflows (two factors where 2^k
+// itself is outside the normal range)
+__device__ __forceinline__ double times_pow2(double x, int k) {
+  auto p2 = [](int j) { return __longlong_as_double((long long)(1023 + j) << 52); };  // -1022 <= j <= 1023
+  if (k >= -1022 && k <= 1023) return x * p2(k);
+  return x * p2(k / 2) * p2(k - k / 2);
+}
+
 __device__ void hessian_metric_vertex(int dim, const double* __restrict__ h, double eps, double hmin, double hmax,
                                       double hs[3], double R[3][3]) {
   if (dim == 2) {
-    const double a = h[0], b = 0.5 * (h[1] + h[3]), c = h[4];
+    const double b0 = 0.5 * (h[1] + h[3]);
+    const int es = hessian_scale_exp(max(max(dbexp(h[0]), dbexp(h[4])), dbexp(b0)));
+    double a = h[0], b = b0, c = h[4];
+    if (es) {
+      a = times_pow2(a, -es);
+      b = times_pow2(b, -es);
+      c = times_pow2(c, -es);
+    }
     const double mid = 0.5 * (a + c), hd = 0.5 * (a - c);
     const double d = sqrt(hd * hd + b * b);
     double l1 = mid + d, l2 = mid - d;
@@ -1388,14 +1417,24 @@ __device__ void hessian_metric_vertex(int dim, const double* __restrict__ h, dou
     R[0][0] = x; R[0][1] = -y; R[0][2] = 0;
     R[1][0] = y; R[1][1] = x;  R[1][2] = 0;
     R[2][0] = 0; R[2][1] = 0;  R[2][2] = 1;
-    hs[0] = metric_size(l1, eps, hmin, hmax);
-    hs[1] = metric_size(l2, eps, hmin, hmax);
+    hs[0] = metric_size(es ? times_pow2(l1, es) : l1, eps, hmin, hmax);
+    hs[1] = metric_size(es ? times_pow2(l2, es) : l2, eps, hmin, hmax);
     hs[2] = hmax;
   } else {
     double A[3][3], lam[3], Vm[3][3];
+    int E = 0;
     for (int i = 0; i < 3; ++i)
-      for (int j = 0; j < 3; ++j) A[i][j] = 0.5 * (h[3 * i + j] + h[3 * j + i]);
+      for (int j = 0; j < 3; ++j) {
+        A[i][j] = 0.5 * (h[3 * i + j] + h[3 * j + i]);
+        E = max(E, dbexp(A[i][j]));
+      }
+    const int es = hessian_scale_exp(E);
+    if (es)
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) A[i][j] = times_pow2(A[i][j], -es);
     sym_eigen3(A, lam, Vm);
+    if (es)
+      for (int i = 0; i < 3; ++i) lam[i] = times_pow2(lam[i], es);
     int o[3] = {0, 1, 2};
     for (int i = 0; i < 3; ++i)
       for (int j = i + 1; j < 3; ++j)
@@ -1887,7 +1926,16 @@ __global__ void __launch_bounds__(kBlock) k_metric_mixed2d(int V, const double* 
   const int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= V) return;
   const double* h = H + 9 * (size_t)v;
-  const double a = h[0], b = 0.5 * (h[1] + h[3]), c = h[4];
+  // the same power-of-two prescaling as hessian_metric_vertex, so every
+  // decision below sees that function's values
+  const double b0 = 0.5 * (h[1] + h[3]);
+  const int es = hessian_scale_exp(max(max(dbexp(h[0]), dbexp(h[4])), dbexp(b0)));
+  double a = h[0], b = b0, c = h[4];
+  if (es) {
+    a = times_pow2(a, -es);
+    b = times_pow2(b, -es);
+    c = times_pow2(c, -es);
+  }
   const double mid = 0.5 * (a + c), hd = 0.5 * (a - c);
   const double d = sqrt(hd * hd + b * b);
   double l1 = mid + d, l2 = mid - d;
@@ -1929,6 +1977,10 @@ __global__ void __launch_bounds__(kBlock) k_metric_mixed2d(int V, const double* 
     if (d_is_zero(l) || (((dbits(l) >> 52) & 0x7ff) == 0x7ff && (dbits(l) << 12) != 0)) return hmaxf;  // 0, NaN
     return fminf(fmaxf(sqrtf(epsf / fabsf(d_to_f32_scaled(l, 0))), hminf), hmaxf);
   };
+  if (es) {
+    l1 = times_pow2(l1, es);
+    l2 = times_pow2(l2, es);
+  }
   const float o[12] = {size_f32(l1), size_f32(l2), hmaxf, xf, -yf, 0.f, yf, xf, 0.f, 0.f, 0.f, 1.f};
   store_met(out + 12 * (size_t)v, o);
   float Q[3][3];

@@ -19,9 +19,32 @@ def _size(lam, eps, hmin, hmax):
     return np.where(a > 0, h, hmax)
 
 
+def _bexp(x):
+    return ((np.asarray(x, np.float64).view(np.int64) >> 52) & 0x7FF).astype(np.int64)
+
+
+def _scale_exp(E):
+    """The metric's power-of-two prescaling of a Hessian, from the largest
+    biased exponent E of its entries: none while the largest entry lies in
+    [2^-400, 2^401) or an entry is not finite, else 2^-(E - 1022) (2^1022
+    when every entry is zero or subnormal)."""
+    E = np.asarray(E)
+    keep = (E == 2047) | ((E >= 623) & (E <= 1423))
+    return np.where(keep, 0, np.where(E == 0, -1022, E - 1022))
+
+
+def _times_pow2(x, k):
+    """x 2^k (two factors where 2^k is outside the normal range)."""
+    k = np.asarray(k)
+    h = k // 2
+    return x * np.ldexp(1.0, h) * np.ldexp(1.0, k - h)
+
+
 def metric_2d(H, eps, hmin, hmax):
     H = np.asarray(H, np.float64).reshape(-1, 9)
-    a, b, c = H[:, 0], 0.5 * (H[:, 1] + H[:, 3]), H[:, 4]
+    b0 = 0.5 * (H[:, 1] + H[:, 3])
+    es = _scale_exp(np.maximum(np.maximum(_bexp(H[:, 0]), _bexp(H[:, 4])), _bexp(b0)))
+    a, b, c = _times_pow2(H[:, 0], -es), _times_pow2(b0, -es), _times_pow2(H[:, 4], -es)
     mid, hd = 0.5 * (a + c), 0.5 * (a - c)
     d = np.sqrt(hd * hd + b * b)
     l1, l2 = mid + d, mid - d
@@ -36,6 +59,7 @@ def metric_2d(H, eps, hmin, hmax):
     x, y = np.where(sw, -y, x), np.where(sw, x, y)
     neg = (x < 0) | ((x == 0) & (y < 0))
     x, y = np.where(neg, -x, x), np.where(neg, -y, y)
+    l1, l2 = _times_pow2(l1, es), _times_pow2(l2, es)
     V = H.shape[0]
     R = np.zeros((V, 3, 3))
     R[:, 0, 0], R[:, 0, 1] = x, -y
@@ -82,7 +106,9 @@ def metric_3d(H, eps, hmin, hmax):
     frames = np.empty((V, 3, 3))
     for v in range(V):
         A = 0.5 * (H[v] + H[v].T)
-        lam, Vm = _jacobi(A)
+        es = int(_scale_exp(_bexp(A).max()))
+        lam, Vm = _jacobi(_times_pow2(A, -es))
+        lam = _times_pow2(lam, es)
         order = [0, 1, 2]
         for i in range(3):
             for j in range(i + 1, 3):

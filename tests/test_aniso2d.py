@@ -36,6 +36,26 @@ def test_metric_restatement_3d_reconstructs():
     assert np.allclose(R @ np.diag([5.0, -2.0, 0.5]) @ R.T, A, atol=1e-12)
 
 
+def test_metric_restatement_tiny_and_huge_hessians():
+    """A Hessian scaled by a power of two has the same frames (the metric
+    prescales it by a power of two before the eigen-decomposition): even at
+    1e-160 scale, where the squares of its entries underflow, and at 1e+150."""
+    rng = np.random.Generator(np.random.PCG64(3))
+    H = np.zeros((50, 9))
+    H[:, [0, 1, 3, 4]] = rng.normal(size=(50, 4))
+    H[:, 3] = H[:, 1]
+    _, f = ao.metric_2d(H, 1.0, 1e-3, 1e3)
+    for k in (-560, -531, 498):
+        s, fk = ao.metric_2d(np.ldexp(H, k), 1.0, 1e-3, 1e3)
+        assert np.all(np.isfinite(fk)) and np.array_equal(fk, f)
+    A = rng.normal(size=(20, 3, 3))
+    A = (A + A.transpose(0, 2, 1)).reshape(20, 9)
+    s3, f3 = ao.metric_3d(A, 1.0, 1e-3, 1e3)
+    for k in (-560, 498):
+        sk, fk = ao.metric_3d(np.ldexp(A, k), 1.0, 1e-3, 1e3)
+        assert np.array_equal(fk, f3)
+
+
 def case(n=48):
     from core_gb300 import workload
     return workload.aniso2d(n)
@@ -189,6 +209,25 @@ def test_mixed_aniso_pass_matches_fp64(gpu_lib, dim):
     assert np.abs(q32 - q64).max() <= 1e-4 * np.abs(q64).max()
     assert np.median(np.abs(q32 - q64) / np.abs(q64)) <= 1e-6
     assert guard < 0.01 * m.n_edges
+
+
+@pytest.mark.gpu
+def test_metric_on_tiny_hessians_matches_restatement(gpu_lib):
+    """The device metric (FP64 function and the mixed pass's records) on
+    Hessians at 1e-160 and 1e-170 scale: finite frames, those of the
+    restatement (whose power-of-two prescaling it shares)."""
+    import core_gb300 as cg
+    m, u, (eps, hmin, hmax) = case(8)
+    rng = np.random.Generator(np.random.PCG64(5))
+    H = np.zeros((m.n_verts, 9))
+    H[:, [0, 1, 4]] = rng.normal(size=(m.n_verts, 3))
+    H[:, 3] = H[:, 1]
+    H = np.ldexp(H, np.where(np.arange(m.n_verts) % 2 == 0, -531, -565)[:, None])
+    with cg.Context(m) as c:
+        sizes, frames = c.hessian_metric(H, eps, hmin, hmax)
+    s_ref, f_ref = ao.metric_2d(H, eps, hmin, hmax)
+    assert np.all(np.isfinite(frames)) and np.array_equal(frames, f_ref)
+    assert np.array_equal(sizes, s_ref)
 
 
 @pytest.mark.gpu
