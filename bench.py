@@ -665,14 +665,27 @@ def gpu_batched(args):
         c.profile(False)
         tune = c.tuning_report()
         c.set_stream(0)
-        _, _, _, _, info = c.estimate_and_mark(u, 1.0)
+        _, flags, _, _, info = c.estimate_and_mark(u, 1.0)
+    # marks of a sample of the meshes (every 32nd) against each mesh's own
+    # FP64 pass (the FP64 path equals the reference's marks)
+    from core_gb300.mesh import Mesh
+    sample = list(range(0, len(ns), 32))
+    differ = 0
+    for k in sample:
+        mk = Mesh(3, m.coords[voff[k]:voff[k + 1]], m.elem_verts[eoff[k]:eoff[k + 1]] - voff[k],
+                  m.edge_verts[doff[k]:doff[k + 1]] - voff[k])
+        with cg.Context(mk, precision="fp64") as c64:
+            _, f64, *_ = c64.estimate_and_mark(u[voff[k]:voff[k + 1]], 0.1)
+        differ += int(np.sum(f64 != flags[doff[k]:doff[k + 1]]))
+    marks = {"meshes_checked": len(sample), "edges_checked": int(sum(doff[k + 1] - doff[k] for k in sample)),
+             "differing_flag_words": differ, "against": "each mesh's own FP64 pass"}
     out = {"metric": METRIC, "value": V / (ms / 1e3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
            "config": {"workload": f"4096 unit tet boxes, n per side log-uniform in [4, 40] (seed 3), 1-8 Gaussian "
                                   f"bumps each; {V} vertices, {T} tets, {E} edges; adapt ratio 0.1 per mesh",
                       "form": "plain FP32, batched, CUDA graph", "l2": "inputs larger than L2"},
-           "tuning": tune, "guard_edges": int(info["n_guard_edges"]),
+           "tuning": tune, "guard_edges": int(info["n_guard_edges"]), "marks": marks,
            "listed_patches": int(info["n_expanded"] + info["n_fp64_refits"]), "clocks": clk,
            "timed_by": "CUDA graph replay", "ms_per_step_profiled_direct": ms_direct,
            "phases": {k: {"launches": n, "total_ms": t, "avg_ms": t / max(n, 1)} for k, (n, t) in prof.items()},

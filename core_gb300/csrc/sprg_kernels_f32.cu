@@ -926,6 +926,19 @@ __global__ void __launch_bounds__(kBlock) k_fast_measure(DevMesh m, const float*
         // finite ends: L moves by at most guard_rel + b_a + b_b relative
         const float band = guard_rel + A[i].y + B[i].y;
         near = fabsf(L - 1.5f) <= band * 1.5f || fabsf(L - 0.5f) <= band * 0.5f;
+        if (near && L < 0.5f) {
+          // a short edge stays a collapse unless the upper end of its length,
+          // from the ends' size lower bounds, reaches 0.5.  An element's
+          // bound b is 0.4 times its deviation's relative error, so q is at
+          // least q (1 + 2.5 b)^(-2/5), and by convexity (Jensen) a vertex
+          // size at least size (1 + 2.5 b_v)^(-2/5) with b_v its q-weighted
+          // mean bound: far tighter than the linear band where flat fields
+          // make b large (margin 1e-6 for this arithmetic and the size factor)
+          const float alo = A[i].x * (powf(1.f + 2.5f * A[i].y, -0.4f) * (1.f - 1e-6f));
+          const float blo = B[i].x * (powf(1.f + 2.5f * B[i].y, -0.4f) * (1.f - 1e-6f));
+          const float Lhi = hl[i] * (1.f / (n0 * alo + n1 * blo) + 1.f / (n1 * alo + n0 * blo)) * (1.f + guard_rel);
+          near = !(Lhi < 0.5f);
+        }
       } else {
         // an infinite end: the upper end of L from the sizes' lower bounds
         const float alo = A[i].y >= 0.f ? A[i].x * fmaxf(1.f - A[i].y, 0.f) : -A[i].y;
