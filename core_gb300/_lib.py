@@ -58,6 +58,7 @@ EXPORTS = [
     "sprg_max_iterations_for_length", "sprg_mark_bad_quality", "sprg_get_min_quality",
     "sprg_measure_edges_log_aniso", "sprg_measure_quality_log_aniso", "sprg_update_mesh",
     "sprg_smb_counts", "sprg_smb_read", "sprg_smb_write", "sprg_e2e_timing", "sprg_e2e_timing_report", "sprg_test_hooks",
+    "sprg_rounding_dominated",
     "sprg_locality_order",
 ]
 NOALLOC_MAX_ELEMS = 1 << 20
@@ -113,6 +114,7 @@ class SizeInfo(ctypes.Structure):
         ("n_guard_edges", ctypes.c_int64),
         ("n_guard_unresolved", ctypes.c_int64),
         ("n_learned_fallback", ctypes.c_int64),
+        ("n_rounding_dominated", ctypes.c_int64),
     ]
 
     def as_dict(self):
@@ -152,6 +154,7 @@ def load():
     lib.sprg_estimate_and_mark.argtypes = [P, P, D, P, P, ctypes.POINTER(ctypes.c_long),
                                            ctypes.POINTER(ctypes.c_long), ctypes.POINTER(SizeInfo)]
     lib.sprg_estimate_and_mark_resident.argtypes = [P, P, D, P, P]
+    lib.sprg_rounding_dominated.argtypes = [P, ctypes.POINTER(ctypes.c_int)]
     lib.sprg_apply_marks.argtypes = [ctypes.c_int64, P, P, P, ctypes.POINTER(ctypes.c_long),
                                      ctypes.POINTER(ctypes.c_long)]
     F = ctypes.c_float

@@ -400,6 +400,14 @@ class Context:
                                                               ctypes.c_void_p(d_split_bits),
                                                               ctypes.c_void_p(d_collapse_bits)))
 
+    def rounding_dominated(self):
+        """After an FP32 resident pass on one mesh: True when the reference's
+        own FP64 rounding would decide its sizes (rerun under FP64 for its
+        marks)."""
+        v = ctypes.c_int(0)
+        self._check(self._lib.sprg_rounding_dominated(self.h, ctypes.byref(v)))
+        return bool(v.value)
+
 
 class SizeField:
     """ma::SizeField over a context (IsoUserField, AnisoSizeField or LogAnisoSizeField)."""

@@ -83,6 +83,7 @@ struct sprg_ctx {
   static constexpr int kSegTets = 2048;  // elements per error segment (8 per thread)
   // binned recover: patch-size bins, tiles, tuned configuration
   DevBuf pcls, bverts, btiles, bnext, bcnt, cent;
+  DevBuf qmax;  // the mesh's largest |cof J|^2 / |det J| (FP64 bits)
   bool bins_ready = false, tuned = false, autotune = true;
   int bin_count[4] = {0, 0, 0, 0};
   int bin_lanes[4] = {4, 4, 4, 4};
@@ -489,6 +490,7 @@ int info_from_stage(sprg_ctx* c, sprg_size_info* info) {
   c->last_info.n_guard_edges = 0;
   c->last_info.n_guard_unresolved = 0;
   c->last_info.n_learned_fallback = 0;
+  c->last_info.n_rounding_dominated = 0;
   if (c->precision == SPRG_LEARNED && c->fbcount.p) {
     if (h->me) return fail(c, SPRG_ECUDA, "learned form: a tensor-core wait ran out of time");
     c->last_info.n_learned_fallback = h->fb;
@@ -499,6 +501,7 @@ int info_from_stage(sprg_ctx* c, sprg_size_info* info) {
     c->last_info.n_fp64_refits = c->n_refit;
     c->last_info.n_guard_edges = h->fc[1];
     c->last_info.n_guard_unresolved = h->fc[4];
+    c->last_info.n_rounding_dominated = c->batch_n ? 0 : h->fc[5];
     c->last_info.n_expanded = c->n_listed - c->n_refit;
   }
   if (info) *info = c->last_info;
@@ -851,7 +854,7 @@ int sprg_destroy(sprg_ctx* c) {
   if (!c) return SPRG_OK;
   cudaSetDevice(c->device);
   if (c->own) cudaStreamSynchronize(c->own);
-  DevBuf* bufs[] = {&c->bcnt, &c->cent, &c->xyz,   &c->xyzq,   &c->ev,   &c->edv,   &c->poff,    &c->pel,    &c->aoff,
+  DevBuf* bufs[] = {&c->qmax, &c->bcnt, &c->cent, &c->xyz,   &c->xyzq,   &c->ev,   &c->edv,   &c->poff,    &c->pel,    &c->aoff,
                     &c->ael,   &c->tmp,     &c->f,    &c->ip,    &c->rec,     &c->err,    &c->esize,
                     &c->size,  &c->L,       &c->flags, &c->q,    &c->sizes3,  &c->frames9, &c->partials,
                     &c->out3,  &c->status,  &c->count, &c->mcount, &c->xitems, &c->xcount, &c->slab, &c->bits, &c->titems, &c->tcountb, &c->Lx, &c->pairs, &c->red, &c->eflags, &c->logm, &c->qw, &c->qwlisted, &c->qwitems, &c->qwcount, &c->tw, &c->twlisted, &c->twitems, &c->twcount, &c->met32, &c->qrec32, &c->cj64, &c->qties, &c->kidx, &c->kval, &c->klen, &c->rec9, &c->cache2d.v, &c->cache2d.n, &c->cache2d.el, &c->agitems, &c->agcount,
@@ -1318,6 +1321,7 @@ static int fast_setup(sprg_ctx* c, ExpandList xl) {
   ENSURE(c->geo, 8 * (size_t)m.T);
   ENSURE(c->geo64, 16 * (size_t)m.T);
   ENSURE(c->cent, 24 * (size_t)m.T);
+  ENSURE(c->qmax, sizeof(unsigned long long));
   ENSURE(c->elen, 4 * (size_t)m.E);
   CK(cudaMemsetAsync(c->fcnt.p, 0, 8 * sizeof(int), c->stream));
   PB("setup_coords");
@@ -1325,7 +1329,8 @@ static int fast_setup(sprg_ctx* c, ExpandList xl) {
   PE();
   c->crec_ready = true;
   PB("setup_geometry");
-  fast_geometry(m, P<float2>(c->geo), P<double2>(c->geo64), P<double>(c->cent), P<float>(c->elen), c->stream);
+  fast_geometry(m, P<float2>(c->geo), P<double2>(c->geo64), P<double>(c->cent), P<unsigned long long>(c->qmax),
+                P<float>(c->elen), c->stream);
   PE();
   PB("setup_weights");
   fast_weights(m, P<double>(c->cent), P<float>(c->wts), P<double>(c->w64), xl, P<int>(c->fcnt),
@@ -1554,7 +1559,9 @@ static int pass_fast(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_
   ENSURE(c->out3, sizeof(double) * 4 * (size_t)(bv.n > 0 ? bv.n : 1));
   if ((rc = reset_status(c))) return rc;
   // fcnt: [0] refit patches, [1] guard edges, [3] listed patches,
-  // [4] unresolved guard edges (0, 3 per mesh; 1, 4 per pass)
+  // [4] unresolved guard edges, [5] rounding dominance (the largest
+  // element share of the reference's rounding, then 0 / 1 from the error
+  // kernel's last block) (0, 3 per mesh; 1, 4, 5 per pass)
   ExpandList xl{P<int>(c->fitems), P<int>(c->fcnt) + 3, m.V};
   float4* vrec = P<float4>(c->vrec);
   float4* rec32 = P<float4>(c->rec32);
@@ -1564,9 +1571,9 @@ static int pass_fast(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_
   bool fork = false;
   if ((rc = listed_fork(c, xl, &fork))) return rc;
   CK(cudaMemsetAsync(P<int>(c->fcnt) + 1, 0, sizeof(int), c->stream));
-  CK(cudaMemsetAsync(P<int>(c->fcnt) + 4, 0, sizeof(int), c->stream));
+  CK(cudaMemsetAsync(P<int>(c->fcnt) + 4, 0, 2 * sizeof(int), c->stream));
   PB("prep_f32");
-  fast_prep(m, P<double>(c->f), P<float4>(c->crec), vrec, c->stream);
+  fast_prep(m, P<double>(c->f), P<float4>(c->crec), vrec, P<int>(c->fcnt) + 5, c->stream);
   PE();
   PB("tet_f32");
   fast_tet(m, vrec, P<double>(c->f), (float)c->frame[3], P<uint4>(c->tetd), P<int>(c->tnext), c->stream);
@@ -1589,7 +1596,7 @@ static int pass_fast(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_
   PB("error_f32");
   fast_error(m, P<uint4>(c->tetd), P<float2>(c->geo), rec32, P<float2>(c->q32), P<double>(c->partials), nb,
              bv.n ? P<int2>(c->bseg) : nullptr, bv.n ? nullptr : P<unsigned>(c->edone), adapt_ratio,
-             P<double>(c->out3), c->stream);
+             P<double>(c->out3), P<int>(c->fcnt) + 5, P<unsigned long long>(c->qmax), c->stream);
   PE();
   if (bv.n) {
     PB("size_factor");
@@ -1762,6 +1769,19 @@ int sprg_estimate_and_mark_resident(sprg_ctx* c, const double* d_u, double adapt
   return pass_resident(c, adapt_ratio, d_split_bits, d_collapse_bits);
 }
 
+int sprg_rounding_dominated(sprg_ctx* c, int* out) {
+  if (!c || !out) return SPRG_EINVAL;
+  *out = 0;
+  if (c->precision != SPRG_FP32 || c->batch_n || !c->fcnt.p) return SPRG_OK;
+  int rc = set_device(c);
+  if (rc) return rc;
+  int v = 0;
+  CK(cudaMemcpyAsync(&v, P<int>(c->fcnt) + 5, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  *out = v ? 1 : 0;
+  return SPRG_OK;
+}
+
 // the resident pass of the host entry point: direct launches for the first
 // two calls with a key, a captured graph from the third on
 static int e2e_pass(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_t* d_collapse) {
@@ -1876,7 +1896,10 @@ int sprg_estimate_and_mark(sprg_ctx* c, const double* u, double adapt_ratio, dou
   CK(mark(3, c->stream));
   PB("apply_marks");
   CK(cudaMemsetAsync(c->mcount.p, 0, 2 * sizeof(unsigned long long), c->stream));
-  launch_apply_marks(m.E, sb, sb + nw, P<int>(c->flags), P<unsigned long long>(c->mcount), P<DevStatus>(c->status),
+  // FP32 on one mesh: a rounding-dominated pass leaves the flags unchanged,
+  // and runs again in FP64 below
+  const int* skip = c->precision == SPRG_FP32 && !c->batch_n ? P<int>(c->fcnt) + 5 : nullptr;
+  launch_apply_marks(m.E, sb, sb + nw, P<int>(c->flags), P<unsigned long long>(c->mcount), P<DevStatus>(c->status), skip,
                      c->stream);
   PE();
   c->launches += 1;
@@ -1928,7 +1951,19 @@ int sprg_estimate_and_mark(sprg_ctx* c, const double* u, double adapt_ratio, dou
   }
   if (n_split) *n_split = (long)c->stage->counts[0];
   if (n_collapse) *n_collapse = (long)c->stage->counts[1];
-  return info_from_stage(c, info);
+  rc = info_from_stage(c, info);
+  if (rc || c->precision != SPRG_FP32 || c->batch_n || c->last_info.n_rounding_dominated == 0) return rc;
+  // Rounding-dominated pass: the reference's size factor, and with it its
+  // sizes, follow its own FP64 rounding, which the FP32 arithmetic (and its
+  // error bounds) does not model.  The flags came back unchanged; the FP64
+  // pass (the reference's operation order) decides them.
+  const int64_t nr = c->last_info.n_rounding_dominated;
+  c->precision = SPRG_FP64;
+  rc = sprg_estimate_and_mark(c, u, adapt_ratio, size_out, flags, n_split, n_collapse, info);
+  c->precision = SPRG_FP32;
+  c->last_info.n_rounding_dominated = nr;
+  if (info) info->n_rounding_dominated = nr;
+  return rc;
 }
 
 int sprg_debug_read(sprg_ctx* c, const char* name, void* host, size_t bytes) {

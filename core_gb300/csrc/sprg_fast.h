@@ -12,10 +12,13 @@ void fast_prep_coords(const DevMesh& m, const double* frame, float4* vrec, cudaS
 // once per mesh: per tet {w dV, h_max} (FP32) and {det J, h_max} (FP64), per
 // edge half its length
 // cent: 3 doubles per element, the integration point (once per mesh, read by
-// fast_weights)
-void fast_geometry(const DevMesh& m, float2* geo, double2* geo64, double* cent, float* half_len, cudaStream_t s);
-// the pass's vertex records: coordinate records with the field pair (u_hi, u_lo)
-void fast_prep(const DevMesh& m, const double* u, const float4* crec, float4* vrec, cudaStream_t s);
+// fast_weights); qmax: one double (as its bits, set here), the largest
+// |cof J|_F^2 / |det J| over the elements
+void fast_geometry(const DevMesh& m, float2* geo, double2* geo64, double* cent, unsigned long long* qmax,
+                   float* half_len, cudaStream_t s);
+// the pass's vertex records: coordinate records with the field pair (u_hi,
+// u_lo); umax_bits (zeroed by the caller): max |u_hi| as float bits
+void fast_prep(const DevMesh& m, const double* u, const float4* crec, float4* vrec, int* umax_bits, cudaStream_t s);
 // per tet: gradient value (3 floats) and packed correction (1 word)
 // gscale = the frame's s (gradients in the mesh's coordinates); u: the FP64
 // field, read for the ill-conditioned tets solved in FP64
@@ -44,9 +47,13 @@ void fast_recover_tiles(const DevMesh& m, const float* w, const uint4* td, float
 // q: (h_max err^(-1/5), its relative error bound) per tet
 // seg (batch): one element range per block, nb = number of segments
 // done (one unsigned, zero between passes) and out3: the last block also
-// computes the size factor (one mesh; pass null for a batch)
+// computes the size factor (one mesh; pass null for a batch); n_round (max
+// |u| from fast_prep) is replaced by the last block with 1 when the
+// reference's FP64 rounding of its IP gradients (bounded with qmax from
+// fast_geometry) could move the error integral by 1e-7 of it, else 0
 void fast_error(const DevMesh& m, const uint4* td, const float2* geo, const float4* rec, float2* q, double* partials,
-                int nb, const int2* seg, unsigned* done, double adapt_ratio, double* out3, cudaStream_t s);
+                int nb, const int2* seg, unsigned* done, double adapt_ratio, double* out3, int* n_round,
+                const unsigned long long* qmax, cudaStream_t s);
 // sz2: (size, its relative error bound) per vertex
 void fast_average(const DevMesh& m, const float2* q, const double* out3, float2* sz2, BatchView bv, cudaStream_t s);
 void fast_measure(const DevMesh& m, const float* half_len, const float2* sz2, uint32_t* split, uint32_t* collapse,

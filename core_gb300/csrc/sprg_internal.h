@@ -123,8 +123,9 @@ void launch_mark_bits(int E, const double* L, uint32_t* split, uint32_t* collaps
 void launch_apply_bits(int E, const uint32_t* bits, int which, int* flags, unsigned long long* count,
                        DevStatus* st, cudaStream_t s);
 // the collapse and split passes in one sweep (counts[0] split, counts[1] collapse)
+// skip (device int, or null): when nonzero the flags stay unchanged
 void launch_apply_marks(int E, const uint32_t* split_bits, const uint32_t* collapse_bits, int* flags,
-                        unsigned long long* counts, DevStatus* st, cudaStream_t s);
+                        unsigned long long* counts, DevStatus* st, const int* skip, cudaStream_t s);
 // MA sweeps around the marks.  kind: 0 identity size field, 1 isotropic
 // (size), 2 anisotropic (sizes, frames), 3 log-interpolated anisotropic
 // (logm); pairs: n x 2 vertex ids, or NULL for the mesh's edges (n = E);

@@ -1017,7 +1017,8 @@ __device__ __forceinline__ int apply_marks_edge(int f, uint32_t split_bit, uint3
 __global__ void __launch_bounds__(kBlock) k_apply_marks(int E, const uint32_t* __restrict__ split_bits,
                                                         const uint32_t* __restrict__ collapse_bits,
                                                         int* __restrict__ flags, unsigned long long* counts,
-                                                        DevStatus* st) {
+                                                        DevStatus* st, const int* __restrict__ skip) {
+  if (skip && *skip) return;  // the caller runs the pass again in FP64
   unsigned ms = 0, mc = 0;
   const int n4 = E >> 2, step = gridDim.x * blockDim.x;
   int4* __restrict__ f4 = reinterpret_cast<int4*>(flags);
@@ -2637,8 +2638,9 @@ void launch_apply_bits(int E, const uint32_t* bits, int which, int* flags, unsig
 }
 
 void launch_apply_marks(int E, const uint32_t* split_bits, const uint32_t* collapse_bits, int* flags,
-                        unsigned long long* counts, DevStatus* st, cudaStream_t s) {
-  if (E) k_apply_marks<<<count_grid((E + 3) / 4), kBlock, 0, s>>>(E, split_bits, collapse_bits, flags, counts, st);
+                        unsigned long long* counts, DevStatus* st, const int* skip, cudaStream_t s) {
+  if (E)
+    k_apply_marks<<<count_grid((E + 3) / 4), kBlock, 0, s>>>(E, split_bits, collapse_bits, flags, counts, st, skip);
 }
 
 void launch_quality_f64(const DevMesh& m, const double* size, const double* sizes, const double* frames, double* q,

@@ -92,6 +92,13 @@ typedef struct sprg_size_info {
   int64_t n_guard_edges;   /* FP32 mode: edges within 2e-6 of 0.5 / 1.5, re-decided in FP64 */
   int64_t n_guard_unresolved; /* FP32 mode: guard edges left to the FP32 decision (patch growth needed) */
   int64_t n_learned_fallback; /* learned mode: vertices recovered by plain SPR instead of the network */
+  int64_t n_rounding_dominated; /* FP32 mode, one mesh: 1 when the reference's own FP64 rounding of the IP
+                                   gradients (about 2^-50 max|u| |J^-1| per element, times 256) could move
+                                   its error integral by 1e-7 or more, or that integral is zero or not
+                                   finite (a constant field, one offset far above its variation, NaN):
+                                   the reference's sizes are then its rounding's, and
+                                   sprg_estimate_and_mark runs the pass again in FP64 (the reference's
+                                   operation order); the resident entry points leave that to the caller */
 } sprg_size_info;
 
 /* ---- context: flatten + upload (the MDS-to-device flattener) ---------- */
@@ -300,6 +307,13 @@ int sprg_estimate_and_mark(sprg_ctx* ctx, const double* u, double adapt_ratio, d
    bitmaps into "ma_flags" words with markEntities semantics. */
 int sprg_estimate_and_mark_resident(sprg_ctx* ctx, const double* d_u, double adapt_ratio, uint32_t* d_split_bits,
                                     uint32_t* d_collapse_bits);
+/* After an SPRG_FP32 resident pass on one mesh (waits for the context
+   stream): *out = 1 when that pass was rounding-dominated (the
+   n_rounding_dominated of sprg_size_info), so its bitmaps follow the FP32
+   arithmetic rather than the reference's rounding; the caller reruns the
+   pass under SPRG_FP64 for the reference's marks.  0 otherwise, and for any
+   other precision or a batch. */
+int sprg_rounding_dominated(sprg_ctx* ctx, int* out);
 /* The anisotropic pass on device buffers (FP64, any precision setting):
    getGradIPField(u) -> recoverField -> getGradIPField of the recovered
    gradient -> recoverField (nodal Hessian) -> sprg_hessian_metric ->

@@ -104,7 +104,7 @@ CTX_CALLS = [
     "sprg_graph_capture", "sprg_graph_replay", "sprg_set_tiling", "sprg_measure_vertex_pairs",
     "sprg_get_maximum_edge_length", "sprg_get_average_edge_length", "sprg_mark_bad_quality",
     "sprg_get_min_quality", "sprg_measure_edges_log_aniso", "sprg_measure_quality_log_aniso",
-    "sprg_update_mesh", "sprg_e2e_timing", "sprg_test_hooks",
+    "sprg_update_mesh", "sprg_e2e_timing", "sprg_test_hooks", "sprg_rounding_dominated",
 ]
 
 

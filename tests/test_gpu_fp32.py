@@ -57,9 +57,46 @@ def test_fp32_against_oracle(gpu_lib, oracle_lib, n, seed):
         bound = ctx.debug_read("sz2", np.float32, 2 * m.n_verts)[1::2].astype(np.float64)
     check_sizes(size, size_o, bound)
     assert abs(info["size_factor"] - info_o["size_factor"]) <= 1e-7 * info_o["size_factor"]
-    assert info["n_guard_unresolved"] == 0
+    assert info["n_guard_unresolved"] == 0 and info["n_rounding_dominated"] == 0
     assert np.array_equal(flags, flags_o)
     assert (ns, nc) == (ns_o, nc_o)
+
+
+@pytest.mark.parametrize("kind", ["constant", "offset", "zero"])
+def test_rounding_dominated_fields_take_the_fp64_pass(gpu_lib, oracle_lib, kind):
+    """Fields whose error integral is set by the reference's own FP64
+    rounding (a constant field, whose IP gradients sum u_i grad N_i are
+    rounding; a bump 1e15 times below its offset) or is zero: the FP32 host
+    entry point finds the pass rounding-dominated, leaves the flags alone
+    and runs the pass in FP64, so the marks are the reference's (the
+    oracle's) all the same.  (An exactly linear field is rounding too, but
+    there no summation order other than the reference's reproduces its
+    marks, the FP64 recovery included.)"""
+    import core_gb300 as cg
+    from core_gb300 import workload
+    n = 12
+    m, u0, o = pair(oracle_lib, n, 3)
+    u = {"constant": np.full(m.n_verts, 2.5), "offset": 1e6 + 1e-9 * u0, "zero": np.zeros(m.n_verts)}[kind]
+    rc, size_o, L_o, flags_o, ns_o, nc_o, info_o = o.estimate_and_mark(u, 0.1)
+    assert rc == 0
+    prior = np.zeros(m.n_edges, np.int32)
+    prior[::7] = 2  # DONT_SPLIT on some edges: kept through the rerun
+    import torch
+    with cg.Context(m, precision="fp32") as c:
+        size, flags, ns, nc, info = c.estimate_and_mark(u, 0.1, flags=prior.copy())
+        # the resident entry leaves the rerun to its caller, who can ask
+        nw = (m.n_edges + 31) // 32
+        d_u = torch.from_numpy(u).cuda()
+        bits = torch.zeros(2 * nw, dtype=torch.int32, device="cuda")
+        torch.cuda.synchronize()
+        c.estimate_and_mark_resident(d_u.data_ptr(), 0.1, bits.data_ptr(), bits.data_ptr() + 4 * nw)
+        assert c.rounding_dominated()
+    assert info["n_rounding_dominated"] == 1
+    want = prior.copy()
+    rc, _ = oracle_lib.mark_edges(L_o, 1, want)
+    rc2, _ = oracle_lib.mark_edges(L_o, 0, want)
+    assert rc == 0 and rc2 == 0
+    assert np.array_equal(flags, want)
 
 
 def test_fp32_matches_fp64_marks_and_is_deterministic(gpu_lib):
@@ -89,6 +126,8 @@ def test_fp32_matches_fp64_marks_and_is_deterministic(gpu_lib):
             outs.append(bits.cpu().numpy().copy())
         sz2 = c32.debug_read("sz2", np.float32, 2 * m.n_verts)
         s32b, bound = sz2[0::2], sz2[1::2].astype(np.float64)
+        assert not c32.rounding_dominated()
+    assert info["n_rounding_dominated"] == 0
     assert np.array_equal(outs[0], outs[1])
     assert np.array_equal(f32, f64)
     check_sizes(s32, s64, bound)
