@@ -349,6 +349,9 @@ class Context:
         self._check(self._lib.sprg_set_autotune(self.h, 1 if on else 0))
 
     def set_tiling(self, lanes, tile_verts=256, blocks_per_sm=8):
+        """Fix the binned recovery's shape: lanes per vertex for each of the
+        four patch-size bins (1, 2, 4, or 0 for the sliced patch lists, which
+        needs tile_verts a multiple of 32)."""
         l = np.ascontiguousarray(lanes, np.int32)
         self._check(self._lib.sprg_set_tiling(self.h, l.ctypes.data, int(tile_verts), int(blocks_per_sm)))
 

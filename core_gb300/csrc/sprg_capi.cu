@@ -84,10 +84,14 @@ struct sprg_ctx {
   // binned recover: patch-size bins, tiles, tuned configuration
   DevBuf pcls, bverts, btiles, bnext, bcnt, cent;
   DevBuf qmax;  // the mesh's largest |cof J|^2 / |det J| (FP64 bits)
+  DevBuf soff, sel, sw;  // sliced copy of the patch lists (offsets, element ids, weights)
+  BinSlices bslices{};
+  bool sliced = false;  // the sliced copy is built (lanes 0 available)
   bool bins_ready = false, tuned = false, autotune = true;
   int bin_count[4] = {0, 0, 0, 0};
   int bin_lanes[4] = {4, 4, 4, 4};
   int tile_verts = 256, grid_per_sm = 8, n_tiles = 0, n_sms = 152;
+  int tile_mode = -1;  // the lane mode every tile shares, or -1
   std::string tune_json;
   // CUDA graph of the resident pass (sprg_graph_capture / sprg_graph_replay)
   cudaGraphExec_t graph_exec = nullptr;
@@ -854,7 +858,7 @@ int sprg_destroy(sprg_ctx* c) {
   if (!c) return SPRG_OK;
   cudaSetDevice(c->device);
   if (c->own) cudaStreamSynchronize(c->own);
-  DevBuf* bufs[] = {&c->qmax, &c->bcnt, &c->cent, &c->xyz,   &c->xyzq,   &c->ev,   &c->edv,   &c->poff,    &c->pel,    &c->aoff,
+  DevBuf* bufs[] = {&c->soff, &c->sel, &c->sw, &c->qmax, &c->bcnt, &c->cent, &c->xyz,   &c->xyzq,   &c->ev,   &c->edv,   &c->poff,    &c->pel,    &c->aoff,
                     &c->ael,   &c->tmp,     &c->f,    &c->ip,    &c->rec,     &c->err,    &c->esize,
                     &c->size,  &c->L,       &c->flags, &c->q,    &c->sizes3,  &c->frames9, &c->partials,
                     &c->out3,  &c->status,  &c->count, &c->mcount, &c->xitems, &c->xcount, &c->slab, &c->bits, &c->titems, &c->tcountb, &c->Lx, &c->pairs, &c->red, &c->eflags, &c->logm, &c->qw, &c->qwlisted, &c->qwitems, &c->qwcount, &c->tw, &c->twlisted, &c->twitems, &c->twcount, &c->met32, &c->qrec32, &c->cj64, &c->qties, &c->kidx, &c->kval, &c->klen, &c->rec9, &c->cache2d.v, &c->cache2d.n, &c->cache2d.el, &c->agitems, &c->agcount,
@@ -1302,6 +1306,10 @@ int sprg_get_min_quality(sprg_ctx* c, double* out) {
   return SPRG_OK;
 }
 
+static SlicedPatches sliced_view(sprg_ctx* c) {
+  return SlicedPatches{P<int>(c->soff), P<int>(c->sel), P<float>(c->sw)};
+}
+
 static BatchView batch_view(sprg_ctx* c) {
   if (!c->batch_n) return BatchView{0, nullptr, nullptr, nullptr, nullptr};
   return BatchView{c->batch_n, P<int>(c->bvoff), P<int2>(c->bseg), P<int>(c->bsegoff), P<double>(c->bratios)};
@@ -1379,6 +1387,47 @@ static int listed_join(sprg_ctx* c, ExpandList xl, bool forked) {
 
 // patch-size bins of the non-listed vertices (stable: ascending ids within a
 // bin), once per mesh
+// the sliced copy of the patch lists over the bins (after the bins and the
+// weights): widths on the device, their exclusive sums x 32 on the host
+static int build_slices(sprg_ctx* c) {
+  DevMesh& m = c->m;
+  BinSlices& bs = c->bslices;
+  int start = 0, slices = 0;
+  for (int b = 0; b < 4; ++b) {
+    bs.start[b] = start;
+    bs.slice0[b] = slices;
+    start += c->bin_count[b];
+    slices += (c->bin_count[b] + 31) / 32;
+  }
+  bs.start[4] = start;
+  bs.slice0[4] = slices;
+  c->sliced = false;
+  ENSURE(c->soff, sizeof(int) * ((size_t)slices + 1));
+  fast_slice_width(m, bs, P<int>(c->bverts), P<int>(c->soff), c->stream);
+  std::vector<int> off((size_t)slices + 1);
+  if (slices) CK(cudaMemcpyAsync(off.data(), c->soff.p, sizeof(int) * slices, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  long long run = 0;
+  for (int k = 0; k < slices; ++k) {
+    const long long wdt = off[k];
+    off[k] = (int)run;
+    run += 32 * wdt;
+    if (run > INT32_MAX) return SPRG_OK;  // too large for int offsets: the CSR lane modes only
+  }
+  off[slices] = (int)run;
+  CK(cudaMemcpyAsync(c->soff.p, off.data(), sizeof(int) * off.size(), cudaMemcpyHostToDevice, c->stream));
+  ENSURE(c->sel, sizeof(int) * (size_t)(run > 0 ? run : 1));
+  ENSURE(c->sw, sizeof(float) * (size_t)(run > 0 ? run : 1));
+  CK(cudaMemsetAsync(c->sel.p, 0, sizeof(int) * (size_t)(run > 0 ? run : 1), c->stream));
+  CK(cudaMemsetAsync(c->sw.p, 0, sizeof(float) * (size_t)(run > 0 ? run : 1), c->stream));
+  fast_slice_fill(m, bs, P<int>(c->bverts), P<float>(c->wts), sliced_view(c), c->stream);
+  CK(cudaStreamSynchronize(c->stream));  // off lives on this frame
+  int rc = check_launch(c, "sliced patch lists");
+  if (rc) return rc;
+  c->sliced = true;
+  return SPRG_OK;
+}
+
 static int build_bins(sprg_ctx* c) {
   if (c->bins_ready) return SPRG_OK;
   DevMesh& m = c->m;
@@ -1410,6 +1459,7 @@ static int build_bins(sprg_ctx* c) {
   fast_bin_scatter(m.V, P<unsigned char>(c->pcls), P<int>(c->bcnt) + 4 * (size_t)nb, P<int>(c->bverts), c->stream);
   CK(cudaStreamSynchronize(c->stream));  // offs lives on this frame
   if ((rc = check_launch(c, "patch-size bins"))) return rc;
+  if ((rc = build_slices(c))) return rc;
   int dev = 0;
   CK(cudaGetDevice(&dev));
   CK(cudaDeviceGetAttribute(&c->n_sms, cudaDevAttrMultiProcessorCount, dev));
@@ -1417,15 +1467,22 @@ static int build_bins(sprg_ctx* c) {
   return SPRG_OK;
 }
 
-// tiles (first, count, lanes, bin) of the current configuration; `only` >= 0
-// keeps one bin (autotuning)
+// tiles (first, count, lanes, slice of first) of the current configuration;
+// `only` >= 0 keeps one bin (autotuning).  A bin in the sliced mode without
+// the sliced copy, or with tiles that do not start on a slice, takes 1 lane.
 static int build_tiles(sprg_ctx* c, int only = -1) {
   std::vector<int4> tiles;
   int first = 0;
+  c->tile_mode = -2;  // no tile yet
   for (int b = 0; b < 4; ++b) {
+    int lanes = c->bin_lanes[b];
+    if (lanes == 0 && (!c->sliced || c->tile_verts % 32)) lanes = 1;
     for (int i = 0; i < c->bin_count[b]; i += c->tile_verts) {
       const int n = std::min(c->tile_verts, c->bin_count[b] - i);
-      if (only < 0 || only == b) tiles.push_back(make_int4(first + i, n, c->bin_lanes[b], b));
+      if (only < 0 || only == b) {
+        tiles.push_back(make_int4(first + i, n, lanes, c->bslices.slice0[b] + i / 32));
+        c->tile_mode = c->tile_mode == -2 || c->tile_mode == lanes ? lanes : -1;
+      }
     }
     first += c->bin_count[b];
   }
@@ -1437,8 +1494,9 @@ static int build_tiles(sprg_ctx* c, int only = -1) {
 }
 
 static void run_tiles(sprg_ctx* c, float4* rec32) {
-  fast_recover_tiles(c->m, P<float>(c->wts), P<uint4>(c->tetd), rec32, P<int>(c->bverts), P<int4>(c->btiles),
-                     c->n_tiles, P<int>(c->bnext), c->n_sms * c->grid_per_sm, c->stream);
+  fast_recover_tiles(c->m, P<float>(c->wts), sliced_view(c), P<uint4>(c->tetd), rec32, P<int>(c->bverts),
+                     P<int4>(c->btiles), c->n_tiles, c->tile_mode < 0 ? -1 : c->tile_mode, P<int>(c->bnext),
+                     c->n_sms * c->grid_per_sm, c->stream);
 }
 
 // CUDA-event time of the binned recover under the current configuration
@@ -1463,8 +1521,9 @@ static float time_tiles(sprg_ctx* c, float4* rec32, int only) {
 }
 
 // Autotuner (first pass, element gradients in place): coordinate descent
-// over lanes per bin {1, 2, 4}, tile size {64, 256, 1024} vertices and
-// blocks per SM {4, 8, 16}; every configuration gives bitwise the same
+// over lanes per bin {1, 2, 4, 0 = sliced}, then that per-bin choice against
+// one lane mode for every bin (a kernel specialised to it), tile size {64,
+// 256, 1024} vertices and blocks per SM {4, 8, 16}; every configuration gives bitwise the same
 // result, so the choice only changes time.  The choice and the timings are
 // kept for sprg_tuning_report.
 static int autotune(sprg_ctx* c, float4* rec32) {
@@ -1477,7 +1536,8 @@ static int autotune(sprg_ctx* c, float4* rec32) {
     if (!c->bin_count[b]) continue;
     int best_l = c->bin_lanes[b];
     float best = 1e30f;
-    for (int l : {1, 2, 4}) {
+    for (int l : {1, 2, 4, 0}) {
+      if (l == 0 && !c->sliced) continue;
       c->bin_lanes[b] = l;
       const float ms = time_tiles(c, rec32, b);
       note(("lanes_bin" + std::to_string(b)).c_str(), l, ms);
@@ -1487,6 +1547,26 @@ static int autotune(sprg_ctx* c, float4* rec32) {
       }
     }
     c->bin_lanes[b] = best_l;
+  }
+  {
+    // one lane mode for every bin runs a kernel specialised to that mode
+    // (fewer registers, more resident warps): the per-bin choice against
+    // each uniform one, over the whole launch
+    int chosen[4];
+    for (int b = 0; b < 4; ++b) chosen[b] = c->bin_lanes[b];
+    float best = time_tiles(c, rec32, -1);
+    note("per_bin_lanes", 1, best);
+    for (int l : {2, 4, 1, 0}) {
+      if (l == 0 && !c->sliced) continue;
+      for (int b = 0; b < 4; ++b) c->bin_lanes[b] = l;
+      const float ms = time_tiles(c, rec32, -1);
+      note("uniform_lanes", l, ms);
+      if (ms < best) {
+        best = ms;
+        for (int b = 0; b < 4; ++b) chosen[b] = l;
+      }
+    }
+    for (int b = 0; b < 4; ++b) c->bin_lanes[b] = chosen[b];
   }
   {
     int best_t = c->tile_verts;
@@ -1559,9 +1639,9 @@ static int pass_fast(sprg_ctx* c, double adapt_ratio, uint32_t* d_split, uint32_
   ENSURE(c->out3, sizeof(double) * 4 * (size_t)(bv.n > 0 ? bv.n : 1));
   if ((rc = reset_status(c))) return rc;
   // fcnt: [0] refit patches, [1] guard edges, [3] listed patches,
-  // [4] unresolved guard edges, [5] rounding dominance (the largest
-  // element share of the reference's rounding, then 0 / 1 from the error
-  // kernel's last block) (0, 3 per mesh; 1, 4, 5 per pass)
+  // [4] unresolved guard edges, [5] rounding dominance (max |u| as float
+  // bits from the prep kernel, then 0 / 1 from the error kernel's last
+  // block) (0, 3 per mesh; 1, 4, 5 per pass)
   ExpandList xl{P<int>(c->fitems), P<int>(c->fcnt) + 3, m.V};
   float4* vrec = P<float4>(c->vrec);
   float4* rec32 = P<float4>(c->rec32);
@@ -2478,8 +2558,12 @@ int sprg_graph_replay(sprg_ctx* c) {
 
 int sprg_set_tiling(sprg_ctx* c, const int* lanes, int tile_verts, int blocks_per_sm) {
   if (!c || !lanes || tile_verts <= 0 || blocks_per_sm <= 0) return SPRG_EINVAL;
-  for (int b = 0; b < 4; ++b)
-    if (lanes[b] != 1 && lanes[b] != 2 && lanes[b] != 4) return fail(c, SPRG_EINVAL, "lanes per vertex: 1, 2 or 4");
+  for (int b = 0; b < 4; ++b) {
+    if (lanes[b] != 0 && lanes[b] != 1 && lanes[b] != 2 && lanes[b] != 4)
+      return fail(c, SPRG_EINVAL, "lanes per vertex: 1, 2 or 4, or 0 (sliced)");
+    if (lanes[b] == 0 && tile_verts % 32)
+      return fail(c, SPRG_EINVAL, "the sliced mode needs tiles of a multiple of 32 vertices");
+  }
   int rc = set_device(c);
   if (rc) return rc;
   for (int b = 0; b < 4; ++b) c->bin_lanes[b] = lanes[b];

@@ -40,10 +40,31 @@ void fast_patch_class(const DevMesh& m, const unsigned char* listed, unsigned ch
 int fast_bin_blocks(int V);
 void fast_bin_count(int V, const unsigned char* cls, int* counts, cudaStream_t s);
 void fast_bin_scatter(int V, const unsigned char* cls, const int* offs, int* order, cudaStream_t s);
-// binned recover: tiles (first, count, lanes in {1, 2, 4}, bin) over verts, taken
-// from a counter by a persistent grid; every tiling gives the same bits
-void fast_recover_tiles(const DevMesh& m, const float* w, const uint4* td, float4* rec, const int* verts,
-                        const int4* tiles, int n_tiles, int* next, int grid, cudaStream_t s);
+// sliced copy of the patch lists (element ids and FP32 weights): the binned
+// vertex order cut into slices of 32 aligned to each bin's start (bin b:
+// entries [start[b], start[b + 1]) of the order, slices [slice0[b],
+// slice0[b + 1])); entry k of the slice's lane i at off[s] + 32 k + i
+struct BinSlices {
+  int start[5], slice0[5];
+};
+struct SlicedPatches {
+  const int* off;
+  const int* el;
+  const float* w;
+};
+// per slice its width (the largest patch of its vertices)
+void fast_slice_width(const DevMesh& m, const BinSlices& bs, const int* verts, int* width, cudaStream_t s);
+// with off set (exclusive sums of 32 x width): the element ids and weights
+void fast_slice_fill(const DevMesh& m, const BinSlices& bs, const int* verts, const float* w, SlicedPatches sp,
+                     cudaStream_t s);
+// binned recover: tiles (first, count, lanes, slice of first) over verts,
+// taken from a counter by a persistent grid; lanes 1, 2, 4 per vertex over
+// the patch-CSR lists, or 0: one per vertex over the sliced copy (tiles then
+// start on a slice); every tiling gives the same bits.  mode: the lane count
+// of every tile (a kernel for that mode alone), or -1 for mixed tiles
+void fast_recover_tiles(const DevMesh& m, const float* w, SlicedPatches sp, const uint4* td, float4* rec,
+                        const int* verts, const int4* tiles, int n_tiles, int mode, int* next, int grid,
+                        cudaStream_t s);
 // q: (h_max err^(-1/5), its relative error bound) per tet
 // seg (batch): one element range per block, nb = number of segments
 // done (one unsigned, zero between passes) and out3: the last block also

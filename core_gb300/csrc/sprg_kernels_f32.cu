@@ -604,11 +604,88 @@ __device__ __forceinline__ void recover_tile(const DevMesh& m, const float* __re
   }
 }
 
-__global__ void __launch_bounds__(kBlock) k_fast_recover_tiles(DevMesh m, const float* __restrict__ w,
-                                                               const uint4* __restrict__ td, float4* __restrict__ rec,
-                                                               const int* __restrict__ verts,
-                                                               const int4* __restrict__ tiles, int n_tiles,
-                                                               int* __restrict__ next) {
+// One lane per vertex over the sliced copy of the patch lists (lanes = 0):
+// warp j of the tile takes slice `slice0 + j`, whose entry k of lane i sits
+// at off + 32 k + i, so each step reads the 32 patches' element ids and
+// weights as two 128-byte lines.  Same operations as recover_tile<1>
+// (classes x_{k mod 4}, then (x0 + x1) + (x2 + x3)): the same bits.
+__device__ __forceinline__ void recover_tile_sliced(const DevMesh& m, SlicedPatches sp,
+                                                    const uint4* __restrict__ td, float4* __restrict__ rec,
+                                                    const int* __restrict__ verts, int first, int count,
+                                                    int slice0) {
+  const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int j = threadIdx.x >> 5; 32 * j < count; j += nw) {
+    const int i = 32 * j + lane;
+    const bool active = i < count;
+    const int v = active ? __ldg(verts + first + i) : 0;
+    const int cnt = active ? m.p_off[v + 1] - m.p_off[v] : 0;
+    const int* __restrict__ el = sp.el + __ldg(sp.off + slice0 + j) + lane;
+    const float* __restrict__ wt = sp.w + (el - sp.el);
+    float gr0 = 0.f, gr1 = 0.f, gr2 = 0.f;
+    if (cnt > 0) {
+      const uint4 a = __ldg(td + __ldg(el));
+      gr0 = __uint_as_float(a.x); gr1 = __uint_as_float(a.y); gr2 = __uint_as_float(a.z);
+    }
+    float x[4][3];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) x[c][0] = x[c][1] = x[c][2] = 0.f;
+    // groups of four entries (entry k + c in class c); the next group's ids
+    // and weights load while this group's gradients are gathered
+    int tn[4];
+    float wn[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      tn[c] = c < cnt ? __ldg(el + 32 * c) : 0;
+      wn[c] = c < cnt ? __ldg(wt + 32 * c) : 0.f;
+    }
+    for (int k = 0; k < cnt; k += 4) {
+      int t[4];
+      float wk[4];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        t[c] = tn[c];
+        wk[c] = wn[c];
+      }
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const bool more = k + 4 + c < cnt;
+        tn[c] = more ? __ldg(el + 32 * (k + 4 + c)) : 0;
+        wn[c] = more ? __ldg(wt + 32 * (k + 4 + c)) : 0.f;
+      }
+      uint4 a[4];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) a[c] = k + c < cnt ? __ldg(td + t[c]) : make_uint4(0, 0, 0, 0);
+#pragma unroll
+      for (int c = 0; c < 4; ++c)
+        if (k + c < cnt) {
+          const Grad g = unpack_grad(a[c]);
+          x[c][0] = fmaf(wk[c], (g.s[0] - gr0) + g.r[0], x[c][0]);
+          x[c][1] = fmaf(wk[c], (g.s[1] - gr1) + g.r[1], x[c][1]);
+          x[c][2] = fmaf(wk[c], (g.s[2] - gr2) + g.r[2], x[c][2]);
+        }
+    }
+    if (active) {
+      float tot[3], s3[3], r3[3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) tot[d] = (x[0][d] + x[1][d]) + (x[2][d] + x[3][d]);
+      two_sum(gr0, tot[0], s3[0], r3[0]);
+      two_sum(gr1, tot[1], s3[1], r3[1]);
+      two_sum(gr2, tot[2], s3[2], r3[2]);
+      rec[2 * (size_t)v] = make_float4(s3[0], s3[1], s3[2], r3[0]);
+      rec[2 * (size_t)v + 1] = make_float4(r3[1], r3[2], 0.f, 0.f);
+    }
+  }
+}
+
+// MODE: the lane mode of every tile (0 sliced, 1, 2, 4), or -1 for tiles of
+// mixed modes (a kernel per mode keeps each mode's own register count).  The
+// gathers want loads in flight more than resident warps: capping 2 lanes at
+// 32 registers for eight blocks per SM made it a third slower.
+template <int MODE>
+__global__ void __launch_bounds__(kBlock, MODE <= 0 ? 4 : 5)
+    k_fast_recover_tiles(DevMesh m, const float* __restrict__ w, SlicedPatches sp, const uint4* __restrict__ td,
+                         float4* __restrict__ rec, const int* __restrict__ verts, const int4* __restrict__ tiles,
+                         int n_tiles, int* __restrict__ next) {
   __shared__ int cur;
   for (;;) {
     if (threadIdx.x == 0) cur = atomicAdd(next, 1);
@@ -616,10 +693,50 @@ __global__ void __launch_bounds__(kBlock) k_fast_recover_tiles(DevMesh m, const 
     const int t = cur;
     __syncthreads();
     if (t >= n_tiles) return;
-    const int4 tile = tiles[t];  // (first, count, lanes, bin)
-    if (tile.z == 1) recover_tile<1>(m, w, td, rec, verts, tile.x, tile.y);
-    else if (tile.z == 2) recover_tile<2>(m, w, td, rec, verts, tile.x, tile.y);
+    const int4 tile = tiles[t];  // (first, count, lanes, slice of `first`)
+    const int mode = MODE >= 0 ? MODE : tile.z;
+    if (mode == 0) recover_tile_sliced(m, sp, td, rec, verts, tile.x, tile.y, tile.w);
+    else if (mode == 1) recover_tile<1>(m, w, td, rec, verts, tile.x, tile.y);
+    else if (mode == 2) recover_tile<2>(m, w, td, rec, verts, tile.x, tile.y);
     else recover_tile<4>(m, w, td, rec, verts, tile.x, tile.y);
+  }
+}
+
+// sliced copy of the patch lists: slice widths (thread per slice), then,
+// with the slices' offsets, the fill (thread per binned vertex)
+__device__ __forceinline__ int slice_bin(const BinSlices& bs, int s) {
+  int b = 0;
+  while (b < 3 && s >= bs.slice0[b + 1]) ++b;
+  return b;
+}
+
+__global__ void k_slice_width(DevMesh m, BinSlices bs, const int* __restrict__ verts, int* __restrict__ width) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= bs.slice0[4]) return;
+  const int b = slice_bin(bs, s);
+  const int i0 = bs.start[b] + 32 * (s - bs.slice0[b]), i1 = min(i0 + 32, bs.start[b + 1]);
+  int wmax = 0;
+  for (int i = i0; i < i1; ++i) {
+    const int v = verts[i];
+    wmax = max(wmax, m.p_off[v + 1] - m.p_off[v]);
+  }
+  width[s] = wmax;
+}
+
+__global__ void k_slice_fill(DevMesh m, BinSlices bs, const int* __restrict__ verts, const float* __restrict__ w,
+                             SlicedPatches sp) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= bs.start[4]) return;
+  int b = 0;
+  while (b < 3 && i >= bs.start[b + 1]) ++b;
+  const int r = i - bs.start[b];
+  const int s = bs.slice0[b] + r / 32, lane = r % 32;
+  const int v = verts[i], beg = m.p_off[v], cnt = m.p_off[v + 1] - beg;
+  int* el = const_cast<int*>(sp.el) + sp.off[s] + lane;
+  float* wt = const_cast<float*>(sp.w) + sp.off[s] + lane;
+  for (int k = 0; k < cnt; ++k) {
+    el[32 * k] = m.p_el[beg + k];
+    wt[32 * k] = w[beg + k];
   }
 }
 
@@ -1098,10 +1215,27 @@ void fast_bin_scatter(int V, const unsigned char* cls, const int* offs, int* ord
   if (V) k_bin_scatter<<<fast_bin_blocks(V), kBinBlock, 0, s>>>(V, cls, offs, order);
 }
 
-void fast_recover_tiles(const DevMesh& m, const float* w, const uint4* td, float4* rec, const int* verts,
-                        const int4* tiles, int n_tiles, int* next, int grid, cudaStream_t s) {
+void fast_recover_tiles(const DevMesh& m, const float* w, SlicedPatches sp, const uint4* td, float4* rec,
+                        const int* verts, const int4* tiles, int n_tiles, int mode, int* next, int grid,
+                        cudaStream_t s) {
   cudaMemsetAsync(next, 0, sizeof(int), s);
-  if (n_tiles) k_fast_recover_tiles<<<grid, kBlock, 0, s>>>(m, w, td, rec, verts, tiles, n_tiles, next);
+  if (!n_tiles) return;
+  switch (mode) {
+    case 0: k_fast_recover_tiles<0><<<grid, kBlock, 0, s>>>(m, w, sp, td, rec, verts, tiles, n_tiles, next); break;
+    case 1: k_fast_recover_tiles<1><<<grid, kBlock, 0, s>>>(m, w, sp, td, rec, verts, tiles, n_tiles, next); break;
+    case 2: k_fast_recover_tiles<2><<<grid, kBlock, 0, s>>>(m, w, sp, td, rec, verts, tiles, n_tiles, next); break;
+    case 4: k_fast_recover_tiles<4><<<grid, kBlock, 0, s>>>(m, w, sp, td, rec, verts, tiles, n_tiles, next); break;
+    default: k_fast_recover_tiles<-1><<<grid, kBlock, 0, s>>>(m, w, sp, td, rec, verts, tiles, n_tiles, next);
+  }
+}
+
+void fast_slice_width(const DevMesh& m, const BinSlices& bs, const int* verts, int* width, cudaStream_t s) {
+  if (bs.slice0[4]) k_slice_width<<<nblk(bs.slice0[4]), kBlock, 0, s>>>(m, bs, verts, width);
+}
+
+void fast_slice_fill(const DevMesh& m, const BinSlices& bs, const int* verts, const float* w, SlicedPatches sp,
+                     cudaStream_t s) {
+  if (bs.start[4]) k_slice_fill<<<nblk(bs.start[4]), kBlock, 0, s>>>(m, bs, verts, w, sp);
 }
 
 void fast_merge_ref(ExpandList xl, const double* rec64, float4* rec, cudaStream_t s) {

@@ -435,8 +435,10 @@ int sprg_batch_info(sprg_ctx* ctx, double* out);
    across sprg_update_mesh; calling this with on = 1 tunes again at the next
    pass.  on = 0 keeps the current configuration. */
 int sprg_set_autotune(sprg_ctx* ctx, int on);
-/* fix the binned recovery's configuration (lanes per bin in {1, 2, 4}, tile
-   size in vertices, blocks per SM); turns the autotuner off */
+/* fix the binned recovery's configuration (lanes per bin in {1, 2, 4} over
+   the patch-CSR lists, or 0: one lane per vertex over a sliced copy of the
+   lists, 32 patches side by side, which needs a tile size that is a multiple
+   of 32; tile size in vertices, blocks per SM); turns the autotuner off */
 int sprg_set_tiling(sprg_ctx* ctx, const int* lanes, int tile_verts, int blocks_per_sm);
 /* JSON: bin sizes, chosen configuration, the autotuner's timings */
 const char* sprg_tuning_report(sprg_ctx* ctx);

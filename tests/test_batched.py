@@ -89,7 +89,9 @@ def test_tilings_give_identical_bits(gpu_lib):
     ratios = np.full(len(ns), 0.05)
     runs = []
     report = None
-    for cfg in [None, ([4, 4, 4, 4], 256, 8), ([1, 1, 1, 1], 64, 4), ([2, 1, 4, 2], 1024, 16)]:
+    # lanes 0: one lane per vertex over the sliced copy of the patch lists
+    for cfg in [None, ([4, 4, 4, 4], 256, 8), ([1, 1, 1, 1], 64, 4), ([2, 1, 4, 2], 1024, 16),
+                ([0, 0, 0, 0], 256, 8), ([0, 2, 0, 1], 64, 16), ([4, 0, 1, 0], 1024, 4)]:
         with cg.Context(m, precision="fp32") as c:
             c.set_batch(voff, eoff, ratios)
             if cfg is not None:
@@ -101,7 +103,12 @@ def test_tilings_give_identical_bits(gpu_lib):
     for size, flags in runs[1:]:
         assert np.array_equal(size, runs[0][0], equal_nan=True) and np.array_equal(flags, runs[0][1])
     assert sum(report["bins"]) > 0 and len(report["lanes"]) == 4 and report["timings"]
-    assert set(report["lanes"]) <= {1, 2, 4}
+    assert set(report["lanes"]) <= {0, 1, 2, 4}
+    with cg.Context(m, precision="fp32") as c:
+        with pytest.raises(cg.SprgError):
+            c.set_tiling([0, 1, 1, 1], 48, 8)  # sliced tiles start on a slice of 32
+        with pytest.raises(cg.SprgError):
+            c.set_tiling([3, 1, 1, 1], 64, 8)
 
 
 def test_graph_replay_matches_direct_passes(gpu_lib):
