@@ -54,6 +54,9 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-accuracy", action="store_true", help="skip the FP64 comparison of the FP32 result")
+    p.add_argument("--tiling", default=None,
+                   help="fix the FP32 recovery's launch shape instead of autotuning it: "
+                        "LANES:TILE_VERTS:BLOCKS_PER_SM, LANES four comma-separated lane modes (0 sliced, 1, 2, 4)")
     return p.parse_args()
 
 
@@ -395,6 +398,9 @@ def gpu_arm(args):
     stream = torch.cuda.Stream(dev)
     torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
+    if args.tiling:
+        lanes, tile_verts, blocks = args.tiling.split(":")
+        ctx.set_tiling([int(x) for x in lanes.split(",")], int(tile_verts), int(blocks))
     d_u = torch.from_numpy(u).to(dev)
     nw = (E + 31) // 32
     bits = torch.zeros(2 * nw, dtype=torch.int32, device=dev)

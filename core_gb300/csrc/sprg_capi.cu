@@ -1420,7 +1420,8 @@ static int build_slices(sprg_ctx* c) {
   ENSURE(c->sw, sizeof(float) * (size_t)(run > 0 ? run : 1));
   CK(cudaMemsetAsync(c->sel.p, 0, sizeof(int) * (size_t)(run > 0 ? run : 1), c->stream));
   CK(cudaMemsetAsync(c->sw.p, 0, sizeof(float) * (size_t)(run > 0 ? run : 1), c->stream));
-  fast_slice_fill(m, bs, P<int>(c->bverts), P<float>(c->wts), sliced_view(c), c->stream);
+  fast_slice_fill(m, bs, P<int>(c->bverts), P<float>(c->wts), P<int>(c->soff), P<int>(c->sel), P<float>(c->sw),
+                  c->stream);
   CK(cudaStreamSynchronize(c->stream));  // off lives on this frame
   int rc = check_launch(c, "sliced patch lists");
   if (rc) return rc;

@@ -55,8 +55,8 @@ struct SlicedPatches {
 // per slice its width (the largest patch of its vertices)
 void fast_slice_width(const DevMesh& m, const BinSlices& bs, const int* verts, int* width, cudaStream_t s);
 // with off set (exclusive sums of 32 x width): the element ids and weights
-void fast_slice_fill(const DevMesh& m, const BinSlices& bs, const int* verts, const float* w, SlicedPatches sp,
-                     cudaStream_t s);
+void fast_slice_fill(const DevMesh& m, const BinSlices& bs, const int* verts, const float* w, const int* off,
+                     int* sel, float* sw, cudaStream_t s);
 // binned recover: tiles (first, count, lanes, slice of first) over verts,
 // taken from a counter by a persistent grid; lanes 1, 2, 4 per vertex over
 // the patch-CSR lists, or 0: one per vertex over the sliced copy (tiles then

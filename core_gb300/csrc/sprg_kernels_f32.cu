@@ -724,7 +724,7 @@ __global__ void k_slice_width(DevMesh m, BinSlices bs, const int* __restrict__ v
 }
 
 __global__ void k_slice_fill(DevMesh m, BinSlices bs, const int* __restrict__ verts, const float* __restrict__ w,
-                             SlicedPatches sp) {
+                             const int* __restrict__ off, int* __restrict__ sel, float* __restrict__ sw) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= bs.start[4]) return;
   int b = 0;
@@ -732,8 +732,8 @@ __global__ void k_slice_fill(DevMesh m, BinSlices bs, const int* __restrict__ ve
   const int r = i - bs.start[b];
   const int s = bs.slice0[b] + r / 32, lane = r % 32;
   const int v = verts[i], beg = m.p_off[v], cnt = m.p_off[v + 1] - beg;
-  int* el = const_cast<int*>(sp.el) + sp.off[s] + lane;
-  float* wt = const_cast<float*>(sp.w) + sp.off[s] + lane;
+  int* el = sel + off[s] + lane;
+  float* wt = sw + off[s] + lane;
   for (int k = 0; k < cnt; ++k) {
     el[32 * k] = m.p_el[beg + k];
     wt[32 * k] = w[beg + k];
@@ -1233,9 +1233,9 @@ void fast_slice_width(const DevMesh& m, const BinSlices& bs, const int* verts, i
   if (bs.slice0[4]) k_slice_width<<<nblk(bs.slice0[4]), kBlock, 0, s>>>(m, bs, verts, width);
 }
 
-void fast_slice_fill(const DevMesh& m, const BinSlices& bs, const int* verts, const float* w, SlicedPatches sp,
-                     cudaStream_t s) {
-  if (bs.start[4]) k_slice_fill<<<nblk(bs.start[4]), kBlock, 0, s>>>(m, bs, verts, w, sp);
+void fast_slice_fill(const DevMesh& m, const BinSlices& bs, const int* verts, const float* w, const int* off,
+                     int* sel, float* sw, cudaStream_t s) {
+  if (bs.start[4]) k_slice_fill<<<nblk(bs.start[4]), kBlock, 0, s>>>(m, bs, verts, w, off, sel, sw);
 }
 
 void fast_merge_ref(ExpandList xl, const double* rec64, float4* rec, cudaStream_t s) {
