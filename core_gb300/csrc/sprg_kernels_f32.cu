@@ -229,7 +229,9 @@ __device__ __forceinline__ float2 split_pair(double w) {
 // one atomic per block)
 __global__ void __launch_bounds__(kBlock) k_prep(int V, const double* __restrict__ u, const float4* __restrict__ crec,
                                                  float4* __restrict__ vrec, int* __restrict__ umax_bits) {
-  float um = 0.f;
+  // |u_hi| as float bits: non-negative floats order as their bit patterns,
+  // a NaN (sign cleared) above +inf, so an integer max keeps it
+  int um = 0;
   const int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v < V) {
     const float2 p = split_pair(__ldg(u + v));
@@ -238,22 +240,17 @@ __global__ void __launch_bounds__(kBlock) k_prep(int V, const double* __restrict
     l.w = p.y;
     vrec[2 * (size_t)v] = h;
     vrec[2 * (size_t)v + 1] = l;
-    um = fmaxf(um, fabsf(p.x));
-    if (!(p.x == p.x)) um = __int_as_float(0x7fc00000);  // NaN stays (fmaxf would drop it)
+    um = __float_as_int(p.x) & 0x7fffffff;
   }
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    const float x = __shfl_xor_sync(0xffffffffu, um, o);
-    um = (x == x) ? fmaxf(um, x) : x;
-  }
-  __shared__ float sw[kBlock / 32];
+  for (int o = 16; o > 0; o >>= 1) um = max(um, __shfl_xor_sync(0xffffffffu, um, o));
+  __shared__ int sw[kBlock / 32];
   if ((threadIdx.x & 31) == 0) sw[threadIdx.x >> 5] = um;
   __syncthreads();
   if (threadIdx.x == 0) {
-    float b = sw[0];
-    for (int i = 1; i < kBlock / 32; ++i) b = (sw[i] == sw[i]) ? fmaxf(b, sw[i]) : sw[i];
-    // non-negative floats order as their bit patterns (NaN above +inf)
-    if (b != 0.f) atomicMax(umax_bits, __float_as_int(b));
+    int b = sw[0];
+    for (int i = 1; i < kBlock / 32; ++i) b = max(b, sw[i]);
+    if (b != 0) atomicMax(umax_bits, b);
   }
 }
 
