@@ -60,6 +60,20 @@ def parse():
     return p.parse_args()
 
 
+def parse_tiling(text):
+    """--tiling LANES:TILE_VERTS:BLOCKS_PER_SM -> ([four lane modes], tile_verts, blocks_per_sm)."""
+    parts = text.split(":")
+    if len(parts) != 3:
+        raise ValueError("--tiling wants LANES:TILE_VERTS:BLOCKS_PER_SM")
+    lanes = [int(x) for x in parts[0].split(",")]
+    if len(lanes) != 4 or any(l not in (0, 1, 2, 4) for l in lanes):
+        raise ValueError("--tiling wants four lane modes out of 0 (sliced), 1, 2, 4")
+    tile_verts, blocks = int(parts[1]), int(parts[2])
+    if tile_verts <= 0 or blocks <= 0:
+        raise ValueError("--tiling wants a positive tile size and block count")
+    return lanes, tile_verts, blocks
+
+
 def workload_desc(n, precision, adapt_ratio=0.008):
     V, T, E = (n + 1) ** 3, 6 * n ** 3, 3 * n * (n + 1) ** 2 + 3 * n ** 2 * (n + 1) + n ** 3
     return {"workload": f"{n}^3 jittered unit box, {T} tets, {V} vertices, {E} edges; u = 4 Gaussian bumps "
@@ -399,8 +413,7 @@ def gpu_arm(args):
     torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
     if args.tiling:
-        lanes, tile_verts, blocks = args.tiling.split(":")
-        ctx.set_tiling([int(x) for x in lanes.split(",")], int(tile_verts), int(blocks))
+        ctx.set_tiling(*parse_tiling(args.tiling))
     d_u = torch.from_numpy(u).to(dev)
     nw = (E + 31) // 32
     bits = torch.zeros(2 * nw, dtype=torch.int32, device=dev)

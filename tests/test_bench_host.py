@@ -86,3 +86,11 @@ def test_reference_arm_other_ranks_exit_without_work():
                         "--steps", "3", "--warmup", "3"], env=env, capture_output=True, text=True, timeout=120)
     assert r.returncode == 0, r.stderr
     assert r.stdout.strip() == ""
+
+
+def test_tiling_option_parses_and_refuses():
+    assert bench.parse_tiling("0,0,0,0:256:16") == ([0, 0, 0, 0], 256, 16)
+    assert bench.parse_tiling("1,2,4,0:1024:4") == ([1, 2, 4, 0], 1024, 4)
+    for bad in ("0,0,0:256:16", "3,0,0,0:256:16", "0,0,0,0:256", "0,0,0,0:0:16", "0,0,0,0:256:-1"):
+        with pytest.raises(ValueError):
+            bench.parse_tiling(bad)
